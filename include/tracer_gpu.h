@@ -1,0 +1,219 @@
+/*
+ * tracer_gpu.h -- C ABI of the GB300 path-tracing hot path.
+ *
+ * This is the drop-in boundary for Tracer's unidirectional path tracer
+ * (reference: src/renderer/path_trace_renderer.cpp). Every entry point takes
+ * plain pointers and sizes, returns a tr_status and never throws. Host
+ * buffers are owned by the caller; device buffers are owned by the context.
+ * One context per host thread; a context owns one CUDA stream and is not
+ * re-entrant.
+ *
+ * Each entry point names the reference interface it replaces (file:line,
+ * relative to the reference project root).
+ */
+#ifndef TRACER_GPU_H
+#define TRACER_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum tr_status {
+  TR_OK = 0,
+  TR_ERR_ARG = 1,            /* invalid argument (null pointer, bad size, NaN ray) */
+  TR_ERR_OOM = 2,            /* device or pinned host allocation failed */
+  TR_ERR_QUEUE_OVERFLOW = 3, /* a device work queue ran past its capacity */
+  TR_ERR_TIMEOUT = 4,        /* a bounded device loop gave up */
+  TR_ERR_CUDA = 5,           /* a CUDA runtime call failed (see tr_ctx_last_error) */
+  TR_ERR_STATE = 6,          /* call out of order (e.g. trace before scene upload) */
+  TR_ERR_CANCELLED = 7,      /* tr_cancel() was called while rendering */
+  TR_ERR_UNSUPPORTED = 8     /* scene feature outside the GPU path (see docs) */
+} tr_status;
+
+/* A ray exactly as the reference stores it after construction
+ * (src/utility/geometry.hpp:789-811). The direction is used as given: callers
+ * that start from an unnormalised direction build the ray with tr_make_ray,
+ * which applies the reference constructor's double-precision normalisation. */
+typedef struct tr_ray {
+  float o[3];
+  float d[3];
+  float t_min;
+  float t_max;
+} tr_ray;
+
+/* Flattened BVH node in the reference's LinearBVHNode layout
+ * (src/accelerator/bvh.cpp:51-64): 32 bytes, depth-first order, interior
+ * nodes store the offset of their second child, leaves the offset of their
+ * first primitive slot. */
+typedef struct tr_bvh_node32 {
+  float lo[3];
+  float hi[3];
+  int32_t offset;
+  uint16_t count; /* > 0: leaf */
+  uint8_t axis;
+  uint8_t pad;
+} tr_bvh_node32;
+
+enum { TR_MAT_PHONG = 0, TR_MAT_DISNEY12 = 1 };
+
+/* Material record. Phong is create_phong_material(ka, kd, ks, ns)
+ * (src/factory/material.hpp:19-24, src/material/phong.cpp:29-70); Disney12 is
+ * create_disney_brdf (src/material/disney_brdf.cpp:278-344). Constant textures
+ * only: every parameter is one value, as in the reference's configs. */
+typedef struct tr_material {
+  int32_t kind;
+  float ka[3];      /* Phong ambient (unused by shading, kept for the API) */
+  float kd[3];      /* Phong diffuse */
+  float ks[3];      /* Phong specular */
+  float ns;         /* Phong exponent */
+  float base_color[3];
+  float subsurface, metallic, specular, specular_tint, roughness;
+  float anisotropic, sheen, sheen_tint, clearcoat, clearcoat_gloss;
+} tr_material;
+
+/* Flat scene description. It records what the reference factory calls build
+ * (create_triangle_mesh, create_sphere, create_geometric_primitive,
+ * scene->lights; src/factory/shape.hpp:15-17, src/factory/primivite.hpp:12-14,
+ * src/core/scene.hpp:29). Vertex data is in world space, i.e. after the
+ * mesh's local_to_world (src/shape/triangle.cpp:216-236). The primitive list
+ * order is the order handed to BVHAccel::build, which fixes the tree. */
+typedef struct tr_scene_desc {
+  uint32_t num_vertices;
+  const float* positions; /* 3 * num_vertices */
+  const float* normals;   /* 3 * num_vertices, normalised on upload like the reference mesh */
+  const float* uvs;       /* 2 * num_vertices */
+  uint32_t num_triangles;
+  const int32_t* indices; /* 3 * num_triangles */
+  uint32_t num_spheres;
+  const float* sphere_radius;   /* num_spheres, local radius */
+  const float* sphere_to_world; /* 16 * num_spheres, row-major local_to_world matrix */
+  const float* sphere_to_local; /* 16 * num_spheres, row-major inverse */
+  uint32_t num_materials;
+  const tr_material* materials;
+  uint32_t num_prims;
+  const int32_t* prim_shape;    /* >= 0: triangle index; < 0: sphere ~index */
+  const int32_t* prim_material; /* material index per primitive */
+  const float* prim_emission;   /* 3 * num_prims; all zero = not a light */
+  uint32_t num_lights;
+  const int32_t* light_prims;   /* primitive indices, in scene.lights order */
+  int32_t max_leaf_prims;       /* create_bvh_accel argument (src/accelerator/bvh.cpp:315) */
+} tr_scene_desc;
+
+/* create_thin_lens_camera arguments (src/camera/thin_lens_camera.cpp:23-36). */
+typedef struct tr_camera {
+  float film_aspect;
+  float pos[3];
+  float target[3];
+  float up[3];
+  float fov; /* radians */
+  float lens_radius;
+  float focal_dist;
+} tr_camera;
+
+/* create_gaussin_filter arguments (src/filter/gaussian_filter.cpp:9-35). */
+typedef struct tr_filter {
+  float radius;
+  float alpha;
+} tr_filter;
+
+/* PTRendererParams (src/factory/renderer.hpp:12-19) plus the film size and
+ * the per-pixel seeding rule: pixel (x, y) draws from one pcg32 stream seeded
+ * with (int32)(seed_base + y * width + x), samples in order, exactly like a
+ * SimpleUniformSampler per pixel (src/core/sampler.hpp:30-86). */
+typedef struct tr_render_params {
+  int32_t width;
+  int32_t height;
+  int32_t spp;
+  int32_t min_depth;
+  int32_t max_depth;
+  int32_t direct_light_sample_num; /* must be 1 on the GPU path */
+  uint32_t seed_base;
+} tr_render_params;
+
+typedef struct tr_stats {
+  uint64_t samples;      /* camera samples finished */
+  uint64_t extend_rays;  /* closest-hit rays traced (continuation + MIS) */
+  uint64_t shadow_rays;  /* any-hit rays traced */
+  uint64_t iterations;   /* wavefront iterations run */
+  double device_ms;      /* device time of the render, CUDA events */
+} tr_stats;
+
+const char* tr_status_string(tr_status s);
+
+/* Reference Ray constructor semantics (src/utility/geometry.hpp:791-792):
+ * d is normalised in double and rounded to float. Host-only helper. */
+tr_status tr_make_ray(const float o[3], const float d[3], float t_min, float t_max,
+                      tr_ray* out);
+
+typedef struct tr_ctx tr_ctx;
+
+/* Context on one CUDA device. Replaces nothing in the reference (its render
+ * state lives in PixelSamplerRenderer, src/renderer/pixel_sampler_renderer.cpp:24-36). */
+tr_status tr_ctx_create(tr_ctx** out, int device);
+void tr_ctx_destroy(tr_ctx* ctx);
+const char* tr_ctx_last_error(const tr_ctx* ctx);
+/* The context's CUDA stream (cudaStream_t), for callers that pass device pointers. */
+void* tr_ctx_stream(tr_ctx* ctx);
+tr_status tr_synchronize(tr_ctx* ctx);
+
+/* Builds the scene on the device: primitive tables, materials, lights and the
+ * binned-SAH BVH. Replaces create_bvh_accel + BVHAccel::build +
+ * create_general_scene (src/accelerator/bvh.cpp:78-105,315;
+ * src/core/scene.cpp:49-53). The BVH is built on the host with the
+ * reference's algorithm, so the tree and the leaf order are the reference's. */
+tr_status tr_scene_upload(tr_ctx* ctx, const tr_scene_desc* desc);
+
+/* Size and contents of the built BVH in the reference layout
+ * (BVHAccel::linear_nodes / primitives, src/accelerator/bvh.cpp:311-312).
+ * prim_order[i] is the scene primitive index stored in leaf slot i. */
+tr_status tr_bvh_info(tr_ctx* ctx, size_t* num_nodes, size_t* num_prims);
+tr_status tr_bvh_export(tr_ctx* ctx, tr_bvh_node32* nodes, uint32_t* prim_order);
+/* Replaces the uploaded scene's BVH with an externally built one (same layout). */
+tr_status tr_bvh_upload(tr_ctx* ctx, const tr_bvh_node32* nodes, size_t num_nodes,
+                        const uint32_t* prim_order, size_t num_prims);
+
+/* Closest hit for n rays: Scene::intersect_p (src/core/scene.cpp:36-38 ->
+ * BVHAccel::intersect_p, src/accelerator/bvh.cpp:149-185). prim[i] is the scene
+ * primitive index of the hit (-1 on a miss) and t[i] the final ray.t_max
+ * (the hit distance; the input t_max on a miss). Host buffers; the call copies
+ * in and out and returns when the results are in the caller's buffers. */
+tr_status tr_trace_closest(tr_ctx* ctx, const tr_ray* rays, size_t n, int32_t* prim,
+                           float* t);
+/* Any hit (shadow rays): Scene::intersect (src/core/scene.cpp:32-34 ->
+ * BVHAccel::intersect, src/accelerator/bvh.cpp:112-147). hit[i] is 0 or 1. */
+tr_status tr_trace_any(tr_ctx* ctx, const tr_ray* rays, size_t n, uint8_t* hit);
+/* Same with device pointers, enqueued on the context stream; returns without
+ * waiting. */
+tr_status tr_trace_closest_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, int32_t* d_prim,
+                               float* d_t);
+tr_status tr_trace_any_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, uint8_t* d_hit);
+
+/* Renders the film: PathTraceRenderer::eval_pixel_li per camera sample
+ * (src/renderer/path_trace_renderer.cpp:27-210) inside the pixel loop of
+ * PixelSamplerRenderer::render (src/renderer/pixel_sampler_renderer.cpp:24-109),
+ * with per-pixel pcg32 streams (see tr_render_params). Output: per pixel the
+ * filtered sums (r, g, b) and the filter weight, i.e. Film::Pixel before
+ * Film::write_render_target divides (src/core/render.hpp:105-127).
+ * Exactly one of rgbw (float, accumulated in float like the reference) and
+ * rgbw64 (accumulated in double) is non-null. Host buffers of
+ * 4 * width * height elements. stats may be null. */
+tr_status tr_render(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter,
+                    const tr_render_params* params, float* rgbw, double* rgbw64,
+                    tr_stats* stats);
+/* Same with a device output buffer, enqueued on the context stream. */
+tr_status tr_render_dev(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter,
+                        const tr_render_params* params, float* d_rgbw, double* d_rgbw64,
+                        tr_stats* stats);
+
+/* Asks a running tr_render on this context to stop after its current
+ * wavefront iteration; that call then returns TR_ERR_CANCELLED. Thread-safe. */
+tr_status tr_cancel(tr_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TRACER_GPU_H */

@@ -1,0 +1,1573 @@
+// tracer_oracle.cpp -- CPU restatement of Tracer's unidirectional path-tracing
+// hot path. TEST INFRASTRUCTURE ONLY: it is the parity checker for the GPU
+// path and the "port" CPU baseline. Nothing in the product links or calls it.
+//
+// Parity is pinned: tests/test_oracle_vs_reference.py compares every entry
+// point here with the reference's own sources compiled by oracle/Makefile
+// (target `ref`), and tests/golden/ holds fixtures made by that build.
+//
+// Every function restates one reference function; the citation is
+// file:line relative to the reference project root. The arithmetic follows
+// the reference operation by operation, including its float/double mixing:
+//  * length_squared() sums in float and widens to double; length() is a
+//    double sqrt; operator/ multiplies by a double reciprocal and rounds to
+//    float (src/utility/geometry.hpp:429-445);
+//  * cross() is evaluated in double and rounded (src/utility/geometry.hpp:584-589);
+//  * the slab test scales tMax by the double constant 1 + 1e-7
+//    (src/utility/geometry.hpp:848-859).
+// Build with -ffp-contract=off (oracle/Makefile) so no multiply-add fuses.
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <thread>
+#include <vector>
+
+#include "tracer_gpu.h"
+
+namespace orc {
+
+typedef float real;
+// common.hpp:47-73
+const real kEps = real(3e-4);
+const real kPi = real(3.141592653589793238462643383);
+const real kInvPi = 1 / kPi;
+const real kInv2Pi = 1 / (2 * kPi);
+const real kPiOver2 = kPi / 2;
+const real kPiOver4 = kPi / 4;
+const real kRealMax = std::numeric_limits<real>::max();
+const real kRealLowest = std::numeric_limits<real>::lowest();
+
+// ---------------------------------------------------------------- vectors
+struct V3 {
+  real x = 0, y = 0, z = 0;
+  V3() {}
+  V3(real a, real b, real c) : x(a), y(b), z(c) {}
+  explicit V3(real v) : x(v), y(v), z(v) {}
+  real operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+inline V3 operator+(V3 a, V3 b) { return V3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline V3 operator-(V3 a, V3 b) { return V3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline V3 operator-(V3 a) { return V3(-a.x, -a.y, -a.z); }
+// Vector3<T>::operator*(U s) with U = float: s * x in float (geometry.hpp:418-421).
+inline V3 mulf(V3 v, real s) { return V3(s * v.x, s * v.y, s * v.z); }
+inline bool all_zero(V3 v) { return !v.x && !v.y && !v.z; }  // geometry.hpp:411-413
+
+// geometry.hpp:444 length_squared(): float sum, returned as double.
+inline real len2f(V3 v) { return v.x * v.x + v.y * v.y + v.z * v.z; }
+inline double length(V3 v) { return std::sqrt((double)len2f(v)); }
+// geometry.hpp:429-433 operator/(U f): double reciprocal, double product, float result.
+inline V3 divd(V3 v, double f) {
+  double inv = (double)1 / f;
+  return V3((real)(v.x * inv), (real)(v.y * inv), (real)(v.z * inv));
+}
+// geometry.hpp:570-572
+inline V3 normalize(V3 v) { return divd(v, length(v)); }
+// geometry.hpp:584-590
+inline V3 cross(V3 a, V3 b) {
+  double ax = a.x, ay = a.y, az = a.z, bx = b.x, by = b.y, bz = b.z;
+  return V3((real)((ay * bz) - (az * by)), (real)((az * bx) - (ax * bz)), (real)((ax * by) - (ay * bx)));
+}
+// geometry.hpp:866-884
+inline real dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+// geometry.hpp:943-949
+inline real cosv(V3 a, V3 b) { return dot(a, b) / (length(a) * length(b)); }
+inline real abs_cos(V3 a, V3 b) { return std::abs(cosv(a, b)); }
+// geometry.hpp:887-894
+inline void coordinate(V3 v1, V3& v2, V3& v3) {
+  if (std::abs(v1.x) > std::abs(v1.y))
+    v2 = divd(V3(-v1.z, 0, v1.x), std::sqrt(v1.x * v1.x + v1.z * v1.z));
+  else
+    v2 = divd(V3(0, v1.z, -v1.y), std::sqrt(v1.y * v1.y + v1.z * v1.z));
+  v3 = cross(v1, v2);
+}
+// geometry.hpp:912-932
+inline real local_phi(V3 w) {
+  if (!w.y && !w.x) return 0;
+  real r = std::atan2(w.y, w.x);
+  return r < 0 ? (r + 2 * kPi) : r;
+}
+inline real local_tan_theta(V3 w) {
+  const real t = 1 - w.z * w.z;
+  if (t <= 0) return 0;
+  return std::sqrt(t) / w.z;
+}
+inline real local_cos_to_sin(real c) { return std::sqrt(std::max<real>(0, 1 - c * c)); }
+
+// Spectrum (core/spectrum.hpp:13-161) as three floats.
+struct Sp {
+  real r = 0, g = 0, b = 0;
+  Sp() {}
+  Sp(real a, real b_, real c) : r(a), g(b_), b(c) {}
+  explicit Sp(real v) : r(v), g(v), b(v) {}
+  bool black() const { return r == 0 && g == 0 && b == 0; }
+  bool finite() const { return std::isfinite(r) && std::isfinite(g) && std::isfinite(b); }
+  bool valid() const { return r >= 0 && g >= 0 && b >= 0 && finite(); }
+  real lum() const { return 0.2126f * r + 0.7152f * g + 0.0722f * b; }
+};
+inline Sp operator+(Sp a, Sp b) { return Sp(a.r + b.r, a.g + b.g, a.b + b.b); }
+inline Sp operator*(Sp a, Sp b) { return Sp(a.r * b.r, a.g * b.g, a.b * b.b); }
+inline Sp operator*(Sp a, real s) { return Sp(a.r * s, a.g * s, a.b * s); }
+inline Sp operator/(Sp a, real s) { return Sp(a.r / s, a.g / s, a.b / s); }
+inline Sp operator+(Sp a, real s) { return Sp(a.r + s, a.g + s, a.b + s); }
+inline void operator+=(Sp& a, Sp b) { a = a + b; }
+// geometry.hpp:989-993 mix() with a Spectrum pair and a float factor
+inline Sp mix(Sp l, Sp r, real f) { return l * (1 - f) + r * f; }
+inline real mixf(real l, real r, real f) { return (1 - f) * l + f * r; }
+
+// --------------------------------------------------------- Coord frames
+// utility/coordinate.hpp:15-116
+struct Coord {
+  V3 x{1, 0, 0}, y{0, 1, 0}, z{0, 0, 1};
+  Coord() {}
+  Coord(V3 a, V3 b, V3 c) : x(normalize(a)), y(normalize(b)), z(normalize(c)) {}
+  static Coord from_z(V3 zz) {
+    V3 nz = normalize(zz), ny;
+    if (std::abs(nz.x) > std::abs(nz.y))
+      ny = normalize(V3(-nz.z, 0, nz.x));
+    else
+      ny = normalize(V3(0, nz.z, -nz.y));
+    return Coord(cross(ny, nz), ny, nz);
+  }
+  V3 to_local(V3 v) const { return V3(dot(x, v), dot(y, v), dot(z, v)); }
+  V3 to_global(V3 v) const { return mulf(x, v.x) + mulf(y, v.y) + mulf(z, v.z); }
+  bool pos_hemi(V3 v) const { return dot(v, z) > 0; }
+};
+// coordinate.hpp:43-52
+inline real normal_correct_factor(const Coord& g, const Coord& s, V3 wi) {
+  real dem = std::abs(cosv(g.z, wi));
+  return dem < kEps ? 1 : std::abs(cosv(s.z, wi)) / dem;
+}
+// coordinate.hpp:54-68
+inline void compute_ss_ts(V3 AB, V3 AC, real abx, real aby, real acx, real acy, V3 n, V3& ss, V3& ts) {
+  const real m00 = abx, m01 = aby, m10 = acx, m11 = acy;
+  const real det = m00 * m11 - m01 * m10;
+  if (det) {
+    const real inv_det = 1 / det;
+    ss = mulf(AB, m11 * inv_det) - mulf(AC, m01 * inv_det);
+    ts = mulf(AB, m10 * inv_det) - mulf(AC, m00 * inv_det);
+  } else {
+    coordinate(n, ss, ts);
+  }
+}
+
+// --------------------------------------------------------------- sampler
+// pcg32 = setseq XSH-RR 64/32 with the default stream, output of the previous
+// state (dep/pcg_random.hpp), as used by SimpleUniformSampler
+// (core/sampler.hpp:30-41). Seeding: state = bump(seed + inc).
+struct Pcg32 {
+  static constexpr uint64_t kMul = 6364136223846793005ULL;
+  static constexpr uint64_t kInc = 1442695040888963407ULL;
+  uint64_t s;
+  explicit Pcg32(uint64_t seed) { s = (seed + kInc) * kMul + kInc; }
+  uint32_t next() {
+    uint64_t old = s;
+    s = old * kMul + kInc;
+    uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+    uint32_t rot = (uint32_t)(old >> 59u);
+    return (xs >> rot) | (xs << ((32u - rot) & 31u));
+  }
+};
+// std::uniform_real_distribution<float>(0,1) over a 32-bit engine in
+// libstdc++: one draw, float(x) / 2^32, clamped below 1.
+struct Sampler {
+  Pcg32 rng;
+  explicit Sampler(int seed) : rng((uint64_t)(int64_t)seed) {}
+  real u() {
+    real v = (real)rng.next() / 4294967296.0f;
+    if (v >= 1) v = std::nextafter(1.0f, 0.0f);
+    return v;
+  }
+};
+
+// --------------------------------------------------------------- sampling
+// core/sampling.cpp:8-22
+inline void concentric_disk(real u, real v, real& ox, real& oy) {
+  real x = u * 2 - 1, y = v * 2 - 1;
+  if (x == 0 && y == 0) { ox = 0; oy = 0; return; }
+  real theta, r;
+  if (std::abs(x) > std::abs(y)) {
+    r = x;
+    theta = kPiOver4 * (y / x);
+  } else {
+    r = y;
+    theta = kPiOver2 - kPiOver4 * (x / y);
+  }
+  ox = r * std::cos(theta);
+  oy = r * std::sin(theta);
+}
+// core/sampling.cpp:24-28
+inline V3 cosine_hemisphere(real u, real v) {
+  real dx, dy;
+  concentric_disk(u, v, dx, dy);
+  real z = std::sqrt(std::max<real>(0, 1 - dx * dx - dy * dy));
+  return V3(dx, dy, z);
+}
+inline real cosine_pdf(real c) { return c * kInvPi; }  // sampling.hpp:228
+// sampling.hpp:230-233
+inline real power_heuristic(real fp, real gp) {
+  real f = 1 * fp, g = 1 * gp;
+  return (f * f) / (f * f + g * g);
+}
+
+// ------------------------------------------------------------------ scene
+struct Tri {
+  V3 A, B, C;       // world positions
+  V3 nA, nB, nC;    // normalised vertex normals
+  real uA[2], uB[2], uC[2];
+};
+struct Sphere {
+  real radius, world_radius;
+  real m[16], inv[16];  // local_to_world and inverse, row-major
+  bool linear_identity;
+};
+struct Mat {
+  int kind;
+  // Phong::shading derived values (material/phong.cpp:29-70)
+  Sp diffuse_coef;   // albedo / PI_r of the DiffuseBXDF
+  Sp specular;       // normalised ks
+  real ns, w_diffuse, w_specular;
+  Sp albedo;         // diffuse + specular (AggregateBSDF albedo)
+  // Disney12 parameters (material/disney_brdf.cpp:278-302)
+  Sp base;
+  real subsurface, metallic, specular_s, specular_tint, roughness, anisotropic, sheen, sheen_tint,
+      clearcoat, clearcoat_gloss;
+};
+struct Prim {
+  int kind;  // 0 triangle, 1 sphere
+  int shape;
+  int material;
+  Sp emission;
+  bool light;
+};
+
+// Point transform (utility/transform.hpp:70-81)
+inline V3 xform_point(const real* m, V3 p) {
+  real x = p.x, y = p.y, z = p.z;
+  real xp = m[0] * x + m[1] * y + m[2] * z + m[3];
+  real yp = m[4] * x + m[5] * y + m[6] * z + m[7];
+  real zp = m[8] * x + m[9] * y + m[10] * z + m[11];
+  real wp = m[12] * x + m[13] * y + m[14] * z + m[15];
+  if (wp == 1) return V3(xp, yp, zp);
+  double inv = (double)1 / wp;  // Point3::operator/ (geometry.hpp:289-293)
+  return V3((real)(inv * xp), (real)(inv * yp), (real)(inv * zp));
+}
+// Vector transform (utility/transform.hpp:89-95)
+inline V3 xform_vec(const real* m, V3 v) {
+  real x = v.x, y = v.y, z = v.z;
+  return V3(m[0] * x + m[1] * y + m[2] * z, m[4] * x + m[5] * y + m[6] * z, m[8] * x + m[9] * y + m[10] * z);
+}
+// Normal transform with the inverse, transposed (utility/transform.hpp:82-88)
+inline V3 xform_normal(const real* inv, V3 n) {
+  real x = n.x, y = n.y, z = n.z;
+  return V3(inv[0] * x + inv[4] * y + inv[8] * z, inv[1] * x + inv[5] * y + inv[9] * z,
+            inv[2] * x + inv[6] * y + inv[10] * z);
+}
+
+struct Bounds {
+  V3 lo{kRealMax, kRealMax, kRealMax}, hi{kRealLowest, kRealLowest, kRealLowest};
+};
+inline real smin(real a, real b) { return (b < a) ? b : a; }  // std::min
+inline real smax(real a, real b) { return (a < b) ? b : a; }  // std::max
+inline V3 vmin(V3 a, V3 b) { return V3(smin(a.x, b.x), smin(a.y, b.y), smin(a.z, b.z)); }
+inline V3 vmax(V3 a, V3 b) { return V3(smax(a.x, b.x), smax(a.y, b.y), smax(a.z, b.z)); }
+inline Bounds unite(const Bounds& b, V3 p) { Bounds r; r.lo = vmin(b.lo, p); r.hi = vmax(b.hi, p); return r; }
+inline Bounds unite(const Bounds& a, const Bounds& b) { Bounds r; r.lo = vmin(a.lo, b.lo); r.hi = vmax(a.hi, b.hi); return r; }
+inline real surface_area(const Bounds& b) {
+  V3 d = b.hi - b.lo;
+  return 2 * (d.x * d.y + d.x * d.z + d.y * d.z);
+}
+inline int max_extent(const Bounds& b) {
+  V3 d = b.hi - b.lo;
+  if (d.x > d.y && d.x > d.z) return 0;
+  if (d.y > d.z) return 1;
+  return 2;
+}
+
+struct Node {  // LinearBVHNode (accelerator/bvh.cpp:51-64)
+  Bounds b;
+  int32_t offset;
+  uint16_t count;
+  uint8_t axis;
+};
+
+struct Camera {
+  real m[16];  // camera_to_world.m
+  real focal_distance, lens_radius, film_w, film_h;
+};
+
+struct Scene {
+  std::vector<Tri> tris;
+  std::vector<Sphere> spheres;
+  std::vector<Mat> mats;
+  std::vector<Prim> prims;
+  std::vector<int> lights;       // primitive ids in scene.lights order
+  std::vector<Node> nodes;
+  std::vector<int> order;        // leaf slot -> primitive id
+  int max_leaf = 1;
+  Camera cam;
+  real filter_radius = 0.5f, filter_alpha = 2, filter_exp = 0;
+};
+
+// ------------------------------------------------------------ shapes: bounds
+// shape/triangle.cpp:47-52
+inline Bounds tri_bound(const Tri& t) {
+  Bounds b;
+  b.lo = V3(smin(t.A.x, t.B.x), smin(t.A.y, t.B.y), smin(t.A.z, t.B.z));
+  b.hi = V3(smax(t.A.x, t.B.x), smax(t.A.y, t.B.y), smax(t.A.z, t.B.z));
+  return unite(b, t.C);
+}
+// shape/sphere.cpp:121-127
+inline Bounds sphere_bound(const Sphere& s) {
+  V3 o = xform_point(s.m, V3(0, 0, 0));
+  Bounds b;
+  b.lo = o - V3(s.world_radius + kEps);
+  b.hi = o + V3(s.world_radius + kEps);
+  return b;
+}
+inline Bounds prim_bound(const Scene& sc, int p) {
+  const Prim& pr = sc.prims[p];
+  return pr.kind == 0 ? tri_bound(sc.tris[pr.shape]) : sphere_bound(sc.spheres[pr.shape]);
+}
+
+// ------------------------------------------------------------- BVH build
+// accelerator/bvh.cpp:15-23
+struct PrimInfo {
+  size_t index;
+  Bounds b;
+  V3 c;
+};
+struct BuildNode {
+  Bounds b;
+  int left = -1, right = -1, axis = 0;
+  size_t first = 0, count = 0;
+};
+
+struct Builder {
+  Scene& sc;
+  std::vector<PrimInfo>& info;
+  std::vector<BuildNode> nodes;
+  std::vector<int> ordered;
+  int max_leaf;
+
+  // accelerator/bvh.cpp:191-288
+  int build(size_t start, size_t end) {
+    int id = (int)nodes.size();
+    nodes.emplace_back();
+    Bounds bounds;
+    for (size_t i = start; i < end; ++i) bounds = unite(bounds, info[i].b);
+    size_t n = end - start;
+    auto leaf = [&]() {
+      size_t first = ordered.size();
+      for (size_t i = start; i < end; ++i) ordered.push_back((int)info[i].index);
+      nodes[id].first = first;
+      nodes[id].count = n;
+      nodes[id].b = bounds;
+    };
+    if (n == 1) {
+      leaf();
+      return id;
+    }
+    Bounds cb;
+    for (size_t i = start; i < end; ++i) cb = unite(cb, info[i].c);
+    int mid = (int)((start + end) >> 1);
+    int dim = max_extent(cb);
+    if (cb.hi[dim] == cb.lo[dim]) {
+      leaf();
+      return id;
+    }
+    // Bounds3::offset(p)[dim] (geometry.hpp:745-751), then the bucket index
+    auto bucket_of = [&](V3 c) {
+      real o = c[dim] - cb.lo[dim];
+      if (cb.hi[dim] > cb.lo[dim]) o /= cb.hi[dim] - cb.lo[dim];
+      int b = (int)(12 * o);
+      if (b == 12) b = 11;
+      return b;
+    };
+    if (n <= 2) {
+      std::nth_element(&info[start], &info[mid], &info[end - 1] + 1,
+                       [dim](const PrimInfo& a, const PrimInfo& b) { return a.c[dim] < b.c[dim]; });
+    } else {
+      size_t cnt[12] = {0};
+      Bounds bb[12];
+      for (size_t i = start; i < end; ++i) {
+        int b = bucket_of(info[i].c);
+        cnt[b]++;
+        bb[b] = unite(bb[b], info[i].b);
+      }
+      real cost[11];
+      for (int i = 0; i < 11; ++i) {
+        Bounds lb, rb;
+        int lc = 0, rc = 0;
+        for (int j = 0; j <= i; ++j) { lb = unite(lb, bb[j]); lc += (int)cnt[j]; }
+        for (int j = i + 1; j < 12; ++j) { rb = unite(rb, bb[j]); rc += (int)cnt[j]; }
+        cost[i] = 1 + (lc * surface_area(lb) + rc * surface_area(rb)) / surface_area(bounds);
+      }
+      long minb = std::min_element(cost, cost + 11) - cost;
+      if (n > (size_t)max_leaf) {
+        PrimInfo* pm = std::partition(&info[start], &info[end - 1] + 1,
+                                      [&](const PrimInfo& pi) { return bucket_of(pi.c) <= minb; });
+        mid = (int)(pm - &info[0]);
+      } else {
+        leaf();
+        return id;
+      }
+    }
+    // The reference passes both recursive calls as arguments of
+    // init_interior (bvh.cpp:283-284); GCC evaluates them right to left, so
+    // the right subtree claims its leaf slots first.
+    int r = build((size_t)mid, end);
+    int l = build(start, (size_t)mid);
+    nodes[id].left = l;
+    nodes[id].right = r;
+    nodes[id].axis = dim;
+    nodes[id].b = unite(nodes[l].b, nodes[r].b);
+    nodes[id].count = 0;
+    return id;
+  }
+  // accelerator/bvh.cpp:290-306
+  int flatten(int b, std::vector<Node>& out) {
+    int off = (int)out.size();
+    out.emplace_back();
+    out[off].b = nodes[b].b;
+    if (nodes[b].count > 0) {
+      out[off].count = (uint16_t)nodes[b].count;
+      out[off].offset = (int32_t)nodes[b].first;
+      out[off].axis = 0;
+    } else {
+      out[off].axis = (uint8_t)nodes[b].axis;
+      out[off].count = 0;
+      flatten(nodes[b].left, out);
+      out[off].offset = flatten(nodes[b].right, out);
+    }
+    return off;
+  }
+};
+
+// accelerator/bvh.cpp:78-105
+void build_bvh(Scene& sc) {
+  sc.nodes.clear();
+  sc.order.clear();
+  size_t n = sc.prims.size();
+  if (!n) return;
+  std::vector<PrimInfo> info(n);
+  for (size_t i = 0; i < n; ++i) {
+    info[i].index = i;
+    info[i].b = prim_bound(sc, (int)i);
+    // 0.5 * low + 0.5 * high: double scale, float point, float add
+    V3 a((real)(0.5 * info[i].b.lo.x), (real)(0.5 * info[i].b.lo.y), (real)(0.5 * info[i].b.lo.z));
+    V3 b((real)(0.5 * info[i].b.hi.x), (real)(0.5 * info[i].b.hi.y), (real)(0.5 * info[i].b.hi.z));
+    info[i].c = a + b;
+  }
+  Builder bl{sc, info, {}, {}, sc.max_leaf};
+  bl.nodes.reserve(2 * n);
+  int root = bl.build(0, n);
+  bl.flatten(root, sc.nodes);
+  sc.order = bl.ordered;
+}
+
+// ------------------------------------------------------------- traversal
+struct Ray {
+  V3 o, d;
+  real t_min = 0, t_max = kRealMax;
+};
+// Ray(o, d, t_min, t_max) normalises d (geometry.hpp:791-793)
+inline Ray make_ray(V3 o, V3 d, real tmin = 0, real tmax = kRealMax) {
+  Ray r;
+  r.o = o;
+  r.d = normalize(d);
+  r.t_min = tmin;
+  r.t_max = tmax;
+  return r;
+}
+
+// geometry.hpp:837-864
+inline bool box_hit(const Bounds& b, const Ray& r, V3 inv, const int neg[3]) {
+  const V3* bs[2] = {&b.lo, &b.hi};
+  real tMin = ((*bs[neg[0]]).x - r.o.x) * inv.x;
+  real tMax = ((*bs[1 - neg[0]]).x - r.o.x) * inv.x;
+  real tyMin = ((*bs[neg[1]]).y - r.o.y) * inv.y;
+  real tyMax = ((*bs[1 - neg[1]]).y - r.o.y) * inv.y;
+  tMax *= 1 + 0.0000001;
+  tyMax *= 1 + 0.0000001;
+  if (tMin > tyMax || tyMin > tMax) return false;
+  if (tyMin > tMin) tMin = tyMin;
+  if (tyMax < tMax) tMax = tyMax;
+  real tzMin = ((*bs[neg[2]]).z - r.o.z) * inv.z;
+  real tzMax = ((*bs[1 - neg[2]]).z - r.o.z) * inv.z;
+  tzMax *= 1 + 0.0000001;
+  if (tMin > tzMax || tzMin > tMax) return false;
+  if (tzMin > tMin) tMin = tzMin;
+  if (tzMax < tMax) tMax = tzMax;
+  return (tMin < r.t_max) && (tMax > 0);
+}
+
+// Möller-Trumbore core shared by Triangle::intersect and ::intersect_p
+// (shape/triangle.cpp:117-143, 145-174). Returns true and t on acceptance.
+inline bool tri_test(const Tri& T, const Ray& r, real& t, real& alpha, real& beta) {
+  const V3 AB = T.B - T.A;
+  const V3 AC = T.C - T.A;
+  V3 s1 = cross(r.d, AC);
+  real div = dot(s1, AB);
+  if (!div) return false;
+  real inv_div = 1 / div;
+  const V3 AO = r.o - T.A;
+  alpha = dot(AO, s1) * inv_div;
+  if (alpha < 0) return false;
+  V3 s2 = cross(AO, AB);
+  beta = dot(r.d, s2) * inv_div;
+  if (beta < 0 || alpha + beta > 1) return false;
+  t = dot(AC, s2) * inv_div;
+  if (t < r.t_min || t > r.t_max) return false;
+  return true;
+}
+
+// TransformedShape::to_local (shape/transformed_shape.hpp:17-21)
+inline Ray sphere_local_ray(const Sphere& s, const Ray& wr) {
+  return make_ray(xform_point(s.inv, wr.o), xform_vec(s.inv, wr.d), wr.t_min, wr.t_max);
+}
+// sphere::get_abc (shape/sphere.cpp:7-13); C widens to double as written
+inline void sphere_abc(real radius_square, const Ray& r, real& A, real& B, real& C) {
+  A = (real)(double)len2f(r.d);
+  B = 2 * dot(r.d, r.o);
+  C = (real)((double)len2f(r.o) - radius_square);
+}
+// sphere::intersect_p (shape/sphere.cpp:28-47), local ray
+inline bool sphere_test_p(const Ray& r, real radius, real& t) {
+  real A, B, C;
+  sphere_abc(radius * radius, r, A, B, C);
+  real delta = B * B - 4 * A * C;
+  if (delta < 0) return false;
+  delta = std::sqrt(delta);
+  real inv2A = real(0.5) / A;
+  real t0 = (-B - delta) * inv2A;
+  real t1 = (-B + delta) * inv2A;
+  if (r.t_max < t0 || t1 < r.t_min) return false;
+  bool not_t0 = t0 < r.t_min;
+  if (not_t0 && t1 > r.t_max) return false;
+  t = not_t0 ? t1 : t0;
+  return true;
+}
+// sphere::intersect (shape/sphere.cpp:15-27)
+inline bool sphere_test_any(const Ray& r, real radius) {
+  real A, B, C;
+  sphere_abc(radius * radius, r, A, B, C);
+  real delta = B * B - 4 * A * C;
+  if (delta < 0) return false;
+  delta = std::sqrt(delta);
+  const real inv2A = real(0.5) / A;
+  const real t0 = (-B - delta) * inv2A;
+  const real t1 = (-B + delta) * inv2A;
+  return (r.t_min <= t0 && t0 <= r.t_max) || (r.t_min <= t1 && t1 <= r.t_max);
+}
+
+struct Counters {
+  uint64_t nodes = 0, prims = 0;
+};
+
+// BVHAccel::intersect_p (accelerator/bvh.cpp:149-185) with the
+// GeometricPrimitive t_max update (shape/geometry.cpp:49-60). Returns the
+// primitive id or -1; ray.t_max holds what the reference leaves there.
+// Sphere::intersect_p never writes its hit_t argument (shape/sphere.cpp:98-119),
+// so after a sphere hit GeometricPrimitive stores the initial 0.0 into
+// ray.t_max: the first sphere hit in traversal order ends the search for
+// everything not at t <= 0. *hit_t receives the accepted primitive's own
+// parameter (the local sphere t for spheres), which the hit record uses.
+int closest_hit(const Scene& sc, Ray& ray, Counters* cnt, real* hit_t = nullptr) {
+  if (sc.nodes.empty()) return -1;
+  V3 inv((real)(1.0 / ray.d.x), (real)(1.0 / ray.d.y), (real)(1.0 / ray.d.z));
+  int neg[3] = {inv.x < 0, inv.y < 0, inv.z < 0};
+  int hit = -1;
+  std::vector<size_t> stack;
+  stack.reserve(64);
+  stack.push_back(0);
+  while (!stack.empty()) {
+    size_t ni = stack.back();
+    stack.pop_back();
+    const Node& nd = sc.nodes[ni];
+    if (cnt) cnt->nodes++;
+    if (!box_hit(nd.b, ray, inv, neg)) continue;
+    if (nd.count > 0) {
+      for (int i = 0; i < nd.count; ++i) {
+        int p = sc.order[nd.offset + i];
+        const Prim& pr = sc.prims[p];
+        if (cnt) cnt->prims++;
+        real t;
+        if (pr.kind == 0) {
+          real a, b;
+          if (tri_test(sc.tris[pr.shape], ray, t, a, b)) { ray.t_max = t; hit = p; if (hit_t) *hit_t = t; }
+        } else {
+          const Sphere& s = sc.spheres[pr.shape];
+          Ray lr = sphere_local_ray(s, ray);
+          if (sphere_test_p(lr, s.radius, t)) { ray.t_max = 0; hit = p; if (hit_t) *hit_t = t; }
+        }
+      }
+    } else {
+      if (neg[nd.axis]) {
+        stack.push_back(ni + 1);
+        stack.push_back((size_t)nd.offset);
+      } else {
+        stack.push_back((size_t)nd.offset);
+        stack.push_back(ni + 1);
+      }
+    }
+  }
+  return hit;
+}
+
+// BVHAccel::intersect (accelerator/bvh.cpp:112-147)
+bool any_hit(const Scene& sc, const Ray& ray, Counters* cnt) {
+  if (sc.nodes.empty()) return false;
+  V3 inv((real)(1.0 / ray.d.x), (real)(1.0 / ray.d.y), (real)(1.0 / ray.d.z));
+  int neg[3] = {inv.x < 0, inv.y < 0, inv.z < 0};
+  std::vector<size_t> stack;
+  stack.reserve(64);
+  stack.push_back(0);
+  while (!stack.empty()) {
+    size_t ni = stack.back();
+    stack.pop_back();
+    const Node& nd = sc.nodes[ni];
+    if (cnt) cnt->nodes++;
+    if (!box_hit(nd.b, ray, inv, neg)) continue;
+    if (nd.count > 0) {
+      for (int i = 0; i < nd.count; ++i) {
+        int p = sc.order[nd.offset + i];
+        const Prim& pr = sc.prims[p];
+        if (cnt) cnt->prims++;
+        if (pr.kind == 0) {
+          real t, a, b;
+          if (tri_test(sc.tris[pr.shape], ray, t, a, b)) return true;
+        } else {
+          const Sphere& s = sc.spheres[pr.shape];
+          if (sphere_test_any(sphere_local_ray(s, ray), s.radius)) return true;
+        }
+      }
+    } else {
+      if (neg[nd.axis]) {
+        stack.push_back(ni + 1);
+        stack.push_back((size_t)nd.offset);
+      } else {
+        stack.push_back((size_t)nd.offset);
+        stack.push_back(ni + 1);
+      }
+    }
+  }
+  return false;
+}
+
+// ------------------------------------------------------ surface interaction
+struct Isect {  // SurfaceIntersection (core/intersection.hpp:13-43)
+  V3 pos;
+  real uv[2];
+  Coord g, s;
+  V3 wo;
+  int prim = -1;
+  // SurfacePoint::eps_offset (intersection.hpp:19-23)
+  V3 eps_offset(V3 dir) const {
+    if (dot(g.z, dir) > 0) return pos + mulf(g.z, kEps);
+    return pos - mulf(g.z, kEps);
+  }
+};
+
+// Triangle::intersect_p hit record (shape/triangle.cpp:175-213)
+void tri_attributes(const Tri& T, const Ray& r, real t, real alpha, real beta, Isect& is) {
+  const V3 AB = T.B - T.A, AC = T.C - T.A;
+  is.uv[0] = T.uA[0] + alpha * (T.uB[0] - T.uA[0]) + beta * (T.uC[0] - T.uA[0]);
+  is.uv[1] = T.uA[1] + alpha * (T.uB[1] - T.uA[1]) + beta * (T.uC[1] - T.uA[1]);
+  is.wo = -r.d;
+  is.pos = r.o + mulf(r.d, t);
+  V3 gn = normalize(cross(AB, AC));
+  V3 dpdu, dpdv;
+  compute_ss_ts(AB, AC, T.uB[0] - T.uA[0], T.uB[1] - T.uA[1], T.uC[0] - T.uA[0], T.uC[1] - T.uA[1], gn,
+                dpdu, dpdv);
+  dpdu = cross(dpdv, gn);
+  dpdv = cross(gn, dpdu);
+  is.g = Coord(dpdu, dpdv, gn);
+  V3 sn = T.nA + mulf(T.nB - T.nA, alpha) + mulf(T.nC - T.nA, beta);
+  V3 dndu, dndv;
+  compute_ss_ts(T.nB - T.nA, T.nC - T.nA, T.uB[0] - T.uA[0], T.uB[1] - T.uA[1], T.uC[0] - T.uA[0],
+                T.uC[1] - T.uA[1], sn, dndu, dndv);
+  if ((real)(double)len2f(dndu) < kEps || (real)(double)len2f(dndv) < kEps) coordinate(sn, dndu, dndv);
+  dndu = cross(dndv, sn);
+  dndv = cross(sn, dndu);
+  is.s = Coord(dndu, dndv, sn);
+}
+
+// sphere::local_geometry_uv_and_coord (shape/sphere.cpp:48-78)
+void sphere_local_geometry(V3 p, real radius, real uv[2], Coord& c) {
+  real phi = (!p.x && !p.y) ? real(0) : std::atan2(p.y, p.x);
+  if (phi < 0) phi += 2 * kPi;
+  const real sin_theta = std::clamp<real>(p.z / radius, -1, 1);
+  const real theta = std::asin(sin_theta);
+  uv[0] = real(0.5) * kInvPi * phi;
+  uv[1] = kInvPi * theta + real(0.5);
+  V3 ex, ey, ez = normalize(p);
+  if (std::abs(ez.z - 1) < kEps) {
+    ex = V3(1, 0, 0); ey = V3(0, 1, 0); ez = V3(0, 0, 1);
+  } else if (std::abs(ez.z + 1) < kEps) {
+    ex = V3(0, 1, 0); ey = V3(1, 0, 0); ez = V3(0, 0, -1);
+  } else {
+    ex = cross(V3(0, 0, 1), ez);
+    ey = cross(ez, ex);
+  }
+  c = Coord(ex, ey, ez);
+}
+
+// Sphere::intersect_p hit record + to_world (shape/sphere.cpp:98-119,
+// transformed_shape.hpp:31-44)
+void sphere_attributes(const Sphere& s, const Ray& wr, real t, Isect& is) {
+  Ray lr = sphere_local_ray(s, wr);
+  V3 pos = lr.o + mulf(lr.d, t);
+  Coord c;
+  sphere_local_geometry(pos, s.radius, is.uv, c);
+  is.pos = xform_point(s.m, pos);
+  is.g = Coord(xform_vec(s.m, c.x), xform_vec(s.m, c.y), xform_vec(s.m, c.z));
+  is.s = is.g;
+  is.wo = xform_vec(s.m, -lr.d);
+}
+
+// Scene::intersect_p with the hit record of the closest primitive
+bool intersect_p(const Scene& sc, Ray& ray, Isect& is, Counters* cnt) {
+  Ray r0 = ray;
+  real hit_t = 0;
+  int p = closest_hit(sc, ray, cnt, &hit_t);
+  if (p < 0) return false;
+  const Prim& pr = sc.prims[p];
+  is.prim = p;
+  if (pr.kind == 0) {
+    // re-run the accepted test on the original ray to recover alpha, beta
+    // (t_max only gates acceptance; alpha, beta, t do not depend on it)
+    Ray rr = r0;
+    rr.t_max = hit_t;
+    real t, a, b;
+    tri_test(sc.tris[pr.shape], rr, t, a, b);
+    tri_attributes(sc.tris[pr.shape], r0, t, a, b, is);
+  } else {
+    sphere_attributes(sc.spheres[pr.shape], r0, hit_t, is);
+  }
+  return true;
+}
+
+// --------------------------------------------------------------- BSDFs
+struct BSDFSample {
+  V3 wi;
+  Sp f;
+  real pdf = 0;
+  bool valid() const { return pdf > 0 && !f.black(); }  // core/bsdf.hpp:21-23
+};
+
+// microfacet helpers (material/utility/microfacet.cpp:7-134, microfacet.hpp:10-14)
+inline real sqr(real x) { return x * x; }
+inline real one_minus_5(real x) { real t = 1 - x; real t2 = t * t; return t2 * t2 * t; }
+inline real compute_alpha(real s, real c, real ax, real ay) { return sqr(c / ax) + sqr(s / ay); }
+inline real anisotropic_gtr2(real sp, real cp, real st, real ct, real ax, real ay) {
+  const real A = compute_alpha(sp, cp, ax, ay);
+  const real RD = sqr(st) * A + sqr(ct);
+  return 1 / (kPi * ax * ay * sqr(RD));
+}
+inline real gtr1(real st, real ct, real alpha) {
+  if (alpha >= 1) return kInvPi;
+  const real U = sqr(alpha) - 1;
+  const real LD = 2 * kPi * std::log(alpha);
+  const real RD = sqr(alpha * ct) + sqr(st);
+  return U / (LD * RD);
+}
+inline real smith_anisotropic_gtr2(real cos_phi, real sin_phi, real ax, real ay, real tan_theta) {
+  const real t = sqr(ax * cos_phi) + sqr(ay * sin_phi);
+  const real sq = 1 + t * sqr(tan_theta);
+  const real lambda = -real(0.5) + real(0.5) * std::sqrt(sq);
+  return 1 / (1 + lambda);
+}
+inline real smith_gtr2(real tan_theta, real alpha) {
+  if (!tan_theta) return 1;
+  const real root = alpha * tan_theta;
+  return 2 / (1 + std::sqrt(1 + root * root));
+}
+inline V3 sample_anisotropic_gtr2(real ax, real ay, real u, real v) {
+  real sp = ay * std::sin(2 * kPi * u);
+  real cp = ax * std::cos(2 * kPi * u);
+  const real nor = 1 / std::sqrt(sqr(sp) + sqr(cp));
+  sp *= nor;
+  cp *= nor;
+  const real A = compute_alpha(sp, cp, ax, ay);
+  const real ct = std::sqrt(A * (1 - v) / ((1 - A) * v + A));
+  const real st = std::sqrt(std::max<real>(0, 1 - sqr(ct)));
+  return normalize(V3(st * cp, st * sp, ct));
+}
+inline V3 sample_gtr1(real alpha, real u, real v) {
+  const real phi = 2 * kPi * u;
+  const real ct = std::sqrt((std::pow(alpha, 2 - 2 * v) - 1) / (sqr(alpha) - 1));
+  const real st = local_cos_to_sin(ct);
+  return normalize(V3(st * std::cos(phi), st * std::sin(phi), ct));
+}
+// utility/reflection.hpp:12-14
+inline V3 reflect(V3 w, V3 n) { return mulf(n, 2 * dot(w, n)) - w; }
+
+// Phong specular lobe (material/bxdf/phong_specular_bxdf.cpp:10-71)
+inline real powcos_pdf(real e, real c) { return (e + 1) * kInv2Pi * std::pow(c, e); }
+inline Sp phong_eval(const Mat& m, V3 lwi, V3 lwo) {
+  if (lwi.z <= 0 || lwo.z <= 0) return Sp();
+  const V3 ideal = reflect(lwo, V3(0, 0, 1));
+  const real c = dot(ideal, lwi) / (length(lwi) * length(ideal));
+  if (c <= 0) return Sp();
+  return m.specular * powcos_pdf(m.ns, c);
+}
+inline real phong_pdf(const Mat& m, V3 lwi, V3 lwo) {
+  if (lwi.z <= 0 || lwo.z <= 0) return 0;
+  const V3 ideal = reflect(lwo, V3(0, 0, 1));
+  const real c = cosv(lwi, ideal);
+  if (c <= 0) return 0;
+  return powcos_pdf(m.ns, c);
+}
+inline bool phong_sample(const Mat& m, V3 lwo, real u, real v, V3& lwi_out, Sp& f, real& pdf) {
+  if (lwo.z <= 0) return false;
+  const V3 ideal = normalize(reflect(lwo, V3(0, 0, 1)));
+  const real ct = std::pow(u, 1 / (m.ns + 1));
+  const real st = std::sqrt(std::max<real>(0, 1 - ct * ct));
+  const real phi = 2 * kPi * v;
+  V3 local = normalize(V3(st * std::cos(phi), st * std::sin(phi), ct));
+  V3 lwi = normalize(Coord::from_z(ideal).to_global(local));
+  if (lwi.z <= 0) return false;
+  pdf = powcos_pdf(m.ns, local.z);
+  f = phong_eval(m, lwi, lwo);
+  lwi_out = lwi;
+  return pdf > 0;
+}
+// DiffuseBXDF (material/bxdf/diffuse_bxdf.cpp:14-38)
+inline Sp diffuse_eval(const Mat& m, V3 lwi, V3 lwo) {
+  if (lwi.z <= 0 || lwo.z <= 0) return Sp();
+  return m.diffuse_coef;
+}
+inline real diffuse_pdf(V3 lwi, V3 lwo) {
+  if (lwi.z <= 0 || lwo.z <= 0) return 0;
+  return cosine_pdf(lwi.z);
+}
+
+struct BSDF {
+  const Mat* m;
+  Coord g, s;
+
+  // LocalBSDF black-fringe helpers (core/bsdf.hpp:55-91)
+  bool fringe(V3 w) const { return g.pos_hemi(w) ^ s.pos_hemi(w); }
+  bool fringe(V3 a, V3 b) const { return fringe(a) | fringe(b); }
+  Sp albedo() const { return m->kind == TR_MAT_PHONG ? m->albedo : m->base; }
+  Sp eval_fringe(V3 wi, V3 wo) const {
+    if (g.pos_hemi(wi) & g.pos_hemi(wo)) return albedo() * kInvPi;
+    return Sp(0);
+  }
+  BSDFSample sample_fringe(V3 wo, real u, real v) const {
+    BSDFSample r;
+    if (!g.pos_hemi(wo)) return r;
+    V3 lwi = cosine_hemisphere(u, v);
+    real pdf = cosine_pdf(lwi.z);
+    if (pdf < kEps) return r;
+    V3 wi = normalize(g.to_global(lwi));
+    real nc = normal_correct_factor(g, s, wi);
+    r.wi = wi;
+    r.f = albedo() * kInvPi * nc;
+    r.pdf = pdf;
+    return r;
+  }
+  real pdf_fringe(V3 wi, V3 wo) const {
+    if (g.pos_hemi(wi) ^ g.pos_hemi(wo)) return 0;
+    return cosine_pdf(normalize(g.to_local(wi)).z);
+  }
+
+  // ---- AggregateBSDF<2> of Phong (material/aggregate_bsdf.hpp:36-118)
+  Sp phong_agg_eval(V3 wi, V3 wo) const {
+    if (fringe(wi, wo)) return eval_fringe(wi, wo);
+    V3 lwi = normalize(s.to_local(wi)), lwo = normalize(s.to_local(wo));
+    if (!lwi.z || !lwo.z) return Sp();
+    Sp r;
+    r += diffuse_eval(*m, lwi, lwo);
+    r += phong_eval(*m, lwi, lwo);
+    return r;
+  }
+  BSDFSample phong_agg_sample(V3 wo, real u, real v, real w) const {
+    if (fringe(wo)) return sample_fringe(wo, u, v);
+    BSDFSample out;
+    const V3 lwo = normalize(s.to_local(wo));
+    if (!lwo.z) return out;
+    real ws = 0;
+    ws += m->w_diffuse;
+    ws += m->w_specular;
+    real sel = (u - real(0.001)) * ws;
+    int which = -1;
+    real weight = 0;
+    const real wts[2] = {m->w_diffuse, m->w_specular};
+    for (int i = 0; i < 2; ++i) {
+      if (sel <= wts[i]) { which = i; weight = wts[i]; break; }
+      sel -= wts[i];
+    }
+    if (which < 0) return out;
+    V3 lwi;
+    Sp f;
+    real pdf;
+    if (which == 0) {
+      if (lwo.z <= 0) return out;
+      lwi = cosine_hemisphere(v, w);
+      pdf = cosine_pdf(lwi.z);
+      if (pdf < real(0.001)) return out;
+      f = m->diffuse_coef;
+    } else {
+      if (!phong_sample(*m, lwo, v, w, lwi, f, pdf)) return out;
+    }
+    lwi = normalize(lwi);
+    pdf *= weight;
+    if (which != 0) { f += diffuse_eval(*m, lwi, lwo); pdf += diffuse_pdf(lwi, lwo) * wts[0]; }
+    if (which != 1) { f += phong_eval(*m, lwi, lwo); pdf += phong_pdf(*m, lwi, lwo) * wts[1]; }
+    V3 wi = s.to_global(lwi);
+    real nc = normal_correct_factor(g, s, wi);
+    out.wi = wi;
+    out.f = f * nc;
+    out.pdf = pdf;
+    return out;
+  }
+  real phong_agg_pdf(V3 wi, V3 wo) const {
+    if (fringe(wi, wo)) return pdf_fringe(wi, wo);
+    V3 lwi = normalize(s.to_local(wi)), lwo = normalize(s.to_local(wo));
+    if (!lwi.z || !lwo.z) return 0;
+    real ws = 0, pdf = 0;
+    ws += m->w_diffuse;
+    pdf += m->w_diffuse * diffuse_pdf(lwi, lwo);
+    ws += m->w_specular;
+    pdf += m->w_specular * phong_pdf(*m, lwi, lwo);
+    return ws > 0 ? pdf / ws : 0;
+  }
+
+  // ---- DisneyBRDF (material/disney_brdf.cpp:56-227)
+  void disney_alphas(real& ax, real& ay) const {
+    real aspect = (real)std::sqrt(1 - m->anisotropic * 0.9);
+    ax = std::max<real>(0.001, m->roughness * m->roughness / aspect);
+    ay = std::max<real>(0.001, m->roughness * m->roughness * aspect);
+  }
+  Sp disney_eval(V3 wi, V3 wo) const {
+    if (fringe(wi, wo)) return eval_fringe(wi, wo);
+    const V3 lwi = normalize(s.to_local(wi));
+    const V3 lwo = normalize(s.to_local(wo));
+    if (lwi.z < kEps || lwo.z < kEps) return Sp();
+    const real NdotL = lwi.z, NdotV = lwo.z;
+    const V3 H = normalize(lwi + lwo);
+    const real LdotH = dot(lwi, H);
+    const Sp& bc = m->base;
+    real lum = bc.lum();
+    Sp Ctint = lum > 0 ? bc / lum : Sp(1);
+    Sp Cspec0 = mix(mix(Sp(1), Ctint, m->specular_tint) * (m->specular_s * 0.08f), bc, m->metallic);
+    Sp Csheen = mix(Sp(1), Ctint, m->sheen_tint);
+    Sp fd;
+    real ax, ay;
+    disney_alphas(ax, ay);
+    real phi_h = local_phi(H);
+    real sph = std::sin(phi_h), cph = std::cos(phi_h);
+    real Ds = anisotropic_gtr2(sph, cph, local_cos_to_sin(H.z), H.z, ax, ay);
+    real FH = one_minus_5(LdotH);
+    Sp Fs = mix(Cspec0, Sp(1), FH);
+    real phi_i = local_phi(lwi);
+    real spi = std::sin(phi_i), cpi = std::cos(phi_i);
+    real Gs = smith_anisotropic_gtr2(spi, cpi, ax, ay, local_tan_theta(lwi));
+    real phi_o = local_phi(lwo);
+    real spo = std::sin(phi_o), cpo = std::cos(phi_o);
+    Gs *= smith_anisotropic_gtr2(spo, cpo, ax, ay, local_tan_theta(lwo));
+    real Dr = gtr1(local_cos_to_sin(H.z), H.z, mixf(0.1f, 0.001f, m->clearcoat_gloss));
+    real Fr = mixf(0.04f, 1.0f, FH);
+    real Gr = smith_gtr2(local_tan_theta(lwi), 0.25f) * smith_gtr2(local_tan_theta(lwo), 0.25f);
+    fd += ((Fs * Ds) * Gs + 0.25f * m->clearcoat * Gr * Fr * Dr) / (4 * NdotL * NdotV);
+    if (m->metallic < 1) {
+      real FL = one_minus_5(NdotL), FV = one_minus_5(NdotV);
+      real Fd90 = (real)(0.5 + 2. * LdotH * LdotH * m->roughness);
+      real Fd = mixf(1, Fd90, FL) * mixf(1, Fd90, FV);
+      real Fss90 = LdotH * LdotH * m->roughness;
+      real Fss = mixf(1, Fss90, FL) * mixf(1, Fss90, FV);
+      real ss = (real)(1.25 * (Fss * (1.0 / (NdotL + NdotV) - 0.5) + 0.5));
+      Sp Fsheen = Csheen * (FH * m->sheen);
+      fd += ((bc * kInvPi) * mixf(Fd, ss, m->subsurface) + Fsheen) * (1 - m->metallic);
+    }
+    return fd * normal_correct_factor(g, s, wi);
+  }
+  real disney_pdf(V3 wi, V3 wo) const {
+    if (fringe(wi, wo)) return pdf_fringe(wi, wo);
+    real p_diffuse = std::min<real>(0.8, 1 - m->metallic);
+    real p_specular = (real)(1.0 / (1.0 + 0.5 * m->clearcoat));
+    real ax, ay;
+    disney_alphas(ax, ay);
+    const V3 lwi = normalize(s.to_local(wi));
+    const V3 lwo = normalize(s.to_local(wo));
+    if (lwi.z < kEps) return 0;
+    const V3 H = normalize(lwi + lwo);
+    real pdf_diffuse = cosine_pdf(lwi.z);
+    real phi_h = local_phi(H);
+    real sph = std::sin(phi_h), cph = std::cos(phi_h);
+    real pdf_spec = anisotropic_gtr2(sph, cph, local_cos_to_sin(H.z), H.z, ax, ay) * H.z / (4 * dot(lwi, H));
+    real pdf_cc = gtr1(sph, cph, m->clearcoat_gloss) * H.z / (4 * dot(lwi, H));
+    real pdf = p_diffuse * pdf_diffuse + (1 - pdf_diffuse) * (p_specular * pdf_spec + (1 - p_specular) * pdf_cc);
+    if (!std::isfinite(pdf)) return 0;
+    return pdf;
+  }
+  BSDFSample disney_sample(V3 wo, real u, real v, real w) const {
+    if (fringe(wo)) return sample_fringe(wo, u, v);
+    BSDFSample r;
+    real p_diffuse = std::min<real>(0.8, 1 - m->metallic);
+    real p_specular = (real)(1.0 / (1.0 + 0.5 * m->clearcoat) * (1 - p_diffuse));
+    const V3 lwo = normalize(s.to_local(wo));
+    V3 lwi;
+    real sel = u;
+    real ax, ay;
+    disney_alphas(ax, ay);
+    if (sel < p_diffuse) lwi = cosine_hemisphere(v, w);
+    sel -= p_diffuse;
+    if (sel < p_specular) {
+      const V3 lwh = sample_anisotropic_gtr2(ax, ay, v, w);
+      if (lwh.z > 0) {
+        lwi = normalize(mulf(lwh, 2 * dot(lwo, lwh)) - lwo);
+        if (lwi.z <= 0) lwi = V3();
+      }
+    } else {
+      const V3 lwh = sample_gtr1(m->clearcoat_gloss, v, w);
+      if (lwh.z > 0) {
+        lwi = normalize(mulf(lwh, 2 * dot(lwo, lwh)) - lwo);
+        if (lwi.z <= 0) lwi = V3();
+      }
+    }
+    if (all_zero(lwi)) return r;
+    r.wi = s.to_global(lwi);
+    r.f = disney_eval(r.wi, wo);
+    r.pdf = disney_pdf(r.wi, wo);
+    return r;
+  }
+
+  Sp eval(V3 wi, V3 wo) const { return m->kind == TR_MAT_PHONG ? phong_agg_eval(wi, wo) : disney_eval(wi, wo); }
+  real pdf(V3 wi, V3 wo) const { return m->kind == TR_MAT_PHONG ? phong_agg_pdf(wi, wo) : disney_pdf(wi, wo); }
+  BSDFSample sample(V3 wo, real u, real v, real w) const {
+    return m->kind == TR_MAT_PHONG ? phong_agg_sample(wo, u, v, w) : disney_sample(wo, u, v, w);
+  }
+};
+
+// --------------------------------------------------------------- lights
+// Triangle::surface_area (shape/triangle.cpp:54-59)
+inline real tri_area(const Tri& T) { return (real)(0.5 * length(cross(T.B - T.A, T.C - T.A))); }
+
+struct LightSample {
+  V3 pos;
+  Sp radiance;
+  real pdf = 0;
+};
+// DiffuseLight::sample_li over Triangle::sample (light/diffuse_light.cpp:44-60,
+// shape/triangle.cpp:61-97, core/sampling.hpp:235-238)
+LightSample light_sample_li(const Scene& sc, int prim, V3 ref, real u, real v) {
+  LightSample out;
+  const Prim& pr = sc.prims[prim];
+  const Tri& T = sc.tris[pr.shape];
+  real su0 = std::sqrt(u);
+  real bx = 1 - su0, by = v * su0;
+  const V3 AB = T.B - T.A, AC = T.C - T.A;
+  V3 pos = mulf(T.A, bx) + mulf(T.B, by) + mulf(T.C, (1 - bx - by));
+  V3 gn = normalize(cross(AB, AC));
+  V3 dpdu, dpdv;
+  compute_ss_ts(AB, AC, T.uB[0] - T.uA[0], T.uB[1] - T.uA[1], T.uC[0] - T.uA[0], T.uC[1] - T.uA[1], gn, dpdu,
+                dpdv);
+  Coord gc(dpdu, dpdv, gn);
+  real area_pdf = 1 / tri_area(T);
+  if (dot(gc.z, ref - pos) <= 0) return out;
+  V3 sp2ref = ref - pos;
+  real dist2 = len2f(sp2ref);
+  out.pdf = (real)(area_pdf * dist2 / std::abs(dot(gc.z, sp2ref) / length(sp2ref)));
+  out.pos = pos;
+  out.radiance = pr.emission;
+  return out;
+}
+// DiffuseLight::pdf (light/diffuse_light.cpp:31-42)
+real light_pdf(const Scene& sc, int prim, V3 ref, V3 pos, V3 n) {
+  if (dot(n, ref - pos) <= 0) return 0;
+  real area = tri_area(sc.tris[sc.prims[prim].shape]);
+  const V3 p2ref = ref - pos;
+  real dist2 = len2f(p2ref);
+  real abscos = (real)std::abs(dot(n, p2ref) / (length(n) * length(p2ref)));
+  area *= abscos;
+  return dist2 / area;
+}
+// DiffuseLight::light_emit (light/diffuse_light.cpp:22-24)
+inline Sp light_emit(const Scene& sc, int prim, const Isect& is, V3 w) {
+  return dot(is.g.z, w) > 0 ? sc.prims[prim].emission : Sp(0);
+}
+
+// ---------------------------------------------------------- ray recording
+struct RayLog {
+  std::vector<tr_ray> closest, any;
+  std::vector<int32_t> closest_prim;
+  std::vector<float> closest_t;
+  std::vector<uint8_t> any_hit;
+};
+inline tr_ray to_tr(const Ray& r) {
+  tr_ray t;
+  t.o[0] = r.o.x; t.o[1] = r.o.y; t.o[2] = r.o.z;
+  t.d[0] = r.d.x; t.d[1] = r.d.y; t.d[2] = r.d.z;
+  t.t_min = r.t_min; t.t_max = r.t_max;
+  return t;
+}
+
+struct Tracer {
+  const Scene& sc;
+  RayLog* log;
+  Counters* cnt;
+  bool trace_p(Ray& r, Isect& is) {
+    tr_ray in = to_tr(r);
+    bool h = intersect_p(sc, r, is, cnt);
+    if (log) {
+      log->closest.push_back(in);
+      log->closest_prim.push_back(h ? is.prim : -1);
+      log->closest_t.push_back(r.t_max);
+    }
+    return h;
+  }
+  bool trace_any(const Ray& r) {
+    bool h = any_hit(sc, r, cnt);
+    if (log) {
+      log->any.push_back(to_tr(r));
+      log->any_hit.push_back(h ? 1 : 0);
+    }
+    return h;
+  }
+};
+
+// ---------------------------------------------------------- integrator
+// sample_area_light (renderer/direct_illumination.cpp:35-71)
+Sp sample_area_light(Tracer& tr, int light, const Isect& is, const BSDF& bsdf, Sampler& smp) {
+  const real u = smp.u(), v = smp.u();
+  smp.u(); smp.u(); smp.u();
+  LightSample ls = light_sample_li(tr.sc, light, is.pos, u, v);
+  if (ls.radiance.black() || !ls.pdf) return Sp();
+  V3 to_light = ls.pos - is.pos;
+  double dist = length(to_light) - kEps;
+  if (dist <= kEps) return Sp();
+  to_light = normalize(to_light);
+  const Ray shadow = make_ray(is.pos, to_light, kEps, (real)dist);
+  if (tr.trace_any(shadow)) return Sp();
+  const Sp bf = bsdf.eval(to_light, is.wo);
+  if (bf.black()) return Sp();
+  const real bpdf = bsdf.pdf(to_light, is.wo);
+  const Sp f = ((Sp(1) * ls.radiance) * bf) * abs_cos(to_light, is.g.z);
+  float weight = power_heuristic(ls.pdf, bpdf);
+  return (f * weight) / ls.pdf;
+}
+// sample_bsdf (renderer/direct_illumination.cpp:144-198)
+Sp sample_bsdf_mis(Tracer& tr, const Isect& is, const BSDF& bsdf, Sampler& smp) {
+  const real u = smp.u(), v = smp.u(), w = smp.u();
+  BSDFSample bs = bsdf.sample(is.wo, u, v, w);
+  if (!bs.valid()) return Sp();
+  bs.wi = normalize(bs.wi);
+  Ray ray = make_ray(is.eps_offset(bs.wi), bs.wi);
+  Isect t;
+  if (!tr.trace_p(ray, t)) return Sp();
+  const Prim& pr = tr.sc.prims[t.prim];
+  if (!pr.light) return Sp();
+  Sp Le = light_emit(tr.sc, t.prim, t, t.wo);
+  if (Le.black()) return Sp();
+  Sp f = ((Sp(1) * Le) * bs.f) * abs_cos(is.g.z, ray.d);
+  real lpdf = light_pdf(tr.sc, t.prim, ray.o, t.pos, t.g.z);
+  real weight = power_heuristic(bs.pdf, lpdf);
+  return (f * weight) / bs.pdf;
+}
+
+// PathTraceRenderer::eval_pixel_li (renderer/path_trace_renderer.cpp:27-210)
+// for vacuum media, no environment light and non-delta BSDFs.
+Sp eval_li(Tracer& tr, Ray ray, Sampler& smp, int min_depth, int max_depth) {
+  const Scene& sc = tr.sc;
+  Sp coef(1), L(0);
+  for (int depth = 0; depth < max_depth; ++depth) {
+    if (depth > min_depth) {
+      if (smp.u() > 0.9) break;
+      coef = coef / (real)0.9;  // Color3::operator/=(T) with T = float
+    }
+    if (!coef.valid()) break;
+    Isect is;
+    bool found = tr.trace_p(ray, is);
+    if (depth == 0 && found && sc.prims[is.prim].light) L += coef * light_emit(sc, is.prim, is, -ray.d);
+    if (!found) break;
+    BSDF bsdf{&sc.mats[sc.prims[is.prim].material], is.g, is.s};
+    const real u = smp.u(), v = smp.u(), w = smp.u();
+    BSDFSample bs = bsdf.sample(is.wo, u, v, w);
+    if (bs.f.black() || bs.pdf < kEps) break;
+    Sp direct;
+    for (int li : sc.lights) direct += coef * sample_area_light(tr, li, is, bsdf, smp);
+    direct += coef * sample_bsdf_mis(tr, is, bsdf, smp);
+    L += direct * (real(1) / 1);
+    coef = coef * ((bs.f * abs_cos(is.g.z, bs.wi)) / bs.pdf);
+    if (!coef.valid()) break;
+    ray = make_ray(is.eps_offset(bs.wi), normalize(bs.wi));
+  }
+  if (!L.valid()) return Sp();
+  return L;
+}
+
+// ThinLensCamera (camera/thin_lens_camera.cpp:23-59) + look_at (utility/transform.cpp:96-124)
+void setup_camera(Camera& c, const tr_camera& p) {
+  V3 pos(p.pos[0], p.pos[1], p.pos[2]), target(p.target[0], p.target[1], p.target[2]);
+  V3 up(p.up[0], p.up[1], p.up[2]);
+  V3 dir = normalize(target - pos);
+  V3 right = normalize(cross(normalize(up), dir));
+  V3 new_up = cross(dir, right);
+  real m[16] = {right.x, new_up.x, dir.x, pos.x, right.y, new_up.y, dir.y, pos.y,
+                right.z, new_up.z, dir.z, pos.z, 0, 0, 0, 1};
+  std::memcpy(c.m, m, sizeof(m));
+  c.focal_distance = p.focal_dist;
+  c.lens_radius = p.lens_radius;
+  c.film_h = (real)(2 * p.focal_dist * std::tan(p.fov * 0.5));
+  c.film_w = p.film_aspect * c.film_h;
+}
+Ray generate_ray(const Camera& c, real fx, real fy, real lu, real lv) {
+  V3 film((real(0.5) - fx) * c.film_w, (real(0.5) - fy) * c.film_h, c.focal_distance);
+  real dx, dy;
+  concentric_disk(lu, lv, dx, dy);
+  V3 lens(c.lens_radius * dx, c.lens_radius * dy, 0);
+  Ray r;
+  r.o = xform_point(c.m, lens);
+  r.d = xform_vec(c.m, normalize(film - lens));
+  return r;
+}
+
+// GaussianFilter (filter/gaussian_filter.cpp:9-31)
+inline real gaussian(real alpha, real d, real expv) { return std::max((real)0, real(std::exp(-alpha * d * d) - expv)); }
+
+struct TilePx {
+  Sp c;
+  real w = 0;
+};
+
+// Film::Tile::add_sample (core/render.hpp:37-57) into a per-pixel tile
+struct PixelTile {
+  int x0, y0, x1, y1;  // tile pixel bounds [x0,x1) x [y0,y1)
+  TilePx px[64];
+};
+
+void pixel_tile_bounds(const Scene& sc, int W, int H, int x, int y, PixelTile& t) {
+  // Film::get_film_tile (core/render.hpp:79-88)
+  real r = sc.filter_radius;
+  int lx = (int)std::ceil((real)x - 0.5f - r), ly = (int)std::ceil((real)y - 0.5f - r);
+  int hx = (int)std::floor((real)(x + 1) - 0.5f + r) + 1, hy = (int)std::floor((real)(y + 1) - 0.5f + r) + 1;
+  t.x0 = std::max(lx, 0); t.y0 = std::max(ly, 0);
+  t.x1 = std::min(hx, W); t.y1 = std::min(hy, H);
+}
+
+void add_sample(const Scene& sc, PixelTile& t, real px, real py, Sp L) {
+  real r = sc.filter_radius;
+  real dx = px - 0.5f, dy = py - 0.5f;
+  int p0x = (int)std::ceil(dx - r), p0y = (int)std::ceil(dy - r);
+  int p1x = (int)std::floor(dx + r) + 1, p1y = (int)std::floor(dy + r) + 1;
+  p0x = std::max(p0x, t.x0); p0y = std::max(p0y, t.y0);
+  p1x = std::min(p1x, t.x1); p1y = std::min(p1y, t.y1);
+  int tw = t.x1 - t.x0;
+  for (int y = p0y; y < p1y; ++y)
+    for (int x = p0x; x < p1x; ++x) {
+      real ox = px - (real)(x + 0.5), oy = py - (real)(y + 0.5);
+      real fw = gaussian(sc.filter_alpha, ox, sc.filter_exp) * gaussian(sc.filter_alpha, oy, sc.filter_exp);
+      TilePx& p = t.px[(x - t.x0) + (y - t.y0) * tw];
+      p.c += (L * fw) * 1.0f;
+      p.w += fw;
+    }
+}
+
+template <class F>
+void parallel_for(int n, int threads, F&& f) {
+  if (threads <= 1) {
+    for (int i = 0; i < n; ++i) f(i, 0);
+    return;
+  }
+  std::atomic<int> next{0};
+  std::vector<std::thread> pool;
+  for (int t = 0; t < threads; ++t)
+    pool.emplace_back([&, t] {
+      for (;;) {
+        int i = next++;
+        if (i >= n) return;
+        f(i, t);
+      }
+    });
+  for (auto& th : pool) th.join();
+}
+
+}  // namespace orc
+
+using namespace orc;
+
+extern "C" {
+
+// Builds the scene the way the reference factories do (shape/triangle.cpp:216-236,
+// shape/sphere.cpp:83-92, material/phong.cpp:29-70) and the BVH.
+void* orc_scene_create(const tr_scene_desc* d) {
+  auto* sc = new Scene();
+  sc->max_leaf = d->max_leaf_prims;
+  const real I[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+  std::vector<V3> P(d->num_vertices), N(d->num_vertices);
+  for (uint32_t v = 0; v < d->num_vertices; ++v) {
+    // local_to_world is the identity Transform(): apply it like the reference
+    P[v] = xform_point(I, V3(d->positions[3 * v], d->positions[3 * v + 1], d->positions[3 * v + 2]));
+    V3 n = xform_normal(I, V3(d->normals[3 * v], d->normals[3 * v + 1], d->normals[3 * v + 2]));
+    N[v] = normalize(n);
+  }
+  sc->tris.resize(d->num_triangles);
+  for (uint32_t t = 0; t < d->num_triangles; ++t) {
+    Tri& T = sc->tris[t];
+    int i0 = d->indices[3 * t], i1 = d->indices[3 * t + 1], i2 = d->indices[3 * t + 2];
+    T.A = P[i0]; T.B = P[i1]; T.C = P[i2];
+    // Triangle::intersect_p/sample normalise the stored normals again on use
+    // (shape/triangle.cpp:73-75,182-184)
+    T.nA = normalize(N[i0]); T.nB = normalize(N[i1]); T.nC = normalize(N[i2]);
+    T.uA[0] = d->uvs[2 * i0]; T.uA[1] = d->uvs[2 * i0 + 1];
+    T.uB[0] = d->uvs[2 * i1]; T.uB[1] = d->uvs[2 * i1 + 1];
+    T.uC[0] = d->uvs[2 * i2]; T.uC[1] = d->uvs[2 * i2 + 1];
+  }
+  sc->spheres.resize(d->num_spheres);
+  for (uint32_t s = 0; s < d->num_spheres; ++s) {
+    Sphere& S = sc->spheres[s];
+    S.radius = d->sphere_radius[s];
+    std::memcpy(S.m, d->sphere_to_world + 16 * s, 64);
+    std::memcpy(S.inv, d->sphere_to_local + 16 * s, 64);
+    real ratio = (real)length(xform_vec(S.m, V3(1, 0, 0)));
+    S.world_radius = ratio * S.radius;
+  }
+  sc->mats.resize(d->num_materials);
+  for (uint32_t i = 0; i < d->num_materials; ++i) {
+    const tr_material& src = d->materials[i];
+    Mat& m = sc->mats[i];
+    m.kind = src.kind;
+    if (src.kind == TR_MAT_PHONG) {
+      Sp diffuse(src.kd[0], src.kd[1], src.kd[2]), spec(src.ks[0], src.ks[1], src.ks[2]);
+      real dem = 1;
+      dem = std::max(dem, diffuse.r + spec.r);
+      dem = std::max(dem, diffuse.g + spec.g);
+      dem = std::max(dem, diffuse.b + spec.b);
+      diffuse = diffuse / dem;
+      spec = spec / dem;
+      real dl = diffuse.lum(), sl = spec.lum();
+      real wd = (dl + sl > kEps) ? dl / (dl + sl) : real(0.5);
+      m.w_diffuse = wd;
+      m.w_specular = 1 - wd;
+      m.albedo = diffuse + spec;
+      m.diffuse_coef = diffuse / kPi;
+      m.specular = spec;
+      m.ns = src.ns;
+      m.base = diffuse;
+    } else {
+      m.base = Sp(src.base_color[0], src.base_color[1], src.base_color[2]);
+      m.subsurface = src.subsurface; m.metallic = src.metallic; m.specular_s = src.specular;
+      m.specular_tint = src.specular_tint; m.roughness = src.roughness; m.anisotropic = src.anisotropic;
+      m.sheen = src.sheen; m.sheen_tint = src.sheen_tint; m.clearcoat = src.clearcoat;
+      m.clearcoat_gloss = src.clearcoat_gloss;
+    }
+  }
+  sc->prims.resize(d->num_prims);
+  for (uint32_t p = 0; p < d->num_prims; ++p) {
+    Prim& pr = sc->prims[p];
+    int sh = d->prim_shape[p];
+    pr.kind = sh >= 0 ? 0 : 1;
+    pr.shape = sh >= 0 ? sh : ~sh;
+    pr.material = d->prim_material[p];
+    pr.emission = Sp(d->prim_emission[3 * p], d->prim_emission[3 * p + 1], d->prim_emission[3 * p + 2]);
+    pr.light = !pr.emission.black();
+  }
+  for (uint32_t l = 0; l < d->num_lights; ++l) sc->lights.push_back(d->light_prims[l]);
+  build_bvh(*sc);
+  return sc;
+}
+
+void orc_scene_destroy(void* h) { delete static_cast<Scene*>(h); }
+
+void orc_set_camera(void* h, const tr_camera* c, const tr_filter* f) {
+  Scene* sc = static_cast<Scene*>(h);
+  setup_camera(sc->cam, *c);
+  sc->filter_radius = f->radius;
+  sc->filter_alpha = f->alpha;
+  sc->filter_exp = std::exp(-f->alpha * f->radius * f->radius);
+}
+
+size_t orc_bvh_num_nodes(void* h) { return static_cast<Scene*>(h)->nodes.size(); }
+
+void orc_bvh_export(void* h, tr_bvh_node32* nodes, uint32_t* order) {
+  Scene* sc = static_cast<Scene*>(h);
+  for (size_t i = 0; i < sc->nodes.size(); ++i) {
+    const Node& n = sc->nodes[i];
+    tr_bvh_node32& o = nodes[i];
+    o.lo[0] = n.b.lo.x; o.lo[1] = n.b.lo.y; o.lo[2] = n.b.lo.z;
+    o.hi[0] = n.b.hi.x; o.hi[1] = n.b.hi.y; o.hi[2] = n.b.hi.z;
+    o.offset = n.offset; o.count = n.count; o.axis = n.axis; o.pad = 0;
+  }
+  for (size_t i = 0; i < sc->order.size(); ++i) order[i] = (uint32_t)sc->order[i];
+}
+
+void orc_make_ray(const float* o, const float* d, float t_min, float t_max, tr_ray* out) {
+  *out = to_tr(make_ray(V3(o[0], o[1], o[2]), V3(d[0], d[1], d[2]), t_min, t_max));
+}
+
+// Closest hit per ray; nodes/prims (optional) receive per-ray visit counts.
+void orc_trace_closest(void* h, const tr_ray* rays, size_t n, int32_t* prim, float* t, uint32_t* nodes,
+                       uint32_t* prims, int threads) {
+  Scene* sc = static_cast<Scene*>(h);
+  const size_t chunk = 4096;
+  parallel_for((int)((n + chunk - 1) / chunk), threads, [&](int c, int) {
+    for (size_t i = c * chunk; i < std::min(n, (c + 1) * chunk); ++i) {
+      Ray r;
+      r.o = V3(rays[i].o[0], rays[i].o[1], rays[i].o[2]);
+      r.d = V3(rays[i].d[0], rays[i].d[1], rays[i].d[2]);
+      r.t_min = rays[i].t_min;
+      r.t_max = rays[i].t_max;
+      Counters cnt;
+      prim[i] = closest_hit(*sc, r, &cnt);
+      t[i] = r.t_max;
+      if (nodes) nodes[i] = (uint32_t)cnt.nodes;
+      if (prims) prims[i] = (uint32_t)cnt.prims;
+    }
+  });
+}
+
+void orc_trace_any(void* h, const tr_ray* rays, size_t n, uint8_t* hit, uint32_t* nodes, uint32_t* prims,
+                   int threads) {
+  Scene* sc = static_cast<Scene*>(h);
+  const size_t chunk = 4096;
+  parallel_for((int)((n + chunk - 1) / chunk), threads, [&](int c, int) {
+    for (size_t i = c * chunk; i < std::min(n, (c + 1) * chunk); ++i) {
+      Ray r;
+      r.o = V3(rays[i].o[0], rays[i].o[1], rays[i].o[2]);
+      r.d = V3(rays[i].d[0], rays[i].d[1], rays[i].d[2]);
+      r.t_min = rays[i].t_min;
+      r.t_max = rays[i].t_max;
+      Counters cnt;
+      hit[i] = any_hit(*sc, r, &cnt) ? 1 : 0;
+      if (nodes) nodes[i] = (uint32_t)cnt.nodes;
+      if (prims) prims[i] = (uint32_t)cnt.prims;
+    }
+  });
+}
+
+// Per-pixel-seeded render over rows [row0, row1) (the whole film when
+// row1 <= row0). rgbw (float) or rgbw64 (double accumulation of the same
+// per-sample values) receive color sums and weights for all W*H pixels;
+// rows outside the range stay untouched. Returns the number of samples.
+uint64_t orc_render(void* h, const tr_render_params* p, int row0, int row1, float* rgbw, double* rgbw64,
+                    int threads) {
+  Scene* sc = static_cast<Scene*>(h);
+  const int W = p->width, H = p->height;
+  if (row1 <= row0) { row0 = 0; row1 = H; }
+  const int nrows = row1 - row0;
+  std::vector<std::vector<PixelTile>> tiles(nrows);
+  std::vector<std::vector<Sp>> sums64;  // unused placeholder for symmetry
+  std::vector<double> acc64;
+  if (rgbw64) acc64.assign((size_t)W * H * 4, 0.0);
+  std::vector<std::vector<double>> row64(rgbw64 ? nrows : 0);
+  parallel_for(nrows, threads, [&](int ri, int) {
+    int y = row0 + ri;
+    Tracer tr{*sc, nullptr, nullptr};
+    tiles[ri].resize(W);
+    if (rgbw64) row64[ri].assign((size_t)W * 4, 0.0);
+    for (int x = 0; x < W; ++x) {
+      PixelTile& tile = tiles[ri][x];
+      pixel_tile_bounds(*sc, W, H, x, y, tile);
+      std::memset(tile.px, 0, sizeof(tile.px));
+      Sampler smp((int)(p->seed_base + (uint32_t)y * (uint32_t)W + (uint32_t)x));
+      for (int i = 0; i < p->spp; ++i) {
+        const real fu = smp.u(), fv = smp.u();
+        const real lu = smp.u(), lv = smp.u();
+        const real pxf = x + fu, pyf = y + fv;
+        Ray ray = generate_ray(sc->cam, pxf / W, pyf / H, lu, lv);
+        Sp L = eval_li(tr, ray, smp, p->min_depth, p->max_depth);
+        if (std::isfinite(L.r) && std::isfinite(L.g) && std::isfinite(L.b)) {
+          add_sample(*sc, tile, pxf, pyf, L);
+          if (rgbw64 && sc->filter_radius <= 0.5f) {
+            // same per-sample terms, summed in double (own pixel only at r <= 0.5)
+            real ox = pxf - (real)(x + 0.5), oy = pyf - (real)(y + 0.5);
+            real fw = gaussian(sc->filter_alpha, ox, sc->filter_exp) * gaussian(sc->filter_alpha, oy, sc->filter_exp);
+            Sp c = (L * fw) * 1.0f;
+            double* a = &row64[ri][4 * x];
+            a[0] += c.r; a[1] += c.g; a[2] += c.b; a[3] += fw;
+          }
+        }
+      }
+    }
+  });
+  if (rgbw) {
+    std::vector<Sp> color((size_t)W * H);
+    std::vector<real> weight((size_t)W * H, 0);
+    for (int i = 0; i < W * H; ++i) {
+      color[i] = Sp(rgbw[4 * i], rgbw[4 * i + 1], rgbw[4 * i + 2]);
+      weight[i] = rgbw[4 * i + 3];
+    }
+    for (int ri = 0; ri < nrows; ++ri)
+      for (int x = 0; x < W; ++x) {
+        const PixelTile& t = tiles[ri][x];
+        int tw = t.x1 - t.x0;
+        for (int yy = t.y0; yy < t.y1; ++yy)
+          for (int xx = t.x0; xx < t.x1; ++xx) {
+            const TilePx& tp = t.px[(xx - t.x0) + (yy - t.y0) * tw];
+            color[xx + yy * W] += tp.c;
+            weight[xx + yy * W] += tp.w;
+          }
+      }
+    for (int i = 0; i < W * H; ++i) {
+      rgbw[4 * i] = color[i].r; rgbw[4 * i + 1] = color[i].g; rgbw[4 * i + 2] = color[i].b;
+      rgbw[4 * i + 3] = weight[i];
+    }
+  }
+  if (rgbw64)
+    for (int ri = 0; ri < nrows; ++ri)
+      for (int k = 0; k < W * 4; ++k) rgbw64[(size_t)(row0 + ri) * W * 4 + k] += row64[ri][k];
+  return (uint64_t)nrows * W * p->spp;
+}
+
+// Renders pixels [pix0, pix1) in row-major order on one thread and records
+// every closest-hit and any-hit query with its result (the ray-replay log).
+// Returns the number of closest rays; call orc_log_fetch to copy them out.
+static RayLog g_log;
+size_t orc_render_log(void* h, const tr_render_params* p, int pix0, int pix1, size_t* n_any) {
+  Scene* sc = static_cast<Scene*>(h);
+  g_log = RayLog();
+  Tracer tr{*sc, &g_log, nullptr};
+  const int W = p->width, H = p->height;
+  for (int pi = pix0; pi < pix1; ++pi) {
+    int x = pi % W, y = pi / W;
+    Sampler smp((int)(p->seed_base + (uint32_t)y * (uint32_t)W + (uint32_t)x));
+    for (int i = 0; i < p->spp; ++i) {
+      const real fu = smp.u(), fv = smp.u();
+      const real lu = smp.u(), lv = smp.u();
+      Ray ray = generate_ray(sc->cam, (x + fu) / W, (y + fv) / H, lu, lv);
+      eval_li(tr, ray, smp, p->min_depth, p->max_depth);
+    }
+  }
+  *n_any = g_log.any.size();
+  return g_log.closest.size();
+}
+void orc_log_fetch(tr_ray* closest, int32_t* prim, float* t, tr_ray* any, uint8_t* hit) {
+  std::memcpy(closest, g_log.closest.data(), g_log.closest.size() * sizeof(tr_ray));
+  std::memcpy(prim, g_log.closest_prim.data(), g_log.closest_prim.size() * 4);
+  std::memcpy(t, g_log.closest_t.data(), g_log.closest_t.size() * 4);
+  std::memcpy(any, g_log.any.data(), g_log.any.size() * sizeof(tr_ray));
+  std::memcpy(hit, g_log.any_hit.data(), g_log.any_hit.size());
+}
+
+// Unit entry points for kernel-level parity tests.
+void orc_cross(const float* a, const float* b, float* out, size_t n) {
+  for (size_t i = 0; i < n; ++i) {
+    V3 r = cross(V3(a[3 * i], a[3 * i + 1], a[3 * i + 2]), V3(b[3 * i], b[3 * i + 1], b[3 * i + 2]));
+    out[3 * i] = r.x; out[3 * i + 1] = r.y; out[3 * i + 2] = r.z;
+  }
+}
+void orc_normalize(const float* a, float* out, size_t n) {
+  for (size_t i = 0; i < n; ++i) {
+    V3 r = normalize(V3(a[3 * i], a[3 * i + 1], a[3 * i + 2]));
+    out[3 * i] = r.x; out[3 * i + 1] = r.y; out[3 * i + 2] = r.z;
+  }
+}
+void orc_slab_scale(const float* x, float* out, size_t n) {
+  for (size_t i = 0; i < n; ++i) {
+    real v = x[i];
+    v *= 1 + 0.0000001;
+    out[i] = v;
+  }
+}
+void orc_pcg_uniform(int seed, float* out, size_t n) {
+  Sampler s(seed);
+  for (size_t i = 0; i < n; ++i) out[i] = s.u();
+}
+
+}  // extern "C"

@@ -1,0 +1,209 @@
+"""ctypes mirror of include/tracer_gpu.h (the C ABI of the GPU path).
+
+The structures here are byte-for-byte the C structs; `SceneBuffers` keeps the
+numpy arrays a `tr_scene_desc` points into alive for as long as it is used.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+TR_OK = 0
+TR_ERR_ARG = 1
+TR_ERR_OOM = 2
+TR_ERR_QUEUE_OVERFLOW = 3
+TR_ERR_TIMEOUT = 4
+TR_ERR_CUDA = 5
+TR_ERR_STATE = 6
+TR_ERR_CANCELLED = 7
+TR_ERR_UNSUPPORTED = 8
+
+TR_MAT_PHONG = 0
+TR_MAT_DISNEY12 = 1
+
+f32p = C.POINTER(C.c_float)
+f64p = C.POINTER(C.c_double)
+i32p = C.POINTER(C.c_int32)
+u32p = C.POINTER(C.c_uint32)
+u8p = C.POINTER(C.c_uint8)
+
+
+class TrRay(C.Structure):
+    _fields_ = [("o", C.c_float * 3), ("d", C.c_float * 3), ("t_min", C.c_float), ("t_max", C.c_float)]
+
+
+RAY_DTYPE = np.dtype([("o", "<f4", 3), ("d", "<f4", 3), ("t_min", "<f4"), ("t_max", "<f4")])
+assert RAY_DTYPE.itemsize == C.sizeof(TrRay) == 32
+
+
+class TrBvhNode32(C.Structure):
+    _fields_ = [("lo", C.c_float * 3), ("hi", C.c_float * 3), ("offset", C.c_int32),
+                ("count", C.c_uint16), ("axis", C.c_uint8), ("pad", C.c_uint8)]
+
+
+NODE_DTYPE = np.dtype([("lo", "<f4", 3), ("hi", "<f4", 3), ("offset", "<i4"), ("count", "<u2"),
+                       ("axis", "u1"), ("pad", "u1")])
+assert NODE_DTYPE.itemsize == C.sizeof(TrBvhNode32) == 32
+
+
+class TrMaterial(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("ka", C.c_float * 3), ("kd", C.c_float * 3), ("ks", C.c_float * 3),
+                ("ns", C.c_float), ("base_color", C.c_float * 3),
+                ("subsurface", C.c_float), ("metallic", C.c_float), ("specular", C.c_float),
+                ("specular_tint", C.c_float), ("roughness", C.c_float), ("anisotropic", C.c_float),
+                ("sheen", C.c_float), ("sheen_tint", C.c_float), ("clearcoat", C.c_float),
+                ("clearcoat_gloss", C.c_float)]
+
+
+class TrSceneDesc(C.Structure):
+    _fields_ = [("num_vertices", C.c_uint32), ("positions", f32p), ("normals", f32p), ("uvs", f32p),
+                ("num_triangles", C.c_uint32), ("indices", i32p),
+                ("num_spheres", C.c_uint32), ("sphere_radius", f32p), ("sphere_to_world", f32p),
+                ("sphere_to_local", f32p),
+                ("num_materials", C.c_uint32), ("materials", C.POINTER(TrMaterial)),
+                ("num_prims", C.c_uint32), ("prim_shape", i32p), ("prim_material", i32p),
+                ("prim_emission", f32p),
+                ("num_lights", C.c_uint32), ("light_prims", i32p),
+                ("max_leaf_prims", C.c_int32)]
+
+
+class TrCamera(C.Structure):
+    _fields_ = [("film_aspect", C.c_float), ("pos", C.c_float * 3), ("target", C.c_float * 3),
+                ("up", C.c_float * 3), ("fov", C.c_float), ("lens_radius", C.c_float),
+                ("focal_dist", C.c_float)]
+
+
+class TrFilter(C.Structure):
+    _fields_ = [("radius", C.c_float), ("alpha", C.c_float)]
+
+
+class TrRenderParams(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32),
+                ("min_depth", C.c_int32), ("max_depth", C.c_int32),
+                ("direct_light_sample_num", C.c_int32), ("seed_base", C.c_uint32)]
+
+
+class TrStats(C.Structure):
+    _fields_ = [("samples", C.c_uint64), ("extend_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("iterations", C.c_uint64), ("device_ms", C.c_double)]
+
+
+def ptr(a: np.ndarray | None, ctype):
+    if a is None:
+        return C.cast(None, C.POINTER(ctype))
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+@dataclass
+class Material:
+    """One tr_material. kind=TR_MAT_PHONG uses ka/kd/ks/ns; Disney12 the rest."""
+    kind: int = TR_MAT_PHONG
+    ka: tuple = (0.0, 0.0, 0.0)
+    kd: tuple = (0.0, 0.0, 0.0)
+    ks: tuple = (0.0, 0.0, 0.0)
+    ns: float = 1.0
+    base_color: tuple = (0.0, 0.0, 0.0)
+    subsurface: float = 0.0
+    metallic: float = 0.0
+    specular: float = 0.0
+    specular_tint: float = 0.0
+    roughness: float = 0.0
+    anisotropic: float = 0.0
+    sheen: float = 0.0
+    sheen_tint: float = 0.0
+    clearcoat: float = 0.0
+    clearcoat_gloss: float = 0.0
+
+    def to_c(self) -> TrMaterial:
+        m = TrMaterial()
+        m.kind = self.kind
+        m.ka[:] = self.ka
+        m.kd[:] = self.kd
+        m.ks[:] = self.ks
+        m.ns = self.ns
+        m.base_color[:] = self.base_color
+        for k in ("subsurface", "metallic", "specular", "specular_tint", "roughness", "anisotropic",
+                  "sheen", "sheen_tint", "clearcoat", "clearcoat_gloss"):
+            setattr(m, k, getattr(self, k))
+        return m
+
+
+@dataclass
+class SceneBuffers:
+    """Owns the arrays of one scene and hands out a tr_scene_desc over them."""
+    positions: np.ndarray            # (V,3) f32
+    normals: np.ndarray              # (V,3) f32
+    uvs: np.ndarray                  # (V,2) f32
+    indices: np.ndarray              # (T,3) i32
+    sphere_radius: np.ndarray        # (S,) f32
+    sphere_to_world: np.ndarray      # (S,16) f32
+    sphere_to_local: np.ndarray      # (S,16) f32
+    materials: list                  # [Material]
+    prim_shape: np.ndarray           # (P,) i32
+    prim_material: np.ndarray        # (P,) i32
+    prim_emission: np.ndarray        # (P,3) f32
+    light_prims: np.ndarray          # (L,) i32
+    max_leaf_prims: int = 3
+    _keep: list = field(default_factory=list, repr=False)
+
+    def desc(self) -> TrSceneDesc:
+        arrs = {}
+        for name in ("positions", "normals", "uvs", "sphere_radius", "sphere_to_world", "sphere_to_local",
+                     "prim_emission"):
+            arrs[name] = np.ascontiguousarray(getattr(self, name), dtype=np.float32)
+        for name in ("indices", "prim_shape", "prim_material", "light_prims"):
+            arrs[name] = np.ascontiguousarray(getattr(self, name), dtype=np.int32)
+        mats = (TrMaterial * max(1, len(self.materials)))(*[m.to_c() for m in self.materials])
+        self._keep = [arrs, mats]
+        d = TrSceneDesc()
+        d.num_vertices = len(arrs["positions"])
+        d.positions = ptr(arrs["positions"], C.c_float)
+        d.normals = ptr(arrs["normals"], C.c_float)
+        d.uvs = ptr(arrs["uvs"], C.c_float)
+        d.num_triangles = len(arrs["indices"])
+        d.indices = ptr(arrs["indices"], C.c_int32)
+        d.num_spheres = len(arrs["sphere_radius"])
+        d.sphere_radius = ptr(arrs["sphere_radius"], C.c_float)
+        d.sphere_to_world = ptr(arrs["sphere_to_world"], C.c_float)
+        d.sphere_to_local = ptr(arrs["sphere_to_local"], C.c_float)
+        d.num_materials = len(self.materials)
+        d.materials = C.cast(mats, C.POINTER(TrMaterial))
+        d.num_prims = len(arrs["prim_shape"])
+        d.prim_shape = ptr(arrs["prim_shape"], C.c_int32)
+        d.prim_material = ptr(arrs["prim_material"], C.c_int32)
+        d.prim_emission = ptr(arrs["prim_emission"], C.c_float)
+        d.num_lights = len(arrs["light_prims"])
+        d.light_prims = ptr(arrs["light_prims"], C.c_int32)
+        d.max_leaf_prims = int(self.max_leaf_prims)
+        return d
+
+
+def make_camera(aspect, pos, target, up, fov_rad, lens_radius=0.0, focal_dist=1.0) -> TrCamera:
+    c = TrCamera()
+    c.film_aspect = aspect
+    c.pos[:] = pos
+    c.target[:] = target
+    c.up[:] = up
+    c.fov = fov_rad
+    c.lens_radius = lens_radius
+    c.focal_dist = focal_dist
+    return c
+
+
+def make_filter(radius=0.5, alpha=0.6) -> TrFilter:
+    f = TrFilter()
+    f.radius = radius
+    f.alpha = alpha
+    return f
+
+
+def make_params(width, height, spp, min_depth, max_depth, seed_base=0, direct_light_sample_num=1):
+    p = TrRenderParams()
+    p.width, p.height, p.spp = width, height, spp
+    p.min_depth, p.max_depth = min_depth, max_depth
+    p.direct_light_sample_num = direct_light_sample_num
+    p.seed_base = seed_base
+    return p

@@ -1,0 +1,300 @@
+"""Seeded synthetic workloads with the shapes of the reference's configurations.
+
+The reference ships no scene data (its OBJ demo scenes are not in its
+repository), so every workload here is procedural and seeded:
+
+* ``cornell``      -- Cornell box, 36 triangles, 2 emissive triangles, Lambert
+                      (Phong with ks = 0) walls, pinhole camera at (0,0,3.5).
+* ``traversal``    -- 1,048,576 random small triangles in the unit cube and
+                      rays from the cube surface (closest-hit and shadow).
+* ``disney_grid``  -- 16x16 Disney12 spheres on a ground quad, two 2x2 area
+                      lights at height 6.
+* ``random_scene`` -- small mixed triangle/sphere scenes for parity tests.
+
+Vertex data is emitted in world space exactly as ``tr_scene_desc`` wants it.
+Vertex normals are made fixed points of the reference's normalisation
+(``normalize(normalize(n)) == normalize(n)``): the reference re-normalises the
+stored mesh normals in place on every hit (src/shape/triangle.cpp:182-184), so
+only fixed points keep its results independent of hit order.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .abi import (RAY_DTYPE, TR_MAT_DISNEY12, TR_MAT_PHONG, Material, SceneBuffers, make_camera,
+                  make_filter, make_params)
+
+F32_MAX = np.float32(np.finfo(np.float32).max)
+
+
+def ref_normalize(v: np.ndarray) -> np.ndarray:
+    """The reference's normalize (src/utility/geometry.hpp:429-445,570-572),
+    vectorised: float32 sum of squares left to right, double sqrt, double
+    reciprocal, double product, rounded to float32. Each numpy ufunc is one
+    IEEE operation, so nothing fuses."""
+    v = np.asarray(v, dtype=np.float32)
+    x, y, z = v[..., 0], v[..., 1], v[..., 2]
+    s = np.multiply(x, x, dtype=np.float32)
+    s = np.add(s, np.multiply(y, y, dtype=np.float32), dtype=np.float32)
+    s = np.add(s, np.multiply(z, z, dtype=np.float32), dtype=np.float32)
+    length = np.sqrt(s.astype(np.float64))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        inv = np.float64(1.0) / length
+        out = np.stack([(x.astype(np.float64) * inv).astype(np.float32),
+                        (y.astype(np.float64) * inv).astype(np.float32),
+                        (z.astype(np.float64) * inv).astype(np.float32)], axis=-1)
+    return out
+
+
+def fixed_normal(n) -> np.ndarray:
+    """Unit normal that the reference's normalize maps to itself."""
+    v0 = np.asarray(n, dtype=np.float64)
+    v0 = (v0 / np.linalg.norm(v0)).astype(np.float32)
+    for attempt in range(64):
+        # some directions cycle under the rounding; nudge one component by ulps
+        v = v0.copy()
+        if attempt:
+            k = attempt % 3
+            v[k] = np.nextafter(v[k], np.float32(np.inf) if attempt % 2 else np.float32(-np.inf))
+            v0 = v.copy()
+        for _ in range(8):
+            w = ref_normalize(v)
+            if np.array_equal(w.view(np.uint32), v.view(np.uint32)):
+                return v
+            v = w
+    raise ValueError(f"no fixed point for normal {n}")
+
+
+def make_rays(o: np.ndarray, d: np.ndarray, t_min, t_max) -> np.ndarray:
+    """Rays through the reference Ray constructor (direction normalised in double)."""
+    n = len(o)
+    r = np.zeros(n, dtype=RAY_DTYPE)
+    r["o"] = np.asarray(o, dtype=np.float32)
+    r["d"] = ref_normalize(d)
+    r["t_min"] = t_min
+    r["t_max"] = t_max
+    return r
+
+
+class _Builder:
+    def __init__(self):
+        self.pos, self.nrm, self.uv, self.idx = [], [], [], []
+        self.sph_r, self.sph_m, self.sph_inv = [], [], []
+        self.mats: list[Material] = []
+        self.prim_shape, self.prim_mat, self.prim_em = [], [], []
+        self.lights = []
+
+    def material(self, m: Material) -> int:
+        self.mats.append(m)
+        return len(self.mats) - 1
+
+    def triangle(self, a, b, c, n, mat, emission=(0, 0, 0), uvs=((0, 0), (1, 0), (1, 1)), light=None):
+        nn = fixed_normal(n)
+        base = len(self.pos)
+        for p, t in zip((a, b, c), uvs):
+            self.pos.append(np.asarray(p, dtype=np.float32) + np.float32(0))  # no -0.0 in positions
+            self.nrm.append(nn)
+            self.uv.append(np.asarray(t, dtype=np.float32))
+        self.idx.append((base, base + 1, base + 2))
+        self.prim_shape.append(len(self.idx) - 1)
+        self.prim_mat.append(mat)
+        self.prim_em.append(emission)
+        pid = len(self.prim_shape) - 1
+        if any(e != 0 for e in emission) and light is not False:
+            self.lights.append(pid)
+        return pid
+
+    def quad(self, p0, p1, p2, p3, normal, mat, emission=(0, 0, 0)):
+        """Two triangles (p0,p1,p2), (p0,p2,p3), wound so cross(AB, AC) points along normal."""
+        p0, p1, p2, p3 = (np.asarray(p, dtype=np.float64) for p in (p0, p1, p2, p3))
+        if np.dot(np.cross(p1 - p0, p2 - p0), normal) < 0:
+            p1, p3 = p3, p1
+        self.triangle(p0, p1, p2, normal, mat, emission, ((0, 0), (1, 0), (1, 1)))
+        self.triangle(p0, p2, p3, normal, mat, emission, ((0, 0), (1, 1), (0, 1)))
+
+    def box(self, center, size, rot_y_deg, mat):
+        c = np.asarray(center, dtype=np.float64)
+        h = np.asarray(size, dtype=np.float64) / 2
+        th = math.radians(rot_y_deg)
+        R = np.array([[math.cos(th), 0, math.sin(th)], [0, 1, 0], [-math.sin(th), 0, math.cos(th)]])
+        def P(sx, sy, sz):
+            return c + R @ (h * np.array([sx, sy, sz], dtype=np.float64))
+        for axis in range(3):
+            for sgn in (-1, 1):
+                n = np.zeros(3); n[axis] = sgn
+                u_ax, v_ax = [a for a in range(3) if a != axis]
+                corners = []
+                for su, sv in ((-1, -1), (1, -1), (1, 1), (-1, 1)):
+                    s = [0, 0, 0]; s[axis] = sgn; s[u_ax] = su; s[v_ax] = sv
+                    corners.append(P(*s))
+                self.quad(*corners, R @ n, mat)
+
+    def sphere(self, center, radius, mat):
+        cx, cy, cz = (float(np.float32(v)) for v in center)
+        # translate(delta) builds m and its explicit inverse (src/utility/transform.cpp:155-165)
+        m = np.array([1, 0, 0, cx, 0, 1, 0, cy, 0, 0, 1, cz, 0, 0, 0, 1], dtype=np.float32)
+        inv = np.array([1, 0, 0, -cx, 0, 1, 0, -cy, 0, 0, 1, -cz, 0, 0, 0, 1], dtype=np.float32)
+        self.sph_r.append(radius)
+        self.sph_m.append(m)
+        self.sph_inv.append(inv)
+        self.prim_shape.append(~(len(self.sph_r) - 1))
+        self.prim_mat.append(mat)
+        self.prim_em.append((0, 0, 0))
+        return len(self.prim_shape) - 1
+
+    def finish(self, max_leaf_prims: int) -> SceneBuffers:
+        def arr(x, shape, dt):
+            return np.asarray(x, dtype=dt).reshape(shape) if len(x) else np.zeros(tuple(0 if d < 0 else d for d in shape), dtype=dt)
+        return SceneBuffers(
+            positions=arr(self.pos, (-1, 3), np.float32), normals=arr(self.nrm, (-1, 3), np.float32),
+            uvs=arr(self.uv, (-1, 2), np.float32), indices=arr(self.idx, (-1, 3), np.int32),
+            sphere_radius=arr(self.sph_r, (-1,), np.float32), sphere_to_world=arr(self.sph_m, (-1, 16), np.float32),
+            sphere_to_local=arr(self.sph_inv, (-1, 16), np.float32), materials=self.mats,
+            prim_shape=arr(self.prim_shape, (-1,), np.int32), prim_material=arr(self.prim_mat, (-1,), np.int32),
+            prim_emission=arr(self.prim_em, (-1, 3), np.float32), light_prims=arr(self.lights, (-1,), np.int32),
+            max_leaf_prims=max_leaf_prims)
+
+
+def lambert(albedo) -> Material:
+    """create_phong_material(0, kd, 0, 1): the reference's Lambertian material."""
+    return Material(kind=TR_MAT_PHONG, kd=tuple(albedo), ks=(0.0, 0.0, 0.0), ns=1.0)
+
+
+def cornell(width=256, height=256, spp=16, max_depth=5, min_depth=5):
+    """Cornell box [-1,1]^3 open at +z: 10 wall triangles, two boxes (12 each),
+    a 0.5x0.5 ceiling light at y = 0.99 emitting (17,12,4): 36 triangles,
+    2 lights. Pinhole camera at (0,0,3.5), 40 degree fov. min_depth >= max_depth
+    disables Russian roulette."""
+    b = _Builder()
+    white = b.material(lambert((0.73, 0.73, 0.73)))
+    red = b.material(lambert((0.65, 0.05, 0.05)))
+    green = b.material(lambert((0.12, 0.45, 0.15)))
+    b.quad((-1, -1, -1), (1, -1, -1), (1, -1, 1), (-1, -1, 1), (0, 1, 0), white)    # floor
+    b.quad((-1, 1, -1), (1, 1, -1), (1, 1, 1), (-1, 1, 1), (0, -1, 0), white)       # ceiling
+    b.quad((-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1), (0, 0, 1), white)    # back
+    b.quad((-1, -1, -1), (-1, 1, -1), (-1, 1, 1), (-1, -1, 1), (1, 0, 0), red)      # left
+    b.quad((1, -1, -1), (1, 1, -1), (1, 1, 1), (1, -1, 1), (-1, 0, 0), green)       # right
+    b.box((-0.35, -0.7, -0.3), (0.6, 0.6, 0.6), 15.0, white)
+    b.box((0.35, -0.4, 0.3), (0.6, 1.2, 0.6), -18.0, white)
+    b.quad((-0.25, 0.99, -0.25), (0.25, 0.99, -0.25), (0.25, 0.99, 0.25), (-0.25, 0.99, 0.25), (0, -1, 0),
+           white, emission=(17.0, 12.0, 4.0))
+    scene = b.finish(max_leaf_prims=3)
+    cam = make_camera(width / height, (0, 0, 3.5), (0, 0, 0), (0, 1, 0), math.radians(40.0), 0.0, 1.0)
+    return scene, cam, make_filter(0.5, 0.6), make_params(width, height, spp, min_depth, max_depth)
+
+
+def disney_grid(width=1024, height=1024, spp=64, max_depth=8, min_depth=5, seed=0, n=16):
+    """n x n Disney12 spheres (radius 0.4, spacing 1.0) on a 40x40 ground quad,
+    parameters uniform in [0,1] from `seed` (sheen_tint fixed at 0.5), two 2x2
+    area lights at height 6 emitting 8 (4 emissive triangles)."""
+    rng = np.random.default_rng(seed)
+    b = _Builder()
+    ground = b.material(lambert((0.5, 0.5, 0.5)))
+    b.quad((-20, 0, -20), (20, 0, -20), (20, 0, 20), (-20, 0, 20), (0, 1, 0), ground)
+    for cx, cz in ((-3.0, -2.0), (3.0, 2.0)):
+        b.quad((cx - 1, 6, cz - 1), (cx + 1, 6, cz - 1), (cx + 1, 6, cz + 1), (cx - 1, 6, cz + 1), (0, -1, 0),
+               ground, emission=(8.0, 8.0, 8.0))
+    for i in range(n):
+        for j in range(n):
+            p = rng.random(12).astype(np.float32)
+            m = Material(kind=TR_MAT_DISNEY12, base_color=tuple(float(v) for v in p[0:3]),
+                         metallic=float(p[3]), roughness=float(p[4]), specular=float(p[5]),
+                         specular_tint=float(p[6]), sheen=float(p[7]), clearcoat=float(p[8]),
+                         clearcoat_gloss=float(p[9]), anisotropic=float(p[10]), subsurface=float(p[11]),
+                         sheen_tint=0.5)
+            mat = b.material(m)
+            b.sphere(((i - (n - 1) / 2) * 1.0, 0.4, (j - (n - 1) / 2) * 1.0), 0.4, mat)
+    scene = b.finish(max_leaf_prims=3)
+    cam = make_camera(width / height, (0, 9, 14), (0, 0, 0), (0, 1, 0), math.radians(45.0), 0.0, 1.0)
+    return scene, cam, make_filter(0.5, 0.6), make_params(width, height, spp, min_depth, max_depth)
+
+
+def traversal(n_tris=1 << 20, seed=0, max_leaf_prims=4):
+    """n_tris triangles: centres uniform in [0,1]^3, each vertex the centre plus
+    an edge vector uniform in [-0.01,0.01]^3. numpy PCG64(seed)."""
+    rng = np.random.default_rng(seed)
+    c = rng.random((n_tris, 3), dtype=np.float64)
+    e = rng.uniform(-0.01, 0.01, size=(n_tris, 3, 3))
+    v = (c[:, None, :] + e).astype(np.float32).reshape(-1, 3) + np.float32(0)
+    idx = np.arange(3 * n_tris, dtype=np.int32).reshape(-1, 3)
+    nrm = np.tile(np.array([0, 0, 1], dtype=np.float32), (3 * n_tris, 1))
+    uv = np.zeros((3 * n_tris, 2), dtype=np.float32)
+    white = lambert((0.7, 0.7, 0.7))
+    return SceneBuffers(positions=v, normals=nrm, uvs=uv, indices=idx,
+                        sphere_radius=np.zeros(0, np.float32), sphere_to_world=np.zeros((0, 16), np.float32),
+                        sphere_to_local=np.zeros((0, 16), np.float32), materials=[white],
+                        prim_shape=np.arange(n_tris, dtype=np.int32), prim_material=np.zeros(n_tris, np.int32),
+                        prim_emission=np.zeros((n_tris, 3), np.float32), light_prims=np.zeros(0, np.int32),
+                        max_leaf_prims=max_leaf_prims)
+
+
+def cube_surface_points(rng, n):
+    face = rng.integers(0, 6, n)
+    uv = rng.random((n, 2))
+    p = np.empty((n, 3))
+    ax = face // 2
+    for a in range(3):
+        m = ax == a
+        others = [k for k in range(3) if k != a]
+        p[m, a] = (face[m] % 2).astype(np.float64)
+        p[m, others[0]] = uv[m, 0]
+        p[m, others[1]] = uv[m, 1]
+    return p.astype(np.float32)
+
+
+def traversal_rays(n_rays=1 << 22, seed=0, shadow=False):
+    """Closest-hit rays (t_max = FLT_MAX) or shadow rays (t_max ~ U(0,1)),
+    origins uniform on the unit-cube surface, directions uniform on the sphere,
+    t_min = 0; through the reference Ray constructor. numpy PCG64(seed + 1/2)."""
+    rng = np.random.default_rng(seed + (2 if shadow else 1))
+    o = cube_surface_points(rng, n_rays)
+    d = rng.normal(size=(n_rays, 3))
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    tmax = rng.random(n_rays).astype(np.float32) if shadow else F32_MAX
+    return make_rays(o, d, 0.0, tmax)
+
+
+def random_scene(seed=0, n_tris=64, n_spheres=8, n_lights=2, disney_frac=0.5, max_leaf_prims=3):
+    """Small closed-ish scene for parity tests: a floor, random triangles and
+    spheres in [-1,1]^3, emissive triangles overhead."""
+    rng = np.random.default_rng(seed)
+    b = _Builder()
+    mats = []
+    for k in range(6):
+        if rng.random() < disney_frac:
+            p = rng.random(12)
+            mats.append(b.material(Material(kind=TR_MAT_DISNEY12, base_color=tuple(p[0:3]), metallic=p[3],
+                                            roughness=p[4], specular=p[5], specular_tint=p[6], sheen=p[7],
+                                            clearcoat=p[8], clearcoat_gloss=p[9], anisotropic=p[10],
+                                            subsurface=p[11], sheen_tint=0.5)))
+        else:
+            kd = tuple(0.2 + 0.7 * rng.random(3))
+            ks = tuple(0.3 * rng.random(3)) if rng.random() < 0.5 else (0.0, 0.0, 0.0)
+            mats.append(b.material(Material(kind=TR_MAT_PHONG, kd=kd, ks=ks, ns=float(1 + 40 * rng.random()))))
+    b.quad((-3, -1, -3), (3, -1, -3), (3, -1, 3), (-3, -1, 3), (0, 1, 0), mats[0])
+    for _ in range(n_lights):
+        c = rng.uniform(-1, 1, 3) * np.array([1.0, 0.0, 1.0]) + np.array([0.0, 2.0, 0.0])
+        s = 0.2 + 0.3 * rng.random()
+        b.triangle(c + [-s, 0, -s], c + [s, 0, -s], c + [0, 0, s], (0, -1, 0), mats[0],
+                   emission=tuple(float(v) for v in 2 + 10 * rng.random(3)))
+        # winding of (a,b,c) above gives cross(AB,AC) along -y
+    for _ in range(n_tris):
+        c = rng.uniform(-1, 1, 3)
+        e = rng.uniform(-0.4, 0.4, (2, 3))
+        a, bb, cc = c, c + e[0], c + e[1]
+        nrm = np.cross(bb - a, cc - a)
+        if np.linalg.norm(nrm) < 1e-6:
+            continue
+        b.triangle(a, bb, cc, nrm, mats[int(rng.integers(0, 6))], uvs=tuple(map(tuple, rng.random((3, 2)))))
+    for _ in range(n_spheres):
+        b.sphere(rng.uniform(-1, 1, 3), float(0.1 + 0.3 * rng.random()), mats[int(rng.integers(0, 6))])
+    scene = b.finish(max_leaf_prims=max_leaf_prims)
+    return scene
+
+
+def random_camera(width, height, seed=0):
+    rng = np.random.default_rng(seed + 1000)
+    pos = (float(rng.uniform(-1, 1)), float(rng.uniform(0.0, 1.5)), float(4 + rng.uniform(0, 1)))
+    return make_camera(width / height, pos, (0, 0, 0), (0, 1, 0), math.radians(45.0), 0.0, 1.0)
