@@ -131,14 +131,19 @@ typedef struct tr_render_params {
   int32_t max_depth;
   int32_t direct_light_sample_num; /* must be 1 on the GPU path */
   uint32_t seed_base;
+  uint32_t flags; /* TR_RENDER_TIME_STAGES: per-stage CUDA-event timing into tr_stats */
 } tr_render_params;
+
+enum { TR_RENDER_TIME_STAGES = 1 };
 
 typedef struct tr_stats {
   uint64_t samples;      /* camera samples finished */
   uint64_t extend_rays;  /* closest-hit rays traced (continuation + MIS) */
   uint64_t shadow_rays;  /* any-hit rays traced */
+  uint64_t shade_items;  /* path vertices processed by the shade stage */
   uint64_t iterations;   /* wavefront iterations run */
   double device_ms;      /* device time of the render, CUDA events */
+  double stage_ms[3];    /* extend, shade, shadow kernels (with TR_RENDER_TIME_STAGES) */
 } tr_stats;
 
 const char* tr_status_string(tr_status s);
@@ -211,6 +216,18 @@ tr_status tr_render_dev(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filt
 /* Asks a running tr_render on this context to stop after its current
  * wavefront iteration; that call then returns TR_ERR_CANCELLED. Thread-safe. */
 tr_status tr_cancel(tr_ctx* ctx);
+
+/* Device self-check of the single-precision evaluations that stand in for
+ * the reference's double-precision expressions: `which` selects 0 the slab
+ * scale of Bounds3::intersect_p (src/utility/geometry.hpp:848-859; n = 2^32
+ * covers every float), 1 cross, 2 normalize, 3 cos (geometry.hpp:570-590,
+ * 943-949), 4 Vector3 / float (:429-433), 5 the shadow-ray length and 6 the
+ * light pdf of sample_area_light / DiffuseLight::sample_li
+ * (src/renderer/direct_illumination.cpp:45-47, src/light/diffuse_light.cpp:50-51),
+ * 7 the Disney Fd90 and subsurface terms (src/material/disney_brdf.cpp:120-125).
+ * Each of n seeded inputs is evaluated both ways on the device; *mismatches
+ * receives how many results differ in any bit. No reference counterpart. */
+tr_status tr_selftest(tr_ctx* ctx, int which, uint64_t n, uint64_t seed, uint64_t* mismatches);
 
 #ifdef __cplusplus
 }

@@ -82,6 +82,8 @@ def _load(kind: str) -> C.CDLL:
         lib.orc_render.restype = C.c_uint64
         lib.orc_render.argtypes = [vp, C.POINTER(TrRenderParams), C.c_int, C.c_int, f32p,
                                    C.POINTER(C.c_double), C.c_int]
+        lib.orc_render_rows.restype = C.c_uint64
+        lib.orc_render_rows.argtypes = [vp, C.POINTER(TrRenderParams), i32p, C.c_int, f32p, C.c_int]
         lib.orc_render_log.restype = sz
         lib.orc_render_log.argtypes = [vp, C.POINTER(TrRenderParams), C.c_int, C.c_int, C.POINTER(sz)]
         lib.orc_log_fetch.argtypes = [C.POINTER(TrRay), i32p, f32p, C.POINTER(TrRay), u8p]
@@ -183,6 +185,14 @@ class Oracle:
         out = np.zeros((H, W, 4), np.float32)
         self.lib.ref_render(self.h, C.byref(params), _p(out, C.c_float), self.threads)
         return out
+
+    def render_rows(self, params: TrRenderParams, rows):
+        """Port only: the given rows of the per-pixel-seeded render, in parallel."""
+        rows = np.ascontiguousarray(rows, np.int32)
+        out = np.zeros((len(rows), params.width, 4), np.float32)
+        n = self.lib.orc_render_rows(self.h, C.byref(params), _p(rows, C.c_int32), len(rows),
+                                     _p(out, C.c_float), self.threads)
+        return out, int(n)
 
     def render_stock_seconds(self, params: TrRenderParams, workers: int = 0):
         """Reference build only: time of the stock create_pt_renderer render()."""

@@ -1515,6 +1515,37 @@ uint64_t orc_render(void* h, const tr_render_params* p, int row0, int row1, floa
   return (uint64_t)nrows * W * p->spp;
 }
 
+// Per-pixel-seeded render of an arbitrary set of rows (in parallel); rgbw
+// receives the rows' own filtered sums (radius <= 0.5: each sample reaches
+// only its pixel), in the order given. Returns the number of samples.
+uint64_t orc_render_rows(void* h, const tr_render_params* p, const int* rows, int nrows, float* rgbw,
+                         int threads) {
+  Scene* sc = static_cast<Scene*>(h);
+  const int W = p->width, H = p->height;
+  parallel_for(nrows, threads, [&](int ri, int) {
+    const int y = rows[ri];
+    Tracer tr{*sc, nullptr, nullptr};
+    for (int x = 0; x < W; ++x) {
+      PixelTile tile;
+      pixel_tile_bounds(*sc, W, H, x, y, tile);
+      std::memset(tile.px, 0, sizeof(tile.px));
+      Sampler smp((int)(p->seed_base + (uint32_t)y * (uint32_t)W + (uint32_t)x));
+      for (int i = 0; i < p->spp; ++i) {
+        const real fu = smp.u(), fv = smp.u();
+        const real lu = smp.u(), lv = smp.u();
+        const real pxf = x + fu, pyf = y + fv;
+        Ray ray = generate_ray(sc->cam, pxf / W, pyf / H, lu, lv);
+        Sp L = eval_li(tr, ray, smp, p->min_depth, p->max_depth);
+        if (std::isfinite(L.r) && std::isfinite(L.g) && std::isfinite(L.b)) add_sample(*sc, tile, pxf, pyf, L);
+      }
+      const TilePx& own = tile.px[(x - tile.x0) + (y - tile.y0) * (tile.x1 - tile.x0)];
+      float* o = rgbw + 4 * ((size_t)ri * W + x);
+      o[0] = own.c.r; o[1] = own.c.g; o[2] = own.c.b; o[3] = own.w;
+    }
+  });
+  return (uint64_t)nrows * W * p->spp;
+}
+
 // Renders pixels [pix0, pix1) in row-major order on one thread and records
 // every closest-hit and any-hit query with its result (the ray-replay log).
 // Returns the number of closest rays; call orc_log_fetch to copy them out.

@@ -1,0 +1,97 @@
+"""Generates tests/golden/*.npz from the REFERENCE's own sources.
+
+Run in a checkout where the reference exists (make -C oracle ref builds it):
+    python tests/golden/make_golden.py
+Each fixture stores its inputs (scene arrays, rays, camera, parameters) and
+the reference's outputs, so checking it needs neither the reference nor the
+random generator that made the inputs.
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+from tracer_gb300 import scenes  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def units():
+    rng = np.random.default_rng(100)
+    a = rng.normal(size=(512, 3)).astype(np.float32)
+    b = rng.normal(size=(512, 3)).astype(np.float32)
+    a[:16] *= np.float32(1e-20)
+    a[16:32] *= np.float32(1e15)
+    a[32:40] = [[0, 0, 1], [0, 1, 0], [1, 0, 0], [0, 0, -1], [1e-30, 0, 0], [3, 4, 0], [-0.0, 0.0, 1.0], [1, 1, 1]]
+    seeds = np.array([0, 1, 7, 12345, -3, 2**31 - 1], np.int64)
+    pcg = np.stack([oracle.pcg_uniform("reference", int(s), 64) for s in seeds])
+    return dict(a=a, b=b, cross=oracle.unit("reference", "cross", a, b, out_shape=(512, 3), n=512),
+                normalize=oracle.unit("reference", "normalize", a, out_shape=(512, 3), n=512),
+                seeds=seeds, pcg=pcg)
+
+
+def traversal():
+    sc = scenes.traversal(4096, seed=3)
+    ref = oracle.Oracle(sc, "reference", threads=8)
+    rays = scenes.traversal_rays(2048, seed=3)
+    srays = scenes.traversal_rays(2048, seed=3, shadow=True)
+    prim, t = ref.trace_closest(rays)
+    hit = ref.trace_any(srays)
+    nodes, order = ref.bvh()
+    d = scenes.pack_scene(sc)
+    d.update(rays=rays.view(np.uint8), shadow_rays=srays.view(np.uint8), prim=prim, t=t, hit=hit,
+             nodes=nodes.view(np.uint8), order=order)
+    return d
+
+
+def mixed():
+    sc = scenes.random_scene(21, n_tris=80, n_spheres=10, n_lights=2)
+    cam = scenes.random_camera(40, 32, 21)
+    par = scenes.make_params(40, 32, 4, 1, 6, seed_base=5)
+    filt = scenes.make_filter(0.5, 0.6)
+    ref = oracle.Oracle(sc, "reference", threads=8)
+    ref.set_camera(cam, filt)
+    rng = np.random.default_rng(22)
+    o = rng.uniform(-2, 2, (2048, 3)).astype(np.float32)
+    dd = rng.normal(size=(2048, 3)).astype(np.float32)
+    rays = scenes.make_rays(o, dd, 0.0, scenes.F32_MAX)
+    prim, t = ref.trace_closest(rays)
+    nodes, order = ref.bvh()
+    d = scenes.pack_scene(sc)
+    d.update(scenes.pack_view(cam, filt, par))
+    d.update(rays=rays.view(np.uint8), prim=prim, t=t, nodes=nodes.view(np.uint8), order=order,
+             rgbw=ref.render(par))
+    return d
+
+
+def render(name, maker):
+    sc, cam, filt, par = maker()
+    ref = oracle.Oracle(sc, "reference", threads=8)
+    ref.set_camera(cam, filt)
+    d = scenes.pack_scene(sc)
+    d.update(scenes.pack_view(cam, filt, par))
+    d["rgbw"] = ref.render(par)
+    return d
+
+
+def main():
+    if not oracle.ref_available():
+        oracle.build_ref()
+    np.savez_compressed(os.path.join(OUT, "units.npz"), **units())
+    np.savez_compressed(os.path.join(OUT, "traversal_4k.npz"), **traversal())
+    np.savez_compressed(os.path.join(OUT, "mixed_scene.npz"), **mixed())
+    np.savez_compressed(os.path.join(OUT, "cornell_32x32_4spp.npz"),
+                        **render("cornell", lambda: scenes.cornell(32, 32, 4)))
+    np.savez_compressed(os.path.join(OUT, "disney_grid_32x32_2spp.npz"),
+                        **render("disney", lambda: scenes.disney_grid(32, 32, 2, min_depth=3)))
+    for f in sorted(os.listdir(OUT)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(OUT, f)))
+
+
+if __name__ == "__main__":
+    main()

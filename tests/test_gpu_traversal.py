@@ -1,0 +1,119 @@
+"""GPU traversal parity: closest-hit primitive ids and distances, and any-hit
+flags, bit-exact against the oracle on the same rays (the reference's
+Scene::intersect_p / Scene::intersect, src/core/scene.cpp:32-38)."""
+import numpy as np
+import pytest
+
+import oracle
+from tracer_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _same_bits(a, b):
+    return np.array_equal(np.asarray(a).view(np.uint32), np.asarray(b).view(np.uint32))
+
+
+def _random_rays(rng, n, lo=-2.0, hi=2.0, shadow=False):
+    o = rng.uniform(lo, hi, (n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    tmax = rng.uniform(0.0, 3.0, n).astype(np.float32) if shadow else scenes.F32_MAX
+    return scenes.make_rays(o, d, 0.0, tmax)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2, 3])
+def test_random_scene_closest_and_any(gpu, seed):
+    sc = scenes.random_scene(seed, n_tris=120, n_spheres=12)
+    orc = oracle.Oracle(sc, "port")
+    gpu.upload(sc)
+    rng = np.random.default_rng(seed)
+    rays = _random_rays(rng, 20000)
+    p0, t0 = orc.trace_closest(rays)
+    p1, t1 = gpu.trace_closest(rays)
+    assert np.array_equal(p0, p1)
+    assert _same_bits(t0, t1)
+    srays = _random_rays(rng, 20000, shadow=True)
+    assert np.array_equal(orc.trace_any(srays), gpu.trace_any(srays))
+
+
+def test_bvh_matches_oracle(gpu):
+    sc = scenes.random_scene(7, n_tris=300, n_spheres=20)
+    orc = oracle.Oracle(sc, "port")
+    gpu.upload(sc)
+    n0, o0 = orc.bvh()
+    n1, o1 = gpu.bvh()
+    assert np.array_equal(n0, n1) and np.array_equal(o0, o1)
+
+
+def test_traversal_workload_subset(gpu):
+    """The 1M-triangle traversal workload's shapes at 1/16 scale."""
+    sc = scenes.traversal(1 << 16, seed=0)
+    orc = oracle.Oracle(sc, "port")
+    gpu.upload(sc)
+    rays = scenes.traversal_rays(1 << 16, seed=0)
+    p0, t0 = orc.trace_closest(rays)
+    p1, t1 = gpu.trace_closest(rays)
+    assert np.array_equal(p0, p1)
+    assert _same_bits(t0, t1)
+    srays = scenes.traversal_rays(1 << 16, seed=0, shadow=True)
+    assert np.array_equal(orc.trace_any(srays), gpu.trace_any(srays))
+
+
+def test_uploaded_oracle_bvh(gpu):
+    """Traversal of an externally built tree (tr_bvh_upload) matches too."""
+    sc = scenes.random_scene(11, n_tris=200, n_spheres=5)
+    orc = oracle.Oracle(sc, "port")
+    gpu.upload(sc)
+    nodes, order = orc.bvh()
+    gpu.upload_bvh(nodes, order)
+    rays = _random_rays(np.random.default_rng(5), 5000)
+    p0, t0 = orc.trace_closest(rays)
+    p1, t1 = gpu.trace_closest(rays)
+    assert np.array_equal(p0, p1) and _same_bits(t0, t1)
+
+
+def test_edge_cases(gpu):
+    # axis-parallel directions (inverse direction = +-inf), rays from vertices
+    # and edges (ties), NaN rays (miss, as in the reference)
+    sc = scenes.cornell(8, 8, 1)[0]
+    orc = oracle.Oracle(sc, "port")
+    gpu.upload(sc)
+    o = []
+    d = []
+    for ax in range(3):
+        for s in (-1.0, 1.0):
+            dd = [0.0, 0.0, 0.0]
+            dd[ax] = s
+            for oo in ([0, 0, 0], [0.25, 0.5, -0.25], [-0.25, 0.99, -0.25], [1, 1, 1], [0.5, -1, 0.3]):
+                o.append(oo)
+                d.append(dd)
+    pos = sc.positions[:30]
+    for p in pos:
+        o.append(p + np.float32(0.0))
+        d.append([0.3, -1.0, 0.2])
+    rays = scenes.make_rays(np.array(o, np.float32), np.array(d, np.float32), 0.0, scenes.F32_MAX)
+    nan = rays[:3].copy()
+    nan["d"][:, 0] = np.nan
+    rays = np.concatenate([rays, nan])
+    p0, t0 = orc.trace_closest(rays)
+    p1, t1 = gpu.trace_closest(rays)
+    assert np.array_equal(p0, p1) and _same_bits(t0, t1)
+    assert np.array_equal(orc.trace_any(rays), gpu.trace_any(rays))
+
+
+def test_empty_and_single(gpu):
+    one = scenes._Builder()
+    m = one.material(scenes.lambert((0.5, 0.5, 0.5)))
+    one.triangle((0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1), m)
+    sc = one.finish(3)
+    gpu.upload(sc)
+    rays = scenes.make_rays(np.array([[0.2, 0.2, 1.0], [2, 2, 1]], np.float32),
+                            np.array([[0, 0, -1], [0, 0, -1]], np.float32), 0.0, scenes.F32_MAX)
+    p, t = gpu.trace_closest(rays)
+    assert p[0] == 0 and p[1] == -1 and t[0] == np.float32(1.0)
+    empty = scenes._Builder()
+    empty.material(scenes.lambert((0.5, 0.5, 0.5)))
+    gpu.upload(empty.finish(3))
+    p, t = gpu.trace_closest(rays)
+    assert (p == -1).all()
+    assert not gpu.trace_any(rays).any()

@@ -1,0 +1,70 @@
+"""The oracle (CPU restatement) against golden fixtures made by the reference's
+own sources (tests/golden/make_golden.py). Bit-exact: the oracle repeats the
+reference's arithmetic operation by operation, including libstdc++'s
+partition/nth_element in the BVH build and glibc's libm.
+
+This is what pins the oracle on machines without the reference checkout."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from tracer_gb300 import scenes
+from tracer_gb300.abi import NODE_DTYPE, RAY_DTYPE
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def test_units():
+    g = load("units.npz")
+    n = len(g["a"])
+    assert np.array_equal(bits(oracle.unit("port", "cross", g["a"], g["b"], out_shape=(n, 3), n=n)), bits(g["cross"]))
+    assert np.array_equal(bits(oracle.unit("port", "normalize", g["a"], out_shape=(n, 3), n=n)), bits(g["normalize"]))
+    for s, row in zip(g["seeds"], g["pcg"]):
+        assert np.array_equal(bits(oracle.pcg_uniform("port", int(s), len(row))), bits(row))
+    # numpy restatement used to build rays and normals
+    assert np.array_equal(bits(scenes.ref_normalize(g["a"])), bits(g["normalize"]))
+
+
+def test_traversal():
+    g = load("traversal_4k.npz")
+    sc = scenes.unpack_scene(g)
+    orc = oracle.Oracle(sc, "port")
+    nodes, order = orc.bvh()
+    assert np.array_equal(nodes.view(np.uint8), g["nodes"])
+    assert np.array_equal(order, g["order"])
+    prim, t = orc.trace_closest(g["rays"].view(RAY_DTYPE))
+    assert np.array_equal(prim, g["prim"]) and np.array_equal(bits(t), bits(g["t"]))
+    assert np.array_equal(orc.trace_any(g["shadow_rays"].view(RAY_DTYPE)), g["hit"])
+
+
+def test_mixed_scene_render_and_trace():
+    g = load("mixed_scene.npz")
+    sc = scenes.unpack_scene(g)
+    cam, filt, par = scenes.unpack_view(g)
+    orc = oracle.Oracle(sc, "port")
+    nodes, order = orc.bvh()
+    assert np.array_equal(nodes.view(np.uint8), g["nodes"]) and np.array_equal(order, g["order"])
+    prim, t = orc.trace_closest(g["rays"].view(RAY_DTYPE))
+    assert np.array_equal(prim, g["prim"]) and np.array_equal(bits(t), bits(g["t"]))
+    orc.set_camera(cam, filt)
+    assert np.array_equal(bits(orc.render(par)), bits(g["rgbw"]))
+
+
+@pytest.mark.parametrize("name", ["cornell_32x32_4spp.npz", "disney_grid_32x32_2spp.npz"])
+def test_renders(name):
+    g = load(name)
+    sc = scenes.unpack_scene(g)
+    cam, filt, par = scenes.unpack_view(g)
+    orc = oracle.Oracle(sc, "port")
+    orc.set_camera(cam, filt)
+    assert np.array_equal(bits(orc.render(par)), bits(g["rgbw"]))

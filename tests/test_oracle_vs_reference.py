@@ -1,0 +1,75 @@
+"""The oracle against the reference's own sources compiled here (oracle/_ref).
+Skipped where the reference checkout is absent (the fixtures in
+test_oracle_golden.py cover that case)."""
+import numpy as np
+import pytest
+
+import oracle
+from tracer_gb300 import scenes
+
+pytestmark = pytest.mark.skipif(not oracle.ref_available(), reason="reference build (oracle/_ref) not present")
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def test_units_random():
+    rng = np.random.default_rng(0)
+    a = rng.normal(size=(20000, 3)).astype(np.float32) * rng.choice([1e-8, 1, 1e8], size=(20000, 1)).astype(np.float32)
+    b = rng.normal(size=(20000, 3)).astype(np.float32)
+    for name, args in (("cross", (a, b)), ("normalize", (a,))):
+        x = oracle.unit("port", name, *args, out_shape=(20000, 3), n=20000)
+        y = oracle.unit("reference", name, *args, out_shape=(20000, 3), n=20000)
+        assert np.array_equal(bits(x), bits(y)), name
+    for s in (0, 99, -7, 2**31 - 1):
+        assert np.array_equal(oracle.pcg_uniform("port", s, 5000), oracle.pcg_uniform("reference", s, 5000))
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_random_scenes(seed):
+    sc = scenes.random_scene(seed, n_tris=70, n_spheres=9)
+    cam = scenes.random_camera(40, 32, seed)
+    par = scenes.make_params(40, 32, 3, seed % 3, 6, seed_base=seed)
+    filt = scenes.make_filter(0.5, 0.6)
+    port, ref = oracle.Oracle(sc, "port"), oracle.Oracle(sc, "reference")
+    n0, o0 = port.bvh()
+    n1, o1 = ref.bvh()
+    assert np.array_equal(n0, n1) and np.array_equal(o0, o1)
+    rng = np.random.default_rng(seed)
+    rays = scenes.make_rays(rng.uniform(-2, 2, (4000, 3)).astype(np.float32),
+                            rng.normal(size=(4000, 3)).astype(np.float32), 0.0, scenes.F32_MAX)
+    p0, t0 = port.trace_closest(rays)
+    p1, t1 = ref.trace_closest(rays)
+    assert np.array_equal(p0, p1) and np.array_equal(bits(t0), bits(t1))
+    srays = rays.copy()
+    srays["t_max"] = rng.uniform(0, 3, 4000).astype(np.float32)
+    assert np.array_equal(port.trace_any(srays), ref.trace_any(srays))
+    port.set_camera(cam, filt)
+    ref.set_camera(cam, filt)
+    assert np.array_equal(bits(port.render(par)), bits(ref.render(par)))
+
+
+def test_traversal_workload_subset():
+    sc = scenes.traversal(1 << 14, seed=1)
+    port, ref = oracle.Oracle(sc, "port"), oracle.Oracle(sc, "reference")
+    rays = scenes.traversal_rays(1 << 14, seed=1)
+    p0, t0 = port.trace_closest(rays)
+    p1, t1 = ref.trace_closest(rays)
+    assert np.array_equal(p0, p1) and np.array_equal(bits(t0), bits(t1))
+
+
+def test_wide_filter_and_disney():
+    sc, cam, filt, par = scenes.disney_grid(24, 24, 2, min_depth=2)
+    filt = scenes.make_filter(1.5, 0.6)
+    port, ref = oracle.Oracle(sc, "port"), oracle.Oracle(sc, "reference")
+    port.set_camera(cam, filt)
+    ref.set_camera(cam, filt)
+    assert np.array_equal(bits(port.render(par)), bits(ref.render(par)))
+
+
+def test_make_ray():
+    for o, d in (((0, 0, 0), (1, 2, 3)), ((1, -1, 0.5), (1e-9, 1, 0)), ((0, 0, 0), (-0.0, 0.0, -3))):
+        a = oracle.make_ray("port", o, d, 0.0, 1.0)
+        b = oracle.make_ray("reference", o, d, 0.0, 1.0)
+        assert bytes(a) == bytes(b)

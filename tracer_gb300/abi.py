@@ -82,12 +82,16 @@ class TrFilter(C.Structure):
 class TrRenderParams(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32),
                 ("min_depth", C.c_int32), ("max_depth", C.c_int32),
-                ("direct_light_sample_num", C.c_int32), ("seed_base", C.c_uint32)]
+                ("direct_light_sample_num", C.c_int32), ("seed_base", C.c_uint32), ("flags", C.c_uint32)]
+
+
+TR_RENDER_TIME_STAGES = 1
 
 
 class TrStats(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("extend_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
-                ("iterations", C.c_uint64), ("device_ms", C.c_double)]
+                ("shade_items", C.c_uint64), ("iterations", C.c_uint64), ("device_ms", C.c_double),
+                ("stage_ms", C.c_double * 3)]
 
 
 def ptr(a: np.ndarray | None, ctype):
@@ -200,8 +204,9 @@ def make_filter(radius=0.5, alpha=0.6) -> TrFilter:
     return f
 
 
-def make_params(width, height, spp, min_depth, max_depth, seed_base=0, direct_light_sample_num=1):
+def make_params(width, height, spp, min_depth, max_depth, seed_base=0, direct_light_sample_num=1, flags=0):
     p = TrRenderParams()
+    p.flags = flags
     p.width, p.height, p.spp = width, height, spp
     p.min_depth, p.max_depth = min_depth, max_depth
     p.direct_light_sample_num = direct_light_sample_num

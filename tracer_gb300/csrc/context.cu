@@ -1,0 +1,570 @@
+// context.cu -- context, scene upload and ray-batch entry points of the C ABI.
+//
+// Scene upload does on the host what the reference does at construction time
+// (src/shape/triangle.cpp:216-236, src/shape/sphere.cpp:83-92,
+// src/material/phong.cpp:29-70, src/accelerator/bvh.cpp:78-105), then packs
+// the device tables described in scene_types.h. Host arithmetic here is
+// compiled with -ffp-contract=off so the precomputed values are the ones the
+// reference computes.
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bvh_build.h"
+#include "context.h"
+#include "traverse.cuh"
+
+namespace trg {
+
+tr_status set_err(tr_ctx* ctx, tr_status s, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return s;
+}
+
+tr_status cuda_fail(tr_ctx* ctx, cudaError_t e, const char* what) {
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    return set_err(ctx, TR_ERR_OOM, std::string(what) + ": " + cudaGetErrorString(e));
+  }
+  return set_err(ctx, TR_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define TR_CUDA(ctx, call)                               \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+namespace {
+
+const float kIdentity[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+
+// Color3::lum (src/core/spectrum.hpp:94-96)
+inline float lum(f3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+
+DMat derive_material(const tr_material& m) {
+  DMat d;
+  std::memset(&d, 0, sizeof(d));
+  if (m.kind == TR_MAT_PHONG) {
+    d.kind = MAT_PHONG;
+    f3 diffuse = mk3(m.kd[0], m.kd[1], m.kd[2]), spec = mk3(m.ks[0], m.ks[1], m.ks[2]);
+    float dem = 1.0f;
+    dem = smax(dem, diffuse.x + spec.x);
+    dem = smax(dem, diffuse.y + spec.y);
+    dem = smax(dem, diffuse.z + spec.z);
+    diffuse = mk3(diffuse.x / dem, diffuse.y / dem, diffuse.z / dem);
+    spec = mk3(spec.x / dem, spec.y / dem, spec.z / dem);
+    const float dl = lum(diffuse), sl = lum(spec);
+    const float wd = (dl + sl > kEps) ? dl / (dl + sl) : 0.5f;
+    d.w_diffuse = wd;
+    d.w_specular = 1.0f - wd;
+    d.albedo = diffuse + spec;
+    d.diffuse_coef = mk3(diffuse.x / kPi, diffuse.y / kPi, diffuse.z / kPi);
+    d.specular = spec;
+    d.ns = m.ns;
+  } else {
+    d.kind = MAT_DISNEY12;
+    d.base = mk3(m.base_color[0], m.base_color[1], m.base_color[2]);
+    d.albedo = d.base;
+    d.subsurface = m.subsurface;
+    d.metallic = m.metallic;
+    d.specular_s = m.specular;
+    d.specular_tint = m.specular_tint;
+    d.roughness = m.roughness;
+    d.anisotropic = m.anisotropic;
+    d.sheen = m.sheen;
+    d.sheen_tint = m.sheen_tint;
+    d.clearcoat = m.clearcoat;
+    d.clearcoat_gloss = m.clearcoat_gloss;
+    // DisneyBRDF's per-call constants (src/material/disney_brdf.cpp:81-83,142-151,188-193)
+    const float aspect = (float)std::sqrt(1.0 - (double)m.anisotropic * 0.9);
+    d.ax = smax(0.001f, m.roughness * m.roughness / aspect);
+    d.ay = smax(0.001f, m.roughness * m.roughness * aspect);
+    d.p_diffuse = smin(0.8f, 1.0f - m.metallic);
+    d.p_spec_sample = (float)(1.0 / (1.0 + 0.5 * (double)m.clearcoat) * (double)(1.0f - d.p_diffuse));
+    d.p_spec_pdf = (float)(1.0 / (1.0 + 0.5 * (double)m.clearcoat));
+  }
+  return d;
+}
+
+inline float as_float(int i) {
+  float f;
+  std::memcpy(&f, &i, 4);
+  return f;
+}
+
+}  // namespace
+
+// Builds DNodes + slots from hs.nodes/hs.order and uploads every table.
+tr_status upload_device_tables(tr_ctx* ctx) {
+  HostScene& hs = ctx->hs;
+  const size_t nn = hs.nodes.size();
+  // validate the flattened tree: children strictly after their parent, leaf
+  // ranges inside the slot array, depth bounded by the traversal stack
+  std::vector<int> dix(nn, -1), depth(nn, 0);
+  int ninterior = 0;
+  for (size_t i = 0; i < nn; ++i) {
+    const tr_bvh_node32& n = hs.nodes[i];
+    if (n.count > 0) {
+      if (n.offset < 0 || (size_t)n.offset + n.count > hs.order.size())
+        return set_err(ctx, TR_ERR_ARG, "bvh leaf range outside the primitive order");
+    } else {
+      if (i + 1 >= nn || n.offset <= (int32_t)(i + 1) || (size_t)n.offset >= nn)
+        return set_err(ctx, TR_ERR_ARG, "bvh interior node with invalid children");
+      dix[i] = ninterior++;
+    }
+  }
+  for (uint32_t p : hs.order)
+    if (p >= hs.prims.size()) return set_err(ctx, TR_ERR_ARG, "bvh primitive order entry out of range");
+  int maxd = 0;
+  for (size_t i = 0; i < nn; ++i) {
+    const tr_bvh_node32& n = hs.nodes[i];
+    if (n.count == 0) {
+      depth[i + 1] = std::max(depth[i + 1], depth[i] + 1);
+      depth[n.offset] = std::max(depth[n.offset], depth[i] + 1);
+    }
+    maxd = std::max(maxd, depth[i]);
+  }
+  if (maxd >= 60) return set_err(ctx, TR_ERR_UNSUPPORTED, "bvh deeper than the device traversal stack (60)");
+  hs.depth = maxd;
+
+  std::vector<DNode> dn(ninterior);
+  for (size_t i = 0; i < nn; ++i) {
+    const tr_bvh_node32& n = hs.nodes[i];
+    if (n.count > 0) continue;
+    const tr_bvh_node32& L = hs.nodes[i + 1];
+    const tr_bvh_node32& R = hs.nodes[n.offset];
+    DNode& d = dn[dix[i]];
+    d.a = float4{L.lo[0], L.lo[1], L.lo[2], L.hi[0]};
+    d.b = float4{L.hi[1], L.hi[2], R.lo[0], R.lo[1]};
+    d.c = float4{R.lo[2], R.hi[0], R.hi[1], R.hi[2]};
+    const int lref = L.count > 0 ? L.offset : dix[i + 1];
+    const int rref = R.count > 0 ? R.offset : dix[n.offset];
+    d.d = int4{lref, rref, (int)((uint32_t)L.count | ((uint32_t)R.count << 16)), (int)n.axis};
+  }
+  std::vector<float4> slots(3 * hs.order.size());
+  for (size_t s = 0; s < hs.order.size(); ++s) {
+    const uint32_t pid = hs.order[s];
+    const DPrim& p = hs.prims[pid];
+    if (p.kind == PRIM_TRIANGLE) {
+      const f3 A = hs.A[p.shape], AB = hs.AB[p.shape], AC = hs.AC[p.shape];
+      slots[3 * s] = float4{A.x, A.y, A.z, as_float((int)pid)};
+      slots[3 * s + 1] = float4{AB.x, AB.y, AB.z, as_float(-1)};
+      slots[3 * s + 2] = float4{AC.x, AC.y, AC.z, 0.0f};
+    } else {
+      slots[3 * s] = float4{0.0f, 0.0f, 0.0f, as_float((int)pid)};
+      slots[3 * s + 1] = float4{0.0f, 0.0f, 0.0f, as_float(p.shape)};
+      slots[3 * s + 2] = float4{0.0f, 0.0f, 0.0f, 0.0f};
+    }
+  }
+  auto put = [&](DevBuf& b, const void* src, size_t bytes) -> cudaError_t {
+    cudaError_t e = b.reserve(bytes ? bytes : 16);
+    if (e != cudaSuccess) return e;
+    if (bytes) return cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    return cudaSuccess;
+  };
+  TR_CUDA(ctx, put(ctx->d_nodes, dn.data(), dn.size() * sizeof(DNode)));
+  TR_CUDA(ctx, put(ctx->d_slots, slots.data(), slots.size() * sizeof(float4)));
+  TR_CUDA(ctx, put(ctx->d_spheres, hs.spheres.data(), hs.spheres.size() * sizeof(DSphere)));
+  TR_CUDA(ctx, put(ctx->d_prims, hs.prims.data(), hs.prims.size() * sizeof(DPrim)));
+  TR_CUDA(ctx, put(ctx->d_tshade, hs.tshade.data(), hs.tshade.size() * sizeof(DTriShade)));
+  TR_CUDA(ctx, put(ctx->d_mats, hs.mats.data(), hs.mats.size() * sizeof(DMat)));
+  TR_CUDA(ctx, put(ctx->d_lights, hs.lights.data(), hs.lights.size() * sizeof(DLight)));
+  TR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+
+  DScene& sc = ctx->dsc;
+  sc.nodes = ctx->d_nodes.as<DNode>();
+  sc.slots = ctx->d_slots.as<float4>();
+  sc.spheres = ctx->d_spheres.as<DSphere>();
+  sc.prims = ctx->d_prims.as<DPrim>();
+  sc.tshade = ctx->d_tshade.as<DTriShade>();
+  sc.mats = ctx->d_mats.as<DMat>();
+  sc.lights = ctx->d_lights.as<DLight>();
+  sc.num_lights = (int)hs.lights.size();
+  if (nn == 0) {
+    sc.root_kind = 0;
+  } else {
+    const tr_bvh_node32& r = hs.nodes[0];
+    for (int k = 0; k < 3; ++k) {
+      sc.root_lo[k] = r.lo[k];
+      sc.root_hi[k] = r.hi[k];
+    }
+    if (r.count > 0) {
+      sc.root_kind = 2;
+      sc.root_offset = r.offset;
+      sc.root_count = r.count;
+    } else {
+      sc.root_kind = 1;
+      sc.root_offset = 0;
+      sc.root_count = 0;
+    }
+  }
+  ctx->has_scene = true;
+  return TR_OK;
+}
+
+// ------------------------------------------------------------ batch kernels
+__global__ void __launch_bounds__(128) k_trace_closest(DScene sc, const float4* __restrict__ rays, int n,
+                                                      int32_t* __restrict__ prim, float* __restrict__ tout,
+                                                      int* err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 r0 = __ldg(rays + 2 * i), r1 = __ldg(rays + 2 * i + 1);
+  float t_max = r1.w;
+  Hit h;
+  Traversal<false>::run(sc, mk3(r0.x, r0.y, r0.z), mk3(r0.w, r1.x, r1.y), r1.z, t_max, h, err);
+  prim[i] = h.prim;
+  tout[i] = t_max;
+}
+
+__global__ void __launch_bounds__(128) k_trace_any(DScene sc, const float4* __restrict__ rays, int n,
+                                                  uint8_t* __restrict__ hit, int* err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 r0 = __ldg(rays + 2 * i), r1 = __ldg(rays + 2 * i + 1);
+  float t_max = r1.w;
+  Hit h;
+  const bool occ = Traversal<true>::run(sc, mk3(r0.x, r0.y, r0.z), mk3(r0.w, r1.x, r1.y), r1.z, t_max, h, err);
+  hit[i] = occ ? 1 : 0;
+}
+
+}  // namespace trg
+
+using namespace trg;
+
+extern "C" {
+
+const char* tr_status_string(tr_status s) {
+  switch (s) {
+    case TR_OK: return "ok";
+    case TR_ERR_ARG: return "invalid argument";
+    case TR_ERR_OOM: return "out of memory";
+    case TR_ERR_QUEUE_OVERFLOW: return "device queue overflow";
+    case TR_ERR_TIMEOUT: return "device loop gave up";
+    case TR_ERR_CUDA: return "CUDA error";
+    case TR_ERR_STATE: return "call out of order";
+    case TR_ERR_CANCELLED: return "cancelled";
+    case TR_ERR_UNSUPPORTED: return "unsupported scene feature";
+  }
+  return "unknown status";
+}
+
+tr_status tr_make_ray(const float o[3], const float d[3], float t_min, float t_max, tr_ray* out) {
+  if (!o || !d || !out) return TR_ERR_ARG;
+  const f3 n = normalize(mk3(d[0], d[1], d[2]));
+  out->o[0] = o[0]; out->o[1] = o[1]; out->o[2] = o[2];
+  out->d[0] = n.x; out->d[1] = n.y; out->d[2] = n.z;
+  out->t_min = t_min;
+  out->t_max = t_max;
+  return TR_OK;
+}
+
+tr_status tr_ctx_create(tr_ctx** out, int device) {
+  if (!out) return TR_ERR_ARG;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+    cudaGetLastError();
+    return TR_ERR_CUDA;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) return TR_ERR_CUDA;
+  tr_ctx* ctx = new tr_ctx();
+  ctx->device = device;
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return TR_ERR_CUDA;
+  }
+  if (ctx->d_err.reserve(64) != cudaSuccess || cudaMemset(ctx->d_err.p, 0, 64) != cudaSuccess) {
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return TR_ERR_OOM;
+  }
+  *out = ctx;
+  return TR_OK;
+}
+
+void tr_ctx_destroy(tr_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  release_render(ctx);
+  for (DevBuf* b : {&ctx->d_nodes, &ctx->d_slots, &ctx->d_spheres, &ctx->d_prims, &ctx->d_tshade, &ctx->d_mats,
+                    &ctx->d_lights, &ctx->d_rays, &ctx->d_out0, &ctx->d_out1, &ctx->d_err})
+    b->release();
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char* tr_ctx_last_error(const tr_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+void* tr_ctx_stream(tr_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+tr_status tr_synchronize(tr_ctx* ctx) {
+  if (!ctx) return TR_ERR_ARG;
+  TR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return TR_OK;
+}
+
+tr_status tr_scene_upload(tr_ctx* ctx, const tr_scene_desc* d) {
+  if (!ctx || !d) return TR_ERR_ARG;
+  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (d->num_vertices && (!d->positions || !d->normals || !d->uvs))
+    return set_err(ctx, TR_ERR_ARG, "vertex arrays missing");
+  if (d->num_triangles && !d->indices) return set_err(ctx, TR_ERR_ARG, "indices missing");
+  if (d->num_spheres && (!d->sphere_radius || !d->sphere_to_world || !d->sphere_to_local))
+    return set_err(ctx, TR_ERR_ARG, "sphere arrays missing");
+  if (d->num_prims && (!d->prim_shape || !d->prim_material || !d->prim_emission))
+    return set_err(ctx, TR_ERR_ARG, "primitive arrays missing");
+  if (d->num_materials && !d->materials) return set_err(ctx, TR_ERR_ARG, "materials missing");
+  if (d->num_lights && !d->light_prims) return set_err(ctx, TR_ERR_ARG, "light list missing");
+  if (d->num_prims > 0x7fffffffu) return set_err(ctx, TR_ERR_ARG, "too many primitives");
+  for (uint32_t i = 0; i < 3 * d->num_triangles; ++i)
+    if (d->indices[i] < 0 || (uint32_t)d->indices[i] >= d->num_vertices)
+      return set_err(ctx, TR_ERR_ARG, "triangle index out of range");
+  for (uint32_t m = 0; m < d->num_materials; ++m)
+    if (d->materials[m].kind != TR_MAT_PHONG && d->materials[m].kind != TR_MAT_DISNEY12)
+      return set_err(ctx, TR_ERR_ARG, "unknown material kind");
+  for (uint32_t s = 0; s < d->num_spheres; ++s)
+    if (!(d->sphere_radius[s] > 0.0f)) return set_err(ctx, TR_ERR_ARG, "invalid sphere radius");  // sphere.cpp:88-90
+
+  ctx->has_scene = false;
+  HostScene hs;
+  // Mesh vertices through the identity local_to_world, normals normalised
+  // at creation (triangle.cpp:224-228) and again on first use (:182-184).
+  std::vector<f3> P(d->num_vertices), N(d->num_vertices);
+  for (uint32_t v = 0; v < d->num_vertices; ++v) {
+    P[v] = xform_point(kIdentity, mk3(d->positions[3 * v], d->positions[3 * v + 1], d->positions[3 * v + 2]));
+    N[v] = normalize(xform_normal_inv(kIdentity, mk3(d->normals[3 * v], d->normals[3 * v + 1], d->normals[3 * v + 2])));
+  }
+  const uint32_t nt = d->num_triangles, ns = d->num_spheres, np = d->num_prims;
+  hs.A.resize(nt);
+  hs.AB.resize(nt);
+  hs.AC.resize(nt);
+  hs.tshade.resize(nt);
+  std::vector<f3> Bv(nt), Cv(nt);
+  for (uint32_t t = 0; t < nt; ++t) {
+    const int i0 = d->indices[3 * t], i1 = d->indices[3 * t + 1], i2 = d->indices[3 * t + 2];
+    const f3 A = P[i0], B = P[i1], C = P[i2];
+    hs.A[t] = A;
+    Bv[t] = B;
+    Cv[t] = C;
+    const f3 AB = B - A, AC = C - A;
+    hs.AB[t] = AB;
+    hs.AC[t] = AC;
+    const float* uA = d->uvs + 2 * i0;
+    const float* uB = d->uvs + 2 * i1;
+    const float* uC = d->uvs + 2 * i2;
+    const float m00 = uB[0] - uA[0], m01 = uB[1] - uA[1], m10 = uC[0] - uA[0], m11 = uC[1] - uA[1];
+    DTriShade& ts = hs.tshade[t];
+    std::memset(&ts, 0, sizeof(ts));
+    // geometry frame (triangle.cpp:193-198): constant per triangle
+    const f3 gn = normalize(cross(AB, AC));
+    f3 dpdu, dpdv;
+    compute_ss_ts(AB, AC, m00, m01, m10, m11, gn, dpdu, dpdv);
+    dpdu = cross(dpdv, gn);
+    dpdv = cross(gn, dpdu);
+    const Frame g = make_frame(dpdu, dpdv, gn);
+    ts.gx = g.x;
+    ts.gy = g.y;
+    ts.gz = g.z;
+    const f3 nA = normalize(N[i0]), nB = normalize(N[i1]), nC = normalize(N[i2]);
+    ts.nA = nA;
+    ts.dn1 = nB - nA;
+    ts.dn2 = nC - nA;
+    const float det = m00 * m11 - m01 * m10;
+    ts.det_nonzero = det ? 1 : 0;
+    if (det) {
+      const float inv_det = 1.0f / det;
+      ts.dndu0 = scale(ts.dn1, m11 * inv_det) - scale(ts.dn2, m01 * inv_det);
+      ts.dndv0 = scale(ts.dn1, m10 * inv_det) - scale(ts.dn2, m00 * inv_det);
+    }
+  }
+  hs.spheres.resize(ns);
+  std::vector<float> sph_wr(ns);
+  for (uint32_t s = 0; s < ns; ++s) {
+    DSphere& S = hs.spheres[s];
+    std::memset(&S, 0, sizeof(S));
+    std::memcpy(S.m, d->sphere_to_world + 16 * s, 64);
+    std::memcpy(S.inv, d->sphere_to_local + 16 * s, 64);
+    S.radius = d->sphere_radius[s];
+    const float ratio = (float)lengthd(xform_vec(S.m, mk3(1.0f, 0.0f, 0.0f)));  // transformed_shape.hpp:13-15
+    sph_wr[s] = ratio * S.radius;
+  }
+  for (uint32_t m = 0; m < d->num_materials; ++m) hs.mats.push_back(derive_material(d->materials[m]));
+  hs.prims.resize(np);
+  std::vector<float> lo(3 * (size_t)np), hi(3 * (size_t)np);
+  for (uint32_t p = 0; p < np; ++p) {
+    DPrim& pr = hs.prims[p];
+    std::memset(&pr, 0, sizeof(pr));
+    const int sh = d->prim_shape[p];
+    if (sh >= 0) {
+      if ((uint32_t)sh >= nt) return set_err(ctx, TR_ERR_ARG, "primitive names a missing triangle");
+      pr.kind = PRIM_TRIANGLE;
+      pr.shape = sh;
+      // Triangle::world_bound: Union(Bounds3f(A, B), C)
+      const f3 A = hs.A[sh], B = Bv[sh], C = Cv[sh];
+      float l[3] = {smin(A.x, B.x), smin(A.y, B.y), smin(A.z, B.z)};
+      float h[3] = {smax(A.x, B.x), smax(A.y, B.y), smax(A.z, B.z)};
+      l[0] = smin(l[0], C.x); l[1] = smin(l[1], C.y); l[2] = smin(l[2], C.z);
+      h[0] = smax(h[0], C.x); h[1] = smax(h[1], C.y); h[2] = smax(h[2], C.z);
+      for (int k = 0; k < 3; ++k) { lo[3 * p + k] = l[k]; hi[3 * p + k] = h[k]; }
+      pr.area = (float)(0.5 * lengthd(cross(B - A, C - A)));  // Triangle::surface_area
+    } else {
+      const uint32_t si = (uint32_t)(~sh);
+      if (si >= ns) return set_err(ctx, TR_ERR_ARG, "primitive names a missing sphere");
+      pr.kind = PRIM_SPHERE;
+      pr.shape = (int)si;
+      // Sphere::world_bound (sphere.cpp:121-127)
+      const f3 o = xform_point(hs.spheres[si].m, mk3(0.0f, 0.0f, 0.0f));
+      const float r = sph_wr[si] + kEps;
+      lo[3 * p] = o.x - r; lo[3 * p + 1] = o.y - r; lo[3 * p + 2] = o.z - r;
+      hi[3 * p] = o.x + r; hi[3 * p + 1] = o.y + r; hi[3 * p + 2] = o.z + r;
+    }
+    const int mi = d->prim_material[p];
+    if (mi < 0 || (uint32_t)mi >= d->num_materials) return set_err(ctx, TR_ERR_ARG, "material index out of range");
+    pr.material = mi;
+    pr.emission = mk3(d->prim_emission[3 * p], d->prim_emission[3 * p + 1], d->prim_emission[3 * p + 2]);
+    pr.emissive = !(pr.emission.x == 0.0f && pr.emission.y == 0.0f && pr.emission.z == 0.0f);
+    if (pr.emissive && pr.kind == PRIM_SPHERE)
+      return set_err(ctx, TR_ERR_UNSUPPORTED, "emissive spheres are outside the GPU path");
+  }
+  for (uint32_t l = 0; l < d->num_lights; ++l) {
+    const int p = d->light_prims[l];
+    if (p < 0 || (uint32_t)p >= np) return set_err(ctx, TR_ERR_ARG, "light primitive out of range");
+    const DPrim& pr = hs.prims[p];
+    if (!pr.emissive) return set_err(ctx, TR_ERR_ARG, "light primitive is not emissive");
+    DLight L;
+    std::memset(&L, 0, sizeof(L));
+    L.A = hs.A[pr.shape];
+    L.B = Bv[pr.shape];
+    L.C = Cv[pr.shape];
+    L.gz = hs.tshade[pr.shape].gz;
+    L.emission = pr.emission;
+    L.area_pdf = 1.0f / pr.area;
+    L.prim = p;
+    hs.lights.push_back(L);
+  }
+  BvhResult bvh = build_reference_bvh(lo.data(), hi.data(), np, d->max_leaf_prims);
+  hs.nodes = std::move(bvh.nodes);
+  hs.order = std::move(bvh.order);
+  ctx->hs = std::move(hs);
+  return upload_device_tables(ctx);
+}
+
+tr_status tr_bvh_info(tr_ctx* ctx, size_t* num_nodes, size_t* num_prims) {
+  if (!ctx || !num_nodes || !num_prims) return TR_ERR_ARG;
+  if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
+  *num_nodes = ctx->hs.nodes.size();
+  *num_prims = ctx->hs.order.size();
+  return TR_OK;
+}
+
+tr_status tr_bvh_export(tr_ctx* ctx, tr_bvh_node32* nodes, uint32_t* prim_order) {
+  if (!ctx || !nodes || !prim_order) return TR_ERR_ARG;
+  if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
+  std::memcpy(nodes, ctx->hs.nodes.data(), ctx->hs.nodes.size() * sizeof(tr_bvh_node32));
+  std::memcpy(prim_order, ctx->hs.order.data(), ctx->hs.order.size() * sizeof(uint32_t));
+  return TR_OK;
+}
+
+tr_status tr_bvh_upload(tr_ctx* ctx, const tr_bvh_node32* nodes, size_t num_nodes, const uint32_t* prim_order,
+                        size_t num_prims) {
+  if (!ctx || (num_nodes && !nodes) || (num_prims && !prim_order)) return TR_ERR_ARG;
+  if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
+  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  std::vector<tr_bvh_node32> keep_nodes = ctx->hs.nodes;
+  std::vector<uint32_t> keep_order = ctx->hs.order;
+  ctx->hs.nodes.assign(nodes, nodes + num_nodes);
+  ctx->hs.order.assign(prim_order, prim_order + num_prims);
+  ctx->has_scene = false;
+  tr_status s = upload_device_tables(ctx);
+  if (s != TR_OK) {
+    ctx->hs.nodes = std::move(keep_nodes);
+    ctx->hs.order = std::move(keep_order);
+    std::string msg = ctx->err;
+    tr_status s2 = upload_device_tables(ctx);
+    ctx->err = msg;
+    (void)s2;
+  }
+  return s;
+}
+
+static tr_status check_err_word(tr_ctx* ctx) {
+  int e = 0;
+  TR_CUDA(ctx, cudaMemcpyAsync(&e, ctx->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  TR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (e) {
+    cudaMemsetAsync(ctx->d_err.p, 0, sizeof(int), ctx->stream);
+    return set_err(ctx, TR_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
+  }
+  return TR_OK;
+}
+
+tr_status tr_trace_closest_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, int32_t* d_prim, float* d_t) {
+  if (!ctx || (n && (!d_rays || !d_prim || !d_t))) return TR_ERR_ARG;
+  if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
+  if (n == 0) return TR_OK;
+  if (n > 0x7fffffffull) return set_err(ctx, TR_ERR_ARG, "too many rays");
+  if (((uintptr_t)d_rays & 15u) != 0) return set_err(ctx, TR_ERR_ARG, "ray buffer must be 16-byte aligned");
+  const int threads = 128;
+  const int blocks = (int)((n + threads - 1) / threads);
+  k_trace_closest<<<blocks, threads, 0, ctx->stream>>>(ctx->dsc, reinterpret_cast<const float4*>(d_rays), (int)n,
+                                                        d_prim, d_t, ctx->d_err.as<int>());
+  TR_CUDA(ctx, cudaGetLastError());
+  return TR_OK;
+}
+
+tr_status tr_trace_any_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, uint8_t* d_hit) {
+  if (!ctx || (n && (!d_rays || !d_hit))) return TR_ERR_ARG;
+  if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
+  if (n == 0) return TR_OK;
+  if (n > 0x7fffffffull) return set_err(ctx, TR_ERR_ARG, "too many rays");
+  if (((uintptr_t)d_rays & 15u) != 0) return set_err(ctx, TR_ERR_ARG, "ray buffer must be 16-byte aligned");
+  const int threads = 128;
+  const int blocks = (int)((n + threads - 1) / threads);
+  k_trace_any<<<blocks, threads, 0, ctx->stream>>>(ctx->dsc, reinterpret_cast<const float4*>(d_rays), (int)n,
+                                                    d_hit, ctx->d_err.as<int>());
+  TR_CUDA(ctx, cudaGetLastError());
+  return TR_OK;
+}
+
+tr_status tr_trace_closest(tr_ctx* ctx, const tr_ray* rays, size_t n, int32_t* prim, float* t) {
+  if (!ctx || (n && (!rays || !prim || !t))) return TR_ERR_ARG;
+  if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
+  if (n == 0) return TR_OK;
+  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  TR_CUDA(ctx, ctx->d_rays.reserve(n * sizeof(tr_ray)));
+  TR_CUDA(ctx, ctx->d_out0.reserve(n * sizeof(int32_t)));
+  TR_CUDA(ctx, ctx->d_out1.reserve(n * sizeof(float)));
+  TR_CUDA(ctx, cudaMemcpyAsync(ctx->d_rays.p, rays, n * sizeof(tr_ray), cudaMemcpyHostToDevice, ctx->stream));
+  tr_status s = tr_trace_closest_dev(ctx, ctx->d_rays.as<tr_ray>(), n, ctx->d_out0.as<int32_t>(), ctx->d_out1.as<float>());
+  if (s != TR_OK) return s;
+  TR_CUDA(ctx, cudaMemcpyAsync(prim, ctx->d_out0.p, n * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  TR_CUDA(ctx, cudaMemcpyAsync(t, ctx->d_out1.p, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  return check_err_word(ctx);
+}
+
+tr_status tr_trace_any(tr_ctx* ctx, const tr_ray* rays, size_t n, uint8_t* hit) {
+  if (!ctx || (n && (!rays || !hit))) return TR_ERR_ARG;
+  if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
+  if (n == 0) return TR_OK;
+  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  TR_CUDA(ctx, ctx->d_rays.reserve(n * sizeof(tr_ray)));
+  TR_CUDA(ctx, ctx->d_out0.reserve(n));
+  TR_CUDA(ctx, cudaMemcpyAsync(ctx->d_rays.p, rays, n * sizeof(tr_ray), cudaMemcpyHostToDevice, ctx->stream));
+  tr_status s = tr_trace_any_dev(ctx, ctx->d_rays.as<tr_ray>(), n, ctx->d_out0.as<uint8_t>());
+  if (s != TR_OK) return s;
+  TR_CUDA(ctx, cudaMemcpyAsync(hit, ctx->d_out0.p, n, cudaMemcpyDeviceToHost, ctx->stream));
+  return check_err_word(ctx);
+}
+
+tr_status tr_cancel(tr_ctx* ctx) {
+  if (!ctx) return TR_ERR_ARG;
+  ctx->cancel.store(1);
+  return TR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,74 @@
+// context.h -- the tr_ctx object behind the C ABI (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <string>
+#include <vector>
+
+#include "../../include/tracer_gpu.h"
+#include "scene_types.h"
+
+namespace trg {
+
+// A device allocation that grows on demand and is freed with the context.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t reserve(size_t n) {
+    if (n <= bytes) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+struct HostScene {
+  // what the device tables were built from (kept for export and re-upload)
+  std::vector<tr_bvh_node32> nodes;
+  std::vector<uint32_t> order;
+  std::vector<DPrim> prims;
+  std::vector<DTriShade> tshade;
+  std::vector<DSphere> spheres;
+  std::vector<DMat> mats;
+  std::vector<DLight> lights;
+  std::vector<f3> A, AB, AC;  // per triangle
+  int depth = 0;
+};
+
+struct RenderBuffers;  // render.cu
+
+}  // namespace trg
+
+struct tr_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  bool has_scene = false;
+  trg::HostScene hs;
+  trg::DScene dsc{};
+  trg::DevBuf d_nodes, d_slots, d_spheres, d_prims, d_tshade, d_mats, d_lights;
+  trg::DevBuf d_rays, d_out0, d_out1, d_err;
+  std::atomic<int> cancel{0};
+  trg::RenderBuffers* rb = nullptr;
+};
+
+namespace trg {
+tr_status cuda_fail(tr_ctx* ctx, cudaError_t e, const char* what);
+tr_status set_err(tr_ctx* ctx, tr_status s, const std::string& msg);
+tr_status upload_device_tables(tr_ctx* ctx);
+void release_render(tr_ctx* ctx);
+}  // namespace trg

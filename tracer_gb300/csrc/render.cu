@@ -1,0 +1,765 @@
+// render.cu -- wavefront path tracer: PathTraceRenderer::eval_pixel_li
+// (src/renderer/path_trace_renderer.cpp:27-210) for every camera sample of
+// PixelSamplerRenderer::render (src/renderer/pixel_sampler_renderer.cpp:24-109).
+//
+// One path slot per pixel. A slot draws its pixel's pcg32 stream in the
+// reference's order and runs its spp samples one after another, so the
+// random numbers, the rays and the film sums are the reference's. Each
+// wavefront iteration runs these kernels over compacted queues:
+//
+//   extend       closest hit for every queued ray (continuation and MIS rays)
+//   logic        per live slot: add the previous vertex's direct lighting
+//                (shadow results + MIS hit), finish samples (film) and start
+//                the next camera sample, add emission at depth 0, and queue
+//                hits by material
+//   material<K>  per hit of material K: BSDF sample, the light-sample draws,
+//                the MIS ray, the throughput update, Russian roulette and the
+//                next continuation ray
+//   nee<K>       per (hit of material K, light): the light sample, BSDF eval
+//                and pdf, and a shadow ray with its would-be contribution
+//   shadow       any hit for every queued shadow ray (zeroes blocked ones)
+//
+// Splitting by material keeps each kernel's code small (the shading code of
+// one monolithic kernel overflowed the instruction cache) and its warps on
+// one code path. All random draws of a vertex happen in `material`, before
+// any of its rays is traced, in the reference's order (its draws never depend
+// on ray results); the contributions are summed back in the reference's
+// order in `logic`. Queues are appended with warp-aggregated atomics.
+
+#include <cooperative_groups.h>
+#include <cooperative_groups/reduce.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "context.h"
+#include "shade.cuh"
+#include "traverse.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace trg {
+
+enum : int {
+  F_PENDING = 1,    // the previous vertex's direct lighting is still to be added
+  F_MIS = 2,        // ...and it includes a MIS ray
+  F_TERMINATE = 4,  // the path ends once that lighting is added
+};
+
+enum : int {  // counter slots
+  C_EXT = 0,      // 2: extend queue sizes (double-buffered)
+  C_ACT = 2,      // 2: live-slot list sizes
+  C_SH = 4,       // shadow queue size
+  C_MAT = 5,      // 2: per-material hit queue sizes
+  C_NEE = 7,      // 2: per-material light-sample queue sizes
+  C_ERR = 15,     // traversal error word
+};
+
+struct RenderBuffers {
+  int n = 0, nl = 0;
+  DevBuf P0, P1, P2, P3, P4, rng, M0, M1, M2, HC, HM, SC, NU, SH, acc, q_ext, q_act, q_mat, q_nee, q_sh, ctr,
+      stats;
+  unsigned int* h_active = nullptr;  // pinned: live-slot count per check
+  std::vector<cudaEvent_t> ev_pool;  // reused by stage timing
+};
+
+struct Launch {
+  DScene sc;
+  Cam cam;
+  int W, H, spp, min_depth, max_depth, nl;
+  unsigned seed_base;
+  float filter_radius, filter_alpha, filter_exp;
+  int fp64;
+  float4 *P0, *P1, *P2, *P3, *P4;  // cont o|flags, cont d|depth, coef|sample, L|px, coef_prev|py
+  unsigned long long* rng;
+  float4 *M0, *M1, *M2;  // mis o|bsdf_pdf, mis d|abs_cos, bsdf_f
+  float4 *HC, *HM;       // hits: prim, t_attr, alpha, beta
+  float4* SC;            // shading context for nee: 7 per slot (pos|mat, wo, g, s frames)
+  float2* NU;            // light-sample draws per (slot, light)
+  float4* SH;            // shadow: 3 per (slot, light): o|t_max, d, contrib|valid
+  float4* acc;           // film sums (float4) or 2 x double2 per pixel
+  int* q_ext[2];
+  int* q_act[2];
+  int* q_mat[2];
+  int* q_nee[2];
+  int* q_sh;
+  unsigned int* ctr;
+  unsigned long long* stats;  // samples, extend rays, shadow rays, shade items
+};
+
+__device__ __forceinline__ int append(unsigned int* ctr) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  unsigned int base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(ctr, g.size());
+  base = g.shfl(base, 0);
+  return (int)(base + g.thread_rank());
+}
+
+__device__ __forceinline__ void count_add(unsigned long long* c, unsigned long long v) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  const unsigned long long s = cg::reduce(g, v, cg::plus<unsigned long long>());
+  if (g.thread_rank() == 0 && s) atomicAdd(c, s);
+}
+
+// Film::Tile::add_sample (src/core/render.hpp:37-57). With radius <= 0.5 a
+// sample reaches only its own pixel with non-zero weight (neighbours get
+// exactly 0), so the slot owns its pixel and adds in sample order.
+__device__ __forceinline__ void film_add(const Launch& P, int slot, float px, float py, f3 L) {
+  const int x = slot % P.W, y = slot / P.W;
+  if (P.filter_radius <= 0.5f) {
+    const float ox = px - ((float)x + 0.5f), oy = py - ((float)y + 0.5f);  // exact for W, H < 2^23
+    const float fw = gaussian(P.filter_alpha, ox, P.filter_exp) * gaussian(P.filter_alpha, oy, P.filter_exp);
+    const f3 c = muls(muls(L, fw), 1.0f);
+    if (P.fp64) {
+      double2* a = reinterpret_cast<double2*>(P.acc) + 2 * slot;
+      double2 a0 = a[0], a1 = a[1];
+      a0.x += c.x;
+      a0.y += c.y;
+      a1.x += c.z;
+      a1.y += fw;
+      a[0] = a0;
+      a[1] = a1;
+    } else {
+      float4 a = P.acc[slot];
+      a.x += c.x;
+      a.y += c.y;
+      a.z += c.z;
+      a.w += fw;
+      P.acc[slot] = a;
+    }
+    return;
+  }
+  // wider filters: scatter with atomics (order of additions not fixed)
+  const float r = P.filter_radius;
+  const float dx = px - 0.5f, dy = py - 0.5f;
+  const int x0 = max((int)ceilf(dx - r), 0), y0 = max((int)ceilf(dy - r), 0);
+  const int x1 = min((int)floorf(dx + r) + 1, P.W), y1 = min((int)floorf(dy + r) + 1, P.H);
+  for (int yy = y0; yy < y1; ++yy)
+    for (int xx = x0; xx < x1; ++xx) {
+      const float ox = px - ((float)xx + 0.5f), oy = py - ((float)yy + 0.5f);
+      const float fw = gaussian(P.filter_alpha, ox, P.filter_exp) * gaussian(P.filter_alpha, oy, P.filter_exp);
+      const f3 c = muls(muls(L, fw), 1.0f);
+      const int o = yy * P.W + xx;
+      if (P.fp64) {
+        double* a = reinterpret_cast<double*>(P.acc) + 4 * o;
+        atomicAdd(a, (double)c.x);
+        atomicAdd(a + 1, (double)c.y);
+        atomicAdd(a + 2, (double)c.z);
+        atomicAdd(a + 3, (double)fw);
+      } else {
+        float* a = reinterpret_cast<float*>(P.acc) + 4 * o;
+        atomicAdd(a, c.x);
+        atomicAdd(a + 1, c.y);
+        atomicAdd(a + 2, c.z);
+        atomicAdd(a + 3, fw);
+      }
+    }
+}
+
+// Starts the slot's next camera sample, finishing samples that Russian
+// roulette ends before their first vertex. Returns false when the pixel has
+// no samples left.
+__device__ __forceinline__ bool start_sample(const Launch& P, int slot, unsigned long long& st, int sample,
+                                             int next_q, unsigned long long& finished) {
+  const int x = slot % P.W, y = slot / P.W;
+  while (sample < P.spp) {
+    const float fu = Pcg::next(st), fv = Pcg::next(st);
+    const float lu = Pcg::next(st), lv = Pcg::next(st);
+    const float px = (float)x + fu, py = (float)y + fv;
+    f3 o, d;
+    camera_ray(P.cam, px / (float)P.W, py / (float)P.H, lu, lv, o, d);
+    f3 coef = mk3(1.0f, 1.0f, 1.0f);
+    bool dead = false;
+    if (0 > P.min_depth) {  // Russian roulette at depth 0
+      if (Pcg::next(st) > 0.9f) dead = true;
+      else coef = divs(coef, 0.9f);
+    }
+    if (!dead && !valid3(coef)) dead = true;
+    if (dead) {
+      film_add(P, slot, px, py, mk3(0.0f, 0.0f, 0.0f));
+      ++finished;
+      ++sample;
+      continue;
+    }
+    P.P0[slot] = make_float4(o.x, o.y, o.z, __int_as_float(0));
+    P.P1[slot] = make_float4(d.x, d.y, d.z, __int_as_float(0));
+    P.P2[slot] = make_float4(coef.x, coef.y, coef.z, __int_as_float(sample));
+    P.P3[slot] = make_float4(0.0f, 0.0f, 0.0f, px);
+    P.P4[slot] = make_float4(0.0f, 0.0f, 0.0f, py);
+    P.q_ext[next_q][append(P.ctr + C_EXT + next_q)] = 2 * slot;
+    return true;
+  }
+  return false;
+}
+
+// Ends the slot's current sample (film) and starts its next one.
+__device__ void finish_sample(const Launch& P, int slot, unsigned long long& st, f3 L, int nxt,
+                              unsigned long long& finished) {
+  if (!valid3(L)) L = mk3(0.0f, 0.0f, 0.0f);  // eval_pixel_li returns {} (path_trace_renderer.cpp:204-209)
+  const float px = P.P3[slot].w, py = P.P4[slot].w;
+  film_add(P, slot, px, py, L);
+  ++finished;
+  const int sample = __float_as_int(P.P2[slot].w) + 1;
+  if (start_sample(P, slot, st, sample, nxt, finished)) P.q_act[nxt][append(P.ctr + C_ACT + nxt)] = slot;
+}
+
+__global__ void __launch_bounds__(256) k_init(Launch P) {
+  const int n = P.W * P.H;
+  unsigned long long finished = 0;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    const int x = s % P.W, y = s / P.W;
+    unsigned long long st = Pcg::seed((int)(P.seed_base + (unsigned)y * (unsigned)P.W + (unsigned)x));
+    const bool live = start_sample(P, s, st, 0, 0, finished);
+    P.rng[s] = st;
+    if (live) P.q_act[0][append(P.ctr + C_ACT)] = s;
+  }
+  count_add(P.stats, finished);
+}
+
+__global__ void __launch_bounds__(128) k_extend(Launch P, int cur) {
+  const unsigned int n = P.ctr[C_EXT + cur];
+  unsigned long long nr = 0;
+  for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int e = P.q_ext[cur][i];
+    const int slot = e >> 1;
+    const bool mis = e & 1;
+    const float4 a = mis ? P.M0[slot] : P.P0[slot];
+    const float4 b = mis ? P.M1[slot] : P.P1[slot];
+    float t_max = kRealMax;
+    Hit h;
+    Traversal<false>::run(P.sc, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), 0.0f, t_max, h, (int*)(P.ctr + C_ERR));
+    const float4 rec = make_float4(__int_as_float(h.prim), h.t_attr, h.alpha, h.beta);
+    if (mis) P.HM[slot] = rec;
+    else P.HC[slot] = rec;
+    ++nr;
+  }
+  count_add(P.stats + 1, nr);
+}
+
+__global__ void __launch_bounds__(128) k_shadow(Launch P) {
+  const unsigned int n = P.ctr[C_SH];
+  unsigned long long nr = 0;
+  for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int r = P.q_sh[i];
+    const float4 a = P.SH[3 * r], b = P.SH[3 * r + 1];
+    float t_max = a.w;
+    Hit h;
+    if (Traversal<true>::run(P.sc, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), kEps, t_max, h, (int*)(P.ctr + C_ERR)))
+      P.SH[3 * r + 2].w = 0.0f;
+    ++nr;
+  }
+  count_add(P.stats + 2, nr);
+}
+
+// sample_bsdf's contribution once its ray has been traced
+// (src/renderer/direct_illumination.cpp:144-198).
+__device__ f3 mis_contribution(const Launch& P, int slot) {
+  const float4 hit = P.HM[slot];
+  const int pid = __float_as_int(hit.x);
+  if (pid < 0) return mk3(0.0f, 0.0f, 0.0f);
+  const DPrim& pr = P.sc.prims[pid];
+  if (!pr.emissive) return mk3(0.0f, 0.0f, 0.0f);
+  const float4 m0 = P.M0[slot], m1 = P.M1[slot], m2 = P.M2[slot];
+  const f3 o = mk3(m0.x, m0.y, m0.z), d = mk3(m1.x, m1.y, m1.z);
+  const f3 gz = P.sc.tshade[pr.shape].gz;
+  // light_emit(t_isect, t_isect.wo) with wo = -ray.d
+  if (!(dot(gz, -d) > 0.0f)) return mk3(0.0f, 0.0f, 0.0f);
+  const f3 f = muls(mulc(pr.emission, mk3(m2.x, m2.y, m2.z)), m1.w);
+  const f3 pos = o + scale(d, hit.y);
+  const float lpdf = light_pdf_at(pr.area, o, pos, gz);
+  const float w = power_heuristic(m0.w, lpdf);
+  return divs(muls(f, w), m0.w);
+}
+
+__global__ void __launch_bounds__(128) k_logic(Launch P, int cur) {
+  const int nxt = cur ^ 1;
+  const unsigned int n = P.ctr[C_ACT + cur];
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.stats + 3, (unsigned long long)n);
+  unsigned long long finished = 0;
+  for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int slot = P.q_act[cur][i];
+    const float4 p0 = P.P0[slot], p3 = P.P3[slot];
+    const int flags = __float_as_int(p0.w);
+    f3 L = mk3(p3.x, p3.y, p3.z);
+    if (flags & F_PENDING) {
+      // direct lighting of the previous vertex, in the reference's order:
+      // lights in scene order, then the MIS term, then L += direct
+      const float4 p4 = P.P4[slot];
+      f3 direct = mk3(0.0f, 0.0f, 0.0f);
+      for (int l = 0; l < P.nl; ++l) {
+        const float4 c = P.SH[3 * (slot * P.nl + l) + 2];
+        if (c.w != 0.0f) direct = direct + mk3(c.x, c.y, c.z);
+      }
+      if (flags & F_MIS) direct = direct + mulc(mk3(p4.x, p4.y, p4.z), mis_contribution(P, slot));
+      L = L + direct;
+    }
+    const float4 hit = P.HC[slot];
+    const int pid = __float_as_int(hit.x);
+    if ((flags & F_TERMINATE) || pid < 0) {
+      unsigned long long st = P.rng[slot];
+      finish_sample(P, slot, st, L, nxt, finished);
+      P.rng[slot] = st;
+      continue;
+    }
+    const DPrim& pr = P.sc.prims[pid];
+    if (__float_as_int(P.P1[slot].w) == 0 && pr.emissive) {
+      // emission seen by the camera ray: light_emit(isect, -ray.d); only
+      // triangles emit on this path
+      const f3 gz = P.sc.tshade[pr.shape].gz;
+      const float4 p1 = P.P1[slot], p2 = P.P2[slot];
+      if (dot(gz, mk3(-p1.x, -p1.y, -p1.z)) > 0.0f) L = L + mulc(mk3(p2.x, p2.y, p2.z), pr.emission);
+    }
+    P.P3[slot] = make_float4(L.x, L.y, L.z, p3.w);
+    const int kind = P.sc.mats[pr.material].kind;
+    P.q_mat[kind][append(P.ctr + C_MAT + kind)] = slot;
+  }
+  count_add(P.stats, finished);
+}
+
+template <int KIND>
+struct MatOps {
+  static __device__ __forceinline__ BsdfSample sample(const Bsdf& b, f3 wo, float u, float v, float w) {
+    return KIND == MAT_PHONG ? b.phong_sample_agg(wo, u, v, w) : b.disney_sample(wo, u, v, w);
+  }
+  static __device__ __forceinline__ f3 eval(const Bsdf& b, f3 wi, f3 wo) {
+    return KIND == MAT_PHONG ? b.phong_eval_agg(wi, wo) : b.disney_eval(wi, wo);
+  }
+  static __device__ __forceinline__ float pdf(const Bsdf& b, f3 wi, f3 wo) {
+    return KIND == MAT_PHONG ? b.phong_pdf_agg(wi, wo) : b.disney_pdf(wi, wo);
+  }
+};
+
+// One path vertex on a material of kind KIND: the body of eval_pixel_li
+// from the BSDF sample to the next continuation ray
+// (src/renderer/path_trace_renderer.cpp:125-163).
+template <int KIND>
+__global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
+  const int nxt = cur ^ 1;
+  const unsigned int n = P.ctr[C_MAT + KIND];
+  unsigned long long finished = 0;
+  for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int slot = P.q_mat[KIND][i];
+    unsigned long long st = P.rng[slot];
+    const float4 p0 = P.P0[slot], p1 = P.P1[slot], p2 = P.P2[slot];
+    const f3 ro = mk3(p0.x, p0.y, p0.z), rd = mk3(p1.x, p1.y, p1.z);
+    int depth = __float_as_int(p1.w);
+    f3 coef = mk3(p2.x, p2.y, p2.z);
+    const float4 hit = P.HC[slot];
+    Isect is;
+    make_isect(P.sc, hit, ro, rd, is);
+    const int mat = P.sc.prims[is.prim].material;
+    Bsdf bsdf;
+    bsdf.m = P.sc.mats + mat;
+    bsdf.g = is.g;
+    bsdf.s = is.s;
+    const float u0 = Pcg::next(st), u1 = Pcg::next(st), u2 = Pcg::next(st);
+    const BsdfSample bs = MatOps<KIND>::sample(bsdf, is.wo, u0, u1, u2);
+    if (black(bs.f) || bs.pdf < kEps) {
+      const float4 p3 = P.P3[slot];
+      finish_sample(P, slot, st, mk3(p3.x, p3.y, p3.z), nxt, finished);
+      P.rng[slot] = st;
+      continue;
+    }
+    // next-event estimation on every light (sample_area_light): the draws
+    // happen here, the rest in k_nee
+    for (int l = 0; l < P.nl; ++l) {
+      const float lu = Pcg::next(st), lv = Pcg::next(st);
+      Pcg::next(st);
+      Pcg::next(st);
+      Pcg::next(st);
+      P.NU[slot * P.nl + l] = make_float2(lu, lv);
+      P.q_nee[KIND][append(P.ctr + C_NEE + KIND)] = slot * P.nl + l;
+    }
+    float4* sc = P.SC + 7 * (size_t)slot;
+    sc[0] = make_float4(is.pos.x, is.pos.y, is.pos.z, __int_as_float(mat));
+    sc[1] = make_float4(is.wo.x, is.wo.y, is.wo.z, is.g.x.x);
+    sc[2] = make_float4(is.g.x.y, is.g.x.z, is.g.y.x, is.g.y.y);
+    sc[3] = make_float4(is.g.y.z, is.g.z.x, is.g.z.y, is.g.z.z);
+    sc[4] = make_float4(is.s.x.x, is.s.x.y, is.s.x.z, is.s.y.x);
+    sc[5] = make_float4(is.s.y.y, is.s.y.z, is.s.z.x, is.s.z.y);
+    sc[6] = make_float4(is.s.z.z, 0.0f, 0.0f, 0.0f);
+    // MIS BSDF ray (sample_bsdf, src/renderer/direct_illumination.cpp:144-155)
+    int flags = F_PENDING;
+    {
+      const float v0 = Pcg::next(st), v1 = Pcg::next(st), v2 = Pcg::next(st);
+      const BsdfSample ms = MatOps<KIND>::sample(bsdf, is.wo, v0, v1, v2);
+      if (ms.valid()) {
+        const f3 wi = normalize(ms.wi);
+        const f3 mo = is.eps_offset(wi);
+        const f3 md = normalize(wi);
+        P.M0[slot] = make_float4(mo.x, mo.y, mo.z, ms.pdf);
+        P.M1[slot] = make_float4(md.x, md.y, md.z, abs_cos(is.g.z, md));
+        P.M2[slot] = make_float4(ms.f.x, ms.f.y, ms.f.z, 0.0f);
+        P.q_ext[nxt][append(P.ctr + C_EXT + nxt)] = 2 * slot + 1;
+        flags |= F_MIS;
+      }
+    }
+    P.P4[slot] = make_float4(coef.x, coef.y, coef.z, P.P4[slot].w);
+    coef = mulc(coef, divs(muls(bs.f, abs_cos(is.g.z, bs.wi)), bs.pdf));
+    bool term = !valid3(coef);
+    if (!term) {
+      ++depth;
+      if (depth >= P.max_depth) {
+        term = true;
+      } else if (depth > P.min_depth) {
+        if (Pcg::next(st) > 0.9f) term = true;
+        else {
+          coef = divs(coef, 0.9f);
+          if (!valid3(coef)) term = true;
+        }
+      }
+    }
+    if (term) {
+      flags |= F_TERMINATE;
+      P.P0[slot] = make_float4(p0.x, p0.y, p0.z, __int_as_float(flags));
+    } else {
+      const f3 no = is.eps_offset(bs.wi);
+      const f3 nd = normalize(normalize(bs.wi));
+      P.P0[slot] = make_float4(no.x, no.y, no.z, __int_as_float(flags));
+      P.P1[slot] = make_float4(nd.x, nd.y, nd.z, __int_as_float(depth));
+      P.q_ext[nxt][append(P.ctr + C_EXT + nxt)] = 2 * slot;
+    }
+    P.P2[slot] = make_float4(coef.x, coef.y, coef.z, p2.w);
+    P.q_act[nxt][append(P.ctr + C_ACT + nxt)] = slot;
+    P.rng[slot] = st;
+  }
+  count_add(P.stats, finished);
+}
+
+// sample_area_light (src/renderer/direct_illumination.cpp:35-71) for one
+// (vertex, light) pair: the shadow ray is traced by k_shadow, which zeroes
+// the contribution when it is blocked.
+template <int KIND>
+__global__ void __launch_bounds__(128) k_nee(Launch P) {
+  const unsigned int n = P.ctr[C_NEE + KIND];
+  for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int item = P.q_nee[KIND][i];
+    const int slot = item / P.nl, l = item - slot * P.nl;
+    const float4* sc = P.SC + 7 * (size_t)slot;
+    const float4 a = sc[0], b = sc[1], c = sc[2], d = sc[3], e = sc[4], f = sc[5], g = sc[6];
+    const f3 pos = mk3(a.x, a.y, a.z), wo = mk3(b.x, b.y, b.z);
+    Bsdf bsdf;
+    bsdf.m = P.sc.mats + __float_as_int(a.w);
+    bsdf.g.x = mk3(b.w, c.x, c.y);
+    bsdf.g.y = mk3(c.z, c.w, d.x);
+    bsdf.g.z = mk3(d.y, d.z, d.w);
+    bsdf.s.x = mk3(e.x, e.y, e.z);
+    bsdf.s.y = mk3(e.w, f.x, f.y);
+    bsdf.s.z = mk3(f.z, f.w, g.x);
+    const float2 uv = P.NU[item];
+    const DLight& lt = P.sc.lights[l];
+    float4* rec = P.SH + 3 * (size_t)item;
+    bool ok = false;
+    // Triangle::sample via UniformSampleTriangle (src/shape/triangle.cpp:61-97)
+    const float su0 = sqrtf(uv.x);
+    const float bx = 1.0f - su0, by = uv.y * su0;
+    const f3 lpos = scale(lt.A, bx) + scale(lt.B, by) + scale(lt.C, 1.0f - bx - by);
+    const f3 sp2ref = pos - lpos;
+    if (dot(lt.gz, sp2ref) > 0.0f) {
+      const float dist2 = len2f(sp2ref);
+      const float lpdf = area_to_solid_pdf(lt.area_pdf * dist2, dot(lt.gz, sp2ref), dist2);
+      if (lpdf) {
+        f3 to_light = lpos - pos;
+        bool too_close;
+        const float dist = dist_minus_eps(len2f(to_light), too_close);
+        if (!too_close) {
+          to_light = normalize(to_light);
+          const f3 bf = MatOps<KIND>::eval(bsdf, to_light, wo);
+          if (!black(bf)) {
+            const float bpdf = MatOps<KIND>::pdf(bsdf, to_light, wo);
+            const f3 fl = muls(mulc(lt.emission, bf), abs_cos(to_light, bsdf.g.z));
+            const float w = power_heuristic(lpdf, bpdf);
+            const float4 p4 = P.P4[slot];
+            const f3 cc = mulc(mk3(p4.x, p4.y, p4.z), divs(muls(fl, w), lpdf));
+            const f3 sd = normalize(to_light);
+            rec[0] = make_float4(pos.x, pos.y, pos.z, dist);
+            rec[1] = make_float4(sd.x, sd.y, sd.z, 0.0f);
+            rec[2] = make_float4(cc.x, cc.y, cc.z, 1.0f);
+            P.q_sh[append(P.ctr + C_SH)] = item;
+            ok = true;
+          }
+        }
+      }
+    }
+    if (!ok) rec[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+}
+
+void release_render(tr_ctx* ctx) {
+  if (!ctx->rb) return;
+  RenderBuffers* rb = ctx->rb;
+  for (DevBuf* b : {&rb->P0, &rb->P1, &rb->P2, &rb->P3, &rb->P4, &rb->rng, &rb->M0, &rb->M1, &rb->M2, &rb->HC,
+                    &rb->HM, &rb->SC, &rb->NU, &rb->SH, &rb->acc, &rb->q_ext, &rb->q_act, &rb->q_mat, &rb->q_nee,
+                    &rb->q_sh, &rb->ctr, &rb->stats})
+    b->release();
+  if (rb->h_active) cudaFreeHost(rb->h_active);
+  for (cudaEvent_t e : rb->ev_pool) cudaEventDestroy(e);
+  delete rb;
+  ctx->rb = nullptr;
+}
+
+namespace {
+
+tr_status reserve_render(tr_ctx* ctx, int n, int nl) {
+  if (!ctx->rb) ctx->rb = new RenderBuffers();
+  RenderBuffers* rb = ctx->rb;
+  const size_t N = (size_t)n;
+  const size_t NL = (size_t)std::max(nl, 1);
+  const size_t f4 = sizeof(float4);
+  struct Need {
+    DevBuf* b;
+    size_t bytes;
+  } needs[] = {{&rb->P0, N * f4},           {&rb->P1, N * f4},          {&rb->P2, N * f4},
+               {&rb->P3, N * f4},           {&rb->P4, N * f4},          {&rb->rng, N * 8},
+               {&rb->M0, N * f4},           {&rb->M1, N * f4},          {&rb->M2, N * f4},
+               {&rb->HC, N * f4},           {&rb->HM, N * f4},          {&rb->SC, N * 7 * f4},
+               {&rb->NU, N * NL * 8},       {&rb->SH, N * NL * 3 * f4}, {&rb->acc, N * 32},
+               {&rb->q_ext, 2 * 2 * N * 4}, {&rb->q_act, 2 * N * 4},   {&rb->q_mat, 2 * N * 4},
+               {&rb->q_nee, 2 * N * NL * 4}, {&rb->q_sh, N * NL * 4},  {&rb->ctr, 64},
+               {&rb->stats, 64}};
+  for (auto& nd : needs) {
+    cudaError_t e = nd.b->reserve(nd.bytes);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "render buffer allocation");
+  }
+  if (!rb->h_active) {
+    cudaError_t e = cudaHostAlloc((void**)&rb->h_active, 64, cudaHostAllocDefault);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "pinned counter allocation");
+  }
+  rb->n = n;
+  rb->nl = nl;
+  return TR_OK;
+}
+
+void setup_camera(Cam& c, const tr_camera& p) {
+  // look_at (src/utility/transform.cpp:96-124) and the ThinLensCamera
+  // constructor (src/camera/thin_lens_camera.cpp:23-36), host arithmetic
+  const f3 pos = mk3(p.pos[0], p.pos[1], p.pos[2]), target = mk3(p.target[0], p.target[1], p.target[2]);
+  const f3 up = mk3(p.up[0], p.up[1], p.up[2]);
+  const f3 dir = normalize(target - pos);
+  const f3 right = normalize(cross(normalize(up), dir));
+  const f3 new_up = cross(dir, right);
+  const float m[16] = {right.x, new_up.x, dir.x, pos.x, right.y, new_up.y, dir.y, pos.y,
+                       right.z, new_up.z, dir.z, pos.z, 0.0f,    0.0f,     0.0f,  1.0f};
+  std::memcpy(c.m, m, sizeof(m));
+  c.focal = p.focal_dist;
+  c.lens_radius = p.lens_radius;
+  c.film_h = (float)(2 * p.focal_dist * std::tan(p.fov * 0.5));
+  c.film_w = p.film_aspect * c.film_h;
+}
+
+}  // namespace
+
+tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter, const tr_render_params* prm,
+                      void* d_out, bool fp64, tr_stats* stats) {
+  if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
+  if (prm->width <= 0 || prm->height <= 0 || prm->spp <= 0 || prm->max_depth < 0)
+    return set_err(ctx, TR_ERR_ARG, "invalid render size, spp or depth");
+  if ((long long)prm->width * prm->height > (1ll << 28)) return set_err(ctx, TR_ERR_ARG, "film too large");
+  if (prm->direct_light_sample_num != 1)
+    return set_err(ctx, TR_ERR_UNSUPPORTED, "direct_light_sample_num must be 1 on the GPU path");
+  if (!(filter->radius > 0.0f) || filter->radius > 16.0f) return set_err(ctx, TR_ERR_ARG, "invalid filter radius");
+  const int n = prm->width * prm->height;
+  const int nl = ctx->dsc.num_lights;
+  if ((long long)n * std::max(nl, 1) > (1ll << 30)) return set_err(ctx, TR_ERR_ARG, "too many shadow records");
+  tr_status s = reserve_render(ctx, n, nl);
+  if (s != TR_OK) return s;
+  RenderBuffers* rb = ctx->rb;
+  cudaStream_t st = ctx->stream;
+
+  Launch P;
+  std::memset(&P, 0, sizeof(P));
+  P.sc = ctx->dsc;
+  setup_camera(P.cam, *cam);
+  P.W = prm->width;
+  P.H = prm->height;
+  P.spp = prm->spp;
+  P.min_depth = prm->min_depth;
+  P.max_depth = prm->max_depth;
+  P.nl = nl;
+  P.seed_base = prm->seed_base;
+  P.filter_radius = filter->radius;
+  P.filter_alpha = filter->alpha;
+  P.filter_exp = std::exp(-filter->alpha * filter->radius * filter->radius);  // GaussianFilter ctor
+  P.fp64 = fp64 ? 1 : 0;
+  P.P0 = rb->P0.as<float4>();
+  P.P1 = rb->P1.as<float4>();
+  P.P2 = rb->P2.as<float4>();
+  P.P3 = rb->P3.as<float4>();
+  P.P4 = rb->P4.as<float4>();
+  P.rng = rb->rng.as<unsigned long long>();
+  P.M0 = rb->M0.as<float4>();
+  P.M1 = rb->M1.as<float4>();
+  P.M2 = rb->M2.as<float4>();
+  P.HC = rb->HC.as<float4>();
+  P.HM = rb->HM.as<float4>();
+  P.SC = rb->SC.as<float4>();
+  P.NU = rb->NU.as<float2>();
+  P.SH = rb->SH.as<float4>();
+  P.acc = d_out ? static_cast<float4*>(d_out) : rb->acc.as<float4>();
+  for (int k = 0; k < 2; ++k) {
+    P.q_ext[k] = rb->q_ext.as<int>() + (size_t)k * 2 * n;
+    P.q_act[k] = rb->q_act.as<int>() + (size_t)k * n;
+    P.q_mat[k] = rb->q_mat.as<int>() + (size_t)k * n;
+    P.q_nee[k] = rb->q_nee.as<int>() + (size_t)k * n * std::max(nl, 1);
+  }
+  P.q_sh = rb->q_sh.as<int>();
+  P.ctr = rb->ctr.as<unsigned int>();
+  P.stats = rb->stats.as<unsigned long long>();
+
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  if (sms <= 0) sms = 1;
+  const int grid = sms * 16, grid_init = sms * 8;
+
+  ctx->cancel.store(0);
+  cudaEvent_t e0, e1, chk;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventCreateWithFlags(&chk, cudaEventDisableTiming);
+  const bool timed = (prm->flags & TR_RENDER_TIME_STAGES) != 0;
+  std::vector<cudaEvent_t>& ev = rb->ev_pool;
+  size_t nev = 0;
+  auto cleanup = [&]() {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(chk);
+  };
+#define RCHK(call)                      \
+  do {                                  \
+    cudaError_t e_ = (call);            \
+    if (e_ != cudaSuccess) {            \
+      cleanup();                        \
+      return cuda_fail(ctx, e_, #call); \
+    }                                   \
+  } while (0)
+  RCHK(cudaMemsetAsync(P.acc, 0, (size_t)n * (fp64 ? 32 : 16), st));
+  RCHK(cudaMemsetAsync(P.ctr, 0, 64, st));
+  RCHK(cudaMemsetAsync(P.stats, 0, 64, st));
+  RCHK(cudaEventRecord(e0, st));
+  k_init<<<grid_init, 256, 0, st>>>(P);
+  RCHK(cudaGetLastError());
+
+  // optional per-stage timing: events around extend, shading (logic,
+  // material, nee) and shadow of every iteration, summed once drained
+  auto mark = [&]() {
+    if (!timed) return;
+    if (nev == ev.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      ev.push_back(e);
+    }
+    cudaEventRecord(ev[nev++], st);
+  };
+  // Every slot finishes within spp * (max_depth + 2) iterations.
+  const long long max_iters = (long long)prm->spp * (prm->max_depth + 2) + 4;
+  const int chunk = 4;
+  long long it = 0;
+  bool done = false, chk_pending = false;
+  tr_status result = TR_OK;
+  while (!done) {
+    for (int c = 0; c < chunk && it < max_iters; ++c, ++it) {
+      const int cur = (int)(it & 1), nxt = cur ^ 1;
+      mark();
+      k_extend<<<grid, 128, 0, st>>>(P, cur);
+      mark();
+      // next iteration's extend and live counts; this iteration's shadow,
+      // material and light-sample counts
+      RCHK(cudaMemsetAsync(P.ctr + C_EXT + nxt, 0, 4, st));
+      RCHK(cudaMemsetAsync(P.ctr + C_ACT + nxt, 0, 4, st));
+      RCHK(cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 5, st));  // C_SH, C_MAT x2, C_NEE x2
+      mark();
+      k_logic<<<grid, 128, 0, st>>>(P, cur);
+      k_material<MAT_PHONG><<<grid, 128, 0, st>>>(P, cur);
+      k_material<MAT_DISNEY12><<<grid, 128, 0, st>>>(P, cur);
+      k_nee<MAT_PHONG><<<grid, 128, 0, st>>>(P);
+      k_nee<MAT_DISNEY12><<<grid, 128, 0, st>>>(P);
+      mark();
+      k_shadow<<<grid, 128, 0, st>>>(P);
+      mark();
+    }
+    RCHK(cudaGetLastError());
+    if (chk_pending) {
+      RCHK(cudaEventSynchronize(chk));
+      if (rb->h_active[0] == 0) done = true;
+    }
+    if (!done) {
+      const int nxt_after = (int)(it & 1);
+      RCHK(cudaMemcpyAsync(rb->h_active, P.ctr + C_ACT + nxt_after, 4, cudaMemcpyDeviceToHost, st));
+      RCHK(cudaEventRecord(chk, st));
+      chk_pending = true;
+      if (it >= max_iters) {
+        RCHK(cudaEventSynchronize(chk));
+        if (rb->h_active[0] != 0)
+          result = set_err(ctx, TR_ERR_TIMEOUT, "wavefront did not drain within its iteration bound");
+        done = true;
+      }
+    }
+    if (ctx->cancel.load()) {
+      result = set_err(ctx, TR_ERR_CANCELLED, "render cancelled");
+      done = true;
+    }
+  }
+  RCHK(cudaEventRecord(e1, st));
+  RCHK(cudaEventSynchronize(e1));
+  unsigned long long hs[4] = {0, 0, 0, 0};
+  RCHK(cudaMemcpy(hs, P.stats, sizeof(hs), cudaMemcpyDeviceToHost));
+  unsigned int ctrs[16];
+  RCHK(cudaMemcpy(ctrs, P.ctr, sizeof(ctrs), cudaMemcpyDeviceToHost));
+  double stage[3] = {0.0, 0.0, 0.0};
+  for (size_t k = 0; k + 5 <= nev; k += 5) {
+    float a = 0.0f, b = 0.0f, c = 0.0f;
+    cudaEventElapsedTime(&a, ev[k], ev[k + 1]);
+    cudaEventElapsedTime(&b, ev[k + 2], ev[k + 3]);
+    cudaEventElapsedTime(&c, ev[k + 3], ev[k + 4]);
+    stage[0] += a;
+    stage[1] += b;
+    stage[2] += c;
+  }
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cleanup();
+  if (ctrs[C_ERR] != 0 && result == TR_OK) result = set_err(ctx, TR_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
+  if (stats) {
+    stats->samples = hs[0];
+    stats->extend_rays = hs[1];
+    stats->shadow_rays = hs[2];
+    stats->shade_items = hs[3];
+    stats->iterations = (uint64_t)it;
+    stats->device_ms = ms;
+    for (int k = 0; k < 3; ++k) stats->stage_ms[k] = stage[k];
+  }
+  return result;
+#undef RCHK
+}
+
+}  // namespace trg
+
+using namespace trg;
+
+extern "C" {
+
+tr_status tr_render_dev(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter, const tr_render_params* params,
+                        float* d_rgbw, double* d_rgbw64, tr_stats* stats) {
+  if (!ctx || !cam || !filter || !params || ((d_rgbw == nullptr) == (d_rgbw64 == nullptr))) return TR_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  void* out = d_rgbw ? (void*)d_rgbw : (void*)d_rgbw64;
+  if (((uintptr_t)out & 15u) != 0) return set_err(ctx, TR_ERR_ARG, "film buffer must be 16-byte aligned");
+  return render_impl(ctx, cam, filter, params, out, d_rgbw64 != nullptr, stats);
+}
+
+tr_status tr_render(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter, const tr_render_params* params,
+                    float* rgbw, double* rgbw64, tr_stats* stats) {
+  if (!ctx || !cam || !filter || !params || ((rgbw == nullptr) == (rgbw64 == nullptr))) return TR_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  tr_status s = render_impl(ctx, cam, filter, params, nullptr, rgbw64 != nullptr, stats);
+  if (s != TR_OK) return s;
+  const size_t n = (size_t)params->width * params->height;
+  cudaError_t e = rgbw64 ? cudaMemcpy(rgbw64, ctx->rb->acc.p, n * 32, cudaMemcpyDeviceToHost)
+                         : cudaMemcpy(rgbw, ctx->rb->acc.p, n * 16, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "film copy");
+  return TR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,112 @@
+// scene_types.h -- device-resident scene layout (HBM), shared by host upload
+// code and kernels.
+//
+// Layout decisions (one scene, read-only during a render):
+//  * DNode: the reference's binary BVH re-packed as child pairs. One 64-byte
+//    record per interior node holds both children's boxes, child references
+//    and the split axis, so a visit is four 16-byte vector loads and two box
+//    tests. Traversal keeps the reference's order and culling exactly (see
+//    traverse.cuh).
+//  * Slots: primitives in BVH leaf order, three float4 (48 bytes) each.
+//    Triangle: (A, id) (B-A, -1) (C-A, 0) -- B-A and C-A are the float
+//    differences the reference computes on every test. Sphere: (0, id)
+//    (0, sphere index) (0).
+//  * Per-primitive, per-triangle, per-sphere, per-material and per-light
+//    tables indexed by the scene description's ids, holding only values
+//    the reference would recompute identically on every hit (constant
+//    frames, material-derived weights).
+#pragma once
+
+#include <stdint.h>
+
+#include "exact32.cuh"
+
+#if !defined(__CUDACC__)
+struct alignas(16) float4 {
+  float x, y, z, w;
+};
+struct alignas(16) int4 {
+  int x, y, z, w;
+};
+#endif
+
+namespace trg {
+
+struct alignas(16) DNode {
+  float4 a;  // L.lo.x L.lo.y L.lo.z L.hi.x
+  float4 b;  // L.hi.y L.hi.z R.lo.x R.lo.y
+  float4 c;  // R.lo.z R.hi.x R.hi.y R.hi.z
+  int4 d;    // L.ref, R.ref, L.count | R.count << 16, axis. count > 0: ref is a
+             // leaf's first slot; count == 0: ref is the child's DNode index.
+};
+static_assert(sizeof(DNode) == 64, "DNode must be 64 bytes");
+
+struct DSphere {
+  float inv[16];  // world_to_local (row-major)
+  float m[16];    // local_to_world
+  float radius;
+  int pad[3];
+};
+
+enum { PRIM_TRIANGLE = 0, PRIM_SPHERE = 1 };
+
+struct DPrim {
+  int kind;
+  int shape;     // triangle or sphere index
+  int material;
+  int emissive;  // 1 if the emission is not black (GeometricPrimitive owns a DiffuseLight)
+  f3 emission;
+  float area;    // Triangle::surface_area() of emissive triangles
+};
+
+struct DTriShade {
+  f3 gx, gy, gz;  // geometry frame: constant per triangle (src/shape/triangle.cpp:193-198)
+  f3 nA, dn1, dn2;  // normalised vertex normal A, nB - nA, nC - nA
+  f3 dndu0, dndv0;  // compute_ss_ts(nB-nA, nC-nA, uv...) when its determinant != 0
+  int det_nonzero;
+  int pad[3];
+};
+
+enum { MAT_PHONG = 0, MAT_DISNEY12 = 1 };
+
+// Phong: the AggregateBSDF<2> that Phong::shading builds (src/material/phong.cpp:29-70)
+// Disney12: the eleven parameters (src/material/disney_brdf.cpp:278-302)
+struct DMat {
+  int kind;
+  float ns, w_diffuse, w_specular;
+  // Disney12 per-material constants the reference recomputes on every call
+  // (src/material/disney_brdf.cpp:81-83,142-151,188-193)
+  float ax, ay, p_diffuse, p_spec_sample, p_spec_pdf;
+  f3 diffuse_coef;  // albedo / PI of DiffuseBXDF
+  f3 specular;      // PhongSpecularBXDF colour
+  f3 albedo;        // LocalBSDF::get_albedo(): diffuse + specular, or Disney base colour
+  float subsurface, metallic, specular_s, specular_tint, roughness, anisotropic;
+  float sheen, sheen_tint, clearcoat, clearcoat_gloss;
+  f3 base;
+};
+
+// A diffuse area light on a triangle (src/light/diffuse_light.cpp:44-60)
+struct DLight {
+  f3 A, B, C;
+  f3 gz;          // geometry normal of sampled points
+  f3 emission;
+  float area_pdf; // 1 / surface_area()
+  int prim;
+  int pad[2];
+};
+
+struct DScene {
+  const DNode* nodes;
+  const float4* slots;
+  const DSphere* spheres;
+  const DPrim* prims;
+  const DTriShade* tshade;
+  const DMat* mats;
+  const DLight* lights;
+  int num_lights;
+  int root_kind;  // 0 empty, 1 interior (DNode 0), 2 leaf
+  int root_offset, root_count;
+  float root_lo[3], root_hi[3];
+};
+
+}  // namespace trg

@@ -1,0 +1,586 @@
+// shade.cuh -- per-vertex shading on the device: sampler, camera, hit
+// records, BSDFs (Phong aggregate and Disney12), area lights, film filter.
+//
+// Each function restates one reference function (cited) with its exact
+// float/double arithmetic; this file is compiled with --fmad=false.
+// Transcendentals (sinf, cosf, atan2f, powf, logf, expf) are CUDA's: they may
+// differ from glibc in the last bit, so paths that pass through them can
+// diverge from the CPU reference after the first such difference; ray
+// arithmetic (traversal, frames, normalisation) is exact.
+#pragma once
+
+#include "scene_types.h"
+
+namespace trg {
+
+// ----------------------------------------------------------------- sampler
+// pcg32 (setseq XSH-RR 64/32, default stream, output of the previous state)
+// behind SimpleUniformSampler and std::uniform_real_distribution<float>
+// (src/core/sampler.hpp:30-86): u = float(x) / 2^32, clamped below 1.
+struct Pcg {
+  static constexpr unsigned long long kMul = 6364136223846793005ULL;
+  static constexpr unsigned long long kInc = 1442695040888963407ULL;
+  static __device__ __forceinline__ unsigned long long seed(int s) {
+    return ((unsigned long long)(long long)s + kInc) * kMul + kInc;
+  }
+  static __device__ __forceinline__ float next(unsigned long long& st) {
+    const unsigned long long old = st;
+    st = old * kMul + kInc;
+    const unsigned xs = (unsigned)(((old >> 18u) ^ old) >> 27u);
+    const unsigned rot = (unsigned)(old >> 59u);
+    const unsigned x = (xs >> rot) | (xs << ((32u - rot) & 31u));
+    float u = __uint2float_rn(x) * 2.3283064365386963e-10f;
+    return u >= 1.0f ? 0.99999994f : u;
+  }
+};
+
+// ---------------------------------------------------------------- sampling
+// ConcentricSampleDisk (src/core/sampling.cpp:8-22)
+__device__ __forceinline__ void concentric_disk(float u, float v, float& ox, float& oy) {
+  const float x = u * 2.0f - 1.0f, y = v * 2.0f - 1.0f;
+  if (x == 0.0f && y == 0.0f) {
+    ox = 0.0f;
+    oy = 0.0f;
+    return;
+  }
+  float theta, r;
+  if (fabsf(x) > fabsf(y)) {
+    r = x;
+    theta = kPiOver4 * (y / x);
+  } else {
+    r = y;
+    theta = kPiOver2 - kPiOver4 * (x / y);
+  }
+  float st, ct;
+  sincosf(theta, &st, &ct);
+  ox = r * ct;
+  oy = r * st;
+}
+// CosineSampleHemisphere (src/core/sampling.cpp:24-28)
+__device__ __forceinline__ f3 cosine_hemisphere(float u, float v) {
+  float dx, dy;
+  concentric_disk(u, v, dx, dy);
+  const float z = sqrtf(smax(0.0f, 1.0f - dx * dx - dy * dy));
+  return mk3(dx, dy, z);
+}
+__device__ __forceinline__ float cosine_pdf(float c) { return c * kInvPi; }
+// PowerHeuristic (src/core/sampling.hpp:230-233)
+__device__ __forceinline__ float power_heuristic(float fp, float gp) { return (fp * fp) / (fp * fp + gp * gp); }
+
+// Spectrum helpers (src/core/spectrum.hpp)
+__device__ __forceinline__ f3 mulc(f3 a, f3 b) { return mk3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ f3 muls(f3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ f3 divs(f3 a, float s) { return mk3(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ f3 adds(f3 a, float s) { return mk3(a.x + s, a.y + s, a.z + s); }
+__device__ __forceinline__ bool black(f3 c) { return c.x == 0.0f && c.y == 0.0f && c.z == 0.0f; }
+__device__ __forceinline__ bool finite3(f3 c) { return isfinite(c.x) && isfinite(c.y) && isfinite(c.z); }
+__device__ __forceinline__ bool valid3(f3 c) { return c.x >= 0.0f && c.y >= 0.0f && c.z >= 0.0f && finite3(c); }
+__device__ __forceinline__ float lum(f3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+// mix(l, r, f) = (1 - f) * l + f * r (src/utility/geometry.hpp:989-993)
+__device__ __forceinline__ f3 mix3(f3 l, f3 r, float f) { return muls(l, 1.0f - f) + muls(r, f); }
+__device__ __forceinline__ float mixf(float l, float r, float f) { return (1.0f - f) * l + f * r; }
+
+// ---------------------------------------------------------------- surface
+struct Isect {
+  f3 pos, wo;
+  Frame g, s;
+  int prim;
+  // SurfacePoint::eps_offset (src/core/intersection.hpp:19-23)
+  __device__ __forceinline__ f3 eps_offset(f3 dir) const {
+    if (dot(g.z, dir) > 0.0f) return pos + scale(g.z, kEps);
+    return pos - scale(g.z, kEps);
+  }
+};
+
+// Triangle::intersect_p hit record (src/shape/triangle.cpp:175-213); the
+// geometry frame and compute_ss_ts of the normals are per-triangle constants.
+__device__ __forceinline__ void triangle_isect(const DTriShade& ts, f3 o, f3 d, float t, float alpha, float beta,
+                                               Isect& is) {
+  is.wo = -d;
+  is.pos = o + scale(d, t);
+  is.g.x = ts.gx;
+  is.g.y = ts.gy;
+  is.g.z = ts.gz;
+  const f3 sn = ts.nA + scale(ts.dn1, alpha) + scale(ts.dn2, beta);
+  f3 dndu, dndv;
+  if (ts.det_nonzero) {
+    dndu = ts.dndu0;
+    dndv = ts.dndv0;
+  } else {
+    coordinate(sn, dndu, dndv);
+  }
+  if (len2f(dndu) < kEps || len2f(dndv) < kEps) coordinate(sn, dndu, dndv);
+  dndu = cross(dndv, sn);
+  dndv = cross(sn, dndu);
+  is.s = make_frame(dndu, dndv, sn);
+}
+
+// Sphere::intersect_p hit record + TransformedShape::to_world
+// (src/shape/sphere.cpp:48-78,98-119; src/shape/transformed_shape.hpp:31-44).
+// The (u, v) coordinates are not formed: constant textures never read them.
+__device__ __forceinline__ void sphere_isect(const DSphere& S, f3 o, f3 d, float t, Isect& is) {
+  const f3 lo = xform_point(S.inv, o);
+  const f3 ld = normalize(xform_vec(S.inv, d));
+  const f3 p = lo + scale(ld, t);
+  f3 ex, ey, ez = normalize(p);
+  if (fabsf(ez.z - 1.0f) < kEps) {
+    ex = mk3(1.0f, 0.0f, 0.0f);
+    ey = mk3(0.0f, 1.0f, 0.0f);
+    ez = mk3(0.0f, 0.0f, 1.0f);
+  } else if (fabsf(ez.z + 1.0f) < kEps) {
+    ex = mk3(0.0f, 1.0f, 0.0f);
+    ey = mk3(1.0f, 0.0f, 0.0f);
+    ez = mk3(0.0f, 0.0f, -1.0f);
+  } else {
+    ex = cross(mk3(0.0f, 0.0f, 1.0f), ez);
+    ey = cross(ez, ex);
+  }
+  const Frame c = make_frame(ex, ey, ez);
+  is.pos = xform_point(S.m, p);
+  is.g = make_frame(xform_vec(S.m, c.x), xform_vec(S.m, c.y), xform_vec(S.m, c.z));
+  is.s = is.g;
+  is.wo = xform_vec(S.m, -ld);
+}
+
+__device__ __forceinline__ void make_isect(const DScene& sc, const float4 hit, f3 o, f3 d, Isect& is) {
+  const int pid = __float_as_int(hit.x);
+  const DPrim& p = sc.prims[pid];
+  is.prim = pid;
+  if (p.kind == PRIM_TRIANGLE)
+    triangle_isect(sc.tshade[p.shape], o, d, hit.y, hit.z, hit.w, is);
+  else
+    sphere_isect(sc.spheres[p.shape], o, d, hit.y, is);
+}
+
+// ------------------------------------------------------------------- BSDFs
+struct BsdfSample {
+  f3 wi, f;
+  float pdf;
+  __device__ __forceinline__ bool valid() const { return pdf > 0.0f && !black(f); }  // core/bsdf.hpp:21-23
+};
+
+// microfacet helpers (src/material/utility/microfacet.cpp:7-134, microfacet.hpp:10-14)
+__device__ __forceinline__ float sqr(float x) { return x * x; }
+__device__ __forceinline__ float one_minus_5(float x) {
+  const float t = 1.0f - x;
+  const float t2 = t * t;
+  return t2 * t2 * t;
+}
+__device__ __forceinline__ float compute_alpha(float sp, float cp, float ax, float ay) {
+  return sqr(cp / ax) + sqr(sp / ay);
+}
+__device__ __forceinline__ float anisotropic_gtr2(float sp, float cp, float st, float ct, float ax, float ay) {
+  const float A = compute_alpha(sp, cp, ax, ay);
+  const float RD = sqr(st) * A + sqr(ct);
+  return 1.0f / (kPi * ax * ay * sqr(RD));
+}
+__device__ __forceinline__ float gtr1(float st, float ct, float alpha) {
+  if (alpha >= 1.0f) return kInvPi;
+  const float U = sqr(alpha) - 1.0f;
+  const float LD = 2.0f * kPi * logf(alpha);
+  const float RD = sqr(alpha * ct) + sqr(st);
+  return U / (LD * RD);
+}
+__device__ __forceinline__ float smith_aniso_gtr2(float cos_phi, float sin_phi, float ax, float ay, float tan_theta) {
+  const float t = sqr(ax * cos_phi) + sqr(ay * sin_phi);
+  const float sq = 1.0f + t * sqr(tan_theta);
+  const float lambda = -0.5f + 0.5f * sqrtf(sq);
+  return 1.0f / (1.0f + lambda);
+}
+__device__ __forceinline__ float smith_gtr2(float tan_theta, float alpha) {
+  if (!tan_theta) return 1.0f;
+  const float root = alpha * tan_theta;
+  return 2.0f / (1.0f + sqrtf(1.0f + root * root));
+}
+__device__ __forceinline__ f3 sample_aniso_gtr2(float ax, float ay, float u, float v) {
+  float s2, c2;
+  sincosf(2.0f * kPi * u, &s2, &c2);
+  float sp = ay * s2;
+  float cp = ax * c2;
+  const float nor = 1.0f / sqrtf(sqr(sp) + sqr(cp));
+  sp *= nor;
+  cp *= nor;
+  const float A = compute_alpha(sp, cp, ax, ay);
+  const float ct = sqrtf(A * (1.0f - v) / ((1.0f - A) * v + A));
+  const float st = sqrtf(smax(0.0f, 1.0f - sqr(ct)));
+  return normalize(mk3(st * cp, st * sp, ct));
+}
+__device__ __forceinline__ float local_cos_to_sin(float c) { return sqrtf(smax(0.0f, 1.0f - c * c)); }
+__device__ __forceinline__ f3 sample_gtr1(float alpha, float u, float v) {
+  const float phi = 2.0f * kPi * u;
+  const float ct = sqrtf((powf(alpha, 2.0f - 2.0f * v) - 1.0f) / (sqr(alpha) - 1.0f));
+  const float st = local_cos_to_sin(ct);
+  float sphi, cphi;
+  sincosf(phi, &sphi, &cphi);
+  return normalize(mk3(st * cphi, st * sphi, ct));
+}
+// local_phi / local_tan_theta (src/utility/geometry.hpp:912-928)
+__device__ __forceinline__ float local_phi(f3 w) {
+  if (!w.y && !w.x) return 0.0f;
+  const float r = atan2f(w.y, w.x);
+  return r < 0.0f ? (r + 2.0f * kPi) : r;
+}
+__device__ __forceinline__ float local_tan_theta(f3 w) {
+  const float t = 1.0f - w.z * w.z;
+  if (t <= 0.0f) return 0.0f;
+  return sqrtf(t) / w.z;
+}
+// reflect (src/utility/reflection.hpp:12-14)
+__device__ __forceinline__ f3 reflect(f3 w, f3 n) { return scale(n, 2.0f * dot(w, n)) - w; }
+
+// PhongSpecularBXDF (src/material/bxdf/phong_specular_bxdf.cpp:10-71)
+__device__ __forceinline__ float powcos_pdf(float e, float c) { return (e + 1.0f) * kInv2Pi * powf(c, e); }
+__device__ __forceinline__ f3 phong_eval(const DMat& m, f3 lwi, f3 lwo) {
+  if (lwi.z <= 0.0f || lwo.z <= 0.0f) return mk3(0.0f, 0.0f, 0.0f);
+  const f3 ideal = reflect(lwo, mk3(0.0f, 0.0f, 1.0f));
+  const float c = cos_x(ideal, lwi);
+  if (c <= 0.0f) return mk3(0.0f, 0.0f, 0.0f);
+  return muls(m.specular, powcos_pdf(m.ns, c));
+}
+__device__ __forceinline__ float phong_pdf(const DMat& m, f3 lwi, f3 lwo) {
+  if (lwi.z <= 0.0f || lwo.z <= 0.0f) return 0.0f;
+  const f3 ideal = reflect(lwo, mk3(0.0f, 0.0f, 1.0f));
+  const float c = cosv(lwi, ideal);
+  if (c <= 0.0f) return 0.0f;
+  return powcos_pdf(m.ns, c);
+}
+__device__ __forceinline__ bool phong_sample(const DMat& m, f3 lwo, float u, float v, f3& lwi_out, f3& f,
+                                             float& pdf) {
+  if (lwo.z <= 0.0f) return false;
+  const f3 ideal = normalize(reflect(lwo, mk3(0.0f, 0.0f, 1.0f)));
+  const float ct = powf(u, 1.0f / (m.ns + 1.0f));
+  const float st = sqrtf(smax(0.0f, 1.0f - ct * ct));
+  const float phi = 2.0f * kPi * v;
+  float sphi, cphi;
+  sincosf(phi, &sphi, &cphi);
+  const f3 local = normalize(mk3(st * cphi, st * sphi, ct));
+  const f3 lwi = normalize(to_global(frame_from_z(ideal), local));
+  if (lwi.z <= 0.0f) return false;
+  pdf = powcos_pdf(m.ns, local.z);
+  f = phong_eval(m, lwi, lwo);
+  lwi_out = lwi;
+  return pdf > 0.0f;
+}
+// DiffuseBXDF (src/material/bxdf/diffuse_bxdf.cpp:14-38)
+__device__ __forceinline__ f3 diffuse_eval(const DMat& m, f3 lwi, f3 lwo) {
+  if (lwi.z <= 0.0f || lwo.z <= 0.0f) return mk3(0.0f, 0.0f, 0.0f);
+  return m.diffuse_coef;
+}
+__device__ __forceinline__ float diffuse_pdf(f3 lwi, f3 lwo) {
+  if (lwi.z <= 0.0f || lwo.z <= 0.0f) return 0.0f;
+  return cosine_pdf(lwi.z);
+}
+
+static __device__ inline float disney_fd90_d(float L, float r) {
+  return (float)(0.5 + 2.0 * (double)L * (double)L * (double)r);
+}
+static __device__ inline float disney_ss_d(float Fss, float S) {
+  return (float)(1.25 * ((double)Fss * (1.0 / (double)S - 0.5) + 0.5));
+}
+
+// Fd90 = 0.5 + 2. * LdotH * LdotH * roughness, evaluated in double by the
+// reference (src/material/disney_brdf.cpp:120); certified float-float form.
+__device__ __forceinline__ float disney_fd90(float L, float r) {
+  if (L == 0.0f || r == 0.0f) return 0.5f;
+  if (in_range(L) && in_range(r)) {
+    const float th = L * L, tl = ffma(L, L, -th);
+    const float a = th * r;
+    if (in_range(a)) {
+      const float al = ffma(th, r, -a) + tl * r;
+      float e;
+      const float s0 = two_sum(0.5f, 2.0f * a, e);
+      const float w = e + 2.0f * al;
+      float res;
+      const float y = two_sum(s0, w, res);
+      if (rounds_to(y, res, 5.6843419e-14f * (2.0f * fabsf(a) + 1.0f))) return y;  // 2^-44
+    }
+  }
+  return disney_fd90_d(L, r);
+}
+// ss = 1.25 * (Fss * (1.0 / (NdotL + NdotV) - 0.5) + 0.5) in double
+// (src/material/disney_brdf.cpp:125); certified float-float form.
+__device__ __forceinline__ float disney_ss(float Fss, float S) {
+  if (in_range(S) && (Fss == 0.0f || in_range(Fss))) {
+    const float i0 = 1.0f / S;
+    const float i1 = i0 * ffma(-i0, S, 1.0f);
+    float e;
+    const float t = two_sum(i0, -0.5f, e);
+    const float tw = e + i1;
+    const float ph = Fss * t;
+    const float pl = ffma(Fss, t, -ph) + Fss * tw;
+    float e2;
+    const float q = two_sum(ph, 0.5f, e2);
+    const float ql = e2 + pl;
+    const float qh2 = q * 1.25f;
+    const float ql2 = ffma(q, 1.25f, -qh2) + ql * 1.25f;
+    float res;
+    const float y = two_sum(qh2, ql2, res);
+    const float err = 2.2737368e-13f * (1.0f + fabsf(Fss) * (fabsf(i0) + 1.0f));  // 2^-42
+    if (rounds_to(y, res, err)) return y;
+  }
+  return disney_ss_d(Fss, S);
+}
+
+// normal_correct_factor (src/utility/coordinate.hpp:43-52)
+__device__ __forceinline__ float normal_correct(const Frame& g, const Frame& s, f3 wi) {
+  const float dem = fabsf(cosv(g.z, wi));
+  return dem < kEps ? 1.0f : fabsf(cosv(s.z, wi)) / dem;
+}
+
+struct Bsdf {
+  const DMat* m;
+  Frame g, s;
+
+  // LocalBSDF black-fringe handling (src/core/bsdf.hpp:55-91)
+  __device__ __forceinline__ bool fringe(f3 w) const { return pos_hemi(g, w) ^ pos_hemi(s, w); }
+  __device__ __forceinline__ f3 eval_fringe(f3 wi, f3 wo) const {
+    if (pos_hemi(g, wi) & pos_hemi(g, wo)) return muls(m->albedo, kInvPi);
+    return mk3(0.0f, 0.0f, 0.0f);
+  }
+  __device__ __forceinline__ BsdfSample sample_fringe(f3 wo, float u, float v) const {
+    BsdfSample r;
+    r.pdf = 0.0f;
+    r.f = mk3(0.0f, 0.0f, 0.0f);
+    r.wi = r.f;
+    if (!pos_hemi(g, wo)) return r;
+    const f3 lwi = cosine_hemisphere(u, v);
+    const float pdf = cosine_pdf(lwi.z);
+    if (pdf < kEps) return r;
+    const f3 wi = normalize(to_global(g, lwi));
+    const float nc = normal_correct(g, s, wi);
+    r.wi = wi;
+    r.f = muls(muls(m->albedo, kInvPi), nc);
+    r.pdf = pdf;
+    return r;
+  }
+  __device__ __forceinline__ float pdf_fringe(f3 wi, f3 wo) const {
+    if (pos_hemi(g, wi) ^ pos_hemi(g, wo)) return 0.0f;
+    return cosine_pdf(normalize(to_local(g, wi)).z);
+  }
+
+  // ---- AggregateBSDF<2> of Phong (src/material/aggregate_bsdf.hpp:36-118)
+  __device__ f3 phong_eval_agg(f3 wi, f3 wo) const {
+    if (fringe(wi) | fringe(wo)) return eval_fringe(wi, wo);
+    const f3 lwi = normalize(to_local(s, wi)), lwo = normalize(to_local(s, wo));
+    if (!lwi.z || !lwo.z) return mk3(0.0f, 0.0f, 0.0f);
+    f3 r = mk3(0.0f, 0.0f, 0.0f);
+    r = r + diffuse_eval(*m, lwi, lwo);
+    r = r + phong_eval(*m, lwi, lwo);
+    return r;
+  }
+  __device__ float phong_pdf_agg(f3 wi, f3 wo) const {
+    if (fringe(wi) | fringe(wo)) return pdf_fringe(wi, wo);
+    const f3 lwi = normalize(to_local(s, wi)), lwo = normalize(to_local(s, wo));
+    if (!lwi.z || !lwo.z) return 0.0f;
+    float ws = 0.0f, pdf = 0.0f;
+    ws += m->w_diffuse;
+    pdf += m->w_diffuse * diffuse_pdf(lwi, lwo);
+    ws += m->w_specular;
+    pdf += m->w_specular * phong_pdf(*m, lwi, lwo);
+    return ws > 0.0f ? pdf / ws : 0.0f;
+  }
+  __device__ BsdfSample phong_sample_agg(f3 wo, float u, float v, float w) const {
+    if (fringe(wo)) return sample_fringe(wo, u, v);
+    BsdfSample out;
+    out.pdf = 0.0f;
+    out.f = mk3(0.0f, 0.0f, 0.0f);
+    out.wi = out.f;
+    const f3 lwo = normalize(to_local(s, wo));
+    if (!lwo.z) return out;
+    float ws = 0.0f;
+    ws += m->w_diffuse;
+    ws += m->w_specular;
+    float sel = (u - 0.001f) * ws;
+    const float w0 = m->w_diffuse, w1 = m->w_specular;
+    int which = -1;
+    float weight = 0.0f;
+    if (sel <= w0) {
+      which = 0;
+      weight = w0;
+    } else {
+      sel -= w0;
+      if (sel <= w1) {
+        which = 1;
+        weight = w1;
+      }
+    }
+    if (which < 0) return out;
+    f3 lwi, f;
+    float pdf;
+    if (which == 0) {
+      if (lwo.z <= 0.0f) return out;
+      lwi = cosine_hemisphere(v, w);
+      pdf = cosine_pdf(lwi.z);
+      if (pdf < 0.001f) return out;
+      f = m->diffuse_coef;
+    } else {
+      if (!phong_sample(*m, lwo, v, w, lwi, f, pdf)) return out;
+    }
+    lwi = normalize(lwi);
+    pdf *= weight;
+    if (which != 0) {
+      f = f + diffuse_eval(*m, lwi, lwo);
+      pdf += diffuse_pdf(lwi, lwo) * w0;
+    }
+    if (which != 1) {
+      f = f + phong_eval(*m, lwi, lwo);
+      pdf += phong_pdf(*m, lwi, lwo) * w1;
+    }
+    const f3 wi = to_global(s, lwi);
+    const float nc = normal_correct(g, s, wi);
+    out.wi = wi;
+    out.f = muls(f, nc);
+    out.pdf = pdf;
+    return out;
+  }
+
+  // ---- DisneyBRDF (src/material/disney_brdf.cpp:56-227); its quirks are kept:
+  // the diffuse draw is overwritten by the specular branch, p_specular differs
+  // between sample and pdf, the pdf mixes with (1 - pdf_diffuse), clearcoat's
+  // pdf passes (sin_phi, cos_phi, gloss) to gtr1, and the Smith term gets
+  // (sin_phi, cos_phi) in its (cos_phi, sin_phi) slots.
+  __device__ __forceinline__ void alphas(float& ax, float& ay) const {
+    ax = m->ax;  // per-material constants computed at upload
+    ay = m->ay;
+  }
+  __device__ f3 disney_eval(f3 wi, f3 wo) const {
+    if (fringe(wi) | fringe(wo)) return eval_fringe(wi, wo);
+    const f3 lwi = normalize(to_local(s, wi));
+    const f3 lwo = normalize(to_local(s, wo));
+    if (lwi.z < kEps || lwo.z < kEps) return mk3(0.0f, 0.0f, 0.0f);
+    const float NdotL = lwi.z, NdotV = lwo.z;
+    const f3 H = normalize(lwi + lwo);
+    const float LdotH = dot(lwi, H);
+    const f3 bc = m->base;
+    const float l = lum(bc);
+    const f3 Ctint = l > 0.0f ? divs(bc, l) : mk3(1.0f, 1.0f, 1.0f);
+    const f3 one = mk3(1.0f, 1.0f, 1.0f);
+    const f3 Cspec0 = mix3(muls(mix3(one, Ctint, m->specular_tint), m->specular_s * 0.08f), bc, m->metallic);
+    const f3 Csheen = mix3(one, Ctint, m->sheen_tint);
+    float ax, ay;
+    alphas(ax, ay);
+    const float phi_h = local_phi(H);
+    float sph, cph;
+    sincosf(phi_h, &sph, &cph);
+    const float Ds = anisotropic_gtr2(sph, cph, local_cos_to_sin(H.z), H.z, ax, ay);
+    const float FH = one_minus_5(LdotH);
+    const f3 Fs = mix3(Cspec0, one, FH);
+    float spi, cpi, spo, cpo;
+    sincosf(local_phi(lwi), &spi, &cpi);
+    float Gs = smith_aniso_gtr2(spi, cpi, ax, ay, local_tan_theta(lwi));
+    sincosf(local_phi(lwo), &spo, &cpo);
+    Gs *= smith_aniso_gtr2(spo, cpo, ax, ay, local_tan_theta(lwo));
+    const float Dr = gtr1(local_cos_to_sin(H.z), H.z, mixf(0.1f, 0.001f, m->clearcoat_gloss));
+    const float Fr = mixf(0.04f, 1.0f, FH);
+    const float Gr = smith_gtr2(local_tan_theta(lwi), 0.25f) * smith_gtr2(local_tan_theta(lwo), 0.25f);
+    f3 fd = mk3(0.0f, 0.0f, 0.0f);
+    fd = fd + divs(adds(muls(muls(Fs, Ds), Gs), 0.25f * m->clearcoat * Gr * Fr * Dr), 4.0f * NdotL * NdotV);
+    if (m->metallic < 1.0f) {
+      const float FL = one_minus_5(NdotL), FV = one_minus_5(NdotV);
+      const float Fd90 = disney_fd90(LdotH, m->roughness);
+      const float Fd = mixf(1.0f, Fd90, FL) * mixf(1.0f, Fd90, FV);
+      const float Fss90 = LdotH * LdotH * m->roughness;
+      const float Fss = mixf(1.0f, Fss90, FL) * mixf(1.0f, Fss90, FV);
+      const float ss = disney_ss(Fss, NdotL + NdotV);
+      const f3 Fsheen = muls(Csheen, FH * m->sheen);
+      fd = fd + muls(muls(muls(bc, kInvPi), mixf(Fd, ss, m->subsurface)) + Fsheen, 1.0f - m->metallic);
+    }
+    return muls(fd, normal_correct(g, s, wi));
+  }
+  __device__ float disney_pdf(f3 wi, f3 wo) const {
+    if (fringe(wi) | fringe(wo)) return pdf_fringe(wi, wo);
+    const float p_diffuse = m->p_diffuse;
+    const float p_specular = m->p_spec_pdf;
+    float ax, ay;
+    alphas(ax, ay);
+    const f3 lwi = normalize(to_local(s, wi));
+    const f3 lwo = normalize(to_local(s, wo));
+    if (lwi.z < kEps) return 0.0f;
+    const f3 H = normalize(lwi + lwo);
+    const float pdf_diffuse = cosine_pdf(lwi.z);
+    float sph, cph;
+    sincosf(local_phi(H), &sph, &cph);
+    const float pdf_spec = anisotropic_gtr2(sph, cph, local_cos_to_sin(H.z), H.z, ax, ay) * H.z / (4.0f * dot(lwi, H));
+    const float pdf_cc = gtr1(sph, cph, m->clearcoat_gloss) * H.z / (4.0f * dot(lwi, H));
+    const float pdf = p_diffuse * pdf_diffuse + (1.0f - pdf_diffuse) * (p_specular * pdf_spec + (1.0f - p_specular) * pdf_cc);
+    if (!isfinite(pdf)) return 0.0f;
+    return pdf;
+  }
+  __device__ BsdfSample disney_sample(f3 wo, float u, float v, float w) const {
+    if (fringe(wo)) return sample_fringe(wo, u, v);
+    BsdfSample r;
+    r.pdf = 0.0f;
+    r.f = mk3(0.0f, 0.0f, 0.0f);
+    r.wi = r.f;
+    const float p_diffuse = m->p_diffuse;
+    const float p_specular = m->p_spec_sample;
+    const f3 lwo = normalize(to_local(s, wo));
+    f3 lwi = mk3(0.0f, 0.0f, 0.0f);
+    float sel = u;
+    float ax, ay;
+    alphas(ax, ay);
+    if (sel < p_diffuse) lwi = cosine_hemisphere(v, w);
+    sel -= p_diffuse;
+    if (sel < p_specular) {
+      const f3 lwh = sample_aniso_gtr2(ax, ay, v, w);
+      if (lwh.z > 0.0f) {
+        lwi = normalize(scale(lwh, 2.0f * dot(lwo, lwh)) - lwo);
+        if (lwi.z <= 0.0f) lwi = mk3(0.0f, 0.0f, 0.0f);
+      }
+    } else {
+      const f3 lwh = sample_gtr1(m->clearcoat_gloss, v, w);
+      if (lwh.z > 0.0f) {
+        lwi = normalize(scale(lwh, 2.0f * dot(lwo, lwh)) - lwo);
+        if (lwi.z <= 0.0f) lwi = mk3(0.0f, 0.0f, 0.0f);
+      }
+    }
+    if (all_zero(lwi)) return r;
+    r.wi = to_global(s, lwi);
+    r.f = disney_eval(r.wi, wo);
+    r.pdf = disney_pdf(r.wi, wo);
+    return r;
+  }
+
+  __device__ __forceinline__ f3 eval(f3 wi, f3 wo) const {
+    return m->kind == MAT_PHONG ? phong_eval_agg(wi, wo) : disney_eval(wi, wo);
+  }
+  __device__ __forceinline__ float pdf(f3 wi, f3 wo) const {
+    return m->kind == MAT_PHONG ? phong_pdf_agg(wi, wo) : disney_pdf(wi, wo);
+  }
+  __device__ __forceinline__ BsdfSample sample(f3 wo, float u, float v, float w) const {
+    return m->kind == MAT_PHONG ? phong_sample_agg(wo, u, v, w) : disney_sample(wo, u, v, w);
+  }
+};
+
+// ------------------------------------------------------------------ lights
+// DiffuseLight::pdf (src/light/diffuse_light.cpp:31-42)
+__device__ __forceinline__ float light_pdf_at(float area, f3 ref, f3 pos, f3 n) {
+  if (dot(n, ref - pos) <= 0.0f) return 0.0f;
+  const f3 p2ref = ref - pos;
+  const float dist2 = len2f(p2ref);
+  const float abscos = fabsf(cos_x(n, p2ref));
+  area *= abscos;
+  return dist2 / area;
+}
+
+// ------------------------------------------------------------------ camera
+struct Cam {
+  float m[16];  // camera_to_world
+  float film_w, film_h, focal, lens_radius;
+};
+// ThinLensCamera::generate_ray (src/camera/thin_lens_camera.cpp:40-59)
+__device__ __forceinline__ void camera_ray(const Cam& c, float fx, float fy, float lu, float lv, f3& o, f3& d) {
+  const f3 film = mk3((0.5f - fx) * c.film_w, (0.5f - fy) * c.film_h, c.focal);
+  float dx, dy;
+  concentric_disk(lu, lv, dx, dy);
+  const f3 lens = mk3(c.lens_radius * dx, c.lens_radius * dy, 0.0f);
+  o = xform_point(c.m, lens);
+  d = xform_vec(c.m, normalize(film - lens));
+}
+
+// GaussianFilter::eval term (src/filter/gaussian_filter.cpp:20-30)
+__device__ __forceinline__ float gaussian(float alpha, float d, float expv) {
+  return smax(0.0f, expf(-alpha * d * d) - expv);
+}
+
+}  // namespace trg

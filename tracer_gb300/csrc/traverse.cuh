@@ -1,0 +1,225 @@
+// traverse.cuh -- BVH traversal and primitive tests on the device.
+//
+// Reference: BVHAccel::intersect_p / ::intersect (src/accelerator/bvh.cpp:112-185),
+// Bounds3::intersect_p (src/utility/geometry.hpp:837-864),
+// Triangle::intersect(_p) (src/shape/triangle.cpp:117-174),
+// sphere::intersect(_p) + TransformedShape::to_local (src/shape/sphere.cpp:15-47,
+// src/shape/transformed_shape.hpp:17-21), GeometricPrimitive::intersect_p
+// (src/shape/geometry.cpp:49-60).
+//
+// Order and culling match the reference exactly on child-pair nodes:
+//  * the reference pops a node, tests its box against the CURRENT ray.t_max,
+//    and pushes the children near-last (near = second child when
+//    dir_is_neg[split_axis]);
+//  * a box test is "slab overlap and tMax > 0" (independent of t_max) and
+//    "tMin < t_max". Here both children of a visited node are tested at once;
+//    the near child is entered immediately (no t_max change can happen in
+//    between in the reference), the far child is pushed with its tMin and
+//    the tMin < t_max part is re-evaluated when it is popped.
+// Triangle arithmetic: the two cross products run in double and round to
+// float, the dot products in float, exactly as the reference (no FMA: this
+// file is compiled with --fmad=false).
+#pragma once
+
+#include "scene_types.h"
+
+namespace trg {
+
+struct RayIn {
+  f3 o, d;
+  float t_min, t_max;
+};
+
+struct Hit {
+  int prim;       // -1: miss
+  float t_attr;   // the accepted primitive's own parameter (triangle t, local sphere t)
+  float alpha, beta;
+};
+
+__device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
+
+// Slab test with the reference's arithmetic. Returns the t_max-independent
+// part ("pass"), and tmin for the "tMin < ray.t_max" part.
+__device__ __forceinline__ bool box_pass(float lx, float ly, float lz, float hx, float hy, float hz, f3 o,
+                                         f3 inv, bool n0, bool n1, bool n2, float& tmin) {
+  float tMin = ((n0 ? hx : lx) - o.x) * inv.x;
+  float tMax = ((n0 ? lx : hx) - o.x) * inv.x;
+  float tyMin = ((n1 ? hy : ly) - o.y) * inv.y;
+  float tyMax = ((n1 ? ly : hy) - o.y) * inv.y;
+  tMax = slab_scale(tMax);
+  tyMax = slab_scale(tyMax);
+  if (tMin > tyMax || tyMin > tMax) return false;
+  if (tyMin > tMin) tMin = tyMin;
+  if (tyMax < tMax) tMax = tyMax;
+  float tzMin = ((n2 ? hz : lz) - o.z) * inv.z;
+  float tzMax = ((n2 ? lz : hz) - o.z) * inv.z;
+  tzMax = slab_scale(tzMax);
+  if (tMin > tzMax || tzMin > tMax) return false;
+  if (tzMin > tMin) tMin = tzMin;
+  if (tzMax < tMax) tMax = tzMax;
+  tmin = tMin;
+  return tMax > 0.0f;
+}
+
+// Möller-Trumbore as the reference writes it. A = s0.xyz, AB = s1.xyz, AC = s2.xyz.
+__device__ __forceinline__ bool tri_test(float4 s0, float4 s1, float4 s2, f3 o, f3 d, float t_min, float t_max,
+                                         float& t, float& alpha, float& beta) {
+  const f3 A = mk3(s0.x, s0.y, s0.z), AB = mk3(s1.x, s1.y, s1.z), AC = mk3(s2.x, s2.y, s2.z);
+  const f3 S1 = cross(d, AC);
+  const float div = dot(S1, AB);
+  if (!div) return false;
+  const float inv_div = 1.0f / div;
+  const f3 AO = o - A;
+  alpha = dot(AO, S1) * inv_div;
+  if (alpha < 0.0f) return false;
+  const f3 S2 = cross(AO, AB);
+  beta = dot(d, S2) * inv_div;
+  if (beta < 0.0f || alpha + beta > 1.0f) return false;
+  t = dot(AC, S2) * inv_div;
+  if (t < t_min || t > t_max) return false;
+  return true;
+}
+
+// Local ray of a TransformedShape: origin by the inverse point transform,
+// direction by the inverse vector transform then the Ray constructor's
+// double normalisation.
+__device__ __forceinline__ void sphere_local(const DSphere& s, f3 o, f3 d, f3& lo, f3& ld) {
+  lo = xform_point(s.inv, o);
+  ld = normalize(xform_vec(s.inv, d));
+}
+
+// sphere::get_abc + the quadratic (src/shape/sphere.cpp:7-47). C widens to
+// double in the reference; for float operands that equals the float
+// difference (an inexact double difference needs an exponent gap > 29 bits,
+// where both roundings give the larger operand).
+__device__ __forceinline__ bool sphere_roots(f3 lo, f3 ld, float radius, float& t0, float& t1) {
+  const float A = len2f(ld);
+  const float B = 2.0f * dot(ld, lo);
+  const float C = len2f(lo) - radius * radius;
+  float delta = B * B - 4.0f * A * C;
+  if (delta < 0.0f) return false;
+  delta = sqrtf(delta);
+  const float inv2A = 0.5f / A;
+  t0 = (-B - delta) * inv2A;
+  t1 = (-B + delta) * inv2A;
+  return true;
+}
+
+template <bool ANY>
+struct Traversal {
+  // Tests one leaf slot. Returns true when ANY and the ray is occluded.
+  static __device__ __forceinline__ bool test_slot(const DScene& sc, int slot, f3 o, f3 d, float t_min,
+                                                   float& t_max, Hit& h) {
+    const float4 s0 = ldg4(sc.slots + 3 * slot);
+    const float4 s1 = ldg4(sc.slots + 3 * slot + 1);
+    const int kind = __float_as_int(s1.w);
+    if (kind < 0) {
+      const float4 s2 = ldg4(sc.slots + 3 * slot + 2);
+      float t, a, b;
+      if (tri_test(s0, s1, s2, o, d, t_min, t_max, t, a, b)) {
+        if (ANY) return true;
+        t_max = t;
+        h.prim = __float_as_int(s0.w);
+        h.t_attr = t;
+        h.alpha = a;
+        h.beta = b;
+      }
+    } else {
+      const DSphere& s = sc.spheres[kind];
+      f3 lo, ld;
+      sphere_local(s, o, d, lo, ld);
+      float t0, t1;
+      if (!sphere_roots(lo, ld, s.radius, t0, t1)) return false;
+      if (ANY) return (t_min <= t0 && t0 <= t_max) || (t_min <= t1 && t1 <= t_max);
+      if (t_max < t0 || t1 < t_min) return false;
+      const bool not_t0 = t0 < t_min;
+      if (not_t0 && t1 > t_max) return false;
+      // Sphere::intersect_p never writes its hit_t argument, so
+      // GeometricPrimitive stores 0 into ray.t_max (src/shape/sphere.cpp:98-119,
+      // src/shape/geometry.cpp:49-57).
+      t_max = 0.0f;
+      h.prim = __float_as_int(s0.w);
+      h.t_attr = not_t0 ? t1 : t0;
+      h.alpha = 0.0f;
+      h.beta = 0.0f;
+    }
+    return false;
+  }
+
+  // Returns true for ANY when occluded; for closest hit fills h and t_max.
+  static __device__ bool run(const DScene& sc, f3 o, f3 d, float t_min, float& t_max, Hit& h, int* err) {
+    h.prim = -1;
+    if (sc.root_kind == 0) return false;
+    // (float)(1.0 / d) in the reference: a single division, so the double
+    // rounding equals the float division.
+    const f3 inv = mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    const bool n0 = inv.x < 0.0f, n1 = inv.y < 0.0f, n2 = inv.z < 0.0f;
+    float tmin;
+    if (!box_pass(sc.root_lo[0], sc.root_lo[1], sc.root_lo[2], sc.root_hi[0], sc.root_hi[1], sc.root_hi[2], o,
+                  inv, n0, n1, n2, tmin) ||
+        !(tmin < t_max))
+      return false;
+    constexpr int kStack = 64;
+    int st_ref[kStack];
+    int st_cnt[kStack];
+    float st_t[kStack];
+    int sp = 0;
+    int cur, cnt;
+    if (sc.root_kind == 2) {
+      cur = sc.root_offset;
+      cnt = sc.root_count;
+    } else {
+      cur = 0;
+      cnt = 0;
+    }
+    for (;;) {
+      if (cnt == 0) {
+        const float4* np = reinterpret_cast<const float4*>(sc.nodes + cur);
+        const float4 a = ldg4(np), b = ldg4(np + 1), c = ldg4(np + 2);
+        const float4 dd = ldg4(np + 3);
+        const int4 di = make_int4(__float_as_int(dd.x), __float_as_int(dd.y), __float_as_int(dd.z),
+                                  __float_as_int(dd.w));
+        float tl, tr;
+        bool hl = box_pass(a.x, a.y, a.z, a.w, b.x, b.y, o, inv, n0, n1, n2, tl) && tl < t_max;
+        bool hr = box_pass(b.z, b.w, c.x, c.y, c.z, c.w, o, inv, n0, n1, n2, tr) && tr < t_max;
+        const int axis = di.w;
+        const bool second_near = axis == 0 ? n0 : (axis == 1 ? n1 : n2);
+        const int lref = di.x, rref = di.y;
+        const int lcnt = di.z & 0xffff, rcnt = (int)((unsigned)di.z >> 16);
+        if (hl && hr) {
+          if (sp >= kStack) {
+            atomicOr(err, 1);
+            return false;
+          }
+          if (second_near) {
+            st_ref[sp] = lref; st_cnt[sp] = lcnt; st_t[sp] = tl; ++sp;
+            cur = rref; cnt = rcnt;
+          } else {
+            st_ref[sp] = rref; st_cnt[sp] = rcnt; st_t[sp] = tr; ++sp;
+            cur = lref; cnt = lcnt;
+          }
+          continue;
+        }
+        if (hl) { cur = lref; cnt = lcnt; continue; }
+        if (hr) { cur = rref; cnt = rcnt; continue; }
+      } else {
+        for (int i = 0; i < cnt; ++i)
+          if (test_slot(sc, cur + i, o, d, t_min, t_max, h)) return true;
+      }
+      bool found = false;
+      while (sp > 0) {
+        --sp;
+        if (st_t[sp] < t_max) {
+          cur = st_ref[sp];
+          cnt = st_cnt[sp];
+          found = true;
+          break;
+        }
+      }
+      if (!found) break;
+    }
+    return false;
+  }
+};
+
+}  // namespace trg

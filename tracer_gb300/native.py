@@ -1,0 +1,194 @@
+"""ctypes binding of libtracer_gb300.so (the C ABI in include/tracer_gpu.h).
+
+Loading fails loudly: there is no CPU fallback. `GpuContext` owns one
+`tr_ctx` (one CUDA device, one stream).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+from .abi import (NODE_DTYPE, RAY_DTYPE, TR_OK, TrBvhNode32, TrCamera, TrFilter, TrRay, TrRenderParams,
+                  TrSceneDesc, TrStats)
+
+_lib = None
+
+
+class TracerError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"tracer_gb300 status {status}: {msg}")
+        self.status = status
+
+
+def lib() -> C.CDLL:
+    """Loads the native library (building it first if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        _build.build()
+    L = C.CDLL(path)
+    vp, sz = C.c_void_p, C.c_size_t
+    st = C.c_int
+    L.tr_status_string.restype = C.c_char_p
+    L.tr_status_string.argtypes = [st]
+    L.tr_make_ray.restype = st
+    L.tr_make_ray.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float, C.c_float, C.POINTER(TrRay)]
+    L.tr_ctx_create.restype = st
+    L.tr_ctx_create.argtypes = [C.POINTER(vp), C.c_int]
+    L.tr_ctx_destroy.restype = None
+    L.tr_ctx_destroy.argtypes = [vp]
+    L.tr_ctx_last_error.restype = C.c_char_p
+    L.tr_ctx_last_error.argtypes = [vp]
+    L.tr_ctx_stream.restype = vp
+    L.tr_ctx_stream.argtypes = [vp]
+    L.tr_synchronize.restype = st
+    L.tr_synchronize.argtypes = [vp]
+    L.tr_scene_upload.restype = st
+    L.tr_scene_upload.argtypes = [vp, C.POINTER(TrSceneDesc)]
+    L.tr_bvh_info.restype = st
+    L.tr_bvh_info.argtypes = [vp, C.POINTER(sz), C.POINTER(sz)]
+    L.tr_bvh_export.restype = st
+    L.tr_bvh_export.argtypes = [vp, C.POINTER(TrBvhNode32), C.POINTER(C.c_uint32)]
+    L.tr_bvh_upload.restype = st
+    L.tr_bvh_upload.argtypes = [vp, C.POINTER(TrBvhNode32), sz, C.POINTER(C.c_uint32), sz]
+    L.tr_trace_closest.restype = st
+    L.tr_trace_closest.argtypes = [vp, C.POINTER(TrRay), sz, C.POINTER(C.c_int32), C.POINTER(C.c_float)]
+    L.tr_trace_any.restype = st
+    L.tr_trace_any.argtypes = [vp, C.POINTER(TrRay), sz, C.POINTER(C.c_uint8)]
+    L.tr_trace_closest_dev.restype = st
+    L.tr_trace_closest_dev.argtypes = [vp, vp, sz, vp, vp]
+    L.tr_trace_any_dev.restype = st
+    L.tr_trace_any_dev.argtypes = [vp, vp, sz, vp]
+    L.tr_render.restype = st
+    L.tr_render.argtypes = [vp, C.POINTER(TrCamera), C.POINTER(TrFilter), C.POINTER(TrRenderParams),
+                            C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(TrStats)]
+    L.tr_render_dev.restype = st
+    L.tr_render_dev.argtypes = [vp, C.POINTER(TrCamera), C.POINTER(TrFilter), C.POINTER(TrRenderParams),
+                                vp, vp, C.POINTER(TrStats)]
+    L.tr_cancel.restype = st
+    L.tr_cancel.argtypes = [vp]
+    L.tr_selftest.restype = st
+    L.tr_selftest.argtypes = [vp, C.c_int, C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64)]
+    _lib = L
+    return L
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class GpuContext:
+    """One tr_ctx on a CUDA device."""
+
+    def __init__(self, device: int = 0):
+        self.L = lib()
+        h = C.c_void_p()
+        s = self.L.tr_ctx_create(C.byref(h), device)
+        if s != TR_OK:
+            raise TracerError(s, "tr_ctx_create failed (no usable CUDA device?)")
+        self.h = h
+        self._keep = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.tr_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, s):
+        if s != TR_OK:
+            raise TracerError(s, self.L.tr_ctx_last_error(self.h).decode())
+
+    @property
+    def stream(self) -> int:
+        return self.L.tr_ctx_stream(self.h)
+
+    def synchronize(self):
+        self._check(self.L.tr_synchronize(self.h))
+
+    def upload(self, scene_buffers):
+        d = scene_buffers.desc()
+        self._keep = (scene_buffers, d)
+        self._check(self.L.tr_scene_upload(self.h, C.byref(d)))
+
+    def bvh(self):
+        nn, npr = C.c_size_t(), C.c_size_t()
+        self._check(self.L.tr_bvh_info(self.h, C.byref(nn), C.byref(npr)))
+        nodes = np.zeros(nn.value, NODE_DTYPE)
+        order = np.zeros(npr.value, np.uint32)
+        self._check(self.L.tr_bvh_export(self.h, _p(nodes, TrBvhNode32), _p(order, C.c_uint32)))
+        return nodes, order
+
+    def upload_bvh(self, nodes, order):
+        nodes = np.ascontiguousarray(nodes, NODE_DTYPE)
+        order = np.ascontiguousarray(order, np.uint32)
+        self._check(self.L.tr_bvh_upload(self.h, _p(nodes, TrBvhNode32), len(nodes), _p(order, C.c_uint32),
+                                         len(order)))
+
+    def trace_closest(self, rays):
+        rays = np.ascontiguousarray(rays, RAY_DTYPE)
+        prim = np.empty(len(rays), np.int32)
+        t = np.empty(len(rays), np.float32)
+        self._check(self.L.tr_trace_closest(self.h, _p(rays, TrRay), len(rays), _p(prim, C.c_int32),
+                                            _p(t, C.c_float)))
+        return prim, t
+
+    def trace_any(self, rays):
+        rays = np.ascontiguousarray(rays, RAY_DTYPE)
+        hit = np.empty(len(rays), np.uint8)
+        self._check(self.L.tr_trace_any(self.h, _p(rays, TrRay), len(rays), _p(hit, C.c_uint8)))
+        return hit
+
+    def trace_closest_dev(self, d_rays: int, n: int, d_prim: int, d_t: int):
+        self._check(self.L.tr_trace_closest_dev(self.h, d_rays, n, d_prim, d_t))
+
+    def trace_any_dev(self, d_rays: int, n: int, d_hit: int):
+        self._check(self.L.tr_trace_any_dev(self.h, d_rays, n, d_hit))
+
+    def render(self, cam: TrCamera, filt: TrFilter, params: TrRenderParams, fp64: bool = False):
+        """Film sums (H, W, 4): r, g, b, weight; plus the run statistics."""
+        W, H = params.width, params.height
+        stats = TrStats()
+        if fp64:
+            out = np.zeros((H, W, 4), np.float64)
+            s = self.L.tr_render(self.h, C.byref(cam), C.byref(filt), C.byref(params), None,
+                                 _p(out, C.c_double), C.byref(stats))
+        else:
+            out = np.zeros((H, W, 4), np.float32)
+            s = self.L.tr_render(self.h, C.byref(cam), C.byref(filt), C.byref(params), _p(out, C.c_float),
+                                 None, C.byref(stats))
+        self._check(s)
+        return out, stats
+
+    def render_dev(self, cam: TrCamera, filt: TrFilter, params: TrRenderParams, d_out: int, fp64: bool = False):
+        stats = TrStats()
+        s = self.L.tr_render_dev(self.h, C.byref(cam), C.byref(filt), C.byref(params),
+                                 None if fp64 else d_out, d_out if fp64 else None, C.byref(stats))
+        self._check(s)
+        return stats
+
+
+def selftest(ctx: "GpuContext", which: int, n: int, seed: int = 1) -> int:
+    bad = C.c_uint64()
+    ctx._check(ctx.L.tr_selftest(ctx.h, which, n, seed, C.byref(bad)))
+    return bad.value
+
+
+def make_ray(o, d, t_min=0.0, t_max=3.4028234663852886e38) -> TrRay:
+    r = TrRay()
+    oa = (C.c_float * 3)(*o)
+    da = (C.c_float * 3)(*d)
+    s = lib().tr_make_ray(oa, da, t_min, t_max, C.byref(r))
+    if s != TR_OK:
+        raise TracerError(s, "tr_make_ray")
+    return r

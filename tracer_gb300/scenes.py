@@ -298,3 +298,64 @@ def random_camera(width, height, seed=0):
     rng = np.random.default_rng(seed + 1000)
     pos = (float(rng.uniform(-1, 1)), float(rng.uniform(0.0, 1.5)), float(4 + rng.uniform(0, 1)))
     return make_camera(width / height, pos, (0, 0, 0), (0, 1, 0), math.radians(45.0), 0.0, 1.0)
+
+
+_MAT_FIELDS = ("ka", "kd", "ks", "ns", "base_color", "subsurface", "metallic", "specular", "specular_tint",
+               "roughness", "anisotropic", "sheen", "sheen_tint", "clearcoat", "clearcoat_gloss")
+
+
+def pack_scene(s: SceneBuffers, prefix: str = "") -> dict:
+    """Flat arrays of a scene (for fixtures)."""
+    mats = []
+    for m in s.materials:
+        row = [float(m.kind)]
+        for f in _MAT_FIELDS:
+            v = getattr(m, f)
+            row.extend(list(v) if isinstance(v, (tuple, list)) else [float(v)])
+        mats.append(row)
+    out = {"positions": s.positions, "normals": s.normals, "uvs": s.uvs, "indices": s.indices,
+           "sphere_radius": s.sphere_radius, "sphere_to_world": s.sphere_to_world,
+           "sphere_to_local": s.sphere_to_local, "materials": np.asarray(mats, np.float32),
+           "prim_shape": s.prim_shape, "prim_material": s.prim_material, "prim_emission": s.prim_emission,
+           "light_prims": s.light_prims, "max_leaf_prims": np.int32(s.max_leaf_prims)}
+    return {prefix + k: np.asarray(v) for k, v in out.items()}
+
+
+def unpack_scene(d, prefix: str = "") -> SceneBuffers:
+    mats = []
+    for row in np.asarray(d[prefix + "materials"], np.float64):
+        m = Material(kind=int(row[0]))
+        i = 1
+        for f in _MAT_FIELDS:
+            if isinstance(getattr(m, f), tuple):
+                setattr(m, f, tuple(float(x) for x in row[i:i + 3]))
+                i += 3
+            else:
+                setattr(m, f, float(row[i]))
+                i += 1
+        mats.append(m)
+    g = lambda k: np.asarray(d[prefix + k])
+    return SceneBuffers(positions=g("positions"), normals=g("normals"), uvs=g("uvs"), indices=g("indices"),
+                        sphere_radius=g("sphere_radius"), sphere_to_world=g("sphere_to_world"),
+                        sphere_to_local=g("sphere_to_local"), materials=mats, prim_shape=g("prim_shape"),
+                        prim_material=g("prim_material"), prim_emission=g("prim_emission"),
+                        light_prims=g("light_prims"), max_leaf_prims=int(g("max_leaf_prims")))
+
+
+def pack_view(cam, filt, par, prefix: str = "") -> dict:
+    return {prefix + "camera": np.array([cam.film_aspect, *cam.pos, *cam.target, *cam.up, cam.fov,
+                                         cam.lens_radius, cam.focal_dist], np.float32),
+            prefix + "filter": np.array([filt.radius, filt.alpha], np.float32),
+            prefix + "params": np.array([par.width, par.height, par.spp, par.min_depth, par.max_depth,
+                                         par.direct_light_sample_num, par.seed_base], np.int64)}
+
+
+def unpack_view(d, prefix: str = ""):
+    c = np.asarray(d[prefix + "camera"], np.float32)
+    cam = make_camera(float(c[0]), tuple(c[1:4]), tuple(c[4:7]), tuple(c[7:10]), float(c[10]), float(c[11]),
+                      float(c[12]))
+    f = np.asarray(d[prefix + "filter"], np.float32)
+    p = np.asarray(d[prefix + "params"], np.int64)
+    par = make_params(int(p[0]), int(p[1]), int(p[2]), int(p[3]), int(p[4]), seed_base=int(p[6]),
+                      direct_light_sample_num=int(p[5]))
+    return cam, make_filter(float(f[0]), float(f[1])), par
