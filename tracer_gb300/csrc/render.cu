@@ -26,8 +26,6 @@
 // on ray results); the contributions are summed back in the reference's
 // order in `logic`. Queues are appended with warp-aggregated atomics.
 
-#include <cooperative_groups.h>
-#include <cooperative_groups/reduce.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -37,8 +35,6 @@
 #include "context.h"
 #include "shade.cuh"
 #include "traverse.cuh"
-
-namespace cg = cooperative_groups;
 
 namespace trg {
 
@@ -89,18 +85,28 @@ struct Launch {
   unsigned long long* stats;  // samples, extend rays, shadow rays, shade items
 };
 
+// Warp-aggregated queue append. The active lanes are grouped by counter
+// address (__match_any_sync): one call site can target different queues per
+// lane (the per-material hit queues), and each group reserves its own range.
 __device__ __forceinline__ int append(unsigned int* ctr) {
-  cg::coalesced_group g = cg::coalesced_threads();
+  const unsigned int active = __activemask();
+  const unsigned int peers = __match_any_sync(active, (unsigned long long)ctr);
+  const int lane = (int)(threadIdx.x & 31u);
+  const int leader = __ffs(peers) - 1;
   unsigned int base = 0;
-  if (g.thread_rank() == 0) base = atomicAdd(ctr, g.size());
-  base = g.shfl(base, 0);
-  return (int)(base + g.thread_rank());
+  if (lane == leader) base = atomicAdd(ctr, (unsigned int)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  return (int)(base + (unsigned int)__popc(peers & ((1u << lane) - 1u)));
 }
 
-__device__ __forceinline__ void count_add(unsigned long long* c, unsigned long long v) {
-  cg::coalesced_group g = cg::coalesced_threads();
-  const unsigned long long s = cg::reduce(g, v, cg::plus<unsigned long long>());
-  if (g.thread_rank() == 0 && s) atomicAdd(c, s);
+// Warp-aggregated add to a 64-bit statistics counter (lanes grouped by
+// address, as in append); per-lane values are per-kernel tallies well below
+// 2^32 / 32.
+__device__ __forceinline__ void count_add(unsigned long long* c, unsigned int v) {
+  const unsigned int active = __activemask();
+  const unsigned int peers = __match_any_sync(active, (unsigned long long)c);
+  const unsigned int s = __reduce_add_sync(peers, v);
+  if ((int)(threadIdx.x & 31u) == __ffs(peers) - 1 && s) atomicAdd(c, (unsigned long long)s);
 }
 
 // Film::Tile::add_sample (src/core/render.hpp:37-57). With radius <= 0.5 a
@@ -162,7 +168,7 @@ __device__ __forceinline__ void film_add(const Launch& P, int slot, float px, fl
 // roulette ends before their first vertex. Returns false when the pixel has
 // no samples left.
 __device__ __forceinline__ bool start_sample(const Launch& P, int slot, unsigned long long& st, int sample,
-                                             int next_q, unsigned long long& finished) {
+                                             int next_q, unsigned int& finished) {
   const int x = slot % P.W, y = slot / P.W;
   while (sample < P.spp) {
     const float fu = Pcg::next(st), fv = Pcg::next(st);
@@ -196,7 +202,7 @@ __device__ __forceinline__ bool start_sample(const Launch& P, int slot, unsigned
 
 // Ends the slot's current sample (film) and starts its next one.
 __device__ void finish_sample(const Launch& P, int slot, unsigned long long& st, f3 L, int nxt,
-                              unsigned long long& finished) {
+                              unsigned int& finished) {
   if (!valid3(L)) L = mk3(0.0f, 0.0f, 0.0f);  // eval_pixel_li returns {} (path_trace_renderer.cpp:204-209)
   const float px = P.P3[slot].w, py = P.P4[slot].w;
   film_add(P, slot, px, py, L);
@@ -207,7 +213,7 @@ __device__ void finish_sample(const Launch& P, int slot, unsigned long long& st,
 
 __global__ void __launch_bounds__(256) k_init(Launch P) {
   const int n = P.W * P.H;
-  unsigned long long finished = 0;
+  unsigned int finished = 0;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
     const int x = s % P.W, y = s / P.W;
     unsigned long long st = Pcg::seed((int)(P.seed_base + (unsigned)y * (unsigned)P.W + (unsigned)x));
@@ -220,7 +226,7 @@ __global__ void __launch_bounds__(256) k_init(Launch P) {
 
 __global__ void __launch_bounds__(128) k_extend(Launch P, int cur) {
   const unsigned int n = P.ctr[C_EXT + cur];
-  unsigned long long nr = 0;
+  unsigned int nr = 0;
   for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int e = P.q_ext[cur][i];
     const int slot = e >> 1;
@@ -240,7 +246,7 @@ __global__ void __launch_bounds__(128) k_extend(Launch P, int cur) {
 
 __global__ void __launch_bounds__(128) k_shadow(Launch P) {
   const unsigned int n = P.ctr[C_SH];
-  unsigned long long nr = 0;
+  unsigned int nr = 0;
   for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int r = P.q_sh[i];
     const float4 a = P.SH[3 * r], b = P.SH[3 * r + 1];
@@ -277,7 +283,7 @@ __global__ void __launch_bounds__(128) k_logic(Launch P, int cur) {
   const int nxt = cur ^ 1;
   const unsigned int n = P.ctr[C_ACT + cur];
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.stats + 3, (unsigned long long)n);
-  unsigned long long finished = 0;
+  unsigned int finished = 0;
   for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int slot = P.q_act[cur][i];
     const float4 p0 = P.P0[slot], p3 = P.P3[slot];
@@ -338,7 +344,7 @@ template <int KIND>
 __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
   const int nxt = cur ^ 1;
   const unsigned int n = P.ctr[C_MAT + KIND];
-  unsigned long long finished = 0;
+  unsigned int finished = 0;
   for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int slot = P.q_mat[KIND][i];
     unsigned long long st = P.rng[slot];
