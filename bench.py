@@ -37,31 +37,68 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 from tracer_gb300 import scenes  # noqa: E402
-from tracer_gb300.abi import TR_RENDER_TIME_STAGES  # noqa: E402
+from tracer_gb300.abi import (STAGE_NAMES, TR_RENDER_COUNT_VISITS, TR_RENDER_TIME_STAGES,  # noqa: E402
+                              TrCamera, TrFilter, TrRenderParams)
+import ctypes  # noqa: E402
 
 METRIC = "Msamples/s (plain GPU path tracing)"
 UNIT = "Msamples/s"
 
-# Bytes each stage must move per work item through HBM (the SoA path state,
-# queues and shadow records of render.cu; scene data is read-only and stays in
-# cache): the roofline numerator. nl = number of lights.
-def stage_bytes(stage: str, nl: int) -> int:
-    if stage == "shade":
-        # reads: P0-P3 64, rng 8, hit 16, P4 16, shadow contributions 16*nl, MIS hit+state 64
-        # writes: P0-P4 80, rng 8, MIS state 48, shadow records 48*nl, queue entries 4*(3+nl)
-        return 168 + 16 * nl + 148 + 52 * nl
+# Algorithmic bytes per work item of each kernel (the roofline numerator).
+# Traversal kernels (per ray): 32 B per box tested (the reference's
+# LinearBVHNode) + 48 B per primitive tested (3 indices + 3 vertices) + the
+# 32-B ray + its result (8 B: prim id and t; 1 B for an occlusion flag).
+# Shading kernels (per item): the path-state words each one reads and writes
+# (float4 SoA records and queue entries of render.cu); scene tables are
+# read-only and cache-resident.
+def kernel_bytes(stage: str, nl: int, boxes_per_ray=0.0, prims_per_ray=0.0) -> float:
     if stage == "extend":
-        return 4 + 32 + 16  # queue entry, ray, hit record
-    return 4 + 32 + 4  # shadow: queue entry, ray record, occlusion flag
+        return 32 * boxes_per_ray + 48 * prims_per_ray + 32 + 8
+    if stage == "shadow":
+        return 32 * boxes_per_ray + 48 * prims_per_ray + 32 + 1
+    if stage == "logic":
+        # queue 4, P0 16, P3 16, HC 16, P4 16, shadow contributions 16*nl, MIS (HM, M0-M2) 64,
+        # writes P3 16 + queue 4; finishing samples also write the film (16) and P0-P4 (80)
+        return 4 + 16 + 16 + 16 + 16 + 16 * nl + 64 + 16 + 4
+    if stage.startswith("material"):
+        # queue 4, rng 8 r/w, P0-P2 48, HC 16, P3 16; writes NU 8*nl + queue 4*nl, SC 112,
+        # M0-M2 48 + queue 4, P4 16, P0-P2 48, queue 8
+        return 4 + 16 + 48 + 16 + 16 + 12 * nl + 112 + 52 + 16 + 48 + 8
+    if stage.startswith("nee"):
+        # queue 4, SC 112, NU 8, P4 16; writes shadow record 48 + queue 4
+        return 4 + 112 + 8 + 16 + 48 + 4
+    return 0.0
 
 
-def workload(name: str):
+KERNEL_NAMES = {"extend": "k_extend", "logic": "k_logic", "material_phong": "k_material<0>",
+                "material_disney": "k_material<1>", "nee_phong": "k_nee<0>", "nee_disney": "k_nee<1>",
+                "shadow": "k_shadow"}
+
+
+def traffic_per_unit(stage: str):
+    """DRAM bytes per work item of a kernel from a committed ncu summary, or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
+            return json.load(f).get(stage)
+    except (OSError, ValueError):
+        return None
+
+
+def workload(name: str, size: str | None = None):
+    """(label, scene, camera, filter, params); size "WxHxSPP" overrides the
+    film and sample count (small cases for profiler captures)."""
     if name == "cornell":
-        sc, cam, filt, par = scenes.cornell(256, 256, 16)
-        label = "cornell_box_36tris_256x256_16spp_depth5"
+        W, H, S = 256, 256, 16
     else:
-        sc, cam, filt, par = scenes.disney_grid(1024, 1024, 64, max_depth=8, min_depth=5)
-        label = "disney12_sphere_grid_16x16_1024x1024_64spp_depth8"
+        W, H, S = 1024, 1024, 64
+    if size:
+        W, H, S = (int(v) for v in size.lower().split("x"))
+    if name == "cornell":
+        sc, cam, filt, par = scenes.cornell(W, H, S)
+        label = f"cornell_box_36tris_{W}x{H}_{S}spp_depth5"
+    else:
+        sc, cam, filt, par = scenes.disney_grid(W, H, S, max_depth=8, min_depth=5)
+        label = f"disney12_sphere_grid_16x16_{W}x{H}_{S}spp_depth8"
     return label, sc, cam, filt, par
 
 
@@ -85,6 +122,9 @@ class ClockSampler:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.perf_counter()
+            while not self.lines and time.perf_counter() - t0 < 5.0:  # NVML up
+                time.sleep(0.05)
         except OSError:
             self.proc = None
         return self
@@ -92,6 +132,10 @@ class ClockSampler:
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+
+    def mark(self) -> int:
+        """Index of the next sample (bracket a region with two marks)."""
+        return len(self.lines)
 
     def __exit__(self, *a):
         if self.proc:
@@ -101,10 +145,10 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
-    def summary(self):
+    def summary(self, lo: int = 0, hi: int | None = None):
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in self.lines[lo:hi]:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) != len(self.FIELDS):
                 continue
@@ -166,7 +210,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    label, sc, cam, filt, par = workload(args.workload)
+    label, sc, cam, filt, par = workload(args.workload, args.size)
     import oracle
     threads = usable_cores()
     orc = oracle.Oracle(sc, "port", threads=threads)
@@ -209,7 +253,7 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group(backend="nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
-    label, sc, cam, filt, par = workload(args.workload)
+    label, sc, cam, filt, par = workload(args.workload, args.size)
     ctx = GpuContext(local)
     ctx.upload(sc)
     nl = len(sc.light_prims)
@@ -224,22 +268,27 @@ def run_ours(args):
         if dist is not None:
             dist.barrier()
 
-    par.flags = TR_RENDER_TIME_STAGES  # also in warm-up: allocates the timing events
+    # The clock sampler starts before the warm-up: its first NVML query
+    # stalls the device, which must not fall into the timed region.
+    clocks = ClockSampler(local).__enter__()
+    par.flags = 0
     for _ in range(args.warmup):
         ctx.render_dev(cam, filt, par, film.data_ptr())
     stats = []
     barrier()
-    with ClockSampler(local) as clocks:
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for k in range(args.steps):
-            if k:
-                with torch.cuda.stream(stream):
-                    flush.zero_()
-            stats.append(ctx.render_dev(cam, filt, par, film.data_ptr()))
-        e1.record(stream)
-        barrier()
+    c0 = clocks.mark()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(args.steps):
+        if k:
+            with torch.cuda.stream(stream):
+                flush.zero_()
+        stats.append(ctx.render_dev(cam, filt, par, film.data_ptr()))
+    e1.record(stream)
+    barrier()
+    c1 = clocks.mark()
+    clocks.__exit__()
     ms = e0.elapsed_time(e1)
     if dist is not None:
         t = torch.tensor([ms], device=f"cuda:{local}")
@@ -248,9 +297,9 @@ def run_ours(args):
     samples = sum(s.samples for s in stats)
     value = world * samples / (ms / 1e3) / 1e6
 
-    # end to end through the host-buffer C ABI call (film copied back each step)
-    par.flags = 0
-    host_film = np.zeros((H, W, 4), np.float32)
+    # end to end through the host-buffer C ABI call: per step the camera,
+    # filter and parameters go in (the scene stays resident, as a reference
+    # Scene outlives its renders) and the film comes back
     barrier()
     t0 = time.perf_counter()
     e2e_samples = 0
@@ -264,7 +313,16 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e = world * e2e_samples / e2e_s / 1e6
-    del host_film
+    h2d = ctypes.sizeof(TrCamera) + ctypes.sizeof(TrFilter) + ctypes.sizeof(TrRenderParams)
+
+    # after the timed region: one step with CUDA events around every kernel,
+    # one with the traversal counting boxes and primitives tested
+    par.flags = TR_RENDER_TIME_STAGES
+    ctx.render_dev(cam, filt, par, film.data_ptr())  # creates the event pool
+    staged = ctx.render_dev(cam, filt, par, film.data_ptr())
+    par.flags = TR_RENDER_COUNT_VISITS
+    counted = ctx.render_dev(cam, filt, par, film.data_ptr())
+    par.flags = 0
 
     if rank != 0:
         ctx.close()
@@ -272,20 +330,38 @@ def run_ours(args):
             dist.destroy_process_group()
         return 0
 
-    # roofline of the dominant stage, from the timed steps' own CUDA events
-    names = ["extend", "shade", "shadow"]
-    stage_ms = [sum(s.stage_ms[i] for s in stats) for i in range(3)]
-    items = [sum(s.extend_rays for s in stats), sum(s.shade_items for s in stats),
-             sum(s.shadow_rays for s in stats)]
-    launches = sum(s.iterations for s in stats)
-    dom = int(np.argmax(stage_ms))
-    per_launch_bytes = stage_bytes(names[dom], nl) * items[dom] / max(launches, 1)
-    per_launch_s = stage_ms[dom] / 1e3 / max(launches, 1)
-    achieved = per_launch_bytes / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
+    # roofline of the dominant kernel, from the stage-timed step's CUDA events
+    stage_ms = dict(zip(STAGE_NAMES, staged.stage_ms))
+    iters = staged.iterations
+    items = {"extend": staged.extend_rays, "shadow": staged.shadow_rays, "logic": staged.shade_items}
+    kernels = [k for k in STAGE_NAMES if k != "reset" and stage_ms[k] > 0]
+    dom = max(kernels, key=lambda k: stage_ms[k])
+    per = {}
+    if staged.extend_rays:
+        per["extend"] = (counted.closest_boxes / counted.extend_rays, counted.closest_prims / counted.extend_rays)
+    if staged.shadow_rays:
+        per["shadow"] = (counted.any_boxes / counted.shadow_rays, counted.any_prims / counted.shadow_rays)
+    bpr = kernel_bytes(dom, nl, *per.get(dom, (0.0, 0.0)))
+    dom_items = items.get(dom)
     peak, peak_kind = measured_peak_hbm()
+    roof = {"bound": "hbm", "kernel": KERNEL_NAMES[dom], "unit": "GB/s", "peak": peak,
+            "peak_source": f"{peak_kind} HBM copy bandwidth (hbm_gbs)", "traffic": None,
+            "launches": iters, "avg_launch_ms": stage_ms[dom] / max(iters, 1)}
+    if dom_items:
+        per_launch_bytes = bpr * dom_items / max(iters, 1)
+        achieved = per_launch_bytes / (roof["avg_launch_ms"] / 1e3) / 1e9
+        roof.update({"achieved": achieved, "frac": achieved / peak, "bytes_per_unit": bpr,
+                     "units_per_launch": dom_items / max(iters, 1)})
+        tr = traffic_per_unit(dom)
+        if tr is not None:
+            roof["traffic"] = tr["bytes_per_unit"] * dom_items / max(iters, 1)
+            roof["traffic_source"] = tr["source"]
+    else:
+        roof.update({"achieved": None, "frac": None})
     cpu_rate, cpu_threads, cpu_desc = (None, None, None)
     if not args.no_cpu_baseline and world == 1:
         cpu_rate, cpu_threads, cpu_desc = cpu_sample(sc, cam, filt, par)
+    rays = staged.extend_rays + staged.shadow_rays
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -293,18 +369,19 @@ def run_ours(args):
         "config": {"workload": label, "width": W, "height": H, "spp": par.spp, "max_depth": par.max_depth,
                    "min_depth": par.min_depth, "lights": nl, "primitives": int(len(sc.prim_shape)),
                    "parallelism": f"replicas x{world}",
-                   "l2": "path state and queues (~450 MB at 1024x1024) exceed L2; 256 MiB buffer "
+                   "l2": "path state and queues exceed L2 (~450 MB at 1024x1024); a 256 MiB buffer is "
                          "written between timed steps"},
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 100, "d2h_bytes_per_step": W * H * 16},
-        "gpu_launches": int(sum(1 + 3 * s.iterations for s in stats)),
-        "roofline": {"bound": "hbm", "kernel": "k_" + names[dom], "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                     "bytes_per_item": stage_bytes(names[dom], nl),
-                     "stage_ms": dict(zip(names, stage_ms)), "stage_items": dict(zip(names, items))},
-        "rays": {"extend": items[0], "shadow": items[2],
-                 "mrays_per_s": (items[0] + items[2]) / (ms / 1e3) / 1e6},
-        "clocks": clocks.summary(),
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": W * H * 16},
+        "gpu_launches": int(sum(1 + 7 * s.iterations for s in stats)),
+        "roofline": roof,
+        "rays": {"extend": staged.extend_rays, "shadow": staged.shadow_rays,
+                 "mrays_per_s": rays / (ms / args.steps / 1e3) / 1e6,
+                 "boxes_per_extend_ray": per.get("extend", (None, None))[0],
+                 "prims_per_extend_ray": per.get("extend", (None, None))[1],
+                 "boxes_per_shadow_ray": per.get("shadow", (None, None))[0],
+                 "prims_per_shadow_ray": per.get("shadow", (None, None))[1]},
+        "stage_ms": {k: round(v, 3) for k, v in stage_ms.items()},
+        "clocks": clocks.summary(c0, c1),
     }
     if cpu_rate is not None:
         line["cpu_baseline"] = {"value": cpu_rate, "unit": UNIT, "cores": cpu_threads, "kind": "port",
@@ -323,6 +400,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["disney_grid", "cornell"], default="disney_grid")
+    ap.add_argument("--size", default=None, help="WxHxSPP override (profiling captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":

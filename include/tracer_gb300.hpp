@@ -1,0 +1,289 @@
+// tracer_gb300.hpp -- C++ host API of the GB300 path tracer.
+//
+// The scene-building and renderer interface of Tracer (reference
+// src/factory/*.hpp, src/core/renderer.hpp, src/core/scene.hpp), kept name
+// for name and argument for argument for the parts the path-tracing hot path
+// uses, so a program written against the reference's factories builds its
+// scene the same way and selects the GPU renderer with
+// create_gpu_pt_renderer beside the reference's create_pt_renderer
+// (src/factory/renderer.hpp:12-21).
+//
+// Underneath, every object records the flat description the C ABI
+// (tracer_gpu.h) uploads: world-space triangle and sphere tables, materials,
+// emissive primitives and the light list. Construction errors throw, as in
+// the reference (src/shape/sphere.cpp:88-90); render errors throw TracerError
+// carrying the C ABI's status.
+//
+// Constant textures only (create_constant_texture2d); the vacuum medium only.
+#pragma once
+
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "tracer_gpu.h"
+
+namespace tracer {
+
+using real = float;
+template <class T>
+using RC = std::shared_ptr<T>;
+template <class T>
+using Box = std::unique_ptr<T>;
+template <class T>
+using Span = std::vector<T>;
+
+class TracerError : public std::runtime_error {
+ public:
+  TracerError(tr_status s, const std::string& what) : std::runtime_error(what), status(s) {}
+  tr_status status;
+};
+
+// ---- values (src/core/spectrum.hpp, src/utility/geometry.hpp) ----
+
+struct Spectrum {
+  real r = 0, g = 0, b = 0;
+  Spectrum() = default;
+  explicit Spectrum(real v) : r(v), g(v), b(v) {}
+  Spectrum(real r_, real g_, real b_) : r(r_), g(g_), b(b_) {}
+  bool is_black() const { return r == 0 && g == 0 && b == 0; }
+  explicit operator bool() const { return !is_black(); }
+};
+
+struct Point2f {
+  real x = 0, y = 0;
+};
+struct Point2i {
+  int x = 0, y = 0;
+};
+struct Point3f {
+  real x = 0, y = 0, z = 0;
+};
+struct Vector3f {
+  real x = 0, y = 0, z = 0;
+};
+struct Normal3f {
+  real x = 0, y = 0, z = 0;
+};
+
+// ---- transforms (src/utility/transform.hpp, transform.cpp) ----
+
+struct Matrix4x4 {
+  real m[4][4];
+  Matrix4x4();  // identity
+  Matrix4x4(real t00, real t01, real t02, real t03, real t10, real t11, real t12, real t13, real t20, real t21,
+            real t22, real t23, real t30, real t31, real t32, real t33);
+  static Matrix4x4 mul(const Matrix4x4& a, const Matrix4x4& b);
+};
+Matrix4x4 transpose(const Matrix4x4& m);
+Matrix4x4 inverse(const Matrix4x4& m);  // throws std::runtime_error when singular
+
+class Transform {
+ public:
+  Transform() = default;
+  explicit Transform(const Matrix4x4& m);
+  Transform(const Matrix4x4& m, const Matrix4x4& inv_m) : m_(m), inv_(inv_m) {}
+  Point3f operator()(const Point3f& p) const;
+  Vector3f operator()(const Vector3f& v) const;
+  Normal3f operator()(const Normal3f& n) const;  // by the inverse transpose
+  const Matrix4x4& matrix() const { return m_; }
+  const Matrix4x4& inverse_matrix() const { return inv_; }
+  friend Transform inverse(const Transform& t) { return Transform(t.inv_, t.m_); }
+  friend Transform operator*(const Transform& a, const Transform& b);
+
+ private:
+  Matrix4x4 m_, inv_;
+};
+Transform translate(const Vector3f& delta);
+Transform scale(real x, real y, real z);
+Transform rotate_x(real theta);  // radians
+Transform rotate_y(real theta);
+Transform rotate_z(real theta);
+
+// ---- meshes (src/utility/mesh_load.hpp:15-89) ----
+
+struct vertex_t {
+  Point3f pos;
+  Normal3f n;
+  Point2f uv;
+};
+struct mesh_t {
+  std::string name;
+  std::vector<vertex_t> vertices;
+  std::vector<int> indices;
+  std::vector<int> materials;
+};
+
+// ---- scene objects ----
+
+class Texture2D {
+ public:
+  virtual ~Texture2D() = default;
+  virtual Spectrum evaluate(const Point2f& uv) const = 0;
+  real evaluate_s(const Point2f& uv) const { return evaluate(uv).r; }  // core/texture.hpp:74-83
+};
+RC<Texture2D> create_constant_texture2d(const Spectrum& constant);
+
+class Shape {
+ public:
+  virtual ~Shape() = default;
+};
+RC<Shape> create_sphere(real radius, const Transform& local_to_world);
+std::vector<RC<Shape>> create_triangle_mesh(const mesh_t& mesh, const Transform& local_to_world);
+
+class Material {
+ public:
+  explicit Material(const tr_material& m) : rec(m) {}
+  tr_material rec;
+};
+RC<Material> create_phong_material(RC<const Texture2D> map_ka, RC<const Texture2D> map_kd,
+                                   RC<const Texture2D> map_ks, RC<const Texture2D> map_ns);
+RC<Material> create_disney_brdf(RC<const Texture2D> base_color, RC<const Texture2D> subsurface,
+                                RC<const Texture2D> metallic, RC<const Texture2D> specular,
+                                RC<const Texture2D> specular_tint, RC<const Texture2D> roughness,
+                                RC<const Texture2D> anisotropic, RC<const Texture2D> sheen,
+                                RC<const Texture2D> sheen_tint, RC<const Texture2D> clearcoat,
+                                RC<const Texture2D> clearcoat_gloss);
+
+class Medium {
+ public:
+  virtual ~Medium() = default;
+};
+RC<Medium> create_vacuum();
+struct MediumInterface {
+  MediumInterface() = default;
+  explicit MediumInterface(RC<const Medium> m) : inside(m), outside(m) {}
+  MediumInterface(RC<const Medium> in, RC<const Medium> out) : inside(std::move(in)), outside(std::move(out)) {}
+  RC<const Medium> inside, outside;
+};
+
+class Light {
+ public:
+  virtual ~Light() = default;
+};
+class AreaLight : public Light {};
+
+class Primitive {
+ public:
+  virtual ~Primitive() = default;
+  virtual const AreaLight* as_area_light() const noexcept = 0;
+};
+RC<Primitive> create_geometric_primitive(const RC<Shape>& shape, const RC<Material>& material,
+                                         const MediumInterface& mi, const Spectrum& emission);
+
+class Aggregate {
+ public:
+  virtual ~Aggregate() = default;
+  virtual void build(std::vector<RC<Primitive>> primitives) = 0;
+};
+RC<Aggregate> create_bvh_accel(int max_leaf_primitives);
+
+class Camera {
+ public:
+  explicit Camera(const tr_camera& c) : rec(c) {}
+  tr_camera rec;
+};
+RC<Camera> create_thin_lens_camera(real film_aspect, const Point3f& cam_pos, const Point3f& target,
+                                   const Vector3f& up, real fov, real lens_radius, real focal_dist);
+
+class Filter {
+ public:
+  explicit Filter(const tr_filter& f) : rec(f) {}
+  real radius() const { return rec.radius; }
+  tr_filter rec;
+};
+RC<Filter> create_gaussin_filter(real radius, real alpha);
+
+// Flat scene as uploaded (owned arrays; tr_scene_desc points into them).
+struct SceneDesc {
+  std::vector<float> positions, normals, uvs;
+  std::vector<int32_t> indices;
+  std::vector<float> sphere_radius, sphere_to_world, sphere_to_local;
+  std::vector<tr_material> materials;
+  std::vector<int32_t> prim_shape, prim_material;
+  std::vector<float> prim_emission;
+  std::vector<int32_t> light_prims;
+  int32_t max_leaf_prims = 1;
+  tr_scene_desc view() const;
+};
+
+class Scene {
+ public:
+  virtual ~Scene() = default;
+  virtual void set_camera(RC<const Camera> camera) = 0;
+  virtual RC<const Camera> get_camera() const noexcept = 0;
+  virtual void prepare_to_render() = 0;
+  Span<const Light*> lights;
+  // GPU-path additions: the description prepare_to_render() assembled and a
+  // counter that changes whenever it is rebuilt.
+  virtual const SceneDesc& desc() const = 0;
+  virtual uint64_t revision() const noexcept = 0;
+};
+RC<Scene> create_general_scene(const RC<Aggregate>& accel);
+
+// ---- film and renderers (src/core/render.hpp, src/core/renderer.hpp) ----
+
+template <class T>
+class Image2D {
+ public:
+  Image2D() = default;
+  Image2D(int w, int h) : w_(w), h_(h), data_((size_t)w * h) {}
+  int width() const { return w_; }
+  int height() const { return h_; }
+  T& at(int x, int y) { return data_[(size_t)y * w_ + x]; }
+  const T& at(int x, int y) const { return data_[(size_t)y * w_ + x]; }
+  T* get_data() { return data_.data(); }
+
+ private:
+  int w_ = 0, h_ = 0;
+  std::vector<T> data_;
+};
+
+struct RenderTarget {
+  Image2D<Spectrum> color;
+};
+
+class Film {
+ public:
+  Film(const Point2i& res, const RC<Filter>& filter) : resolution(res), filter(filter) {}
+  int width() const { return resolution.x; }
+  int height() const { return resolution.y; }
+  const RC<Filter>& get_filter() const { return filter; }
+
+ private:
+  Point2i resolution;
+  RC<Filter> filter;
+};
+
+class Renderer {
+ public:
+  virtual ~Renderer() = default;
+  virtual RenderTarget render(const Scene& scene, Film film) = 0;
+};
+
+// PTRendererParams (src/factory/renderer.hpp:12-19) for the GPU: the device
+// replaces worker_count/task_tile_size; seed_base fixes the per-pixel pcg32
+// seeds ((int32)(seed_base + y * width + x)).
+struct GPUPTRendererParams {
+  int device = 0;
+  int spp = 1;
+  int min_depth = 3;
+  int max_depth = 10;
+  int direct_light_sample_num = 1;
+  uint32_t seed_base = 0;
+  bool fp64_film = false;  // accumulate the film sums in double
+};
+
+// The GPU renderer; render() returns sum / weight per pixel like
+// Film::write_render_target (src/core/render.hpp:104-115). The raw sums of
+// the last render and its statistics stay readable for checks.
+class GpuPathTraceRenderer : public Renderer {
+ public:
+  virtual const std::vector<double>& film_sums() const = 0;  // W*H*4: r, g, b, weight
+  virtual tr_stats last_stats() const = 0;
+};
+RC<GpuPathTraceRenderer> create_gpu_pt_renderer(const GPUPTRendererParams& params);
+
+}  // namespace tracer

@@ -131,10 +131,26 @@ typedef struct tr_render_params {
   int32_t max_depth;
   int32_t direct_light_sample_num; /* must be 1 on the GPU path */
   uint32_t seed_base;
-  uint32_t flags; /* TR_RENDER_TIME_STAGES: per-stage CUDA-event timing into tr_stats */
+  uint32_t flags; /* TR_RENDER_* bits below */
 } tr_render_params;
 
-enum { TR_RENDER_TIME_STAGES = 1 };
+enum {
+  TR_RENDER_TIME_STAGES = 1,  /* CUDA events around every kernel of every iteration -> stage_ms */
+  TR_RENDER_COUNT_VISITS = 2, /* traversal counts boxes and primitives tested -> *_boxes, *_prims */
+};
+
+/* Indices of tr_stats.stage_ms: one per kernel of a wavefront iteration. */
+enum {
+  TR_STAGE_EXTEND = 0,          /* closest hit of continuation and MIS rays */
+  TR_STAGE_LOGIC = 1,           /* direct-light resolve, film, sample restart, routing */
+  TR_STAGE_MATERIAL_PHONG = 2,  /* BSDF sample and next rays, Phong/Lambert vertices */
+  TR_STAGE_MATERIAL_DISNEY = 3, /* same, Disney12 vertices */
+  TR_STAGE_NEE_PHONG = 4,       /* light sample + BSDF eval/pdf per (vertex, light), Phong */
+  TR_STAGE_NEE_DISNEY = 5,      /* same, Disney12 */
+  TR_STAGE_SHADOW = 6,          /* any hit of shadow rays */
+  TR_STAGE_RESET = 7,           /* queue-counter resets */
+  TR_NUM_STAGES = 8
+};
 
 typedef struct tr_stats {
   uint64_t samples;      /* camera samples finished */
@@ -143,7 +159,11 @@ typedef struct tr_stats {
   uint64_t shade_items;  /* path vertices processed by the shade stage */
   uint64_t iterations;   /* wavefront iterations run */
   double device_ms;      /* device time of the render, CUDA events */
-  double stage_ms[3];    /* extend, shade, shadow kernels (with TR_RENDER_TIME_STAGES) */
+  double stage_ms[8];    /* per kernel, TR_STAGE_* order (with TR_RENDER_TIME_STAGES) */
+  uint64_t closest_boxes; /* with TR_RENDER_COUNT_VISITS: boxes tested by closest-hit rays */
+  uint64_t closest_prims; /*   primitives tested by closest-hit rays */
+  uint64_t any_boxes;     /*   boxes tested by shadow rays */
+  uint64_t any_prims;     /*   primitives tested by shadow rays */
 } tr_stats;
 
 const char* tr_status_string(tr_status s);

@@ -1,0 +1,121 @@
+"""The C++ factory API (include/tracer_gb300.hpp): a program builds the
+Cornell box the way a Tracer program does (create_triangle_mesh,
+create_geometric_primitive, create_bvh_accel, create_general_scene, ...) and
+renders it with create_gpu_pt_renderer. The recorded scene description is
+checked on the CPU; the GPU render is compared with the oracle on that same
+description."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from tracer_gb300 import build
+from tracer_gb300.abi import SceneBuffers, TrCamera, TrMaterial, make_filter, make_params
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SRC = os.path.join(ROOT, "tests", "cpp", "cornell_host.cpp")
+
+
+class _Raw:
+    """Materials passed through unchanged as tr_material records."""
+
+    def __init__(self, rec):
+        self.rec = rec
+
+    def to_c(self):
+        return self.rec
+
+
+@pytest.fixture(scope="module")
+def program(tmp_path_factory):
+    so = build.build()
+    out = str(tmp_path_factory.mktemp("host") / "cornell_host")
+    libdir = os.path.dirname(so)
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", f"-I{os.path.join(ROOT, 'include')}", SRC,
+                    f"-L{libdir}", "-ltracer_gb300", f"-Wl,-rpath,{libdir}", "-o", out], check=True)
+    return out
+
+
+def _read_desc(path):
+    with open(path, "rb") as f:
+        buf = f.read()
+    off = 0
+
+    def take(dtype, cols=None):
+        nonlocal off
+        n = int(np.frombuffer(buf, np.uint64, 1, off)[0])
+        off += 8
+        if dtype == "mat":
+            recs = [TrMaterial.from_buffer_copy(buf, off + i * ctypes.sizeof(TrMaterial)) for i in range(n)]
+            off += n * ctypes.sizeof(TrMaterial)
+            return recs
+        a = np.frombuffer(buf, dtype, n, off).copy()
+        off += n * np.dtype(dtype).itemsize
+        return a.reshape(-1, cols) if cols else a
+
+    pos, nrm, uv, idx = take(np.float32, 3), take(np.float32, 3), take(np.float32, 2), take(np.int32, 3)
+    sr, sw, sl = take(np.float32), take(np.float32, 16), take(np.float32, 16)
+    mats = take("mat")
+    ps, pm, pe, lp = take(np.int32), take(np.int32), take(np.float32, 3), take(np.int32)
+    max_leaf = int(np.frombuffer(buf, np.int32, 1, off)[0])
+    off += 4
+    cam = TrCamera.from_buffer_copy(buf, off)
+    sb = SceneBuffers(positions=pos, normals=nrm, uvs=uv, indices=idx, sphere_radius=sr, sphere_to_world=sw,
+                      sphere_to_local=sl, materials=[_Raw(m) for m in mats], prim_shape=ps, prim_material=pm,
+                      prim_emission=pe, light_prims=lp, max_leaf_prims=max_leaf)
+    return sb, cam
+
+
+def test_factory_scene_description(program, tmp_path):
+    out = str(tmp_path / "c")
+    r = subprocess.run([program, out, "32", "32", "2"], check=True, capture_output=True, text=True)
+    assert "36 triangles, 2 lights, 3 materials" in r.stdout
+    sb, cam = _read_desc(out + ".desc")
+    assert sb.indices.shape == (36, 3) and len(sb.light_prims) == 2
+    assert np.array_equal(sb.prim_shape, np.arange(36))
+    # emissive primitives are exactly the scene's lights, in order
+    assert np.array_equal(np.nonzero(sb.prim_emission.any(1))[0], sb.light_prims)
+    # normals are fixed points of the reference normalize (settled as in a render)
+    from tracer_gb300.scenes import ref_normalize
+    assert np.array_equal(ref_normalize(sb.normals).view(np.uint32), sb.normals.view(np.uint32))
+    # every triangle's cross(B - A, C - A) agrees with its shading normal
+    p = sb.positions[sb.indices]
+    g = np.cross(p[:, 1] - p[:, 0], p[:, 2] - p[:, 0])
+    assert (np.einsum("ij,ij->i", g, sb.normals[sb.indices[:, 0]]) > 0).all()
+    # the rotated boxes: translate * rotate_y * scale of the unit cube
+    box1 = sb.positions[sb.indices[10:22].ravel()]
+    assert np.allclose(box1.mean(0), [-0.35, -0.7, -0.3], atol=1e-6)
+    assert np.allclose(np.linalg.norm(box1 - box1.mean(0), axis=1), np.sqrt(3 * 0.3 ** 2), atol=1e-6)
+    # the oracle accepts the description
+    orc = oracle.Oracle(sb, "port")
+    nodes, order = orc.bvh()
+    assert len(order) == 36 and len(nodes) > 0
+    assert abs(cam.film_aspect - 1.0) < 1e-7
+
+
+@pytest.mark.gpu
+def test_factory_scene_renders_like_the_oracle(program, tmp_path):
+    W, H, S = 48, 40, 4
+    out = str(tmp_path / "c")
+    r = subprocess.run([program, out, str(W), str(H), str(S), "render"], check=True, capture_output=True,
+                       text=True)
+    assert f"{W * H * S} samples" in r.stdout
+    sb, cam = _read_desc(out + ".desc")
+    sums = np.fromfile(out + ".sums", np.float64).reshape(H, W, 4)
+    rgb = np.fromfile(out + ".rgb", np.float32).reshape(H, W, 3)
+    orc = oracle.Oracle(sb, "port")
+    orc.set_camera(cam, make_filter(0.5, 0.6))
+    ref = orc.render(make_params(W, H, S, 5, 5)).astype(np.float64)
+    a = sums[..., :3] / sums[..., 3:4]
+    b = ref[..., :3] / ref[..., 3:4]
+    rel = np.abs(a - b) / np.maximum(np.abs(b), 1e-6)
+    close = (rel.max(-1) <= 1e-5).mean()
+    mre = float(np.mean(np.abs(a - b) / np.maximum(np.abs(b), 1e-3)))
+    print(f"pixels within 1e-5: {close:.4f}  MRE {mre:.2e}")
+    assert close >= 0.9 and mre < 0.01
+    # RenderTarget = sum / weight (Film::write_render_target)
+    want = (sums[..., :3].astype(np.float32) / sums[..., 3:4].astype(np.float32))
+    assert np.array_equal(rgb, want)

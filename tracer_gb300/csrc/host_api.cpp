@@ -1,0 +1,504 @@
+// host_api.cpp -- the C++ scene/factory/renderer API of tracer_gb300.hpp.
+//
+// Objects record the flat scene description; create_gpu_pt_renderer's
+// render() uploads it through the C ABI and renders on the GPU. Transform
+// arithmetic is the reference's float arithmetic in the same operation order
+// (src/utility/transform.hpp:70-96, transform.cpp:127-177), so world-space
+// vertices equal the ones the reference's create_triangle_mesh stores
+// (src/shape/triangle.cpp:216-236).
+
+#include <cmath>
+#include <cstring>
+#include <unordered_map>
+#include <utility>
+
+#include "tracer_gb300.hpp"
+
+namespace tracer {
+
+// ---------------------------------------------------------------- transforms
+
+Matrix4x4::Matrix4x4() {
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) m[i][j] = i == j ? 1.0f : 0.0f;
+}
+
+Matrix4x4::Matrix4x4(real t00, real t01, real t02, real t03, real t10, real t11, real t12, real t13, real t20,
+                     real t21, real t22, real t23, real t30, real t31, real t32, real t33) {
+  const real v[16] = {t00, t01, t02, t03, t10, t11, t12, t13, t20, t21, t22, t23, t30, t31, t32, t33};
+  std::memcpy(m, v, sizeof(v));
+}
+
+Matrix4x4 Matrix4x4::mul(const Matrix4x4& a, const Matrix4x4& b) {
+  Matrix4x4 r;
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j)
+      r.m[i][j] = a.m[i][0] * b.m[0][j] + a.m[i][1] * b.m[1][j] + a.m[i][2] * b.m[2][j] + a.m[i][3] * b.m[3][j];
+  return r;
+}
+
+Matrix4x4 transpose(const Matrix4x4& a) {
+  Matrix4x4 r;
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) r.m[i][j] = a.m[j][i];
+  return r;
+}
+
+// Gauss-Jordan elimination with partial pivoting, in double.
+Matrix4x4 inverse(const Matrix4x4& a) {
+  double w[4][8];
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) {
+      w[i][j] = a.m[i][j];
+      w[i][j + 4] = i == j ? 1.0 : 0.0;
+    }
+  for (int c = 0; c < 4; ++c) {
+    int p = c;
+    for (int r = c + 1; r < 4; ++r)
+      if (std::fabs(w[r][c]) > std::fabs(w[p][c])) p = r;
+    if (w[p][c] == 0.0) throw std::runtime_error("singular matrix in inverse");
+    if (p != c)
+      for (int j = 0; j < 8; ++j) std::swap(w[p][j], w[c][j]);
+    const double s = 1.0 / w[c][c];
+    for (int j = 0; j < 8; ++j) w[c][j] *= s;
+    for (int r = 0; r < 4; ++r) {
+      if (r == c || w[r][c] == 0.0) continue;
+      const double f = w[r][c];
+      for (int j = 0; j < 8; ++j) w[r][j] -= f * w[c][j];
+    }
+  }
+  Matrix4x4 r;
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) r.m[i][j] = (real)w[i][j + 4];
+  return r;
+}
+
+Transform::Transform(const Matrix4x4& m) : m_(m), inv_(inverse(m)) {}
+
+Point3f Transform::operator()(const Point3f& p) const {
+  const auto& m = m_.m;
+  const real x = p.x, y = p.y, z = p.z;
+  const real xp = m[0][0] * x + m[0][1] * y + m[0][2] * z + m[0][3];
+  const real yp = m[1][0] * x + m[1][1] * y + m[1][2] * z + m[1][3];
+  const real zp = m[2][0] * x + m[2][1] * y + m[2][2] * z + m[2][3];
+  const real wp = m[3][0] * x + m[3][1] * y + m[3][2] * z + m[3][3];
+  if (wp == 1) return {xp, yp, zp};
+  const double inv = 1.0 / wp;  // Point3::operator/ multiplies by a double reciprocal
+  return {(real)(inv * xp), (real)(inv * yp), (real)(inv * zp)};
+}
+
+Vector3f Transform::operator()(const Vector3f& v) const {
+  const auto& m = m_.m;
+  return {m[0][0] * v.x + m[0][1] * v.y + m[0][2] * v.z, m[1][0] * v.x + m[1][1] * v.y + m[1][2] * v.z,
+          m[2][0] * v.x + m[2][1] * v.y + m[2][2] * v.z};
+}
+
+Normal3f Transform::operator()(const Normal3f& n) const {
+  const auto& m = inv_.m;
+  return {m[0][0] * n.x + m[1][0] * n.y + m[2][0] * n.z, m[0][1] * n.x + m[1][1] * n.y + m[2][1] * n.z,
+          m[0][2] * n.x + m[1][2] * n.y + m[2][2] * n.z};
+}
+
+Transform operator*(const Transform& a, const Transform& b) {
+  return Transform(Matrix4x4::mul(a.m_, b.m_), Matrix4x4::mul(b.inv_, a.inv_));
+}
+
+Transform translate(const Vector3f& d) {
+  return Transform(Matrix4x4(1, 0, 0, d.x, 0, 1, 0, d.y, 0, 0, 1, d.z, 0, 0, 0, 1),
+                   Matrix4x4(1, 0, 0, -d.x, 0, 1, 0, -d.y, 0, 0, 1, -d.z, 0, 0, 0, 1));
+}
+
+Transform scale(real x, real y, real z) {
+  return Transform(Matrix4x4(x, 0, 0, 0, 0, y, 0, 0, 0, 0, z, 0, 0, 0, 0, 1),
+                   Matrix4x4((real)(1.0 / x), 0, 0, 0, 0, (real)(1.0 / y), 0, 0, 0, 0, (real)(1.0 / z), 0, 0, 0,
+                             0, 1));
+}
+
+Transform rotate_x(real theta) {
+  const real s = std::sin(theta), c = std::cos(theta);
+  const Matrix4x4 m(1, 0, 0, 0, 0, c, -s, 0, 0, s, c, 0, 0, 0, 0, 1);
+  return Transform(m, transpose(m));
+}
+
+Transform rotate_y(real theta) {
+  const real s = std::sin(theta), c = std::cos(theta);
+  const Matrix4x4 m(c, 0, s, 0, 0, 1, 0, 0, -s, 0, c, 0, 0, 0, 0, 1);
+  return Transform(m, transpose(m));
+}
+
+Transform rotate_z(real theta) {
+  const real s = std::sin(theta), c = std::cos(theta);
+  const Matrix4x4 m(c, -s, 0, 0, s, c, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1);
+  return Transform(m, transpose(m));
+}
+
+// ---------------------------------------------------------------- textures
+
+namespace {
+
+class ConstantTexture : public Texture2D {
+ public:
+  explicit ConstantTexture(const Spectrum& c) : c_(c) {}
+  Spectrum evaluate(const Point2f&) const override { return c_; }
+
+ private:
+  Spectrum c_;
+};
+
+Spectrum tex(const RC<const Texture2D>& t, const char* what) {
+  if (!t) throw std::invalid_argument(std::string("null texture: ") + what);
+  return t->evaluate(Point2f{});
+}
+
+real tex_s(const RC<const Texture2D>& t, const char* what) { return tex(t, what).r; }
+
+// ---------------------------------------------------------------- shapes
+
+struct MeshData {
+  std::vector<Point3f> p;
+  std::vector<Normal3f> n;
+  std::vector<Point2f> uv;
+  std::vector<int> indices;
+};
+
+class TriangleShape : public Shape {
+ public:
+  TriangleShape(RC<const MeshData> m, int i) : mesh(std::move(m)), index(i) {}
+  RC<const MeshData> mesh;
+  int index;
+};
+
+class SphereShape : public Shape {
+ public:
+  SphereShape(real r, const Transform& t) : radius(r), local_to_world(t) {}
+  real radius;
+  Transform local_to_world;
+};
+
+class VacuumMedium : public Medium {};
+
+class DiffuseAreaLight : public AreaLight {
+ public:
+  explicit DiffuseAreaLight(const Primitive* p) : prim(p) {}
+  const Primitive* prim;
+};
+
+class GeometricPrimitive : public Primitive {
+ public:
+  GeometricPrimitive(RC<Shape> s, RC<Material> m, const Spectrum& e)
+      : shape(std::move(s)), material(std::move(m)), emission(e), light(this) {}
+  // only emitting primitives are area lights (src/shape/geometry.cpp:31-41,66-68)
+  const AreaLight* as_area_light() const noexcept override { return emission ? &light : nullptr; }
+  RC<Shape> shape;
+  RC<Material> material;
+  Spectrum emission;
+  DiffuseAreaLight light;
+};
+
+class BvhAggregate : public Aggregate {
+ public:
+  explicit BvhAggregate(int max_leaf) : max_leaf_prims(max_leaf) {}
+  void build(std::vector<RC<Primitive>> primitives) override {
+    prims = std::move(primitives);
+    ++built;
+  }
+  int max_leaf_prims;
+  std::vector<RC<Primitive>> prims;
+  uint64_t built = 0;
+};
+
+// Normal3::normalize (src/utility/geometry.hpp:492-515): float sum of squares
+// widened to double, double reciprocal of the double sqrt, products rounded.
+Normal3f normalize_ref(const Normal3f& n) {
+  const float s = n.x * n.x + n.y * n.y + n.z * n.z;
+  const double inv = 1.0 / std::sqrt((double)s);
+  return {(float)(n.x * inv), (float)(n.y * inv), (float)(n.z * inv)};
+}
+
+// The reference normalises mesh normals on creation and again, in place, on
+// every hit (src/shape/triangle.cpp:216-236, :178-211), so a normal settles
+// on a fixed point of normalize during a render; start from that point.
+Normal3f settled_normal(const Normal3f& n) {
+  Normal3f v = normalize_ref(n);
+  for (int i = 0; i < 8; ++i) {
+    const Normal3f w = normalize_ref(v);
+    if (w.x == v.x && w.y == v.y && w.z == v.z) break;
+    v = w;
+  }
+  return v;
+}
+
+void put_matrix(std::vector<float>& out, const Matrix4x4& m) {
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) out.push_back(m.m[i][j]);
+}
+
+class GeneralScene : public Scene {
+ public:
+  explicit GeneralScene(RC<BvhAggregate> a) : accel_(std::move(a)) {}
+  void set_camera(RC<const Camera> c) override { camera_ = std::move(c); }
+  RC<const Camera> get_camera() const noexcept override { return camera_; }
+
+  void prepare_to_render() override {
+    SceneDesc d;
+    d.max_leaf_prims = accel_->max_leaf_prims;
+    std::unordered_map<const MeshData*, int> mesh_base;
+    std::unordered_map<const Material*, int> mat_index;
+    std::unordered_map<const Light*, int> light_index;
+    for (size_t i = 0; i < accel_->prims.size(); ++i) {
+      const auto* gp = dynamic_cast<const GeometricPrimitive*>(accel_->prims[i].get());
+      if (!gp) throw std::invalid_argument("primitive not made by create_geometric_primitive");
+      if (!gp->material) throw std::invalid_argument("primitive without material");
+      auto mi = mat_index.find(gp->material.get());
+      if (mi == mat_index.end()) {
+        mi = mat_index.emplace(gp->material.get(), (int)d.materials.size()).first;
+        d.materials.push_back(gp->material->rec);
+      }
+      if (const auto* ts = dynamic_cast<const TriangleShape*>(gp->shape.get())) {
+        auto mb = mesh_base.find(ts->mesh.get());
+        if (mb == mesh_base.end()) {
+          mb = mesh_base.emplace(ts->mesh.get(), (int)(d.positions.size() / 3)).first;
+          for (size_t v = 0; v < ts->mesh->p.size(); ++v) {
+            const Point3f& p = ts->mesh->p[v];
+            const Normal3f& n = ts->mesh->n[v];
+            const Point2f& uv = ts->mesh->uv[v];
+            d.positions.insert(d.positions.end(), {p.x, p.y, p.z});
+            d.normals.insert(d.normals.end(), {n.x, n.y, n.z});
+            d.uvs.insert(d.uvs.end(), {uv.x, uv.y});
+          }
+        }
+        const int tri = (int)(d.indices.size() / 3);
+        for (int k = 0; k < 3; ++k) d.indices.push_back(mb->second + ts->mesh->indices[3 * ts->index + k]);
+        d.prim_shape.push_back(tri);
+      } else if (const auto* ss = dynamic_cast<const SphereShape*>(gp->shape.get())) {
+        const int s = (int)d.sphere_radius.size();
+        d.sphere_radius.push_back(ss->radius);
+        put_matrix(d.sphere_to_world, ss->local_to_world.matrix());
+        put_matrix(d.sphere_to_local, ss->local_to_world.inverse_matrix());
+        d.prim_shape.push_back(~s);
+      } else {
+        throw std::invalid_argument("unknown shape");
+      }
+      d.prim_material.push_back(mi->second);
+      d.prim_emission.insert(d.prim_emission.end(), {gp->emission.r, gp->emission.g, gp->emission.b});
+      light_index.emplace(&gp->light, (int)i);
+    }
+    for (const Light* l : lights) {
+      auto it = light_index.find(l);
+      if (it == light_index.end()) throw std::invalid_argument("scene light is not a primitive of this scene");
+      d.light_prims.push_back(it->second);
+    }
+    desc_ = std::move(d);
+    ++revision_;
+  }
+
+  const SceneDesc& desc() const override { return desc_; }
+  uint64_t revision() const noexcept override { return revision_; }
+
+ private:
+  RC<BvhAggregate> accel_;
+  RC<const Camera> camera_;
+  SceneDesc desc_;
+  uint64_t revision_ = 0;
+};
+
+// ---------------------------------------------------------------- renderer
+
+class GpuRenderer : public GpuPathTraceRenderer {
+ public:
+  explicit GpuRenderer(const GPUPTRendererParams& p) : params_(p) {
+    tr_status s = tr_ctx_create(&ctx_, p.device);
+    if (s != TR_OK) throw TracerError(s, std::string("tr_ctx_create: ") + tr_status_string(s));
+  }
+  ~GpuRenderer() override { tr_ctx_destroy(ctx_); }
+
+  RenderTarget render(const Scene& scene, Film film) override {
+    if (!scene.get_camera()) throw std::invalid_argument("scene has no camera");
+    if (!film.get_filter()) throw std::invalid_argument("film has no filter");
+    if (&scene != uploaded_scene_ || scene.revision() != uploaded_revision_) {
+      const tr_scene_desc d = scene.desc().view();
+      check(tr_scene_upload(ctx_, &d));
+      uploaded_scene_ = &scene;
+      uploaded_revision_ = scene.revision();
+    }
+    tr_render_params rp{};
+    rp.width = film.width();
+    rp.height = film.height();
+    rp.spp = params_.spp;
+    rp.min_depth = params_.min_depth;
+    rp.max_depth = params_.max_depth;
+    rp.direct_light_sample_num = params_.direct_light_sample_num;
+    rp.seed_base = params_.seed_base;
+    const size_t n = (size_t)rp.width * (size_t)rp.height;
+    sums_.assign(4 * n, 0.0);
+    if (params_.fp64_film) {
+      check(tr_render(ctx_, &scene.get_camera()->rec, &film.get_filter()->rec, &rp, nullptr, sums_.data(),
+                      &stats_));
+    } else {
+      std::vector<float> f(4 * n);
+      check(tr_render(ctx_, &scene.get_camera()->rec, &film.get_filter()->rec, &rp, f.data(), nullptr, &stats_));
+      for (size_t i = 0; i < 4 * n; ++i) sums_[i] = f[i];
+    }
+    // Film::write_render_target: color / weight where weight > 0
+    RenderTarget rt;
+    rt.color = Image2D<Spectrum>(rp.width, rp.height);
+    for (int y = 0; y < rp.height; ++y)
+      for (int x = 0; x < rp.width; ++x) {
+        const double* s = &sums_[4 * ((size_t)y * rp.width + x)];
+        const real w = (real)s[3];
+        if (w > 0) rt.color.at(x, y) = Spectrum((real)s[0] / w, (real)s[1] / w, (real)s[2] / w);
+      }
+    return rt;
+  }
+
+  const std::vector<double>& film_sums() const override { return sums_; }
+  tr_stats last_stats() const override { return stats_; }
+
+ private:
+  void check(tr_status s) {
+    if (s != TR_OK) throw TracerError(s, tr_ctx_last_error(ctx_));
+  }
+  GPUPTRendererParams params_;
+  tr_ctx* ctx_ = nullptr;
+  const Scene* uploaded_scene_ = nullptr;
+  uint64_t uploaded_revision_ = 0;
+  std::vector<double> sums_;
+  tr_stats stats_{};
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------- factories
+
+RC<Texture2D> create_constant_texture2d(const Spectrum& constant) { return std::make_shared<ConstantTexture>(constant); }
+
+RC<Shape> create_sphere(real radius, const Transform& local_to_world) {
+  if (radius <= 0) throw std::runtime_error("invalid sphere radius");  // src/shape/sphere.cpp:88-90
+  return std::make_shared<SphereShape>(radius, local_to_world);
+}
+
+std::vector<RC<Shape>> create_triangle_mesh(const mesh_t& mesh, const Transform& local_to_world) {
+  if (mesh.indices.size() % 3 != 0) throw std::invalid_argument("mesh index count is not a multiple of 3");
+  for (int i : mesh.indices)
+    if (i < 0 || (size_t)i >= mesh.vertices.size()) throw std::invalid_argument("mesh index out of range");
+  auto m = std::make_shared<MeshData>();
+  m->indices = mesh.indices;
+  for (const vertex_t& v : mesh.vertices) {
+    m->p.push_back(local_to_world(v.pos));
+    m->n.push_back(settled_normal(local_to_world(v.n)));
+    m->uv.push_back(v.uv);
+  }
+  std::vector<RC<Shape>> out;
+  for (size_t t = 0; t < mesh.indices.size() / 3; ++t) out.push_back(std::make_shared<TriangleShape>(m, (int)t));
+  return out;
+}
+
+RC<Material> create_phong_material(RC<const Texture2D> map_ka, RC<const Texture2D> map_kd,
+                                   RC<const Texture2D> map_ks, RC<const Texture2D> map_ns) {
+  tr_material m{};
+  m.kind = TR_MAT_PHONG;
+  const Spectrum ka = tex(map_ka, "ka"), kd = tex(map_kd, "kd"), ks = tex(map_ks, "ks");
+  const float a[3] = {ka.r, ka.g, ka.b}, d[3] = {kd.r, kd.g, kd.b}, s[3] = {ks.r, ks.g, ks.b};
+  std::memcpy(m.ka, a, sizeof(a));
+  std::memcpy(m.kd, d, sizeof(d));
+  std::memcpy(m.ks, s, sizeof(s));
+  m.ns = tex_s(map_ns, "ns");
+  return std::make_shared<Material>(m);
+}
+
+RC<Material> create_disney_brdf(RC<const Texture2D> base_color, RC<const Texture2D> subsurface,
+                                RC<const Texture2D> metallic, RC<const Texture2D> specular,
+                                RC<const Texture2D> specular_tint, RC<const Texture2D> roughness,
+                                RC<const Texture2D> anisotropic, RC<const Texture2D> sheen,
+                                RC<const Texture2D> sheen_tint, RC<const Texture2D> clearcoat,
+                                RC<const Texture2D> clearcoat_gloss) {
+  tr_material m{};
+  m.kind = TR_MAT_DISNEY12;
+  const Spectrum bc = tex(base_color, "base_color");
+  m.base_color[0] = bc.r;
+  m.base_color[1] = bc.g;
+  m.base_color[2] = bc.b;
+  m.subsurface = tex_s(subsurface, "subsurface");
+  m.metallic = tex_s(metallic, "metallic");
+  m.specular = tex_s(specular, "specular");
+  m.specular_tint = tex_s(specular_tint, "specular_tint");
+  m.roughness = tex_s(roughness, "roughness");
+  m.anisotropic = tex_s(anisotropic, "anisotropic");
+  m.sheen = tex_s(sheen, "sheen");
+  m.sheen_tint = tex_s(sheen_tint, "sheen_tint");
+  m.clearcoat = tex_s(clearcoat, "clearcoat");
+  m.clearcoat_gloss = tex_s(clearcoat_gloss, "clearcoat_gloss");
+  return std::make_shared<Material>(m);
+}
+
+RC<Medium> create_vacuum() { return std::make_shared<VacuumMedium>(); }
+
+RC<Primitive> create_geometric_primitive(const RC<Shape>& shape, const RC<Material>& material,
+                                         const MediumInterface& mi, const Spectrum& emission) {
+  if (!shape) throw std::invalid_argument("null shape");
+  for (const RC<const Medium>& m : {mi.inside, mi.outside})
+    if (m && !dynamic_cast<const VacuumMedium*>(m.get()))
+      throw std::invalid_argument("only the vacuum medium is on the GPU path");
+  return std::make_shared<GeometricPrimitive>(shape, material, emission);
+}
+
+RC<Aggregate> create_bvh_accel(int max_leaf_primitives) {
+  if (max_leaf_primitives < 1) throw std::invalid_argument("max_leaf_primitives must be >= 1");
+  return std::make_shared<BvhAggregate>(max_leaf_primitives);
+}
+
+RC<Camera> create_thin_lens_camera(real film_aspect, const Point3f& cam_pos, const Point3f& target,
+                                   const Vector3f& up, real fov, real lens_radius, real focal_dist) {
+  tr_camera c{};
+  c.film_aspect = film_aspect;
+  const float p[3] = {cam_pos.x, cam_pos.y, cam_pos.z}, t[3] = {target.x, target.y, target.z},
+              u[3] = {up.x, up.y, up.z};
+  std::memcpy(c.pos, p, sizeof(p));
+  std::memcpy(c.target, t, sizeof(t));
+  std::memcpy(c.up, u, sizeof(u));
+  c.fov = fov;
+  c.lens_radius = lens_radius;
+  c.focal_dist = focal_dist;
+  return std::make_shared<Camera>(c);
+}
+
+RC<Filter> create_gaussin_filter(real radius, real alpha) {
+  if (!(radius > 0)) throw std::invalid_argument("filter radius must be positive");
+  return std::make_shared<Filter>(tr_filter{radius, alpha});
+}
+
+RC<Scene> create_general_scene(const RC<Aggregate>& accel) {
+  auto b = std::dynamic_pointer_cast<BvhAggregate>(accel);
+  if (!b) throw std::invalid_argument("aggregate not made by create_bvh_accel");
+  return std::make_shared<GeneralScene>(b);
+}
+
+RC<GpuPathTraceRenderer> create_gpu_pt_renderer(const GPUPTRendererParams& params) {
+  return std::make_shared<GpuRenderer>(params);
+}
+
+tr_scene_desc SceneDesc::view() const {
+  tr_scene_desc d{};
+  d.num_vertices = (uint32_t)(positions.size() / 3);
+  d.positions = positions.data();
+  d.normals = normals.data();
+  d.uvs = uvs.data();
+  d.num_triangles = (uint32_t)(indices.size() / 3);
+  d.indices = indices.data();
+  d.num_spheres = (uint32_t)sphere_radius.size();
+  d.sphere_radius = sphere_radius.data();
+  d.sphere_to_world = sphere_to_world.data();
+  d.sphere_to_local = sphere_to_local.data();
+  d.num_materials = (uint32_t)materials.size();
+  d.materials = materials.data();
+  d.num_prims = (uint32_t)prim_shape.size();
+  d.prim_shape = prim_shape.data();
+  d.prim_material = prim_material.data();
+  d.prim_emission = prim_emission.data();
+  d.num_lights = (uint32_t)light_prims.size();
+  d.light_prims = light_prims.data();
+  d.max_leaf_prims = max_leaf_prims;
+  return d;
+}
+
+}  // namespace tracer

@@ -82,7 +82,7 @@ struct Launch {
   int* q_nee[2];
   int* q_sh;
   unsigned int* ctr;
-  unsigned long long* stats;  // samples, extend rays, shadow rays, shade items
+  unsigned long long* stats;  // samples, extend rays, shadow rays, shade items, visit counts (4-7)
 };
 
 // Warp-aggregated queue append. The active lanes are grouped by counter
@@ -224,9 +224,11 @@ __global__ void __launch_bounds__(256) k_init(Launch P) {
   count_add(P.stats, finished);
 }
 
+template <bool COUNT>
 __global__ void __launch_bounds__(128) k_extend(Launch P, int cur) {
   const unsigned int n = P.ctr[C_EXT + cur];
   unsigned int nr = 0;
+  VisitCount vc;
   for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int e = P.q_ext[cur][i];
     const int slot = e >> 1;
@@ -235,28 +237,40 @@ __global__ void __launch_bounds__(128) k_extend(Launch P, int cur) {
     const float4 b = mis ? P.M1[slot] : P.P1[slot];
     float t_max = kRealMax;
     Hit h;
-    Traversal<false>::run(P.sc, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), 0.0f, t_max, h, (int*)(P.ctr + C_ERR));
+    Traversal<false, COUNT>::run(P.sc, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), 0.0f, t_max, h,
+                                 (int*)(P.ctr + C_ERR), &vc);
     const float4 rec = make_float4(__int_as_float(h.prim), h.t_attr, h.alpha, h.beta);
     if (mis) P.HM[slot] = rec;
     else P.HC[slot] = rec;
     ++nr;
   }
   count_add(P.stats + 1, nr);
+  if (COUNT) {
+    count_add(P.stats + 4, vc.boxes);
+    count_add(P.stats + 5, vc.prims);
+  }
 }
 
+template <bool COUNT>
 __global__ void __launch_bounds__(128) k_shadow(Launch P) {
   const unsigned int n = P.ctr[C_SH];
   unsigned int nr = 0;
+  VisitCount vc;
   for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int r = P.q_sh[i];
     const float4 a = P.SH[3 * r], b = P.SH[3 * r + 1];
     float t_max = a.w;
     Hit h;
-    if (Traversal<true>::run(P.sc, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), kEps, t_max, h, (int*)(P.ctr + C_ERR)))
+    if (Traversal<true, COUNT>::run(P.sc, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), kEps, t_max, h,
+                                    (int*)(P.ctr + C_ERR), &vc))
       P.SH[3 * r + 2].w = 0.0f;
     ++nr;
   }
   count_add(P.stats + 2, nr);
+  if (COUNT) {
+    count_add(P.stats + 6, vc.boxes);
+    count_add(P.stats + 7, vc.prims);
+  }
 }
 
 // sample_bsdf's contribution once its ray has been traced
@@ -647,8 +661,8 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
   k_init<<<grid_init, 256, 0, st>>>(P);
   RCHK(cudaGetLastError());
 
-  // optional per-stage timing: events around extend, shading (logic,
-  // material, nee) and shadow of every iteration, summed once drained
+  // optional per-kernel timing: an event before the first kernel of every
+  // iteration and after each of its kernels, summed once drained
   auto mark = [&]() {
     if (!timed) return;
     if (nev == ev.size()) {
@@ -658,6 +672,7 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
     }
     cudaEventRecord(ev[nev++], st);
   };
+  const bool count = (prm->flags & TR_RENDER_COUNT_VISITS) != 0;
   // Every slot finishes within spp * (max_depth + 2) iterations.
   const long long max_iters = (long long)prm->spp * (prm->max_depth + 2) + 4;
   const int chunk = 4;
@@ -668,7 +683,8 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
     for (int c = 0; c < chunk && it < max_iters; ++c, ++it) {
       const int cur = (int)(it & 1), nxt = cur ^ 1;
       mark();
-      k_extend<<<grid, 128, 0, st>>>(P, cur);
+      if (count) k_extend<true><<<grid, 128, 0, st>>>(P, cur);
+      else k_extend<false><<<grid, 128, 0, st>>>(P, cur);
       mark();
       // next iteration's extend and live counts; this iteration's shadow,
       // material and light-sample counts
@@ -677,12 +693,17 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
       RCHK(cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 5, st));  // C_SH, C_MAT x2, C_NEE x2
       mark();
       k_logic<<<grid, 128, 0, st>>>(P, cur);
+      mark();
       k_material<MAT_PHONG><<<grid, 128, 0, st>>>(P, cur);
+      mark();
       k_material<MAT_DISNEY12><<<grid, 128, 0, st>>>(P, cur);
+      mark();
       k_nee<MAT_PHONG><<<grid, 128, 0, st>>>(P);
+      mark();
       k_nee<MAT_DISNEY12><<<grid, 128, 0, st>>>(P);
       mark();
-      k_shadow<<<grid, 128, 0, st>>>(P);
+      if (count) k_shadow<true><<<grid, 128, 0, st>>>(P);
+      else k_shadow<false><<<grid, 128, 0, st>>>(P);
       mark();
     }
     RCHK(cudaGetLastError());
@@ -709,20 +730,21 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
   }
   RCHK(cudaEventRecord(e1, st));
   RCHK(cudaEventSynchronize(e1));
-  unsigned long long hs[4] = {0, 0, 0, 0};
+  unsigned long long hs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   RCHK(cudaMemcpy(hs, P.stats, sizeof(hs), cudaMemcpyDeviceToHost));
   unsigned int ctrs[16];
   RCHK(cudaMemcpy(ctrs, P.ctr, sizeof(ctrs), cudaMemcpyDeviceToHost));
-  double stage[3] = {0.0, 0.0, 0.0};
-  for (size_t k = 0; k + 5 <= nev; k += 5) {
-    float a = 0.0f, b = 0.0f, c = 0.0f;
-    cudaEventElapsedTime(&a, ev[k], ev[k + 1]);
-    cudaEventElapsedTime(&b, ev[k + 2], ev[k + 3]);
-    cudaEventElapsedTime(&c, ev[k + 3], ev[k + 4]);
-    stage[0] += a;
-    stage[1] += b;
-    stage[2] += c;
-  }
+  // event k of an iteration's 9 precedes kernel k; stage of each interval
+  static const int kStageOf[8] = {TR_STAGE_EXTEND,          TR_STAGE_RESET,     TR_STAGE_LOGIC,
+                                  TR_STAGE_MATERIAL_PHONG,  TR_STAGE_MATERIAL_DISNEY,
+                                  TR_STAGE_NEE_PHONG,       TR_STAGE_NEE_DISNEY, TR_STAGE_SHADOW};
+  double stage[TR_NUM_STAGES] = {};
+  for (size_t k = 0; k + 9 <= nev; k += 9)
+    for (int j = 0; j < 8; ++j) {
+      float a = 0.0f;
+      cudaEventElapsedTime(&a, ev[k + j], ev[k + j + 1]);
+      stage[kStageOf[j]] += a;
+    }
   float ms = 0.0f;
   cudaEventElapsedTime(&ms, e0, e1);
   cleanup();
@@ -734,7 +756,11 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
     stats->shade_items = hs[3];
     stats->iterations = (uint64_t)it;
     stats->device_ms = ms;
-    for (int k = 0; k < 3; ++k) stats->stage_ms[k] = stage[k];
+    for (int k = 0; k < TR_NUM_STAGES; ++k) stats->stage_ms[k] = stage[k];
+    stats->closest_boxes = hs[4];
+    stats->closest_prims = hs[5];
+    stats->any_boxes = hs[6];
+    stats->any_prims = hs[7];
   }
   return result;
 #undef RCHK

@@ -105,7 +105,13 @@ __device__ __forceinline__ bool sphere_roots(f3 lo, f3 ld, float radius, float& 
   return true;
 }
 
-template <bool ANY>
+// Boxes tested and leaf primitives tested by one traversal (the per-ray
+// units of the traversal's algorithmic-bytes figure).
+struct VisitCount {
+  unsigned int boxes = 0, prims = 0;
+};
+
+template <bool ANY, bool COUNT = false>
 struct Traversal {
   // Tests one leaf slot. Returns true when ANY and the ray is occluded.
   static __device__ __forceinline__ bool test_slot(const DScene& sc, int slot, f3 o, f3 d, float t_min,
@@ -147,9 +153,11 @@ struct Traversal {
   }
 
   // Returns true for ANY when occluded; for closest hit fills h and t_max.
-  static __device__ bool run(const DScene& sc, f3 o, f3 d, float t_min, float& t_max, Hit& h, int* err) {
+  static __device__ bool run(const DScene& sc, f3 o, f3 d, float t_min, float& t_max, Hit& h, int* err,
+                             VisitCount* vc = nullptr) {
     h.prim = -1;
     if (sc.root_kind == 0) return false;
+    if (COUNT) ++vc->boxes;
     // (float)(1.0 / d) in the reference: a single division, so the double
     // rounding equals the float division.
     const f3 inv = mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
@@ -179,6 +187,7 @@ struct Traversal {
         const float4 dd = ldg4(np + 3);
         const int4 di = make_int4(__float_as_int(dd.x), __float_as_int(dd.y), __float_as_int(dd.z),
                                   __float_as_int(dd.w));
+        if (COUNT) vc->boxes += 2;
         float tl, tr;
         bool hl = box_pass(a.x, a.y, a.z, a.w, b.x, b.y, o, inv, n0, n1, n2, tl) && tl < t_max;
         bool hr = box_pass(b.z, b.w, c.x, c.y, c.z, c.w, o, inv, n0, n1, n2, tr) && tr < t_max;
@@ -203,8 +212,10 @@ struct Traversal {
         if (hl) { cur = lref; cnt = lcnt; continue; }
         if (hr) { cur = rref; cnt = rcnt; continue; }
       } else {
-        for (int i = 0; i < cnt; ++i)
+        for (int i = 0; i < cnt; ++i) {
+          if (COUNT) ++vc->prims;
           if (test_slot(sc, cur + i, o, d, t_min, t_max, h)) return true;
+        }
       }
       bool found = false;
       while (sp > 0) {
