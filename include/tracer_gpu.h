@@ -233,6 +233,28 @@ tr_status tr_render_dev(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filt
                         const tr_render_params* params, float* d_rgbw, double* d_rgbw64,
                         tr_stats* stats);
 
+/* No reference counterpart. tr_render_dev (float film only) without any
+ * allocation: every scratch buffer lives in one 16 MiB file-scope device
+ * array of the library, so the call makes no cudaMalloc, cudaFree, pinned or
+ * event allocation. For callers that render previews inside a frame loop and
+ * cannot take cudaFree's implicit device synchronisation, or that share the
+ * GPU with a caching allocator holding the rest of its memory.
+ *  - Limit: width * height * (312 + 68 * lights) bytes (plus alignment) must
+ *    fit in 16 MiB, e.g. 128x128 with 8 lights; larger films return
+ *    TR_ERR_ARG with the size needed.
+ *  - The first call on a device looks up the array's address
+ *    (cudaGetSymbolAddress), which can load the module; make that call
+ *    before any stream capture.
+ *  - The call zeroes its counters, statistics and d_rgbw itself on the
+ *    context stream; nothing needs to start at zero.
+ *  - The array is shared by every context on a device: calls that overlap
+ *    in time on one device (two contexts, two threads) race and corrupt
+ *    each other's results. Calls on one context run in order.
+ *  - Blocks until done; runs a fixed number of wavefront iterations, so
+ *    tr_cancel does not stop it; stats->device_ms and stage_ms stay 0. */
+tr_status tr_render_dev_noalloc(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter,
+                                const tr_render_params* params, float* d_rgbw, tr_stats* stats);
+
 /* Asks a running tr_render on this context to stop after its current
  * wavefront iteration; that call then returns TR_ERR_CANCELLED. Thread-safe. */
 tr_status tr_cancel(tr_ctx* ctx);

@@ -28,8 +28,11 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "context.h"
@@ -795,3 +798,184 @@ tr_status tr_render(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter, 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// No-allocation render (tr_render_dev_noalloc). The same kernels as
+// render_impl, with every scratch buffer carved from one file-scope device
+// array instead of cudaMalloc'd RenderBuffers, a fixed iteration count instead
+// of polling a pinned live count, and no CUDA events.
+
+namespace trg {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;  // 16 MiB per device
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mtx;
+void* g_noalloc_base[kMaxDevices] = {};
+
+// Scratch bytes a film of n pixels with nl lights needs (each buffer 256-byte aligned).
+struct NoAllocLayout {
+  size_t off = 0;
+  size_t take(size_t bytes) {
+    const size_t at = off;
+    off = (off + bytes + 255) & ~size_t(255);
+    return at;
+  }
+};
+
+}  // namespace
+
+tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter,
+                              const tr_render_params* prm, float* d_rgbw, tr_stats* stats) {
+  if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
+  if (prm->width <= 0 || prm->height <= 0 || prm->spp <= 0 || prm->max_depth < 0)
+    return set_err(ctx, TR_ERR_ARG, "invalid render size, spp or depth");
+  if (prm->direct_light_sample_num != 1)
+    return set_err(ctx, TR_ERR_UNSUPPORTED, "direct_light_sample_num must be 1 on the GPU path");
+  if (!(filter->radius > 0.0f) || filter->radius > 16.0f) return set_err(ctx, TR_ERR_ARG, "invalid filter radius");
+  if (ctx->device < 0 || ctx->device >= kMaxDevices) return set_err(ctx, TR_ERR_ARG, "device ordinal out of range");
+  const long long npix = (long long)prm->width * prm->height;
+  const int nl = ctx->dsc.num_lights;
+  const size_t NL = (size_t)std::max(nl, 1);
+  // carve the layout first: reject what does not fit before touching the device
+  const size_t N = npix > (1ll << 24) ? (size_t(1) << 24) : (size_t)npix;
+  NoAllocLayout L;
+  const size_t f4 = sizeof(float4);
+  const size_t oP = L.take(5 * N * f4), oRng = L.take(N * 8), oM = L.take(3 * N * f4), oH = L.take(2 * N * f4),
+               oSC = L.take(N * 7 * f4), oNU = L.take(N * NL * 8), oSH = L.take(N * NL * 3 * f4),
+               oQe = L.take(2 * 2 * N * 4), oQa = L.take(2 * N * 4), oQm = L.take(2 * N * 4),
+               oQn = L.take(2 * N * NL * 4), oQs = L.take(N * NL * 4), oCtr = L.take(64), oSt = L.take(64);
+  if (npix > (1ll << 24) || L.off > kNoAllocScratchBytes) {
+    char msg[256];
+    std::snprintf(msg, sizeof(msg),
+                  "film %dx%d with %d lights needs %zu bytes of scratch; tr_render_dev_noalloc has %zu "
+                  "(about 312 + 68 * lights bytes per pixel)",
+                  prm->width, prm->height, nl, (size_t)L.off, kNoAllocScratchBytes);
+    return set_err(ctx, TR_ERR_ARG, msg);
+  }
+  const int n = (int)npix;
+  unsigned char* base = nullptr;
+  {
+    // once per device: the address of this device's copy of the array
+    std::lock_guard<std::mutex> lk(g_noalloc_mtx);
+    if (!g_noalloc_base[ctx->device]) {
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGetSymbolAddress(scratch)");
+      g_noalloc_base[ctx->device] = p;
+    }
+    base = static_cast<unsigned char*>(g_noalloc_base[ctx->device]);
+  }
+  cudaStream_t st = ctx->stream;
+
+  Launch P;
+  std::memset(&P, 0, sizeof(P));
+  P.sc = ctx->dsc;
+  setup_camera(P.cam, *cam);
+  P.W = prm->width;
+  P.H = prm->height;
+  P.spp = prm->spp;
+  P.min_depth = prm->min_depth;
+  P.max_depth = prm->max_depth;
+  P.nl = nl;
+  P.seed_base = prm->seed_base;
+  P.filter_radius = filter->radius;
+  P.filter_alpha = filter->alpha;
+  P.filter_exp = std::exp(-filter->alpha * filter->radius * filter->radius);  // GaussianFilter ctor
+  P.fp64 = 0;
+  float4* Pb = reinterpret_cast<float4*>(base + oP);
+  P.P0 = Pb;
+  P.P1 = Pb + N;
+  P.P2 = Pb + 2 * N;
+  P.P3 = Pb + 3 * N;
+  P.P4 = Pb + 4 * N;
+  P.rng = reinterpret_cast<unsigned long long*>(base + oRng);
+  float4* Mb = reinterpret_cast<float4*>(base + oM);
+  P.M0 = Mb;
+  P.M1 = Mb + N;
+  P.M2 = Mb + 2 * N;
+  P.HC = reinterpret_cast<float4*>(base + oH);
+  P.HM = P.HC + N;
+  P.SC = reinterpret_cast<float4*>(base + oSC);
+  P.NU = reinterpret_cast<float2*>(base + oNU);
+  P.SH = reinterpret_cast<float4*>(base + oSH);
+  P.acc = reinterpret_cast<float4*>(d_rgbw);
+  int* qe = reinterpret_cast<int*>(base + oQe);
+  int* qa = reinterpret_cast<int*>(base + oQa);
+  int* qm = reinterpret_cast<int*>(base + oQm);
+  int* qn = reinterpret_cast<int*>(base + oQn);
+  for (int k = 0; k < 2; ++k) {
+    P.q_ext[k] = qe + (size_t)k * 2 * N;
+    P.q_act[k] = qa + (size_t)k * N;
+    P.q_mat[k] = qm + (size_t)k * N;
+    P.q_nee[k] = qn + (size_t)k * N * NL;
+  }
+  P.q_sh = reinterpret_cast<int*>(base + oQs);
+  P.ctr = reinterpret_cast<unsigned int*>(base + oCtr);
+  P.stats = reinterpret_cast<unsigned long long*>(base + oSt);
+
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  if (sms <= 0) sms = 1;
+  const int grid = sms * 16, grid_init = sms * 8;
+#define NCHK(call)                                      \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+  // the counters, statistics and film start at zero on every call; the
+  // rest of the scratch is written before it is read
+  NCHK(cudaMemsetAsync(P.acc, 0, (size_t)n * 16, st));
+  NCHK(cudaMemsetAsync(P.ctr, 0, 64, st));
+  NCHK(cudaMemsetAsync(P.stats, 0, 64, st));
+  k_init<<<grid_init, 256, 0, st>>>(P);
+  NCHK(cudaGetLastError());
+  // Every slot finishes within spp * (max_depth + 2) iterations; iterations
+  // past the drain find empty queues and return at once.
+  const long long iters = (long long)prm->spp * (prm->max_depth + 2) + 4;
+  for (long long it = 0; it < iters; ++it) {
+    const int cur = (int)(it & 1), nxt = cur ^ 1;
+    k_extend<false><<<grid, 128, 0, st>>>(P, cur);
+    NCHK(cudaMemsetAsync(P.ctr + C_EXT + nxt, 0, 4, st));
+    NCHK(cudaMemsetAsync(P.ctr + C_ACT + nxt, 0, 4, st));
+    NCHK(cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 5, st));
+    k_logic<<<grid, 128, 0, st>>>(P, cur);
+    k_material<MAT_PHONG><<<grid, 128, 0, st>>>(P, cur);
+    k_material<MAT_DISNEY12><<<grid, 128, 0, st>>>(P, cur);
+    k_nee<MAT_PHONG><<<grid, 128, 0, st>>>(P);
+    k_nee<MAT_DISNEY12><<<grid, 128, 0, st>>>(P);
+    k_shadow<false><<<grid, 128, 0, st>>>(P);
+  }
+  NCHK(cudaGetLastError());
+  NCHK(cudaStreamSynchronize(st));
+  unsigned long long hs[8];
+  unsigned int ctrs[16];
+  NCHK(cudaMemcpy(hs, P.stats, sizeof(hs), cudaMemcpyDeviceToHost));
+  NCHK(cudaMemcpy(ctrs, P.ctr, sizeof(ctrs), cudaMemcpyDeviceToHost));
+#undef NCHK
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->samples = hs[0];
+    stats->extend_rays = hs[1];
+    stats->shadow_rays = hs[2];
+    stats->shade_items = hs[3];
+    stats->iterations = (uint64_t)iters;
+  }
+  if (ctrs[C_ERR] != 0) return set_err(ctx, TR_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
+  if (ctrs[C_ACT + (int)(iters & 1)] != 0)
+    return set_err(ctx, TR_ERR_TIMEOUT, "wavefront did not drain within its iteration bound");
+  return TR_OK;
+}
+
+}  // namespace trg
+
+extern "C" tr_status tr_render_dev_noalloc(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter,
+                                           const tr_render_params* params, float* d_rgbw, tr_stats* stats) {
+  if (!ctx || !cam || !filter || !params || !d_rgbw) return TR_ERR_ARG;
+  if (((uintptr_t)d_rgbw & 15u) != 0) return trg::set_err(ctx, TR_ERR_ARG, "film buffer must be 16-byte aligned");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return trg::cuda_fail(ctx, e, "cudaSetDevice");
+  return trg::render_noalloc_impl(ctx, cam, filter, params, d_rgbw, stats);
+}
