@@ -208,28 +208,49 @@ tr_status upload_device_tables(tr_ctx* ctx) {
 }
 
 // ------------------------------------------------------------ batch kernels
-__global__ void __launch_bounds__(128) k_trace_closest(DScene sc, const float4* __restrict__ rays, int n,
-                                                      int32_t* __restrict__ prim, float* __restrict__ tout,
-                                                      int* err) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float4 r0 = __ldg(rays + 2 * i), r1 = __ldg(rays + 2 * i + 1);
-  float t_max = r1.w;
-  Hit h;
-  Traversal<false>::run(sc, mk3(r0.x, r0.y, r0.z), mk3(r0.w, r1.x, r1.y), r1.z, t_max, h, err);
-  prim[i] = h.prim;
-  tout[i] = t_max;
+// Rays as two float4: (o.xyz, d.x), (d.y, d.z, t_min, t_max).
+struct BatchJob {
+  const float4* __restrict__ rays;
+  unsigned int n;
+  int32_t* prim;  // closest: prim id and t; any: hit flags
+  float* tout;
+  uint8_t* hit;
+  __device__ __forceinline__ unsigned int count() const { return n; }
+  __device__ __forceinline__ void load(unsigned int i, f3& o, f3& d, float& t_min, float& t_max) const {
+    const float4 r0 = __ldg(rays + 2 * (size_t)i), r1 = __ldg(rays + 2 * (size_t)i + 1);
+    o = mk3(r0.x, r0.y, r0.z);
+    d = mk3(r0.w, r1.x, r1.y);
+    t_min = r1.z;
+    t_max = r1.w;
+  }
+  __device__ __forceinline__ void store(unsigned int i, const Hit& h, float t_max, bool occluded) const {
+    if (prim) {
+      prim[i] = h.prim;
+      tout[i] = t_max;
+    } else {
+      hit[i] = occluded ? 1 : 0;
+    }
+  }
+};
+
+template <bool ANY>
+__global__ void __launch_bounds__(128) k_trace_batch(DScene sc, BatchJob job, unsigned int* fetch, int* err) {
+  VisitCount vc;
+  persistent_traverse<ANY, false, 20>(sc, job, fetch, err, vc);
 }
 
-__global__ void __launch_bounds__(128) k_trace_any(DScene sc, const float4* __restrict__ rays, int n,
-                                                  uint8_t* __restrict__ hit, int* err) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float4 r0 = __ldg(rays + 2 * i), r1 = __ldg(rays + 2 * i + 1);
-  float t_max = r1.w;
-  Hit h;
-  const bool occ = Traversal<true>::run(sc, mk3(r0.x, r0.y, r0.z), mk3(r0.w, r1.x, r1.y), r1.z, t_max, h, err);
-  hit[i] = occ ? 1 : 0;
+// Resident blocks of a persistent traversal kernel (whole device).
+template <bool ANY>
+static int trace_grid(int device) {
+  static int per_sm[2] = {0, 0};
+  if (!per_sm[ANY]) {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace_batch<ANY>, 128, 0) != cudaSuccess || b <= 0) b = 4;
+    per_sm[ANY] = b;
+  }
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  return std::max(sms, 1) * per_sm[ANY];
 }
 
 }  // namespace trg
@@ -509,10 +530,10 @@ tr_status tr_trace_closest_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, int3
   if (n == 0) return TR_OK;
   if (n > 0x7fffffffull) return set_err(ctx, TR_ERR_ARG, "too many rays");
   if (((uintptr_t)d_rays & 15u) != 0) return set_err(ctx, TR_ERR_ARG, "ray buffer must be 16-byte aligned");
-  const int threads = 128;
-  const int blocks = (int)((n + threads - 1) / threads);
-  k_trace_closest<<<blocks, threads, 0, ctx->stream>>>(ctx->dsc, reinterpret_cast<const float4*>(d_rays), (int)n,
-                                                        d_prim, d_t, ctx->d_err.as<int>());
+  TR_CUDA(ctx, cudaMemsetAsync(ctx->d_err.as<int>() + 1, 0, sizeof(int), ctx->stream));  // fetch position
+  const BatchJob job{reinterpret_cast<const float4*>(d_rays), (unsigned int)n, d_prim, d_t, nullptr};
+  k_trace_batch<false><<<trace_grid<false>(ctx->device), 128, 0, ctx->stream>>>(
+      ctx->dsc, job, reinterpret_cast<unsigned int*>(ctx->d_err.as<int>() + 1), ctx->d_err.as<int>());
   TR_CUDA(ctx, cudaGetLastError());
   return TR_OK;
 }
@@ -523,10 +544,10 @@ tr_status tr_trace_any_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, uint8_t*
   if (n == 0) return TR_OK;
   if (n > 0x7fffffffull) return set_err(ctx, TR_ERR_ARG, "too many rays");
   if (((uintptr_t)d_rays & 15u) != 0) return set_err(ctx, TR_ERR_ARG, "ray buffer must be 16-byte aligned");
-  const int threads = 128;
-  const int blocks = (int)((n + threads - 1) / threads);
-  k_trace_any<<<blocks, threads, 0, ctx->stream>>>(ctx->dsc, reinterpret_cast<const float4*>(d_rays), (int)n,
-                                                    d_hit, ctx->d_err.as<int>());
+  TR_CUDA(ctx, cudaMemsetAsync(ctx->d_err.as<int>() + 1, 0, sizeof(int), ctx->stream));  // fetch position
+  const BatchJob job{reinterpret_cast<const float4*>(d_rays), (unsigned int)n, nullptr, nullptr, d_hit};
+  k_trace_batch<true><<<trace_grid<true>(ctx->device), 128, 0, ctx->stream>>>(
+      ctx->dsc, job, reinterpret_cast<unsigned int*>(ctx->d_err.as<int>() + 1), ctx->d_err.as<int>());
   TR_CUDA(ctx, cudaGetLastError());
   return TR_OK;
 }

@@ -53,6 +53,8 @@ enum : int {  // counter slots
   C_SH = 4,       // shadow queue size
   C_MAT = 5,      // 2: per-material hit queue sizes
   C_NEE = 7,      // 2: per-material light-sample queue sizes
+  C_FEXT = 9,     // extend kernel's work-fetch position
+  C_FSH = 10,     // shadow kernel's work-fetch position
   C_ERR = 15,     // traversal error word
 };
 
@@ -227,27 +229,54 @@ __global__ void __launch_bounds__(256) k_init(Launch P) {
   count_add(P.stats, finished);
 }
 
-template <bool COUNT>
-__global__ void __launch_bounds__(128) k_extend(Launch P, int cur) {
-  const unsigned int n = P.ctr[C_EXT + cur];
-  unsigned int nr = 0;
-  VisitCount vc;
-  for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+// Work items of the extend kernel: queue entry 2*slot (+1 for the MIS ray).
+struct ExtendJob {
+  const Launch& P;
+  int cur;
+  __device__ __forceinline__ unsigned int count() const { return P.ctr[C_EXT + cur]; }
+  __device__ __forceinline__ void load(unsigned int i, f3& o, f3& d, float& t_min, float& t_max) const {
     const int e = P.q_ext[cur][i];
     const int slot = e >> 1;
-    const bool mis = e & 1;
-    const float4 a = mis ? P.M0[slot] : P.P0[slot];
-    const float4 b = mis ? P.M1[slot] : P.P1[slot];
-    float t_max = kRealMax;
-    Hit h;
-    Traversal<false, COUNT>::run(P.sc, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), 0.0f, t_max, h,
-                                 (int*)(P.ctr + C_ERR), &vc);
-    const float4 rec = make_float4(__int_as_float(h.prim), h.t_attr, h.alpha, h.beta);
-    if (mis) P.HM[slot] = rec;
-    else P.HC[slot] = rec;
-    ++nr;
+    const float4 a = (e & 1) ? P.M0[slot] : P.P0[slot];
+    const float4 b = (e & 1) ? P.M1[slot] : P.P1[slot];
+    o = mk3(a.x, a.y, a.z);
+    d = mk3(b.x, b.y, b.z);
+    t_min = 0.0f;
+    t_max = kRealMax;
   }
-  count_add(P.stats + 1, nr);
+  __device__ __forceinline__ void store(unsigned int i, const Hit& h, float, bool) const {
+    const int e = P.q_ext[cur][i];
+    const float4 rec = make_float4(__int_as_float(h.prim), h.t_attr, h.alpha, h.beta);
+    if (e & 1) P.HM[e >> 1] = rec;
+    else P.HC[e >> 1] = rec;
+  }
+};
+
+// Work items of the shadow kernel: shadow records o|t_max, d, contrib|valid.
+struct ShadowJob {
+  const Launch& P;
+  __device__ __forceinline__ unsigned int count() const { return P.ctr[C_SH]; }
+  __device__ __forceinline__ void load(unsigned int i, f3& o, f3& d, float& t_min, float& t_max) const {
+    const int r = P.q_sh[i];
+    const float4 a = P.SH[3 * r], b = P.SH[3 * r + 1];
+    o = mk3(a.x, a.y, a.z);
+    d = mk3(b.x, b.y, b.z);
+    t_min = kEps;
+    t_max = a.w;
+  }
+  __device__ __forceinline__ void store(unsigned int i, const Hit&, float, bool occluded) const {
+    if (occluded) P.SH[3 * P.q_sh[i] + 2].w = 0.0f;
+  }
+};
+
+constexpr int kRefillLanes = 20;  // refill a warp's finished lanes once fewer than this many trace
+
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_extend(Launch P, int cur) {
+  ExtendJob job{P, cur};
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.stats + 1, (unsigned long long)job.count());
+  VisitCount vc;
+  persistent_traverse<false, COUNT, kRefillLanes>(P.sc, job, P.ctr + C_FEXT, (int*)(P.ctr + C_ERR), vc);
   if (COUNT) {
     count_add(P.stats + 4, vc.boxes);
     count_add(P.stats + 5, vc.prims);
@@ -256,20 +285,10 @@ __global__ void __launch_bounds__(128) k_extend(Launch P, int cur) {
 
 template <bool COUNT>
 __global__ void __launch_bounds__(128) k_shadow(Launch P) {
-  const unsigned int n = P.ctr[C_SH];
-  unsigned int nr = 0;
+  ShadowJob job{P};
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.stats + 2, (unsigned long long)job.count());
   VisitCount vc;
-  for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int r = P.q_sh[i];
-    const float4 a = P.SH[3 * r], b = P.SH[3 * r + 1];
-    float t_max = a.w;
-    Hit h;
-    if (Traversal<true, COUNT>::run(P.sc, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), kEps, t_max, h,
-                                    (int*)(P.ctr + C_ERR), &vc))
-      P.SH[3 * r + 2].w = 0.0f;
-    ++nr;
-  }
-  count_add(P.stats + 2, nr);
+  persistent_traverse<true, COUNT, kRefillLanes>(P.sc, job, P.ctr + C_FSH, (int*)(P.ctr + C_ERR), vc);
   if (COUNT) {
     count_add(P.stats + 6, vc.boxes);
     count_add(P.stats + 7, vc.prims);
@@ -354,6 +373,14 @@ struct MatOps {
   }
 };
 
+// The BSDF sample, shared out of line by the two call sites of k_material
+// (the path's sample and the MIS sample): one copy of the sampling code
+// instead of two keeps the kernel within the instruction cache.
+template <int KIND>
+__device__ __noinline__ BsdfSample sample_bsdf_shared(const Bsdf& b, f3 wo, float u, float v, float w) {
+  return MatOps<KIND>::sample(b, wo, u, v, w);
+}
+
 // One path vertex on a material of kind KIND: the body of eval_pixel_li
 // from the BSDF sample to the next continuation ray
 // (src/renderer/path_trace_renderer.cpp:125-163).
@@ -378,7 +405,7 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
     bsdf.g = is.g;
     bsdf.s = is.s;
     const float u0 = Pcg::next(st), u1 = Pcg::next(st), u2 = Pcg::next(st);
-    const BsdfSample bs = MatOps<KIND>::sample(bsdf, is.wo, u0, u1, u2);
+    const BsdfSample bs = sample_bsdf_shared<KIND>(bsdf, is.wo, u0, u1, u2);
     if (black(bs.f) || bs.pdf < kEps) {
       const float4 p3 = P.P3[slot];
       finish_sample(P, slot, st, mk3(p3.x, p3.y, p3.z), nxt, finished);
@@ -407,7 +434,7 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
     int flags = F_PENDING;
     {
       const float v0 = Pcg::next(st), v1 = Pcg::next(st), v2 = Pcg::next(st);
-      const BsdfSample ms = MatOps<KIND>::sample(bsdf, is.wo, v0, v1, v2);
+      const BsdfSample ms = sample_bsdf_shared<KIND>(bsdf, is.wo, v0, v1, v2);
       if (ms.valid()) {
         const f3 wi = normalize(ms.wi);
         const f3 mo = is.eps_offset(wi);
@@ -693,7 +720,7 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
       // material and light-sample counts
       RCHK(cudaMemsetAsync(P.ctr + C_EXT + nxt, 0, 4, st));
       RCHK(cudaMemsetAsync(P.ctr + C_ACT + nxt, 0, 4, st));
-      RCHK(cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 5, st));  // C_SH, C_MAT x2, C_NEE x2
+      RCHK(cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 7, st));  // C_SH, C_MAT x2, C_NEE x2, C_FEXT, C_FSH
       mark();
       k_logic<<<grid, 128, 0, st>>>(P, cur);
       mark();
@@ -940,7 +967,7 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
     k_extend<false><<<grid, 128, 0, st>>>(P, cur);
     NCHK(cudaMemsetAsync(P.ctr + C_EXT + nxt, 0, 4, st));
     NCHK(cudaMemsetAsync(P.ctr + C_ACT + nxt, 0, 4, st));
-    NCHK(cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 5, st));
+    NCHK(cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 7, st));
     k_logic<<<grid, 128, 0, st>>>(P, cur);
     k_material<MAT_PHONG><<<grid, 128, 0, st>>>(P, cur);
     k_material<MAT_DISNEY12><<<grid, 128, 0, st>>>(P, cur);

@@ -102,22 +102,25 @@ TR_HD f3 xform_normal_inv(const float* inv, f3 n) {
 // Exhaustively checked against the double expression over all 2^32 inputs.
 TR_HD float slab_scale(float x) {
 #if defined(__CUDA_ARCH__)
-  uint32_t b = __float_as_uint(x);
+  const uint32_t b = __float_as_uint(x);
 #else
   uint32_t b;
   memcpy(&b, &x, 4);
 #endif
-  uint32_t mag = b & 0x7fffffffu;
-  if (mag == 0u || mag >= 0x7f800000u) return x;  // zero, inf, nan
+  const uint32_t mag = b & 0x7fffffffu;
   uint32_t k;
-  if (mag < 0x00800000u) {
-    k = mag >= 5000001u ? 1u : 0u;  // subnormal: m * 1e-7 reaches half an ulp
+  if (mag - 0x00800000u < 0x7f000000u) {
+    // normal: m = 2^23 + frac; m * 1e-7 rounds to 2 ulps from m = 15000000
+    // (frac = 6611392) on, except at m = 2^24 - 1 where the product
+    // crosses into the next binade and one ulp of the larger spacing wins
+    const uint32_t frac = b & 0x007fffffu;
+    k = (frac >= 6611392u && frac != 0x007fffffu) ? 2u : 1u;
+  } else if (mag == 0u || mag >= 0x7f800000u) {
+    return x;  // zero, inf, nan
   } else {
-    uint32_t m = (mag & 0x007fffffu) | 0x00800000u;
-    k = m >= 15000000u ? 2u : 1u;
-    if (m == 0x00ffffffu) k = 1u;  // crossing into the next binade
+    k = mag >= 5000001u ? 1u : 0u;  // subnormal: m * 1e-7 reaches half an ulp
   }
-  uint32_t r = b + k;
+  const uint32_t r = b + k;
 #if defined(__CUDA_ARCH__)
   return __uint_as_float(r);
 #else

@@ -152,27 +152,56 @@ struct Traversal {
     return false;
   }
 
-  // Returns true for ANY when occluded; for closest hit fills h and t_max.
-  static __device__ bool run(const DScene& sc, f3 o, f3 d, float t_min, float& t_max, Hit& h, int* err,
-                             VisitCount* vc = nullptr) {
+};
+
+// ---------------------------------------------------------------------------
+// Persistent traversal with dynamic fetch. Each lane runs the same per-ray
+// algorithm as Traversal::run (same order, same culling, same tests), cut
+// into steps so that a warp can keep its lanes busy: interior steps repeat
+// while any lane of the warp is at an interior node, then the lanes at
+// leaves test their primitives; when fewer than kRefill lanes still hold a
+// ray, the finished lanes take new rays from the work queue (one atomic per
+// warp). Every loop decision is warp-uniform; all 32 lanes stay in the loop
+// until the queue is exhausted, so the kernel must be launched with whole
+// warps and no lane may return early.
+
+struct StackEntry {  // one 16-byte local store per push
+  int ref, cnt;
+  float t;
+  int pad;
+};
+
+template <bool ANY, bool COUNT>
+struct TravLane {
+  static constexpr int kStack = 64;
+  f3 o, d, inv;
+  bool n0, n1, n2;
+  float t_min, t_max;
+  int cur, cnt, sp;
+  Hit h;
+  bool occluded;
+  StackEntry st[kStack];
+
+  // Starts a ray; returns false when it misses the root box (done at once).
+  __device__ __forceinline__ bool start(const DScene& sc, f3 o_, f3 d_, float tmin_, float tmax_, VisitCount& vc) {
+    o = o_;
+    d = d_;
+    t_min = tmin_;
+    t_max = tmax_;
     h.prim = -1;
+    occluded = false;
+    sp = 0;
     if (sc.root_kind == 0) return false;
-    if (COUNT) ++vc->boxes;
-    // (float)(1.0 / d) in the reference: a single division, so the double
-    // rounding equals the float division.
-    const f3 inv = mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
-    const bool n0 = inv.x < 0.0f, n1 = inv.y < 0.0f, n2 = inv.z < 0.0f;
+    if (COUNT) ++vc.boxes;
+    inv = mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    n0 = inv.x < 0.0f;
+    n1 = inv.y < 0.0f;
+    n2 = inv.z < 0.0f;
     float tmin;
-    if (!box_pass(sc.root_lo[0], sc.root_lo[1], sc.root_lo[2], sc.root_hi[0], sc.root_hi[1], sc.root_hi[2], o,
-                  inv, n0, n1, n2, tmin) ||
+    if (!box_pass(sc.root_lo[0], sc.root_lo[1], sc.root_lo[2], sc.root_hi[0], sc.root_hi[1], sc.root_hi[2], o, inv,
+                  n0, n1, n2, tmin) ||
         !(tmin < t_max))
       return false;
-    constexpr int kStack = 64;
-    int st_ref[kStack];
-    int st_cnt[kStack];
-    float st_t[kStack];
-    int sp = 0;
-    int cur, cnt;
     if (sc.root_kind == 2) {
       cur = sc.root_offset;
       cnt = sc.root_count;
@@ -180,57 +209,138 @@ struct Traversal {
       cur = 0;
       cnt = 0;
     }
-    for (;;) {
-      if (cnt == 0) {
-        const float4* np = reinterpret_cast<const float4*>(sc.nodes + cur);
-        const float4 a = ldg4(np), b = ldg4(np + 1), c = ldg4(np + 2);
-        const float4 dd = ldg4(np + 3);
-        const int4 di = make_int4(__float_as_int(dd.x), __float_as_int(dd.y), __float_as_int(dd.z),
-                                  __float_as_int(dd.w));
-        if (COUNT) vc->boxes += 2;
-        float tl, tr;
-        bool hl = box_pass(a.x, a.y, a.z, a.w, b.x, b.y, o, inv, n0, n1, n2, tl) && tl < t_max;
-        bool hr = box_pass(b.z, b.w, c.x, c.y, c.z, c.w, o, inv, n0, n1, n2, tr) && tr < t_max;
-        const int axis = di.w;
-        const bool second_near = axis == 0 ? n0 : (axis == 1 ? n1 : n2);
-        const int lref = di.x, rref = di.y;
-        const int lcnt = di.z & 0xffff, rcnt = (int)((unsigned)di.z >> 16);
-        if (hl && hr) {
-          if (sp >= kStack) {
-            atomicOr(err, 1);
-            return false;
-          }
-          if (second_near) {
-            st_ref[sp] = lref; st_cnt[sp] = lcnt; st_t[sp] = tl; ++sp;
-            cur = rref; cnt = rcnt;
-          } else {
-            st_ref[sp] = rref; st_cnt[sp] = rcnt; st_t[sp] = tr; ++sp;
-            cur = lref; cnt = lcnt;
-          }
-          continue;
-        }
-        if (hl) { cur = lref; cnt = lcnt; continue; }
-        if (hr) { cur = rref; cnt = rcnt; continue; }
-      } else {
-        for (int i = 0; i < cnt; ++i) {
-          if (COUNT) ++vc->prims;
-          if (test_slot(sc, cur + i, o, d, t_min, t_max, h)) return true;
-        }
+    return true;
+  }
+
+  // Next entry from the stack whose box entry is still before t_max;
+  // returns false when the traversal is over.
+  __device__ __forceinline__ bool pop() {
+    while (sp > 0) {
+      --sp;
+      const StackEntry e = st[sp];
+      if (e.t < t_max) {
+        cur = e.ref;
+        cnt = e.cnt;
+        return true;
       }
-      bool found = false;
-      while (sp > 0) {
-        --sp;
-        if (st_t[sp] < t_max) {
-          cur = st_ref[sp];
-          cnt = st_cnt[sp];
-          found = true;
-          break;
-        }
-      }
-      if (!found) break;
     }
     return false;
   }
+
+  // One child-pair visit at interior node `cur`; returns false when done.
+  __device__ __forceinline__ bool interior(const DScene& sc, int* err, VisitCount& vc) {
+    const float4* np = reinterpret_cast<const float4*>(sc.nodes + cur);
+    const float4 a = ldg4(np), b = ldg4(np + 1), c = ldg4(np + 2);
+    const float4 dd = ldg4(np + 3);
+    if (COUNT) vc.boxes += 2;
+    float tl, tr;
+    const bool hl = box_pass(a.x, a.y, a.z, a.w, b.x, b.y, o, inv, n0, n1, n2, tl) && tl < t_max;
+    const bool hr = box_pass(b.z, b.w, c.x, c.y, c.z, c.w, o, inv, n0, n1, n2, tr) && tr < t_max;
+    const int axis = __float_as_int(dd.w);
+    const bool second_near = axis == 0 ? n0 : (axis == 1 ? n1 : n2);
+    const int lref = __float_as_int(dd.x), rref = __float_as_int(dd.y);
+    const unsigned cc = (unsigned)__float_as_int(dd.z);
+    const int lcnt = (int)(cc & 0xffffu), rcnt = (int)(cc >> 16);
+    if (hl && hr) {
+      if (sp >= kStack) {
+        atomicOr(err, 1);
+        h.prim = -1;
+        occluded = false;
+        return false;
+      }
+      StackEntry e;
+      e.pad = 0;
+      if (second_near) {
+        e.ref = lref;
+        e.cnt = lcnt;
+        e.t = tl;
+        cur = rref;
+        cnt = rcnt;
+      } else {
+        e.ref = rref;
+        e.cnt = rcnt;
+        e.t = tr;
+        cur = lref;
+        cnt = lcnt;
+      }
+      st[sp++] = e;
+      return true;
+    }
+    if (hl) {
+      cur = lref;
+      cnt = lcnt;
+      return true;
+    }
+    if (hr) {
+      cur = rref;
+      cnt = rcnt;
+      return true;
+    }
+    return pop();
+  }
+
+  // The primitives of leaf `cur`; returns false when done.
+  __device__ __forceinline__ bool leaf(const DScene& sc, VisitCount& vc) {
+    for (int i = 0; i < cnt; ++i) {
+      if (COUNT) ++vc.prims;
+      if (Traversal<ANY, COUNT>::test_slot(sc, cur + i, o, d, t_min, t_max, h)) {
+        occluded = true;
+        return false;
+      }
+    }
+    return pop();
+  }
 };
+
+// Job: unsigned count() const; void load(unsigned i, f3& o, f3& d, float& t_min, float& t_max);
+//      void store(unsigned i, const Hit& h, float t_max, bool occluded).
+template <bool ANY, bool COUNT, int kRefill, class Job>
+__device__ __forceinline__ void persistent_traverse(const DScene& sc, Job& job, unsigned int* fetch, int* err,
+                                                    VisitCount& vc) {
+  const unsigned int n = job.count();
+  const unsigned int lane = threadIdx.x & 31u;
+  const unsigned int below = (1u << lane) - 1u;
+  TravLane<ANY, COUNT> L;
+  unsigned int item = 0;
+  bool live = false, exhausted = false;
+  for (;;) {
+    const unsigned int need = __ballot_sync(0xffffffffu, !live && !exhausted);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned int base = 0;
+      if ((int)lane == leader) base = atomicAdd(fetch, (unsigned int)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (!live && !exhausted) {
+        item = base + (unsigned int)__popc(need & below);
+        if (item < n) {
+          f3 o, d;
+          float tmin, tmax;
+          job.load(item, o, d, tmin, tmax);
+          live = L.start(sc, o, d, tmin, tmax, vc);
+          if (!live) job.store(item, L.h, L.t_max, false);
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, live)) {
+      if (__all_sync(0xffffffffu, exhausted)) break;
+      continue;
+    }
+    for (;;) {
+      while (__any_sync(0xffffffffu, live && L.cnt == 0)) {
+        if (live && L.cnt == 0) {
+          live = L.interior(sc, err, vc);
+          if (!live) job.store(item, L.h, L.t_max, L.occluded);
+        }
+      }
+      if (live) {
+        live = L.leaf(sc, vc);
+        if (!live) job.store(item, L.h, L.t_max, L.occluded);
+      }
+      if (__popc(__ballot_sync(0xffffffffu, live)) < kRefill) break;
+    }
+  }
+}
 
 }  // namespace trg
