@@ -184,6 +184,23 @@ const char* tr_ctx_last_error(const tr_ctx* ctx);
 void* tr_ctx_stream(tr_ctx* ctx);
 tr_status tr_synchronize(tr_ctx* ctx);
 
+/* Launch tuning of a context. Replaces PTRendererParams::worker_count and
+ * task_tile_size, the reference's only performance knobs
+ * (src/factory/renderer.hpp:13-14); results never depend on it.
+ *  - trav_refill_lanes (1..32): a traversal warp refills its finished lanes
+ *    once fewer than this many lanes still trace;
+ *  - trav_blocks_per_sm: resident 128-thread blocks per SM of the
+ *    persistent traversal kernels (0: as many as fit);
+ *  - shade_blocks_per_sm: 128-thread blocks per SM of the shading kernels
+ *    (grid-stride loops). */
+typedef struct tr_tuning {
+  int32_t trav_refill_lanes;
+  int32_t trav_blocks_per_sm;
+  int32_t shade_blocks_per_sm;
+} tr_tuning;
+tr_status tr_ctx_set_tuning(tr_ctx* ctx, const tr_tuning* t);
+tr_status tr_ctx_get_tuning(const tr_ctx* ctx, tr_tuning* t);
+
 /* Builds the scene on the device: primitive tables, materials, lights and the
  * binned-SAH BVH. Replaces create_bvh_accel + BVHAccel::build +
  * create_general_scene (src/accelerator/bvh.cpp:78-105,315;

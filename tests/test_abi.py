@@ -56,3 +56,8 @@ def test_status_strings():
     L = lib()
     for s in range(9):
         assert L.tr_status_string(s)
+
+
+def test_tuning_struct_layout():
+    from tracer_gb300.abi import TrTuning
+    assert ctypes.sizeof(TrTuning) == 12

@@ -129,3 +129,18 @@ def test_visit_counts_match_oracle(gpu):
     # traces a subset of the reference's shadow rays with the same result.
     assert 0 < st.shadow_rays <= len(ar)
     assert st.any_boxes <= an.sum() and st.any_prims <= ap.sum()
+
+
+def test_tuning_does_not_change_results(gpu):
+    """Launch tuning (grid sizes, lane refill threshold) never changes the film."""
+    sc, cam, filt, par = scenes.disney_grid(48, 32, 2)
+    gpu.upload(sc)
+    base, _ = gpu.render(cam, filt, par)
+    old = gpu.tuning()
+    try:
+        for refill, tb, sb in ((1, 1, 1), (32, 3, 40), (7, 0, 9)):
+            gpu.set_tuning(refill, tb, sb)
+            out, _ = gpu.render(cam, filt, par)
+            assert np.array_equal(out.view(np.uint32), base.view(np.uint32))
+    finally:
+        gpu.set_tuning(old.trav_refill_lanes, old.trav_blocks_per_sm, old.shade_blocks_per_sm)

@@ -98,6 +98,11 @@ class TrStats(C.Structure):
                 ("any_boxes", C.c_uint64), ("any_prims", C.c_uint64)]
 
 
+class TrTuning(C.Structure):
+    _fields_ = [("trav_refill_lanes", C.c_int32), ("trav_blocks_per_sm", C.c_int32),
+                ("shade_blocks_per_sm", C.c_int32)]
+
+
 def ptr(a: np.ndarray | None, ctype):
     if a is None:
         return C.cast(None, C.POINTER(ctype))

@@ -9,6 +9,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -234,23 +235,23 @@ struct BatchJob {
 };
 
 template <bool ANY>
-__global__ void __launch_bounds__(128) k_trace_batch(DScene sc, BatchJob job, unsigned int* fetch, int* err) {
+__global__ void __launch_bounds__(128) k_trace_batch(DScene sc, BatchJob job, unsigned int* fetch, int* err,
+                                                    int refill) {
   VisitCount vc;
-  persistent_traverse<ANY, false, 20>(sc, job, fetch, err, vc);
+  persistent_traverse<ANY, false>(sc, job, fetch, err, vc, refill);
 }
 
-// Resident blocks of a persistent traversal kernel (whole device).
-template <bool ANY>
-static int trace_grid(int device) {
-  static int per_sm[2] = {0, 0};
-  if (!per_sm[ANY]) {
-    int b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace_batch<ANY>, 128, 0) != cudaSuccess || b <= 0) b = 4;
-    per_sm[ANY] = b;
-  }
+int traversal_grid(const tr_ctx* ctx, const void* kernel) {
   int sms = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  return std::max(sms, 1) * per_sm[ANY];
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  int per_sm = ctx->tune.trav_blocks_per_sm;
+  if (per_sm <= 0) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0) != cudaSuccess || per_sm <= 0) {
+      cudaGetLastError();
+      per_sm = 4;
+    }
+  }
+  return std::max(sms, 1) * per_sm;
 }
 
 }  // namespace trg
@@ -322,6 +323,21 @@ void tr_ctx_destroy(tr_ctx* ctx) {
 
 const char* tr_ctx_last_error(const tr_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 void* tr_ctx_stream(tr_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+tr_status tr_ctx_set_tuning(tr_ctx* ctx, const tr_tuning* t) {
+  if (!ctx || !t) return TR_ERR_ARG;
+  if (t->trav_refill_lanes < 1 || t->trav_refill_lanes > 32 || t->trav_blocks_per_sm < 0 ||
+      t->trav_blocks_per_sm > 64 || t->shade_blocks_per_sm < 1 || t->shade_blocks_per_sm > 64)
+    return set_err(ctx, TR_ERR_ARG, "tuning out of range");
+  ctx->tune = *t;
+  return TR_OK;
+}
+
+tr_status tr_ctx_get_tuning(const tr_ctx* ctx, tr_tuning* t) {
+  if (!ctx || !t) return TR_ERR_ARG;
+  *t = ctx->tune;
+  return TR_OK;
+}
 
 tr_status tr_synchronize(tr_ctx* ctx) {
   if (!ctx) return TR_ERR_ARG;
@@ -532,8 +548,9 @@ tr_status tr_trace_closest_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, int3
   if (((uintptr_t)d_rays & 15u) != 0) return set_err(ctx, TR_ERR_ARG, "ray buffer must be 16-byte aligned");
   TR_CUDA(ctx, cudaMemsetAsync(ctx->d_err.as<int>() + 1, 0, sizeof(int), ctx->stream));  // fetch position
   const BatchJob job{reinterpret_cast<const float4*>(d_rays), (unsigned int)n, d_prim, d_t, nullptr};
-  k_trace_batch<false><<<trace_grid<false>(ctx->device), 128, 0, ctx->stream>>>(
-      ctx->dsc, job, reinterpret_cast<unsigned int*>(ctx->d_err.as<int>() + 1), ctx->d_err.as<int>());
+  k_trace_batch<false><<<traversal_grid(ctx, (const void*)k_trace_batch<false>), 128, 0, ctx->stream>>>(
+      ctx->dsc, job, reinterpret_cast<unsigned int*>(ctx->d_err.as<int>() + 1), ctx->d_err.as<int>(),
+      ctx->tune.trav_refill_lanes);
   TR_CUDA(ctx, cudaGetLastError());
   return TR_OK;
 }
@@ -546,8 +563,9 @@ tr_status tr_trace_any_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, uint8_t*
   if (((uintptr_t)d_rays & 15u) != 0) return set_err(ctx, TR_ERR_ARG, "ray buffer must be 16-byte aligned");
   TR_CUDA(ctx, cudaMemsetAsync(ctx->d_err.as<int>() + 1, 0, sizeof(int), ctx->stream));  // fetch position
   const BatchJob job{reinterpret_cast<const float4*>(d_rays), (unsigned int)n, nullptr, nullptr, d_hit};
-  k_trace_batch<true><<<trace_grid<true>(ctx->device), 128, 0, ctx->stream>>>(
-      ctx->dsc, job, reinterpret_cast<unsigned int*>(ctx->d_err.as<int>() + 1), ctx->d_err.as<int>());
+  k_trace_batch<true><<<traversal_grid(ctx, (const void*)k_trace_batch<true>), 128, 0, ctx->stream>>>(
+      ctx->dsc, job, reinterpret_cast<unsigned int*>(ctx->d_err.as<int>() + 1), ctx->d_err.as<int>(),
+      ctx->tune.trav_refill_lanes);
   TR_CUDA(ctx, cudaGetLastError());
   return TR_OK;
 }

@@ -64,11 +64,14 @@ struct tr_ctx {
   trg::DevBuf d_rays, d_out0, d_out1, d_err;
   std::atomic<int> cancel{0};
   trg::RenderBuffers* rb = nullptr;
+  tr_tuning tune{20, 0, 16};
 };
 
 namespace trg {
 tr_status cuda_fail(tr_ctx* ctx, cudaError_t e, const char* what);
 tr_status set_err(tr_ctx* ctx, tr_status s, const std::string& msg);
 tr_status upload_device_tables(tr_ctx* ctx);
+// Grid of a persistent traversal kernel: SMs x resident blocks (tuned or as many as fit).
+int traversal_grid(const tr_ctx* ctx, const void* kernel);
 void release_render(tr_ctx* ctx);
 }  // namespace trg

@@ -73,6 +73,7 @@ struct Launch {
   unsigned seed_base;
   float filter_radius, filter_alpha, filter_exp;
   int fp64;
+  int refill;                      // traversal lane-refill threshold (tr_tuning)
   float4 *P0, *P1, *P2, *P3, *P4;  // cont o|flags, cont d|depth, coef|sample, L|px, coef_prev|py
   unsigned long long* rng;
   float4 *M0, *M1, *M2;  // mis o|bsdf_pdf, mis d|abs_cos, bsdf_f
@@ -269,14 +270,12 @@ struct ShadowJob {
   }
 };
 
-constexpr int kRefillLanes = 20;  // refill a warp's finished lanes once fewer than this many trace
-
 template <bool COUNT>
 __global__ void __launch_bounds__(128) k_extend(Launch P, int cur) {
   ExtendJob job{P, cur};
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.stats + 1, (unsigned long long)job.count());
   VisitCount vc;
-  persistent_traverse<false, COUNT, kRefillLanes>(P.sc, job, P.ctr + C_FEXT, (int*)(P.ctr + C_ERR), vc);
+  persistent_traverse<false, COUNT>(P.sc, job, P.ctr + C_FEXT, (int*)(P.ctr + C_ERR), vc, P.refill);
   if (COUNT) {
     count_add(P.stats + 4, vc.boxes);
     count_add(P.stats + 5, vc.prims);
@@ -288,7 +287,7 @@ __global__ void __launch_bounds__(128) k_shadow(Launch P) {
   ShadowJob job{P};
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.stats + 2, (unsigned long long)job.count());
   VisitCount vc;
-  persistent_traverse<true, COUNT, kRefillLanes>(P.sc, job, P.ctr + C_FSH, (int*)(P.ctr + C_ERR), vc);
+  persistent_traverse<true, COUNT>(P.sc, job, P.ctr + C_FSH, (int*)(P.ctr + C_ERR), vc, P.refill);
   if (COUNT) {
     count_add(P.stats + 6, vc.boxes);
     count_add(P.stats + 7, vc.prims);
@@ -661,7 +660,10 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
   if (sms <= 0) sms = 1;
-  const int grid = sms * 16, grid_init = sms * 8;
+  const int grid = sms * ctx->tune.shade_blocks_per_sm, grid_init = sms * 8;
+  const int grid_ext = traversal_grid(ctx, (const void*)k_extend<false>);
+  const int grid_sh = traversal_grid(ctx, (const void*)k_shadow<false>);
+  P.refill = ctx->tune.trav_refill_lanes;
 
   ctx->cancel.store(0);
   cudaEvent_t e0, e1, chk;
@@ -713,8 +715,8 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
     for (int c = 0; c < chunk && it < max_iters; ++c, ++it) {
       const int cur = (int)(it & 1), nxt = cur ^ 1;
       mark();
-      if (count) k_extend<true><<<grid, 128, 0, st>>>(P, cur);
-      else k_extend<false><<<grid, 128, 0, st>>>(P, cur);
+      if (count) k_extend<true><<<grid_ext, 128, 0, st>>>(P, cur);
+      else k_extend<false><<<grid_ext, 128, 0, st>>>(P, cur);
       mark();
       // next iteration's extend and live counts; this iteration's shadow,
       // material and light-sample counts
@@ -732,8 +734,8 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
       mark();
       k_nee<MAT_DISNEY12><<<grid, 128, 0, st>>>(P);
       mark();
-      if (count) k_shadow<true><<<grid, 128, 0, st>>>(P);
-      else k_shadow<false><<<grid, 128, 0, st>>>(P);
+      if (count) k_shadow<true><<<grid_sh, 128, 0, st>>>(P);
+      else k_shadow<false><<<grid_sh, 128, 0, st>>>(P);
       mark();
     }
     RCHK(cudaGetLastError());
@@ -946,7 +948,10 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
   if (sms <= 0) sms = 1;
-  const int grid = sms * 16, grid_init = sms * 8;
+  const int grid = sms * ctx->tune.shade_blocks_per_sm, grid_init = sms * 8;
+  const int grid_ext = traversal_grid(ctx, (const void*)k_extend<false>);
+  const int grid_sh = traversal_grid(ctx, (const void*)k_shadow<false>);
+  P.refill = ctx->tune.trav_refill_lanes;
 #define NCHK(call)                                      \
   do {                                                  \
     cudaError_t e_ = (call);                            \
@@ -964,7 +969,7 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   const long long iters = (long long)prm->spp * (prm->max_depth + 2) + 4;
   for (long long it = 0; it < iters; ++it) {
     const int cur = (int)(it & 1), nxt = cur ^ 1;
-    k_extend<false><<<grid, 128, 0, st>>>(P, cur);
+    k_extend<false><<<grid_ext, 128, 0, st>>>(P, cur);
     NCHK(cudaMemsetAsync(P.ctr + C_EXT + nxt, 0, 4, st));
     NCHK(cudaMemsetAsync(P.ctr + C_ACT + nxt, 0, 4, st));
     NCHK(cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 7, st));
@@ -973,7 +978,7 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
     k_material<MAT_DISNEY12><<<grid, 128, 0, st>>>(P, cur);
     k_nee<MAT_PHONG><<<grid, 128, 0, st>>>(P);
     k_nee<MAT_DISNEY12><<<grid, 128, 0, st>>>(P);
-    k_shadow<false><<<grid, 128, 0, st>>>(P);
+    k_shadow<false><<<grid_sh, 128, 0, st>>>(P);
   }
   NCHK(cudaGetLastError());
   NCHK(cudaStreamSynchronize(st));

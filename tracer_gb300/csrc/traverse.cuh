@@ -159,7 +159,7 @@ struct Traversal {
 // algorithm as Traversal::run (same order, same culling, same tests), cut
 // into steps so that a warp can keep its lanes busy: interior steps repeat
 // while any lane of the warp is at an interior node, then the lanes at
-// leaves test their primitives; when fewer than kRefill lanes still hold a
+// leaves test their primitives; when fewer than `refill` lanes still hold a
 // ray, the finished lanes take new rays from the work queue (one atomic per
 // warp). Every loop decision is warp-uniform; all 32 lanes stay in the loop
 // until the queue is exhausted, so the kernel must be launched with whole
@@ -294,9 +294,9 @@ struct TravLane {
 
 // Job: unsigned count() const; void load(unsigned i, f3& o, f3& d, float& t_min, float& t_max);
 //      void store(unsigned i, const Hit& h, float t_max, bool occluded).
-template <bool ANY, bool COUNT, int kRefill, class Job>
+template <bool ANY, bool COUNT, class Job>
 __device__ __forceinline__ void persistent_traverse(const DScene& sc, Job& job, unsigned int* fetch, int* err,
-                                                    VisitCount& vc) {
+                                                    VisitCount& vc, int refill) {
   const unsigned int n = job.count();
   const unsigned int lane = threadIdx.x & 31u;
   const unsigned int below = (1u << lane) - 1u;
@@ -338,7 +338,7 @@ __device__ __forceinline__ void persistent_traverse(const DScene& sc, Job& job, 
         live = L.leaf(sc, vc);
         if (!live) job.store(item, L.h, L.t_max, L.occluded);
       }
-      if (__popc(__ballot_sync(0xffffffffu, live)) < kRefill) break;
+      if (__popc(__ballot_sync(0xffffffffu, live)) < refill) break;
     }
   }
 }

@@ -11,7 +11,7 @@ import os
 import numpy as np
 
 from . import build as _build
-from .abi import (NODE_DTYPE, RAY_DTYPE, TR_OK, TrBvhNode32, TrCamera, TrFilter, TrRay, TrRenderParams,
+from .abi import (NODE_DTYPE, RAY_DTYPE, TR_OK, TrBvhNode32, TrCamera, TrFilter, TrRay, TrRenderParams, TrTuning,
                   TrSceneDesc, TrStats)
 
 _lib = None
@@ -67,6 +67,10 @@ def lib() -> C.CDLL:
     L.tr_render.restype = st
     L.tr_render.argtypes = [vp, C.POINTER(TrCamera), C.POINTER(TrFilter), C.POINTER(TrRenderParams),
                             C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(TrStats)]
+    L.tr_ctx_set_tuning.restype = st
+    L.tr_ctx_set_tuning.argtypes = [vp, C.POINTER(TrTuning)]
+    L.tr_ctx_get_tuning.restype = st
+    L.tr_ctx_get_tuning.argtypes = [vp, C.POINTER(TrTuning)]
     L.tr_render_dev.restype = st
     L.tr_render_dev.argtypes = [vp, C.POINTER(TrCamera), C.POINTER(TrFilter), C.POINTER(TrRenderParams),
                                 vp, vp, C.POINTER(TrStats)]
@@ -169,6 +173,22 @@ class GpuContext:
                                  None, C.byref(stats))
         self._check(s)
         return out, stats
+
+    def tuning(self) -> TrTuning:
+        t = TrTuning()
+        self._check(self.L.tr_ctx_get_tuning(self.h, C.byref(t)))
+        return t
+
+    def set_tuning(self, refill: int | None = None, trav_blocks_per_sm: int | None = None,
+                   shade_blocks_per_sm: int | None = None) -> None:
+        t = self.tuning()
+        if refill is not None:
+            t.trav_refill_lanes = refill
+        if trav_blocks_per_sm is not None:
+            t.trav_blocks_per_sm = trav_blocks_per_sm
+        if shade_blocks_per_sm is not None:
+            t.shade_blocks_per_sm = shade_blocks_per_sm
+        self._check(self.L.tr_ctx_set_tuning(self.h, C.byref(t)))
 
     def render_dev(self, cam: TrCamera, filt: TrFilter, params: TrRenderParams, d_out: int, fp64: bool = False):
         stats = TrStats()
