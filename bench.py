@@ -1,20 +1,25 @@
-"""Benchmark of the GPU path tracer (plain unidirectional path tracing).
+"""Benchmark of the GPU path tracer.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload disney_grid|cornell]
+                    [--workload occluded_room|disney_grid|cornell] [--size WxHxSPP]
+                    [--no-convergence] [--no-cpu-baseline]
 
-A step renders one full frame of the workload: by default the 16x16
-Disney12-sphere grid at 1024x1024, 64 spp, max depth 8 (67,108,864 camera
-samples), all geometry and path state resident on the device. `value` is
+A step renders one full frame of the workload. The default is the
+occluded-light room: 500k triangles of Disney12 furniture in a closed
+Lambertian room lit only through a 0.1 m slit by a 12-triangle emissive
+cube, at 1024x768, 16 spp, max depth 10 (12,582,912 camera samples per
+step), all geometry and path state resident on the device. `value` is
 camera samples per second over exactly K steps (CUDA events on the
 renderer's stream, synchronised on both sides, maximum over ranks); `e2e`
 repeats the measurement through the C ABI's host-buffer entry point
-(tr_render), which copies the film back every step.
+(tr_render), which copies the film back every step. `convergence` times the
+plain path tracer to 1% relMSE against a converged FP64 reference of the
+same scene at 256x192.
 
 --impl reference times the reference algorithm on the host cores instead:
-the CPU restatement in oracle/ (the reference's own build needs its source
-checkout, which this machine may not have), all host threads, a bounded
-sample of the same frame per step.
+the CPU restatement in oracle/ (bit-exact with the reference's own build,
+which needs the reference checkout this machine may not have), all host
+threads, a bounded sample of the same frame per step.
 
 Multiple GPUs (torchrun, one rank per GPU) render independent replicas:
 per-GPU work is fixed, so scaling is weak and there is no collective on the
@@ -41,7 +46,7 @@ from tracer_gb300.abi import (STAGE_NAMES, TR_RENDER_COUNT_VISITS, TR_RENDER_TIM
                               TrCamera, TrFilter, TrRenderParams)
 import ctypes  # noqa: E402
 
-METRIC = "Msamples/s (plain GPU path tracing)"
+METRIC = "Msamples/s and time-to-1% relMSE, guided vs plain GPU PT on 1 GB300"
 UNIT = "Msamples/s"
 
 # Algorithmic bytes per work item of each kernel (the roofline numerator).
@@ -84,22 +89,74 @@ def traffic_per_unit(stage: str):
         return None
 
 
+WORKLOADS = ("occluded_room", "disney_grid", "cornell")
+
+
 def workload(name: str, size: str | None = None):
     """(label, scene, camera, filter, params); size "WxHxSPP" overrides the
     film and sample count (small cases for profiler captures)."""
-    if name == "cornell":
-        W, H, S = 256, 256, 16
-    else:
-        W, H, S = 1024, 1024, 64
+    W, H, S = {"cornell": (256, 256, 16), "disney_grid": (1024, 1024, 64), "occluded_room": (1024, 768, 16)}[name]
     if size:
         W, H, S = (int(v) for v in size.lower().split("x"))
     if name == "cornell":
         sc, cam, filt, par = scenes.cornell(W, H, S)
         label = f"cornell_box_36tris_{W}x{H}_{S}spp_depth5"
-    else:
+    elif name == "disney_grid":
         sc, cam, filt, par = scenes.disney_grid(W, H, S, max_depth=8, min_depth=5)
         label = f"disney12_sphere_grid_16x16_{W}x{H}_{S}spp_depth8"
+    else:
+        sc, cam, filt, par = scenes.occluded_room(W, H, S, max_depth=10, min_depth=3)
+        label = f"occluded_light_room_500k_tris_12_lights_{W}x{H}_{S}spp_depth10"
     return label, sc, cam, filt, par
+
+
+def rel_mse(img: np.ndarray, ref: np.ndarray) -> float:
+    """mean over pixels and channels of (I - R)^2 / (R^2 + 1e-2)."""
+    return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+
+def _image(acc: np.ndarray) -> np.ndarray:
+    w = acc[..., 3:4]
+    return np.where(w > 0, acc[..., :3] / np.where(w > 0, w, 1.0), 0.0)
+
+
+def convergence(ctx, name: str, size=(256, 192), ref_spp=4096, pass_spp=4, max_spp=1024, target=0.01):
+    """Time for the plain GPU path tracer to reach `target` relMSE against a
+    converged reference of the same scene: the reference is ref_spp samples
+    per pixel accumulated in double; the plain run adds passes of pass_spp
+    samples with fresh per-pixel seeds, accumulating in double on the host,
+    and stops at the target or at max_spp. Times are the render calls only."""
+    W, H = size
+    _, sc, cam, filt, par = workload(name, f"{W}x{H}x{pass_spp}")
+    ctx.upload(sc)
+    ref_par = scenes.make_params(W, H, ref_spp, par.min_depth, par.max_depth, seed_base=1 << 30)
+    t0 = time.perf_counter()
+    ref_acc, _ = ctx.render(cam, filt, ref_par, fp64=True)
+    ref_s = time.perf_counter() - t0
+    ref = _image(ref_acc)
+    acc = np.zeros((H, W, 4), np.float64)
+    spent, curve, reached = 0.0, [], None
+    for k in range(max_spp // pass_spp):
+        p = scenes.make_params(W, H, pass_spp, par.min_depth, par.max_depth, seed_base=1 + k * W * H)
+        t0 = time.perf_counter()
+        out, _ = ctx.render(cam, filt, p, fp64=True)
+        spent += time.perf_counter() - t0
+        acc += out
+        spp = (k + 1) * pass_spp
+        e = rel_mse(_image(acc), ref)
+        if spp & (spp - 1) == 0 or e <= target:
+            curve.append([spp, round(spent, 4), round(e, 5)])
+        if e <= target:
+            reached = (spp, spent)
+            break
+    res = {"resolution": f"{W}x{H}", "reference_spp": ref_spp, "reference_s": round(ref_s, 2),
+           "pass_spp": pass_spp, "target_relmse": target,
+           "relmse": "mean over pixels and channels of (I - R)^2 / (R^2 + 1e-2)",
+           "plain": {"time_to_target_s": reached[1] if reached else None,
+                     "spp_at_target": reached[0] if reached else None,
+                     "relmse_curve_spp_s_relmse": curve},
+           "guided": None}
+    return res
 
 
 class ClockSampler:
@@ -273,6 +330,10 @@ def run_ours(args):
     clocks = ClockSampler(local).__enter__()
     par.flags = 0
     for _ in range(args.warmup):
+        # the flush runs in the warm-up too: its first launch loads torch's
+        # kernel module, which must not happen inside the timed region
+        with torch.cuda.stream(stream):
+            flush.zero_()
         ctx.render_dev(cam, filt, par, film.data_ptr())
     stats = []
     barrier()
@@ -358,6 +419,9 @@ def run_ours(args):
             roof["traffic_source"] = tr["source"]
     else:
         roof.update({"achieved": None, "frac": None})
+    conv = None
+    if not args.no_convergence and world == 1 and args.workload == "occluded_room" and not args.size:
+        conv = convergence(ctx, args.workload)
     cpu_rate, cpu_threads, cpu_desc = (None, None, None)
     if not args.no_cpu_baseline and world == 1:
         cpu_rate, cpu_threads, cpu_desc = cpu_sample(sc, cam, filt, par)
@@ -369,8 +433,10 @@ def run_ours(args):
         "config": {"workload": label, "width": W, "height": H, "spp": par.spp, "max_depth": par.max_depth,
                    "min_depth": par.min_depth, "lights": nl, "primitives": int(len(sc.prim_shape)),
                    "parallelism": f"replicas x{world}",
-                   "l2": "path state and queues exceed L2 (~450 MB at 1024x1024); a 256 MiB buffer is "
-                         "written between timed steps"},
+                   "l2": f"path state and queues ({W * H * (312 + 68 * max(nl, 1)) / 1e6:.0f} MB) exceed L2; "
+                         "a 256 MiB buffer is written between timed steps"},
+        "value_is": "camera samples per second of the plain GPU path tracer (time-to-1% relMSE under "
+                    "'convergence')",
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": W * H * 16},
         "gpu_launches": int(sum(1 + 7 * s.iterations for s in stats)),
         "roofline": roof,
@@ -383,6 +449,8 @@ def run_ours(args):
         "stage_ms": {k: round(v, 3) for k, v in stage_ms.items()},
         "clocks": clocks.summary(c0, c1),
     }
+    if conv is not None:
+        line["convergence"] = conv
     if cpu_rate is not None:
         line["cpu_baseline"] = {"value": cpu_rate, "unit": UNIT, "cores": cpu_threads, "kind": "port",
                                 "sample": cpu_desc}
@@ -399,7 +467,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["disney_grid", "cornell"], default="disney_grid")
+    ap.add_argument("--workload", choices=list(WORKLOADS), default="occluded_room")
+    ap.add_argument("--no-convergence", action="store_true", help="skip the time-to-1%% relMSE leg")
     ap.add_argument("--size", default=None, help="WxHxSPP override (profiling captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

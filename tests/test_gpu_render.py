@@ -144,3 +144,16 @@ def test_tuning_does_not_change_results(gpu):
             assert np.array_equal(out.view(np.uint32), base.view(np.uint32))
     finally:
         gpu.set_tuning(old.trav_refill_lanes, old.trav_blocks_per_sm, old.shade_blocks_per_sm)
+
+
+def test_occluded_room_small(gpu):
+    """The occluded-light room (12 emissive triangles, Disney furniture,
+    min depth 3 with Russian roulette, max depth 10) at 20k triangles."""
+    sc, cam, filt, par = scenes.occluded_room(64, 48, 4, n_tris=20000)
+    orc = oracle.Oracle(sc, "port")
+    orc.set_camera(cam, filt)
+    ref = orc.render(par)
+    gpu.upload(sc)
+    out, stats = gpu.render(cam, filt, par)
+    assert stats.samples == 64 * 48 * 4
+    _compare(out, ref, 0.8)

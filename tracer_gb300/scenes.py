@@ -67,6 +67,23 @@ def fixed_normal(n) -> np.ndarray:
     raise ValueError(f"no fixed point for normal {n}")
 
 
+def settle_normals(n: np.ndarray) -> np.ndarray:
+    """Vectorised fixed_normal: each row normalised, then iterated to a fixed
+    point of the reference's normalize (rows caught in a 2-cycle get an ulp
+    nudge, as fixed_normal does)."""
+    v = ref_normalize(np.asarray(n, dtype=np.float64).astype(np.float32))
+    for attempt in range(64):
+        for _ in range(8):
+            w = ref_normalize(v)
+            if np.array_equal(w.view(np.uint32), v.view(np.uint32)):
+                return v
+            v = w
+        bad = np.nonzero((ref_normalize(v).view(np.uint32) != v.view(np.uint32)).any(-1))[0]
+        k = attempt % 3
+        v[bad, k] = np.nextafter(v[bad, k], np.float32(np.inf) if attempt % 2 else np.float32(-np.inf))
+    raise ValueError("normals without a fixed point")
+
+
 def make_rays(o: np.ndarray, d: np.ndarray, t_min, t_max) -> np.ndarray:
     """Rays through the reference Ray constructor (direction normalised in double)."""
     n = len(o)
@@ -143,6 +160,23 @@ class _Builder:
         self.prim_mat.append(mat)
         self.prim_em.append((0, 0, 0))
         return len(self.prim_shape) - 1
+
+    def mesh(self, tris: np.ndarray, normals: np.ndarray, mat: int):
+        """Bulk triangles: tris (T, 3, 3) positions, normals (T, 3, 3) per
+        vertex (settled to fixed points of the reference normalize)."""
+        T = len(tris)
+        if T == 0:
+            return
+        base = len(self.pos)
+        self.pos.extend(np.asarray(tris, np.float32).reshape(-1, 3) + np.float32(0))
+        self.nrm.extend(settle_normals(np.asarray(normals).reshape(-1, 3)))
+        uv = np.tile(np.array([[0, 0], [1, 0], [1, 1]], np.float32), (T, 1))
+        self.uv.extend(uv)
+        first = len(self.idx)
+        self.idx.extend((base + 3 * np.arange(T)[:, None] + np.arange(3)[None, :]).tolist())
+        self.prim_shape.extend(range(first, first + T))
+        self.prim_mat.extend([mat] * T)
+        self.prim_em.extend([(0, 0, 0)] * T)
 
     def finish(self, max_leaf_prims: int) -> SceneBuffers:
         def arr(x, shape, dt):
@@ -359,3 +393,123 @@ def unpack_view(d, prefix: str = ""):
     par = make_params(int(p[0]), int(p[1]), int(p[2]), int(p[3]), int(p[4]), seed_base=int(p[6]),
                       direct_light_sample_num=int(p[5]))
     return cam, make_filter(float(f[0]), float(f[1])), par
+
+
+def _grid_box(center, size, rot_y, k):
+    """Box tessellated into k x k quads per face: (12 k^2, 3, 3) triangles
+    with outward winding, and their normals."""
+    c = np.asarray(center, np.float64)
+    h = np.asarray(size, np.float64) / 2
+    cs, sn = math.cos(rot_y), math.sin(rot_y)
+    R = np.array([[cs, 0, sn], [0, 1, 0], [-sn, 0, cs]])
+    t = np.linspace(-1.0, 1.0, k + 1)
+    tris, nrms = [], []
+    for axis in range(3):
+        u, v = (axis + 1) % 3, (axis + 2) % 3
+        for sgn in (-1.0, 1.0):
+            P = np.zeros((k + 1, k + 1, 3))
+            P[..., axis] = sgn
+            P[..., u] = t[:, None]
+            P[..., v] = t[None, :]
+            P = c + (P * h) @ R.T
+            a, b, cc, d = P[:-1, :-1], P[1:, :-1], P[1:, 1:], P[:-1, 1:]
+            if sgn > 0:
+                q = np.concatenate([np.stack([a, b, cc], -2), np.stack([a, cc, d], -2)], 0)
+            else:
+                q = np.concatenate([np.stack([a, cc, b], -2), np.stack([a, d, cc], -2)], 0)
+            q = q.reshape(-1, 3, 3)
+            n = np.zeros(3)
+            n[axis] = sgn
+            tris.append(q)
+            nrms.append(np.broadcast_to(R @ n, q.shape))
+    return np.concatenate(tris), np.concatenate(nrms)
+
+
+def _cylinder(center, radius, height, segs, rings):
+    """Upright capped cylinder: side 2 * segs * rings triangles with radial
+    normals, two caps of segs triangles."""
+    c = np.asarray(center, np.float64)
+    th = np.linspace(0, 2 * math.pi, segs + 1)
+    y = np.linspace(0, height, rings + 1)
+    ring = np.stack([np.cos(th), np.zeros_like(th), np.sin(th)], -1)  # (segs+1, 3)
+    P = c + radius * ring[None, :, :] + y[:, None, None] * np.array([0, 1, 0])
+    N = np.broadcast_to(ring[None], P.shape)
+    a, b, cc, d = P[:-1, :-1], P[:-1, 1:], P[1:, 1:], P[1:, :-1]
+    na, nb, nc, nd = N[:-1, :-1], N[:-1, 1:], N[1:, 1:], N[1:, :-1]
+    # outward winding: (a, d, c) and (a, c, b) have cross pointing along the radial normal
+    side = np.concatenate([np.stack([a, d, cc], -2), np.stack([a, cc, b], -2)], 0).reshape(-1, 3, 3)
+    sn = np.concatenate([np.stack([na, nd, nc], -2), np.stack([na, nc, nb], -2)], 0).reshape(-1, 3, 3)
+    top_c = c + np.array([0, height, 0])
+    r0, r1 = P[-1, :-1], P[-1, 1:]
+    top = np.stack([np.broadcast_to(top_c, r0.shape), r1, r0], -2)
+    b0, b1 = P[0, :-1], P[0, 1:]
+    bot = np.stack([np.broadcast_to(c, b0.shape), b0, b1], -2)
+    tris = np.concatenate([side, top, bot])
+    nrms = np.concatenate([sn, np.broadcast_to([0.0, 1.0, 0.0], top.shape),
+                           np.broadcast_to([0.0, -1.0, 0.0], bot.shape)])
+    return tris, nrms
+
+
+def occluded_room(width=1024, height=768, spp=16, max_depth=10, min_depth=3, n_tris=500_000, seed=0):
+    """The occluded-light room: a closed 8 x 4 x 6 m room (x in [-4, 4],
+    y in [0, 4], z in [-3, 3]) of Lambertian walls (albedo 0.7). The only
+    light is a 3 m emissive cube (12 triangles, Le 50) outside the +x wall,
+    seen from inside through a 0.1 m x 3 m slit in that wall. n_tris
+    triangles of furniture (tessellated boxes and cylinders on the floor),
+    each piece a Disney12 material with roughness uniform in [0.05, 1].
+    Camera near the -x wall looking toward the slit, 60 degree fov."""
+    rng = np.random.default_rng(seed)
+    b = _Builder()
+    wall = b.material(lambert((0.7, 0.7, 0.7)))
+    X, Y, Z = 4.0, 4.0, 3.0
+    b.quad((-X, 0, -Z), (X, 0, -Z), (X, 0, Z), (-X, 0, Z), (0, 1, 0), wall)         # floor
+    b.quad((-X, Y, -Z), (X, Y, -Z), (X, Y, Z), (-X, Y, Z), (0, -1, 0), wall)         # ceiling
+    b.quad((-X, 0, -Z), (X, 0, -Z), (X, Y, -Z), (-X, Y, -Z), (0, 0, 1), wall)        # back (z = -3)
+    b.quad((-X, 0, Z), (X, 0, Z), (X, Y, Z), (-X, Y, Z), (0, 0, -1), wall)           # front (z = +3)
+    b.quad((-X, 0, -Z), (-X, Y, -Z), (-X, Y, Z), (-X, 0, Z), (1, 0, 0), wall)        # -x wall
+    # +x wall with the slit z in [-0.05, 0.05], y in [0.5, 3.5]
+    g, y0, y1 = 0.05, 0.5, 3.5
+    b.quad((X, 0, -Z), (X, Y, -Z), (X, Y, -g), (X, 0, -g), (-1, 0, 0), wall)
+    b.quad((X, 0, g), (X, Y, g), (X, Y, Z), (X, 0, Z), (-1, 0, 0), wall)
+    b.quad((X, 0, -g), (X, y0, -g), (X, y0, g), (X, 0, g), (-1, 0, 0), wall)
+    b.quad((X, y1, -g), (X, Y, -g), (X, Y, g), (X, y1, g), (-1, 0, 0), wall)
+    # furniture: boxes and cylinders until n_tris
+    pieces, total = [], 0
+    while total < n_tris:
+        kind = rng.random() < 0.5
+        cx, cz = rng.uniform(-3.3, 2.8), rng.uniform(-2.4, 2.4)
+        if kind:
+            k = int(rng.integers(8, 33))
+            size = (rng.uniform(0.3, 1.2), rng.uniform(0.3, 1.6), rng.uniform(0.3, 1.2))
+            tris, nrm = _grid_box((cx, size[1] / 2, cz), size, rng.uniform(0, math.pi), k)
+        else:
+            segs, rings = int(rng.integers(32, 129)), int(rng.integers(8, 64))
+            tris, nrm = _cylinder((cx, 0.0, cz), rng.uniform(0.1, 0.5), rng.uniform(0.3, 2.0), segs, rings)
+        tris, nrm = tris[: n_tris - total], nrm[: n_tris - total]
+        p = rng.random(4)
+        mat = b.material(Material(kind=TR_MAT_DISNEY12, base_color=tuple(float(v) for v in 0.2 + 0.6 * rng.random(3)),
+                                  metallic=float(0.3 * p[0]), roughness=float(0.05 + 0.95 * p[1]),
+                                  specular=0.5, specular_tint=float(p[2]), sheen=0.0, sheen_tint=0.5,
+                                  clearcoat=float(0.5 * p[3]), clearcoat_gloss=0.5, anisotropic=0.0,
+                                  subsurface=0.0))
+        b.mesh(tris, nrm, mat)
+        total += len(tris)
+    # the light: a 3 m cube outside the slit, every face emitting outward
+    emit = (50.0, 50.0, 50.0)
+    lo, hi = np.array([X + 0.5, 0.5, -1.5]), np.array([X + 3.5, 3.5, 1.5])
+    for axis in range(3):
+        u, v = (axis + 1) % 3, (axis + 2) % 3
+        for sgn in (-1, 1):
+            n = [0, 0, 0]
+            n[axis] = sgn
+            corners = []
+            for su, sv in ((0, 0), (1, 0), (1, 1), (0, 1)):
+                q = [0.0, 0.0, 0.0]
+                q[axis] = hi[axis] if sgn > 0 else lo[axis]
+                q[u] = hi[u] if su else lo[u]
+                q[v] = hi[v] if sv else lo[v]
+                corners.append(q)
+            b.quad(*corners, n, wall, emission=emit)
+    scene = b.finish(max_leaf_prims=3)
+    cam = make_camera(width / height, (-3.6, 1.8, 2.4), (2.0, 1.6, -0.6), (0, 1, 0), math.radians(60.0), 0.0, 1.0)
+    return scene, cam, make_filter(0.5, 0.6), make_params(width, height, spp, min_depth, max_depth)
