@@ -276,6 +276,21 @@ tr_status tr_render_dev_noalloc(tr_ctx* ctx, const tr_camera* cam, const tr_filt
  * wavefront iteration; that call then returns TR_ERR_CANCELLED. Thread-safe. */
 tr_status tr_cancel(tr_ctx* ctx);
 
+/* Path-guiding model. No reference counterpart: Tracer has no path
+ * guiding. A multilayer perceptron 7 -> 64 -> 64 -> 64 -> 64 -> 40 (ReLU),
+ * fp16 weights and activations with fp32 accumulation on the tensor cores,
+ * mapping a path vertex (position normalised to the scene box, outgoing
+ * direction, roughness) to an 8-lobe von Mises-Fisher mixture (per lobe: a
+ * weight logit, log concentration, unnormalised mean direction). The flat
+ * fp32 parameter vector holds, per layer, W (out x in, row-major) then b. */
+enum { TR_GUIDE_INPUTS = 7, TR_GUIDE_OUTPUTS = 40, TR_GUIDE_PARAMS = 15592 };
+/* Initialises the parameters (uniform in +-1/sqrt(fan_in), seeded). */
+tr_status tr_guide_init(tr_ctx* ctx, uint64_t seed);
+tr_status tr_guide_set_params(tr_ctx* ctx, const float* params, size_t n);
+tr_status tr_guide_get_params(tr_ctx* ctx, float* params, size_t n);
+/* d_out (n x 40 fp32) = network(d_in (n x 7 fp32)), device buffers, synchronous. */
+tr_status tr_guide_forward_dev(tr_ctx* ctx, const float* d_in, size_t n, float* d_out);
+
 /* Device self-check of the single-precision evaluations that stand in for
  * the reference's double-precision expressions: `which` selects 0 the slab
  * scale of Bounds3::intersect_p (src/utility/geometry.hpp:848-859; n = 2^32

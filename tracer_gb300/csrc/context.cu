@@ -34,11 +34,6 @@ tr_status cuda_fail(tr_ctx* ctx, cudaError_t e, const char* what) {
   return set_err(ctx, TR_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define TR_CUDA(ctx, call)                               \
-  do {                                                   \
-    cudaError_t e_ = (call);                             \
-    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
-  } while (0)
 
 namespace {
 
@@ -314,6 +309,7 @@ void tr_ctx_destroy(tr_ctx* ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   release_render(ctx);
+  release_guide(ctx);
   for (DevBuf* b : {&ctx->d_nodes, &ctx->d_slots, &ctx->d_spheres, &ctx->d_prims, &ctx->d_tshade, &ctx->d_mats,
                     &ctx->d_lights, &ctx->d_rays, &ctx->d_out0, &ctx->d_out1, &ctx->d_err})
     b->release();

@@ -11,6 +11,7 @@
 #include "scene_types.h"
 
 namespace trg {
+struct GuideModel;
 
 // A device allocation that grows on demand and is freed with the context.
 struct DevBuf {
@@ -65,6 +66,7 @@ struct tr_ctx {
   std::atomic<int> cancel{0};
   trg::RenderBuffers* rb = nullptr;
   tr_tuning tune{20, 0, 16};
+  trg::GuideModel* guide = nullptr;
 };
 
 namespace trg {
@@ -74,4 +76,13 @@ tr_status upload_device_tables(tr_ctx* ctx);
 // Grid of a persistent traversal kernel: SMs x resident blocks (tuned or as many as fit).
 int traversal_grid(const tr_ctx* ctx, const void* kernel);
 void release_render(tr_ctx* ctx);
+void release_guide(tr_ctx* ctx);
 }  // namespace trg
+
+// Returns from the enclosing C ABI function with the context's error when a
+// CUDA runtime call fails.
+#define TR_CUDA(ctx, call)                                          \
+  do {                                                              \
+    cudaError_t e_ = (call);                                        \
+    if (e_ != cudaSuccess) return trg::cuda_fail(ctx, e_, #call);   \
+  } while (0)

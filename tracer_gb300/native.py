@@ -71,6 +71,14 @@ def lib() -> C.CDLL:
     L.tr_ctx_set_tuning.argtypes = [vp, C.POINTER(TrTuning)]
     L.tr_ctx_get_tuning.restype = st
     L.tr_ctx_get_tuning.argtypes = [vp, C.POINTER(TrTuning)]
+    L.tr_guide_init.restype = st
+    L.tr_guide_init.argtypes = [vp, C.c_uint64]
+    L.tr_guide_set_params.restype = st
+    L.tr_guide_set_params.argtypes = [vp, C.POINTER(C.c_float), C.c_size_t]
+    L.tr_guide_get_params.restype = st
+    L.tr_guide_get_params.argtypes = [vp, C.POINTER(C.c_float), C.c_size_t]
+    L.tr_guide_forward_dev.restype = st
+    L.tr_guide_forward_dev.argtypes = [vp, C.c_void_p, C.c_size_t, C.c_void_p]
     L.tr_render_dev.restype = st
     L.tr_render_dev.argtypes = [vp, C.POINTER(TrCamera), C.POINTER(TrFilter), C.POINTER(TrRenderParams),
                                 vp, vp, C.POINTER(TrStats)]
@@ -189,6 +197,24 @@ class GpuContext:
         if shade_blocks_per_sm is not None:
             t.shade_blocks_per_sm = shade_blocks_per_sm
         self._check(self.L.tr_ctx_set_tuning(self.h, C.byref(t)))
+
+    # ---- path-guiding model
+    GUIDE_PARAMS = 15592
+
+    def guide_init(self, seed: int = 0) -> None:
+        self._check(self.L.tr_guide_init(self.h, seed))
+
+    def guide_set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        self._check(self.L.tr_guide_set_params(self.h, _p(p, C.c_float), p.size))
+
+    def guide_params(self) -> np.ndarray:
+        p = np.zeros(self.GUIDE_PARAMS, np.float32)
+        self._check(self.L.tr_guide_get_params(self.h, _p(p, C.c_float), p.size))
+        return p
+
+    def guide_forward_dev(self, d_in: int, n: int, d_out: int) -> None:
+        self._check(self.L.tr_guide_forward_dev(self.h, d_in, n, d_out))
 
     def render_dev(self, cam: TrCamera, filt: TrFilter, params: TrRenderParams, d_out: int, fp64: bool = False):
         stats = TrStats()
