@@ -290,6 +290,20 @@ tr_status tr_guide_set_params(tr_ctx* ctx, const float* params, size_t n);
 tr_status tr_guide_get_params(tr_ctx* ctx, float* params, size_t n);
 /* d_out (n x 40 fp32) = network(d_in (n x 7 fp32)), device buffers, synchronous. */
 tr_status tr_guide_forward_dev(tr_ctx* ctx, const float* d_in, size_t n, float* d_out);
+/* d_grads (TR_GUIDE_PARAMS fp32) = gradient of sum_i d_dout_i . network(d_in_i)
+ * w.r.t. the parameters (fp16 operands, fp32 accumulation on the tensor cores). */
+tr_status tr_guide_backward_dev(tr_ctx* ctx, const float* d_in, const float* d_dout, size_t n,
+                                float* d_grads);
+/* Training loss of a batch: -sum_i w_i log p(dir_i | in_i) / sum_i w_i, p the
+ * network's vMF mixture (lobe j: out[5j] weight logit, out[5j+1] log kappa
+ * clamped to [-4, 7], out[5j+2..4] mean direction, normalised); d_dir unit
+ * vectors (n x 3), d_weight >= 0 (n). d_dout receives d loss / d out (n x 40). */
+tr_status tr_guide_loss_dev(tr_ctx* ctx, const float* d_in, const float* d_dir, const float* d_weight,
+                            size_t n, float* d_dout, float* loss);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8, learning rate lr) on that loss.
+ * set_params and init reset the Adam state. */
+tr_status tr_guide_train_step_dev(tr_ctx* ctx, const float* d_in, const float* d_dir,
+                                  const float* d_weight, size_t n, float lr, float* loss);
 
 /* Device self-check of the single-precision evaluations that stand in for
  * the reference's double-precision expressions: `which` selects 0 the slab

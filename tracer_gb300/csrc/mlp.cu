@@ -16,7 +16,9 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
+#include <utility>
 #include <cstring>
 #include <vector>
 
@@ -164,6 +166,280 @@ __global__ void __launch_bounds__(128, 1)
   }
 }
 
+// ------------------------------------------------------------ backward
+//
+// For a 128-row tile and layer l = 4 .. 0, with in_l the layer's input
+// (x for l = 0, h_{l-1} otherwise):
+//   dW_l (+)= dZ_l^T in_l       M = 128 (rows of dZ^T: the layer's outputs,
+//                                zero-padded), N = 16 or 80, K = 128 rows;
+//                                in_l^T carries a row of ones after its
+//                                inputs, so the same MMA yields db_l
+//   dH     = dZ_l W_l           M = 128 rows, N = 64, K = 48 or 64
+//   dZ_{l-1} = dH * (h_{l-1} > 0)
+// dW accumulates in tensor memory over all tiles of the CTA and is added to
+// the global gradient once at the end.
+
+// transposed weights W_l^T (k_in x n_out, core layout, K = n_out padded) for l = 1..4
+__host__ __device__ constexpr uint32_t wt_off(int l) { return (uint32_t)(l - 1) * 8192u; }
+constexpr uint32_t kWtBytes = 3 * 8192 + 64 * 48 * 2;  // 30720
+__host__ __device__ constexpr int bk_n(int l) { return l == 0 ? 16 : 80; }                 // dW MMA N
+__host__ __device__ constexpr uint32_t bk_col(int l) { return l == 0 ? 64u : 80u + 80u * (uint32_t)(l - 1); }
+constexpr uint32_t kBDz = kWtBytes;                   // dZ tile, 128 x 64 (K = 48 or 64)
+constexpr uint32_t kBDzT = kBDz + 16384;              // dZ^T tile, 128 (outputs) x 128 (rows)
+constexpr uint32_t kBInT = kBDzT + 32768;             // in^T tile, 80 x 128
+constexpr uint32_t kBMbar = kBInT + 80 * 128 * 2;
+constexpr uint32_t kBSlot = kBMbar + 8;
+constexpr uint32_t kBSmemBytes = kBSlot + 8;
+
+__global__ void k_pack_t(const float* __restrict__ p, uint8_t* __restrict__ img) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;  // element (k, n) of W_l^T, l = 1..4
+  int base = 0;
+  for (int l = 1; l < kLayers; ++l) {
+    const int KK = layer_n(l);  // MMA K of dH: the layer's outputs (48 or 64)
+    if (i < base + 64 * KK) {
+      const int e = i - base, k = e / KK, n = e % KK;
+      const float v = n < layer_nout(l) ? p[param_w(l) + n * kHid + k] : 0.0f;
+      *reinterpret_cast<__half*>(img + wt_off(l) + tc05::core_off(k, n, KK)) = __float2half_rn(v);
+      return;
+    }
+    base += 64 * KK;
+  }
+}
+constexpr int kPackTThreads = 3 * 64 * 64 + 64 * 48;
+
+__device__ __forceinline__ void st_half(uint8_t* base, uint32_t off, float v) {
+  *reinterpret_cast<__half*>(base + off) = __float2half_rn(v);
+}
+
+// x: n x 7, acts: 4 x n x 64 (fp16, forward outputs of the hidden layers),
+// dout: n x 40 (gradient of the loss w.r.t. the network outputs).
+// grads (fp32, parameter layout) += this CTA's share.
+__global__ void __launch_bounds__(128, 1)
+    k_backward(const uint8_t* __restrict__ wt_img, const float* __restrict__ x, const __half* __restrict__ acts,
+               const float* __restrict__ dout, int n, float* __restrict__ grads, int* err) {
+  extern __shared__ __align__(1024) uint8_t sm[];
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int i = tid; i < (int)(kWtBytes / 16); i += blockDim.x)
+    reinterpret_cast<int4*>(sm)[i] = reinterpret_cast<const int4*>(wt_img)[i];
+  for (int i = tid; i < (int)((kBMbar - kBDz) / 16); i += blockDim.x)
+    reinterpret_cast<int4*>(sm + kBDz)[i] = make_int4(0, 0, 0, 0);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + kBMbar);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(sm + kBSlot);
+  if (tid == 0) tc05::mbar_init(mbar, 1);
+  if (warp == 0) tc05::tmem_alloc(slot, 512);
+  tc05::fence_before();
+  __syncthreads();
+  tc05::fence_after();
+  const uint32_t tmem = *slot;
+  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+  uint8_t* Dz = sm + kBDz;
+  uint8_t* DzT = sm + kBDzT;
+  uint8_t* InT = sm + kBInT;
+  const uint32_t a_dz = tc05::smem_u32(Dz), a_dzt = tc05::smem_u32(DzT), a_int = tc05::smem_u32(InT),
+                 a_wt = tc05::smem_u32(sm);
+  uint32_t phase = 0;
+  bool ok = true;
+  int tiles_done = 0;
+  const int ntiles = (n + kTile - 1) / kTile;
+  for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+    const int r = tid, g = t * kTile + tid;
+    const bool live = g < n;
+    // layer 4: dZ4 = dout, in_4 = h3
+    float hin[64];  // in_l of the current layer (the ReLU mask of the next dZ)
+    {
+      float dz[48];
+#pragma unroll
+      for (int c = 0; c < 48; ++c) dz[c] = (live && c < kOut) ? dout[(size_t)g * kOut + c] : 0.0f;
+#pragma unroll
+      for (int c = 0; c < 48; ++c) st_half(Dz, tc05::core_off(r, c, 48), dz[c]);
+#pragma unroll
+      for (int c = 0; c < 64; ++c) st_half(DzT, tc05::core_off(c, r, 128), c < 48 ? dz[c] : 0.0f);
+    }
+#pragma unroll
+    for (int k = 0; k < 64; ++k) hin[k] = live ? __half2float(acts[((size_t)3 * n + g) * kHid + k]) : 0.0f;
+#pragma unroll
+    for (int k = 0; k < 80; ++k)
+      st_half(InT, tc05::core_off(k, r, 128), k < 64 ? hin[k] : (k == 64 && live ? 1.0f : 0.0f));
+    for (int l = kLayers - 1; l >= 0 && ok; --l) {
+      tc05::fence_proxy_async();
+      __syncthreads();
+      if (tid == 0) {
+        tc05::fence_after();
+        const uint32_t acc0 = tiles_done > 0 ? 1u : 0u;
+        for (int kk = 0; kk < 8; ++kk)
+          tc05::mma_f16(tmem + bk_col(l), tc05::smem_desc(a_dzt + kk * 256u, 128u, 2048u),
+                        tc05::smem_desc(a_int + kk * 256u, 128u, 2048u), tc05::idesc_f16_f32(128, bk_n(l)),
+                        (acc0 || kk > 0) ? 1u : 0u);
+        if (l > 0) {
+          const int KK = layer_n(l);
+          const uint32_t sbo = (uint32_t)(KK / 8) * 128u;
+          for (int kk = 0; kk < KK / 16; ++kk)
+            tc05::mma_f16(tmem, tc05::smem_desc(a_dz + kk * 256u, 128u, sbo),
+                          tc05::smem_desc(a_wt + wt_off(l) + kk * 256u, 128u, sbo), tc05::idesc_f16_f32(128, 64),
+                          kk > 0 ? 1u : 0u);
+        }
+        tc05::commit(mbar);
+      }
+      const bool got = tc05::mbar_wait(mbar, phase);
+      ok = __syncthreads_and(got) != 0;
+      if (!ok) break;
+      phase ^= 1u;
+      if (l == 0) break;
+      tc05::fence_after();
+      // dZ_{l-1} = dH * (h_{l-1} > 0); h_{l-1} is this layer's input (hin)
+      float dz[64];
+#pragma unroll
+      for (int c0 = 0; c0 < 64; c0 += 16) {
+        float v[16];
+        tc05::tmem_ld16(tmem + lane_base + (uint32_t)c0, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) dz[c0 + j] = hin[c0 + j] > 0.0f ? v[j] : 0.0f;
+      }
+      tc05::fence_before();
+#pragma unroll
+      for (int c = 0; c < 64; ++c) st_half(Dz, tc05::core_off(r, c, 64), dz[c]);
+#pragma unroll
+      for (int c = 0; c < 64; ++c) st_half(DzT, tc05::core_off(c, r, 128), dz[c]);
+      // the input of layer l-1
+      if (l - 1 > 0) {
+#pragma unroll
+        for (int k = 0; k < 64; ++k)
+          hin[k] = live ? __half2float(acts[((size_t)(l - 2) * n + g) * kHid + k]) : 0.0f;
+#pragma unroll
+        for (int k = 0; k < 80; ++k)
+          st_half(InT, tc05::core_off(k, r, 128), k < 64 ? hin[k] : (k == 64 && live ? 1.0f : 0.0f));
+      } else {
+#pragma unroll
+        for (int k = 0; k < 16; ++k)
+          st_half(InT, tc05::core_off(k, r, 128),
+                  k < kIn ? (live ? x[(size_t)g * kIn + k] : 0.0f) : (k == kIn && live ? 1.0f : 0.0f));
+      }
+    }
+    ++tiles_done;
+  }
+  if (!ok) {
+    if (tid == 0) atomicOr(err, 1);
+    tc05::mbar_wait(mbar, phase);
+  }
+  __syncthreads();
+  tc05::fence_after();
+  if (ok && tiles_done > 0 && warp < 2) {
+    // rows (lanes) 0..63 of the dW accumulators: output unit `o` of each layer
+    const int o = tid;
+    for (int l = 0; l < kLayers; ++l) {
+      const int N = bk_n(l), kin = layer_kin(l);
+      for (int c0 = 0; c0 < N; c0 += 16) {
+        float v[16];
+        tc05::tmem_ld16(tmem + lane_base + bk_col(l) + (uint32_t)c0, v);
+        if (o < layer_nout(l)) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int k = c0 + j;
+            if (k < kin) atomicAdd(grads + param_w(l) + o * kin + k, v[j]);
+            else if (k == kin) atomicAdd(grads + param_b(l) + o, v[j]);
+          }
+        }
+      }
+    }
+  }
+  tc05::fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc05::tmem_dealloc(tmem, 512);
+    tc05::tmem_relinquish();
+  }
+}
+
+// ------------------------------------------------------------ loss, Adam
+//
+// Negative log-likelihood of the directions under the 8-lobe vMF mixture,
+// weighted per row: loss = -sum_i w_i log p(omega_i | x_i) / sum_i w_i.
+// Lobe j of row i: out[5j] weight logit, out[5j+1] log kappa (clamped to
+// [-4, 7]), out[5j+2..4] unnormalised mean direction;
+// vMF(omega) = kappa / (2 pi (1 - exp(-2 kappa))) exp(kappa (mu.omega - 1)).
+
+struct Lobe {
+  float pi, kappa, mlen, c;
+  float3 mu;
+};
+
+__device__ __forceinline__ float vmf_log_norm(float kappa) {
+  // log(kappa / (2 pi (1 - exp(-2 kappa))))
+  return logf(kappa) - 1.8378770664093453f - log1pf(-expf(-2.0f * kappa));
+}
+
+__global__ void k_loss(const float* __restrict__ out, const float* __restrict__ dir, const float* __restrict__ w,
+                       int n, const float* __restrict__ wsum, float* __restrict__ dout, float* __restrict__ loss) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float li = 0.0f;
+  if (i < n) {
+    const float* z = out + (size_t)i * kOut;
+    const float3 om = make_float3(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]);
+    const float wi = w[i] / fmaxf(*wsum, 1e-30f);
+    float a_max = -INFINITY;
+    for (int j = 0; j < kLobes; ++j) a_max = fmaxf(a_max, z[5 * j]);
+    float esum = 0.0f, lq[kLobes], pi[kLobes];
+    for (int j = 0; j < kLobes; ++j) {
+      pi[j] = expf(z[5 * j] - a_max);
+      esum += pi[j];
+    }
+    float lmax = -INFINITY;
+    Lobe L[kLobes];
+    for (int j = 0; j < kLobes; ++j) {
+      pi[j] /= esum;
+      const float s = fminf(fmaxf(z[5 * j + 1], -4.0f), 7.0f);
+      const float kappa = expf(s);
+      const float3 m = make_float3(z[5 * j + 2], z[5 * j + 3], z[5 * j + 4]);
+      const float mlen = sqrtf(m.x * m.x + m.y * m.y + m.z * m.z) + 1e-6f;
+      const float3 mu = make_float3(m.x / mlen, m.y / mlen, m.z / mlen);
+      const float c = mu.x * om.x + mu.y * om.y + mu.z * om.z;
+      L[j] = Lobe{pi[j], kappa, mlen, c, mu};
+      lq[j] = logf(fmaxf(pi[j], 1e-30f)) + vmf_log_norm(kappa) + kappa * (c - 1.0f);
+      lmax = fmaxf(lmax, lq[j]);
+    }
+    float qs = 0.0f;
+    for (int j = 0; j < kLobes; ++j) qs += expf(lq[j] - lmax);
+    const float logp = lmax + logf(qs);
+    li = -wi * logp;
+    float* d = dout + (size_t)i * kOut;
+    for (int j = 0; j < kLobes; ++j) {
+      const float q = expf(lq[j] - logp);  // responsibility
+      const Lobe& b = L[j];
+      d[5 * j] = -wi * (q - b.pi);
+      const float s = z[5 * j + 1];
+      const float e2 = expf(-2.0f * b.kappa);
+      const float dlogk = 1.0f - 2.0f * b.kappa * e2 / fmaxf(-expm1f(-2.0f * b.kappa), 1e-30f) + b.kappa * (b.c - 1.0f);
+      d[5 * j + 1] = (s > -4.0f && s < 7.0f) ? -wi * q * dlogk : 0.0f;
+      const float f = -wi * q * b.kappa / b.mlen;
+      d[5 * j + 2] = f * (om.x - b.c * b.mu.x);
+      d[5 * j + 3] = f * (om.y - b.c * b.mu.y);
+      d[5 * j + 4] = f * (om.z - b.c * b.mu.z);
+    }
+  }
+  // block sum of the loss
+  for (int o = 16; o > 0; o >>= 1) li += __shfl_xor_sync(0xffffffffu, li, o);
+  if ((threadIdx.x & 31) == 0 && li != 0.0f) atomicAdd(loss, li);
+}
+
+__global__ void k_sum(const float* __restrict__ w, int n, float* __restrict__ out) {
+  float s = 0.0f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s += w[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, float lr, float c1, float c2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kParams) return;
+  const float gi = g[i];
+  const float mi = 0.9f * m[i] + 0.1f * gi;
+  const float vi = 0.999f * v[i] + 0.001f * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + 1e-8f);
+}
+
 }  // namespace mlp
 
 // ------------------------------------------------------------------ host
@@ -184,40 +460,131 @@ tr_status guide_reserve(tr_ctx* ctx) {
   if (!ctx->guide) ctx->guide = new GuideModel();
   GuideModel* g = ctx->guide;
   if (g->params.p) return TR_OK;
-  cudaError_t e;
-  if ((e = g->params.reserve(mlp::kParams * 4)) != cudaSuccess || (e = g->img.reserve(mlp::kPackedBytes)) != cudaSuccess)
-    return cuda_fail(ctx, e, "guide model allocation");
+  cudaError_t e = cudaSuccess;
+  for (auto pr : {std::make_pair(&g->params, (size_t)mlp::kParams * 4), std::make_pair(&g->img, (size_t)mlp::kPackedBytes),
+                  std::make_pair(&g->img_t, (size_t)mlp::kWtBytes), std::make_pair(&g->grads, (size_t)mlp::kParams * 4),
+                  std::make_pair(&g->adam_m, (size_t)mlp::kParams * 4),
+                  std::make_pair(&g->adam_v, (size_t)mlp::kParams * 4), std::make_pair(&g->scal, (size_t)64)})
+    if ((e = pr.first->reserve(pr.second)) != cudaSuccess) return cuda_fail(ctx, e, "guide model allocation");
   if (!g->attr_set) {
     if ((e = cudaFuncSetAttribute(mlp::k_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::kSmemBytes)) !=
-        cudaSuccess)
-      return cuda_fail(ctx, e, "forward kernel shared memory");
+            cudaSuccess ||
+        (e = cudaFuncSetAttribute(mlp::k_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::kBSmemBytes)) !=
+            cudaSuccess)
+      return cuda_fail(ctx, e, "guide kernels' shared memory");
     g->attr_set = true;
   }
   return TR_OK;
 }
 
-tr_status guide_pack(tr_ctx* ctx) {
-  mlp::k_pack<<<(mlp::kPackThreads + 255) / 256, 256, 0, ctx->stream>>>(ctx->guide->params.as<float>(),
-                                                                         ctx->guide->img.as<uint8_t>());
-  cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? TR_OK : cuda_fail(ctx, e, "k_pack");
+// Resets the Adam state (new parameters start a new optimisation).
+static tr_status guide_reset_adam(tr_ctx* ctx) {
+  GuideModel* g = ctx->guide;
+  TR_CUDA(ctx, cudaMemsetAsync(g->adam_m.p, 0, mlp::kParams * 4, ctx->stream));
+  TR_CUDA(ctx, cudaMemsetAsync(g->adam_v.p, 0, mlp::kParams * 4, ctx->stream));
+  g->step = 0;
+  return TR_OK;
 }
 
-tr_status guide_forward(tr_ctx* ctx, const float* d_in, int n, float* d_out, __half* d_acts) {
+tr_status guide_pack(tr_ctx* ctx) {
+  GuideModel* g = ctx->guide;
+  mlp::k_pack<<<(mlp::kPackThreads + 255) / 256, 256, 0, ctx->stream>>>(g->params.as<float>(), g->img.as<uint8_t>());
+  mlp::k_pack_t<<<(mlp::kPackTThreads + 255) / 256, 256, 0, ctx->stream>>>(g->params.as<float>(),
+                                                                            g->img_t.as<uint8_t>());
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? TR_OK : cuda_fail(ctx, e, "guide weight packing");
+}
+
+static int guide_grid(tr_ctx* ctx, int n) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
   const int tiles = (n + mlp::kTile - 1) / mlp::kTile;
-  const int grid = std::max(1, std::min(tiles, sms));
-  mlp::k_forward<<<grid, 128, mlp::kSmemBytes, ctx->stream>>>(ctx->guide->img.as<uint8_t>(), d_in, n, d_out, d_acts,
-                                                              ctx->d_err.as<int>() + 2);
+  return std::max(1, std::min(tiles, sms));
+}
+
+tr_status guide_forward(tr_ctx* ctx, const float* d_in, int n, float* d_out, __half* d_acts) {
+  mlp::k_forward<<<guide_grid(ctx, n), 128, mlp::kSmemBytes, ctx->stream>>>(
+      ctx->guide->img.as<uint8_t>(), d_in, n, d_out, d_acts, ctx->d_err.as<int>() + 2);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? TR_OK : cuda_fail(ctx, e, "k_forward");
+}
+
+static tr_status guide_workspace(tr_ctx* ctx, int n) {
+  GuideModel* g = ctx->guide;
+  cudaError_t e;
+  if ((e = g->acts.reserve((size_t)4 * n * mlp::kHid * 2)) != cudaSuccess ||
+      (e = g->out.reserve((size_t)n * mlp::kOut * 4)) != cudaSuccess ||
+      (e = g->dout.reserve((size_t)n * mlp::kOut * 4)) != cudaSuccess)
+    return cuda_fail(ctx, e, "guide training workspace");
+  return TR_OK;
+}
+
+tr_status guide_backward(tr_ctx* ctx, const float* d_in, const float* d_dout, int n, float* d_grads) {
+  tr_status s = guide_workspace(ctx, n);
+  if (s != TR_OK) return s;
+  GuideModel* g = ctx->guide;
+  s = guide_forward(ctx, d_in, n, g->out.as<float>(), g->acts.as<__half>());
+  if (s != TR_OK) return s;
+  TR_CUDA(ctx, cudaMemsetAsync(d_grads, 0, mlp::kParams * 4, ctx->stream));
+  mlp::k_backward<<<guide_grid(ctx, n), 128, mlp::kBSmemBytes, ctx->stream>>>(
+      g->img_t.as<uint8_t>(), d_in, g->acts.as<__half>(), d_dout, n, d_grads, ctx->d_err.as<int>() + 2);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? TR_OK : cuda_fail(ctx, e, "k_backward");
+}
+
+// Loss and its gradient w.r.t. the network outputs (g->dout) for a batch;
+// the loss lands in scal[1].
+static tr_status guide_loss(tr_ctx* ctx, const float* d_in, const float* d_dir, const float* d_w, int n) {
+  tr_status s = guide_workspace(ctx, n);
+  if (s != TR_OK) return s;
+  GuideModel* g = ctx->guide;
+  s = guide_forward(ctx, d_in, n, g->out.as<float>(), g->acts.as<__half>());
+  if (s != TR_OK) return s;
+  float* scal = g->scal.as<float>();
+  TR_CUDA(ctx, cudaMemsetAsync(scal, 0, 8, ctx->stream));
+  mlp::k_sum<<<64, 256, 0, ctx->stream>>>(d_w, n, scal);
+  mlp::k_loss<<<(n + 255) / 256, 256, 0, ctx->stream>>>(g->out.as<float>(), d_dir, d_w, n, scal,
+                                                         g->dout.as<float>(), scal + 1);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? TR_OK : cuda_fail(ctx, e, "k_loss");
+}
+
+tr_status guide_train_step(tr_ctx* ctx, const float* d_in, const float* d_dir, const float* d_w, int n, float lr) {
+  tr_status s = guide_loss(ctx, d_in, d_dir, d_w, n);
+  if (s != TR_OK) return s;
+  GuideModel* g = ctx->guide;
+  TR_CUDA(ctx, cudaMemsetAsync(g->grads.p, 0, mlp::kParams * 4, ctx->stream));
+  mlp::k_backward<<<guide_grid(ctx, n), 128, mlp::kBSmemBytes, ctx->stream>>>(
+      g->img_t.as<uint8_t>(), d_in, g->acts.as<__half>(), g->dout.as<float>(), n, g->grads.as<float>(),
+      ctx->d_err.as<int>() + 2);
+  ++g->step;
+  const float c1 = 1.0f - std::pow(0.9f, (float)g->step), c2 = 1.0f - std::pow(0.999f, (float)g->step);
+  mlp::k_adam<<<(mlp::kParams + 255) / 256, 256, 0, ctx->stream>>>(g->params.as<float>(), g->grads.as<float>(),
+                                                                    g->adam_m.as<float>(), g->adam_v.as<float>(), lr,
+                                                                    c1, c2);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "guide training step");
+  return guide_pack(ctx);
+}
+
+// Synchronises and turns a timed-out tensor-core wait into an error.
+static tr_status guide_check(tr_ctx* ctx) {
+  int e = 0;
+  TR_CUDA(ctx, cudaMemcpyAsync(&e, ctx->d_err.as<int>() + 2, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  TR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (e) {
+    cudaMemsetAsync(ctx->d_err.as<int>() + 2, 0, 4, ctx->stream);
+    return set_err(ctx, TR_ERR_TIMEOUT, "tensor-core MMA wait timed out");
+  }
+  return TR_OK;
 }
 
 void release_guide(tr_ctx* ctx) {
   if (!ctx->guide) return;
   GuideModel* g = ctx->guide;
-  for (DevBuf* b : {&g->params, &g->img}) b->release();
+  for (DevBuf* b : {&g->params, &g->img, &g->img_t, &g->grads, &g->adam_m, &g->adam_v, &g->acts, &g->out, &g->dout,
+                    &g->scal})
+    b->release();
   delete g;
   ctx->guide = nullptr;
 }
@@ -253,6 +620,8 @@ tr_status tr_guide_set_params(tr_ctx* ctx, const float* params, size_t n) {
   tr_status s = guide_reserve(ctx);
   if (s != TR_OK) return s;
   TR_CUDA(ctx, cudaMemcpyAsync(ctx->guide->params.p, params, n * 4, cudaMemcpyHostToDevice, ctx->stream));
+  s = guide_reset_adam(ctx);
+  if (s != TR_OK) return s;
   s = guide_pack(ctx);
   if (s != TR_OK) return s;
   TR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -275,15 +644,48 @@ tr_status tr_guide_forward_dev(tr_ctx* ctx, const float* d_in, size_t n, float* 
   if (n == 0) return TR_OK;
   TR_CUDA(ctx, cudaSetDevice(ctx->device));
   tr_status s = guide_forward(ctx, d_in, (int)n, d_out, nullptr);
-  if (s != TR_OK) return s;
-  int e = 0;
-  TR_CUDA(ctx, cudaMemcpyAsync(&e, ctx->d_err.as<int>() + 2, 4, cudaMemcpyDeviceToHost, ctx->stream));
-  TR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  if (e) {
-    cudaMemsetAsync(ctx->d_err.as<int>() + 2, 0, 4, ctx->stream);
-    return set_err(ctx, TR_ERR_TIMEOUT, "tensor-core MMA wait timed out");
+  return s != TR_OK ? s : guide_check(ctx);
+}
+
+tr_status tr_guide_backward_dev(tr_ctx* ctx, const float* d_in, const float* d_dout, size_t n, float* d_grads) {
+  if (!ctx || !d_grads || (n && (!d_in || !d_dout))) return TR_ERR_ARG;
+  if (!ctx->guide || !ctx->guide->params.p) return set_err(ctx, TR_ERR_STATE, "guide model not initialised");
+  if (n > (1u << 26)) return set_err(ctx, TR_ERR_ARG, "too many rows");
+  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (n == 0) {
+    TR_CUDA(ctx, cudaMemsetAsync(d_grads, 0, mlp::kParams * 4, ctx->stream));
+    return guide_check(ctx);
   }
-  return TR_OK;
+  tr_status s = guide_backward(ctx, d_in, d_dout, (int)n, d_grads);
+  return s != TR_OK ? s : guide_check(ctx);
+}
+
+tr_status tr_guide_loss_dev(tr_ctx* ctx, const float* d_in, const float* d_dir, const float* d_weight, size_t n,
+                            float* d_dout, float* loss) {
+  if (!ctx || !loss || !d_dout || n == 0 || !d_in || !d_dir || !d_weight) return TR_ERR_ARG;
+  if (!ctx->guide || !ctx->guide->params.p) return set_err(ctx, TR_ERR_STATE, "guide model not initialised");
+  if (n > (1u << 26)) return set_err(ctx, TR_ERR_ARG, "too many rows");
+  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  tr_status s = guide_loss(ctx, d_in, d_dir, d_weight, (int)n);
+  if (s != TR_OK) return s;
+  TR_CUDA(ctx, cudaMemcpyAsync(d_dout, ctx->guide->dout.p, n * mlp::kOut * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+  TR_CUDA(ctx, cudaMemcpyAsync(loss, ctx->guide->scal.as<float>() + 1, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  return guide_check(ctx);
+}
+
+tr_status tr_guide_train_step_dev(tr_ctx* ctx, const float* d_in, const float* d_dir, const float* d_weight,
+                                  size_t n, float lr, float* loss) {
+  if (!ctx || n == 0 || !d_in || !d_dir || !d_weight || !(lr > 0.0f)) return TR_ERR_ARG;
+  if (!ctx->guide || !ctx->guide->params.p) return set_err(ctx, TR_ERR_STATE, "guide model not initialised");
+  if (n > (1u << 26)) return set_err(ctx, TR_ERR_ARG, "too many rows");
+  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  tr_status s = guide_train_step(ctx, d_in, d_dir, d_weight, (int)n, lr);
+  if (s != TR_OK) return s;
+  float l = 0.0f;
+  TR_CUDA(ctx, cudaMemcpyAsync(&l, ctx->guide->scal.as<float>() + 1, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  s = guide_check(ctx);
+  if (loss) *loss = l;
+  return s;
 }
 
 }  // extern "C"

@@ -22,13 +22,21 @@ constexpr int kParams = 15592;
 
 struct GuideModel {
   DevBuf params;  // fp32 master parameters (flat, mlp::param_w / param_b)
-  DevBuf img;     // fp16 weights in the MMA layout + fp32 biases
+  DevBuf img;     // fp16 weights in the forward MMA layout + fp32 biases
+  DevBuf img_t;   // fp16 transposed weights of layers 1..4 (backward)
+  DevBuf grads, adam_m, adam_v;
+  DevBuf acts, out, dout, scal;  // training workspace (grown on demand)
+  int64_t step = 0;              // Adam steps taken
   bool attr_set = false;
 };
 
 tr_status guide_reserve(tr_ctx* ctx);
 tr_status guide_pack(tr_ctx* ctx);
 tr_status guide_forward(tr_ctx* ctx, const float* d_in, int n, float* d_out, __half* d_acts);
+// Gradient of sum_i dout_i . net(x_i) w.r.t. the parameters into grads (overwritten).
+tr_status guide_backward(tr_ctx* ctx, const float* d_in, const float* d_dout, int n, float* d_grads);
+// One Adam step on the weighted vMF-mixture NLL of a batch; *d_loss (device) receives the loss.
+tr_status guide_train_step(tr_ctx* ctx, const float* d_in, const float* d_dir, const float* d_w, int n, float lr);
 void release_guide(tr_ctx* ctx);
 
 }  // namespace trg

@@ -79,6 +79,14 @@ def lib() -> C.CDLL:
     L.tr_guide_get_params.argtypes = [vp, C.POINTER(C.c_float), C.c_size_t]
     L.tr_guide_forward_dev.restype = st
     L.tr_guide_forward_dev.argtypes = [vp, C.c_void_p, C.c_size_t, C.c_void_p]
+    L.tr_guide_backward_dev.restype = st
+    L.tr_guide_backward_dev.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]
+    L.tr_guide_loss_dev.restype = st
+    L.tr_guide_loss_dev.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p,
+                                    C.POINTER(C.c_float)]
+    L.tr_guide_train_step_dev.restype = st
+    L.tr_guide_train_step_dev.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_float,
+                                          C.POINTER(C.c_float)]
     L.tr_render_dev.restype = st
     L.tr_render_dev.argtypes = [vp, C.POINTER(TrCamera), C.POINTER(TrFilter), C.POINTER(TrRenderParams),
                                 vp, vp, C.POINTER(TrStats)]
@@ -215,6 +223,19 @@ class GpuContext:
 
     def guide_forward_dev(self, d_in: int, n: int, d_out: int) -> None:
         self._check(self.L.tr_guide_forward_dev(self.h, d_in, n, d_out))
+
+    def guide_backward_dev(self, d_in: int, d_dout: int, n: int, d_grads: int) -> None:
+        self._check(self.L.tr_guide_backward_dev(self.h, d_in, d_dout, n, d_grads))
+
+    def guide_loss_dev(self, d_in: int, d_dir: int, d_w: int, n: int, d_dout: int) -> float:
+        loss = C.c_float()
+        self._check(self.L.tr_guide_loss_dev(self.h, d_in, d_dir, d_w, n, d_dout, C.byref(loss)))
+        return loss.value
+
+    def guide_train_step_dev(self, d_in: int, d_dir: int, d_w: int, n: int, lr: float = 1e-3) -> float:
+        loss = C.c_float()
+        self._check(self.L.tr_guide_train_step_dev(self.h, d_in, d_dir, d_w, n, lr, C.byref(loss)))
+        return loss.value
 
     def render_dev(self, cam: TrCamera, filt: TrFilter, params: TrRenderParams, d_out: int, fp64: bool = False):
         stats = TrStats()
