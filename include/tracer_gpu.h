@@ -164,6 +164,7 @@ typedef struct tr_stats {
   uint64_t closest_prims; /*   primitives tested by closest-hit rays */
   uint64_t any_boxes;     /*   boxes tested by shadow rays */
   uint64_t any_prims;     /*   primitives tested by shadow rays */
+  uint64_t guide_records; /* guided renders: training records kept */
 } tr_stats;
 
 const char* tr_status_string(tr_status s);
@@ -304,6 +305,33 @@ tr_status tr_guide_loss_dev(tr_ctx* ctx, const float* d_in, const float* d_dir, 
  * set_params and init reset the Adam state. */
 tr_status tr_guide_train_step_dev(tr_ctx* ctx, const float* d_in, const float* d_dir,
                                   const float* d_weight, size_t n, float lr, float* loss);
+
+/* Guided rendering. No reference counterpart. tr_render_dev with the
+ * continuation direction of every Lambertian vertex (Phong material without
+ * specular lobe) drawn by one-sample MIS from the guide network's mixture
+ * (probability alpha) and the BSDF (1 - alpha); the estimator keeps the
+ * plain path's expectation. Next-event estimation is unchanged; Disney12
+ * vertices keep BSDF sampling (the reference's Disney12 sampler draws from
+ * a density other than its pdf, so a mixture pdf would change the image it
+ * converges to). alpha = 0 renders exactly like tr_render_dev.
+ * With record != 0 every traced continuation of the render also becomes a
+ * training record (network input, direction, incident-radiance estimate /
+ * pdf), up to max_records (0: 4M), for tr_guide_train_on_records. The
+ * random stream differs from the plain renderer's when alpha > 0. */
+typedef struct tr_guide_params {
+  float alpha;
+  float box_lo[3]; /* scene box of the position inputs */
+  float box_hi[3];
+  int32_t record;
+  uint32_t max_records;
+} tr_guide_params;
+tr_status tr_render_guided_dev(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter,
+                               const tr_render_params* params, const tr_guide_params* guide,
+                               float* d_rgbw, double* d_rgbw64, tr_stats* stats);
+/* `steps` Adam steps on random batches of `batch` records of the last
+ * recording render of this context. */
+tr_status tr_guide_train_on_records(tr_ctx* ctx, int32_t steps, uint32_t batch, float lr, uint64_t seed,
+                                    float* mean_loss);
 
 /* Device self-check of the single-precision evaluations that stand in for
  * the reference's double-precision expressions: `which` selects 0 the slab

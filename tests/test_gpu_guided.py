@@ -1,0 +1,74 @@
+"""Guided rendering: the one-sample MIS of the guide network's mixture and
+the BSDF on Lambertian vertices, and online training on the render's own
+records."""
+import numpy as np
+import pytest
+
+from tracer_gb300 import scenes
+from tracer_gb300.abi import make_guide
+
+pytestmark = pytest.mark.gpu
+
+
+def _film(gpu, cam, filt, par, guide, fp64=True):
+    import torch
+    H, W = par.height, par.width
+    out = torch.zeros((H, W, 4), dtype=torch.float64 if fp64 else torch.float32, device="cuda:0")
+    torch.cuda.synchronize()
+    st = gpu.render_guided_dev(cam, filt, par, guide, out.data_ptr(), fp64)
+    return out.cpu().numpy(), st
+
+
+def _image(acc):
+    w = acc[..., 3:4]
+    return np.where(w > 0, acc[..., :3] / np.where(w > 0, w, 1), 0)
+
+
+def test_alpha_zero_is_the_plain_renderer(gpu):
+    sc, cam, filt, par = scenes.cornell(48, 40, 4)
+    gpu.upload(sc)
+    plain, pst = gpu.render(cam, filt, par, fp64=True)
+    for record in (False, True):
+        g = make_guide(0.0, (-1, -1, -1), (1, 1, 1), record=record)
+        got, st = _film(gpu, cam, filt, par, g)
+        assert np.array_equal(got, plain)
+        assert st.samples == pst.samples and st.extend_rays == pst.extend_rays
+        if record:
+            assert st.guide_records > 0
+        else:
+            assert st.guide_records == 0
+
+
+def test_guided_estimator_keeps_the_plain_expectation(gpu):
+    """alpha = 0.5 with an untrained (random) mixture: a different proposal,
+    the same expected image. Compared on 8x8-pixel blocks at 1024 spp."""
+    sc, cam, filt, _ = scenes.cornell(32, 32, 1)
+    gpu.upload(sc)
+    gpu.guide_init(seed=4)
+    par = scenes.make_params(32, 32, 1024, 5, 5, seed_base=1)
+    plain, _ = gpu.render(cam, filt, par, fp64=True)
+    par_g = scenes.make_params(32, 32, 1024, 5, 5, seed_base=7_000_000)
+    guided, st = _film(gpu, cam, filt, par_g, make_guide(0.5, (-1, -1, -1), (1, 1, 1)))
+    assert st.samples == 32 * 32 * 1024
+    a = _image(plain).reshape(4, 8, 4, 8, 3).mean((1, 3))
+    b = _image(guided).reshape(4, 8, 4, 8, 3).mean((1, 3))
+    rel = np.abs(a - b) / np.maximum(a, 1e-3)
+    print(f"block means: max rel diff {rel.max():.4f}, image mean plain {a.mean():.5f} guided {b.mean():.5f}")
+    assert abs(a.mean() - b.mean()) <= 0.01 * a.mean()
+    assert rel.max() < 0.08
+
+
+def test_training_on_render_records(gpu):
+    sc, cam, filt, par = scenes.occluded_room(64, 48, 8, n_tris=20000)
+    gpu.upload(sc)
+    gpu.guide_init(seed=0)
+    box = ((-4.0, 0.0, -3.0), (4.0, 4.0, 3.0))
+    _, st = _film(gpu, cam, filt, par, make_guide(0.0, *box, record=True))
+    assert st.guide_records > 1000
+    first = gpu.guide_train_on_records(5, 8192, 1e-3, seed=1)
+    later = gpu.guide_train_on_records(100, 8192, 1e-3, seed=2)
+    print(f"records {st.guide_records}: loss {first:.3f} -> {later:.3f}")
+    assert np.isfinite(first) and np.isfinite(later) and later < first
+    # the trained model guides a render without errors and with finite output
+    out, st2 = _film(gpu, cam, filt, par, make_guide(0.5, *box, record=True))
+    assert st2.samples == 64 * 48 * 8 and np.isfinite(out).all()

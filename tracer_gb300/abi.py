@@ -95,7 +95,12 @@ class TrStats(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("extend_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
                 ("shade_items", C.c_uint64), ("iterations", C.c_uint64), ("device_ms", C.c_double),
                 ("stage_ms", C.c_double * 8), ("closest_boxes", C.c_uint64), ("closest_prims", C.c_uint64),
-                ("any_boxes", C.c_uint64), ("any_prims", C.c_uint64)]
+                ("any_boxes", C.c_uint64), ("any_prims", C.c_uint64), ("guide_records", C.c_uint64)]
+
+
+class TrGuideParams(C.Structure):
+    _fields_ = [("alpha", C.c_float), ("box_lo", C.c_float * 3), ("box_hi", C.c_float * 3), ("record", C.c_int32),
+                ("max_records", C.c_uint32)]
 
 
 class TrTuning(C.Structure):
@@ -211,6 +216,16 @@ def make_filter(radius=0.5, alpha=0.6) -> TrFilter:
     f.radius = radius
     f.alpha = alpha
     return f
+
+
+def make_guide(alpha: float, box_lo, box_hi, record: bool = False, max_records: int = 0) -> "TrGuideParams":
+    g = TrGuideParams()
+    g.alpha = alpha
+    g.box_lo[:] = box_lo
+    g.box_hi[:] = box_hi
+    g.record = 1 if record else 0
+    g.max_records = max_records
+    return g
 
 
 def make_params(width, height, spp, min_depth, max_depth, seed_base=0, direct_light_sample_num=1, flags=0):

@@ -82,8 +82,9 @@ constexpr int kPackThreads = 64 * 16 + 3 * 64 * 64 + 48 * 64 + 304;  // W0, W1..
 // the four hidden layers are stored too (acts[l][row][64]) for training.
 __global__ void __launch_bounds__(128, 1)
     k_forward(const uint8_t* __restrict__ img, const float* __restrict__ x, int n, float* __restrict__ out,
-              __half* __restrict__ acts, int* err) {
+              __half* __restrict__ acts, int* err, const unsigned int* __restrict__ n_dev) {
   extern __shared__ __align__(1024) uint8_t sm[];
+  if (n_dev) n = (int)*n_dev;  // row count produced on the device (guided rendering)
   const int tid = threadIdx.x, warp = tid >> 5;
   for (int i = tid; i < (int)(kPackedBytes / 16); i += blockDim.x)
     reinterpret_cast<int4*>(sm)[i] = reinterpret_cast<const int4*>(img)[i];
@@ -504,9 +505,57 @@ static int guide_grid(tr_ctx* ctx, int n) {
 
 tr_status guide_forward(tr_ctx* ctx, const float* d_in, int n, float* d_out, __half* d_acts) {
   mlp::k_forward<<<guide_grid(ctx, n), 128, mlp::kSmemBytes, ctx->stream>>>(
-      ctx->guide->img.as<uint8_t>(), d_in, n, d_out, d_acts, ctx->d_err.as<int>() + 2);
+      ctx->guide->img.as<uint8_t>(), d_in, n, d_out, d_acts, ctx->d_err.as<int>() + 2, nullptr);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? TR_OK : cuda_fail(ctx, e, "k_forward");
+}
+
+tr_status guide_forward_rows_on_device(tr_ctx* ctx, const float* d_in, const unsigned int* d_n, float* d_out) {
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  mlp::k_forward<<<std::max(sms, 1), 128, mlp::kSmemBytes, ctx->stream>>>(
+      ctx->guide->img.as<uint8_t>(), d_in, 0, d_out, nullptr, ctx->d_err.as<int>() + 2, d_n);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? TR_OK : cuda_fail(ctx, e, "k_forward");
+}
+
+// Random batch of training records: rows idx = hash(seed, i) % count.
+__global__ void k_gather(const float* __restrict__ in, const float* __restrict__ dir, const float* __restrict__ w,
+                         unsigned int count, unsigned int batch, unsigned long long seed, float* __restrict__ bin,
+                         float* __restrict__ bdir, float* __restrict__ bw) {
+  const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= batch) return;
+  unsigned long long h = seed * 0x9E3779B97F4A7C15ull + i * 0xBF58476D1CE4E5B9ull + 0x94D049BB133111EBull;
+  h ^= h >> 31;
+  h *= 0xD6E8FEB86659FD93ull;
+  h ^= h >> 32;
+  const unsigned int j = (unsigned int)(h % count);
+  for (int k = 0; k < mlp::kIn; ++k) bin[(size_t)i * mlp::kIn + k] = in[(size_t)j * mlp::kIn + k];
+  for (int k = 0; k < 3; ++k) bdir[(size_t)i * 3 + k] = dir[(size_t)j * 3 + k];
+  bw[i] = w[j];
+}
+
+tr_status guide_train_on(tr_ctx* ctx, const float* rec_in, const float* rec_dir, const float* rec_w, unsigned int count,
+                         int steps, unsigned int batch, float lr, unsigned long long seed, float* mean_loss) {
+  GuideModel* g = ctx->guide;
+  cudaError_t e;
+  if ((e = g->batch.reserve((size_t)batch * 11 * 4)) != cudaSuccess) return cuda_fail(ctx, e, "training batch");
+  float* bin = g->batch.as<float>();
+  float* bdir = bin + (size_t)batch * 7;
+  float* bw = bdir + (size_t)batch * 3;
+  double sum = 0.0;
+  for (int s = 0; s < steps; ++s) {
+    k_gather<<<(batch + 255) / 256, 256, 0, ctx->stream>>>(rec_in, rec_dir, rec_w, count, batch,
+                                                            seed * 1000003ull + (unsigned long long)s, bin, bdir, bw);
+    tr_status st = guide_train_step(ctx, bin, bdir, bw, (int)batch, lr);
+    if (st != TR_OK) return st;
+    float l = 0.0f;
+    TR_CUDA(ctx, cudaMemcpyAsync(&l, g->scal.as<float>() + 1, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    TR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    sum += l;
+  }
+  if (mean_loss) *mean_loss = steps ? (float)(sum / steps) : 0.0f;
+  return TR_OK;
 }
 
 static tr_status guide_workspace(tr_ctx* ctx, int n) {
@@ -583,7 +632,7 @@ void release_guide(tr_ctx* ctx) {
   if (!ctx->guide) return;
   GuideModel* g = ctx->guide;
   for (DevBuf* b : {&g->params, &g->img, &g->img_t, &g->grads, &g->adam_m, &g->adam_v, &g->acts, &g->out, &g->dout,
-                    &g->scal})
+                    &g->scal, &g->batch})
     b->release();
   delete g;
   ctx->guide = nullptr;

@@ -26,6 +26,7 @@ struct GuideModel {
   DevBuf img_t;   // fp16 transposed weights of layers 1..4 (backward)
   DevBuf grads, adam_m, adam_v;
   DevBuf acts, out, dout, scal;  // training workspace (grown on demand)
+  DevBuf batch;                  // gathered training batch (in, dir, weight)
   int64_t step = 0;              // Adam steps taken
   bool attr_set = false;
 };
@@ -38,5 +39,10 @@ tr_status guide_backward(tr_ctx* ctx, const float* d_in, const float* d_dout, in
 // One Adam step on the weighted vMF-mixture NLL of a batch; *d_loss (device) receives the loss.
 tr_status guide_train_step(tr_ctx* ctx, const float* d_in, const float* d_dir, const float* d_w, int n, float lr);
 void release_guide(tr_ctx* ctx);
+// Forward pass over *d_n rows (a count produced on the device), no host sync.
+tr_status guide_forward_rows_on_device(tr_ctx* ctx, const float* d_in, const unsigned int* d_n, float* d_out);
+// `steps` Adam steps on random batches of `batch` rows drawn from `count` records.
+tr_status guide_train_on(tr_ctx* ctx, const float* rec_in, const float* rec_dir, const float* rec_w, unsigned int count,
+                         int steps, unsigned int batch, float lr, unsigned long long seed, float* mean_loss);
 
 }  // namespace trg

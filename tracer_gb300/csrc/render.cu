@@ -36,6 +36,7 @@
 #include <vector>
 
 #include "context.h"
+#include "mlp.h"
 #include "shade.cuh"
 #include "traverse.cuh"
 
@@ -45,6 +46,7 @@ enum : int {
   F_PENDING = 1,    // the previous vertex's direct lighting is still to be added
   F_MIS = 2,        // ...and it includes a MIS ray
   F_TERMINATE = 4,  // the path ends once that lighting is added
+  F_REC = 8,        // the previous vertex wrote a guiding record awaiting its radiance
 };
 
 enum : int {  // counter slots
@@ -55,6 +57,7 @@ enum : int {  // counter slots
   C_NEE = 7,      // 2: per-material light-sample queue sizes
   C_FEXT = 9,     // extend kernel's work-fetch position
   C_FSH = 10,     // shadow kernel's work-fetch position
+  C_TB = 11,      // guiding training records written (whole render)
   C_ERR = 15,     // traversal error word
 };
 
@@ -62,6 +65,8 @@ struct RenderBuffers {
   int n = 0, nl = 0;
   DevBuf P0, P1, P2, P3, P4, rng, M0, M1, M2, HC, HM, SC, NU, SH, acc, q_ext, q_act, q_mat, q_nee, q_sh, ctr,
       stats;
+  DevBuf VR, NV, gfeat, gout, tb;  // path guiding: vertex records, network rows, training records
+  unsigned int tb_count = 0, tb_cap = 0;  // training records of the last guided render
   unsigned int* h_active = nullptr;  // pinned: live-slot count per check
   std::vector<cudaEvent_t> ev_pool;  // reused by stage timing
 };
@@ -89,6 +94,79 @@ struct Launch {
   int* q_sh;
   unsigned int* ctr;
   unsigned long long* stats;  // samples, extend rays, shadow rays, shade items, visit counts (4-7)
+  // path guiding (alpha > 0: sample Lambertian continuations from the network's mixture;
+  // record: keep training records)
+  float guide_alpha;
+  int guide_record, maxd;
+  float gbox_lo[3], gbox_scale[3];
+  float* gfeat;  // network inputs, one row per entry of q_mat[0]
+  float* gout;   // network outputs (mixture parameters), same rows
+  float4* VR;    // 4 per (slot, vertex): features 0-3 | features 4-6, pdf | direction, throughput | radiance
+  int* NV;       // records of the slot's current sample
+  float *tb_in, *tb_dir, *tb_w;
+  unsigned int tb_cap;
+};
+
+// Network inputs of a vertex: position in the scene box mapped to [-1, 1],
+// outgoing direction, roughness.
+__device__ __forceinline__ void guide_features(const Launch& P, f3 pos, f3 wo, float rough, float (&f)[7]) {
+  f[0] = (pos.x - P.gbox_lo[0]) * P.gbox_scale[0] - 1.0f;
+  f[1] = (pos.y - P.gbox_lo[1]) * P.gbox_scale[1] - 1.0f;
+  f[2] = (pos.z - P.gbox_lo[2]) * P.gbox_scale[2] - 1.0f;
+  f[3] = wo.x;
+  f[4] = wo.y;
+  f[5] = wo.z;
+  f[6] = rough;
+}
+
+// The network's 8-lobe von Mises-Fisher mixture (parametrisation of the
+// guiding loss in mlp.cu).
+struct Mixture {
+  float pi[8], kappa[8], norm[8];
+  f3 mu[8];
+  __device__ void decode(const float* __restrict__ z) {
+    float amax = -INFINITY;
+    for (int j = 0; j < 8; ++j) amax = fmaxf(amax, z[5 * j]);
+    float sum = 0.0f;
+    for (int j = 0; j < 8; ++j) {
+      pi[j] = expf(z[5 * j] - amax);
+      sum += pi[j];
+    }
+    for (int j = 0; j < 8; ++j) {
+      pi[j] /= sum;
+      kappa[j] = expf(fminf(fmaxf(z[5 * j + 1], -4.0f), 7.0f));
+      norm[j] = kappa[j] / (6.283185307179586f * -expm1f(-2.0f * kappa[j]));
+      const f3 m = mk3(z[5 * j + 2], z[5 * j + 3], z[5 * j + 4]);
+      const float len = sqrtf(m.x * m.x + m.y * m.y + m.z * m.z) + 1e-6f;
+      mu[j] = mk3(m.x / len, m.y / len, m.z / len);
+    }
+  }
+  __device__ float pdf(f3 w) const {
+    float p = 0.0f;
+    for (int j = 0; j < 8; ++j) p += pi[j] * norm[j] * expf(kappa[j] * (dot(mu[j], w) - 1.0f));
+    return p;
+  }
+  // lobe by u_lobe, then the numerically stable vMF sampling of W. Jakob,
+  // "Numerically stable sampling of the von Mises-Fisher distribution on
+  // S^2" (2012), in the frame of the lobe's mean (Duff et al. 2017 basis).
+  __device__ f3 sample(float u_lobe, float u1, float u2) const {
+    int j = 0;
+    float c = pi[0];
+    while (j < 7 && u_lobe >= c) c += pi[++j];
+    const float k = kappa[j];
+    float w = 1.0f + logf(u1 + (1.0f - u1) * expf(-2.0f * k)) / k;
+    w = fminf(fmaxf(w, -1.0f), 1.0f);
+    const float r = sqrtf(fmaxf(0.0f, 1.0f - w * w));
+    float sp, cp;
+    sincosf(6.283185307179586f * u2, &sp, &cp);
+    const f3 n = mu[j];
+    const float sgn = copysignf(1.0f, n.z);
+    const float a = -1.0f / (sgn + n.z);
+    const float b = n.x * n.y * a;
+    const f3 b1 = mk3(1.0f + sgn * n.x * n.x * a, sgn * b, -sgn * n.x);
+    const f3 b2 = mk3(b, sgn + n.y * n.y * a, -n.y);
+    return scale(b1, r * cp) + scale(b2, r * sp) + scale(n, w);
+  }
 };
 
 // Warp-aggregated queue append. The active lanes are grouped by counter
@@ -210,6 +288,27 @@ __device__ __forceinline__ bool start_sample(const Launch& P, int slot, unsigned
 __device__ void finish_sample(const Launch& P, int slot, unsigned long long& st, f3 L, int nxt,
                               unsigned int& finished) {
   if (!valid3(L)) L = mk3(0.0f, 0.0f, 0.0f);  // eval_pixel_li returns {} (path_trace_renderer.cpp:204-209)
+  if (P.guide_record) {
+    // training records of this sample's vertices: the radiance that arrived
+    // along each continuation direction, (L - L_after_vertex) / throughput,
+    // over the pdf the direction was drawn with
+    const int nv = P.NV[slot];
+    for (int k = 0; k < nv; ++k) {
+      const float4* r = P.VR + ((size_t)slot * P.maxd + k) * 4;
+      const float4 a = r[0], b = r[1], c = r[2], d = r[3];
+      const float li = lum(mk3(L.x - d.x, L.y - d.y, L.z - d.z)) / fmaxf(c.w, 1e-20f);
+      const float w = li / b.w;
+      if (!(w > 0.0f) || !(w < 1e30f)) continue;
+      const unsigned int idx = (unsigned int)append(P.ctr + C_TB);
+      if (idx >= P.tb_cap) continue;
+      float* fi = P.tb_in + (size_t)idx * 7;
+      fi[0] = a.x; fi[1] = a.y; fi[2] = a.z; fi[3] = a.w; fi[4] = b.x; fi[5] = b.y; fi[6] = b.z;
+      float* di = P.tb_dir + (size_t)idx * 3;
+      di[0] = c.x; di[1] = c.y; di[2] = c.z;
+      P.tb_w[idx] = w;
+    }
+    P.NV[slot] = 0;
+  }
   const float px = P.P3[slot].w, py = P.P4[slot].w;
   film_add(P, slot, px, py, L);
   ++finished;
@@ -223,6 +322,7 @@ __global__ void __launch_bounds__(256) k_init(Launch P) {
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
     const int x = s % P.W, y = s / P.W;
     unsigned long long st = Pcg::seed((int)(P.seed_base + (unsigned)y * (unsigned)P.W + (unsigned)x));
+    if (P.guide_record) P.NV[s] = 0;
     const bool live = start_sample(P, s, st, 0, 0, finished);
     P.rng[s] = st;
     if (live) P.q_act[0][append(P.ctr + C_ACT)] = s;
@@ -335,6 +435,7 @@ __global__ void __launch_bounds__(128) k_logic(Launch P, int cur) {
       }
       if (flags & F_MIS) direct = direct + mulc(mk3(p4.x, p4.y, p4.z), mis_contribution(P, slot));
       L = L + direct;
+      if (flags & F_REC) P.VR[((size_t)slot * P.maxd + P.NV[slot] - 1) * 4 + 3] = make_float4(L.x, L.y, L.z, 0.0f);
     }
     const float4 hit = P.HC[slot];
     const int pid = __float_as_int(hit.x);
@@ -372,6 +473,48 @@ struct MatOps {
   }
 };
 
+// One-sample MIS of the network's mixture and the BSDF for the continuation
+// direction of a Lambertian vertex (Phong with no specular lobe, not a
+// fringe vertex). The integrand is exactly what the plain sampler returns
+// for a direction -- diffuse_coef times the normal correction, zero where
+// the plain sampler rejects (cosine pdf below 0.001) -- and the BSDF's
+// density there is the cosine pdf, so the estimator has the plain path's
+// expectation. With probability alpha the direction comes from the
+// mixture, else it is the plain sample already drawn.
+__device__ __noinline__ void guided_lambert(const Launch& P, const Bsdf& bsdf, const Isect& is, unsigned int row,
+                                            unsigned long long& st, BsdfSample& bs) {
+  const float sel = Pcg::next(st), g0 = Pcg::next(st), g1 = Pcg::next(st);
+  Mixture mx;
+  mx.decode(P.gout + (size_t)row * 40);
+  f3 wi;
+  if (sel < P.guide_alpha) {
+    wi = normalize(mx.sample(sel / P.guide_alpha, g0, g1));
+  } else {
+    wi = bs.wi;  // the plain sample (valid: the caller checked it)
+  }
+  const f3 lwo = normalize(to_local(bsdf.s, is.wo)), lwi = normalize(to_local(bsdf.s, wi));
+  const float pb = cosine_pdf(lwi.z);
+  const bool ok = lwo.z > 0.0f && pb >= 0.001f;
+  bs.wi = wi;
+  bs.f = ok ? muls(bsdf.m->diffuse_coef, normal_correct(bsdf.g, bsdf.s, wi)) : mk3(0.0f, 0.0f, 0.0f);
+  bs.pdf = P.guide_alpha * mx.pdf(wi) + (1.0f - P.guide_alpha) * (ok ? pb : 0.0f);
+}
+
+// Network inputs of every Phong-material vertex of this iteration (rows in
+// q_mat[0] order), for the guided continuation of k_material<MAT_PHONG>.
+__global__ void __launch_bounds__(128) k_features(Launch P) {
+  const unsigned int n = P.ctr[C_MAT + MAT_PHONG];
+  for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int slot = P.q_mat[MAT_PHONG][i];
+    const float4 p0 = P.P0[slot], p1 = P.P1[slot];
+    const f3 o = mk3(p0.x, p0.y, p0.z), d = mk3(p1.x, p1.y, p1.z);
+    float f[7];
+    guide_features(P, o + scale(d, P.HC[slot].y), -d, 1.0f, f);
+    float* out = P.gfeat + (size_t)i * 7;
+    for (int k = 0; k < 7; ++k) out[k] = f[k];
+  }
+}
+
 // The BSDF sample, shared out of line by the two call sites of k_material
 // (the path's sample and the MIS sample): one copy of the sampling code
 // instead of two keeps the kernel within the instruction cache.
@@ -404,12 +547,20 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
     bsdf.g = is.g;
     bsdf.s = is.s;
     const float u0 = Pcg::next(st), u1 = Pcg::next(st), u2 = Pcg::next(st);
-    const BsdfSample bs = sample_bsdf_shared<KIND>(bsdf, is.wo, u0, u1, u2);
+    BsdfSample bs = sample_bsdf_shared<KIND>(bsdf, is.wo, u0, u1, u2);
     if (black(bs.f) || bs.pdf < kEps) {
       const float4 p3 = P.P3[slot];
       finish_sample(P, slot, st, mk3(p3.x, p3.y, p3.z), nxt, finished);
       P.rng[slot] = st;
       continue;
+    }
+    // Guided continuation. The plain sample above still decides, as in the
+    // reference, whether this vertex gets direct lighting at all; a guided
+    // direction without contribution only ends the path after it.
+    bool guided_end = false;
+    if (KIND == MAT_PHONG && P.guide_alpha > 0.0f && bsdf.m->w_specular == 0.0f && !bsdf.fringe(is.wo)) {
+      guided_lambert(P, bsdf, is, i, st, bs);
+      guided_end = black(bs.f) || bs.pdf < kEps;
     }
     // next-event estimation on every light (sample_area_light): the draws
     // happen here, the rest in k_nee
@@ -447,7 +598,7 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
     }
     P.P4[slot] = make_float4(coef.x, coef.y, coef.z, P.P4[slot].w);
     coef = mulc(coef, divs(muls(bs.f, abs_cos(is.g.z, bs.wi)), bs.pdf));
-    bool term = !valid3(coef);
+    bool term = guided_end || !valid3(coef);
     if (!term) {
       ++depth;
       if (depth >= P.max_depth) {
@@ -466,6 +617,20 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
     } else {
       const f3 no = is.eps_offset(bs.wi);
       const f3 nd = normalize(normalize(bs.wi));
+      if (P.guide_record) {
+        const int nv = P.NV[slot];
+        if (nv < P.maxd) {
+          float f[7];
+          const float t = P.HC[slot].y;
+          guide_features(P, ro + scale(rd, t), -rd, KIND == MAT_PHONG ? 1.0f : bsdf.m->roughness, f);
+          float4* r = P.VR + ((size_t)slot * P.maxd + nv) * 4;
+          r[0] = make_float4(f[0], f[1], f[2], f[3]);
+          r[1] = make_float4(f[4], f[5], f[6], bs.pdf);
+          r[2] = make_float4(nd.x, nd.y, nd.z, lum(coef));
+          P.NV[slot] = nv + 1;
+          flags |= F_REC;
+        }
+      }
       P.P0[slot] = make_float4(no.x, no.y, no.z, __int_as_float(flags));
       P.P1[slot] = make_float4(nd.x, nd.y, nd.z, __int_as_float(depth));
       P.q_ext[nxt][append(P.ctr + C_EXT + nxt)] = 2 * slot;
@@ -541,7 +706,7 @@ void release_render(tr_ctx* ctx) {
   RenderBuffers* rb = ctx->rb;
   for (DevBuf* b : {&rb->P0, &rb->P1, &rb->P2, &rb->P3, &rb->P4, &rb->rng, &rb->M0, &rb->M1, &rb->M2, &rb->HC,
                     &rb->HM, &rb->SC, &rb->NU, &rb->SH, &rb->acc, &rb->q_ext, &rb->q_act, &rb->q_mat, &rb->q_nee,
-                    &rb->q_sh, &rb->ctr, &rb->stats})
+                    &rb->q_sh, &rb->ctr, &rb->stats, &rb->VR, &rb->NV, &rb->gfeat, &rb->gout, &rb->tb})
     b->release();
   if (rb->h_active) cudaFreeHost(rb->h_active);
   for (cudaEvent_t e : rb->ev_pool) cudaEventDestroy(e);
@@ -601,7 +766,7 @@ void setup_camera(Cam& c, const tr_camera& p) {
 }  // namespace
 
 tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter, const tr_render_params* prm,
-                      void* d_out, bool fp64, tr_stats* stats) {
+                      void* d_out, bool fp64, tr_stats* stats, const tr_guide_params* gp = nullptr) {
   if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
   if (prm->width <= 0 || prm->height <= 0 || prm->spp <= 0 || prm->max_depth < 0)
     return set_err(ctx, TR_ERR_ARG, "invalid render size, spp or depth");
@@ -656,6 +821,40 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
   P.q_sh = rb->q_sh.as<int>();
   P.ctr = rb->ctr.as<unsigned int>();
   P.stats = rb->stats.as<unsigned long long>();
+  if (gp) {
+    if (!(gp->alpha >= 0.0f && gp->alpha < 1.0f)) return set_err(ctx, TR_ERR_ARG, "guide alpha must be in [0, 1)");
+    if (gp->alpha > 0.0f && (!ctx->guide || !ctx->guide->params.p))
+      return set_err(ctx, TR_ERR_STATE, "guide model not initialised");
+    for (int k = 0; k < 3; ++k) {
+      if (!(gp->box_hi[k] > gp->box_lo[k])) return set_err(ctx, TR_ERR_ARG, "empty guide box");
+      P.gbox_lo[k] = gp->box_lo[k];
+      P.gbox_scale[k] = 2.0f / (gp->box_hi[k] - gp->box_lo[k]);
+    }
+    P.guide_alpha = gp->alpha;
+    P.guide_record = gp->record ? 1 : 0;
+    P.maxd = std::max(prm->max_depth, 1);
+    const size_t N = (size_t)n;
+    const unsigned int cap = gp->max_records ? gp->max_records : (4u << 20);
+    cudaError_t e = cudaSuccess;
+    if (P.guide_alpha > 0.0f) {
+      if ((e = rb->gfeat.reserve(N * 7 * 4)) != cudaSuccess || (e = rb->gout.reserve(N * 40 * 4)) != cudaSuccess)
+        return cuda_fail(ctx, e, "guide inference buffers");
+      P.gfeat = rb->gfeat.as<float>();
+      P.gout = rb->gout.as<float>();
+    }
+    if (P.guide_record) {
+      if ((e = rb->VR.reserve(N * P.maxd * 64)) != cudaSuccess || (e = rb->NV.reserve(N * 4)) != cudaSuccess ||
+          (e = rb->tb.reserve((size_t)cap * 11 * 4)) != cudaSuccess)
+        return cuda_fail(ctx, e, "guide record buffers");
+      P.VR = rb->VR.as<float4>();
+      P.NV = rb->NV.as<int>();
+      P.tb_in = rb->tb.as<float>();
+      P.tb_dir = P.tb_in + (size_t)cap * 7;
+      P.tb_w = P.tb_dir + (size_t)cap * 3;
+      P.tb_cap = cap;
+      rb->tb_cap = cap;
+    }
+  }
 
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
@@ -725,6 +924,15 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
       RCHK(cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 7, st));  // C_SH, C_MAT x2, C_NEE x2, C_FEXT, C_FSH
       mark();
       k_logic<<<grid, 128, 0, st>>>(P, cur);
+      if (P.guide_alpha > 0.0f) {
+        // network rows for this iteration's Phong-material vertices
+        k_features<<<grid, 128, 0, st>>>(P);
+        tr_status gs = guide_forward_rows_on_device(ctx, P.gfeat, P.ctr + C_MAT + MAT_PHONG, P.gout);
+        if (gs != TR_OK) {
+          cleanup();
+          return gs;
+        }
+      }
       mark();
       k_material<MAT_PHONG><<<grid, 128, 0, st>>>(P, cur);
       mark();
@@ -781,6 +989,15 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
   cudaEventElapsedTime(&ms, e0, e1);
   cleanup();
   if (ctrs[C_ERR] != 0 && result == TR_OK) result = set_err(ctx, TR_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
+  rb->tb_count = P.guide_record ? std::min(ctrs[C_TB], P.tb_cap) : 0;
+  if (P.guide_alpha > 0.0f && result == TR_OK) {
+    int ge = 0;
+    RCHK(cudaMemcpy(&ge, ctx->d_err.as<int>() + 2, 4, cudaMemcpyDeviceToHost));
+    if (ge) {
+      cudaMemset(ctx->d_err.as<int>() + 2, 0, 4);
+      result = set_err(ctx, TR_ERR_TIMEOUT, "tensor-core MMA wait timed out");
+    }
+  }
   if (stats) {
     stats->samples = hs[0];
     stats->extend_rays = hs[1];
@@ -793,6 +1010,7 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
     stats->closest_prims = hs[5];
     stats->any_boxes = hs[6];
     stats->any_prims = hs[7];
+    stats->guide_records = P.guide_record ? std::min(ctrs[C_TB], P.tb_cap) : 0;
   }
   return result;
 #undef RCHK
@@ -1002,6 +1220,40 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
 }
 
 }  // namespace trg
+
+extern "C" tr_status tr_render_guided_dev(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter,
+                                          const tr_render_params* params, const tr_guide_params* guide,
+                                          float* d_rgbw, double* d_rgbw64, tr_stats* stats) {
+  if (!ctx || !cam || !filter || !params || !guide || ((d_rgbw == nullptr) == (d_rgbw64 == nullptr))) return TR_ERR_ARG;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return trg::cuda_fail(ctx, e, "cudaSetDevice");
+  void* out = d_rgbw ? (void*)d_rgbw : (void*)d_rgbw64;
+  if (((uintptr_t)out & 15u) != 0) return trg::set_err(ctx, TR_ERR_ARG, "film buffer must be 16-byte aligned");
+  return trg::render_impl(ctx, cam, filter, params, out, d_rgbw64 != nullptr, stats, guide);
+}
+
+extern "C" tr_status tr_guide_train_on_records(tr_ctx* ctx, int32_t steps, uint32_t batch, float lr, uint64_t seed,
+                                               float* mean_loss) {
+  if (!ctx || steps < 0 || batch == 0 || batch > (1u << 22) || !(lr > 0.0f)) return TR_ERR_ARG;
+  if (!ctx->guide || !ctx->guide->params.p) return trg::set_err(ctx, TR_ERR_STATE, "guide model not initialised");
+  if (!ctx->rb || ctx->rb->tb_count == 0) return trg::set_err(ctx, TR_ERR_STATE, "no training records");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return trg::cuda_fail(ctx, e, "cudaSetDevice");
+  trg::RenderBuffers* rb = ctx->rb;
+  const float* in = rb->tb.as<float>();
+  const float* dir = in + (size_t)rb->tb_cap * 7;
+  const float* w = dir + (size_t)rb->tb_cap * 3;
+  tr_status s = trg::guide_train_on(ctx, in, dir, w, rb->tb_count, steps, batch, lr, seed, mean_loss);
+  if (s != TR_OK) return s;
+  int ge = 0;
+  e = cudaMemcpy(&ge, ctx->d_err.as<int>() + 2, 4, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return trg::cuda_fail(ctx, e, "guide error word");
+  if (ge) {
+    cudaMemset(ctx->d_err.as<int>() + 2, 0, 4);
+    return trg::set_err(ctx, TR_ERR_TIMEOUT, "tensor-core MMA wait timed out");
+  }
+  return TR_OK;
+}
 
 extern "C" tr_status tr_render_dev_noalloc(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter,
                                            const tr_render_params* params, float* d_rgbw, tr_stats* stats) {

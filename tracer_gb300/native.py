@@ -11,7 +11,7 @@ import os
 import numpy as np
 
 from . import build as _build
-from .abi import (NODE_DTYPE, RAY_DTYPE, TR_OK, TrBvhNode32, TrCamera, TrFilter, TrRay, TrRenderParams, TrTuning,
+from .abi import (NODE_DTYPE, RAY_DTYPE, TR_OK, TrBvhNode32, TrCamera, TrFilter, TrRay, TrRenderParams, TrTuning, TrGuideParams,
                   TrSceneDesc, TrStats)
 
 _lib = None
@@ -87,6 +87,11 @@ def lib() -> C.CDLL:
     L.tr_guide_train_step_dev.restype = st
     L.tr_guide_train_step_dev.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_float,
                                           C.POINTER(C.c_float)]
+    L.tr_render_guided_dev.restype = st
+    L.tr_render_guided_dev.argtypes = [vp, C.POINTER(TrCamera), C.POINTER(TrFilter), C.POINTER(TrRenderParams),
+                                       C.POINTER(TrGuideParams), C.c_void_p, C.c_void_p, C.POINTER(TrStats)]
+    L.tr_guide_train_on_records.restype = st
+    L.tr_guide_train_on_records.argtypes = [vp, C.c_int32, C.c_uint32, C.c_float, C.c_uint64, C.POINTER(C.c_float)]
     L.tr_render_dev.restype = st
     L.tr_render_dev.argtypes = [vp, C.POINTER(TrCamera), C.POINTER(TrFilter), C.POINTER(TrRenderParams),
                                 vp, vp, C.POINTER(TrStats)]
@@ -235,6 +240,18 @@ class GpuContext:
     def guide_train_step_dev(self, d_in: int, d_dir: int, d_w: int, n: int, lr: float = 1e-3) -> float:
         loss = C.c_float()
         self._check(self.L.tr_guide_train_step_dev(self.h, d_in, d_dir, d_w, n, lr, C.byref(loss)))
+        return loss.value
+
+    def render_guided_dev(self, cam: TrCamera, filt: TrFilter, params: TrRenderParams, guide: TrGuideParams,
+                          d_out: int, fp64: bool = False) -> TrStats:
+        stats = TrStats()
+        self._check(self.L.tr_render_guided_dev(self.h, C.byref(cam), C.byref(filt), C.byref(params), C.byref(guide),
+                                                None if fp64 else d_out, d_out if fp64 else None, C.byref(stats)))
+        return stats
+
+    def guide_train_on_records(self, steps: int, batch: int = 65536, lr: float = 1e-3, seed: int = 0) -> float:
+        loss = C.c_float()
+        self._check(self.L.tr_guide_train_on_records(self.h, steps, batch, lr, seed, C.byref(loss)))
         return loss.value
 
     def render_dev(self, cam: TrCamera, filt: TrFilter, params: TrRenderParams, d_out: int, fp64: bool = False):
