@@ -120,12 +120,25 @@ def _image(acc: np.ndarray) -> np.ndarray:
     return np.where(w > 0, acc[..., :3] / np.where(w > 0, w, 1.0), 0.0)
 
 
-def convergence(ctx, name: str, size=(256, 192), ref_spp=4096, pass_spp=4, max_spp=1024, target=0.01):
-    """Time for the plain GPU path tracer to reach `target` relMSE against a
-    converged reference of the same scene: the reference is ref_spp samples
-    per pixel accumulated in double; the plain run adds passes of pass_spp
-    samples with fresh per-pixel seeds, accumulating in double on the host,
-    and stops at the target or at max_spp. Times are the render calls only."""
+GUIDE_BOX = {"occluded_room": ((-4.0, 0.0, -3.0), (4.0, 4.0, 3.0))}
+
+
+def convergence(ctx, name: str, size=(256, 192), ref_spp=4096, pass_spp=4, max_spp=1024, target=0.01,
+                alpha=0.5, train_steps=32, warm_steps=200, batch=65536, lr=1e-3):
+    """Time for the plain and the guided GPU path tracer to reach `target`
+    relMSE against a converged reference of the same scene. The reference
+    is ref_spp samples per pixel accumulated in double. Each run adds
+    passes of pass_spp samples with fresh per-pixel seeds, accumulated in
+    double on the host, until the target or max_spp. The guided run starts
+    from an untrained network: its first pass renders plainly (alpha 0) and
+    records training data, every later pass samples Lambertian
+    continuations from the network's mixture with probability `alpha`,
+    records, and is followed by `train_steps` Adam steps on `batch` random
+    records (`warm_steps` more after the first pass; online training is
+    inside the timed region). If a training
+    loss is not finite the network is re-initialised and the next pass
+    renders plainly (the plain path is the fallback)."""
+    from tracer_gb300.abi import make_guide
     W, H = size
     _, sc, cam, filt, par = workload(name, f"{W}x{H}x{pass_spp}")
     ctx.upload(sc)
@@ -134,28 +147,57 @@ def convergence(ctx, name: str, size=(256, 192), ref_spp=4096, pass_spp=4, max_s
     ref_acc, _ = ctx.render(cam, filt, ref_par, fp64=True)
     ref_s = time.perf_counter() - t0
     ref = _image(ref_acc)
-    acc = np.zeros((H, W, 4), np.float64)
-    spent, curve, reached = 0.0, [], None
-    for k in range(max_spp // pass_spp):
-        p = scenes.make_params(W, H, pass_spp, par.min_depth, par.max_depth, seed_base=1 + k * W * H)
-        t0 = time.perf_counter()
-        out, _ = ctx.render(cam, filt, p, fp64=True)
-        spent += time.perf_counter() - t0
-        acc += out
-        spp = (k + 1) * pass_spp
-        e = rel_mse(_image(acc), ref)
-        if spp & (spp - 1) == 0 or e <= target:
-            curve.append([spp, round(spent, 4), round(e, 5)])
-        if e <= target:
-            reached = (spp, spent)
-            break
+    box = GUIDE_BOX.get(name)
+
+    def run(guided: bool):
+        import torch
+        film = torch.zeros((H, W, 4), dtype=torch.float64, device=f"cuda:{torch.cuda.current_device()}")
+        acc = np.zeros((H, W, 4), np.float64)
+        spent, curve, reached, losses = 0.0, [], None, []
+        use_alpha = 0.0
+        if guided:
+            ctx.guide_init(seed=0)
+        for k in range(max_spp // pass_spp):
+            p = scenes.make_params(W, H, pass_spp, par.min_depth, par.max_depth, seed_base=1 + k * W * H)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if guided:
+                ctx.render_guided_dev(cam, filt, p, make_guide(use_alpha, *box, record=True), film.data_ptr(),
+                                      fp64=True)
+                loss = ctx.guide_train_on_records(train_steps + (warm_steps if k == 0 else 0), batch, lr, seed=k)
+                if np.isfinite(loss):
+                    use_alpha = alpha
+                else:
+                    ctx.guide_init(seed=k + 1)
+                    use_alpha = 0.0
+                losses.append(round(float(loss), 4))
+                out = film.cpu().numpy()
+            else:
+                out, _ = ctx.render(cam, filt, p, fp64=True)
+            spent += time.perf_counter() - t0
+            acc += out
+            spp = (k + 1) * pass_spp
+            e = rel_mse(_image(acc), ref)
+            if spp & (spp - 1) == 0 or e <= target:
+                curve.append([spp, round(spent, 4), round(e, 5)])
+            if e <= target:
+                reached = (spp, spent)
+                break
+        res = {"time_to_target_s": reached[1] if reached else None,
+               "spp_at_target": reached[0] if reached else None,
+               "relmse_curve_spp_s_relmse": curve}
+        if guided:
+            res.update({"alpha": alpha, "train_steps_per_pass": train_steps, "warm_steps": warm_steps, "batch": batch,
+                        "lr": lr,
+                        "mean_loss_per_pass": losses[:8] + (["..."] if len(losses) > 9 else []) + losses[-1:]})
+        return res
+
     res = {"resolution": f"{W}x{H}", "reference_spp": ref_spp, "reference_s": round(ref_s, 2),
            "pass_spp": pass_spp, "target_relmse": target,
            "relmse": "mean over pixels and channels of (I - R)^2 / (R^2 + 1e-2)",
-           "plain": {"time_to_target_s": reached[1] if reached else None,
-                     "spp_at_target": reached[0] if reached else None,
-                     "relmse_curve_spp_s_relmse": curve},
-           "guided": None}
+           "plain": run(False), "guided": run(True) if box else None}
+    pt, gt = res["plain"]["time_to_target_s"], (res["guided"] or {}).get("time_to_target_s")
+    res["guided_over_plain_time"] = (gt / pt) if (pt and gt) else None
     return res
 
 

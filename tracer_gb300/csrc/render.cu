@@ -291,7 +291,7 @@ __device__ void finish_sample(const Launch& P, int slot, unsigned long long& st,
   if (P.guide_record) {
     // training records of this sample's vertices: the radiance that arrived
     // along each continuation direction, (L - L_after_vertex) / throughput,
-    // over the pdf the direction was drawn with
+    // times |cos| over the pdf the direction was drawn with
     const int nv = P.NV[slot];
     for (int k = 0; k < nv; ++k) {
       const float4* r = P.VR + ((size_t)slot * P.maxd + k) * 4;
@@ -473,31 +473,37 @@ struct MatOps {
   }
 };
 
-// One-sample MIS of the network's mixture and the BSDF for the continuation
-// direction of a Lambertian vertex (Phong with no specular lobe, not a
-// fringe vertex). The integrand is exactly what the plain sampler returns
+// Guided directions at a Lambertian vertex (Phong with no specular lobe, not
+// a fringe vertex). The integrand is exactly what the plain sampler returns
 // for a direction -- diffuse_coef times the normal correction, zero where
 // the plain sampler rejects (cosine pdf below 0.001) -- and the BSDF's
-// density there is the cosine pdf, so the estimator has the plain path's
-// expectation. With probability alpha the direction comes from the
-// mixture, else it is the plain sample already drawn.
-__device__ __noinline__ void guided_lambert(const Launch& P, const Bsdf& bsdf, const Isect& is, unsigned int row,
-                                            unsigned long long& st, BsdfSample& bs) {
-  const float sel = Pcg::next(st), g0 = Pcg::next(st), g1 = Pcg::next(st);
+// density there is the cosine pdf, so a one-sample MIS of the network's
+// mixture (probability alpha) and the BSDF keeps the plain estimator's
+// expectation.
+__device__ __forceinline__ float lambert_plain_pdf(const Bsdf& bsdf, f3 wo, f3 wi) {
+  const f3 lwo = normalize(to_local(bsdf.s, wo)), lwi = normalize(to_local(bsdf.s, wi));
+  const float pb = cosine_pdf(lwi.z);
+  return (lwo.z > 0.0f && pb >= 0.001f) ? pb : 0.0f;
+}
+
+// Replaces the plain sample `bs` by the one-sample MIS choice: with
+// probability alpha (sel < alpha) a mixture direction, else the plain
+// sample itself (which may be invalid: then nothing is returned).
+__device__ __noinline__ void guided_pick(const Launch& P, const Bsdf& bsdf, const Isect& is, unsigned int row,
+                                         float sel, float g0, float g1, BsdfSample& bs) {
   Mixture mx;
   mx.decode(P.gout + (size_t)row * 40);
   f3 wi;
   if (sel < P.guide_alpha) {
     wi = normalize(mx.sample(sel / P.guide_alpha, g0, g1));
   } else {
-    wi = bs.wi;  // the plain sample (valid: the caller checked it)
+    if (!bs.valid()) return;
+    wi = bs.wi;
   }
-  const f3 lwo = normalize(to_local(bsdf.s, is.wo)), lwi = normalize(to_local(bsdf.s, wi));
-  const float pb = cosine_pdf(lwi.z);
-  const bool ok = lwo.z > 0.0f && pb >= 0.001f;
+  const float pb = lambert_plain_pdf(bsdf, is.wo, wi);
   bs.wi = wi;
-  bs.f = ok ? muls(bsdf.m->diffuse_coef, normal_correct(bsdf.g, bsdf.s, wi)) : mk3(0.0f, 0.0f, 0.0f);
-  bs.pdf = P.guide_alpha * mx.pdf(wi) + (1.0f - P.guide_alpha) * (ok ? pb : 0.0f);
+  bs.f = pb > 0.0f ? muls(bsdf.m->diffuse_coef, normal_correct(bsdf.g, bsdf.s, wi)) : mk3(0.0f, 0.0f, 0.0f);
+  bs.pdf = P.guide_alpha * mx.pdf(wi) + (1.0f - P.guide_alpha) * pb;
 }
 
 // Network inputs of every Phong-material vertex of this iteration (rows in
@@ -558,8 +564,11 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
     // reference, whether this vertex gets direct lighting at all; a guided
     // direction without contribution only ends the path after it.
     bool guided_end = false;
-    if (KIND == MAT_PHONG && P.guide_alpha > 0.0f && bsdf.m->w_specular == 0.0f && !bsdf.fringe(is.wo)) {
-      guided_lambert(P, bsdf, is, i, st, bs);
+    const bool gv =
+        KIND == MAT_PHONG && P.guide_alpha > 0.0f && bsdf.m->w_specular == 0.0f && !bsdf.fringe(is.wo);
+    if (gv) {
+      const float sel = Pcg::next(st), g0 = Pcg::next(st), g1 = Pcg::next(st);
+      guided_pick(P, bsdf, is, i, sel, g0, g1, bs);
       guided_end = black(bs.f) || bs.pdf < kEps;
     }
     // next-event estimation on every light (sample_area_light): the draws
@@ -625,7 +634,9 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
           guide_features(P, ro + scale(rd, t), -rd, KIND == MAT_PHONG ? 1.0f : bsdf.m->roughness, f);
           float4* r = P.VR + ((size_t)slot * P.maxd + nv) * 4;
           r[0] = make_float4(f[0], f[1], f[2], f[3]);
-          r[1] = make_float4(f[4], f[5], f[6], bs.pdf);
+          // training target: incident radiance times |cos| (the Lambertian
+          // product), over the pdf the direction was drawn with
+          r[1] = make_float4(f[4], f[5], f[6], bs.pdf / fmaxf(abs_cos(is.g.z, bs.wi), 1e-6f));
           r[2] = make_float4(nd.x, nd.y, nd.z, lum(coef));
           P.NV[slot] = nv + 1;
           flags |= F_REC;
