@@ -193,11 +193,14 @@ tr_status tr_synchronize(tr_ctx* ctx);
  *  - trav_blocks_per_sm: resident 128-thread blocks per SM of the
  *    persistent traversal kernels (0: as many as fit);
  *  - shade_blocks_per_sm: 128-thread blocks per SM of the shading kernels
- *    (grid-stride loops). */
+ *    (grid-stride loops);
+ *  - graph_iterations: wavefront iterations captured into one CUDA graph
+ *    and replayed as one launch (rounded up to even; 0: no graph). */
 typedef struct tr_tuning {
   int32_t trav_refill_lanes;
   int32_t trav_blocks_per_sm;
   int32_t shade_blocks_per_sm;
+  int32_t graph_iterations;
 } tr_tuning;
 tr_status tr_ctx_set_tuning(tr_ctx* ctx, const tr_tuning* t);
 tr_status tr_ctx_get_tuning(const tr_ctx* ctx, tr_tuning* t);
@@ -208,6 +211,12 @@ tr_status tr_ctx_get_tuning(const tr_ctx* ctx, tr_tuning* t);
  * src/core/scene.cpp:49-53). The BVH is built on the host with the
  * reference's algorithm, so the tree and the leaf order are the reference's. */
 tr_status tr_scene_upload(tr_ctx* ctx, const tr_scene_desc* desc);
+/* A set of scenes for batched rendering (tr_render_batch_dev), replacing the
+ * context's scene: each is built like tr_scene_upload (its own reference
+ * BVH; scenes are built on parallel host threads) and the device tables are
+ * concatenated. Scene 0 is the one tr_trace_* and tr_render* use. No
+ * reference counterpart (the reference renders one scene per call). */
+tr_status tr_scene_set_upload(tr_ctx* ctx, const tr_scene_desc* descs, uint32_t n);
 
 /* Size and contents of the built BVH in the reference layout
  * (BVHAccel::linear_nodes / primitives, src/accelerator/bvh.cpp:311-312).
@@ -272,6 +281,21 @@ tr_status tr_render_dev(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filt
  *    tr_cancel does not stop it; stats->device_ms and stage_ms stay 0. */
 tr_status tr_render_dev_noalloc(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter,
                                 const tr_render_params* params, float* d_rgbw, tr_stats* stats);
+
+/* Batched rendering. No reference counterpart. Many renders -- any scenes
+ * of the uploaded set (tr_scene_set_upload), each with its own camera,
+ * filter, size, spp, depths and seeds -- run in one wavefront: their path
+ * slots share the queues and every kernel launch, so small films keep the
+ * GPU as full as one large one. Results equal rendering the jobs one by
+ * one with tr_render_dev (float films). The flags of jobs[0] apply. */
+typedef struct tr_batch_job {
+  uint32_t scene;
+  tr_camera camera;
+  tr_filter filter;
+  tr_render_params params;
+  float* d_rgbw; /* device film sums, 4 * width * height floats, 16-byte aligned */
+} tr_batch_job;
+tr_status tr_render_batch_dev(tr_ctx* ctx, const tr_batch_job* jobs, uint32_t n, tr_stats* stats);
 
 /* Asks a running tr_render on this context to stop after its current
  * wavefront iteration; that call then returns TR_ERR_CANCELLED. Thread-safe. */

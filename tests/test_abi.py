@@ -60,4 +60,4 @@ def test_status_strings():
 
 def test_tuning_struct_layout():
     from tracer_gb300.abi import TrTuning
-    assert ctypes.sizeof(TrTuning) == 12
+    assert ctypes.sizeof(TrTuning) == 16

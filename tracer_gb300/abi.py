@@ -105,7 +105,12 @@ class TrGuideParams(C.Structure):
 
 class TrTuning(C.Structure):
     _fields_ = [("trav_refill_lanes", C.c_int32), ("trav_blocks_per_sm", C.c_int32),
-                ("shade_blocks_per_sm", C.c_int32)]
+                ("shade_blocks_per_sm", C.c_int32), ("graph_iterations", C.c_int32)]
+
+
+class TrBatchJob(C.Structure):
+    _fields_ = [("scene", C.c_uint32), ("camera", TrCamera), ("filter", TrFilter), ("params", TrRenderParams),
+                ("d_rgbw", C.c_void_p)]
 
 
 def ptr(a: np.ndarray | None, ctype):

@@ -11,6 +11,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <thread>
+#include <atomic>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -170,6 +172,37 @@ tr_status upload_device_tables(tr_ctx* ctx) {
   TR_CUDA(ctx, put(ctx->d_tshade, hs.tshade.data(), hs.tshade.size() * sizeof(DTriShade)));
   TR_CUDA(ctx, put(ctx->d_mats, hs.mats.data(), hs.mats.size() * sizeof(DMat)));
   TR_CUDA(ctx, put(ctx->d_lights, hs.lights.data(), hs.lights.size() * sizeof(DLight)));
+
+  // one root per scene of the set
+  const size_t nsc = hs.scene_node.size();
+  std::vector<SceneRoot> roots(nsc);
+  int max_lights = 0;
+  for (size_t k = 0; k < nsc; ++k) {
+    SceneRoot& R = roots[k];
+    std::memset(&R, 0, sizeof(R));
+    const size_t first = hs.scene_node[k], end = k + 1 < nsc ? hs.scene_node[k + 1] : nn;
+    R.light_base = (int)hs.scene_light[k];
+    R.num_lights = (int)hs.scene_nlight[k];
+    max_lights = std::max(max_lights, R.num_lights);
+    if (first >= end) {
+      R.kind = 0;
+      continue;
+    }
+    const tr_bvh_node32& r = hs.nodes[first];
+    for (int c = 0; c < 3; ++c) {
+      R.lo[c] = r.lo[c];
+      R.hi[c] = r.hi[c];
+    }
+    if (r.count > 0) {
+      R.kind = 2;
+      R.offset = r.offset;
+      R.count = r.count;
+    } else {
+      R.kind = 1;
+      R.offset = dix[first];
+    }
+  }
+  TR_CUDA(ctx, put(ctx->d_roots, roots.data(), roots.size() * sizeof(SceneRoot)));
   TR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
 
   DScene& sc = ctx->dsc;
@@ -180,25 +213,9 @@ tr_status upload_device_tables(tr_ctx* ctx) {
   sc.tshade = ctx->d_tshade.as<DTriShade>();
   sc.mats = ctx->d_mats.as<DMat>();
   sc.lights = ctx->d_lights.as<DLight>();
-  sc.num_lights = (int)hs.lights.size();
-  if (nn == 0) {
-    sc.root_kind = 0;
-  } else {
-    const tr_bvh_node32& r = hs.nodes[0];
-    for (int k = 0; k < 3; ++k) {
-      sc.root_lo[k] = r.lo[k];
-      sc.root_hi[k] = r.hi[k];
-    }
-    if (r.count > 0) {
-      sc.root_kind = 2;
-      sc.root_offset = r.offset;
-      sc.root_count = r.count;
-    } else {
-      sc.root_kind = 1;
-      sc.root_offset = 0;
-      sc.root_count = 0;
-    }
-  }
+  sc.roots = ctx->d_roots.as<SceneRoot>();
+  sc.num_scenes = (int)nsc;
+  sc.max_lights = max_lights;
   ctx->has_scene = true;
   return TR_OK;
 }
@@ -212,7 +229,8 @@ struct BatchJob {
   float* tout;
   uint8_t* hit;
   __device__ __forceinline__ unsigned int count() const { return n; }
-  __device__ __forceinline__ void load(unsigned int i, f3& o, f3& d, float& t_min, float& t_max) const {
+  __device__ __forceinline__ void load(unsigned int i, f3& o, f3& d, float& t_min, float& t_max, int& scene) const {
+    scene = 0;
     const float4 r0 = __ldg(rays + 2 * (size_t)i), r1 = __ldg(rays + 2 * (size_t)i + 1);
     o = mk3(r0.x, r0.y, r0.z);
     d = mk3(r0.w, r1.x, r1.y);
@@ -311,7 +329,7 @@ void tr_ctx_destroy(tr_ctx* ctx) {
   release_render(ctx);
   release_guide(ctx);
   for (DevBuf* b : {&ctx->d_nodes, &ctx->d_slots, &ctx->d_spheres, &ctx->d_prims, &ctx->d_tshade, &ctx->d_mats,
-                    &ctx->d_lights, &ctx->d_rays, &ctx->d_out0, &ctx->d_out1, &ctx->d_err})
+                    &ctx->d_lights, &ctx->d_roots, &ctx->d_rays, &ctx->d_out0, &ctx->d_out1, &ctx->d_err})
     b->release();
   cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -323,7 +341,8 @@ void* tr_ctx_stream(tr_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 tr_status tr_ctx_set_tuning(tr_ctx* ctx, const tr_tuning* t) {
   if (!ctx || !t) return TR_ERR_ARG;
   if (t->trav_refill_lanes < 1 || t->trav_refill_lanes > 32 || t->trav_blocks_per_sm < 0 ||
-      t->trav_blocks_per_sm > 64 || t->shade_blocks_per_sm < 1 || t->shade_blocks_per_sm > 64)
+      t->trav_blocks_per_sm > 64 || t->shade_blocks_per_sm < 1 || t->shade_blocks_per_sm > 64 ||
+      t->graph_iterations < 0 || t->graph_iterations > 64)
     return set_err(ctx, TR_ERR_ARG, "tuning out of range");
   ctx->tune = *t;
   return TR_OK;
@@ -341,9 +360,8 @@ tr_status tr_synchronize(tr_ctx* ctx) {
   return TR_OK;
 }
 
-tr_status tr_scene_upload(tr_ctx* ctx, const tr_scene_desc* d) {
-  if (!ctx || !d) return TR_ERR_ARG;
-  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+// Host tables and reference BVH of one scene description.
+static tr_status build_host_scene(tr_ctx* ctx, const tr_scene_desc* d, HostScene& hs) {
   if (d->num_vertices && (!d->positions || !d->normals || !d->uvs))
     return set_err(ctx, TR_ERR_ARG, "vertex arrays missing");
   if (d->num_triangles && !d->indices) return set_err(ctx, TR_ERR_ARG, "indices missing");
@@ -363,8 +381,6 @@ tr_status tr_scene_upload(tr_ctx* ctx, const tr_scene_desc* d) {
   for (uint32_t s = 0; s < d->num_spheres; ++s)
     if (!(d->sphere_radius[s] > 0.0f)) return set_err(ctx, TR_ERR_ARG, "invalid sphere radius");  // sphere.cpp:88-90
 
-  ctx->has_scene = false;
-  HostScene hs;
   // Mesh vertices through the identity local_to_world, normals normalised
   // at creation (triangle.cpp:224-228) and again on first use (:182-184).
   std::vector<f3> P(d->num_vertices), N(d->num_vertices);
@@ -483,6 +499,80 @@ tr_status tr_scene_upload(tr_ctx* ctx, const tr_scene_desc* d) {
   BvhResult bvh = build_reference_bvh(lo.data(), hi.data(), np, d->max_leaf_prims);
   hs.nodes = std::move(bvh.nodes);
   hs.order = std::move(bvh.order);
+  hs.scene_node = {0};
+  hs.scene_light = {0};
+  hs.scene_nlight = {(uint32_t)hs.lights.size()};
+  return TR_OK;
+}
+
+// Concatenates scene `src` into `dst`, offsetting every index.
+static void append_scene(HostScene& dst, const HostScene& src) {
+  const uint32_t node_base = (uint32_t)dst.nodes.size(), order_base = (uint32_t)dst.order.size();
+  const uint32_t prim_base = (uint32_t)dst.prims.size(), tri_base = (uint32_t)dst.tshade.size();
+  const uint32_t sph_base = (uint32_t)dst.spheres.size(), mat_base = (uint32_t)dst.mats.size();
+  const uint32_t light_base = (uint32_t)dst.lights.size();
+  dst.scene_node.push_back(node_base);
+  dst.scene_light.push_back(light_base);
+  dst.scene_nlight.push_back((uint32_t)src.lights.size());
+  for (tr_bvh_node32 n : src.nodes) {
+    n.offset += (int32_t)(n.count > 0 ? order_base : node_base);
+    dst.nodes.push_back(n);
+  }
+  for (uint32_t o : src.order) dst.order.push_back(o + prim_base);
+  for (DPrim p : src.prims) {
+    p.shape += (int)(p.kind == PRIM_TRIANGLE ? tri_base : sph_base);
+    p.material += (int)mat_base;
+    dst.prims.push_back(p);
+  }
+  dst.tshade.insert(dst.tshade.end(), src.tshade.begin(), src.tshade.end());
+  dst.spheres.insert(dst.spheres.end(), src.spheres.begin(), src.spheres.end());
+  dst.mats.insert(dst.mats.end(), src.mats.begin(), src.mats.end());
+  for (DLight l : src.lights) {
+    l.prim += (int)prim_base;
+    dst.lights.push_back(l);
+  }
+  dst.A.insert(dst.A.end(), src.A.begin(), src.A.end());
+  dst.AB.insert(dst.AB.end(), src.AB.begin(), src.AB.end());
+  dst.AC.insert(dst.AC.end(), src.AC.begin(), src.AC.end());
+}
+
+tr_status tr_scene_upload(tr_ctx* ctx, const tr_scene_desc* d) {
+  if (!ctx || !d) return TR_ERR_ARG;
+  return tr_scene_set_upload(ctx, d, 1);
+}
+
+tr_status tr_scene_set_upload(tr_ctx* ctx, const tr_scene_desc* descs, uint32_t n) {
+  if (!ctx || !descs || n == 0 || n > 65536) return TR_ERR_ARG;
+  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  ctx->has_scene = false;
+  // each scene's tables and tree on its own host thread
+  std::vector<HostScene> parts(n);
+  std::vector<tr_status> st(n, TR_OK);
+  std::vector<std::string> msg(n);
+  const unsigned int workers = std::max(1u, std::min(n, std::thread::hardware_concurrency()));
+  std::atomic<uint32_t> next{0};
+  auto work = [&]() {
+    tr_ctx scratch;  // per-thread error sink
+    for (uint32_t k; (k = next.fetch_add(1)) < n;) {
+      st[k] = build_host_scene(&scratch, descs + k, parts[k]);
+      if (st[k] != TR_OK) msg[k] = scratch.err;
+    }
+  };
+  std::vector<std::thread> pool;
+  for (unsigned int w = 1; w < workers; ++w) pool.emplace_back(work);
+  work();
+  for (auto& t : pool) t.join();
+  for (uint32_t k = 0; k < n; ++k)
+    if (st[k] != TR_OK) return set_err(ctx, st[k], "scene " + std::to_string(k) + ": " + msg[k]);
+  HostScene hs;
+  if (n == 1) {
+    hs = std::move(parts[0]);
+  } else {
+    for (uint32_t k = 0; k < n; ++k) {
+      append_scene(hs, parts[k]);
+      HostScene().A.swap(parts[k].A);  // release as we go
+    }
+  }
   ctx->hs = std::move(hs);
   return upload_device_tables(ctx);
 }
@@ -507,6 +597,7 @@ tr_status tr_bvh_upload(tr_ctx* ctx, const tr_bvh_node32* nodes, size_t num_node
                         size_t num_prims) {
   if (!ctx || (num_nodes && !nodes) || (num_prims && !prim_order)) return TR_ERR_ARG;
   if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
+  if (ctx->hs.scene_node.size() != 1) return set_err(ctx, TR_ERR_STATE, "tr_bvh_upload replaces the tree of a single scene");
   TR_CUDA(ctx, cudaSetDevice(ctx->device));
   std::vector<tr_bvh_node32> keep_nodes = ctx->hs.nodes;
   std::vector<uint32_t> keep_order = ctx->hs.order;

@@ -48,6 +48,8 @@ struct HostScene {
   std::vector<DLight> lights;
   std::vector<f3> A, AB, AC;  // per triangle
   int depth = 0;
+  // scene set: first node, first light and light count of every scene
+  std::vector<uint32_t> scene_node, scene_light, scene_nlight;
 };
 
 struct RenderBuffers;  // render.cu
@@ -61,11 +63,11 @@ struct tr_ctx {
   bool has_scene = false;
   trg::HostScene hs;
   trg::DScene dsc{};
-  trg::DevBuf d_nodes, d_slots, d_spheres, d_prims, d_tshade, d_mats, d_lights;
+  trg::DevBuf d_nodes, d_slots, d_spheres, d_prims, d_tshade, d_mats, d_lights, d_roots;
   trg::DevBuf d_rays, d_out0, d_out1, d_err;
   std::atomic<int> cancel{0};
   trg::RenderBuffers* rb = nullptr;
-  tr_tuning tune{20, 0, 16};
+  tr_tuning tune{20, 0, 16, 8};
   trg::GuideModel* guide = nullptr;
 };
 

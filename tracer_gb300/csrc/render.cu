@@ -66,19 +66,31 @@ struct RenderBuffers {
   DevBuf P0, P1, P2, P3, P4, rng, M0, M1, M2, HC, HM, SC, NU, SH, acc, q_ext, q_act, q_mat, q_nee, q_sh, ctr,
       stats;
   DevBuf VR, NV, gfeat, gout, tb;  // path guiding: vertex records, network rows, training records
+  DevBuf jobs;                      // JobDev table of the current render
   unsigned int tb_count = 0, tb_cap = 0;  // training records of the last guided render
   unsigned int* h_active = nullptr;  // pinned: live-slot count per check
   std::vector<cudaEvent_t> ev_pool;  // reused by stage timing
 };
 
-struct Launch {
-  DScene sc;
+// One render of a batch: a scene of the set seen through a camera onto a
+// film. Its path slots are slot_base .. slot_base + W * H - 1, one per pixel.
+struct JobDev {
   Cam cam;
-  int W, H, spp, min_depth, max_depth, nl;
-  unsigned seed_base;
+  int W, H, spp, min_depth, max_depth;
+  unsigned int seed_base;
+  int scene, slot_base;
+  int light_base, nl;  // the scene's lights in DScene::lights
   float filter_radius, filter_alpha, filter_exp;
   int fp64;
-  int refill;                      // traversal lane-refill threshold (tr_tuning)
+  float4* film;  // film sums (float4 per pixel, or 2 x double2)
+};
+
+struct Launch {
+  DScene sc;
+  const JobDev* jobs;
+  int njobs, nslots;
+  int nl_max;  // stride of the per-(slot, light) records
+  int refill;  // traversal lane-refill threshold (tr_tuning)
   float4 *P0, *P1, *P2, *P3, *P4;  // cont o|flags, cont d|depth, coef|sample, L|px, coef_prev|py
   unsigned long long* rng;
   float4 *M0, *M1, *M2;  // mis o|bsdf_pdf, mis d|abs_cos, bsdf_f
@@ -86,7 +98,6 @@ struct Launch {
   float4* SC;            // shading context for nee: 7 per slot (pos|mat, wo, g, s frames)
   float2* NU;            // light-sample draws per (slot, light)
   float4* SH;            // shadow: 3 per (slot, light): o|t_max, d, contrib|valid
-  float4* acc;           // film sums (float4) or 2 x double2 per pixel
   int* q_ext[2];
   int* q_act[2];
   int* q_mat[2];
@@ -106,6 +117,17 @@ struct Launch {
   float *tb_in, *tb_dir, *tb_w;
   unsigned int tb_cap;
 };
+
+// The job a path slot belongs to (slot bases ascend with the job index).
+__device__ __forceinline__ const JobDev& job_of(const Launch& P, int slot) {
+  int lo = 0, hi = P.njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (P.jobs[mid].slot_base <= slot) lo = mid;
+    else hi = mid - 1;
+  }
+  return P.jobs[lo];
+}
 
 // Network inputs of a vertex: position in the scene box mapped to [-1, 1],
 // outgoing direction, roughness.
@@ -196,14 +218,15 @@ __device__ __forceinline__ void count_add(unsigned long long* c, unsigned int v)
 // Film::Tile::add_sample (src/core/render.hpp:37-57). With radius <= 0.5 a
 // sample reaches only its own pixel with non-zero weight (neighbours get
 // exactly 0), so the slot owns its pixel and adds in sample order.
-__device__ __forceinline__ void film_add(const Launch& P, int slot, float px, float py, f3 L) {
-  const int x = slot % P.W, y = slot / P.W;
-  if (P.filter_radius <= 0.5f) {
+__device__ __forceinline__ void film_add(const JobDev& J, int slot, float px, float py, f3 L) {
+  const int pix = slot - J.slot_base;
+  const int x = pix % J.W, y = pix / J.W;
+  if (J.filter_radius <= 0.5f) {
     const float ox = px - ((float)x + 0.5f), oy = py - ((float)y + 0.5f);  // exact for W, H < 2^23
-    const float fw = gaussian(P.filter_alpha, ox, P.filter_exp) * gaussian(P.filter_alpha, oy, P.filter_exp);
+    const float fw = gaussian(J.filter_alpha, ox, J.filter_exp) * gaussian(J.filter_alpha, oy, J.filter_exp);
     const f3 c = muls(muls(L, fw), 1.0f);
-    if (P.fp64) {
-      double2* a = reinterpret_cast<double2*>(P.acc) + 2 * slot;
+    if (J.fp64) {
+      double2* a = reinterpret_cast<double2*>(J.film) + 2 * pix;
       double2 a0 = a[0], a1 = a[1];
       a0.x += c.x;
       a0.y += c.y;
@@ -212,34 +235,34 @@ __device__ __forceinline__ void film_add(const Launch& P, int slot, float px, fl
       a[0] = a0;
       a[1] = a1;
     } else {
-      float4 a = P.acc[slot];
+      float4 a = J.film[pix];
       a.x += c.x;
       a.y += c.y;
       a.z += c.z;
       a.w += fw;
-      P.acc[slot] = a;
+      J.film[pix] = a;
     }
     return;
   }
   // wider filters: scatter with atomics (order of additions not fixed)
-  const float r = P.filter_radius;
+  const float r = J.filter_radius;
   const float dx = px - 0.5f, dy = py - 0.5f;
   const int x0 = max((int)ceilf(dx - r), 0), y0 = max((int)ceilf(dy - r), 0);
-  const int x1 = min((int)floorf(dx + r) + 1, P.W), y1 = min((int)floorf(dy + r) + 1, P.H);
+  const int x1 = min((int)floorf(dx + r) + 1, J.W), y1 = min((int)floorf(dy + r) + 1, J.H);
   for (int yy = y0; yy < y1; ++yy)
     for (int xx = x0; xx < x1; ++xx) {
       const float ox = px - ((float)xx + 0.5f), oy = py - ((float)yy + 0.5f);
-      const float fw = gaussian(P.filter_alpha, ox, P.filter_exp) * gaussian(P.filter_alpha, oy, P.filter_exp);
+      const float fw = gaussian(J.filter_alpha, ox, J.filter_exp) * gaussian(J.filter_alpha, oy, J.filter_exp);
       const f3 c = muls(muls(L, fw), 1.0f);
-      const int o = yy * P.W + xx;
-      if (P.fp64) {
-        double* a = reinterpret_cast<double*>(P.acc) + 4 * o;
+      const int o = yy * J.W + xx;
+      if (J.fp64) {
+        double* a = reinterpret_cast<double*>(J.film) + 4 * o;
         atomicAdd(a, (double)c.x);
         atomicAdd(a + 1, (double)c.y);
         atomicAdd(a + 2, (double)c.z);
         atomicAdd(a + 3, (double)fw);
       } else {
-        float* a = reinterpret_cast<float*>(P.acc) + 4 * o;
+        float* a = reinterpret_cast<float*>(J.film) + 4 * o;
         atomicAdd(a, c.x);
         atomicAdd(a + 1, c.y);
         atomicAdd(a + 2, c.z);
@@ -253,22 +276,24 @@ __device__ __forceinline__ void film_add(const Launch& P, int slot, float px, fl
 // no samples left.
 __device__ __forceinline__ bool start_sample(const Launch& P, int slot, unsigned long long& st, int sample,
                                              int next_q, unsigned int& finished) {
-  const int x = slot % P.W, y = slot / P.W;
-  while (sample < P.spp) {
+  const JobDev& J = job_of(P, slot);
+  const int pix = slot - J.slot_base;
+  const int x = pix % J.W, y = pix / J.W;
+  while (sample < J.spp) {
     const float fu = Pcg::next(st), fv = Pcg::next(st);
     const float lu = Pcg::next(st), lv = Pcg::next(st);
     const float px = (float)x + fu, py = (float)y + fv;
     f3 o, d;
-    camera_ray(P.cam, px / (float)P.W, py / (float)P.H, lu, lv, o, d);
+    camera_ray(J.cam, px / (float)J.W, py / (float)J.H, lu, lv, o, d);
     f3 coef = mk3(1.0f, 1.0f, 1.0f);
     bool dead = false;
-    if (0 > P.min_depth) {  // Russian roulette at depth 0
+    if (0 > J.min_depth) {  // Russian roulette at depth 0
       if (Pcg::next(st) > 0.9f) dead = true;
       else coef = divs(coef, 0.9f);
     }
     if (!dead && !valid3(coef)) dead = true;
     if (dead) {
-      film_add(P, slot, px, py, mk3(0.0f, 0.0f, 0.0f));
+      film_add(J, slot, px, py, mk3(0.0f, 0.0f, 0.0f));
       ++finished;
       ++sample;
       continue;
@@ -310,18 +335,20 @@ __device__ void finish_sample(const Launch& P, int slot, unsigned long long& st,
     P.NV[slot] = 0;
   }
   const float px = P.P3[slot].w, py = P.P4[slot].w;
-  film_add(P, slot, px, py, L);
+  film_add(job_of(P, slot), slot, px, py, L);
   ++finished;
   const int sample = __float_as_int(P.P2[slot].w) + 1;
   if (start_sample(P, slot, st, sample, nxt, finished)) P.q_act[nxt][append(P.ctr + C_ACT + nxt)] = slot;
 }
 
 __global__ void __launch_bounds__(256) k_init(Launch P) {
-  const int n = P.W * P.H;
+  const int n = P.nslots;
   unsigned int finished = 0;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
-    const int x = s % P.W, y = s / P.W;
-    unsigned long long st = Pcg::seed((int)(P.seed_base + (unsigned)y * (unsigned)P.W + (unsigned)x));
+    const JobDev& J = job_of(P, s);
+    const int pix = s - J.slot_base;
+    const int x = pix % J.W, y = pix / J.W;
+    unsigned long long st = Pcg::seed((int)(J.seed_base + (unsigned)y * (unsigned)J.W + (unsigned)x));
     if (P.guide_record) P.NV[s] = 0;
     const bool live = start_sample(P, s, st, 0, 0, finished);
     P.rng[s] = st;
@@ -335,9 +362,10 @@ struct ExtendJob {
   const Launch& P;
   int cur;
   __device__ __forceinline__ unsigned int count() const { return P.ctr[C_EXT + cur]; }
-  __device__ __forceinline__ void load(unsigned int i, f3& o, f3& d, float& t_min, float& t_max) const {
+  __device__ __forceinline__ void load(unsigned int i, f3& o, f3& d, float& t_min, float& t_max, int& scene) const {
     const int e = P.q_ext[cur][i];
     const int slot = e >> 1;
+    scene = job_of(P, slot).scene;
     const float4 a = (e & 1) ? P.M0[slot] : P.P0[slot];
     const float4 b = (e & 1) ? P.M1[slot] : P.P1[slot];
     o = mk3(a.x, a.y, a.z);
@@ -357,8 +385,9 @@ struct ExtendJob {
 struct ShadowJob {
   const Launch& P;
   __device__ __forceinline__ unsigned int count() const { return P.ctr[C_SH]; }
-  __device__ __forceinline__ void load(unsigned int i, f3& o, f3& d, float& t_min, float& t_max) const {
+  __device__ __forceinline__ void load(unsigned int i, f3& o, f3& d, float& t_min, float& t_max, int& scene) const {
     const int r = P.q_sh[i];
+    scene = job_of(P, r / P.nl_max).scene;
     const float4 a = P.SH[3 * r], b = P.SH[3 * r + 1];
     o = mk3(a.x, a.y, a.z);
     d = mk3(b.x, b.y, b.z);
@@ -429,8 +458,9 @@ __global__ void __launch_bounds__(128) k_logic(Launch P, int cur) {
       // lights in scene order, then the MIS term, then L += direct
       const float4 p4 = P.P4[slot];
       f3 direct = mk3(0.0f, 0.0f, 0.0f);
-      for (int l = 0; l < P.nl; ++l) {
-        const float4 c = P.SH[3 * (slot * P.nl + l) + 2];
+      const int nl = job_of(P, slot).nl;
+      for (int l = 0; l < nl; ++l) {
+        const float4 c = P.SH[3 * (slot * P.nl_max + l) + 2];
         if (c.w != 0.0f) direct = direct + mk3(c.x, c.y, c.z);
       }
       if (flags & F_MIS) direct = direct + mulc(mk3(p4.x, p4.y, p4.z), mis_contribution(P, slot));
@@ -573,13 +603,14 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
     }
     // next-event estimation on every light (sample_area_light): the draws
     // happen here, the rest in k_nee
-    for (int l = 0; l < P.nl; ++l) {
+    const JobDev& J = job_of(P, slot);
+    for (int l = 0; l < J.nl; ++l) {
       const float lu = Pcg::next(st), lv = Pcg::next(st);
       Pcg::next(st);
       Pcg::next(st);
       Pcg::next(st);
-      P.NU[slot * P.nl + l] = make_float2(lu, lv);
-      P.q_nee[KIND][append(P.ctr + C_NEE + KIND)] = slot * P.nl + l;
+      P.NU[slot * P.nl_max + l] = make_float2(lu, lv);
+      P.q_nee[KIND][append(P.ctr + C_NEE + KIND)] = slot * P.nl_max + l;
     }
     float4* sc = P.SC + 7 * (size_t)slot;
     sc[0] = make_float4(is.pos.x, is.pos.y, is.pos.z, __int_as_float(mat));
@@ -610,9 +641,9 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
     bool term = guided_end || !valid3(coef);
     if (!term) {
       ++depth;
-      if (depth >= P.max_depth) {
+      if (depth >= J.max_depth) {
         term = true;
-      } else if (depth > P.min_depth) {
+      } else if (depth > J.min_depth) {
         if (Pcg::next(st) > 0.9f) term = true;
         else {
           coef = divs(coef, 0.9f);
@@ -661,7 +692,7 @@ __global__ void __launch_bounds__(128) k_nee(Launch P) {
   const unsigned int n = P.ctr[C_NEE + KIND];
   for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int item = P.q_nee[KIND][i];
-    const int slot = item / P.nl, l = item - slot * P.nl;
+    const int slot = item / P.nl_max, l = item - slot * P.nl_max;
     const float4* sc = P.SC + 7 * (size_t)slot;
     const float4 a = sc[0], b = sc[1], c = sc[2], d = sc[3], e = sc[4], f = sc[5], g = sc[6];
     const f3 pos = mk3(a.x, a.y, a.z), wo = mk3(b.x, b.y, b.z);
@@ -674,7 +705,7 @@ __global__ void __launch_bounds__(128) k_nee(Launch P) {
     bsdf.s.y = mk3(e.w, f.x, f.y);
     bsdf.s.z = mk3(f.z, f.w, g.x);
     const float2 uv = P.NU[item];
-    const DLight& lt = P.sc.lights[l];
+    const DLight& lt = P.sc.lights[job_of(P, slot).light_base + l];
     float4* rec = P.SH + 3 * (size_t)item;
     bool ok = false;
     // Triangle::sample via UniformSampleTriangle (src/shape/triangle.cpp:61-97)
@@ -717,7 +748,7 @@ void release_render(tr_ctx* ctx) {
   RenderBuffers* rb = ctx->rb;
   for (DevBuf* b : {&rb->P0, &rb->P1, &rb->P2, &rb->P3, &rb->P4, &rb->rng, &rb->M0, &rb->M1, &rb->M2, &rb->HC,
                     &rb->HM, &rb->SC, &rb->NU, &rb->SH, &rb->acc, &rb->q_ext, &rb->q_act, &rb->q_mat, &rb->q_nee,
-                    &rb->q_sh, &rb->ctr, &rb->stats, &rb->VR, &rb->NV, &rb->gfeat, &rb->gout, &rb->tb})
+                    &rb->q_sh, &rb->ctr, &rb->stats, &rb->VR, &rb->NV, &rb->gfeat, &rb->gout, &rb->tb, &rb->jobs})
     b->release();
   if (rb->h_active) cudaFreeHost(rb->h_active);
   for (cudaEvent_t e : rb->ev_pool) cudaEventDestroy(e);
@@ -776,38 +807,92 @@ void setup_camera(Cam& c, const tr_camera& p) {
 
 }  // namespace
 
-tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter, const tr_render_params* prm,
-                      void* d_out, bool fp64, tr_stats* stats, const tr_guide_params* gp = nullptr) {
-  if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
+// One render of a batch as the host describes it.
+struct JobSpec {
+  int scene;
+  tr_camera cam;
+  tr_filter filter;
+  tr_render_params prm;
+  void* film;  // device sums (float4 or 2 x double2 per pixel); null: the context's film buffer
+  bool fp64;
+};
+
+static tr_status validate_job(tr_ctx* ctx, const JobSpec& j) {
+  const tr_render_params* prm = &j.prm;
+  if (j.scene < 0 || j.scene >= ctx->dsc.num_scenes) return set_err(ctx, TR_ERR_ARG, "scene index out of range");
   if (prm->width <= 0 || prm->height <= 0 || prm->spp <= 0 || prm->max_depth < 0)
     return set_err(ctx, TR_ERR_ARG, "invalid render size, spp or depth");
   if ((long long)prm->width * prm->height > (1ll << 28)) return set_err(ctx, TR_ERR_ARG, "film too large");
   if (prm->direct_light_sample_num != 1)
     return set_err(ctx, TR_ERR_UNSUPPORTED, "direct_light_sample_num must be 1 on the GPU path");
-  if (!(filter->radius > 0.0f) || filter->radius > 16.0f) return set_err(ctx, TR_ERR_ARG, "invalid filter radius");
-  const int n = prm->width * prm->height;
-  const int nl = ctx->dsc.num_lights;
+  if (!(j.filter.radius > 0.0f) || j.filter.radius > 16.0f) return set_err(ctx, TR_ERR_ARG, "invalid filter radius");
+  if (j.film && ((uintptr_t)j.film & 15u) != 0) return set_err(ctx, TR_ERR_ARG, "film buffer must be 16-byte aligned");
+  return TR_OK;
+}
+
+static JobDev make_job_dev(tr_ctx* ctx, const JobSpec& j, int slot_base, void* film) {
+  JobDev J;
+  std::memset(&J, 0, sizeof(J));
+  setup_camera(J.cam, j.cam);
+  J.W = j.prm.width;
+  J.H = j.prm.height;
+  J.spp = j.prm.spp;
+  J.min_depth = j.prm.min_depth;
+  J.max_depth = j.prm.max_depth;
+  J.seed_base = j.prm.seed_base;
+  J.scene = j.scene;
+  J.slot_base = slot_base;
+  J.light_base = (int)ctx->hs.scene_light[j.scene];
+  J.nl = (int)ctx->hs.scene_nlight[j.scene];
+  J.filter_radius = j.filter.radius;
+  J.filter_alpha = j.filter.alpha;
+  J.filter_exp = std::exp(-j.filter.alpha * j.filter.radius * j.filter.radius);  // GaussianFilter ctor
+  J.fp64 = j.fp64 ? 1 : 0;
+  J.film = static_cast<float4*>(film);
+  return J;
+}
+
+tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flags, tr_stats* stats,
+                      const tr_guide_params* gp = nullptr) {
+  if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
+  if (njobs <= 0) return set_err(ctx, TR_ERR_ARG, "no jobs");
+  long long total = 0;
+  long long max_iters = 0;  // every slot finishes within spp * (max_depth + 2) iterations
+  for (int k = 0; k < njobs; ++k) {
+    tr_status v = validate_job(ctx, jobs[k]);
+    if (v != TR_OK) return v;
+    if (!jobs[k].film && njobs != 1) return set_err(ctx, TR_ERR_ARG, "batch jobs need device films");
+    total += (long long)jobs[k].prm.width * jobs[k].prm.height;
+    max_iters = std::max(max_iters, (long long)jobs[k].prm.spp * (jobs[k].prm.max_depth + 2) + 4);
+  }
+  if (total > (1ll << 28)) return set_err(ctx, TR_ERR_ARG, "batch too large");
+  const int n = (int)total;
+  const int nl = ctx->dsc.max_lights;
   if ((long long)n * std::max(nl, 1) > (1ll << 30)) return set_err(ctx, TR_ERR_ARG, "too many shadow records");
   tr_status s = reserve_render(ctx, n, nl);
   if (s != TR_OK) return s;
   RenderBuffers* rb = ctx->rb;
   cudaStream_t st = ctx->stream;
+  cudaError_t ce = rb->jobs.reserve((size_t)njobs * sizeof(JobDev));
+  if (ce != cudaSuccess) return cuda_fail(ctx, ce, "job table");
+  std::vector<JobDev> jd(njobs);
+  {
+    int base = 0;
+    for (int k = 0; k < njobs; ++k) {
+      jd[k] = make_job_dev(ctx, jobs[k], base, jobs[k].film ? jobs[k].film : rb->acc.p);
+      base += jobs[k].prm.width * jobs[k].prm.height;
+    }
+  }
+  ce = cudaMemcpyAsync(rb->jobs.p, jd.data(), jd.size() * sizeof(JobDev), cudaMemcpyHostToDevice, st);
+  if (ce != cudaSuccess) return cuda_fail(ctx, ce, "job table upload");
 
   Launch P;
   std::memset(&P, 0, sizeof(P));
   P.sc = ctx->dsc;
-  setup_camera(P.cam, *cam);
-  P.W = prm->width;
-  P.H = prm->height;
-  P.spp = prm->spp;
-  P.min_depth = prm->min_depth;
-  P.max_depth = prm->max_depth;
-  P.nl = nl;
-  P.seed_base = prm->seed_base;
-  P.filter_radius = filter->radius;
-  P.filter_alpha = filter->alpha;
-  P.filter_exp = std::exp(-filter->alpha * filter->radius * filter->radius);  // GaussianFilter ctor
-  P.fp64 = fp64 ? 1 : 0;
+  P.jobs = rb->jobs.as<JobDev>();
+  P.njobs = njobs;
+  P.nslots = n;
+  P.nl_max = std::max(nl, 1);
   P.P0 = rb->P0.as<float4>();
   P.P1 = rb->P1.as<float4>();
   P.P2 = rb->P2.as<float4>();
@@ -822,7 +907,6 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
   P.SC = rb->SC.as<float4>();
   P.NU = rb->NU.as<float2>();
   P.SH = rb->SH.as<float4>();
-  P.acc = d_out ? static_cast<float4*>(d_out) : rb->acc.as<float4>();
   for (int k = 0; k < 2; ++k) {
     P.q_ext[k] = rb->q_ext.as<int>() + (size_t)k * 2 * n;
     P.q_act[k] = rb->q_act.as<int>() + (size_t)k * n;
@@ -833,6 +917,7 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
   P.ctr = rb->ctr.as<unsigned int>();
   P.stats = rb->stats.as<unsigned long long>();
   if (gp) {
+    if (njobs != 1) return set_err(ctx, TR_ERR_ARG, "guided rendering takes one job");
     if (!(gp->alpha >= 0.0f && gp->alpha < 1.0f)) return set_err(ctx, TR_ERR_ARG, "guide alpha must be in [0, 1)");
     if (gp->alpha > 0.0f && (!ctx->guide || !ctx->guide->params.p))
       return set_err(ctx, TR_ERR_STATE, "guide model not initialised");
@@ -843,7 +928,7 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
     }
     P.guide_alpha = gp->alpha;
     P.guide_record = gp->record ? 1 : 0;
-    P.maxd = std::max(prm->max_depth, 1);
+    P.maxd = std::max(jobs[0].prm.max_depth, 1);
     const size_t N = (size_t)n;
     const unsigned int cap = gp->max_records ? gp->max_records : (4u << 20);
     cudaError_t e = cudaSuccess;
@@ -880,13 +965,18 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventCreateWithFlags(&chk, cudaEventDisableTiming);
-  const bool timed = (prm->flags & TR_RENDER_TIME_STAGES) != 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  const bool timed = (flags & TR_RENDER_TIME_STAGES) != 0;
+  const bool count = (flags & TR_RENDER_COUNT_VISITS) != 0;
   std::vector<cudaEvent_t>& ev = rb->ev_pool;
   size_t nev = 0;
   auto cleanup = [&]() {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaEventDestroy(chk);
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
   };
 #define RCHK(call)                      \
   do {                                  \
@@ -896,7 +986,8 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
       return cuda_fail(ctx, e_, #call); \
     }                                   \
   } while (0)
-  RCHK(cudaMemsetAsync(P.acc, 0, (size_t)n * (fp64 ? 32 : 16), st));
+  for (int k = 0; k < njobs; ++k)
+    RCHK(cudaMemsetAsync(jd[k].film, 0, (size_t)jd[k].W * jd[k].H * (jd[k].fp64 ? 32 : 16), st));
   RCHK(cudaMemsetAsync(P.ctr, 0, 64, st));
   RCHK(cudaMemsetAsync(P.stats, 0, 64, st));
   RCHK(cudaEventRecord(e0, st));
@@ -914,48 +1005,73 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
     }
     cudaEventRecord(ev[nev++], st);
   };
-  const bool count = (prm->flags & TR_RENDER_COUNT_VISITS) != 0;
-  // Every slot finishes within spp * (max_depth + 2) iterations.
-  const long long max_iters = (long long)prm->spp * (prm->max_depth + 2) + 4;
-  const int chunk = 4;
+  // one wavefront iteration; returns the first launch error
+  auto iteration = [&](int cur) -> tr_status {
+    const int nxt = cur ^ 1;
+    mark();
+    if (count) k_extend<true><<<grid_ext, 128, 0, st>>>(P, cur);
+    else k_extend<false><<<grid_ext, 128, 0, st>>>(P, cur);
+    mark();
+    // next iteration's extend and live counts; this iteration's shadow,
+    // material and light-sample counts and the fetch positions
+    cudaMemsetAsync(P.ctr + C_EXT + nxt, 0, 4, st);
+    cudaMemsetAsync(P.ctr + C_ACT + nxt, 0, 4, st);
+    cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 7, st);  // C_SH, C_MAT x2, C_NEE x2, C_FEXT, C_FSH
+    mark();
+    k_logic<<<grid, 128, 0, st>>>(P, cur);
+    if (P.guide_alpha > 0.0f) {
+      // network rows for this iteration's Phong-material vertices
+      k_features<<<grid, 128, 0, st>>>(P);
+      tr_status gs = guide_forward_rows_on_device(ctx, P.gfeat, P.ctr + C_MAT + MAT_PHONG, P.gout);
+      if (gs != TR_OK) return gs;
+    }
+    mark();
+    k_material<MAT_PHONG><<<grid, 128, 0, st>>>(P, cur);
+    mark();
+    k_material<MAT_DISNEY12><<<grid, 128, 0, st>>>(P, cur);
+    mark();
+    k_nee<MAT_PHONG><<<grid, 128, 0, st>>>(P);
+    mark();
+    k_nee<MAT_DISNEY12><<<grid, 128, 0, st>>>(P);
+    mark();
+    if (count) k_shadow<true><<<grid_sh, 128, 0, st>>>(P);
+    else k_shadow<false><<<grid_sh, 128, 0, st>>>(P);
+    mark();
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? TR_OK : cuda_fail(ctx, e, "wavefront launch");
+  };
+  // Without per-kernel instrumentation, a chunk of iterations (an even
+  // number, so each chunk starts on the same queue parity) is captured once
+  // into a CUDA graph and replayed: one launch per chunk instead of ten
+  // per iteration. The host still polls the live count between chunks.
+  const int chunk = (!timed && !count && ctx->tune.graph_iterations > 0) ? (ctx->tune.graph_iterations + 1) & ~1 : 4;
+  if (!timed && !count && ctx->tune.graph_iterations > 0) {
+    RCHK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    tr_status cs = TR_OK;
+    for (int c = 0; c < chunk && cs == TR_OK; ++c) cs = iteration(c & 1);
+    cudaError_t ee = cudaStreamEndCapture(st, &graph);
+    if (cs != TR_OK) {
+      cleanup();
+      return cs;
+    }
+    RCHK(ee);
+    RCHK(cudaGraphInstantiate(&gexec, graph, 0));
+  }
   long long it = 0;
   bool done = false, chk_pending = false;
   tr_status result = TR_OK;
   while (!done) {
-    for (int c = 0; c < chunk && it < max_iters; ++c, ++it) {
-      const int cur = (int)(it & 1), nxt = cur ^ 1;
-      mark();
-      if (count) k_extend<true><<<grid_ext, 128, 0, st>>>(P, cur);
-      else k_extend<false><<<grid_ext, 128, 0, st>>>(P, cur);
-      mark();
-      // next iteration's extend and live counts; this iteration's shadow,
-      // material and light-sample counts
-      RCHK(cudaMemsetAsync(P.ctr + C_EXT + nxt, 0, 4, st));
-      RCHK(cudaMemsetAsync(P.ctr + C_ACT + nxt, 0, 4, st));
-      RCHK(cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 7, st));  // C_SH, C_MAT x2, C_NEE x2, C_FEXT, C_FSH
-      mark();
-      k_logic<<<grid, 128, 0, st>>>(P, cur);
-      if (P.guide_alpha > 0.0f) {
-        // network rows for this iteration's Phong-material vertices
-        k_features<<<grid, 128, 0, st>>>(P);
-        tr_status gs = guide_forward_rows_on_device(ctx, P.gfeat, P.ctr + C_MAT + MAT_PHONG, P.gout);
-        if (gs != TR_OK) {
+    if (gexec) {
+      RCHK(cudaGraphLaunch(gexec, st));
+      it += chunk;
+    } else {
+      for (int c = 0; c < chunk && it < max_iters; ++c, ++it) {
+        tr_status is = iteration((int)(it & 1));
+        if (is != TR_OK) {
           cleanup();
-          return gs;
+          return is;
         }
       }
-      mark();
-      k_material<MAT_PHONG><<<grid, 128, 0, st>>>(P, cur);
-      mark();
-      k_material<MAT_DISNEY12><<<grid, 128, 0, st>>>(P, cur);
-      mark();
-      k_nee<MAT_PHONG><<<grid, 128, 0, st>>>(P);
-      mark();
-      k_nee<MAT_DISNEY12><<<grid, 128, 0, st>>>(P);
-      mark();
-      if (count) k_shadow<true><<<grid_sh, 128, 0, st>>>(P);
-      else k_shadow<false><<<grid_sh, 128, 0, st>>>(P);
-      mark();
     }
     RCHK(cudaGetLastError());
     if (chk_pending) {
@@ -1010,6 +1126,7 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
     }
   }
   if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
     stats->samples = hs[0];
     stats->extend_rays = hs[1];
     stats->shadow_rays = hs[2];
@@ -1021,10 +1138,22 @@ tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter
     stats->closest_prims = hs[5];
     stats->any_boxes = hs[6];
     stats->any_prims = hs[7];
-    stats->guide_records = P.guide_record ? std::min(ctrs[C_TB], P.tb_cap) : 0;
+    stats->guide_records = rb->tb_count;
   }
   return result;
 #undef RCHK
+}
+
+tr_status render_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter, const tr_render_params* prm,
+                      void* d_out, bool fp64, tr_stats* stats, const tr_guide_params* gp = nullptr) {
+  JobSpec j;
+  j.scene = 0;
+  j.cam = *cam;
+  j.filter = *filter;
+  j.prm = *prm;
+  j.film = d_out;
+  j.fp64 = fp64;
+  return render_jobs(ctx, &j, 1, prm->flags, stats, gp);
 }
 
 }  // namespace trg
@@ -1095,7 +1224,7 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   if (!(filter->radius > 0.0f) || filter->radius > 16.0f) return set_err(ctx, TR_ERR_ARG, "invalid filter radius");
   if (ctx->device < 0 || ctx->device >= kMaxDevices) return set_err(ctx, TR_ERR_ARG, "device ordinal out of range");
   const long long npix = (long long)prm->width * prm->height;
-  const int nl = ctx->dsc.num_lights;
+  const int nl = ctx->dsc.max_lights;
   const size_t NL = (size_t)std::max(nl, 1);
   // carve the layout first: reject what does not fit before touching the device
   const size_t N = npix > (1ll << 24) ? (size_t(1) << 24) : (size_t)npix;
@@ -1104,7 +1233,8 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   const size_t oP = L.take(5 * N * f4), oRng = L.take(N * 8), oM = L.take(3 * N * f4), oH = L.take(2 * N * f4),
                oSC = L.take(N * 7 * f4), oNU = L.take(N * NL * 8), oSH = L.take(N * NL * 3 * f4),
                oQe = L.take(2 * 2 * N * 4), oQa = L.take(2 * N * 4), oQm = L.take(2 * N * 4),
-               oQn = L.take(2 * N * NL * 4), oQs = L.take(N * NL * 4), oCtr = L.take(64), oSt = L.take(64);
+               oQn = L.take(2 * N * NL * 4), oQs = L.take(N * NL * 4), oCtr = L.take(64), oSt = L.take(64),
+               oJob = L.take(sizeof(JobDev));
   if (npix > (1ll << 24) || L.off > kNoAllocScratchBytes) {
     char msg[256];
     std::snprintf(msg, sizeof(msg),
@@ -1127,22 +1257,30 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
     base = static_cast<unsigned char*>(g_noalloc_base[ctx->device]);
   }
   cudaStream_t st = ctx->stream;
+#define NCHK(call)                                      \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+  JobSpec spec;
+  spec.scene = 0;
+  spec.cam = *cam;
+  spec.filter = *filter;
+  spec.prm = *prm;
+  spec.film = d_rgbw;
+  spec.fp64 = false;
+  const JobDev job = make_job_dev(ctx, spec, 0, d_rgbw);
+  // the job record is copied from host stack memory into the array
+  NCHK(cudaMemcpyAsync(base + oJob, &job, sizeof(job), cudaMemcpyHostToDevice, st));
 
   Launch P;
   std::memset(&P, 0, sizeof(P));
   P.sc = ctx->dsc;
-  setup_camera(P.cam, *cam);
-  P.W = prm->width;
-  P.H = prm->height;
-  P.spp = prm->spp;
-  P.min_depth = prm->min_depth;
-  P.max_depth = prm->max_depth;
-  P.nl = nl;
-  P.seed_base = prm->seed_base;
-  P.filter_radius = filter->radius;
-  P.filter_alpha = filter->alpha;
-  P.filter_exp = std::exp(-filter->alpha * filter->radius * filter->radius);  // GaussianFilter ctor
-  P.fp64 = 0;
+  P.jobs = reinterpret_cast<const JobDev*>(base + oJob);
+  P.njobs = 1;
+  P.nslots = n;
+  P.nl_max = (int)NL;
+  P.refill = ctx->tune.trav_refill_lanes;
   float4* Pb = reinterpret_cast<float4*>(base + oP);
   P.P0 = Pb;
   P.P1 = Pb + N;
@@ -1159,7 +1297,6 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   P.SC = reinterpret_cast<float4*>(base + oSC);
   P.NU = reinterpret_cast<float2*>(base + oNU);
   P.SH = reinterpret_cast<float4*>(base + oSH);
-  P.acc = reinterpret_cast<float4*>(d_rgbw);
   int* qe = reinterpret_cast<int*>(base + oQe);
   int* qa = reinterpret_cast<int*>(base + oQa);
   int* qm = reinterpret_cast<int*>(base + oQm);
@@ -1180,15 +1317,9 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   const int grid = sms * ctx->tune.shade_blocks_per_sm, grid_init = sms * 8;
   const int grid_ext = traversal_grid(ctx, (const void*)k_extend<false>);
   const int grid_sh = traversal_grid(ctx, (const void*)k_shadow<false>);
-  P.refill = ctx->tune.trav_refill_lanes;
-#define NCHK(call)                                      \
-  do {                                                  \
-    cudaError_t e_ = (call);                            \
-    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
-  } while (0)
   // the counters, statistics and film start at zero on every call; the
   // rest of the scratch is written before it is read
-  NCHK(cudaMemsetAsync(P.acc, 0, (size_t)n * 16, st));
+  NCHK(cudaMemsetAsync(d_rgbw, 0, (size_t)n * 16, st));
   NCHK(cudaMemsetAsync(P.ctr, 0, 64, st));
   NCHK(cudaMemsetAsync(P.stats, 0, 64, st));
   k_init<<<grid_init, 256, 0, st>>>(P);
@@ -1231,6 +1362,23 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
 }
 
 }  // namespace trg
+
+extern "C" tr_status tr_render_batch_dev(tr_ctx* ctx, const tr_batch_job* jobs, uint32_t n, tr_stats* stats) {
+  if (!ctx || !jobs || n == 0 || n > (1u << 20)) return TR_ERR_ARG;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return trg::cuda_fail(ctx, e, "cudaSetDevice");
+  std::vector<trg::JobSpec> spec(n);
+  for (uint32_t k = 0; k < n; ++k) {
+    if (!jobs[k].d_rgbw) return trg::set_err(ctx, TR_ERR_ARG, "batch job without a film");
+    spec[k].scene = (int)jobs[k].scene;
+    spec[k].cam = jobs[k].camera;
+    spec[k].filter = jobs[k].filter;
+    spec[k].prm = jobs[k].params;
+    spec[k].film = jobs[k].d_rgbw;
+    spec[k].fp64 = false;
+  }
+  return trg::render_jobs(ctx, spec.data(), (int)n, jobs[0].params.flags, stats);
+}
 
 extern "C" tr_status tr_render_guided_dev(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter,
                                           const tr_render_params* params, const tr_guide_params* guide,

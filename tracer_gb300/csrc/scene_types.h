@@ -95,6 +95,17 @@ struct DLight {
   int pad[2];
 };
 
+// Root of one scene of the uploaded set: its tree and its lights.
+struct SceneRoot {
+  int kind;    // 0 empty, 1 interior (DNode `offset`), 2 leaf (slots offset .. offset + count)
+  int offset, count;
+  int light_base, num_lights;  // the scene's lights in DScene::lights
+  float lo[3], hi[3];          // root box
+  int pad;
+};
+
+// The device tables of a scene set: every scene's nodes, slots, primitives,
+// materials and lights concatenated, indices already offset.
 struct DScene {
   const DNode* nodes;
   const float4* slots;
@@ -103,10 +114,9 @@ struct DScene {
   const DTriShade* tshade;
   const DMat* mats;
   const DLight* lights;
-  int num_lights;
-  int root_kind;  // 0 empty, 1 interior (DNode 0), 2 leaf
-  int root_offset, root_count;
-  float root_lo[3], root_hi[3];
+  const SceneRoot* roots;
+  int num_scenes;
+  int max_lights;  // most lights of one scene
 };
 
 }  // namespace trg

@@ -182,8 +182,10 @@ struct TravLane {
   bool occluded;
   StackEntry st[kStack];
 
-  // Starts a ray; returns false when it misses the root box (done at once).
-  __device__ __forceinline__ bool start(const DScene& sc, f3 o_, f3 d_, float tmin_, float tmax_, VisitCount& vc) {
+  // Starts a ray in scene `scene` of the set; returns false when it misses
+  // the root box (done at once).
+  __device__ __forceinline__ bool start(const DScene& sc, int scene, f3 o_, f3 d_, float tmin_, float tmax_,
+                                        VisitCount& vc) {
     o = o_;
     d = d_;
     t_min = tmin_;
@@ -191,24 +193,18 @@ struct TravLane {
     h.prim = -1;
     occluded = false;
     sp = 0;
-    if (sc.root_kind == 0) return false;
+    const SceneRoot& R = sc.roots[scene];
+    if (R.kind == 0) return false;
     if (COUNT) ++vc.boxes;
     inv = mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
     n0 = inv.x < 0.0f;
     n1 = inv.y < 0.0f;
     n2 = inv.z < 0.0f;
     float tmin;
-    if (!box_pass(sc.root_lo[0], sc.root_lo[1], sc.root_lo[2], sc.root_hi[0], sc.root_hi[1], sc.root_hi[2], o, inv,
-                  n0, n1, n2, tmin) ||
-        !(tmin < t_max))
+    if (!box_pass(R.lo[0], R.lo[1], R.lo[2], R.hi[0], R.hi[1], R.hi[2], o, inv, n0, n1, n2, tmin) || !(tmin < t_max))
       return false;
-    if (sc.root_kind == 2) {
-      cur = sc.root_offset;
-      cnt = sc.root_count;
-    } else {
-      cur = 0;
-      cnt = 0;
-    }
+    cur = R.offset;
+    cnt = R.kind == 2 ? R.count : 0;
     return true;
   }
 
@@ -292,7 +288,8 @@ struct TravLane {
   }
 };
 
-// Job: unsigned count() const; void load(unsigned i, f3& o, f3& d, float& t_min, float& t_max);
+// Job: unsigned count() const;
+//      void load(unsigned i, f3& o, f3& d, float& t_min, float& t_max, int& scene);
 //      void store(unsigned i, const Hit& h, float t_max, bool occluded).
 template <bool ANY, bool COUNT, class Job>
 __device__ __forceinline__ void persistent_traverse(const DScene& sc, Job& job, unsigned int* fetch, int* err,
@@ -315,8 +312,9 @@ __device__ __forceinline__ void persistent_traverse(const DScene& sc, Job& job, 
         if (item < n) {
           f3 o, d;
           float tmin, tmax;
-          job.load(item, o, d, tmin, tmax);
-          live = L.start(sc, o, d, tmin, tmax, vc);
+          int scene;
+          job.load(item, o, d, tmin, tmax, scene);
+          live = L.start(sc, scene, o, d, tmin, tmax, vc);
           if (!live) job.store(item, L.h, L.t_max, false);
         } else {
           exhausted = true;

@@ -11,7 +11,7 @@ import os
 import numpy as np
 
 from . import build as _build
-from .abi import (NODE_DTYPE, RAY_DTYPE, TR_OK, TrBvhNode32, TrCamera, TrFilter, TrRay, TrRenderParams, TrTuning, TrGuideParams,
+from .abi import (NODE_DTYPE, RAY_DTYPE, TR_OK, TrBvhNode32, TrCamera, TrFilter, TrRay, TrRenderParams, TrTuning, TrGuideParams, TrBatchJob,
                   TrSceneDesc, TrStats)
 
 _lib = None
@@ -92,6 +92,10 @@ def lib() -> C.CDLL:
                                        C.POINTER(TrGuideParams), C.c_void_p, C.c_void_p, C.POINTER(TrStats)]
     L.tr_guide_train_on_records.restype = st
     L.tr_guide_train_on_records.argtypes = [vp, C.c_int32, C.c_uint32, C.c_float, C.c_uint64, C.POINTER(C.c_float)]
+    L.tr_scene_set_upload.restype = st
+    L.tr_scene_set_upload.argtypes = [vp, C.POINTER(TrSceneDesc), C.c_uint32]
+    L.tr_render_batch_dev.restype = st
+    L.tr_render_batch_dev.argtypes = [vp, C.POINTER(TrBatchJob), C.c_uint32, C.POINTER(TrStats)]
     L.tr_render_dev.restype = st
     L.tr_render_dev.argtypes = [vp, C.POINTER(TrCamera), C.POINTER(TrFilter), C.POINTER(TrRenderParams),
                                 vp, vp, C.POINTER(TrStats)]
@@ -201,8 +205,10 @@ class GpuContext:
         return t
 
     def set_tuning(self, refill: int | None = None, trav_blocks_per_sm: int | None = None,
-                   shade_blocks_per_sm: int | None = None) -> None:
+                   shade_blocks_per_sm: int | None = None, graph_iterations: int | None = None) -> None:
         t = self.tuning()
+        if graph_iterations is not None:
+            t.graph_iterations = graph_iterations
         if refill is not None:
             t.trav_refill_lanes = refill
         if trav_blocks_per_sm is not None:
@@ -253,6 +259,25 @@ class GpuContext:
         loss = C.c_float()
         self._check(self.L.tr_guide_train_on_records(self.h, steps, batch, lr, seed, C.byref(loss)))
         return loss.value
+
+    def upload_set(self, scenes) -> None:
+        """Uploads a scene set (list of SceneBuffers) for batched rendering."""
+        descs = (TrSceneDesc * len(scenes))(*[sb.desc() for sb in scenes])
+        self._keep_set = (scenes, descs)
+        self._check(self.L.tr_scene_set_upload(self.h, descs, len(scenes)))
+
+    def render_batch_dev(self, jobs) -> TrStats:
+        """jobs: list of (scene index, camera, filter, params, device film pointer)."""
+        arr = (TrBatchJob * len(jobs))()
+        for k, (scene, cam, filt, par, film) in enumerate(jobs):
+            arr[k].scene = scene
+            arr[k].camera = cam
+            arr[k].filter = filt
+            arr[k].params = par
+            arr[k].d_rgbw = film
+        stats = TrStats()
+        self._check(self.L.tr_render_batch_dev(self.h, arr, len(jobs), C.byref(stats)))
+        return stats
 
     def render_dev(self, cam: TrCamera, filt: TrFilter, params: TrRenderParams, d_out: int, fp64: bool = False):
         stats = TrStats()
