@@ -89,7 +89,7 @@ def traffic_per_unit(stage: str):
         return None
 
 
-WORKLOADS = ("occluded_room", "disney_grid", "cornell")
+WORKLOADS = ("occluded_room", "disney_grid", "cornell", "batch64")
 
 
 def workload(name: str, size: str | None = None):
@@ -309,9 +309,39 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    label, sc, cam, filt, par = workload(args.workload, args.size)
     import oracle
     threads = usable_cores()
+    if args.workload == "batch64":
+        # rows of the batch's first four jobs, one job per step in turn
+        label = "batch_64_scenes_10k_2M_tris_mixed_res_spp_depth6"
+        items = scenes.batch(4)
+        orcs = []
+        for sc, cam, filt, par in items:
+            o = oracle.Oracle(sc, "port", threads=threads)
+            o.set_camera(cam, filt)
+            orcs.append((o, par))
+        nrows = 2 * threads
+        for _ in range(args.warmup):
+            orcs[0][0].render_rows(orcs[0][1], np.arange(threads, dtype=np.int32) % orcs[0][1].height)
+        t0 = time.perf_counter()
+        total = 0
+        for k in range(args.steps):
+            o, par = orcs[k % len(orcs)]
+            rows = np.linspace(0, par.height - 1, nrows).round().astype(np.int32)
+            total += o.render_rows(par, rows)[1]
+        dt = time.perf_counter() - t0
+        value = total / dt / 1e6
+        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(args.steps, 1),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded procedural scenes)", "config": {"workload": label},
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": f"{nrows} rows per step of one of the batch's first four jobs in turn, "
+                                           "CPU restatement of the reference (oracle/tracer_oracle.cpp)"},
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return 0
+    label, sc, cam, filt, par = workload(args.workload, args.size)
     orc = oracle.Oracle(sc, "port", threads=threads)
     orc.set_camera(cam, filt)
     nrows = 2 * threads
@@ -338,6 +368,119 @@ def run_reference(args):
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def run_batch(args):
+    """The batched-rendering workload: 64 scenes (10k-2M triangles each,
+    log-uniform) at mixed resolutions and spp rendered as one batch per step
+    after the launch autotuner has picked the tuning on a 1-spp probe."""
+    import torch
+    from tracer_gb300.abi import TR_RENDER_TIME_STAGES as TS
+    from tracer_gb300.native import GpuContext
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend="nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    items = scenes.batch(64)
+    gen_s = time.perf_counter() - t0
+    ctx = GpuContext(local)
+    t0 = time.perf_counter()
+    ctx.upload_set([it[0] for it in items])
+    upload_s = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(ctx.stream, device=local)
+    films = [torch.zeros((p.height, p.width, 4), device=f"cuda:{local}") for _, _, _, p in items]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    torch.cuda.synchronize()
+    jobs = [(k, it[1], it[2], it[3], films[k].data_ptr()) for k, it in enumerate(items)]
+    t0 = time.perf_counter()
+    tuning, probe_ms = ctx.autotune(jobs, probe_spp=1)
+    tune_s = time.perf_counter() - t0
+
+    def barrier():
+        ctx.synchronize()
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    clocks = ClockSampler(local).__enter__()
+    for _ in range(args.warmup):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        ctx.render_batch_dev(jobs)
+    barrier()
+    c0 = clocks.mark()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    stats = []
+    for k in range(args.steps):
+        if k:
+            with torch.cuda.stream(stream):
+                flush.zero_()
+        stats.append(ctx.render_batch_dev(jobs))
+    e1.record(stream)
+    barrier()
+    c1 = clocks.mark()
+    clocks.__exit__()
+    ms = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    samples = sum(s.samples for s in stats)
+    value = world * samples / (ms / 1e3) / 1e6
+    # end to end: the batch call plus every film copied back to the host
+    barrier()
+    t0 = time.perf_counter()
+    e2e_samples = 0
+    for _ in range(args.steps):
+        st = ctx.render_batch_dev(jobs)
+        host = [f.cpu() for f in films]
+        e2e_samples += st.samples
+    barrier()
+    e2e = world * e2e_samples / (time.perf_counter() - t0) / 1e6
+    d2h = sum(int(f.numel()) * 4 for f in films)
+    del host
+    staged_jobs = [(k, c, f, _flagged(p, TS), film) for k, c, f, p, film in jobs]
+    ctx.render_batch_dev(staged_jobs)
+    staged = ctx.render_batch_dev(staged_jobs)
+    if rank != 0:
+        ctx.close()
+        return 0
+    stage_ms = dict(zip(STAGE_NAMES, staged.stage_ms))
+    dom = max((k for k in STAGE_NAMES if k != "reset"), key=lambda k: stage_ms[k])
+    tris = int(sum(len(it[0].indices) for it in items))
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (64 seeded procedural scenes, no dataset)",
+        "config": {"workload": "batch_64_scenes_10k_2M_tris_mixed_res_spp_depth6", "scenes": 64, "triangles": tris,
+                   "samples_per_step": int(stats[0].samples), "parallelism": f"replicas x{world}",
+                   "l2": "path state of all jobs exceeds L2; a 256 MiB buffer is written between timed steps"},
+        "value_is": "camera samples per second over the whole batch (one tr_render_batch_dev call per step)",
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 64 * 200, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(sum(1 + 7 * s.iterations for s in stats)),
+        "autotune": {"trav_refill_lanes": tuning.trav_refill_lanes, "trav_blocks_per_sm": tuning.trav_blocks_per_sm,
+                     "shade_blocks_per_sm": tuning.shade_blocks_per_sm, "graph_iterations": tuning.graph_iterations,
+                     "probe_ms": round(probe_ms, 2), "tune_s": round(tune_s, 1)},
+        "setup_s": {"generate": round(gen_s, 1), "upload_and_bvh": round(upload_s, 1)},
+        "stage_ms": {k: round(v, 3) for k, v in stage_ms.items()}, "dominant_kernel": KERNEL_NAMES[dom],
+        "clocks": clocks.summary(c0, c1),
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
+def _flagged(par, flags):
+    p = TrRenderParams()
+    ctypes.memmove(ctypes.byref(p), ctypes.byref(par), ctypes.sizeof(p))
+    p.flags = flags
+    return p
 
 
 def run_ours(args):
@@ -516,6 +659,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch64":
+        return run_batch(args)
     return run_ours(args)
 
 

@@ -296,6 +296,16 @@ typedef struct tr_batch_job {
   float* d_rgbw; /* device film sums, 4 * width * height floats, 16-byte aligned */
 } tr_batch_job;
 tr_status tr_render_batch_dev(tr_ctx* ctx, const tr_batch_job* jobs, uint32_t n, tr_stats* stats);
+/* Launch autotuner. No reference counterpart. Times the batch (each job
+ * capped at probe_spp samples per pixel; the jobs' films are overwritten)
+ * under candidate tr_tuning settings -- resident traversal blocks per SM,
+ * lane-refill threshold, shading grid, CUDA-graph chunk length -- by
+ * coordinate descent (median of three timed renders each, a change kept
+ * only if 2% faster), sets the best on the context and returns it with its
+ * time. The BVH node width stays 2: wider nodes would change the traversal
+ * order, and with it which of two equal-distance primitives is reported. */
+tr_status tr_autotune(tr_ctx* ctx, const tr_batch_job* jobs, uint32_t n, int32_t probe_spp,
+                      tr_tuning* best, double* best_ms);
 
 /* Asks a running tr_render on this context to stop after its current
  * wavefront iteration; that call then returns TR_ERR_CANCELLED. Thread-safe. */

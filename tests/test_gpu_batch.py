@@ -68,3 +68,27 @@ def test_scene_set_traversal_uses_scene_zero(gpu):
     gpu.upload_set([sc0, sc1])
     p1, t1 = gpu.trace_closest(rays)
     assert np.array_equal(p0, p1) and np.array_equal(t0.view(np.uint32), t1.view(np.uint32))
+
+
+def test_autotune_picks_a_valid_tuning_and_keeps_results(gpu):
+    import torch
+    items = _set()
+    gpu.upload_set([it[0] for it in items])
+    films = [torch.zeros((p.height, p.width, 4), device="cuda:0") for _, _, _, p in items]
+    torch.cuda.synchronize()
+    jobs = [(k, it[1], it[2], it[3], films[k].data_ptr()) for k, it in enumerate(items)]
+    gpu.render_batch_dev(jobs)
+    before = [f.cpu().numpy() for f in films]
+    old = gpu.tuning()
+    try:
+        best, ms = gpu.autotune(jobs, probe_spp=1)
+        assert ms > 0
+        t = gpu.tuning()
+        assert (t.trav_refill_lanes, t.trav_blocks_per_sm, t.shade_blocks_per_sm, t.graph_iterations) == \
+               (best.trav_refill_lanes, best.trav_blocks_per_sm, best.shade_blocks_per_sm, best.graph_iterations)
+        assert 1 <= t.trav_refill_lanes <= 32 and t.shade_blocks_per_sm >= 1
+        gpu.render_batch_dev(jobs)
+        for b, f in zip(before, films):
+            assert np.array_equal(b.view(np.uint32), f.cpu().numpy().view(np.uint32))
+    finally:
+        gpu.set_tuning(old.trav_refill_lanes, old.trav_blocks_per_sm, old.shade_blocks_per_sm, old.graph_iterations)

@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1378,6 +1379,65 @@ extern "C" tr_status tr_render_batch_dev(tr_ctx* ctx, const tr_batch_job* jobs, 
     spec[k].fp64 = false;
   }
   return trg::render_jobs(ctx, spec.data(), (int)n, jobs[0].params.flags, stats);
+}
+
+extern "C" tr_status tr_autotune(tr_ctx* ctx, const tr_batch_job* jobs, uint32_t n, int32_t probe_spp,
+                                  tr_tuning* best, double* best_ms) {
+  if (!ctx || !jobs || n == 0 || !best || probe_spp <= 0) return TR_ERR_ARG;
+  // the probe: the caller's jobs with at most probe_spp samples per pixel
+  std::vector<tr_batch_job> probe(jobs, jobs + n);
+  for (auto& j : probe) {
+    j.params.spp = std::min(j.params.spp, probe_spp);
+    j.params.flags = 0;
+  }
+  auto time_once = [&](const tr_tuning& t, double& ms) -> tr_status {
+    tr_status s = tr_ctx_set_tuning(ctx, &t);
+    if (s != TR_OK) return s;
+    double v[3];
+    for (int r = 0; r < 4; ++r) {  // one warm-up, median of three
+      const auto t0 = std::chrono::steady_clock::now();
+      s = tr_render_batch_dev(ctx, probe.data(), n, nullptr);
+      if (s != TR_OK) return s;
+      if (r) v[r - 1] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    std::sort(v, v + 3);
+    ms = v[1];
+    return TR_OK;
+  };
+  // coordinate descent over the discrete settings
+  static const int kBlocks[] = {0, 4, 6, 8}, kRefill[] = {12, 20, 28}, kShade[] = {8, 16, 32},
+                   kGraph[] = {0, 4, 8, 16};
+  tr_tuning cur = ctx->tune;
+  double cur_ms = 0.0;
+  tr_status s = time_once(cur, cur_ms);
+  if (s != TR_OK) return s;
+  for (int pass = 0; pass < 2; ++pass) {
+    bool improved = false;
+    for (int dim = 0; dim < 4; ++dim) {
+      const int* vals = dim == 0 ? kBlocks : dim == 1 ? kRefill : dim == 2 ? kShade : kGraph;
+      const int nv = dim == 0 ? 4 : dim == 3 ? 4 : 3;
+      for (int k = 0; k < nv; ++k) {
+        tr_tuning t = cur;
+        int* field = dim == 0 ? &t.trav_blocks_per_sm
+                              : dim == 1 ? &t.trav_refill_lanes : dim == 2 ? &t.shade_blocks_per_sm : &t.graph_iterations;
+        if (*field == vals[k]) continue;
+        *field = vals[k];
+        double ms = 0.0;
+        s = time_once(t, ms);
+        if (s != TR_OK) return s;
+        if (ms < 0.98 * cur_ms) {  // keep only clear wins
+          cur = t;
+          cur_ms = ms;
+          improved = true;
+        }
+      }
+    }
+    if (!improved) break;
+  }
+  s = tr_ctx_set_tuning(ctx, &cur);
+  *best = cur;
+  if (best_ms) *best_ms = cur_ms;
+  return s;
 }
 
 extern "C" tr_status tr_render_guided_dev(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter,

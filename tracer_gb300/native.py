@@ -96,6 +96,9 @@ def lib() -> C.CDLL:
     L.tr_scene_set_upload.argtypes = [vp, C.POINTER(TrSceneDesc), C.c_uint32]
     L.tr_render_batch_dev.restype = st
     L.tr_render_batch_dev.argtypes = [vp, C.POINTER(TrBatchJob), C.c_uint32, C.POINTER(TrStats)]
+    L.tr_autotune.restype = st
+    L.tr_autotune.argtypes = [vp, C.POINTER(TrBatchJob), C.c_uint32, C.c_int32, C.POINTER(TrTuning),
+                              C.POINTER(C.c_double)]
     L.tr_render_dev.restype = st
     L.tr_render_dev.argtypes = [vp, C.POINTER(TrCamera), C.POINTER(TrFilter), C.POINTER(TrRenderParams),
                                 vp, vp, C.POINTER(TrStats)]
@@ -268,6 +271,13 @@ class GpuContext:
 
     def render_batch_dev(self, jobs) -> TrStats:
         """jobs: list of (scene index, camera, filter, params, device film pointer)."""
+        arr = self._jobs(jobs)
+        stats = TrStats()
+        self._check(self.L.tr_render_batch_dev(self.h, arr, len(jobs), C.byref(stats)))
+        return stats
+
+    @staticmethod
+    def _jobs(jobs):
         arr = (TrBatchJob * len(jobs))()
         for k, (scene, cam, filt, par, film) in enumerate(jobs):
             arr[k].scene = scene
@@ -275,9 +285,13 @@ class GpuContext:
             arr[k].filter = filt
             arr[k].params = par
             arr[k].d_rgbw = film
-        stats = TrStats()
-        self._check(self.L.tr_render_batch_dev(self.h, arr, len(jobs), C.byref(stats)))
-        return stats
+        return arr
+
+    def autotune(self, jobs, probe_spp: int = 2):
+        """Tunes the launch settings on (a short version of) a batch; returns (tuning, ms)."""
+        best, ms = TrTuning(), C.c_double()
+        self._check(self.L.tr_autotune(self.h, self._jobs(jobs), len(jobs), probe_spp, C.byref(best), C.byref(ms)))
+        return best, ms.value
 
     def render_dev(self, cam: TrCamera, filt: TrFilter, params: TrRenderParams, d_out: int, fp64: bool = False):
         stats = TrStats()

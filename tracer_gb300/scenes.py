@@ -96,29 +96,40 @@ def make_rays(o: np.ndarray, d: np.ndarray, t_min, t_max) -> np.ndarray:
 
 
 class _Builder:
+    """Accumulates primitives as array chunks; finish() concatenates them."""
+
     def __init__(self):
         self.pos, self.nrm, self.uv, self.idx = [], [], [], []
+        self.nv = 0  # vertices so far
+        self.nt = 0  # triangles so far
         self.sph_r, self.sph_m, self.sph_inv = [], [], []
         self.mats: list[Material] = []
         self.prim_shape, self.prim_mat, self.prim_em = [], [], []
         self.lights = []
+        self.np = 0  # primitives so far
 
     def material(self, m: Material) -> int:
         self.mats.append(m)
         return len(self.mats) - 1
 
+    def _prims(self, shapes, mat, emission):
+        k = len(shapes)
+        self.prim_shape.append(np.asarray(shapes, np.int32))
+        self.prim_mat.append(np.full(k, mat, np.int32))
+        self.prim_em.append(np.tile(np.asarray(emission, np.float32), (k, 1)))
+        first = self.np
+        self.np += k
+        return first
+
     def triangle(self, a, b, c, n, mat, emission=(0, 0, 0), uvs=((0, 0), (1, 0), (1, 1)), light=None):
         nn = fixed_normal(n)
-        base = len(self.pos)
-        for p, t in zip((a, b, c), uvs):
-            self.pos.append(np.asarray(p, dtype=np.float32) + np.float32(0))  # no -0.0 in positions
-            self.nrm.append(nn)
-            self.uv.append(np.asarray(t, dtype=np.float32))
-        self.idx.append((base, base + 1, base + 2))
-        self.prim_shape.append(len(self.idx) - 1)
-        self.prim_mat.append(mat)
-        self.prim_em.append(emission)
-        pid = len(self.prim_shape) - 1
+        self.pos.append(np.asarray([a, b, c], dtype=np.float32).reshape(3, 3) + np.float32(0))  # no -0.0
+        self.nrm.append(np.tile(nn, (3, 1)))
+        self.uv.append(np.asarray(uvs, dtype=np.float32))
+        self.idx.append(np.array([[self.nv, self.nv + 1, self.nv + 2]], np.int32))
+        self.nv += 3
+        pid = self._prims([self.nt], mat, emission)
+        self.nt += 1
         if any(e != 0 for e in emission) and light is not False:
             self.lights.append(pid)
         return pid
@@ -150,45 +161,46 @@ class _Builder:
 
     def sphere(self, center, radius, mat):
         cx, cy, cz = (float(np.float32(v)) for v in center)
-        # translate(delta) builds m and its explicit inverse (src/utility/transform.cpp:155-165)
+        # translate(delta) builds m and its explicit inverse (src/utility/transform.cpp:163-173)
         m = np.array([1, 0, 0, cx, 0, 1, 0, cy, 0, 0, 1, cz, 0, 0, 0, 1], dtype=np.float32)
         inv = np.array([1, 0, 0, -cx, 0, 1, 0, -cy, 0, 0, 1, -cz, 0, 0, 0, 1], dtype=np.float32)
         self.sph_r.append(radius)
         self.sph_m.append(m)
         self.sph_inv.append(inv)
-        self.prim_shape.append(~(len(self.sph_r) - 1))
-        self.prim_mat.append(mat)
-        self.prim_em.append((0, 0, 0))
-        return len(self.prim_shape) - 1
+        return self._prims([~(len(self.sph_r) - 1)], mat, (0, 0, 0))
 
-    def mesh(self, tris: np.ndarray, normals: np.ndarray, mat: int):
+    def mesh(self, tris: np.ndarray, normals: np.ndarray, mat: int, settle: bool = True):
         """Bulk triangles: tris (T, 3, 3) positions, normals (T, 3, 3) per
-        vertex (settled to fixed points of the reference normalize)."""
+        vertex (settled to fixed points of the reference normalize unless
+        settle is False; the upload normalises them either way)."""
         T = len(tris)
         if T == 0:
             return
-        base = len(self.pos)
-        self.pos.extend(np.asarray(tris, np.float32).reshape(-1, 3) + np.float32(0))
-        self.nrm.extend(settle_normals(np.asarray(normals).reshape(-1, 3)))
-        uv = np.tile(np.array([[0, 0], [1, 0], [1, 1]], np.float32), (T, 1))
-        self.uv.extend(uv)
-        first = len(self.idx)
-        self.idx.extend((base + 3 * np.arange(T)[:, None] + np.arange(3)[None, :]).tolist())
-        self.prim_shape.extend(range(first, first + T))
-        self.prim_mat.extend([mat] * T)
-        self.prim_em.extend([(0, 0, 0)] * T)
+        self.pos.append(np.asarray(tris, np.float32).reshape(-1, 3) + np.float32(0))
+        n = np.asarray(normals, np.float64).reshape(-1, 3)
+        self.nrm.append(settle_normals(n) if settle else (n / np.linalg.norm(n, axis=1, keepdims=True)).astype(np.float32))
+        self.uv.append(np.tile(np.array([[0, 0], [1, 0], [1, 1]], np.float32), (T, 1)))
+        self.idx.append((self.nv + 3 * np.arange(T, dtype=np.int64)[:, None] + np.arange(3)[None, :]).astype(np.int32))
+        self.nv += 3 * T
+        self._prims(np.arange(self.nt, self.nt + T), mat, (0, 0, 0))
+        self.nt += T
 
     def finish(self, max_leaf_prims: int) -> SceneBuffers:
+        def cat(chunks, cols, dt):
+            return np.concatenate(chunks).astype(dt, copy=False) if chunks else np.zeros((0, cols), dt)
+
         def arr(x, shape, dt):
             return np.asarray(x, dtype=dt).reshape(shape) if len(x) else np.zeros(tuple(0 if d < 0 else d for d in shape), dtype=dt)
         return SceneBuffers(
-            positions=arr(self.pos, (-1, 3), np.float32), normals=arr(self.nrm, (-1, 3), np.float32),
-            uvs=arr(self.uv, (-1, 2), np.float32), indices=arr(self.idx, (-1, 3), np.int32),
+            positions=cat(self.pos, 3, np.float32), normals=cat(self.nrm, 3, np.float32),
+            uvs=cat(self.uv, 2, np.float32), indices=cat(self.idx, 3, np.int32),
             sphere_radius=arr(self.sph_r, (-1,), np.float32), sphere_to_world=arr(self.sph_m, (-1, 16), np.float32),
             sphere_to_local=arr(self.sph_inv, (-1, 16), np.float32), materials=self.mats,
-            prim_shape=arr(self.prim_shape, (-1,), np.int32), prim_material=arr(self.prim_mat, (-1,), np.int32),
-            prim_emission=arr(self.prim_em, (-1, 3), np.float32), light_prims=arr(self.lights, (-1,), np.int32),
-            max_leaf_prims=max_leaf_prims)
+            prim_shape=np.concatenate(self.prim_shape).astype(np.int32) if self.prim_shape else np.zeros(0, np.int32),
+            prim_material=np.concatenate(self.prim_mat).astype(np.int32) if self.prim_mat else np.zeros(0, np.int32),
+            prim_emission=(np.concatenate(self.prim_em).astype(np.float32) if self.prim_em
+                           else np.zeros((0, 3), np.float32)),
+            light_prims=arr(self.lights, (-1,), np.int32), max_leaf_prims=max_leaf_prims)
 
 
 def lambert(albedo) -> Material:
@@ -513,3 +525,90 @@ def occluded_room(width=1024, height=768, spp=16, max_depth=10, min_depth=3, n_t
     scene = b.finish(max_leaf_prims=3)
     cam = make_camera(width / height, (-3.6, 1.8, 2.4), (2.0, 1.6, -0.6), (0, 1, 0), math.radians(60.0), 0.0, 1.0)
     return scene, cam, make_filter(0.5, 0.6), make_params(width, height, spp, min_depth, max_depth)
+
+
+def _uv_sphere(center, radius, segs, rings):
+    """UV sphere: 2 * segs * rings triangles with radial normals."""
+    th = np.linspace(0.0, math.pi, rings + 1)
+    ph = np.linspace(0.0, 2 * math.pi, segs + 1)
+    N = np.stack([np.sin(th)[:, None] * np.cos(ph)[None], np.cos(th)[:, None] * np.ones_like(ph)[None],
+                  np.sin(th)[:, None] * np.sin(ph)[None]], -1)
+    P = np.asarray(center) + radius * N
+    a, b, c, d = P[:-1, :-1], P[:-1, 1:], P[1:, 1:], P[1:, :-1]
+    na, nb, nc, nd = N[:-1, :-1], N[:-1, 1:], N[1:, 1:], N[1:, :-1]
+    # (a, b, c): b steps along phi, c along theta and phi; cross(phi, theta) points outward
+    tris = np.concatenate([np.stack([a, b, c], -2), np.stack([a, c, d], -2)], 0).reshape(-1, 3, 3)
+    nrms = np.concatenate([np.stack([na, nb, nc], -2), np.stack([na, nc, nd], -2)], 0).reshape(-1, 3, 3)
+    keep = np.linalg.norm(np.cross(tris[:, 1] - tris[:, 0], tris[:, 2] - tris[:, 0]), axis=1) > 0
+    return tris[keep], nrms[keep]
+
+
+def _torus(center, R, r, nu, nv):
+    """Torus around the y axis: 2 * nu * nv triangles, normals from the tube centre."""
+    u = np.linspace(0.0, 2 * math.pi, nu + 1)
+    v = np.linspace(0.0, 2 * math.pi, nv + 1)
+    cu, su, cv, sv = np.cos(u)[:, None], np.sin(u)[:, None], np.cos(v)[None], np.sin(v)[None]
+    N = np.stack([cv * cu, sv * np.ones_like(cu), cv * su], -1)
+    C = np.stack([R * cu * np.ones_like(cv), np.zeros_like(cu * cv), R * su * np.ones_like(cv)], -1)
+    P = np.asarray(center) + C + r * N
+    a, b, c, d = P[:-1, :-1], P[:-1, 1:], P[1:, 1:], P[1:, :-1]
+    na, nb, nc, nd = N[:-1, :-1], N[:-1, 1:], N[1:, 1:], N[1:, :-1]
+    tris = np.concatenate([np.stack([a, b, c], -2), np.stack([a, c, d], -2)], 0).reshape(-1, 3, 3)
+    nrms = np.concatenate([np.stack([na, nb, nc], -2), np.stack([na, nc, nd], -2)], 0).reshape(-1, 3, 3)
+    return tris, nrms
+
+
+def batch_scene(seed: int, tri_range=(10_000, 2_000_000)):
+    """One scene of the batched-rendering workload: a ground quad and one to
+    five tessellated spheres, boxes or tori sharing a triangle count drawn
+    log-uniformly from tri_range, each Lambertian or Disney12 at random,
+    one to four 1x1 area-light quads; film 128^2 .. 1024^2, 4, 16 or 64 spp,
+    max depth 6. Returns (scene, camera, filter, params)."""
+    rng = np.random.default_rng(1000 + seed)
+    total = int(math.exp(rng.uniform(math.log(tri_range[0]), math.log(tri_range[1]))))
+    res = int(rng.choice([128, 256, 512, 1024]))
+    spp = int(rng.choice([4, 16, 64]))
+    b = _Builder()
+    ground = b.material(lambert((0.6, 0.6, 0.6)))
+    b.quad((-6, 0, -6), (6, 0, -6), (6, 0, 6), (-6, 0, 6), (0, 1, 0), ground)
+    nobj = int(rng.integers(1, 6))
+    share = np.maximum(rng.dirichlet(np.ones(nobj)) * total, 100).astype(int)
+    for k in range(nobj):
+        if rng.random() < 0.5:
+            mat = b.material(lambert(tuple(float(v) for v in 0.2 + 0.7 * rng.random(3))))
+        else:
+            q = rng.random(6)
+            mat = b.material(Material(kind=TR_MAT_DISNEY12, base_color=tuple(float(v) for v in 0.2 + 0.7 * rng.random(3)),
+                                      metallic=float(q[0]), roughness=float(0.05 + 0.95 * q[1]), specular=0.5,
+                                      specular_tint=float(q[2]), sheen=float(q[3]), sheen_tint=0.5,
+                                      clearcoat=float(q[4]), clearcoat_gloss=float(q[5]), anisotropic=0.0,
+                                      subsurface=0.0))
+        c = (rng.uniform(-3.5, 3.5), 0.0, rng.uniform(-3.5, 3.5))
+        kind = int(rng.integers(0, 3))
+        t = int(share[k])
+        if kind == 0:
+            n = max(4, int(math.sqrt(t / 4)))
+            rad = rng.uniform(0.4, 1.2)
+            tris, nrm = _uv_sphere((c[0], rad, c[2]), rad, 2 * n, n)
+        elif kind == 1:
+            kk = max(1, int(math.sqrt(t / 12)))
+            size = rng.uniform(0.5, 2.0, 3)
+            tris, nrm = _grid_box((c[0], size[1] / 2, c[2]), size, rng.uniform(0, math.pi), kk)
+        else:
+            n = max(4, int(math.sqrt(t / 2)))
+            Rr = rng.uniform(0.6, 1.2)
+            tris, nrm = _torus((c[0], 0.45 * Rr, c[2]), Rr, 0.4 * Rr, n, n)
+        b.mesh(tris, nrm, mat, settle=False)
+    for _ in range(int(rng.integers(1, 5))):
+        x, z = rng.uniform(-4, 4), rng.uniform(-4, 4)
+        y = rng.uniform(4.0, 6.0)
+        b.quad((x - 0.5, y, z - 0.5), (x + 0.5, y, z - 0.5), (x + 0.5, y, z + 0.5), (x - 0.5, y, z + 0.5), (0, -1, 0),
+               ground, emission=tuple(float(v) for v in 10 + 20 * rng.random(3)))
+    scene = b.finish(max_leaf_prims=3)
+    cam = make_camera(1.0, (0.0, 5.0, 11.0), (0.0, 0.5, 0.0), (0, 1, 0), math.radians(50.0), 0.0, 1.0)
+    return scene, cam, make_filter(0.5, 0.6), make_params(res, res, spp, 3, 6, seed_base=seed * 7919)
+
+
+def batch(n: int = 64, seed: int = 0, tri_range=(10_000, 2_000_000)):
+    """The batched-rendering workload: n scenes of batch_scene."""
+    return [batch_scene(seed * 1000 + k, tri_range) for k in range(n)]
