@@ -89,7 +89,7 @@ def traffic_per_unit(stage: str):
         return None
 
 
-WORKLOADS = ("occluded_room", "disney_grid", "cornell", "batch64")
+WORKLOADS = ("occluded_room", "disney_grid", "cornell", "batch64", "traversal")
 
 
 def workload(name: str, size: str | None = None):
@@ -245,6 +245,10 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self, lo: int = 0, hi: int | None = None):
+        if hi is not None and hi - lo < 2:
+            # a timed region shorter than the sampling period: the samples
+            # next to it (warm-up and the work right after)
+            lo, hi = max(0, lo - 3), hi + 3
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines[lo:hi]:
@@ -339,6 +343,33 @@ def run_reference(args):
                                  "sample": f"{nrows} rows per step of one of the batch's first four jobs in turn, "
                                            "CPU restatement of the reference (oracle/tracer_oracle.cpp)"},
                 "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return 0
+    if args.workload == "traversal":
+        label = "traversal_1M_tris_leaf4_4M_closest_4M_shadow_rays"
+        sc = scenes.traversal(1 << 20)
+        orc = oracle.Oracle(sc, "port", threads=threads)
+        m = 1 << 17
+        closest = scenes.traversal_rays(1 << 22, shadow=False)
+        shadow = scenes.traversal_rays(1 << 22, shadow=True)
+        for _ in range(args.warmup):
+            orc.trace_closest(closest[:m // 4])
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            sl = slice((k * m) % (1 << 22), (k * m) % (1 << 22) + m)
+            orc.trace_closest(closest[sl])
+            orc.trace_any(shadow[sl])
+        dt = time.perf_counter() - t0
+        value = 2 * m * args.steps / dt / 1e6
+        line = {"impl": "reference", "metric": "Mrays/s (BVH traversal: closest hit + shadow any hit)",
+                "value": value, "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * dt / max(args.steps, 1), "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded random triangles and rays)",
+                "config": {"workload": label},
+                "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                                 "sample": f"{m} closest-hit and {m} shadow rays per step, CPU restatement of "
+                                           "BVHAccel::intersect_p / intersect (oracle/tracer_oracle.cpp)"},
+                "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return 0
     label, sc, cam, filt, par = workload(args.workload, args.size)
@@ -471,6 +502,138 @@ def run_batch(args):
         "stage_ms": {k: round(v, 3) for k, v in stage_ms.items()}, "dominant_kernel": KERNEL_NAMES[dom],
         "clocks": clocks.summary(c0, c1),
     }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
+def run_traversal(args):
+    """The traversal kernel test: 1M random triangles (leaf <= 4), 4M
+    closest-hit rays and 4M shadow rays per step through tr_trace_*_dev;
+    Mrays/s over both."""
+    import torch
+    from tracer_gb300.abi import RAY_DTYPE
+    from tracer_gb300.native import GpuContext
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend="nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    n_tris, n_rays = 1 << 20, 1 << 22
+    sc = scenes.traversal(n_tris)
+    closest = scenes.traversal_rays(n_rays, shadow=False)
+    shadow = scenes.traversal_rays(n_rays, shadow=True)
+    ctx = GpuContext(local)
+    t0 = time.perf_counter()
+    ctx.upload(sc)
+    upload_s = time.perf_counter() - t0
+    dev = f"cuda:{local}"
+    dc = torch.from_numpy(closest.view(np.uint8)).to(dev)
+    ds = torch.from_numpy(shadow.view(np.uint8)).to(dev)
+    prim = torch.empty(n_rays, dtype=torch.int32, device=dev)
+    tout = torch.empty(n_rays, dtype=torch.float32, device=dev)
+    hit = torch.empty(n_rays, dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=local)
+    torch.cuda.synchronize()
+
+    def step():
+        ctx.trace_closest_dev(dc.data_ptr(), n_rays, prim.data_ptr(), tout.data_ptr())
+        ctx.trace_any_dev(ds.data_ptr(), n_rays, hit.data_ptr())
+
+    def barrier():
+        ctx.synchronize()
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    clocks = ClockSampler(local).__enter__()
+    for _ in range(args.warmup):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        step()
+    barrier()
+    c0 = clocks.mark()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ec = [torch.cuda.Event(enable_timing=True) for _ in range(3 * args.steps)]
+    e0.record(stream)
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        ec[3 * k].record(stream)
+        ctx.trace_closest_dev(dc.data_ptr(), n_rays, prim.data_ptr(), tout.data_ptr())
+        ec[3 * k + 1].record(stream)
+        ctx.trace_any_dev(ds.data_ptr(), n_rays, hit.data_ptr())
+        ec[3 * k + 2].record(stream)
+    e1.record(stream)
+    barrier()
+    c1 = clocks.mark()
+    clocks.__exit__()
+    ms = e0.elapsed_time(e1)
+    closest_ms = sum(ec[3 * k].elapsed_time(ec[3 * k + 1]) for k in range(args.steps)) / args.steps
+    any_ms = sum(ec[3 * k + 1].elapsed_time(ec[3 * k + 2]) for k in range(args.steps)) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * 2 * n_rays * args.steps / (ms / 1e3) / 1e6
+    # end to end: the host-buffer calls, rays in and results out every step
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.trace_closest(closest)
+        ctx.trace_any(shadow)
+    barrier()
+    e2e = world * 2 * n_rays * args.steps / (time.perf_counter() - t0) / 1e6
+    cb, cp = ctx.trace_count_dev(dc.data_ptr(), n_rays, False)
+    ab, ap = ctx.trace_count_dev(ds.data_ptr(), n_rays, True)
+    if rank != 0:
+        ctx.close()
+        return 0
+    peak, peak_kind = measured_peak_hbm()
+    bytes_c = 32 * cb + 48 * cp + 40 * n_rays
+    bytes_a = 32 * ab + 48 * ap + 33 * n_rays
+    dom_closest = closest_ms >= any_ms
+    ach = (bytes_c / (closest_ms / 1e3) if dom_closest else bytes_a / (any_ms / 1e3)) / 1e9
+    cpu_rate, cpu_threads, cpu_desc = None, None, None
+    if not args.no_cpu_baseline and world == 1:
+        import oracle
+        cpu_threads = usable_cores()
+        orc = oracle.Oracle(sc, "port", threads=cpu_threads)
+        m = 1 << 18
+        t0 = time.perf_counter()
+        orc.trace_closest(closest[:m])
+        orc.trace_any(shadow[:m])
+        dt = time.perf_counter() - t0
+        cpu_rate = 2 * m / dt / 1e6
+        cpu_desc = f"the first {m} closest-hit and {m} shadow rays ({dt:.2f} s wall), CPU restatement of BVHAccel"
+    line = {
+        "metric": "Mrays/s (BVH traversal: closest hit + shadow any hit)", "value": value, "unit": "Mrays/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded random triangles and rays, no dataset)",
+        "config": {"workload": "traversal_1M_tris_leaf4_4M_closest_4M_shadow_rays", "triangles": n_tris,
+                   "rays_per_step": 2 * n_rays, "parallelism": f"replicas x{world}",
+                   "l2": "a 256 MiB buffer is written before each timed step (nodes + slots ~ 90 MB, rays 256 MB)"},
+        "e2e": {"value": e2e, "unit": "Mrays/s", "h2d_bytes_per_step": 2 * 32 * n_rays,
+                "d2h_bytes_per_step": n_rays * 8 + n_rays},
+        "gpu_launches": 2 * args.steps,
+        "per_kernel": {"closest_mrays_per_s": n_rays / closest_ms / 1e3, "any_mrays_per_s": n_rays / any_ms / 1e3,
+                       "boxes_per_closest_ray": cb / n_rays, "prims_per_closest_ray": cp / n_rays,
+                       "boxes_per_shadow_ray": ab / n_rays, "prims_per_shadow_ray": ap / n_rays},
+        "roofline": {"bound": "hbm", "kernel": "k_trace_batch<false>" if dom_closest else "k_trace_batch<true>",
+                     "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "traffic": None,
+                     "peak_source": f"{peak_kind} HBM copy bandwidth (hbm_gbs)",
+                     "bytes_per_unit": (bytes_c if dom_closest else bytes_a) / n_rays},
+        "setup_s": {"upload_and_bvh": round(upload_s, 2)},
+        "clocks": clocks.summary(c0, c1),
+    }
+    if cpu_rate is not None:
+        line["cpu_baseline"] = {"value": cpu_rate, "unit": "Mrays/s", "cores": cpu_threads, "kind": "port",
+                                "sample": cpu_desc}
     print(json.dumps(line), flush=True)
     ctx.close()
     return 0
@@ -661,6 +824,8 @@ def main():
         return run_reference(args)
     if args.workload == "batch64":
         return run_batch(args)
+    if args.workload == "traversal":
+        return run_traversal(args)
     return run_ours(args)
 
 

@@ -242,6 +242,12 @@ tr_status tr_trace_any(tr_ctx* ctx, const tr_ray* rays, size_t n, uint8_t* hit);
 tr_status tr_trace_closest_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, int32_t* d_prim,
                                float* d_t);
 tr_status tr_trace_any_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, uint8_t* d_hit);
+/* Boxes and primitives the closest-hit (any = 0) or any-hit (any != 0)
+ * traversal of the rays tests, in total: the per-ray units of the
+ * traversal's algorithmic bytes (32 B per LinearBVHNode box, 48 B per
+ * triangle test). Synchronous. No reference counterpart. */
+tr_status tr_trace_count_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, int32_t any, uint64_t* boxes,
+                             uint64_t* prims);
 
 /* Renders the film: PathTraceRenderer::eval_pixel_li per camera sample
  * (src/renderer/path_trace_renderer.cpp:27-210) inside the pixel loop of

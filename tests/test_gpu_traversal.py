@@ -117,3 +117,29 @@ def test_empty_and_single(gpu):
     p, t = gpu.trace_closest(rays)
     assert (p == -1).all()
     assert not gpu.trace_any(rays).any()
+
+
+def test_trace_visit_counts_equal_the_oracle(gpu):
+    """Boxes and primitives tested per traversal (the roofline's units)
+    against the reference traversal's on the same rays: equal for closest
+    hits. For any hits the primitive tests are equal; the boxes can only be
+    more, because both child boxes are tested when their parent is visited
+    while the reference tests a box when it pops it, and an early exit
+    leaves pushed entries the reference never pops."""
+    import torch
+    import oracle
+    sc = scenes.traversal(1 << 14, seed=3)
+    rays_c = scenes.traversal_rays(1 << 13, seed=3, shadow=False)
+    rays_a = scenes.traversal_rays(1 << 13, seed=3, shadow=True)
+    orc = oracle.Oracle(sc, "port")
+    _, _, cn, cp = orc.trace_closest(rays_c, counts=True)
+    _, an, ap = orc.trace_any(rays_a, counts=True)
+    gpu.upload(sc)
+    dc = torch.from_numpy(rays_c.view(np.uint8)).to("cuda:0")
+    da = torch.from_numpy(rays_a.view(np.uint8)).to("cuda:0")
+    torch.cuda.synchronize()
+    got_c = gpu.trace_count_dev(dc.data_ptr(), len(rays_c), False)
+    got_a = gpu.trace_count_dev(da.data_ptr(), len(rays_a), True)
+    print("closest", got_c, (int(cn.sum()), int(cp.sum())), "any", got_a, (int(an.sum()), int(ap.sum())))
+    assert got_c == (int(cn.sum()), int(cp.sum()))
+    assert got_a[1] == int(ap.sum()) and int(an.sum()) <= got_a[0] <= int(an.sum()) * 1.05

@@ -225,7 +225,7 @@ tr_status upload_device_tables(tr_ctx* ctx) {
 struct BatchJob {
   const float4* __restrict__ rays;
   unsigned int n;
-  int32_t* prim;  // closest: prim id and t; any: hit flags
+  int32_t* prim;  // closest: prim id and t (prim, tout); any: hit flags (hit); all null: no output
   float* tout;
   uint8_t* hit;
   __device__ __forceinline__ unsigned int count() const { return n; }
@@ -241,9 +241,9 @@ struct BatchJob {
     if (prim) {
       prim[i] = h.prim;
       tout[i] = t_max;
-    } else {
+    } else if (hit) {
       hit[i] = occluded ? 1 : 0;
-    }
+    }  // neither: a counting run without outputs
   }
 };
 
@@ -252,6 +252,20 @@ __global__ void __launch_bounds__(128) k_trace_batch(DScene sc, BatchJob job, un
                                                     int refill) {
   VisitCount vc;
   persistent_traverse<ANY, false>(sc, job, fetch, err, vc, refill);
+}
+
+// The same traversal counting boxes and primitives tested (all lanes leave
+// the persistent loop together, so the warp reduction sees every lane).
+template <bool ANY>
+__global__ void __launch_bounds__(128) k_trace_count(DScene sc, BatchJob job, unsigned int* fetch, int* err,
+                                                    int refill, unsigned long long* counts) {
+  VisitCount vc;
+  persistent_traverse<ANY, true>(sc, job, fetch, err, vc, refill);
+  const unsigned int b = __reduce_add_sync(0xffffffffu, vc.boxes), p = __reduce_add_sync(0xffffffffu, vc.prims);
+  if ((threadIdx.x & 31u) == 0) {
+    atomicAdd(counts, (unsigned long long)b);
+    atomicAdd(counts + 1, (unsigned long long)p);
+  }
 }
 
 int traversal_grid(const tr_ctx* ctx, const void* kernel) {
@@ -655,6 +669,36 @@ tr_status tr_trace_any_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, uint8_t*
       ctx->tune.trav_refill_lanes);
   TR_CUDA(ctx, cudaGetLastError());
   return TR_OK;
+}
+
+tr_status tr_trace_count_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, int32_t any, uint64_t* boxes,
+                             uint64_t* prims) {
+  if (!ctx || !boxes || !prims || (n && !d_rays)) return TR_ERR_ARG;
+  if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
+  if (n > 0x7fffffffull) return set_err(ctx, TR_ERR_ARG, "too many rays");
+  if (((uintptr_t)d_rays & 15u) != 0) return set_err(ctx, TR_ERR_ARG, "ray buffer must be 16-byte aligned");
+  *boxes = *prims = 0;
+  if (n == 0) return TR_OK;
+  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  // scratch: the words after the error word and the fetch position
+  unsigned long long* counts = reinterpret_cast<unsigned long long*>(ctx->d_err.as<char>() + 16);
+  TR_CUDA(ctx, cudaMemsetAsync(ctx->d_err.as<int>() + 1, 0, sizeof(int), ctx->stream));
+  TR_CUDA(ctx, cudaMemsetAsync(counts, 0, 16, ctx->stream));
+  const BatchJob job{reinterpret_cast<const float4*>(d_rays), (unsigned int)n, nullptr, nullptr, nullptr};
+  unsigned int* fetch = reinterpret_cast<unsigned int*>(ctx->d_err.as<int>() + 1);
+  if (any)
+    k_trace_count<true><<<traversal_grid(ctx, (const void*)k_trace_count<true>), 128, 0, ctx->stream>>>(
+        ctx->dsc, job, fetch, ctx->d_err.as<int>(), ctx->tune.trav_refill_lanes, counts);
+  else
+    k_trace_count<false><<<traversal_grid(ctx, (const void*)k_trace_count<false>), 128, 0, ctx->stream>>>(
+        ctx->dsc, job, fetch, ctx->d_err.as<int>(), ctx->tune.trav_refill_lanes, counts);
+  TR_CUDA(ctx, cudaGetLastError());
+  unsigned long long h[2];
+  TR_CUDA(ctx, cudaMemcpyAsync(h, counts, 16, cudaMemcpyDeviceToHost, ctx->stream));
+  tr_status s = check_err_word(ctx);
+  *boxes = h[0];
+  *prims = h[1];
+  return s;
 }
 
 tr_status tr_trace_closest(tr_ctx* ctx, const tr_ray* rays, size_t n, int32_t* prim, float* t) {

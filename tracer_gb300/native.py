@@ -99,6 +99,9 @@ def lib() -> C.CDLL:
     L.tr_autotune.restype = st
     L.tr_autotune.argtypes = [vp, C.POINTER(TrBatchJob), C.c_uint32, C.c_int32, C.POINTER(TrTuning),
                               C.POINTER(C.c_double)]
+    L.tr_trace_count_dev.restype = st
+    L.tr_trace_count_dev.argtypes = [vp, C.c_void_p, C.c_size_t, C.c_int32, C.POINTER(C.c_uint64),
+                                     C.POINTER(C.c_uint64)]
     L.tr_render_dev.restype = st
     L.tr_render_dev.argtypes = [vp, C.POINTER(TrCamera), C.POINTER(TrFilter), C.POINTER(TrRenderParams),
                                 vp, vp, C.POINTER(TrStats)]
@@ -292,6 +295,12 @@ class GpuContext:
         best, ms = TrTuning(), C.c_double()
         self._check(self.L.tr_autotune(self.h, self._jobs(jobs), len(jobs), probe_spp, C.byref(best), C.byref(ms)))
         return best, ms.value
+
+    def trace_count_dev(self, d_rays: int, n: int, any_hit: bool):
+        """(boxes, primitives) tested by the traversal of n device rays."""
+        b, p = C.c_uint64(), C.c_uint64()
+        self._check(self.L.tr_trace_count_dev(self.h, d_rays, n, 1 if any_hit else 0, C.byref(b), C.byref(p)))
+        return b.value, p.value
 
     def render_dev(self, cam: TrCamera, filt: TrFilter, params: TrRenderParams, d_out: int, fp64: bool = False):
         stats = TrStats()
