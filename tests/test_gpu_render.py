@@ -157,3 +157,26 @@ def test_occluded_room_small(gpu):
     out, stats = gpu.render(cam, filt, par)
     assert stats.samples == 64 * 48 * 4
     _compare(out, ref, 0.8)
+
+
+@pytest.mark.parametrize("maker", ["cornell", "room"])
+def test_converged_fp64_image_within_one_percent(gpu, maker):
+    """The image bar: a 4096-spp render accumulated in FP64 on the GPU is
+    within 1% mean relative error of the oracle's 4096-spp FP64 render of
+    the same scene and seeds."""
+    if maker == "cornell":
+        sc, cam, filt, _ = scenes.cornell(24, 24, 1)
+        par = scenes.make_params(24, 24, 4096, 5, 5)
+    else:
+        sc, cam, filt, _ = scenes.occluded_room(20, 16, 1, n_tris=5000)
+        par = scenes.make_params(20, 16, 4096, 3, 10)
+    orc = oracle.Oracle(sc, "port")
+    orc.set_camera(cam, filt)
+    ref = orc.render(par, fp64=True)
+    gpu.upload(sc)
+    out, st = gpu.render(cam, filt, par, fp64=True)
+    assert st.samples == par.width * par.height * 4096
+    a, b = _image(out), _image(ref)
+    mre = mean_relative_error(a, b)
+    print(f"{maker}: 4096-spp FP64 MRE vs the oracle {mre:.2e}")
+    assert mre < 0.01

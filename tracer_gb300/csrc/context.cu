@@ -128,6 +128,8 @@ tr_status upload_device_tables(tr_ctx* ctx) {
     maxd = std::max(maxd, depth[i]);
   }
   if (maxd >= 60) return set_err(ctx, TR_ERR_UNSUPPORTED, "bvh deeper than the device traversal stack (60)");
+  if (hs.order.size() >= (1u << 26) || (size_t)ninterior >= (1u << 26))
+    return set_err(ctx, TR_ERR_UNSUPPORTED, "more than 2^26 primitives or interior nodes in one upload");
   hs.depth = maxd;
 
   std::vector<DNode> dn(ninterior);

@@ -165,12 +165,13 @@ struct Traversal {
 // until the queue is exhausted, so the kernel must be launched with whole
 // warps and no lane may return early.
 
-struct StackEntry {  // one 16-byte local store per push
-  int ref, cnt;
-  float t;
-  int pad;
-};
-
+// The traversal stack, in (L1-cached) local memory: 8 bytes per entry, one
+// 8-byte store per push. An entry holds the child reference shifted left by
+// 5 with its primitive count in the low 5 bits (count 31 stands for "31 or
+// more": the true count is then kept in a rarely touched second array) and
+// the child's box entry t. Child references stay below 2^26 (checked on
+// upload). A stack in shared memory was slower: shared memory takes its
+// space from the L1 that serves the node and triangle reads.
 template <bool ANY, bool COUNT>
 struct TravLane {
   static constexpr int kStack = 64;
@@ -180,7 +181,13 @@ struct TravLane {
   int cur, cnt, sp;
   Hit h;
   bool occluded;
-  StackEntry st[kStack];
+  int2 st[kStack];      // (ref << 5 | min(count, 31), t bits)
+  int big_cnt[kStack];  // counts of 31 or more, by stack index
+
+  __device__ __forceinline__ void push(int ref, int c, float t) {
+    if (c >= 31) big_cnt[sp] = c;
+    st[sp++] = make_int2((ref << 5) | min(c, 31), __float_as_int(t));
+  }
 
   // Starts a ray in scene `scene` of the set; returns false when it misses
   // the root box (done at once).
@@ -212,11 +219,11 @@ struct TravLane {
   // returns false when the traversal is over.
   __device__ __forceinline__ bool pop() {
     while (sp > 0) {
-      --sp;
-      const StackEntry e = st[sp];
-      if (e.t < t_max) {
-        cur = e.ref;
-        cnt = e.cnt;
+      const int2 e = st[--sp];
+      if (__int_as_float(e.y) < t_max) {
+        cur = e.x >> 5;
+        cnt = e.x & 31;
+        if (cnt == 31) cnt = big_cnt[sp];
         return true;
       }
     }
@@ -244,22 +251,15 @@ struct TravLane {
         occluded = false;
         return false;
       }
-      StackEntry e;
-      e.pad = 0;
       if (second_near) {
-        e.ref = lref;
-        e.cnt = lcnt;
-        e.t = tl;
+        push(lref, lcnt, tl);
         cur = rref;
         cnt = rcnt;
       } else {
-        e.ref = rref;
-        e.cnt = rcnt;
-        e.t = tr;
+        push(rref, rcnt, tr);
         cur = lref;
         cnt = lcnt;
       }
-      st[sp++] = e;
       return true;
     }
     if (hl) {
