@@ -509,6 +509,8 @@ static tr_status build_host_scene(tr_ctx* ctx, const tr_scene_desc* d, HostScene
     L.gz = hs.tshade[pr.shape].gz;
     L.emission = pr.emission;
     L.area_pdf = 1.0f / pr.area;
+    L.extent = fabsf(L.A.x) + fabsf(L.A.y) + fabsf(L.A.z) + fabsf(L.B.x) + fabsf(L.B.y) + fabsf(L.B.z) + fabsf(L.C.x) +
+               fabsf(L.C.y) + fabsf(L.C.z) + 1.0f;
     L.prim = p;
     hs.lights.push_back(L);
   }

@@ -605,13 +605,27 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
     // next-event estimation on every light (sample_area_light): the draws
     // happen here, the rest in k_nee
     const JobDev& J = job_of(P, slot);
+    const float pos_mag = fabsf(is.pos.x) + fabsf(is.pos.y) + fabsf(is.pos.z);
     for (int l = 0; l < J.nl; ++l) {
       const float lu = Pcg::next(st), lv = Pcg::next(st);
       Pcg::next(st);
       Pcg::next(st);
       Pcg::next(st);
-      P.NU[slot * P.nl_max + l] = make_float2(lu, lv);
-      P.q_nee[KIND][append(P.ctr + C_NEE + KIND)] = slot * P.nl_max + l;
+      const int item = slot * P.nl_max + l;
+      // A vertex well behind a light's plane gets nothing from it:
+      // k_nee's test dot(n, pos - light point) > 0 fails for every point
+      // of the (planar) light. The margin covers the rounding of the
+      // sampled point and of that dot product, so only items the exact test
+      // would reject are skipped here.
+      const DLight& lt = P.sc.lights[J.light_base + l];
+      const float side = dot(lt.gz, is.pos - lt.A);
+      const float tol = 1e-4f * (pos_mag + lt.extent);
+      if (side < -tol) {
+        P.SH[3 * (size_t)item + 2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        continue;
+      }
+      P.NU[item] = make_float2(lu, lv);
+      P.q_nee[KIND][append(P.ctr + C_NEE + KIND)] = item;
     }
     float4* sc = P.SC + 7 * (size_t)slot;
     sc[0] = make_float4(is.pos.x, is.pos.y, is.pos.z, __int_as_float(mat));

@@ -92,7 +92,8 @@ struct DLight {
   f3 emission;
   float area_pdf; // 1 / surface_area()
   int prim;
-  int pad[2];
+  float extent;   // sum of |coordinates| of A, B, C plus 1 (scale of the back-side margin)
+  int pad;
 };
 
 // Root of one scene of the uploaded set: its tree and its lights.
