@@ -13,8 +13,8 @@ camera samples per second over exactly K steps (CUDA events on the
 renderer's stream, synchronised on both sides, maximum over ranks); `e2e`
 repeats the measurement through the C ABI's host-buffer entry point
 (tr_render), which copies the film back every step. `convergence` times the
-plain path tracer to 1% relMSE against a converged FP64 reference of the
-same scene at 256x192.
+plain and the guided path tracer to 1% relMSE against a 2048-spp FP64
+reference of the same scene at 1024x768.
 
 --impl reference times the reference algorithm on the host cores instead:
 the CPU restatement in oracle/ (bit-exact with the reference's own build,
@@ -123,7 +123,7 @@ def _image(acc: np.ndarray) -> np.ndarray:
 GUIDE_BOX = {"occluded_room": ((-4.0, 0.0, -3.0), (4.0, 4.0, 3.0))}
 
 
-def convergence(ctx, name: str, size=(256, 192), ref_spp=4096, pass_spp=4, max_spp=1024, target=0.01,
+def convergence(ctx, name: str, size=(1024, 768), ref_spp=2048, pass_spp=8, max_spp=768, target=0.01,
                 alpha=0.5, train_steps=32, warm_steps=200, batch=65536, lr=1e-3):
     """Time for the plain and the guided GPU path tracer to reach `target`
     relMSE against a converged reference of the same scene. The reference
