@@ -269,6 +269,33 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def ranks():
+    """(rank, world size, local rank) from the torchrun environment."""
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def init_ranks(world: int):
+    """One process group per job of more than one rank: NCCL on GPUs, gloo
+    otherwise (the replicas exchange only timings, never data)."""
+    if world <= 1:
+        return None
+    import torch
+    import torch.distributed as dist
+    dist.init_process_group(backend="nccl" if torch.cuda.is_available() else "gloo")
+    return dist
+
+
+def max_over_ranks(value: float, dist, device) -> float:
+    """The largest value over all ranks (the slowest replica's time)."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def measured_peak_hbm():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -408,13 +435,8 @@ def run_batch(args):
     import torch
     from tracer_gb300.abi import TR_RENDER_TIME_STAGES as TS
     from tracer_gb300.native import GpuContext
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group(backend="nccl" if torch.cuda.is_available() else "gloo")
+    rank, world, local = ranks()
+    dist = init_ranks(world)
     torch.cuda.set_device(local)
     t0 = time.perf_counter()
     items = scenes.batch(64)
@@ -458,10 +480,7 @@ def run_batch(args):
     c1 = clocks.mark()
     clocks.__exit__()
     ms = e0.elapsed_time(e1)
-    if dist is not None:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist, f"cuda:{local}")
     samples = sum(s.samples for s in stats)
     value = world * samples / (ms / 1e3) / 1e6
     # end to end: the batch call plus every film copied back to the host
@@ -514,13 +533,8 @@ def run_traversal(args):
     import torch
     from tracer_gb300.abi import RAY_DTYPE
     from tracer_gb300.native import GpuContext
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group(backend="nccl" if torch.cuda.is_available() else "gloo")
+    rank, world, local = ranks()
+    dist = init_ranks(world)
     torch.cuda.set_device(local)
     n_tris, n_rays = 1 << 20, 1 << 22
     sc = scenes.traversal(n_tris)
@@ -575,10 +589,7 @@ def run_traversal(args):
     ms = e0.elapsed_time(e1)
     closest_ms = sum(ec[3 * k].elapsed_time(ec[3 * k + 1]) for k in range(args.steps)) / args.steps
     any_ms = sum(ec[3 * k + 1].elapsed_time(ec[3 * k + 2]) for k in range(args.steps)) / args.steps
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist, dev)
     value = world * 2 * n_rays * args.steps / (ms / 1e3) / 1e6
     # end to end: the host-buffer calls, rays in and results out every step
     barrier()
@@ -650,13 +661,8 @@ def run_ours(args):
     import torch
     from tracer_gb300.native import GpuContext
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group(backend="nccl" if torch.cuda.is_available() else "gloo")
+    rank, world, local = ranks()
+    dist = init_ranks(world)
     torch.cuda.set_device(local)
     label, sc, cam, filt, par = workload(args.workload, args.size)
     ctx = GpuContext(local)
@@ -699,10 +705,7 @@ def run_ours(args):
     c1 = clocks.mark()
     clocks.__exit__()
     ms = e0.elapsed_time(e1)
-    if dist is not None:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist, f"cuda:{local}")
     samples = sum(s.samples for s in stats)
     value = world * samples / (ms / 1e3) / 1e6
 
@@ -717,10 +720,7 @@ def run_ours(args):
         e2e_samples += st.samples
     barrier()
     e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, dist, f"cuda:{local}")
     e2e = world * e2e_samples / e2e_s / 1e6
     h2d = ctypes.sizeof(TrCamera) + ctypes.sizeof(TrFilter) + ctypes.sizeof(TrRenderParams)
 
