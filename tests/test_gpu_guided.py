@@ -72,3 +72,4 @@ def test_training_on_render_records(gpu):
     # the trained model guides a render without errors and with finite output
     out, st2 = _film(gpu, cam, filt, par, make_guide(0.5, *box, record=True))
     assert st2.samples == 64 * 48 * 8 and np.isfinite(out).all()
+
