@@ -316,14 +316,15 @@ __device__ void finish_sample(const Launch& P, int slot, unsigned long long& st,
   if (!valid3(L)) L = mk3(0.0f, 0.0f, 0.0f);  // eval_pixel_li returns {} (path_trace_renderer.cpp:204-209)
   if (P.guide_record) {
     // training records of this sample's vertices: the radiance that arrived
-    // along each continuation direction -- (L - L_after_vertex) / throughput
-    // plus the emission the ray reached -- times |cos| over the pdf the
-    // direction was drawn with
+    // along each continuation direction, (L - L_after_vertex) / throughput --
+    // what this integrator gains from it: emission reached by a continuation
+    // past depth 0 is not counted, so it is not a target either -- times
+    // |cos| over the pdf the direction was drawn with
     const int nv = P.NV[slot];
     for (int k = 0; k < nv; ++k) {
       const float4* r = P.VR + ((size_t)slot * P.maxd + k) * 4;
       const float4 a = r[0], b = r[1], c = r[2], d = r[3];
-      const float li = lum(mk3(L.x - d.x, L.y - d.y, L.z - d.z)) / fmaxf(c.w, 1e-20f) + d.w;
+      const float li = lum(mk3(L.x - d.x, L.y - d.y, L.z - d.z)) / fmaxf(c.w, 1e-20f);
       const float w = li / b.w;
       if (!(w > 0.0f) || !(w < 1e30f)) continue;
       const unsigned int idx = (unsigned int)append(P.ctr + C_TB);
@@ -467,23 +468,7 @@ __global__ void __launch_bounds__(128) k_logic(Launch P, int cur) {
       }
       if (flags & F_MIS) direct = direct + mulc(mk3(p4.x, p4.y, p4.z), mis_contribution(P, slot));
       L = L + direct;
-      if (flags & F_REC) {
-        // the recorded vertex's continuation: radiance after its direct
-        // light, and the emission its ray reached (not counted by the
-        // integrator past depth 0, but part of the incident radiance the
-        // network learns)
-        float le = 0.0f;
-        const float4 hc = P.HC[slot];
-        const int hp = __float_as_int(hc.x);
-        if (hp >= 0 && !(flags & F_TERMINATE)) {
-          const DPrim& hpr = P.sc.prims[hp];
-          if (hpr.emissive && hpr.kind == PRIM_TRIANGLE) {
-            const float4 p1 = P.P1[slot];
-            if (dot(P.sc.tshade[hpr.shape].gz, mk3(-p1.x, -p1.y, -p1.z)) > 0.0f) le = lum(hpr.emission);
-          }
-        }
-        P.VR[((size_t)slot * P.maxd + P.NV[slot] - 1) * 4 + 3] = make_float4(L.x, L.y, L.z, le);
-      }
+      if (flags & F_REC) P.VR[((size_t)slot * P.maxd + P.NV[slot] - 1) * 4 + 3] = make_float4(L.x, L.y, L.z, 0.0f);
     }
     const float4 hit = P.HC[slot];
     const int pid = __float_as_int(hit.x);
