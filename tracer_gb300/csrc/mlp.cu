@@ -496,15 +496,18 @@ tr_status guide_pack(tr_ctx* ctx) {
   return e == cudaSuccess ? TR_OK : cuda_fail(ctx, e, "guide weight packing");
 }
 
-static int guide_grid(tr_ctx* ctx, int n) {
+// Forward: up to four CTAs per SM (50 KB of shared memory and 64 TMEM
+// columns each), so that one CTA's MMAs overlap another's epilogue.
+// Backward: one per SM (each holds 512 TMEM columns, the whole SM's).
+static int guide_grid(tr_ctx* ctx, int n, int per_sm) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
   const int tiles = (n + mlp::kTile - 1) / mlp::kTile;
-  return std::max(1, std::min(tiles, sms));
+  return std::max(1, std::min(tiles, sms * per_sm));
 }
 
 tr_status guide_forward(tr_ctx* ctx, const float* d_in, int n, float* d_out, __half* d_acts) {
-  mlp::k_forward<<<guide_grid(ctx, n), 128, mlp::kSmemBytes, ctx->stream>>>(
+  mlp::k_forward<<<guide_grid(ctx, n, 4), 128, mlp::kSmemBytes, ctx->stream>>>(
       ctx->guide->img.as<uint8_t>(), d_in, n, d_out, d_acts, ctx->d_err.as<int>() + 2, nullptr);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? TR_OK : cuda_fail(ctx, e, "k_forward");
@@ -513,7 +516,7 @@ tr_status guide_forward(tr_ctx* ctx, const float* d_in, int n, float* d_out, __h
 tr_status guide_forward_rows_on_device(tr_ctx* ctx, const float* d_in, const unsigned int* d_n, float* d_out) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-  mlp::k_forward<<<std::max(sms, 1), 128, mlp::kSmemBytes, ctx->stream>>>(
+  mlp::k_forward<<<std::max(sms, 1) * 4, 128, mlp::kSmemBytes, ctx->stream>>>(
       ctx->guide->img.as<uint8_t>(), d_in, 0, d_out, nullptr, ctx->d_err.as<int>() + 2, d_n);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? TR_OK : cuda_fail(ctx, e, "k_forward");
@@ -575,7 +578,7 @@ tr_status guide_backward(tr_ctx* ctx, const float* d_in, const float* d_dout, in
   s = guide_forward(ctx, d_in, n, g->out.as<float>(), g->acts.as<__half>());
   if (s != TR_OK) return s;
   TR_CUDA(ctx, cudaMemsetAsync(d_grads, 0, mlp::kParams * 4, ctx->stream));
-  mlp::k_backward<<<guide_grid(ctx, n), 128, mlp::kBSmemBytes, ctx->stream>>>(
+  mlp::k_backward<<<guide_grid(ctx, n, 1), 128, mlp::kBSmemBytes, ctx->stream>>>(
       g->img_t.as<uint8_t>(), d_in, g->acts.as<__half>(), d_dout, n, d_grads, ctx->d_err.as<int>() + 2);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? TR_OK : cuda_fail(ctx, e, "k_backward");
@@ -603,7 +606,7 @@ tr_status guide_train_step(tr_ctx* ctx, const float* d_in, const float* d_dir, c
   if (s != TR_OK) return s;
   GuideModel* g = ctx->guide;
   TR_CUDA(ctx, cudaMemsetAsync(g->grads.p, 0, mlp::kParams * 4, ctx->stream));
-  mlp::k_backward<<<guide_grid(ctx, n), 128, mlp::kBSmemBytes, ctx->stream>>>(
+  mlp::k_backward<<<guide_grid(ctx, n, 1), 128, mlp::kBSmemBytes, ctx->stream>>>(
       g->img_t.as<uint8_t>(), d_in, g->acts.as<__half>(), g->dout.as<float>(), n, g->grads.as<float>(),
       ctx->d_err.as<int>() + 2);
   ++g->step;
