@@ -325,6 +325,9 @@ tr_status tr_cancel(tr_ctx* ctx);
  * weight logit, log concentration, unnormalised mean direction). The flat
  * fp32 parameter vector holds, per layer, W (out x in, row-major) then b. */
 enum { TR_GUIDE_INPUTS = 7, TR_GUIDE_OUTPUTS = 40, TR_GUIDE_PARAMS = 15592 };
+/* Range the log concentration outputs are clamped to. */
+#define TR_GUIDE_LOG_KAPPA_MIN (-4.0f)
+#define TR_GUIDE_LOG_KAPPA_MAX (7.0f)
 /* Initialises the parameters (uniform in +-1/sqrt(fan_in), seeded). */
 tr_status tr_guide_init(tr_ctx* ctx, uint64_t seed);
 tr_status tr_guide_set_params(tr_ctx* ctx, const float* params, size_t n);
@@ -337,7 +340,7 @@ tr_status tr_guide_backward_dev(tr_ctx* ctx, const float* d_in, const float* d_d
                                 float* d_grads);
 /* Training loss of a batch: -sum_i w_i log p(dir_i | in_i) / sum_i w_i, p the
  * network's vMF mixture (lobe j: out[5j] weight logit, out[5j+1] log kappa
- * clamped to [-4, 7], out[5j+2..4] mean direction, normalised); d_dir unit
+ * clamped to [TR_GUIDE_LOG_KAPPA_MIN, TR_GUIDE_LOG_KAPPA_MAX], out[5j+2..4] mean direction, normalised); d_dir unit
  * vectors (n x 3), d_weight >= 0 (n). d_dout receives d loss / d out (n x 40). */
 tr_status tr_guide_loss_dev(tr_ctx* ctx, const float* d_in, const float* d_dir, const float* d_weight,
                             size_t n, float* d_dout, float* loss);

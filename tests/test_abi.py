@@ -61,3 +61,14 @@ def test_status_strings():
 def test_tuning_struct_layout():
     from tracer_gb300.abi import TrTuning
     assert ctypes.sizeof(TrTuning) == 16
+
+
+def test_guide_kappa_range_matches_header():
+    import re
+    from pathlib import Path
+
+    from tracer_gb300.native import GpuContext
+    h = (Path(__file__).resolve().parents[1] / "include" / "tracer_gpu.h").read_text()
+    lo = float(re.search(r"#define TR_GUIDE_LOG_KAPPA_MIN \(([-0-9.]+)f\)", h).group(1))
+    hi = float(re.search(r"#define TR_GUIDE_LOG_KAPPA_MAX \(([-0-9.]+)f\)", h).group(1))
+    assert GpuContext.GUIDE_LOG_KAPPA == (lo, hi)

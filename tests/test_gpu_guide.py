@@ -133,7 +133,8 @@ def mixture_nll(out, d, w):
     import torch
     z = out.reshape(-1, 8, 5)
     logpi = torch.log_softmax(z[..., 0], -1)
-    s = z[..., 1].clamp(-4, 7)
+    from tracer_gb300.native import GpuContext
+    s = z[..., 1].clamp(*GpuContext.GUIDE_LOG_KAPPA)
     kappa = torch.exp(s)
     m = z[..., 2:5]
     mu = m / (m.norm(dim=-1, keepdim=True) + 1e-6)

@@ -356,7 +356,8 @@ __global__ void __launch_bounds__(128, 1)
 // Negative log-likelihood of the directions under the 8-lobe vMF mixture,
 // weighted per row: loss = -sum_i w_i log p(omega_i | x_i) / sum_i w_i.
 // Lobe j of row i: out[5j] weight logit, out[5j+1] log kappa (clamped to
-// [-4, 7]), out[5j+2..4] unnormalised mean direction;
+// [TR_GUIDE_LOG_KAPPA_MIN, TR_GUIDE_LOG_KAPPA_MAX]), out[5j+2..4]
+// unnormalised mean direction;
 // vMF(omega) = kappa / (2 pi (1 - exp(-2 kappa))) exp(kappa (mu.omega - 1)).
 
 struct Lobe {
@@ -388,7 +389,7 @@ __global__ void k_loss(const float* __restrict__ out, const float* __restrict__ 
     Lobe L[kLobes];
     for (int j = 0; j < kLobes; ++j) {
       pi[j] /= esum;
-      const float s = fminf(fmaxf(z[5 * j + 1], -4.0f), 7.0f);
+      const float s = fminf(fmaxf(z[5 * j + 1], TR_GUIDE_LOG_KAPPA_MIN), TR_GUIDE_LOG_KAPPA_MAX);
       const float kappa = expf(s);
       const float3 m = make_float3(z[5 * j + 2], z[5 * j + 3], z[5 * j + 4]);
       const float mlen = sqrtf(m.x * m.x + m.y * m.y + m.z * m.z) + 1e-6f;
@@ -410,7 +411,7 @@ __global__ void k_loss(const float* __restrict__ out, const float* __restrict__ 
       const float s = z[5 * j + 1];
       const float e2 = expf(-2.0f * b.kappa);
       const float dlogk = 1.0f - 2.0f * b.kappa * e2 / fmaxf(-expm1f(-2.0f * b.kappa), 1e-30f) + b.kappa * (b.c - 1.0f);
-      d[5 * j + 1] = (s > -4.0f && s < 7.0f) ? -wi * q * dlogk : 0.0f;
+      d[5 * j + 1] = (s > TR_GUIDE_LOG_KAPPA_MIN && s < TR_GUIDE_LOG_KAPPA_MAX) ? -wi * q * dlogk : 0.0f;
       const float f = -wi * q * b.kappa / b.mlen;
       d[5 * j + 2] = f * (om.x - b.c * b.mu.x);
       d[5 * j + 3] = f * (om.y - b.c * b.mu.y);

@@ -48,6 +48,7 @@ enum : int {
   F_MIS = 2,        // ...and it includes a MIS ray
   F_TERMINATE = 4,  // the path ends once that lighting is added
   F_REC = 8,        // the previous vertex wrote a guiding record awaiting its radiance
+  F_GCONT = 16,     // ...and its guided continuation is the MIS ray of its direct lighting
 };
 
 enum : int {  // counter slots
@@ -94,9 +95,10 @@ struct Launch {
   int refill;  // traversal lane-refill threshold (tr_tuning)
   float4 *P0, *P1, *P2, *P3, *P4;  // cont o|flags, cont d|depth, coef|sample, L|px, coef_prev|py
   unsigned long long* rng;
-  float4 *M0, *M1, *M2;  // mis o|bsdf_pdf, mis d|abs_cos, bsdf_f
+  float4 *M0, *M1, *M2;  // mis o|bsdf_pdf, mis d|abs_cos, bsdf_f (guided: o|p_guided, d|p_bsdf, f_eval|p_plain)
   float4 *HC, *HM;       // hits: prim, t_attr, alpha, beta
-  float4* SC;            // shading context for nee: 7 per slot (pos|mat, wo, g, s frames)
+  float4* SC;            // shading context for nee: 7 per slot (pos|mat, wo, g, s frames; the last
+                         // also holds the guided vertex's network row, normal correction and |cos|)
   float2* NU;            // light-sample draws per (slot, light)
   float4* SH;            // shadow: 3 per (slot, light): o|t_max, d, contrib|valid
   int* q_ext[2];
@@ -157,7 +159,7 @@ struct Mixture {
     }
     for (int j = 0; j < 8; ++j) {
       pi[j] /= sum;
-      kappa[j] = expf(fminf(fmaxf(z[5 * j + 1], -4.0f), 7.0f));
+      kappa[j] = expf(fminf(fmaxf(z[5 * j + 1], TR_GUIDE_LOG_KAPPA_MIN), TR_GUIDE_LOG_KAPPA_MAX));
       norm[j] = kappa[j] / (6.283185307179586f * -expm1f(-2.0f * kappa[j]));
       const f3 m = mk3(z[5 * j + 2], z[5 * j + 3], z[5 * j + 4]);
       const float len = sqrtf(m.x * m.x + m.y * m.y + m.z * m.z) + 1e-6f;
@@ -316,10 +318,10 @@ __device__ void finish_sample(const Launch& P, int slot, unsigned long long& st,
   if (!valid3(L)) L = mk3(0.0f, 0.0f, 0.0f);  // eval_pixel_li returns {} (path_trace_renderer.cpp:204-209)
   if (P.guide_record) {
     // training records of this sample's vertices: the radiance that arrived
-    // along each continuation direction, (L - L_after_vertex) / throughput --
-    // what this integrator gains from it: emission reached by a continuation
-    // past depth 0 is not counted, so it is not a target either -- times
-    // |cos| over the pdf the direction was drawn with
+    // along each continuation direction, (L - L_after_vertex) / throughput,
+    // where L_after_vertex leaves out the emission the continuation reached
+    // (so that emission is part of the target), times |cos| over the pdf
+    // the direction was drawn with
     const int nv = P.NV[slot];
     for (int k = 0; k < nv; ++k) {
       const float4* r = P.VR + ((size_t)slot * P.maxd + k) * 4;
@@ -446,6 +448,53 @@ __device__ f3 mis_contribution(const Launch& P, int slot) {
   return divs(muls(f, w), m0.w);
 }
 
+// Power-heuristic weight of a strategy of density a against one of density
+// b, zero when a is (no 0/0).
+__device__ __forceinline__ float mis_w(float a, float b) { return a > 0.0f ? power_heuristic(a, b) : 0.0f; }
+
+// The direct-lighting integrand of a Lambertian vertex over incident
+// direction w, per unit emitted radiance and |cos|: what the reference's
+// two strategies sum to in expectation (sample_area_light with the BSDF's
+// eval and pdf, sample_bsdf with the sampler's own integrand and density,
+// src/renderer/direct_illumination.cpp:35-71,144-198). fe, pb: eval and pdf
+// at w; fs, ps: the plain sampler's integrand and density at w; lpdf: the
+// light's solid-angle density at w.
+__device__ __forceinline__ f3 direct_integrand(f3 fe, float pb, f3 fs, float ps, float lpdf) {
+  return muls(fe, mis_w(lpdf, pb)) + muls(fs, mis_w(ps, lpdf));
+}
+
+// A guided vertex's continuation doubles as its MIS ray: the emission it
+// reaches, weighted against next-event estimation by the guided density
+// (the other half of k_nee_guided). `hit` is the continuation's hit.
+__device__ f3 guided_mis_contribution(const Launch& P, int slot, float4 hit) {
+  const int pid = __float_as_int(hit.x);
+  if (pid < 0) return mk3(0.0f, 0.0f, 0.0f);
+  const DPrim& pr = P.sc.prims[pid];
+  if (!pr.emissive) return mk3(0.0f, 0.0f, 0.0f);
+  const float4 m0 = P.M0[slot], m1 = P.M1[slot], m2 = P.M2[slot];
+  const f3 o = mk3(m0.x, m0.y, m0.z), d = mk3(m1.x, m1.y, m1.z);
+  const f3 gz = P.sc.tshade[pr.shape].gz;
+  if (!(dot(gz, -d) > 0.0f)) return mk3(0.0f, 0.0f, 0.0f);
+  const float4 sc0 = P.SC[7 * (size_t)slot], sc6 = P.SC[7 * (size_t)slot + 6];
+  const float lpdf = light_pdf_at(pr.area, o, o + scale(d, hit.y), gz);
+  const float pg = m0.w, pb = m1.w, ps = m2.w;
+  const f3 fs = ps > 0.0f ? muls(P.sc.mats[__float_as_int(sc0.w)].diffuse_coef, sc6.z) : mk3(0.0f, 0.0f, 0.0f);
+  const f3 g = direct_integrand(mk3(m2.x, m2.y, m2.z), pb, fs, ps, lpdf);
+  return muls(mulc(pr.emission, g), sc6.w * mis_w(pg, lpdf) / pg);
+}
+
+// Emission the continuation of a recorded vertex reaches (full, unweighted):
+// part of the radiance that arrived along it, and so of the training target.
+__device__ __forceinline__ f3 continuation_emission(const Launch& P, int slot, float4 hit) {
+  const int pid = __float_as_int(hit.x);
+  if (pid < 0) return mk3(0.0f, 0.0f, 0.0f);
+  const DPrim& pr = P.sc.prims[pid];
+  if (!pr.emissive) return mk3(0.0f, 0.0f, 0.0f);
+  const float4 p1 = P.P1[slot];
+  if (!(dot(P.sc.tshade[pr.shape].gz, mk3(-p1.x, -p1.y, -p1.z)) > 0.0f)) return mk3(0.0f, 0.0f, 0.0f);
+  return pr.emission;
+}
+
 __global__ void __launch_bounds__(128) k_logic(Launch P, int cur) {
   const int nxt = cur ^ 1;
   const unsigned int n = P.ctr[C_ACT + cur];
@@ -467,8 +516,17 @@ __global__ void __launch_bounds__(128) k_logic(Launch P, int cur) {
         if (c.w != 0.0f) direct = direct + mk3(c.x, c.y, c.z);
       }
       if (flags & F_MIS) direct = direct + mulc(mk3(p4.x, p4.y, p4.z), mis_contribution(P, slot));
+      if (flags & F_GCONT)
+        direct = direct + mulc(mk3(p4.x, p4.y, p4.z),
+                               guided_mis_contribution(P, slot, (flags & F_TERMINATE) ? P.HM[slot] : P.HC[slot]));
       L = L + direct;
-      if (flags & F_REC) P.VR[((size_t)slot * P.maxd + P.NV[slot] - 1) * 4 + 3] = make_float4(L.x, L.y, L.z, 0.0f);
+      if (flags & F_REC) {
+        // the record's baseline leaves out the continuation's own emission,
+        // so the target is the whole radiance that arrived along it
+        const float4 p2 = P.P2[slot];
+        const f3 Lb = L - mulc(mk3(p2.x, p2.y, p2.z), continuation_emission(P, slot, P.HC[slot]));
+        P.VR[((size_t)slot * P.maxd + P.NV[slot] - 1) * 4 + 3] = make_float4(Lb.x, Lb.y, Lb.z, 0.0f);
+      }
     }
     const float4 hit = P.HC[slot];
     const int pid = __float_as_int(hit.x);
@@ -521,9 +579,11 @@ __device__ __forceinline__ float lambert_plain_pdf(const Bsdf& bsdf, f3 wo, f3 w
 
 // Replaces the plain sample `bs` by the one-sample MIS choice: with
 // probability alpha (sel < alpha) a mixture direction, else the plain
-// sample itself (which may be invalid: then nothing is returned).
+// sample itself (which may be invalid: then nothing is returned). ps and nc
+// receive the plain sampler's density at the chosen direction and the
+// normal correction of its integrand (0 where that density is 0).
 __device__ __noinline__ void guided_pick(const Launch& P, const Bsdf& bsdf, const Isect& is, unsigned int row,
-                                         float sel, float g0, float g1, BsdfSample& bs) {
+                                         float sel, float g0, float g1, BsdfSample& bs, float& ps, float& nc) {
   Mixture mx;
   mx.decode(P.gout + (size_t)row * 40);
   f3 wi;
@@ -533,10 +593,26 @@ __device__ __noinline__ void guided_pick(const Launch& P, const Bsdf& bsdf, cons
     if (!bs.valid()) return;
     wi = bs.wi;
   }
-  const float pb = lambert_plain_pdf(bsdf, is.wo, wi);
+  ps = lambert_plain_pdf(bsdf, is.wo, wi);
+  nc = ps > 0.0f ? normal_correct(bsdf.g, bsdf.s, wi) : 0.0f;
   bs.wi = wi;
-  bs.f = pb > 0.0f ? muls(bsdf.m->diffuse_coef, normal_correct(bsdf.g, bsdf.s, wi)) : mk3(0.0f, 0.0f, 0.0f);
-  bs.pdf = P.guide_alpha * mx.pdf(wi) + (1.0f - P.guide_alpha) * pb;
+  bs.f = muls(bsdf.m->diffuse_coef, nc);
+  bs.pdf = P.guide_alpha * mx.pdf(wi) + (1.0f - P.guide_alpha) * ps;
+}
+
+// Next-event estimation at a guided vertex: the light sample of direction
+// wl, weighted against the guided continuation (density pg at wl) instead
+// of the plain BSDF sample. With guided_mis_contribution it estimates the
+// same direct-lighting integral as the reference's pair of strategies.
+// Returns that integrand times |cos| per unit emission, times the weight.
+__device__ __noinline__ f3 guided_nee_factor(const Launch& P, const Bsdf& bsdf, f3 wo, f3 wl, int row, float lpdf) {
+  Mixture mx;
+  mx.decode(P.gout + (size_t)row * 40);
+  const float ps = lambert_plain_pdf(bsdf, wo, wl);
+  const f3 fs = ps > 0.0f ? muls(bsdf.m->diffuse_coef, normal_correct(bsdf.g, bsdf.s, wl)) : mk3(0.0f, 0.0f, 0.0f);
+  const f3 g = direct_integrand(bsdf.phong_eval_agg(wl, wo), bsdf.phong_pdf_agg(wl, wo), fs, ps, lpdf);
+  const float pg = P.guide_alpha * mx.pdf(wl) + (1.0f - P.guide_alpha) * ps;
+  return muls(g, abs_cos(wl, bsdf.g.z) * mis_w(lpdf, pg));
 }
 
 // Network inputs of every Phong-material vertex of this iteration (rows in
@@ -596,13 +672,25 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
     // Guided continuation. The plain sample above still decides, as in the
     // reference, whether this vertex gets direct lighting at all; a guided
     // direction without contribution only ends the path after it.
-    bool guided_end = false;
+    // At a guided vertex the continuation is also the MIS ray of the
+    // direct lighting (traced even when the path ends here, as long as the
+    // integrand can be non-zero along it), so emission it reaches counts.
+    bool guided_end = false, g_trace = false;
+    float g_ps = 0.0f, g_nc = 0.0f, g_pb = 0.0f, g_cos = 0.0f;
+    f3 g_fe = mk3(0.0f, 0.0f, 0.0f);
     const bool gv =
         KIND == MAT_PHONG && P.guide_alpha > 0.0f && bsdf.m->w_specular == 0.0f && !bsdf.fringe(is.wo);
     if (gv) {
       const float sel = Pcg::next(st), g0 = Pcg::next(st), g1 = Pcg::next(st);
-      guided_pick(P, bsdf, is, i, sel, g0, g1, bs);
+      guided_pick(P, bsdf, is, i, sel, g0, g1, bs, g_ps, g_nc);
       guided_end = black(bs.f) || bs.pdf < kEps;
+      if (bs.pdf >= kEps) {
+        const f3 wc = normalize(normalize(bs.wi));
+        g_fe = bsdf.phong_eval_agg(wc, is.wo);
+        g_pb = bsdf.phong_pdf_agg(wc, is.wo);
+        g_cos = abs_cos(is.g.z, wc);
+        g_trace = !black(bs.f) || !black(g_fe);
+      }
     }
     // next-event estimation on every light (sample_area_light): the draws
     // happen here, the rest in k_nee
@@ -636,10 +724,19 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
     sc[3] = make_float4(is.g.y.z, is.g.z.x, is.g.z.y, is.g.z.z);
     sc[4] = make_float4(is.s.x.x, is.s.x.y, is.s.x.z, is.s.y.x);
     sc[5] = make_float4(is.s.y.y, is.s.y.z, is.s.z.x, is.s.z.y);
-    sc[6] = make_float4(is.s.z.z, 0.0f, 0.0f, 0.0f);
+    sc[6] = make_float4(is.s.z.z, __int_as_float(gv ? (int)i : -1), g_nc, g_cos);
     // MIS BSDF ray (sample_bsdf, src/renderer/direct_illumination.cpp:144-155)
     int flags = F_PENDING;
-    {
+    if (gv) {
+      if (g_trace) {
+        const f3 mo = is.eps_offset(bs.wi);
+        const f3 md = normalize(normalize(bs.wi));
+        P.M0[slot] = make_float4(mo.x, mo.y, mo.z, bs.pdf);
+        P.M1[slot] = make_float4(md.x, md.y, md.z, g_pb);
+        P.M2[slot] = make_float4(g_fe.x, g_fe.y, g_fe.z, g_ps);
+        flags |= F_GCONT;
+      }
+    } else {
       const float v0 = Pcg::next(st), v1 = Pcg::next(st), v2 = Pcg::next(st);
       const BsdfSample ms = sample_bsdf_shared<KIND>(bsdf, is.wo, v0, v1, v2);
       if (ms.valid()) {
@@ -671,6 +768,8 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
     if (term) {
       flags |= F_TERMINATE;
       P.P0[slot] = make_float4(p0.x, p0.y, p0.z, __int_as_float(flags));
+      // a guided continuation still traced for its emission only
+      if (flags & F_GCONT) P.q_ext[nxt][append(P.ctr + C_EXT + nxt)] = 2 * slot + 1;
     } else {
       const f3 no = is.eps_offset(bs.wi);
       const f3 nd = normalize(normalize(bs.wi));
@@ -739,13 +838,25 @@ __global__ void __launch_bounds__(128) k_nee(Launch P) {
         const float dist = dist_minus_eps(len2f(to_light), too_close);
         if (!too_close) {
           to_light = normalize(to_light);
-          const f3 bf = MatOps<KIND>::eval(bsdf, to_light, wo);
-          if (!black(bf)) {
-            const float bpdf = MatOps<KIND>::pdf(bsdf, to_light, wo);
-            const f3 fl = muls(mulc(lt.emission, bf), abs_cos(to_light, bsdf.g.z));
-            const float w = power_heuristic(lpdf, bpdf);
-            const float4 p4 = P.P4[slot];
-            const f3 cc = mulc(mk3(p4.x, p4.y, p4.z), divs(muls(fl, w), lpdf));
+          const int grow = __float_as_int(g.y);  // network row of a guided vertex, else -1
+          f3 cc = mk3(0.0f, 0.0f, 0.0f);          // contribution before the shadow test
+          bool trace = false;
+          const float4 p4 = P.P4[slot];
+          if (KIND == MAT_PHONG && grow >= 0) {
+            const f3 fw = guided_nee_factor(P, bsdf, wo, to_light, grow, lpdf);
+            trace = !black(fw);
+            cc = mulc(mk3(p4.x, p4.y, p4.z), divs(mulc(lt.emission, fw), lpdf));
+          } else {
+            const f3 bf = MatOps<KIND>::eval(bsdf, to_light, wo);
+            trace = !black(bf);
+            if (trace) {
+              const float bpdf = MatOps<KIND>::pdf(bsdf, to_light, wo);
+              const f3 fl = muls(mulc(lt.emission, bf), abs_cos(to_light, bsdf.g.z));
+              const float w = power_heuristic(lpdf, bpdf);
+              cc = mulc(mk3(p4.x, p4.y, p4.z), divs(muls(fl, w), lpdf));
+            }
+          }
+          if (trace) {
             const f3 sd = normalize(to_light);
             rec[0] = make_float4(pos.x, pos.y, pos.z, dist);
             rec[1] = make_float4(sd.x, sd.y, sd.z, 0.0f);

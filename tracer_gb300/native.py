@@ -225,6 +225,7 @@ class GpuContext:
 
     # ---- path-guiding model
     GUIDE_PARAMS = 15592
+    GUIDE_LOG_KAPPA = (-4.0, 7.0)  # TR_GUIDE_LOG_KAPPA_MIN / _MAX
 
     def guide_init(self, seed: int = 0) -> None:
         self._check(self.L.tr_guide_init(self.h, seed))
