@@ -80,7 +80,7 @@ def test_trained_guide_keeps_the_plain_expectation_in_the_room(gpu):
     MIS rays of guided vertices) now pass through the slit and reach the
     light, so the guided weights of next-event estimation and the
     continuation's emission term both carry weight. Block means over
-    16x16-pixel blocks at 1024 spp match the plain renderer's."""
+    16x16-pixel blocks at 4096 spp match the plain renderer's."""
     sc, cam, filt, _ = scenes.occluded_room(64, 48, 8, n_tris=20000)
     gpu.upload(sc)
     gpu.guide_init(seed=0)
@@ -90,11 +90,11 @@ def test_trained_guide_keeps_the_plain_expectation_in_the_room(gpu):
         _film(gpu, cam, filt, par, make_guide(0.0 if k == 0 else 0.5, *box, record=True))
         loss = gpu.guide_train_on_records(200, 65536, 1e-3, seed=k)
         assert np.isfinite(loss)
-    par = scenes.make_params(64, 48, 1024, 3, 10, seed_base=1)
+    par = scenes.make_params(64, 48, 4096, 3, 10, seed_base=1)
     plain, _ = gpu.render(cam, filt, par, fp64=True)
-    par_g = scenes.make_params(64, 48, 1024, 3, 10, seed_base=9_000_000)
+    par_g = scenes.make_params(64, 48, 4096, 3, 10, seed_base=9_000_000)
     guided, st = _film(gpu, cam, filt, par_g, make_guide(0.5, *box))
-    assert st.samples == 64 * 48 * 1024
+    assert st.samples == 64 * 48 * 4096
     a = _image(plain).reshape(3, 16, 4, 16, 3).mean((1, 3))
     b = _image(guided).reshape(3, 16, 4, 16, 3).mean((1, 3))
     rel = np.abs(a - b) / np.maximum(a, 1e-3)

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "context.h"
+#include "mixture.cuh"
 #include "mlp.h"
 #include "tc05.cuh"
 
@@ -82,7 +83,7 @@ constexpr int kPackThreads = 64 * 16 + 3 * 64 * 64 + 48 * 64 + 304;  // W0, W1..
 // the four hidden layers are stored too (acts[l][row][64]) for training.
 __global__ void __launch_bounds__(128, 1)
     k_forward(const uint8_t* __restrict__ img, const float* __restrict__ x, int n, float* __restrict__ out,
-              __half* __restrict__ acts, int* err, const unsigned int* __restrict__ n_dev) {
+              __half* __restrict__ acts, int* err, const unsigned int* __restrict__ n_dev, int decode) {
   extern __shared__ __align__(1024) uint8_t sm[];
   if (n_dev) n = (int)*n_dev;  // row count produced on the device (guided rendering)
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -131,10 +132,10 @@ __global__ void __launch_bounds__(128, 1)
       if (!ok) break;
       phase ^= 1u;
       tc05::fence_after();
-      for (int c0 = 0; c0 < N; c0 += 16) {
-        float v[16];
-        tc05::tmem_ld16(tmem + lane_base + (uint32_t)c0, v);
-        if (l < kLayers - 1) {
+      if (l < kLayers - 1) {
+        for (int c0 = 0; c0 < N; c0 += 16) {
+          float v[16];
+          tc05::tmem_ld16(tmem + lane_base + (uint32_t)c0, v);
           __align__(16) __half h[16];
 #pragma unroll
           for (int j = 0; j < 16; ++j) h[j] = __float2half_rn(fmaxf(v[j] + bias[l * 64 + c0 + j], 0.0f));
@@ -145,10 +146,30 @@ __global__ void __launch_bounds__(128, 1)
             *reinterpret_cast<int4*>(dst) = *reinterpret_cast<const int4*>(h);
             *reinterpret_cast<int4*>(dst + 8) = *reinterpret_cast<const int4*>(h + 8);
           }
-        } else if (row < n) {
+        }
+      } else {
+        // the output row, whole in this thread: raw, or decoded into the
+        // mixture's lobe parameters (guided rendering)
+        float o[kOutPad];
 #pragma unroll
-          for (int j = 0; j < 16; ++j)
-            if (c0 + j < kOut) out[(size_t)row * kOut + c0 + j] = v[j] + bias[256 + c0 + j];
+        for (int c = 0; c < kOutPad / 16; ++c) {
+          float v[16];
+          tc05::tmem_ld16(tmem + lane_base + (uint32_t)(16 * c), v);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) o[16 * c + j] = 16 * c + j < kOut ? v[j] + bias[256 + 16 * c + j] : 0.0f;
+        }
+        if (row < n) {
+          if (decode) {
+            float dd[kMixFloats];
+            mixture_decode(o, dd);
+            float4* dst = reinterpret_cast<float4*>(out + (size_t)row * kMixFloats);
+#pragma unroll
+            for (int q = 0; q < kMixFloats / 4; ++q)
+              dst[q] = make_float4(dd[4 * q], dd[4 * q + 1], dd[4 * q + 2], dd[4 * q + 3]);
+          } else {
+#pragma unroll
+            for (int j = 0; j < kOut; ++j) out[(size_t)row * kOut + j] = o[j];
+          }
         }
       }
       tc05::fence_before();
@@ -509,7 +530,7 @@ static int guide_grid(tr_ctx* ctx, int n, int per_sm) {
 
 tr_status guide_forward(tr_ctx* ctx, const float* d_in, int n, float* d_out, __half* d_acts) {
   mlp::k_forward<<<guide_grid(ctx, n, 4), 128, mlp::kSmemBytes, ctx->stream>>>(
-      ctx->guide->img.as<uint8_t>(), d_in, n, d_out, d_acts, ctx->d_err.as<int>() + 2, nullptr);
+      ctx->guide->img.as<uint8_t>(), d_in, n, d_out, d_acts, ctx->d_err.as<int>() + 2, nullptr, 0);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? TR_OK : cuda_fail(ctx, e, "k_forward");
 }
@@ -518,7 +539,7 @@ tr_status guide_forward_rows_on_device(tr_ctx* ctx, const float* d_in, const uns
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
   mlp::k_forward<<<std::max(sms, 1) * 4, 128, mlp::kSmemBytes, ctx->stream>>>(
-      ctx->guide->img.as<uint8_t>(), d_in, 0, d_out, nullptr, ctx->d_err.as<int>() + 2, d_n);
+      ctx->guide->img.as<uint8_t>(), d_in, 0, d_out, nullptr, ctx->d_err.as<int>() + 2, d_n, 1);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? TR_OK : cuda_fail(ctx, e, "k_forward");
 }

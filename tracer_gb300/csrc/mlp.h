@@ -39,7 +39,8 @@ tr_status guide_backward(tr_ctx* ctx, const float* d_in, const float* d_dout, in
 // One Adam step on the weighted vMF-mixture NLL of a batch; *d_loss (device) receives the loss.
 tr_status guide_train_step(tr_ctx* ctx, const float* d_in, const float* d_dir, const float* d_w, int n, float lr);
 void release_guide(tr_ctx* ctx);
-// Forward pass over *d_n rows (a count produced on the device), no host sync.
+// Forward pass over *d_n rows (a count produced on the device), no host sync;
+// each output row is the decoded mixture (kMixFloats floats, mixture.cuh).
 tr_status guide_forward_rows_on_device(tr_ctx* ctx, const float* d_in, const unsigned int* d_n, float* d_out);
 // `steps` Adam steps on random batches of `batch` rows drawn from `count` records.
 tr_status guide_train_on(tr_ctx* ctx, const float* rec_in, const float* rec_dir, const float* rec_w, unsigned int count,

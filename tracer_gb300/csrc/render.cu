@@ -37,6 +37,7 @@
 #include <vector>
 
 #include "context.h"
+#include "mixture.cuh"
 #include "mlp.h"
 #include "shade.cuh"
 #include "traverse.cuh"
@@ -114,7 +115,7 @@ struct Launch {
   int guide_record, maxd;
   float gbox_lo[3], gbox_scale[3];
   float* gfeat;  // network inputs, one row per entry of q_mat[0]
-  float* gout;   // network outputs (mixture parameters), same rows
+  float* gout;   // decoded mixtures (kMixFloats per row), same rows
   float4* VR;    // 4 per (slot, vertex): features 0-3 | features 4-6, pdf | direction, throughput | radiance
   int* NV;       // records of the slot's current sample
   float *tb_in, *tb_dir, *tb_w;
@@ -143,56 +144,6 @@ __device__ __forceinline__ void guide_features(const Launch& P, f3 pos, f3 wo, f
   f[5] = wo.z;
   f[6] = rough;
 }
-
-// The network's 8-lobe von Mises-Fisher mixture (parametrisation of the
-// guiding loss in mlp.cu).
-struct Mixture {
-  float pi[8], kappa[8], norm[8];
-  f3 mu[8];
-  __device__ void decode(const float* __restrict__ z) {
-    float amax = -INFINITY;
-    for (int j = 0; j < 8; ++j) amax = fmaxf(amax, z[5 * j]);
-    float sum = 0.0f;
-    for (int j = 0; j < 8; ++j) {
-      pi[j] = expf(z[5 * j] - amax);
-      sum += pi[j];
-    }
-    for (int j = 0; j < 8; ++j) {
-      pi[j] /= sum;
-      kappa[j] = expf(fminf(fmaxf(z[5 * j + 1], TR_GUIDE_LOG_KAPPA_MIN), TR_GUIDE_LOG_KAPPA_MAX));
-      norm[j] = kappa[j] / (6.283185307179586f * -expm1f(-2.0f * kappa[j]));
-      const f3 m = mk3(z[5 * j + 2], z[5 * j + 3], z[5 * j + 4]);
-      const float len = sqrtf(m.x * m.x + m.y * m.y + m.z * m.z) + 1e-6f;
-      mu[j] = mk3(m.x / len, m.y / len, m.z / len);
-    }
-  }
-  __device__ float pdf(f3 w) const {
-    float p = 0.0f;
-    for (int j = 0; j < 8; ++j) p += pi[j] * norm[j] * expf(kappa[j] * (dot(mu[j], w) - 1.0f));
-    return p;
-  }
-  // lobe by u_lobe, then the numerically stable vMF sampling of W. Jakob,
-  // "Numerically stable sampling of the von Mises-Fisher distribution on
-  // S^2" (2012), in the frame of the lobe's mean (Duff et al. 2017 basis).
-  __device__ f3 sample(float u_lobe, float u1, float u2) const {
-    int j = 0;
-    float c = pi[0];
-    while (j < 7 && u_lobe >= c) c += pi[++j];
-    const float k = kappa[j];
-    float w = 1.0f + logf(u1 + (1.0f - u1) * expf(-2.0f * k)) / k;
-    w = fminf(fmaxf(w, -1.0f), 1.0f);
-    const float r = sqrtf(fmaxf(0.0f, 1.0f - w * w));
-    float sp, cp;
-    sincosf(6.283185307179586f * u2, &sp, &cp);
-    const f3 n = mu[j];
-    const float sgn = copysignf(1.0f, n.z);
-    const float a = -1.0f / (sgn + n.z);
-    const float b = n.x * n.y * a;
-    const f3 b1 = mk3(1.0f + sgn * n.x * n.x * a, sgn * b, -sgn * n.x);
-    const f3 b2 = mk3(b, sgn + n.y * n.y * a, -n.y);
-    return scale(b1, r * cp) + scale(b2, r * sp) + scale(n, w);
-  }
-};
 
 // Warp-aggregated queue append. The active lanes are grouped by counter
 // address (__match_any_sync): one call site can target different queues per
@@ -546,7 +497,17 @@ __global__ void __launch_bounds__(128) k_logic(Launch P, int cur) {
     }
     P.P3[slot] = make_float4(L.x, L.y, L.z, p3.w);
     const int kind = P.sc.mats[pr.material].kind;
-    P.q_mat[kind][append(P.ctr + C_MAT + kind)] = slot;
+    const int qi = append(P.ctr + C_MAT + kind);
+    P.q_mat[kind][qi] = slot;
+    if (kind == MAT_PHONG && P.guide_alpha > 0.0f) {
+      // network inputs of the vertex, row qi of this iteration's forward pass
+      const float4 p1 = P.P1[slot];
+      const f3 d = mk3(p1.x, p1.y, p1.z);
+      float f[7];
+      guide_features(P, mk3(p0.x, p0.y, p0.z) + scale(d, hit.y), -d, 1.0f, f);
+      float* out = P.gfeat + (size_t)qi * 7;
+      for (int k = 0; k < 7; ++k) out[k] = f[k];
+    }
   }
   count_add(P.stats, finished);
 }
@@ -584,8 +545,7 @@ __device__ __forceinline__ float lambert_plain_pdf(const Bsdf& bsdf, f3 wo, f3 w
 // normal correction of its integrand (0 where that density is 0).
 __device__ __noinline__ void guided_pick(const Launch& P, const Bsdf& bsdf, const Isect& is, unsigned int row,
                                          float sel, float g0, float g1, BsdfSample& bs, float& ps, float& nc) {
-  Mixture mx;
-  mx.decode(P.gout + (size_t)row * 40);
+  const Mixture mx{P.gout + (size_t)row * kMixFloats};
   f3 wi;
   if (sel < P.guide_alpha) {
     wi = normalize(mx.sample(sel / P.guide_alpha, g0, g1));
@@ -606,28 +566,12 @@ __device__ __noinline__ void guided_pick(const Launch& P, const Bsdf& bsdf, cons
 // same direct-lighting integral as the reference's pair of strategies.
 // Returns that integrand times |cos| per unit emission, times the weight.
 __device__ __noinline__ f3 guided_nee_factor(const Launch& P, const Bsdf& bsdf, f3 wo, f3 wl, int row, float lpdf) {
-  Mixture mx;
-  mx.decode(P.gout + (size_t)row * 40);
+  const Mixture mx{P.gout + (size_t)row * kMixFloats};
   const float ps = lambert_plain_pdf(bsdf, wo, wl);
   const f3 fs = ps > 0.0f ? muls(bsdf.m->diffuse_coef, normal_correct(bsdf.g, bsdf.s, wl)) : mk3(0.0f, 0.0f, 0.0f);
   const f3 g = direct_integrand(bsdf.phong_eval_agg(wl, wo), bsdf.phong_pdf_agg(wl, wo), fs, ps, lpdf);
   const float pg = P.guide_alpha * mx.pdf(wl) + (1.0f - P.guide_alpha) * ps;
   return muls(g, abs_cos(wl, bsdf.g.z) * mis_w(lpdf, pg));
-}
-
-// Network inputs of every Phong-material vertex of this iteration (rows in
-// q_mat[0] order), for the guided continuation of k_material<MAT_PHONG>.
-__global__ void __launch_bounds__(128) k_features(Launch P) {
-  const unsigned int n = P.ctr[C_MAT + MAT_PHONG];
-  for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int slot = P.q_mat[MAT_PHONG][i];
-    const float4 p0 = P.P0[slot], p1 = P.P1[slot];
-    const f3 o = mk3(p0.x, p0.y, p0.z), d = mk3(p1.x, p1.y, p1.z);
-    float f[7];
-    guide_features(P, o + scale(d, P.HC[slot].y), -d, 1.0f, f);
-    float* out = P.gfeat + (size_t)i * 7;
-    for (int k = 0; k < 7; ++k) out[k] = f[k];
-  }
 }
 
 // The BSDF sample, shared out of line by the two call sites of k_material
@@ -1061,7 +1005,7 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     const unsigned int cap = gp->max_records ? gp->max_records : (4u << 20);
     cudaError_t e = cudaSuccess;
     if (P.guide_alpha > 0.0f) {
-      if ((e = rb->gfeat.reserve(N * 7 * 4)) != cudaSuccess || (e = rb->gout.reserve(N * 40 * 4)) != cudaSuccess)
+      if ((e = rb->gfeat.reserve(N * 7 * 4)) != cudaSuccess || (e = rb->gout.reserve(N * kMixFloats * 4)) != cudaSuccess)
         return cuda_fail(ctx, e, "guide inference buffers");
       P.gfeat = rb->gfeat.as<float>();
       P.gout = rb->gout.as<float>();
@@ -1148,8 +1092,7 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     mark();
     k_logic<<<grid, 128, 0, st>>>(P, cur);
     if (P.guide_alpha > 0.0f) {
-      // network rows for this iteration's Phong-material vertices
-      k_features<<<grid, 128, 0, st>>>(P);
+      // decoded mixtures for this iteration's Phong-material vertices (inputs written by k_logic)
       tr_status gs = guide_forward_rows_on_device(ctx, P.gfeat, P.ctr + C_MAT + MAT_PHONG, P.gout);
       if (gs != TR_OK) return gs;
     }
