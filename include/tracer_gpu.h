@@ -195,12 +195,22 @@ tr_status tr_synchronize(tr_ctx* ctx);
  *  - shade_blocks_per_sm: 128-thread blocks per SM of the shading kernels
  *    (grid-stride loops);
  *  - graph_iterations: wavefront iterations captured into one CUDA graph
- *    and replayed as one launch (rounded up to even; 0: no graph). */
+ *    and replayed as one launch (rounded up to even; 0: no graph);
+ *  - any_node_width (2 or 4): BVH node width of any-hit (shadow) traversal.
+ *    Width 4 walks a tree collapsed from the reference's binary BVH: its
+ *    boxes are a subset of the binary tree's, and the slab test passes a box
+ *    whenever it passes a box inside it, so a ray reaches the same primitives
+ *    and the occlusion result is identical; only the visiting order, the
+ *    primitive tests before an early exit and the visit counts differ.
+ *    Closest-hit traversal always keeps the reference's binary order (it
+ *    decides which of two equal-distance primitives is reported). A scene
+ *    whose collapsed tree could overflow the traversal stack uses width 2. */
 typedef struct tr_tuning {
   int32_t trav_refill_lanes;
   int32_t trav_blocks_per_sm;
   int32_t shade_blocks_per_sm;
   int32_t graph_iterations;
+  int32_t any_node_width;
 } tr_tuning;
 tr_status tr_ctx_set_tuning(tr_ctx* ctx, const tr_tuning* t);
 tr_status tr_ctx_get_tuning(const tr_ctx* ctx, tr_tuning* t);
@@ -226,6 +236,11 @@ tr_status tr_bvh_export(tr_ctx* ctx, tr_bvh_node32* nodes, uint32_t* prim_order)
 /* Replaces the uploaded scene's BVH with an externally built one (same layout). */
 tr_status tr_bvh_upload(tr_ctx* ctx, const tr_bvh_node32* nodes, size_t num_nodes,
                         const uint32_t* prim_order, size_t num_prims);
+/* The four-wide any-hit tree built at upload (tr_tuning.any_node_width):
+ * its node count (0 when the scene uses binary any-hit traversal only) and
+ * the bound on the traversal stack its walk can need. No reference
+ * counterpart. */
+tr_status tr_any_tree_info(const tr_ctx* ctx, uint64_t* num_nodes4, int32_t* stack_bound);
 
 /* Closest hit for n rays: Scene::intersect_p (src/core/scene.cpp:36-38 ->
  * BVHAccel::intersect_p, src/accelerator/bvh.cpp:149-185). prim[i] is the scene
@@ -305,11 +320,10 @@ tr_status tr_render_batch_dev(tr_ctx* ctx, const tr_batch_job* jobs, uint32_t n,
 /* Launch autotuner. No reference counterpart. Times the batch (each job
  * capped at probe_spp samples per pixel; the jobs' films are overwritten)
  * under candidate tr_tuning settings -- resident traversal blocks per SM,
- * lane-refill threshold, shading grid, CUDA-graph chunk length -- by
- * coordinate descent (median of three timed renders each, a change kept
- * only if 2% faster), sets the best on the context and returns it with its
- * time. The BVH node width stays 2: wider nodes would change the traversal
- * order, and with it which of two equal-distance primitives is reported. */
+ * lane-refill threshold, shading grid, CUDA-graph chunk length, any-hit BVH
+ * node width -- by coordinate descent (median of three timed renders each, a
+ * change kept only if 2% faster), sets the best on the context and returns
+ * it with its time. */
 tr_status tr_autotune(tr_ctx* ctx, const tr_batch_job* jobs, uint32_t n, int32_t probe_spp,
                       tr_tuning* best, double* best_ms);
 

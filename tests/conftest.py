@@ -19,3 +19,25 @@ def gpu():
     ctx = GpuContext(0)
     yield ctx
     ctx.close()
+
+
+class tuned:
+    """Context manager: the GPU context's launch tuning with some fields
+    changed, restored afterwards (the `gpu` fixture is shared)."""
+
+    FIELDS = ("trav_refill_lanes", "trav_blocks_per_sm", "shade_blocks_per_sm", "graph_iterations", "any_node_width")
+
+    def __init__(self, gpu, **fields):
+        self.gpu, self.fields = gpu, fields
+
+    def __enter__(self):
+        self.old = {f: getattr(self.gpu.tuning(), f) for f in self.FIELDS}
+        self._apply({**self.old, **self.fields})
+        return self.gpu
+
+    def __exit__(self, *exc):
+        self._apply(self.old)
+
+    def _apply(self, v):
+        self.gpu.set_tuning(v["trav_refill_lanes"], v["trav_blocks_per_sm"], v["shade_blocks_per_sm"],
+                            v["graph_iterations"], v["any_node_width"])

@@ -55,7 +55,8 @@ def test_graph_replay_changes_nothing(gpu):
         for o in outs[1:]:
             assert np.array_equal(o.view(np.uint32), outs[0].view(np.uint32))
     finally:
-        gpu.set_tuning(old.trav_refill_lanes, old.trav_blocks_per_sm, old.shade_blocks_per_sm, old.graph_iterations)
+        gpu.set_tuning(old.trav_refill_lanes, old.trav_blocks_per_sm, old.shade_blocks_per_sm, old.graph_iterations,
+                       old.any_node_width)
 
 
 def test_scene_set_traversal_uses_scene_zero(gpu):
@@ -84,11 +85,12 @@ def test_autotune_picks_a_valid_tuning_and_keeps_results(gpu):
         best, ms = gpu.autotune(jobs, probe_spp=1)
         assert ms > 0
         t = gpu.tuning()
-        assert (t.trav_refill_lanes, t.trav_blocks_per_sm, t.shade_blocks_per_sm, t.graph_iterations) == \
-               (best.trav_refill_lanes, best.trav_blocks_per_sm, best.shade_blocks_per_sm, best.graph_iterations)
-        assert 1 <= t.trav_refill_lanes <= 32 and t.shade_blocks_per_sm >= 1
+        fields = ("trav_refill_lanes", "trav_blocks_per_sm", "shade_blocks_per_sm", "graph_iterations", "any_node_width")
+        assert [getattr(t, f) for f in fields] == [getattr(best, f) for f in fields]
+        assert 1 <= t.trav_refill_lanes <= 32 and t.shade_blocks_per_sm >= 1 and t.any_node_width in (2, 4)
         gpu.render_batch_dev(jobs)
         for b, f in zip(before, films):
             assert np.array_equal(b.view(np.uint32), f.cpu().numpy().view(np.uint32))
     finally:
-        gpu.set_tuning(old.trav_refill_lanes, old.trav_blocks_per_sm, old.shade_blocks_per_sm, old.graph_iterations)
+        gpu.set_tuning(old.trav_refill_lanes, old.trav_blocks_per_sm, old.shade_blocks_per_sm, old.graph_iterations,
+                       old.any_node_width)

@@ -117,7 +117,9 @@ def test_visit_counts_match_oracle(gpu):
     _, an, ap = orc.trace_any(ar, counts=True)
     gpu.upload(sc)
     par.flags = TR_RENDER_COUNT_VISITS
-    _, st = gpu.render(cam, filt, par)
+    from conftest import tuned
+    with tuned(gpu, any_node_width=2):  # the reference's binary order (the four-wide walk counts differently)
+        _, st = gpu.render(cam, filt, par)
     # paths are the oracle's up to CUDA-vs-glibc transcendentals in sampling
     pairs = ((st.extend_rays, len(cr)), (st.closest_boxes, cn.sum()), (st.closest_prims, cp.sum()))
     print("gpu vs oracle:", [(int(g), int(w)) for g, w in pairs], "shadow rays", st.shadow_rays, len(ar))
@@ -132,18 +134,19 @@ def test_visit_counts_match_oracle(gpu):
 
 
 def test_tuning_does_not_change_results(gpu):
-    """Launch tuning (grid sizes, lane refill threshold) never changes the film."""
-    sc, cam, filt, par = scenes.disney_grid(48, 32, 2)
-    gpu.upload(sc)
-    base, _ = gpu.render(cam, filt, par)
-    old = gpu.tuning()
-    try:
-        for refill, tb, sb in ((1, 1, 1), (32, 3, 40), (7, 0, 9)):
-            gpu.set_tuning(refill, tb, sb)
-            out, _ = gpu.render(cam, filt, par)
+    """Launch tuning (grid sizes, lane refill threshold, any-hit node
+    width) never changes the film."""
+    from conftest import tuned
+    for make in (lambda: scenes.disney_grid(48, 32, 2), lambda: scenes.occluded_room(48, 32, 2, n_tris=20000)):
+        sc, cam, filt, par = make()
+        gpu.upload(sc)
+        with tuned(gpu, any_node_width=2):
+            base, _ = gpu.render(cam, filt, par)
+        for refill, tb, sb, w in ((1, 1, 1, 2), (32, 3, 40, 4), (7, 0, 9, 4), (20, 0, 16, 4)):
+            with tuned(gpu, trav_refill_lanes=refill, trav_blocks_per_sm=tb, shade_blocks_per_sm=sb,
+                       any_node_width=w):
+                out, _ = gpu.render(cam, filt, par)
             assert np.array_equal(out.view(np.uint32), base.view(np.uint32))
-    finally:
-        gpu.set_tuning(old.trav_refill_lanes, old.trav_blocks_per_sm, old.shade_blocks_per_sm)
 
 
 def test_occluded_room_small(gpu):

@@ -138,8 +138,60 @@ def test_trace_visit_counts_equal_the_oracle(gpu):
     dc = torch.from_numpy(rays_c.view(np.uint8)).to("cuda:0")
     da = torch.from_numpy(rays_a.view(np.uint8)).to("cuda:0")
     torch.cuda.synchronize()
-    got_c = gpu.trace_count_dev(dc.data_ptr(), len(rays_c), False)
-    got_a = gpu.trace_count_dev(da.data_ptr(), len(rays_a), True)
+    from conftest import tuned
+    with tuned(gpu, any_node_width=2):
+        got_c = gpu.trace_count_dev(dc.data_ptr(), len(rays_c), False)
+        got_a = gpu.trace_count_dev(da.data_ptr(), len(rays_a), True)
     print("closest", got_c, (int(cn.sum()), int(cp.sum())), "any", got_a, (int(an.sum()), int(ap.sum())))
     assert got_c == (int(cn.sum()), int(cp.sum()))
     assert got_a[1] == int(ap.sum()) and int(an.sum()) <= got_a[0] <= int(an.sum()) * 1.05
+
+
+@pytest.mark.parametrize("case", ["random0", "random1", "random2", "traversal", "room", "edges"])
+def test_four_wide_any_hit_equals_the_oracle(gpu, case):
+    """Any-hit traversal of the four-wide tree collapsed from the reference's
+    binary BVH: the occlusion flags are the oracle's, bit for bit, and the
+    primitive tests stay within the binary walk's set (an early exit can
+    only stop sooner or elsewhere)."""
+    from conftest import tuned
+    rng = np.random.default_rng(17)
+    if case.startswith("random"):
+        sc = scenes.random_scene(int(case[-1]), n_tris=400, n_spheres=30)
+        rays = _random_rays(rng, 30000, shadow=True)
+    elif case == "traversal":
+        sc = scenes.traversal(1 << 16, seed=1)
+        rays = scenes.traversal_rays(1 << 16, seed=1, shadow=True)
+    elif case == "edges":
+        # axis-parallel rays (infinite inverse directions, NaN slabs where an
+        # origin lies on a box plane) from vertices, from box-plane values and
+        # from random points, with finite lengths
+        sc = scenes.cornell(8, 8, 1)[0]
+        pts = np.concatenate([sc.positions.astype(np.float32),
+                              rng.choice(np.float32([-1, -0.5, 0, 0.25, 0.5, 0.99, 1]), (200, 3)),
+                              rng.uniform(-1.2, 1.2, (200, 3)).astype(np.float32)])
+        o, d = [], []
+        for p in pts:
+            for ax in range(3):
+                for sgn in (-1.0, 1.0):
+                    dd = np.zeros(3, np.float32)
+                    dd[ax] = sgn
+                    o.append(p)
+                    d.append(dd)
+        o, d = np.array(o, np.float32), np.array(d, np.float32)
+        rays = scenes.make_rays(o, d, 0.0, rng.uniform(0.1, 3.0, len(o)).astype(np.float32))
+    else:
+        sc, cam, filt, par = scenes.occluded_room(32, 24, 1, n_tris=30000)
+        o = rng.uniform([-3.9, 0.1, -2.9], [3.9, 3.9, 2.9], (30000, 3)).astype(np.float32)
+        tgt = rng.uniform([4.5, 0.5, -1.5], [7.5, 3.5, 1.5], (30000, 3)).astype(np.float32)
+        rays = scenes.make_rays(o, tgt - o, 0.0, np.linalg.norm(tgt - o, axis=1).astype(np.float32) * 0.999)
+    orc = oracle.Oracle(sc, "port")
+    gpu.upload(sc)
+    nodes4, bound = gpu.any_tree_info()
+    print(case, "four-wide nodes", nodes4, "stack bound", bound)
+    assert nodes4 > 0 and bound <= 96
+    want = orc.trace_any(rays)
+    with tuned(gpu, any_node_width=4):
+        assert gpu.tuning().any_node_width == 4
+        got = gpu.trace_any(rays)
+    print(case, "occluded", int(want.sum()), "of", len(rays))
+    assert np.array_equal(want, got)

@@ -95,6 +95,73 @@ inline float as_float(int i) {
   return f;
 }
 
+// A child of a four-wide node under construction.
+struct Child4 {
+  float lo[3], hi[3];
+  int ref, cnt;
+};
+
+void node_children(const DNode& n, Child4& l, Child4& r) {
+  const uint32_t cc = (uint32_t)n.d.z;
+  l = Child4{{n.a.x, n.a.y, n.a.z}, {n.a.w, n.b.x, n.b.y}, n.d.x, (int)(cc & 0xffffu)};
+  r = Child4{{n.b.z, n.b.w, n.c.x}, {n.c.y, n.c.z, n.c.w}, n.d.y, (int)(cc >> 16)};
+}
+
+float half_area(const Child4& c) {
+  const float x = c.hi[0] - c.lo[0], y = c.hi[1] - c.lo[1], z = c.hi[2] - c.lo[2];
+  return x * y + y * z + z * x;
+}
+
+// Collapses the child-pair tree below DNode `root` into four-wide nodes
+// appended to `out` (the interior child of largest surface area is opened
+// until four children or only leaves remain) and returns the root's index.
+// `stack` receives a bound on the traversal stack its any-hit walk needs: a
+// node pushes at most all its children but the one it enters, so the bound
+// is (children - 1) plus the largest bound of an interior child.
+int collapse4(const std::vector<DNode>& dn, int root, std::vector<DNode4>& out, int& stack) {
+  Child4 ch[4];
+  int k = 2;
+  node_children(dn[root], ch[0], ch[1]);
+  while (k < 4) {
+    int best = -1;
+    float area = -1.0f;
+    for (int i = 0; i < k; ++i)
+      if (ch[i].cnt == 0 && half_area(ch[i]) > area) {
+        area = half_area(ch[i]);
+        best = i;
+      }
+    if (best < 0) break;
+    node_children(dn[ch[best].ref], ch[best], ch[k]);
+    ++k;
+  }
+  const int idx = (int)out.size();
+  out.emplace_back();
+  int refs[4] = {0, 0, 0, 0}, cnts[4] = {-1, -1, -1, -1}, deepest = 0;
+  for (int i = 0; i < k; ++i) {
+    cnts[i] = ch[i].cnt;
+    if (ch[i].cnt > 0) {
+      refs[i] = ch[i].ref;
+    } else {
+      int sub = 0;
+      refs[i] = collapse4(dn, ch[i].ref, out, sub);
+      deepest = std::max(deepest, sub);
+    }
+  }
+  stack = (k - 1) + deepest;
+  float v[6][4] = {};
+  for (int i = 0; i < k; ++i)
+    for (int c = 0; c < 3; ++c) {
+      v[c][i] = ch[i].lo[c];
+      v[3 + c][i] = ch[i].hi[c];
+    }
+  DNode4& o = out[idx];
+  float4* box = &o.lox;
+  for (int r = 0; r < 6; ++r) box[r] = float4{v[r][0], v[r][1], v[r][2], v[r][3]};
+  o.ref = int4{refs[0], refs[1], refs[2], refs[3]};
+  o.cnt = int4{cnts[0], cnts[1], cnts[2], cnts[3]};
+  return idx;
+}
+
 }  // namespace
 
 // Builds DNodes + slots from hs.nodes/hs.order and uploads every table.
@@ -204,11 +271,27 @@ tr_status upload_device_tables(tr_ctx* ctx) {
       R.offset = dix[first];
     }
   }
+  // the four-wide any-hit tree of every scene, unless its stack bound is
+  // above the traversal stack
+  std::vector<DNode4> dn4;
+  dn4.reserve(dn.size() / 2 + nsc);
+  int stack4 = 0;
+  for (size_t k = 0; k < nsc; ++k)
+    if (roots[k].kind == 1) {
+      int sub = 0;
+      roots[k].offset4 = collapse4(dn, roots[k].offset, dn4, sub);
+      stack4 = std::max(stack4, sub);
+    }
+  const bool wide = stack4 <= kStackWide;
+  if (wide) TR_CUDA(ctx, put(ctx->d_nodes4, dn4.data(), dn4.size() * sizeof(DNode4)));
+  ctx->any4_nodes = wide ? dn4.size() : 0;
+  ctx->any4_stack = stack4;
   TR_CUDA(ctx, put(ctx->d_roots, roots.data(), roots.size() * sizeof(SceneRoot)));
   TR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
 
   DScene& sc = ctx->dsc;
   sc.nodes = ctx->d_nodes.as<DNode>();
+  sc.nodes4 = wide ? ctx->d_nodes4.as<DNode4>() : nullptr;
   sc.slots = ctx->d_slots.as<float4>();
   sc.spheres = ctx->d_spheres.as<DSphere>();
   sc.prims = ctx->d_prims.as<DPrim>();
@@ -249,20 +332,20 @@ struct BatchJob {
   }
 };
 
-template <bool ANY>
+template <bool ANY, bool WIDE = false>
 __global__ void __launch_bounds__(128) k_trace_batch(DScene sc, BatchJob job, unsigned int* fetch, int* err,
                                                     int refill) {
   VisitCount vc;
-  persistent_traverse<ANY, false>(sc, job, fetch, err, vc, refill);
+  persistent_traverse<ANY, false, WIDE>(sc, job, fetch, err, vc, refill);
 }
 
 // The same traversal counting boxes and primitives tested (all lanes leave
 // the persistent loop together, so the warp reduction sees every lane).
-template <bool ANY>
+template <bool ANY, bool WIDE = false>
 __global__ void __launch_bounds__(128) k_trace_count(DScene sc, BatchJob job, unsigned int* fetch, int* err,
                                                     int refill, unsigned long long* counts) {
   VisitCount vc;
-  persistent_traverse<ANY, true>(sc, job, fetch, err, vc, refill);
+  persistent_traverse<ANY, true, WIDE>(sc, job, fetch, err, vc, refill);
   const unsigned int b = __reduce_add_sync(0xffffffffu, vc.boxes), p = __reduce_add_sync(0xffffffffu, vc.prims);
   if ((threadIdx.x & 31u) == 0) {
     atomicAdd(counts, (unsigned long long)b);
@@ -358,7 +441,7 @@ tr_status tr_ctx_set_tuning(tr_ctx* ctx, const tr_tuning* t) {
   if (!ctx || !t) return TR_ERR_ARG;
   if (t->trav_refill_lanes < 1 || t->trav_refill_lanes > 32 || t->trav_blocks_per_sm < 0 ||
       t->trav_blocks_per_sm > 64 || t->shade_blocks_per_sm < 1 || t->shade_blocks_per_sm > 64 ||
-      t->graph_iterations < 0 || t->graph_iterations > 64)
+      t->graph_iterations < 0 || t->graph_iterations > 64 || (t->any_node_width != 2 && t->any_node_width != 4))
     return set_err(ctx, TR_ERR_ARG, "tuning out of range");
   ctx->tune = *t;
   return TR_OK;
@@ -603,6 +686,13 @@ tr_status tr_bvh_info(tr_ctx* ctx, size_t* num_nodes, size_t* num_prims) {
   return TR_OK;
 }
 
+tr_status tr_any_tree_info(const tr_ctx* ctx, uint64_t* num_nodes4, int32_t* stack_bound) {
+  if (!ctx || !num_nodes4 || !stack_bound) return TR_ERR_ARG;
+  *num_nodes4 = ctx->any4_nodes;
+  *stack_bound = ctx->any4_stack;
+  return TR_OK;
+}
+
 tr_status tr_bvh_export(tr_ctx* ctx, tr_bvh_node32* nodes, uint32_t* prim_order) {
   if (!ctx || !nodes || !prim_order) return TR_ERR_ARG;
   if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
@@ -668,9 +758,13 @@ tr_status tr_trace_any_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, uint8_t*
   if (((uintptr_t)d_rays & 15u) != 0) return set_err(ctx, TR_ERR_ARG, "ray buffer must be 16-byte aligned");
   TR_CUDA(ctx, cudaMemsetAsync(ctx->d_err.as<int>() + 1, 0, sizeof(int), ctx->stream));  // fetch position
   const BatchJob job{reinterpret_cast<const float4*>(d_rays), (unsigned int)n, nullptr, nullptr, d_hit};
-  k_trace_batch<true><<<traversal_grid(ctx, (const void*)k_trace_batch<true>), 128, 0, ctx->stream>>>(
-      ctx->dsc, job, reinterpret_cast<unsigned int*>(ctx->d_err.as<int>() + 1), ctx->d_err.as<int>(),
-      ctx->tune.trav_refill_lanes);
+  unsigned int* fetch = reinterpret_cast<unsigned int*>(ctx->d_err.as<int>() + 1);
+  if (any_wide(ctx))
+    k_trace_batch<true, true><<<traversal_grid(ctx, (const void*)k_trace_batch<true, true>), 128, 0, ctx->stream>>>(
+        ctx->dsc, job, fetch, ctx->d_err.as<int>(), ctx->tune.trav_refill_lanes);
+  else
+    k_trace_batch<true><<<traversal_grid(ctx, (const void*)k_trace_batch<true>), 128, 0, ctx->stream>>>(
+        ctx->dsc, job, fetch, ctx->d_err.as<int>(), ctx->tune.trav_refill_lanes);
   TR_CUDA(ctx, cudaGetLastError());
   return TR_OK;
 }
@@ -690,7 +784,10 @@ tr_status tr_trace_count_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, int32_
   TR_CUDA(ctx, cudaMemsetAsync(counts, 0, 16, ctx->stream));
   const BatchJob job{reinterpret_cast<const float4*>(d_rays), (unsigned int)n, nullptr, nullptr, nullptr};
   unsigned int* fetch = reinterpret_cast<unsigned int*>(ctx->d_err.as<int>() + 1);
-  if (any)
+  if (any && any_wide(ctx))
+    k_trace_count<true, true><<<traversal_grid(ctx, (const void*)k_trace_count<true, true>), 128, 0, ctx->stream>>>(
+        ctx->dsc, job, fetch, ctx->d_err.as<int>(), ctx->tune.trav_refill_lanes, counts);
+  else if (any)
     k_trace_count<true><<<traversal_grid(ctx, (const void*)k_trace_count<true>), 128, 0, ctx->stream>>>(
         ctx->dsc, job, fetch, ctx->d_err.as<int>(), ctx->tune.trav_refill_lanes, counts);
   else

@@ -63,11 +63,13 @@ struct tr_ctx {
   bool has_scene = false;
   trg::HostScene hs;
   trg::DScene dsc{};
-  trg::DevBuf d_nodes, d_slots, d_spheres, d_prims, d_tshade, d_mats, d_lights, d_roots;
+  trg::DevBuf d_nodes, d_nodes4, d_slots, d_spheres, d_prims, d_tshade, d_mats, d_lights, d_roots;
   trg::DevBuf d_rays, d_out0, d_out1, d_err;
   std::atomic<int> cancel{0};
   trg::RenderBuffers* rb = nullptr;
-  tr_tuning tune{20, 0, 16, 8};
+  tr_tuning tune{20, 0, 16, 8, 2};
+  size_t any4_nodes = 0;  // four-wide any-hit tree of the uploaded set (0: not available)
+  int any4_stack = 0;     // its traversal stack bound
   trg::GuideModel* guide = nullptr;
 };
 
@@ -77,6 +79,8 @@ tr_status set_err(tr_ctx* ctx, tr_status s, const std::string& msg);
 tr_status upload_device_tables(tr_ctx* ctx);
 // Grid of a persistent traversal kernel: SMs x resident blocks (tuned or as many as fit).
 int traversal_grid(const tr_ctx* ctx, const void* kernel);
+// Whether any-hit traversal walks the four-wide tree (tuning and scene allow it).
+inline bool any_wide(const tr_ctx* ctx) { return ctx->tune.any_node_width == 4 && ctx->dsc.nodes4 != nullptr; }
 void release_render(tr_ctx* ctx);
 void release_guide(tr_ctx* ctx);
 }  // namespace trg

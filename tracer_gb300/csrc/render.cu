@@ -367,12 +367,12 @@ __global__ void __launch_bounds__(128) k_extend(Launch P, int cur) {
   }
 }
 
-template <bool COUNT>
+template <bool COUNT, bool WIDE = false>
 __global__ void __launch_bounds__(128) k_shadow(Launch P) {
   ShadowJob job{P};
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.stats + 2, (unsigned long long)job.count());
   VisitCount vc;
-  persistent_traverse<true, COUNT>(P.sc, job, P.ctr + C_FSH, (int*)(P.ctr + C_ERR), vc, P.refill);
+  persistent_traverse<true, COUNT, WIDE>(P.sc, job, P.ctr + C_FSH, (int*)(P.ctr + C_ERR), vc, P.refill);
   if (COUNT) {
     count_add(P.stats + 6, vc.boxes);
     count_add(P.stats + 7, vc.prims);
@@ -1029,7 +1029,8 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   if (sms <= 0) sms = 1;
   const int grid = sms * ctx->tune.shade_blocks_per_sm, grid_init = sms * 8;
   const int grid_ext = traversal_grid(ctx, (const void*)k_extend<false>);
-  const int grid_sh = traversal_grid(ctx, (const void*)k_shadow<false>);
+  const bool wide = any_wide(ctx);
+  const int grid_sh = traversal_grid(ctx, wide ? (const void*)k_shadow<false, true> : (const void*)k_shadow<false>);
   P.refill = ctx->tune.trav_refill_lanes;
 
   ctx->cancel.store(0);
@@ -1105,7 +1106,9 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     mark();
     k_nee<MAT_DISNEY12><<<grid, 128, 0, st>>>(P);
     mark();
-    if (count) k_shadow<true><<<grid_sh, 128, 0, st>>>(P);
+    if (count && wide) k_shadow<true, true><<<grid_sh, 128, 0, st>>>(P);
+    else if (count) k_shadow<true><<<grid_sh, 128, 0, st>>>(P);
+    else if (wide) k_shadow<false, true><<<grid_sh, 128, 0, st>>>(P);
     else k_shadow<false><<<grid_sh, 128, 0, st>>>(P);
     mark();
     cudaError_t e = cudaGetLastError();
@@ -1387,7 +1390,8 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   if (sms <= 0) sms = 1;
   const int grid = sms * ctx->tune.shade_blocks_per_sm, grid_init = sms * 8;
   const int grid_ext = traversal_grid(ctx, (const void*)k_extend<false>);
-  const int grid_sh = traversal_grid(ctx, (const void*)k_shadow<false>);
+  const bool wide = any_wide(ctx);
+  const int grid_sh = traversal_grid(ctx, wide ? (const void*)k_shadow<false, true> : (const void*)k_shadow<false>);
   // the counters, statistics and film start at zero on every call; the
   // rest of the scratch is written before it is read
   NCHK(cudaMemsetAsync(d_rgbw, 0, (size_t)n * 16, st));
@@ -1409,7 +1413,8 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
     k_material<MAT_DISNEY12><<<grid, 128, 0, st>>>(P, cur);
     k_nee<MAT_PHONG><<<grid, 128, 0, st>>>(P);
     k_nee<MAT_DISNEY12><<<grid, 128, 0, st>>>(P);
-    k_shadow<false><<<grid_sh, 128, 0, st>>>(P);
+    if (wide) k_shadow<false, true><<<grid_sh, 128, 0, st>>>(P);
+    else k_shadow<false><<<grid_sh, 128, 0, st>>>(P);
   }
   NCHK(cudaGetLastError());
   NCHK(cudaStreamSynchronize(st));
@@ -1476,20 +1481,23 @@ extern "C" tr_status tr_autotune(tr_ctx* ctx, const tr_batch_job* jobs, uint32_t
   };
   // coordinate descent over the discrete settings
   static const int kBlocks[] = {0, 4, 6, 8}, kRefill[] = {12, 20, 28}, kShade[] = {8, 16, 32},
-                   kGraph[] = {0, 4, 8, 16};
+                   kGraph[] = {0, 4, 8, 16}, kWidth[] = {2, 4};
   tr_tuning cur = ctx->tune;
   double cur_ms = 0.0;
   tr_status s = time_once(cur, cur_ms);
   if (s != TR_OK) return s;
   for (int pass = 0; pass < 2; ++pass) {
     bool improved = false;
-    for (int dim = 0; dim < 4; ++dim) {
-      const int* vals = dim == 0 ? kBlocks : dim == 1 ? kRefill : dim == 2 ? kShade : kGraph;
-      const int nv = dim == 0 ? 4 : dim == 3 ? 4 : 3;
+    for (int dim = 0; dim < 5; ++dim) {
+      const int* vals = dim == 0 ? kBlocks : dim == 1 ? kRefill : dim == 2 ? kShade : dim == 3 ? kGraph : kWidth;
+      const int nv = dim == 0 || dim == 3 ? 4 : dim == 4 ? 2 : 3;
       for (int k = 0; k < nv; ++k) {
         tr_tuning t = cur;
-        int* field = dim == 0 ? &t.trav_blocks_per_sm
-                              : dim == 1 ? &t.trav_refill_lanes : dim == 2 ? &t.shade_blocks_per_sm : &t.graph_iterations;
+        int* field = dim == 0   ? &t.trav_blocks_per_sm
+                     : dim == 1 ? &t.trav_refill_lanes
+                     : dim == 2 ? &t.shade_blocks_per_sm
+                     : dim == 3 ? &t.graph_iterations
+                                : &t.any_node_width;
         if (*field == vals[k]) continue;
         *field = vals[k];
         double ms = 0.0;

@@ -7,6 +7,8 @@
 //    and the split axis, so a visit is four 16-byte vector loads and two box
 //    tests. Traversal keeps the reference's order and culling exactly (see
 //    traverse.cuh).
+//  * DNode4: the same tree collapsed to four-wide nodes for any-hit rays,
+//    whose result does not depend on the visiting order.
 //  * Slots: primitives in BVH leaf order, three float4 (48 bytes) each.
 //    Triangle: (A, id) (B-A, -1) (C-A, 0) -- B-A and C-A are the float
 //    differences the reference computes on every test. Sphere: (0, id)
@@ -40,6 +42,15 @@ struct alignas(16) DNode {
              // leaf's first slot; count == 0: ref is the child's DNode index.
 };
 static_assert(sizeof(DNode) == 64, "DNode must be 64 bytes");
+
+// Any-hit tree: the binary tree collapsed to up to four children per node
+// (128 bytes, boxes as structure of arrays). cnt > 0: ref is a leaf's first
+// slot; cnt == 0: ref is a DNode4 index; cnt < 0: no child.
+struct alignas(16) DNode4 {
+  float4 lox, loy, loz, hix, hiy, hiz;
+  int4 ref, cnt;
+};
+static_assert(sizeof(DNode4) == 128, "DNode4 must be 128 bytes");
 
 struct DSphere {
   float inv[16];  // world_to_local (row-major)
@@ -102,13 +113,14 @@ struct SceneRoot {
   int offset, count;
   int light_base, num_lights;  // the scene's lights in DScene::lights
   float lo[3], hi[3];          // root box
-  int pad;
+  int offset4;                 // kind 1: the root's DNode4 index
 };
 
 // The device tables of a scene set: every scene's nodes, slots, primitives,
 // materials and lights concatenated, indices already offset.
 struct DScene {
   const DNode* nodes;
+  const DNode4* nodes4;  // null when the any-hit tree is not available
   const float4* slots;
   const DSphere* spheres;
   const DPrim* prims;

@@ -172,9 +172,13 @@ struct Traversal {
 // the child's box entry t. Child references stay below 2^26 (checked on
 // upload). A stack in shared memory was slower: shared memory takes its
 // space from the L1 that serves the node and triangle reads.
-template <bool ANY, bool COUNT>
+constexpr int kStackBinary = 64;  // entries; the host rejects binary trees 60 or more levels deep
+constexpr int kStackWide = 96;    // entries; the host keeps four-wide trees whose stack bound fits
+
+template <bool ANY, bool COUNT, bool WIDE = false>
 struct TravLane {
-  static constexpr int kStack = 64;
+  static_assert(ANY || !WIDE, "closest-hit traversal keeps the binary order");
+  static constexpr int kStack = WIDE ? kStackWide : kStackBinary;
   f3 o, d, inv;
   bool n0, n1, n2;
   float t_min, t_max;
@@ -210,7 +214,7 @@ struct TravLane {
     float tmin;
     if (!box_pass(R.lo[0], R.lo[1], R.lo[2], R.hi[0], R.hi[1], R.hi[2], o, inv, n0, n1, n2, tmin) || !(tmin < t_max))
       return false;
-    cur = R.offset;
+    cur = WIDE && R.kind == 1 ? R.offset4 : R.offset;
     cnt = R.kind == 2 ? R.count : 0;
     return true;
   }
@@ -275,6 +279,47 @@ struct TravLane {
     return pop();
   }
 
+  // One visit of four-wide node `cur` (any-hit only): the children whose
+  // boxes pass are all taken, the nearest entered and the others pushed;
+  // returns false when done.
+  __device__ __forceinline__ bool interior4(const DScene& sc, int* err, VisitCount& vc) {
+    const float4* np = reinterpret_cast<const float4*>(sc.nodes4 + cur);
+    const float4 lx = ldg4(np), ly = ldg4(np + 1), lz = ldg4(np + 2);
+    const float4 hx = ldg4(np + 3), hy = ldg4(np + 4), hz = ldg4(np + 5);
+    const float4 rf = ldg4(np + 6), ct = ldg4(np + 7);
+    const int refs[4] = {__float_as_int(rf.x), __float_as_int(rf.y), __float_as_int(rf.z), __float_as_int(rf.w)};
+    const int cnts[4] = {__float_as_int(ct.x), __float_as_int(ct.y), __float_as_int(ct.z), __float_as_int(ct.w)};
+    float t[4];
+    bool hit[4];
+    hit[0] = cnts[0] >= 0 && box_pass(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, o, inv, n0, n1, n2, t[0]) && t[0] < t_max;
+    hit[1] = cnts[1] >= 0 && box_pass(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, o, inv, n0, n1, n2, t[1]) && t[1] < t_max;
+    hit[2] = cnts[2] >= 0 && box_pass(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, o, inv, n0, n1, n2, t[2]) && t[2] < t_max;
+    hit[3] = cnts[3] >= 0 && box_pass(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, o, inv, n0, n1, n2, t[3]) && t[3] < t_max;
+    if (COUNT) vc.boxes += (cnts[0] >= 0) + (cnts[1] >= 0) + (cnts[2] >= 0) + (cnts[3] >= 0);
+    int best = -1;
+    float bt = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      if (hit[i] && (best < 0 || t[i] < bt)) {
+        best = i;
+        bt = t[i];
+      }
+    if (best < 0) return pop();
+    const int npush = hit[0] + hit[1] + hit[2] + hit[3] - 1;
+    if (sp + npush > kStack) {
+      atomicOr(err, 1);
+      h.prim = -1;
+      occluded = false;
+      return false;
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      if (hit[i] && i != best) push(refs[i], cnts[i], t[i]);
+    cur = best == 0 ? refs[0] : best == 1 ? refs[1] : best == 2 ? refs[2] : refs[3];
+    cnt = best == 0 ? cnts[0] : best == 1 ? cnts[1] : best == 2 ? cnts[2] : cnts[3];
+    return true;
+  }
+
   // The primitives of leaf `cur`; returns false when done.
   __device__ __forceinline__ bool leaf(const DScene& sc, VisitCount& vc) {
     for (int i = 0; i < cnt; ++i) {
@@ -291,13 +336,13 @@ struct TravLane {
 // Job: unsigned count() const;
 //      void load(unsigned i, f3& o, f3& d, float& t_min, float& t_max, int& scene);
 //      void store(unsigned i, const Hit& h, float t_max, bool occluded).
-template <bool ANY, bool COUNT, class Job>
+template <bool ANY, bool COUNT, bool WIDE = false, class Job>
 __device__ __forceinline__ void persistent_traverse(const DScene& sc, Job& job, unsigned int* fetch, int* err,
                                                     VisitCount& vc, int refill) {
   const unsigned int n = job.count();
   const unsigned int lane = threadIdx.x & 31u;
   const unsigned int below = (1u << lane) - 1u;
-  TravLane<ANY, COUNT> L;
+  TravLane<ANY, COUNT, WIDE> L;
   unsigned int item = 0;
   bool live = false, exhausted = false;
   for (;;) {
@@ -328,7 +373,7 @@ __device__ __forceinline__ void persistent_traverse(const DScene& sc, Job& job, 
     for (;;) {
       while (__any_sync(0xffffffffu, live && L.cnt == 0)) {
         if (live && L.cnt == 0) {
-          live = L.interior(sc, err, vc);
+          live = WIDE ? L.interior4(sc, err, vc) : L.interior(sc, err, vc);
           if (!live) job.store(item, L.h, L.t_max, L.occluded);
         }
       }

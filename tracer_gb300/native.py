@@ -67,6 +67,8 @@ def lib() -> C.CDLL:
     L.tr_render.restype = st
     L.tr_render.argtypes = [vp, C.POINTER(TrCamera), C.POINTER(TrFilter), C.POINTER(TrRenderParams),
                             C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(TrStats)]
+    L.tr_any_tree_info.restype = st
+    L.tr_any_tree_info.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_int32)]
     L.tr_ctx_set_tuning.restype = st
     L.tr_ctx_set_tuning.argtypes = [vp, C.POINTER(TrTuning)]
     L.tr_ctx_get_tuning.restype = st
@@ -211,8 +213,11 @@ class GpuContext:
         return t
 
     def set_tuning(self, refill: int | None = None, trav_blocks_per_sm: int | None = None,
-                   shade_blocks_per_sm: int | None = None, graph_iterations: int | None = None) -> None:
+                   shade_blocks_per_sm: int | None = None, graph_iterations: int | None = None,
+                   any_node_width: int | None = None) -> None:
         t = self.tuning()
+        if any_node_width is not None:
+            t.any_node_width = any_node_width
         if graph_iterations is not None:
             t.graph_iterations = graph_iterations
         if refill is not None:
@@ -222,6 +227,12 @@ class GpuContext:
         if shade_blocks_per_sm is not None:
             t.shade_blocks_per_sm = shade_blocks_per_sm
         self._check(self.L.tr_ctx_set_tuning(self.h, C.byref(t)))
+
+    def any_tree_info(self) -> tuple[int, int]:
+        """(four-wide any-hit tree nodes, its traversal stack bound)."""
+        n, b = C.c_uint64(), C.c_int32()
+        self._check(self.L.tr_any_tree_info(self.h, C.byref(n), C.byref(b)))
+        return n.value, b.value
 
     # ---- path-guiding model
     GUIDE_PARAMS = 15592
