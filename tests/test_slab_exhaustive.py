@@ -1,6 +1,6 @@
 """The slab test's `tMax *= 1 + 0.0000001` (src/utility/geometry.hpp:848-859)
-is float(double(x) * 1.0000001); the kernels evaluate it with integer
-operations (trg::slab_scale in tracer_gb300/csrc/tr_math.cuh). This compiles
+is float(double(x) * 1.0000001); the kernels evaluate it with one fused
+multiply-add and a select (trg::slab_scale in tracer_gb300/csrc/tr_math.cuh). This compiles
 that same function for the host and compares it with the double expression
 on all 2^32 float bit patterns."""
 import os

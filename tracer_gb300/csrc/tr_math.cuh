@@ -98,36 +98,26 @@ TR_HD f3 xform_normal_inv(const float* inv, f3 n) {
 // The slab test's `tMax *= 1 + 0.0000001` (geometry.hpp:848,849,859) is
 // float(double(x) * 1.0000001). For a finite non-zero x the result is x
 // moved away from zero by 0, 1 or 2 units in the last place, as a function
-// of x's significand only; this evaluates it with integer operations.
-// Exhaustively checked against the double expression over all 2^32 inputs.
+// of x's significand m only: 2 for normal m >= 15000000 (except m = 2^24 - 1,
+// whose sum crosses into the next binade, where one unit of the larger
+// spacing wins), else 1; for subnormals 1 from m = 5000001 on, else 0.
+// One correctly rounded fma(x, c, x) with c = float(1e-7) (slightly above
+// 1e-7, below 1.5 / 14999999) adds m * c units and rounds to nearest: the
+// same unit counts for every m except the subnormal tie m = 5000000, whose
+// exact sum m + 0.5 rounds to even (m) in double but lies just above the
+// tie here. Zero, inf and nan pass unchanged, and the largest finite values
+// overflow to inf as the double expression does. Exhaustively checked
+// against the double expression over all 2^32 inputs.
 TR_HD float slab_scale(float x) {
 #if defined(__CUDA_ARCH__)
-  const uint32_t b = __float_as_uint(x);
+  const uint32_t mag = __float_as_uint(x) & 0x7fffffffu;
 #else
-  uint32_t b;
-  memcpy(&b, &x, 4);
+  uint32_t mag;
+  memcpy(&mag, &x, 4);
+  mag &= 0x7fffffffu;
 #endif
-  const uint32_t mag = b & 0x7fffffffu;
-  uint32_t k;
-  if (mag - 0x00800000u < 0x7f000000u) {
-    // normal: m = 2^23 + frac; m * 1e-7 rounds to 2 ulps from m = 15000000
-    // (frac = 6611392) on, except at m = 2^24 - 1 where the product
-    // crosses into the next binade and one ulp of the larger spacing wins
-    const uint32_t frac = b & 0x007fffffu;
-    k = (frac >= 6611392u && frac != 0x007fffffu) ? 2u : 1u;
-  } else if (mag == 0u || mag >= 0x7f800000u) {
-    return x;  // zero, inf, nan
-  } else {
-    k = mag >= 5000001u ? 1u : 0u;  // subnormal: m * 1e-7 reaches half an ulp
-  }
-  const uint32_t r = b + k;
-#if defined(__CUDA_ARCH__)
-  return __uint_as_float(r);
-#else
-  float f;
-  memcpy(&f, &r, 4);
-  return f;
-#endif
+  const float r = fmaf(x, 1e-7f, x);
+  return mag == 5000000u ? x : r;
 }
 
 }  // namespace trg

@@ -40,25 +40,26 @@ __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 
 // Slab test with the reference's arithmetic. Returns the t_max-independent
 // part ("pass"), and tmin for the "tMin < ray.t_max" part.
+// Written without branches (the reference's early returns become flags;
+// each conditional assignment is a select with the same NaN behaviour), so
+// the lanes of a warp never diverge inside a box test. tmin is meaningful
+// only when the test passes.
 __device__ __forceinline__ bool box_pass(float lx, float ly, float lz, float hx, float hy, float hz, f3 o,
                                          f3 inv, bool n0, bool n1, bool n2, float& tmin) {
   float tMin = ((n0 ? hx : lx) - o.x) * inv.x;
-  float tMax = ((n0 ? lx : hx) - o.x) * inv.x;
-  float tyMin = ((n1 ? hy : ly) - o.y) * inv.y;
-  float tyMax = ((n1 ? ly : hy) - o.y) * inv.y;
-  tMax = slab_scale(tMax);
-  tyMax = slab_scale(tyMax);
-  if (tMin > tyMax || tyMin > tMax) return false;
-  if (tyMin > tMin) tMin = tyMin;
-  if (tyMax < tMax) tMax = tyMax;
-  float tzMin = ((n2 ? hz : lz) - o.z) * inv.z;
-  float tzMax = ((n2 ? lz : hz) - o.z) * inv.z;
-  tzMax = slab_scale(tzMax);
-  if (tMin > tzMax || tzMin > tMax) return false;
-  if (tzMin > tMin) tMin = tzMin;
-  if (tzMax < tMax) tMax = tzMax;
+  float tMax = slab_scale(((n0 ? lx : hx) - o.x) * inv.x);
+  const float tyMin = ((n1 ? hy : ly) - o.y) * inv.y;
+  const float tyMax = slab_scale(((n1 ? ly : hy) - o.y) * inv.y);
+  const float tzMin = ((n2 ? hz : lz) - o.z) * inv.z;
+  const float tzMax = slab_scale(((n2 ? lz : hz) - o.z) * inv.z);
+  const bool miss_y = (tMin > tyMax) | (tyMin > tMax);
+  tMin = tyMin > tMin ? tyMin : tMin;
+  tMax = tyMax < tMax ? tyMax : tMax;
+  const bool miss_z = (tMin > tzMax) | (tzMin > tMax);
+  tMin = tzMin > tMin ? tzMin : tMin;
+  tMax = tzMax < tMax ? tzMax : tMax;
   tmin = tMin;
-  return tMax > 0.0f;
+  return !miss_y & !miss_z & (tMax > 0.0f);
 }
 
 // Möller-Trumbore as the reference writes it. A = s0.xyz, AB = s1.xyz, AC = s2.xyz.
@@ -182,9 +183,11 @@ struct TravLane {
   f3 o, d, inv;
   bool n0, n1, n2;
   float t_min, t_max;
-  int cur, cnt, sp;
+  int cur, cnt, sp;  // current node: cnt 0 interior, > 0 leaf, -1 none (stack ran dry, a leaf is postponed)
+  int pl, pc;        // postponed leaf (pc > 0), speculative traversal
+  float path_t;      // largest box entry t on the path taken since the last pop
   Hit h;
-  bool occluded;
+  bool occluded, failed;
   int2 st[kStack];      // (ref << 5 | min(count, 31), t bits)
   int big_cnt[kStack];  // counts of 31 or more, by stack index
 
@@ -203,7 +206,10 @@ struct TravLane {
     t_max = tmax_;
     h.prim = -1;
     occluded = false;
+    failed = false;
     sp = 0;
+    pc = 0;
+    path_t = -INFINITY;
     const SceneRoot& R = sc.roots[scene];
     if (R.kind == 0) return false;
     if (COUNT) ++vc.boxes;
@@ -228,6 +234,7 @@ struct TravLane {
         cur = e.x >> 5;
         cnt = e.x & 31;
         if (cnt == 31) cnt = big_cnt[sp];
+        path_t = __int_as_float(e.y);
         return true;
       }
     }
@@ -253,30 +260,65 @@ struct TravLane {
         atomicOr(err, 1);
         h.prim = -1;
         occluded = false;
+        failed = true;
         return false;
       }
       if (second_near) {
         push(lref, lcnt, tl);
         cur = rref;
         cnt = rcnt;
+        path_t = fmaxf(path_t, tr);
       } else {
         push(rref, rcnt, tr);
         cur = lref;
         cnt = lcnt;
+        path_t = fmaxf(path_t, tl);
       }
       return true;
     }
     if (hl) {
       cur = lref;
       cnt = lcnt;
+      path_t = fmaxf(path_t, tl);
       return true;
     }
     if (hr) {
       cur = rref;
       cnt = rcnt;
+      path_t = fmaxf(path_t, tr);
       return true;
     }
     return pop();
+  }
+
+  // Speculative traversal: the leaf just reached is postponed and the walk
+  // goes on from the stack (with the t_max from before the leaf's tests).
+  __device__ __forceinline__ void postpone() {
+    pl = cur;
+    pc = cnt;
+    if (!pop()) cnt = -1;
+  }
+
+  // Tests the postponed leaf; returns false when the traversal is over.
+  // Closest hit: the walk made since the postponement used a t_max that the
+  // leaf may have lowered. Every box entry t on the current path (path_t is
+  // their maximum, counted from the last pop) still below the new t_max means
+  // the reference, testing the leaf first, takes the same path and pushes
+  // the same entries; otherwise the reference would have culled a box on it:
+  // the path is dropped and the next entry popped (entries pushed along it
+  // are culled when popped, their boxes lying inside the dropped one).
+  __device__ __forceinline__ bool postponed_leaf(const DScene& sc, VisitCount& vc) {
+    for (int i = 0; i < pc; ++i) {
+      if (COUNT) ++vc.prims;
+      if (Traversal<ANY, COUNT>::test_slot(sc, pl + i, o, d, t_min, t_max, h)) {
+        occluded = true;
+        return false;
+      }
+    }
+    pc = 0;
+    if (!ANY && cnt >= 0 && !(path_t < t_max)) cnt = -1;
+    if (cnt < 0) return pop();
+    return true;
   }
 
   // One visit of four-wide node `cur` (any-hit only): the children whose
@@ -310,6 +352,7 @@ struct TravLane {
       atomicOr(err, 1);
       h.prim = -1;
       occluded = false;
+      failed = true;
       return false;
     }
 #pragma unroll
@@ -370,18 +413,47 @@ __device__ __forceinline__ void persistent_traverse(const DScene& sc, Job& job, 
       if (__all_sync(0xffffffffu, exhausted)) break;
       continue;
     }
-    for (;;) {
-      while (__any_sync(0xffffffffu, live && L.cnt == 0)) {
-        if (live && L.cnt == 0) {
-          live = WIDE ? L.interior4(sc, err, vc) : L.interior(sc, err, vc);
+    if (COUNT) {
+      // the reference's walk step for step (its box and primitive counts)
+      for (;;) {
+        while (__any_sync(0xffffffffu, live && L.cnt == 0)) {
+          if (live && L.cnt == 0) {
+            live = WIDE ? L.interior4(sc, err, vc) : L.interior(sc, err, vc);
+            if (!live) job.store(item, L.h, L.t_max, L.occluded);
+          }
+        }
+        if (live) {
+          live = L.leaf(sc, vc);
           if (!live) job.store(item, L.h, L.t_max, L.occluded);
         }
+        if (__popc(__ballot_sync(0xffffffffu, live)) < refill) break;
       }
-      if (live) {
-        live = L.leaf(sc, vc);
-        if (!live) job.store(item, L.h, L.t_max, L.occluded);
+    } else {
+      // speculative while-while: interior steps go on while some lane has
+      // not found a leaf; a lane holding a postponed leaf keeps walking
+      // (and waits at a second leaf); then the postponed leaves are tested
+      for (;;) {
+        for (;;) {
+          if (live && L.cnt > 0 && L.pc == 0) L.postpone();
+          if (!__any_sync(0xffffffffu, live && L.pc == 0)) break;
+          if (live && L.cnt == 0) {
+            const bool more = WIDE ? L.interior4(sc, err, vc) : L.interior(sc, err, vc);
+            if (!more) {
+              if (L.failed || L.pc == 0) {
+                live = false;
+                job.store(item, L.h, L.t_max, L.occluded);
+              } else {
+                L.cnt = -1;
+              }
+            }
+          }
+        }
+        if (live) {
+          live = L.postponed_leaf(sc, vc);
+          if (!live) job.store(item, L.h, L.t_max, L.occluded);
+        }
+        if (__popc(__ballot_sync(0xffffffffu, live)) < refill) break;
       }
-      if (__popc(__ballot_sync(0xffffffffu, live)) < refill) break;
     }
   }
 }
