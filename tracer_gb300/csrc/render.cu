@@ -585,7 +585,7 @@ __device__ __noinline__ BsdfSample sample_bsdf_shared(const Bsdf& b, f3 wo, floa
 // One path vertex on a material of kind KIND: the body of eval_pixel_li
 // from the BSDF sample to the next continuation ray
 // (src/renderer/path_trace_renderer.cpp:125-163).
-template <int KIND>
+template <int KIND, bool GUIDED = false>
 __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
   const int nxt = cur ^ 1;
   const unsigned int n = P.ctr[C_MAT + KIND];
@@ -622,8 +622,8 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
     bool guided_end = false, g_trace = false;
     float g_ps = 0.0f, g_nc = 0.0f, g_pb = 0.0f, g_cos = 0.0f;
     f3 g_fe = mk3(0.0f, 0.0f, 0.0f);
-    const bool gv =
-        KIND == MAT_PHONG && P.guide_alpha > 0.0f && bsdf.m->w_specular == 0.0f && !bsdf.fringe(is.wo);
+    const bool gv = GUIDED && KIND == MAT_PHONG && P.guide_alpha > 0.0f && bsdf.m->w_specular == 0.0f &&
+                    !bsdf.fringe(is.wo);
     if (gv) {
       const float sel = Pcg::next(st), g0 = Pcg::next(st), g1 = Pcg::next(st);
       guided_pick(P, bsdf, is, i, sel, g0, g1, bs, g_ps, g_nc);
@@ -641,23 +641,23 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
     const JobDev& J = job_of(P, slot);
     const float pos_mag = fabsf(is.pos.x) + fabsf(is.pos.y) + fabsf(is.pos.z);
     for (int l = 0; l < J.nl; ++l) {
-      const float lu = Pcg::next(st), lv = Pcg::next(st);
-      Pcg::next(st);
-      Pcg::next(st);
-      Pcg::next(st);
       const int item = slot * P.nl_max + l;
       // A vertex well behind a light's plane gets nothing from it:
       // k_nee's test dot(n, pos - light point) > 0 fails for every point
       // of the (planar) light. The margin covers the rounding of the
       // sampled point and of that dot product, so only items the exact test
-      // would reject are skipped here.
+      // would reject are skipped here (their five draws only advance the
+      // stream). Of a kept light's five draws the sample uses the first two.
       const DLight& lt = P.sc.lights[J.light_base + l];
       const float side = dot(lt.gz, is.pos - lt.A);
       const float tol = 1e-4f * (pos_mag + lt.extent);
       if (side < -tol) {
+        Pcg::skip<5>(st);
         P.SH[3 * (size_t)item + 2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         continue;
       }
+      const float lu = Pcg::next(st), lv = Pcg::next(st);
+      Pcg::skip<3>(st);
       P.NU[item] = make_float2(lu, lv);
       P.q_nee[KIND][append(P.ctr + C_NEE + KIND)] = item;
     }
@@ -1098,7 +1098,9 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
       if (gs != TR_OK) return gs;
     }
     mark();
-    k_material<MAT_PHONG><<<grid, 128, 0, st>>>(P, cur);
+    // the guided instantiation only when guiding (its code would slow the plain kernel)
+    if (P.guide_alpha > 0.0f) k_material<MAT_PHONG, true><<<grid, 128, 0, st>>>(P, cur);
+    else k_material<MAT_PHONG><<<grid, 128, 0, st>>>(P, cur);
     mark();
     k_material<MAT_DISNEY12><<<grid, 128, 0, st>>>(P, cur);
     mark();

@@ -32,6 +32,23 @@ struct Pcg {
     float u = __uint2float_rn(x) * 2.3283064365386963e-10f;
     return u >= 1.0f ? 0.99999994f : u;
   }
+  // Jump-ahead of the LCG state by n draws: s_n = mul_n * s + inc_n.
+  static __host__ __device__ constexpr unsigned long long jump_mul(int n) {
+    unsigned long long r = 1;
+    for (int i = 0; i < n; ++i) r *= kMul;
+    return r;
+  }
+  static __host__ __device__ constexpr unsigned long long jump_inc(int n) {
+    unsigned long long r = 0;
+    for (int i = 0; i < n; ++i) r = r * kMul + kInc;
+    return r;
+  }
+  // Advances the state past N draws whose values are not used.
+  template <int N>
+  static __device__ __forceinline__ void skip(unsigned long long& st) {
+    constexpr unsigned long long m = jump_mul(N), c = jump_inc(N);
+    st = st * m + c;
+  }
 };
 
 // ---------------------------------------------------------------- sampling

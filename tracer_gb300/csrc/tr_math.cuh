@@ -110,14 +110,14 @@ TR_HD f3 xform_normal_inv(const float* inv, f3 n) {
 // against the double expression over all 2^32 inputs.
 TR_HD float slab_scale(float x) {
 #if defined(__CUDA_ARCH__)
-  const uint32_t mag = __float_as_uint(x) & 0x7fffffffu;
+  const float tie = __uint_as_float(5000000u);  // the subnormal 5000000 * 2^-149
 #else
-  uint32_t mag;
-  memcpy(&mag, &x, 4);
-  mag &= 0x7fffffffu;
+  const uint32_t tb = 5000000u;
+  float tie;
+  memcpy(&tie, &tb, 4);
 #endif
   const float r = fmaf(x, 1e-7f, x);
-  return mag == 5000000u ? x : r;
+  return fabsf(x) == tie ? x : r;
 }
 
 }  // namespace trg
