@@ -124,7 +124,7 @@ GUIDE_BOX = {"occluded_room": ((-4.0, 0.0, -3.0), (4.0, 4.0, 3.0))}
 
 
 def convergence(ctx, name: str, size=(1024, 768), ref_spp=2048, pass_spp=8, max_spp=768, target=0.01,
-                alpha=0.5, train_steps=32, warm_steps=200, batch=65536, lr=1e-3):
+                alpha=0.25, train_steps=24, warm_steps=200, batch=65536, lr=1e-3, record_every=8):
     """Time for the plain and the guided GPU path tracer to reach `target`
     relMSE against a converged reference of the same scene. The reference
     is ref_spp samples per pixel accumulated in double. Each run adds
@@ -132,10 +132,12 @@ def convergence(ctx, name: str, size=(1024, 768), ref_spp=2048, pass_spp=8, max_
     double on the host, until the target or max_spp. The guided run starts
     from an untrained network: its first pass renders plainly (alpha 0) and
     records training data, every later pass samples Lambertian
-    continuations from the network's mixture with probability `alpha`,
-    records, and is followed by `train_steps` Adam steps on `batch` random
-    records (`warm_steps` more after the first pass; online training is
-    inside the timed region). If a training
+    continuations from the network's mixture with probability `alpha` and
+    traces a ray from the mixture alone for their direct light; every pass
+    records the paths of one sample in `record_every` per pixel and is
+    followed by `train_steps` Adam steps on `batch` random records
+    (`warm_steps` more after the first pass; online training is inside the
+    timed region). If a training
     loss is not finite the network is re-initialised and the next pass
     renders plainly (the plain path is the fallback)."""
     from tracer_gb300.abi import make_guide
@@ -162,8 +164,8 @@ def convergence(ctx, name: str, size=(1024, 768), ref_spp=2048, pass_spp=8, max_
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             if guided:
-                ctx.render_guided_dev(cam, filt, p, make_guide(use_alpha, *box, record=True), film.data_ptr(),
-                                      fp64=True)
+                ctx.render_guided_dev(cam, filt, p, make_guide(use_alpha, *box, record=record_every),
+                                      film.data_ptr(), fp64=True)
                 loss = ctx.guide_train_on_records(train_steps + (warm_steps if k == 0 else 0), batch, lr, seed=k)
                 if np.isfinite(loss):
                     use_alpha = alpha
@@ -188,7 +190,7 @@ def convergence(ctx, name: str, size=(1024, 768), ref_spp=2048, pass_spp=8, max_
                "relmse_curve_spp_s_relmse": curve}
         if guided:
             res.update({"alpha": alpha, "train_steps_per_pass": train_steps, "warm_steps": warm_steps, "batch": batch,
-                        "lr": lr,
+                        "lr": lr, "record_every": record_every,
                         "mean_loss_per_pass": losses[:8] + (["..."] if len(losses) > 9 else []) + losses[-1:]})
         return res
 

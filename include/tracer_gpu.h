@@ -366,20 +366,24 @@ tr_status tr_guide_train_step_dev(tr_ctx* ctx, const float* d_in, const float* d
 /* Guided rendering. No reference counterpart. tr_render_dev with the
  * continuation direction of every Lambertian vertex (Phong material without
  * specular lobe) drawn by one-sample MIS from the guide network's mixture
- * (probability alpha) and the BSDF (1 - alpha); the estimator keeps the
- * plain path's expectation. Next-event estimation is unchanged; Disney12
- * vertices keep BSDF sampling (the reference's Disney12 sampler draws from
- * a density other than its pdf, so a mixture pdf would change the image it
- * converges to). alpha = 0 renders exactly like tr_render_dev.
- * With record != 0 every traced continuation of the render also becomes a
- * training record (network input, direction, incident-radiance estimate /
- * pdf), up to max_records (0: 4M), for tr_guide_train_on_records. The
- * random stream differs from the plain renderer's when alpha > 0. */
+ * (probability alpha) and the BSDF (1 - alpha). At those vertices the
+ * direct lighting combines next-event estimation, the continuation and a
+ * ray drawn from the mixture alone by the power heuristic, estimating the
+ * same integral as the reference's light sample + BSDF-sampled MIS ray, so
+ * the image converges to the plain renderer's. Disney12 vertices keep the
+ * plain strategies (the reference's Disney12 sampler draws from a density
+ * other than its pdf, so a mixture pdf would change the image it converges
+ * to). alpha = 0 renders exactly like tr_render_dev.
+ * With record = n > 0 the continuations traced by the first of every n
+ * samples of a pixel (sample index % n == 0) also become training records
+ * (network input, direction, incident-radiance estimate / pdf), up to
+ * max_records (0: 4M), for tr_guide_train_on_records. The random stream
+ * differs from the plain renderer's when alpha > 0. */
 typedef struct tr_guide_params {
   float alpha;
   float box_lo[3]; /* scene box of the position inputs */
   float box_hi[3];
-  int32_t record;
+  int32_t record;   /* 0: no records; n > 0: record every n-th sample of a pixel */
   uint32_t max_records;
 } tr_guide_params;
 tr_status tr_render_guided_dev(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter,

@@ -224,12 +224,13 @@ def make_filter(radius=0.5, alpha=0.6) -> TrFilter:
     return f
 
 
-def make_guide(alpha: float, box_lo, box_hi, record: bool = False, max_records: int = 0) -> "TrGuideParams":
+def make_guide(alpha: float, box_lo, box_hi, record: bool | int = False, max_records: int = 0) -> "TrGuideParams":
+    """record: False/0 none, True/1 every sample, n the first of every n samples of a pixel."""
     g = TrGuideParams()
     g.alpha = alpha
     g.box_lo[:] = box_lo
     g.box_hi[:] = box_hi
-    g.record = 1 if record else 0
+    g.record = int(record)
     g.max_records = max_records
     return g
 

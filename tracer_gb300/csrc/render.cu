@@ -49,7 +49,8 @@ enum : int {
   F_MIS = 2,        // ...and it includes a MIS ray
   F_TERMINATE = 4,  // the path ends once that lighting is added
   F_REC = 8,        // the previous vertex wrote a guiding record awaiting its radiance
-  F_GCONT = 16,     // ...and its guided continuation is the MIS ray of its direct lighting
+  F_GCONT = 16,     // ...and its guided continuation is an MIS strategy of its direct lighting
+  F_GX = 32,        // ...and so is a ray drawn from the mixture alone (in the MIS slot)
 };
 
 enum : int {  // counter slots
@@ -69,6 +70,7 @@ struct RenderBuffers {
   DevBuf P0, P1, P2, P3, P4, rng, M0, M1, M2, HC, HM, SC, NU, SH, acc, q_ext, q_act, q_mat, q_nee, q_sh, ctr,
       stats;
   DevBuf VR, NV, gfeat, gout, tb;  // path guiding: vertex records, network rows, training records
+  DevBuf GX;                        // path guiding: the continuation's MIS data (4 float4 per slot)
   DevBuf jobs;                      // JobDev table of the current render
   unsigned int tb_count = 0, tb_cap = 0;  // training records of the last guided render
   unsigned int* h_active = nullptr;  // pinned: live-slot count per check
@@ -112,10 +114,11 @@ struct Launch {
   // path guiding (alpha > 0: sample Lambertian continuations from the network's mixture;
   // record: keep training records)
   float guide_alpha;
-  int guide_record, maxd;
+  int guide_record, maxd;  // record: 0 off, n > 0 every n-th sample of a pixel
   float gbox_lo[3], gbox_scale[3];
   float* gfeat;  // network inputs, one row per entry of q_mat[0]
   float* gout;   // decoded mixtures (kMixFloats per row), same rows
+  float4* GX;    // 4 per slot: continuation o|p_g, d|p_bsdf, f_eval|p_plain, (nc, |cos|, p_mix, p_g of the mixture ray)
   float4* VR;    // 4 per (slot, vertex): features 0-3 | features 4-6, pdf | direction, throughput | radiance
   int* NV;       // records of the slot's current sample
   float *tb_in, *tb_dir, *tb_w;
@@ -414,24 +417,46 @@ __device__ __forceinline__ f3 direct_integrand(f3 fe, float pb, f3 fs, float ps,
   return muls(fe, mis_w(lpdf, pb)) + muls(fs, mis_w(ps, lpdf));
 }
 
-// A guided vertex's continuation doubles as its MIS ray: the emission it
-// reaches, weighted against next-event estimation by the guided density
-// (the other half of k_nee_guided). `hit` is the continuation's hit.
-__device__ f3 guided_mis_contribution(const Launch& P, int slot, float4 hit) {
+// Emission reached by a ray of a guided vertex that is one of its MIS
+// strategies for direct lighting, weighted by the power heuristic against
+// next-event estimation and the other guided strategy (the other half of
+// guided_nee_factor). The ray's data: origin o, direction d, its own density
+// pr, the other strategy's density there po (0: two strategies), the BSDF's
+// eval fe and pdf pb, the plain sampler's density ps, the normal correction
+// nc and |cos|. `hit` is the ray's hit.
+__device__ f3 guided_strategy_emission(const Launch& P, int slot, float4 hit, f3 o, f3 d, float pr, float po, f3 fe,
+                                       float pb, float ps, float nc, float cosv) {
   const int pid = __float_as_int(hit.x);
   if (pid < 0) return mk3(0.0f, 0.0f, 0.0f);
-  const DPrim& pr = P.sc.prims[pid];
-  if (!pr.emissive) return mk3(0.0f, 0.0f, 0.0f);
-  const float4 m0 = P.M0[slot], m1 = P.M1[slot], m2 = P.M2[slot];
-  const f3 o = mk3(m0.x, m0.y, m0.z), d = mk3(m1.x, m1.y, m1.z);
-  const f3 gz = P.sc.tshade[pr.shape].gz;
+  const DPrim& pr_ = P.sc.prims[pid];
+  if (!pr_.emissive) return mk3(0.0f, 0.0f, 0.0f);
+  const f3 gz = P.sc.tshade[pr_.shape].gz;
   if (!(dot(gz, -d) > 0.0f)) return mk3(0.0f, 0.0f, 0.0f);
-  const float4 sc0 = P.SC[7 * (size_t)slot], sc6 = P.SC[7 * (size_t)slot + 6];
-  const float lpdf = light_pdf_at(pr.area, o, o + scale(d, hit.y), gz);
-  const float pg = m0.w, pb = m1.w, ps = m2.w;
-  const f3 fs = ps > 0.0f ? muls(P.sc.mats[__float_as_int(sc0.w)].diffuse_coef, sc6.z) : mk3(0.0f, 0.0f, 0.0f);
-  const f3 g = direct_integrand(mk3(m2.x, m2.y, m2.z), pb, fs, ps, lpdf);
-  return muls(mulc(pr.emission, g), sc6.w * mis_w(pg, lpdf) / pg);
+  const float lpdf = light_pdf_at(pr_.area, o, o + scale(d, hit.y), gz);
+  const int mat = __float_as_int(P.SC[7 * (size_t)slot].w);
+  const f3 fs = ps > 0.0f ? muls(P.sc.mats[mat].diffuse_coef, nc) : mk3(0.0f, 0.0f, 0.0f);
+  const f3 g = direct_integrand(fe, pb, fs, ps, lpdf);
+  const float w = pr * pr / (pr * pr + lpdf * lpdf + po * po);
+  return muls(mulc(pr_.emission, g), cosv * w / pr);
+}
+
+// The strategy in the MIS slot (M0-M2, normal correction and |cos| in the
+// shading context): the continuation of a vertex whose path ends there, or
+// the mixture ray (whose continuation-density is in GX).
+__device__ f3 guided_mis_slot_emission(const Launch& P, int slot, bool mixture_ray) {
+  const float4 m0 = P.M0[slot], m1 = P.M1[slot], m2 = P.M2[slot], sc6 = P.SC[7 * (size_t)slot + 6];
+  const float po = mixture_ray ? P.GX[4 * (size_t)slot + 3].w : 0.0f;
+  return guided_strategy_emission(P, slot, P.HM[slot], mk3(m0.x, m0.y, m0.z), mk3(m1.x, m1.y, m1.z), m0.w, po,
+                                  mk3(m2.x, m2.y, m2.z), m1.w, m2.w, sc6.z, sc6.w);
+}
+
+// The continuation of a vertex whose path goes on (data in GX, hit in HC),
+// against next-event estimation and the mixture ray.
+__device__ f3 guided_continuation_emission(const Launch& P, int slot) {
+  const float4* g = P.GX + 4 * (size_t)slot;
+  const float4 a = g[0], b = g[1], c = g[2], e = g[3];
+  return guided_strategy_emission(P, slot, P.HC[slot], mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), a.w, e.z,
+                                  mk3(c.x, c.y, c.z), b.w, c.w, e.x, e.y);
 }
 
 // Emission the continuation of a recorded vertex reaches (full, unweighted):
@@ -467,9 +492,13 @@ __global__ void __launch_bounds__(128) k_logic(Launch P, int cur) {
         if (c.w != 0.0f) direct = direct + mk3(c.x, c.y, c.z);
       }
       if (flags & F_MIS) direct = direct + mulc(mk3(p4.x, p4.y, p4.z), mis_contribution(P, slot));
-      if (flags & F_GCONT)
-        direct = direct + mulc(mk3(p4.x, p4.y, p4.z),
-                               guided_mis_contribution(P, slot, (flags & F_TERMINATE) ? P.HM[slot] : P.HC[slot]));
+      if (flags & (F_GCONT | F_GX)) {
+        f3 ge = mk3(0.0f, 0.0f, 0.0f);
+        if ((flags & F_GCONT) && (flags & F_TERMINATE)) ge = guided_mis_slot_emission(P, slot, false);
+        if ((flags & F_GCONT) && !(flags & F_TERMINATE)) ge = guided_continuation_emission(P, slot);
+        if (flags & F_GX) ge = ge + guided_mis_slot_emission(P, slot, true);
+        direct = direct + mulc(mk3(p4.x, p4.y, p4.z), ge);
+      }
       L = L + direct;
       if (flags & F_REC) {
         // the record's baseline leaves out the continuation's own emission,
@@ -540,11 +569,13 @@ __device__ __forceinline__ float lambert_plain_pdf(const Bsdf& bsdf, f3 wo, f3 w
 
 // Replaces the plain sample `bs` by the one-sample MIS choice: with
 // probability alpha (sel < alpha) a mixture direction, else the plain
-// sample itself (which may be invalid: then nothing is returned). ps and nc
-// receive the plain sampler's density at the chosen direction and the
-// normal correction of its integrand (0 where that density is 0).
+// sample itself (which may be invalid: then nothing is returned). ps, nc
+// and pm receive the plain sampler's density at the chosen direction, the
+// normal correction of its integrand (0 where that density is 0) and the
+// mixture's density.
 __device__ __noinline__ void guided_pick(const Launch& P, const Bsdf& bsdf, const Isect& is, unsigned int row,
-                                         float sel, float g0, float g1, BsdfSample& bs, float& ps, float& nc) {
+                                         float sel, float g0, float g1, BsdfSample& bs, float& ps, float& nc,
+                                         float& pm) {
   const Mixture mx{P.gout + (size_t)row * kMixFloats};
   f3 wi;
   if (sel < P.guide_alpha) {
@@ -555,23 +586,55 @@ __device__ __noinline__ void guided_pick(const Launch& P, const Bsdf& bsdf, cons
   }
   ps = lambert_plain_pdf(bsdf, is.wo, wi);
   nc = ps > 0.0f ? normal_correct(bsdf.g, bsdf.s, wi) : 0.0f;
+  pm = mx.pdf(wi);
   bs.wi = wi;
   bs.f = muls(bsdf.m->diffuse_coef, nc);
-  bs.pdf = P.guide_alpha * mx.pdf(wi) + (1.0f - P.guide_alpha) * ps;
+  bs.pdf = P.guide_alpha * pm + (1.0f - P.guide_alpha) * ps;
+}
+
+// A guided vertex's ray for one MIS strategy of its direct lighting: its
+// direction, the densities of the strategies there and what the direct
+// integrand needs (the BSDF's eval and pdf, the plain sampler's density,
+// the normal correction, |cos|).
+struct GuidedRay {
+  f3 wi, fe;
+  float p_mix, p_g, pb, ps, nc, cosv;
+  bool trace;  // the direct integrand can be non-zero along it
+};
+
+// The mixture ray: a direction drawn from the mixture alone (lobe u, v, w).
+__device__ __noinline__ void guided_mixture_ray(const Launch& P, const Bsdf& bsdf, const Isect& is, unsigned int row,
+                                                float u, float v, float w, GuidedRay& r) {
+  const Mixture mx{P.gout + (size_t)row * kMixFloats};
+  r.wi = normalize(mx.sample(u, v, w));
+  r.p_mix = mx.pdf(r.wi);
+  r.ps = lambert_plain_pdf(bsdf, is.wo, r.wi);
+  r.nc = r.ps > 0.0f ? normal_correct(bsdf.g, bsdf.s, r.wi) : 0.0f;
+  r.p_g = P.guide_alpha * r.p_mix + (1.0f - P.guide_alpha) * r.ps;
+  const f3 wc = normalize(r.wi);
+  r.fe = bsdf.phong_eval_agg(wc, is.wo);
+  r.pb = bsdf.phong_pdf_agg(wc, is.wo);
+  r.cosv = abs_cos(is.g.z, wc);
+  r.trace = r.p_mix >= kEps && (r.ps > 0.0f || !black(r.fe));
 }
 
 // Next-event estimation at a guided vertex: the light sample of direction
-// wl, weighted against the guided continuation (density pg at wl) instead
-// of the plain BSDF sample. With guided_mis_contribution it estimates the
+// wl, weighted against the guided continuation (density p_g at wl) and,
+// when the vertex also traced a mixture ray, the mixture (p_mix), instead
+// of the plain BSDF sample. With guided_strategy_emission it estimates the
 // same direct-lighting integral as the reference's pair of strategies.
 // Returns that integrand times |cos| per unit emission, times the weight.
-__device__ __noinline__ f3 guided_nee_factor(const Launch& P, const Bsdf& bsdf, f3 wo, f3 wl, int row, float lpdf) {
+__device__ __noinline__ f3 guided_nee_factor(const Launch& P, const Bsdf& bsdf, f3 wo, f3 wl, int row, bool three,
+                                             float lpdf) {
   const Mixture mx{P.gout + (size_t)row * kMixFloats};
   const float ps = lambert_plain_pdf(bsdf, wo, wl);
   const f3 fs = ps > 0.0f ? muls(bsdf.m->diffuse_coef, normal_correct(bsdf.g, bsdf.s, wl)) : mk3(0.0f, 0.0f, 0.0f);
   const f3 g = direct_integrand(bsdf.phong_eval_agg(wl, wo), bsdf.phong_pdf_agg(wl, wo), fs, ps, lpdf);
-  const float pg = P.guide_alpha * mx.pdf(wl) + (1.0f - P.guide_alpha) * ps;
-  return muls(g, abs_cos(wl, bsdf.g.z) * mis_w(lpdf, pg));
+  const float pm = mx.pdf(wl);
+  const float pg = P.guide_alpha * pm + (1.0f - P.guide_alpha) * ps;
+  const float po = three ? pm : 0.0f;
+  const float w = lpdf * lpdf / (lpdf * lpdf + pg * pg + po * po);
+  return muls(g, abs_cos(wl, bsdf.g.z) * w);
 }
 
 // The BSDF sample, shared out of line by the two call sites of k_material
@@ -616,17 +679,17 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
     // Guided continuation. The plain sample above still decides, as in the
     // reference, whether this vertex gets direct lighting at all; a guided
     // direction without contribution only ends the path after it.
-    // At a guided vertex the continuation is also the MIS ray of the
+    // At a guided vertex the continuation is also an MIS strategy of the
     // direct lighting (traced even when the path ends here, as long as the
     // integrand can be non-zero along it), so emission it reaches counts.
     bool guided_end = false, g_trace = false;
-    float g_ps = 0.0f, g_nc = 0.0f, g_pb = 0.0f, g_cos = 0.0f;
+    float g_ps = 0.0f, g_nc = 0.0f, g_pb = 0.0f, g_cos = 0.0f, g_pm = 0.0f;
     f3 g_fe = mk3(0.0f, 0.0f, 0.0f);
     const bool gv = GUIDED && KIND == MAT_PHONG && P.guide_alpha > 0.0f && bsdf.m->w_specular == 0.0f &&
                     !bsdf.fringe(is.wo);
     if (gv) {
       const float sel = Pcg::next(st), g0 = Pcg::next(st), g1 = Pcg::next(st);
-      guided_pick(P, bsdf, is, i, sel, g0, g1, bs, g_ps, g_nc);
+      guided_pick(P, bsdf, is, i, sel, g0, g1, bs, g_ps, g_nc, g_pm);
       guided_end = black(bs.f) || bs.pdf < kEps;
       if (bs.pdf >= kEps) {
         const f3 wc = normalize(normalize(bs.wi));
@@ -668,18 +731,14 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
     sc[3] = make_float4(is.g.y.z, is.g.z.x, is.g.z.y, is.g.z.z);
     sc[4] = make_float4(is.s.x.x, is.s.x.y, is.s.x.z, is.s.y.x);
     sc[5] = make_float4(is.s.y.y, is.s.y.z, is.s.z.x, is.s.z.y);
-    sc[6] = make_float4(is.s.z.z, __int_as_float(gv ? (int)i : -1), g_nc, g_cos);
-    // MIS BSDF ray (sample_bsdf, src/renderer/direct_illumination.cpp:144-155)
+    // MIS BSDF ray (sample_bsdf, src/renderer/direct_illumination.cpp:144-155);
+    // a guided vertex draws a direction from the mixture alone instead
     int flags = F_PENDING;
+    GuidedRay gx;
+    gx.trace = false;
     if (gv) {
-      if (g_trace) {
-        const f3 mo = is.eps_offset(bs.wi);
-        const f3 md = normalize(normalize(bs.wi));
-        P.M0[slot] = make_float4(mo.x, mo.y, mo.z, bs.pdf);
-        P.M1[slot] = make_float4(md.x, md.y, md.z, g_pb);
-        P.M2[slot] = make_float4(g_fe.x, g_fe.y, g_fe.z, g_ps);
-        flags |= F_GCONT;
-      }
+      const float x0 = Pcg::next(st), x1 = Pcg::next(st), x2 = Pcg::next(st);
+      guided_mixture_ray(P, bsdf, is, i, x0, x1, x2, gx);
     } else {
       const float v0 = Pcg::next(st), v1 = Pcg::next(st), v2 = Pcg::next(st);
       const BsdfSample ms = sample_bsdf_shared<KIND>(bsdf, is.wo, v0, v1, v2);
@@ -709,15 +768,53 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
         }
       }
     }
+    // The guided strategies of the direct lighting. A path that ends here
+    // traces its continuation in the MIS slot for its emission only (next-
+    // event estimation and the continuation); a path that goes on traces
+    // the continuation (hit in HC, its data in GX) and the mixture ray in
+    // the MIS slot (three strategies; bit 30 of the shading context's row
+    // tells k_nee).
+    int gcode = gv ? (int)i : -1;
+    float sc6z = 0.0f, sc6w = 0.0f;
+    if (gv && g_trace) {
+      const f3 mo = is.eps_offset(bs.wi);
+      const f3 md = normalize(normalize(bs.wi));
+      flags |= F_GCONT;
+      if (term) {
+        P.M0[slot] = make_float4(mo.x, mo.y, mo.z, bs.pdf);
+        P.M1[slot] = make_float4(md.x, md.y, md.z, g_pb);
+        P.M2[slot] = make_float4(g_fe.x, g_fe.y, g_fe.z, g_ps);
+        sc6z = g_nc;
+        sc6w = g_cos;
+        P.q_ext[nxt][append(P.ctr + C_EXT + nxt)] = 2 * slot + 1;
+      } else {
+        gcode |= 1 << 30;
+        float4* gxr = P.GX + 4 * (size_t)slot;
+        gxr[0] = make_float4(mo.x, mo.y, mo.z, bs.pdf);
+        gxr[1] = make_float4(md.x, md.y, md.z, g_pb);
+        gxr[2] = make_float4(g_fe.x, g_fe.y, g_fe.z, g_ps);
+        gxr[3] = make_float4(g_nc, g_cos, g_pm, gx.p_g);
+        if (gx.trace) {
+          const f3 xo = is.eps_offset(gx.wi);
+          const f3 xd = normalize(gx.wi);
+          P.M0[slot] = make_float4(xo.x, xo.y, xo.z, gx.p_mix);
+          P.M1[slot] = make_float4(xd.x, xd.y, xd.z, gx.pb);
+          P.M2[slot] = make_float4(gx.fe.x, gx.fe.y, gx.fe.z, gx.ps);
+          sc6z = gx.nc;
+          sc6w = gx.cosv;
+          flags |= F_GX;
+          P.q_ext[nxt][append(P.ctr + C_EXT + nxt)] = 2 * slot + 1;
+        }
+      }
+    }
+    sc[6] = make_float4(is.s.z.z, __int_as_float(gcode), sc6z, sc6w);
     if (term) {
       flags |= F_TERMINATE;
       P.P0[slot] = make_float4(p0.x, p0.y, p0.z, __int_as_float(flags));
-      // a guided continuation still traced for its emission only
-      if (flags & F_GCONT) P.q_ext[nxt][append(P.ctr + C_EXT + nxt)] = 2 * slot + 1;
     } else {
       const f3 no = is.eps_offset(bs.wi);
       const f3 nd = normalize(normalize(bs.wi));
-      if (P.guide_record) {
+      if (P.guide_record && __float_as_int(p2.w) % P.guide_record == 0) {
         const int nv = P.NV[slot];
         if (nv < P.maxd) {
           float f[7];
@@ -782,12 +879,13 @@ __global__ void __launch_bounds__(128) k_nee(Launch P) {
         const float dist = dist_minus_eps(len2f(to_light), too_close);
         if (!too_close) {
           to_light = normalize(to_light);
-          const int grow = __float_as_int(g.y);  // network row of a guided vertex, else -1
+          const int gcode = __float_as_int(g.y);  // guided vertex: network row (bit 30: three strategies), else -1
+          const int grow = gcode < 0 ? -1 : (gcode & 0x3fffffff);
           f3 cc = mk3(0.0f, 0.0f, 0.0f);          // contribution before the shadow test
           bool trace = false;
           const float4 p4 = P.P4[slot];
           if (KIND == MAT_PHONG && grow >= 0) {
-            const f3 fw = guided_nee_factor(P, bsdf, wo, to_light, grow, lpdf);
+            const f3 fw = guided_nee_factor(P, bsdf, wo, to_light, grow, (gcode >> 30) & 1, lpdf);
             trace = !black(fw);
             cc = mulc(mk3(p4.x, p4.y, p4.z), divs(mulc(lt.emission, fw), lpdf));
           } else {
@@ -820,7 +918,8 @@ void release_render(tr_ctx* ctx) {
   RenderBuffers* rb = ctx->rb;
   for (DevBuf* b : {&rb->P0, &rb->P1, &rb->P2, &rb->P3, &rb->P4, &rb->rng, &rb->M0, &rb->M1, &rb->M2, &rb->HC,
                     &rb->HM, &rb->SC, &rb->NU, &rb->SH, &rb->acc, &rb->q_ext, &rb->q_act, &rb->q_mat, &rb->q_nee,
-                    &rb->q_sh, &rb->ctr, &rb->stats, &rb->VR, &rb->NV, &rb->gfeat, &rb->gout, &rb->tb, &rb->jobs})
+                    &rb->q_sh, &rb->ctr, &rb->stats, &rb->VR, &rb->NV, &rb->gfeat, &rb->gout, &rb->tb, &rb->jobs,
+                    &rb->GX})
     b->release();
   if (rb->h_active) cudaFreeHost(rb->h_active);
   for (cudaEvent_t e : rb->ev_pool) cudaEventDestroy(e);
@@ -999,16 +1098,19 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
       P.gbox_scale[k] = 2.0f / (gp->box_hi[k] - gp->box_lo[k]);
     }
     P.guide_alpha = gp->alpha;
-    P.guide_record = gp->record ? 1 : 0;
+    if (gp->record < 0) return set_err(ctx, TR_ERR_ARG, "guide record stride must be >= 0");
+    P.guide_record = gp->record;
     P.maxd = std::max(jobs[0].prm.max_depth, 1);
     const size_t N = (size_t)n;
     const unsigned int cap = gp->max_records ? gp->max_records : (4u << 20);
     cudaError_t e = cudaSuccess;
     if (P.guide_alpha > 0.0f) {
-      if ((e = rb->gfeat.reserve(N * 7 * 4)) != cudaSuccess || (e = rb->gout.reserve(N * kMixFloats * 4)) != cudaSuccess)
+      if ((e = rb->gfeat.reserve(N * 7 * 4)) != cudaSuccess || (e = rb->gout.reserve(N * kMixFloats * 4)) != cudaSuccess ||
+          (e = rb->GX.reserve(N * 4 * sizeof(float4))) != cudaSuccess)
         return cuda_fail(ctx, e, "guide inference buffers");
       P.gfeat = rb->gfeat.as<float>();
       P.gout = rb->gout.as<float>();
+      P.GX = rb->GX.as<float4>();
     }
     if (P.guide_record) {
       if ((e = rb->VR.reserve(N * P.maxd * 64)) != cudaSuccess || (e = rb->NV.reserve(N * 4)) != cudaSuccess ||
