@@ -215,6 +215,22 @@ typedef struct tr_tuning {
 tr_status tr_ctx_set_tuning(tr_ctx* ctx, const tr_tuning* t);
 tr_status tr_ctx_get_tuning(const tr_ctx* ctx, tr_tuning* t);
 
+/* BVH builder of later uploads. TR_BVH_REFERENCE (default): the reference's
+ * binned-SAH tree built on the host (bvh.cpp:191-306; parallel over the
+ * scenes of a set), so hits are the reference's bit for bit.
+ * TR_BVH_DEVICE: a tree built on the GPU by parallel locally-ordered
+ * clustering of Morton-sorted primitives (one primitive per leaf) -- for
+ * uploads where the host build would dominate (large batches). Its tree
+ * differs from the reference's, so closest hits may differ where two
+ * primitives are hit at the same distance, and images agree statistically,
+ * not bit for bit; tr_bvh_export/upload and the four-wide any-hit tree are
+ * not available for it. No reference counterpart. */
+enum { TR_BVH_REFERENCE = 0, TR_BVH_DEVICE = 1 };
+tr_status tr_ctx_set_bvh_builder(tr_ctx* ctx, int32_t builder);
+/* The uploaded set's tree: the builder that made it and its depth (levels
+ * below the deepest root; uploads of trees 92 or more levels deep fail). */
+tr_status tr_bvh_stats(const tr_ctx* ctx, int32_t* builder, int32_t* depth);
+
 /* Builds the scene on the device: primitive tables, materials, lights and the
  * binned-SAH BVH. Replaces create_bvh_accel + BVHAccel::build +
  * create_general_scene (src/accelerator/bvh.cpp:78-105,315;

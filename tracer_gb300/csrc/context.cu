@@ -167,6 +167,7 @@ int collapse4(const std::vector<DNode>& dn, int root, std::vector<DNode4>& out, 
 // Builds DNodes + slots from hs.nodes/hs.order and uploads every table.
 tr_status upload_device_tables(tr_ctx* ctx) {
   HostScene& hs = ctx->hs;
+  if (hs.device_bvh) return upload_device_built(ctx);
   const size_t nn = hs.nodes.size();
   // validate the flattened tree: children strictly after their parent, leaf
   // ranges inside the slot array, depth bounded by the traversal stack
@@ -194,7 +195,8 @@ tr_status upload_device_tables(tr_ctx* ctx) {
     }
     maxd = std::max(maxd, depth[i]);
   }
-  if (maxd >= 60) return set_err(ctx, TR_ERR_UNSUPPORTED, "bvh deeper than the device traversal stack (60)");
+  if (maxd >= kMaxDepth)
+    return set_err(ctx, TR_ERR_UNSUPPORTED, "bvh deeper than the device traversal stack (" + std::to_string(kMaxDepth) + ")");
   if (hs.order.size() >= (1u << 26) || (size_t)ninterior >= (1u << 26))
     return set_err(ctx, TR_ERR_UNSUPPORTED, "more than 2^26 primitives or interior nodes in one upload");
   hs.depth = maxd;
@@ -460,7 +462,7 @@ tr_status tr_synchronize(tr_ctx* ctx) {
 }
 
 // Host tables and reference BVH of one scene description.
-static tr_status build_host_scene(tr_ctx* ctx, const tr_scene_desc* d, HostScene& hs) {
+static tr_status build_host_scene(tr_ctx* ctx, const tr_scene_desc* d, HostScene& hs, bool device_bvh) {
   if (d->num_vertices && (!d->positions || !d->normals || !d->uvs))
     return set_err(ctx, TR_ERR_ARG, "vertex arrays missing");
   if (d->num_triangles && !d->indices) return set_err(ctx, TR_ERR_ARG, "indices missing");
@@ -597,9 +599,17 @@ static tr_status build_host_scene(tr_ctx* ctx, const tr_scene_desc* d, HostScene
     L.prim = p;
     hs.lights.push_back(L);
   }
-  BvhResult bvh = build_reference_bvh(lo.data(), hi.data(), np, d->max_leaf_prims);
-  hs.nodes = std::move(bvh.nodes);
-  hs.order = std::move(bvh.order);
+  if (device_bvh) {  // the tree is built on the device at upload
+    hs.device_bvh = true;
+    hs.blo = std::move(lo);
+    hs.bhi = std::move(hi);
+  } else {
+    BvhResult bvh = build_reference_bvh(lo.data(), hi.data(), np, d->max_leaf_prims);
+    hs.nodes = std::move(bvh.nodes);
+    hs.order = std::move(bvh.order);
+  }
+  hs.scene_prim = {0};
+  hs.scene_leaf = {(int)d->max_leaf_prims};
   hs.scene_node = {0};
   hs.scene_light = {0};
   hs.scene_nlight = {(uint32_t)hs.lights.size()};
@@ -615,6 +625,11 @@ static void append_scene(HostScene& dst, const HostScene& src) {
   dst.scene_node.push_back(node_base);
   dst.scene_light.push_back(light_base);
   dst.scene_nlight.push_back((uint32_t)src.lights.size());
+  dst.scene_prim.push_back(prim_base);
+  dst.scene_leaf.insert(dst.scene_leaf.end(), src.scene_leaf.begin(), src.scene_leaf.end());
+  dst.device_bvh = src.device_bvh;
+  dst.blo.insert(dst.blo.end(), src.blo.begin(), src.blo.end());
+  dst.bhi.insert(dst.bhi.end(), src.bhi.begin(), src.bhi.end());
   for (tr_bvh_node32 n : src.nodes) {
     n.offset += (int32_t)(n.count > 0 ? order_base : node_base);
     dst.nodes.push_back(n);
@@ -646,6 +661,7 @@ tr_status tr_scene_set_upload(tr_ctx* ctx, const tr_scene_desc* descs, uint32_t 
   if (!ctx || !descs || n == 0 || n > 65536) return TR_ERR_ARG;
   TR_CUDA(ctx, cudaSetDevice(ctx->device));
   ctx->has_scene = false;
+  const bool device_bvh = ctx->bvh_builder == TR_BVH_DEVICE;
   // each scene's tables and tree on its own host thread
   std::vector<HostScene> parts(n);
   std::vector<tr_status> st(n, TR_OK);
@@ -655,7 +671,7 @@ tr_status tr_scene_set_upload(tr_ctx* ctx, const tr_scene_desc* descs, uint32_t 
   auto work = [&]() {
     tr_ctx scratch;  // per-thread error sink
     for (uint32_t k; (k = next.fetch_add(1)) < n;) {
-      st[k] = build_host_scene(&scratch, descs + k, parts[k]);
+      st[k] = build_host_scene(&scratch, descs + k, parts[k], device_bvh);
       if (st[k] != TR_OK) msg[k] = scratch.err;
     }
   };
@@ -678,9 +694,24 @@ tr_status tr_scene_set_upload(tr_ctx* ctx, const tr_scene_desc* descs, uint32_t 
   return upload_device_tables(ctx);
 }
 
+tr_status tr_ctx_set_bvh_builder(tr_ctx* ctx, int32_t builder) {
+  if (!ctx || (builder != TR_BVH_REFERENCE && builder != TR_BVH_DEVICE)) return TR_ERR_ARG;
+  ctx->bvh_builder = builder;
+  return TR_OK;
+}
+
+tr_status tr_bvh_stats(const tr_ctx* ctx, int32_t* builder, int32_t* depth) {
+  if (!ctx || !builder || !depth) return TR_ERR_ARG;
+  if (!ctx->has_scene) return TR_ERR_STATE;
+  *builder = ctx->hs.device_bvh ? TR_BVH_DEVICE : TR_BVH_REFERENCE;
+  *depth = ctx->hs.depth;
+  return TR_OK;
+}
+
 tr_status tr_bvh_info(tr_ctx* ctx, size_t* num_nodes, size_t* num_prims) {
   if (!ctx || !num_nodes || !num_prims) return TR_ERR_ARG;
   if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
+  if (ctx->hs.device_bvh) return set_err(ctx, TR_ERR_STATE, "the BVH was built on the device (TR_BVH_DEVICE)");
   *num_nodes = ctx->hs.nodes.size();
   *num_prims = ctx->hs.order.size();
   return TR_OK;
@@ -696,6 +727,7 @@ tr_status tr_any_tree_info(const tr_ctx* ctx, uint64_t* num_nodes4, int32_t* sta
 tr_status tr_bvh_export(tr_ctx* ctx, tr_bvh_node32* nodes, uint32_t* prim_order) {
   if (!ctx || !nodes || !prim_order) return TR_ERR_ARG;
   if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
+  if (ctx->hs.device_bvh) return set_err(ctx, TR_ERR_STATE, "the BVH was built on the device (TR_BVH_DEVICE)");
   std::memcpy(nodes, ctx->hs.nodes.data(), ctx->hs.nodes.size() * sizeof(tr_bvh_node32));
   std::memcpy(prim_order, ctx->hs.order.data(), ctx->hs.order.size() * sizeof(uint32_t));
   return TR_OK;
@@ -705,6 +737,7 @@ tr_status tr_bvh_upload(tr_ctx* ctx, const tr_bvh_node32* nodes, size_t num_node
                         size_t num_prims) {
   if (!ctx || (num_nodes && !nodes) || (num_prims && !prim_order)) return TR_ERR_ARG;
   if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
+  if (ctx->hs.device_bvh) return set_err(ctx, TR_ERR_STATE, "the BVH was built on the device (TR_BVH_DEVICE)");
   if (ctx->hs.scene_node.size() != 1) return set_err(ctx, TR_ERR_STATE, "tr_bvh_upload replaces the tree of a single scene");
   TR_CUDA(ctx, cudaSetDevice(ctx->device));
   std::vector<tr_bvh_node32> keep_nodes = ctx->hs.nodes;

@@ -50,6 +50,11 @@ struct HostScene {
   int depth = 0;
   // scene set: first node, first light and light count of every scene
   std::vector<uint32_t> scene_node, scene_light, scene_nlight;
+  std::vector<uint32_t> scene_prim;  // first primitive of every scene
+  std::vector<int> scene_leaf;       // max_leaf_prims of every scene
+  // TR_BVH_DEVICE: no host tree; the primitive bounds (3 floats each) for the device build
+  bool device_bvh = false;
+  std::vector<float> blo, bhi;
 };
 
 struct RenderBuffers;  // render.cu
@@ -68,6 +73,7 @@ struct tr_ctx {
   std::atomic<int> cancel{0};
   trg::RenderBuffers* rb = nullptr;
   tr_tuning tune{20, 0, 16, 8, 2};
+  int bvh_builder = TR_BVH_REFERENCE;
   size_t any4_nodes = 0;  // four-wide any-hit tree of the uploaded set (0: not available)
   int any4_stack = 0;     // its traversal stack bound
   trg::GuideModel* guide = nullptr;
@@ -77,6 +83,7 @@ namespace trg {
 tr_status cuda_fail(tr_ctx* ctx, cudaError_t e, const char* what);
 tr_status set_err(tr_ctx* ctx, tr_status s, const std::string& msg);
 tr_status upload_device_tables(tr_ctx* ctx);
+tr_status upload_device_built(tr_ctx* ctx);  // bvh_gpu.cu: the TR_BVH_DEVICE path
 // Grid of a persistent traversal kernel: SMs x resident blocks (tuned or as many as fit).
 int traversal_grid(const tr_ctx* ctx, const void* kernel);
 // Whether any-hit traversal walks the four-wide tree (tuning and scene allow it).

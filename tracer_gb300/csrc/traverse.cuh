@@ -173,8 +173,9 @@ struct Traversal {
 // the child's box entry t. Child references stay below 2^26 (checked on
 // upload). A stack in shared memory was slower: shared memory takes its
 // space from the L1 that serves the node and triangle reads.
-constexpr int kStackBinary = 64;  // entries; the host rejects binary trees 60 or more levels deep
-constexpr int kStackWide = 96;    // entries; the host keeps four-wide trees whose stack bound fits
+constexpr int kStackBinary = 96;               // entries (a binary walk pushes at most one per level)
+constexpr int kMaxDepth = kStackBinary - 4;      // the host rejects binary trees this many levels deep
+constexpr int kStackWide = 96;                   // entries; the host keeps four-wide trees whose stack bound fits
 
 template <bool ANY, bool COUNT, bool WIDE = false>
 struct TravLane {

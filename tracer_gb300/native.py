@@ -67,6 +67,10 @@ def lib() -> C.CDLL:
     L.tr_render.restype = st
     L.tr_render.argtypes = [vp, C.POINTER(TrCamera), C.POINTER(TrFilter), C.POINTER(TrRenderParams),
                             C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(TrStats)]
+    L.tr_ctx_set_bvh_builder.restype = st
+    L.tr_ctx_set_bvh_builder.argtypes = [vp, C.c_int32]
+    L.tr_bvh_stats.restype = st
+    L.tr_bvh_stats.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     L.tr_any_tree_info.restype = st
     L.tr_any_tree_info.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_int32)]
     L.tr_ctx_set_tuning.restype = st
@@ -227,6 +231,16 @@ class GpuContext:
         if shade_blocks_per_sm is not None:
             t.shade_blocks_per_sm = shade_blocks_per_sm
         self._check(self.L.tr_ctx_set_tuning(self.h, C.byref(t)))
+
+    def set_bvh_builder(self, device: bool) -> None:
+        """Builder of later uploads: the reference's host tree (False) or the device tree (True)."""
+        self._check(self.L.tr_ctx_set_bvh_builder(self.h, 1 if device else 0))
+
+    def bvh_stats(self) -> tuple[int, int]:
+        """(builder of the uploaded tree: 0 reference, 1 device; its depth)."""
+        b, d = C.c_int32(), C.c_int32()
+        self._check(self.L.tr_bvh_stats(self.h, C.byref(b), C.byref(d)))
+        return b.value, d.value
 
     def any_tree_info(self) -> tuple[int, int]:
         """(four-wide any-hit tree nodes, its traversal stack bound)."""
