@@ -506,6 +506,22 @@ def run_batch(args):
     stage_ms = dict(zip(STAGE_NAMES, staged.stage_ms))
     dom = max((k for k in STAGE_NAMES if k != "reset"), key=lambda k: stage_ms[k])
     tris = int(sum(len(it[0].indices) for it in items))
+    # the same set with the device BVH builder (outside the timed region):
+    # upload time and rendering rate over its trees
+    ctx.set_bvh_builder(True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ctx.upload_set([it[0] for it in items])
+    torch.cuda.synchronize()
+    dev_upload_s = time.perf_counter() - t0
+    _, dev_depth = ctx.bvh_stats()
+    ctx.render_batch_dev(jobs)
+    barrier()
+    t0 = time.perf_counter()
+    dev_samples = sum(ctx.render_batch_dev(jobs).samples for _ in range(args.steps))
+    barrier()
+    dev_rate = dev_samples / (time.perf_counter() - t0) / 1e6
+    ctx.set_bvh_builder(False)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -518,8 +534,14 @@ def run_batch(args):
         "gpu_launches": int(sum(1 + 7 * s.iterations for s in stats)),
         "autotune": {"trav_refill_lanes": tuning.trav_refill_lanes, "trav_blocks_per_sm": tuning.trav_blocks_per_sm,
                      "shade_blocks_per_sm": tuning.shade_blocks_per_sm, "graph_iterations": tuning.graph_iterations,
-                     "probe_ms": round(probe_ms, 2), "tune_s": round(tune_s, 1)},
+                     "any_node_width": tuning.any_node_width, "probe_ms": round(probe_ms, 2),
+                     "tune_s": round(tune_s, 1)},
         "setup_s": {"generate": round(gen_s, 1), "upload_and_bvh": round(upload_s, 1)},
+        "device_bvh": {"upload_and_bvh_s": round(dev_upload_s, 2), "msamples_per_s": round(dev_rate, 1),
+                       "depth": dev_depth,
+                       "note": "tr_ctx_set_bvh_builder(TR_BVH_DEVICE): trees built on the GPU (PLOC); "
+                               "host-timed render calls; images agree with the reference trees' up to "
+                               "equal-distance ties"},
         "stage_ms": {k: round(v, 3) for k, v in stage_ms.items()}, "dominant_kernel": KERNEL_NAMES[dom],
         "clocks": clocks.summary(c0, c1),
     }
