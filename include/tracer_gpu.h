@@ -343,6 +343,32 @@ tr_status tr_render_batch_dev(tr_ctx* ctx, const tr_batch_job* jobs, uint32_t n,
 tr_status tr_autotune(tr_ctx* ctx, const tr_batch_job* jobs, uint32_t n, int32_t probe_spp,
                       tr_tuning* best, double* best_ms);
 
+/* Output path. No GPU counterpart in the reference, whose output runs on
+ * the host. The *_dev calls are ordered on the context's stream
+ * (tr_synchronize or tr_ctx_stream before reading their results).
+ *  - tr_film_resolve_dev: Film::write_render_target (src/core/render.hpp:105-115):
+ *    d_rgb (3 floats per pixel) = film sum / weight where the weight is
+ *    positive, else 0; the film of tr_render_dev / tr_render_batch_dev
+ *    (exactly one of d_rgbw, d_rgbw64; 16-byte aligned).
+ *  - tr_aces_tone_map_dev: create_aces_tone_mapper(exposure)->process
+ *    (src/post_processor/aces.cpp) in place; a negative exposure becomes 1.
+ *  - tr_gamma_correct_dev: create_gamma_corrector(gamma)->process
+ *    (src/post_processor/gamma.cpp), pow per channel; gamma <= 0 becomes 1.
+ *  - tr_to_rgb8_dev: the 8-bit image of the demo driver (src/main.hpp:171-178),
+ *    clamp(int(pow(c, inv_gamma) * 255), 0, 255) per channel, the float to
+ *    int conversion truncating and saturating (NaN: 0).
+ *  - tr_to_rgbe_dev: Radiance RGBE bytes, 4 per pixel (4-byte aligned).
+ *  - tr_write_png / tr_write_hdr: write_image_to_png / write_image_to_hdr
+ *    (src/utility/image_file.cpp:14-24) from host buffers: an 8-bit RGB PNG
+ *    (rows top to bottom) and a Radiance HDR file. Host only. */
+tr_status tr_film_resolve_dev(tr_ctx* ctx, const float* d_rgbw, const double* d_rgbw64, size_t pixels, float* d_rgb);
+tr_status tr_aces_tone_map_dev(tr_ctx* ctx, float* d_rgb, size_t pixels, float exposure);
+tr_status tr_gamma_correct_dev(tr_ctx* ctx, float* d_rgb, size_t pixels, float gamma);
+tr_status tr_to_rgb8_dev(tr_ctx* ctx, const float* d_rgb, size_t pixels, float inv_gamma, uint8_t* d_rgb8);
+tr_status tr_to_rgbe_dev(tr_ctx* ctx, const float* d_rgb, size_t pixels, uint8_t* d_rgbe);
+tr_status tr_write_png(const char* path, const uint8_t* rgb8, uint32_t width, uint32_t height);
+tr_status tr_write_hdr(const char* path, const uint8_t* rgbe, uint32_t width, uint32_t height);
+
 /* Asks a running tr_render on this context to stop after its current
  * wavefront iteration; that call then returns TR_ERR_CANCELLED. Thread-safe. */
 tr_status tr_cancel(tr_ctx* ctx);

@@ -251,3 +251,55 @@ def pcg_uniform(kind, seed, n):
     out = np.zeros(n, np.float32)
     getattr(lib, pre + "pcg_uniform")(seed, _p(out, C.c_float), n)
     return out
+
+
+# ---- output path: film resolve, post-processors, 8-bit and RGBE encodings
+def _post_lib(kind):
+    lib = _load(kind)
+    f32p, u8p, sz = C.POINTER(C.c_float), C.POINTER(C.c_uint8), C.c_size_t
+    if kind == "port":
+        lib.orc_post_resolve.argtypes = [f32p, sz, f32p]
+        lib.orc_post_aces.argtypes = [f32p, sz, C.c_float]
+        lib.orc_post_gamma.argtypes = [f32p, sz, C.c_float]
+        lib.orc_post_rgb8.argtypes = [f32p, sz, C.c_float, u8p]
+        lib.orc_post_rgbe.argtypes = [f32p, sz, u8p]
+    else:
+        lib.ref_post_process.argtypes = [f32p, C.c_int, C.c_int, C.c_int, C.c_float]
+    return lib
+
+
+def post_resolve(film: np.ndarray) -> np.ndarray:
+    """(H, W, 4) float32 film sums -> (H, W, 3) image (Film::write_render_target)."""
+    film = np.ascontiguousarray(film, np.float32)
+    out = np.zeros(film.shape[:-1] + (3,), np.float32)
+    _post_lib("port").orc_post_resolve(_p(film, C.c_float), film.size // 4, _p(out, C.c_float))
+    return out
+
+
+def post_process(kind: str, rgb: np.ndarray, which: str, param: float) -> np.ndarray:
+    """ACES tone mapper ("aces", exposure) or gamma corrector ("gamma", gamma)
+    on an (H, W, 3) image: the restatement ("port") or the reference's own
+    post-processors ("reference")."""
+    img = np.array(rgb, np.float32, copy=True, order="C")
+    lib = _post_lib(kind)
+    if kind == "port":
+        fn = lib.orc_post_aces if which == "aces" else lib.orc_post_gamma
+        fn(_p(img, C.c_float), img.size, param)
+    else:
+        h, w = img.shape[:2]
+        lib.ref_post_process(_p(img, C.c_float), w, h, 0 if which == "aces" else 1, param)
+    return img
+
+
+def post_rgb8(rgb: np.ndarray, inv_gamma: float = 1.0 / 2.2) -> np.ndarray:
+    img = np.ascontiguousarray(rgb, np.float32)
+    out = np.zeros(img.shape, np.uint8)
+    _post_lib("port").orc_post_rgb8(_p(img, C.c_float), img.size, inv_gamma, _p(out, C.c_uint8))
+    return out
+
+
+def post_rgbe(rgb: np.ndarray) -> np.ndarray:
+    img = np.ascontiguousarray(rgb, np.float32)
+    out = np.zeros(img.shape[:-1] + (4,), np.uint8)
+    _post_lib("port").orc_post_rgbe(_p(img, C.c_float), img.size // 3, _p(out, C.c_uint8))
+    return out

@@ -336,3 +336,32 @@ size_t ref_bvh_export(void* h, tr_bvh_node32* out, uint32_t* order) {
   return n;
 }
 }
+
+#include "core/post_processor.hpp"
+#include "factory/post_processor.hpp"
+
+extern "C" {
+// The reference's post-processors on a w x h RGB float image, in place:
+// kind 0 create_aces_tone_mapper(param), kind 1 create_gamma_corrector(param)
+// (src/post_processor/aces.cpp, src/post_processor/gamma.cpp), applied by
+// PostProcessor::process to a RenderTarget holding the image.
+void ref_post_process(float* rgb, int w, int h, int kind, float param) {
+  RenderTarget rt;
+  rt.color = Image2D<Spectrum>(w, h);
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      const float* p = rgb + 3 * ((size_t)y * w + x);
+      rt.color.at(x, y) = Spectrum(p[0], p[1], p[2]);
+    }
+  RC<PostProcessor> pp = kind == 0 ? create_aces_tone_mapper(param) : create_gamma_corrector(param);
+  pp->process(rt);
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      float* p = rgb + 3 * ((size_t)y * w + x);
+      const Spectrum& c = rt.color.at(x, y);
+      p[0] = c.r;
+      p[1] = c.g;
+      p[2] = c.b;
+    }
+}
+}

@@ -1601,4 +1601,65 @@ void orc_pcg_uniform(int seed, float* out, size_t n) {
   for (size_t i = 0; i < n; ++i) out[i] = s.u();
 }
 
+
+// ---- output path (test restatement)
+// Film::write_render_target (src/core/render.hpp:105-115): sum / weight per
+// channel where the weight is positive, else 0. film: r, g, b, w per pixel.
+void orc_post_resolve(const float* film, size_t n, float* rgb) {
+  for (size_t i = 0; i < n; ++i) {
+    const float w = film[4 * i + 3];
+    for (int c = 0; c < 3; ++c) rgb[3 * i + c] = w > 0.0f ? film[4 * i + c] / w : 0.0f;
+  }
+}
+// ACESToneMapper::process (src/post_processor/aces.cpp:9-43): per channel
+// clamp(x (2.51 x + 0.03) / (x (2.43 x + 0.59) + 0.14), 0, 1), x = c * exposure;
+// a negative exposure is replaced by 1.
+void orc_post_aces(float* rgb, size_t n3, float exposure) {
+  if (exposure < 0.0f) exposure = 1.0f;
+  for (size_t i = 0; i < n3; ++i) {
+    const float x = rgb[i] * exposure;
+    const float v = (x * (2.51f * x + 0.03f)) / (x * (2.43f * x + 0.59f) + 0.14f);
+    rgb[i] = v < 0.0f ? 0.0f : (1.0f < v ? 1.0f : v);
+  }
+}
+// GammaCorrector::process (src/post_processor/gamma.cpp:26-38): pow(c, gamma)
+// per channel; gamma <= 0 is replaced by 1.
+void orc_post_gamma(float* rgb, size_t n3, float gamma) {
+  if (gamma <= 0.0f) gamma = 1.0f;
+  for (size_t i = 0; i < n3; ++i) rgb[i] = std::pow(rgb[i], gamma);
+}
+// The demo driver's 8-bit image (src/main.hpp:171-178): clamp<int>(pow(c,
+// inv_gamma) * 255, 0, 255), the float converted to int by truncation
+// (NaN and out-of-range values: 0 below, 255 above, as a saturating
+// conversion gives).
+void orc_post_rgb8(const float* rgb, size_t n3, float inv_gamma, uint8_t* out) {
+  for (size_t i = 0; i < n3; ++i) {
+    const float v = std::pow(rgb[i], inv_gamma) * 255;
+    int iv = v != v ? 0 : (v >= 2147483647.0f ? 2147483647 : (v <= -2147483648.0f ? (-2147483647 - 1) : (int)v));
+    out[i] = (uint8_t)(iv < 0 ? 0 : (iv > 255 ? 255 : iv));
+  }
+}
+// Radiance RGBE (G. Ward, "Real Pixels", Graphics Gems II): the largest
+// channel v = m 2^e with m in [0.5, 1) sets the shared exponent e + 128 and
+// each channel becomes floor(c * m * 256 / v); v < 1e-32 encodes as zeros.
+void orc_post_rgbe(const float* rgb, size_t n, uint8_t* out) {
+  for (size_t i = 0; i < n; ++i) {
+    const float r = rgb[3 * i], g = rgb[3 * i + 1], b = rgb[3 * i + 2];
+    float v = r;
+    if (g > v) v = g;
+    if (b > v) v = b;
+    uint8_t* o = out + 4 * i;
+    if (!(v >= 1e-32f)) {
+      o[0] = o[1] = o[2] = o[3] = 0;
+      continue;
+    }
+    int e;
+    const float m = std::frexp(v, &e);
+    const float s = m * 256.0f / v;
+    const float c[3] = {r * s, g * s, b * s};
+    for (int k = 0; k < 3; ++k) o[k] = (uint8_t)(c[k] > 0.0f ? (c[k] < 255.0f ? (int)c[k] : 255) : 0);
+    o[3] = (uint8_t)(e + 128);
+  }
+}
+
 }  // extern "C"

@@ -71,6 +71,13 @@ def lib() -> C.CDLL:
     L.tr_ctx_set_bvh_builder.argtypes = [vp, C.c_int32]
     L.tr_bvh_stats.restype = st
     L.tr_bvh_stats.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    for name, args in (("tr_film_resolve_dev", [vp, vp, vp, sz, vp]), ("tr_aces_tone_map_dev", [vp, vp, sz, C.c_float]),
+                       ("tr_gamma_correct_dev", [vp, vp, sz, C.c_float]),
+                       ("tr_to_rgb8_dev", [vp, vp, sz, C.c_float, vp]), ("tr_to_rgbe_dev", [vp, vp, sz, vp]),
+                       ("tr_write_png", [C.c_char_p, vp, C.c_uint32, C.c_uint32]),
+                       ("tr_write_hdr", [C.c_char_p, vp, C.c_uint32, C.c_uint32])):
+        getattr(L, name).restype = st
+        getattr(L, name).argtypes = args
     L.tr_any_tree_info.restype = st
     L.tr_any_tree_info.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_int32)]
     L.tr_ctx_set_tuning.restype = st
@@ -242,6 +249,22 @@ class GpuContext:
         self._check(self.L.tr_bvh_stats(self.h, C.byref(b), C.byref(d)))
         return b.value, d.value
 
+    # ---- output path (device buffers, ordered on the context's stream)
+    def film_resolve_dev(self, d_film: int, pixels: int, d_rgb: int, fp64: bool = False) -> None:
+        self._check(self.L.tr_film_resolve_dev(self.h, None if fp64 else d_film, d_film if fp64 else None, pixels, d_rgb))
+
+    def aces_tone_map_dev(self, d_rgb: int, pixels: int, exposure: float) -> None:
+        self._check(self.L.tr_aces_tone_map_dev(self.h, d_rgb, pixels, exposure))
+
+    def gamma_correct_dev(self, d_rgb: int, pixels: int, gamma: float) -> None:
+        self._check(self.L.tr_gamma_correct_dev(self.h, d_rgb, pixels, gamma))
+
+    def to_rgb8_dev(self, d_rgb: int, pixels: int, d_out: int, inv_gamma: float = 1.0 / 2.2) -> None:
+        self._check(self.L.tr_to_rgb8_dev(self.h, d_rgb, pixels, inv_gamma, d_out))
+
+    def to_rgbe_dev(self, d_rgb: int, pixels: int, d_out: int) -> None:
+        self._check(self.L.tr_to_rgbe_dev(self.h, d_rgb, pixels, d_out))
+
     def any_tree_info(self) -> tuple[int, int]:
         """(four-wide any-hit tree nodes, its traversal stack bound)."""
         n, b = C.c_uint64(), C.c_int32()
@@ -350,3 +373,19 @@ def make_ray(o, d, t_min=0.0, t_max=3.4028234663852886e38) -> TrRay:
     if s != TR_OK:
         raise TracerError(s, "tr_make_ray")
     return r
+
+
+def write_png(path: str, rgb8: np.ndarray) -> None:
+    """(H, W, 3) uint8 image to an 8-bit RGB PNG (tr_write_png; host only)."""
+    a = np.ascontiguousarray(rgb8, np.uint8)
+    s = lib().tr_write_png(str(path).encode(), a.ctypes.data, a.shape[1], a.shape[0])
+    if s != TR_OK:
+        raise TracerError(s, f"tr_write_png failed for {path}")
+
+
+def write_hdr(path: str, rgbe: np.ndarray) -> None:
+    """(H, W, 4) uint8 RGBE image to a Radiance HDR file (tr_write_hdr; host only)."""
+    a = np.ascontiguousarray(rgbe, np.uint8)
+    s = lib().tr_write_hdr(str(path).encode(), a.ctypes.data, a.shape[1], a.shape[0])
+    if s != TR_OK:
+        raise TracerError(s, f"tr_write_hdr failed for {path}")
