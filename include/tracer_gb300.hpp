@@ -146,6 +146,8 @@ RC<Material> create_disney_brdf(RC<const Texture2D> base_color, RC<const Texture
                                 RC<const Texture2D> anisotropic, RC<const Texture2D> sheen,
                                 RC<const Texture2D> sheen_tint, RC<const Texture2D> clearcoat,
                                 RC<const Texture2D> clearcoat_gloss);
+// create_glass (src/factory/material.hpp:13-17, src/material/glass.cpp:145-154)
+RC<Material> create_glass(RC<const Texture2D> map_kr, RC<const Texture2D> map_kt, RC<const Texture2D> map_ior);
 
 class Medium {
  public:

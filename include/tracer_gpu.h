@@ -57,7 +57,7 @@ typedef struct tr_bvh_node32 {
   uint8_t pad;
 } tr_bvh_node32;
 
-enum { TR_MAT_PHONG = 0, TR_MAT_DISNEY12 = 1 };
+enum { TR_MAT_PHONG = 0, TR_MAT_DISNEY12 = 1, TR_MAT_GLASS = 2 };
 
 /* Material record. Phong is create_phong_material(ka, kd, ks, ns)
  * (src/factory/material.hpp:19-24, src/material/phong.cpp:29-70); Disney12 is
@@ -72,6 +72,10 @@ typedef struct tr_material {
   float base_color[3];
   float subsurface, metallic, specular, specular_tint, roughness;
   float anisotropic, sheen, sheen_tint, clearcoat, clearcoat_gloss;
+  /* Glass: create_glass(kr, kt, ior) (src/material/glass.cpp:117-154), a
+   * delta BSDF: Fresnel-weighted specular reflection (colour kr) or
+   * refraction (colour sqrt(kt)) at index of refraction ior. */
+  float kr[3], kt[3], ior;
 } tr_material;
 
 /* Flat scene description. It records what the reference factory calls build

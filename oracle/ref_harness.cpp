@@ -100,6 +100,8 @@ void* ref_scene_create(const tr_scene_desc* d) {
     const tr_material& m = d->materials[i];
     if (m.kind == TR_MAT_PHONG) {
       s->materials.push_back(create_phong_material(ctex3(m.ka), ctex3(m.kd), ctex3(m.ks), ctex(m.ns)));
+    } else if (m.kind == TR_MAT_GLASS) {
+      s->materials.push_back(create_glass(ctex3(m.kr), ctex3(m.kt), ctex(m.ior)));
     } else {
       s->materials.push_back(create_disney_brdf(
           ctex3(m.base_color), ctex(m.subsurface), ctex(m.metallic), ctex(m.specular),

@@ -235,6 +235,10 @@ struct Mat {
   Sp base;
   real subsurface, metallic, specular_s, specular_tint, roughness, anisotropic, sheen, sheen_tint,
       clearcoat, clearcoat_gloss;
+  // Glass::shading (material/glass.cpp:117-140): reflect colour, sqrt of the
+  // transmit colour, index of refraction
+  Sp kr, kt_sqrt;
+  real ior;
 };
 struct Prim {
   int kind;  // 0 triangle, 1 sphere
@@ -756,8 +760,34 @@ struct BSDFSample {
   V3 wi;
   Sp f;
   real pdf = 0;
+  bool delta = false;
   bool valid() const { return pdf > 0 && !f.black(); }  // core/bsdf.hpp:21-23
 };
+
+// dielectric_fresnel (utility/reflection.hpp:16-40)
+inline real dielectric_fresnel(real eta_i, real eta_o, real cos_theta_i) {
+  if (cos_theta_i < 0) {
+    std::swap(eta_i, eta_o);
+    cos_theta_i = -cos_theta_i;
+  }
+  const real sin_theta_i = std::sqrt(std::max(real(0), 1 - cos_theta_i * cos_theta_i));
+  const real sin_theta_t = eta_o / eta_i * sin_theta_i;
+  if (sin_theta_t >= 1) return 1;
+  const real cos_theta_t = std::sqrt(std::max(real(0), 1 - sin_theta_t * sin_theta_t));
+  const real para = (eta_i * cos_theta_i - eta_o * cos_theta_t) / (eta_i * cos_theta_i + eta_o * cos_theta_t);
+  const real perp = (eta_o * cos_theta_i - eta_i * cos_theta_t) / (eta_o * cos_theta_i + eta_i * cos_theta_t);
+  return real(0.5) * (para * para + perp * perp);
+}
+// refract_dir (utility/reflection.hpp:43-51); false: total internal reflection
+inline bool refract_dir(V3 lwo, V3 n, real eta, V3& out) {
+  const real cos_theta_i = std::abs(lwo.z);
+  const real sin_theta_i_2 = std::max(real(0), 1 - cos_theta_i * cos_theta_i);
+  const real sin_theta_t_2 = eta * eta * sin_theta_i_2;
+  if (sin_theta_t_2 >= 1) return false;
+  const real cos_theta_t = std::sqrt(1 - sin_theta_t_2);
+  out = mulf(n, eta * cos_theta_i - cos_theta_t) - mulf(lwo, eta);
+  return true;
+}
 
 // microfacet helpers (material/utility/microfacet.cpp:7-134, microfacet.hpp:10-14)
 inline real sqr(real x) { return x * x; }
@@ -1038,9 +1068,47 @@ struct BSDF {
     return r;
   }
 
-  Sp eval(V3 wi, V3 wo) const { return m->kind == TR_MAT_PHONG ? phong_agg_eval(wi, wo) : disney_eval(wi, wo); }
-  real pdf(V3 wi, V3 wo) const { return m->kind == TR_MAT_PHONG ? phong_agg_pdf(wi, wo) : disney_pdf(wi, wo); }
+  // GlassBSDF::sample (material/glass.cpp:29-80), DielectricFresnelPoint(ior, 1),
+  // TransportMode::Radiance; eval and pdf are 0 (a delta BSDF)
+  BSDFSample glass_sample(V3 wo, real u) const {
+    BSDFSample out;
+    const V3 lwo = normalize(s.to_local(wo));
+    const V3 nor = lwo.z > 0 ? V3(0, 0, 1) : V3(0, 0, -1);
+    const real fr = dielectric_fresnel(m->ior, 1, lwo.z);
+    if (u < fr) {
+      const V3 lwi(-lwo.x, -lwo.y, lwo.z);
+      const V3 wi = s.to_global(lwi);
+      const real q = fr / std::abs(lwi.z);
+      const Sp f(m->kr.r * q, m->kr.g * q, m->kr.b * q);
+      out.wi = wi;
+      out.f = f * normal_correct_factor(g, s, wi);
+      out.pdf = fr;
+      out.delta = true;
+      return out;
+    }
+    const real eta_i = lwo.z > 0 ? real(1) : m->ior, eta_t = lwo.z > 0 ? m->ior : real(1);
+    const real eta = eta_i / eta_t;
+    V3 t;
+    if (!refract_dir(lwo, nor, eta, t)) return out;
+    const V3 lwi = normalize(t);
+    const V3 wi = s.to_global(lwi);
+    const real corr = eta * eta, az = std::abs(lwi.z);
+    const Sp f(((corr * m->kt_sqrt.r) * (1 - fr)) / az, ((corr * m->kt_sqrt.g) * (1 - fr)) / az,
+               ((corr * m->kt_sqrt.b) * (1 - fr)) / az);
+    out.wi = wi;
+    out.f = f * normal_correct_factor(g, s, wi);
+    out.pdf = 1 - fr;
+    out.delta = true;
+    return out;
+  }
+  Sp eval(V3 wi, V3 wo) const {
+    return m->kind == TR_MAT_PHONG ? phong_agg_eval(wi, wo) : (m->kind == TR_MAT_DISNEY12 ? disney_eval(wi, wo) : Sp());
+  }
+  real pdf(V3 wi, V3 wo) const {
+    return m->kind == TR_MAT_PHONG ? phong_agg_pdf(wi, wo) : (m->kind == TR_MAT_DISNEY12 ? disney_pdf(wi, wo) : 0);
+  }
   BSDFSample sample(V3 wo, real u, real v, real w) const {
+    if (m->kind == TR_MAT_GLASS) return glass_sample(wo, u);
     return m->kind == TR_MAT_PHONG ? phong_agg_sample(wo, u, v, w) : disney_sample(wo, u, v, w);
   }
 };
@@ -1172,11 +1240,15 @@ Sp sample_bsdf_mis(Tracer& tr, const Isect& is, const BSDF& bsdf, Sampler& smp) 
 }
 
 // PathTraceRenderer::eval_pixel_li (renderer/path_trace_renderer.cpp:27-210)
-// for vacuum media, no environment light and non-delta BSDFs.
+// for vacuum media and no environment light. A delta sample gets no direct
+// lighting, the emission its ray reaches counts, and up to
+// max_specular_depth (20, path_trace_renderer.cpp:20) of them do not count
+// toward the depth (:131-139).
 Sp eval_li(Tracer& tr, Ray ray, Sampler& smp, int min_depth, int max_depth) {
   const Scene& sc = tr.sc;
   Sp coef(1), L(0);
-  for (int depth = 0; depth < max_depth; ++depth) {
+  bool specular = false;
+  for (int depth = 0, s_depth = 0; depth < max_depth; ++depth) {
     if (depth > min_depth) {
       if (smp.u() > 0.9) break;
       coef = coef / (real)0.9;  // Color3::operator/=(T) with T = float
@@ -1184,16 +1256,23 @@ Sp eval_li(Tracer& tr, Ray ray, Sampler& smp, int min_depth, int max_depth) {
     if (!coef.valid()) break;
     Isect is;
     bool found = tr.trace_p(ray, is);
-    if (depth == 0 && found && sc.prims[is.prim].light) L += coef * light_emit(sc, is.prim, is, -ray.d);
+    if ((depth == 0 || specular) && found && sc.prims[is.prim].light) L += coef * light_emit(sc, is.prim, is, -ray.d);
     if (!found) break;
     BSDF bsdf{&sc.mats[sc.prims[is.prim].material], is.g, is.s};
     const real u = smp.u(), v = smp.u(), w = smp.u();
     BSDFSample bs = bsdf.sample(is.wo, u, v, w);
     if (bs.f.black() || bs.pdf < kEps) break;
-    Sp direct;
-    for (int li : sc.lights) direct += coef * sample_area_light(tr, li, is, bsdf, smp);
-    direct += coef * sample_bsdf_mis(tr, is, bsdf, smp);
-    L += direct * (real(1) / 1);
+    specular = bs.delta;
+    if (specular && s_depth < 20) {
+      s_depth++;
+      depth--;
+    }
+    if (!specular) {
+      Sp direct;
+      for (int li : sc.lights) direct += coef * sample_area_light(tr, li, is, bsdf, smp);
+      direct += coef * sample_bsdf_mis(tr, is, bsdf, smp);
+      L += direct * (real(1) / 1);
+    }
     coef = coef * ((bs.f * abs_cos(is.g.z, bs.wi)) / bs.pdf);
     if (!coef.valid()) break;
     ray = make_ray(is.eps_offset(bs.wi), normalize(bs.wi));
@@ -1350,6 +1429,10 @@ void* orc_scene_create(const tr_scene_desc* d) {
       m.specular = spec;
       m.ns = src.ns;
       m.base = diffuse;
+    } else if (src.kind == TR_MAT_GLASS) {
+      m.kr = Sp(src.kr[0], src.kr[1], src.kr[2]);
+      m.kt_sqrt = Sp(std::sqrt(src.kt[0]), std::sqrt(src.kt[1]), std::sqrt(src.kt[2]));
+      m.ior = src.ior;
     } else {
       m.base = Sp(src.base_color[0], src.base_color[1], src.base_color[2]);
       m.subsurface = src.subsurface; m.metallic = src.metallic; m.specular_s = src.specular;

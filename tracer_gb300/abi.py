@@ -22,6 +22,7 @@ TR_ERR_UNSUPPORTED = 8
 
 TR_MAT_PHONG = 0
 TR_MAT_DISNEY12 = 1
+TR_MAT_GLASS = 2
 
 f32p = C.POINTER(C.c_float)
 f64p = C.POINTER(C.c_double)
@@ -54,7 +55,7 @@ class TrMaterial(C.Structure):
                 ("subsurface", C.c_float), ("metallic", C.c_float), ("specular", C.c_float),
                 ("specular_tint", C.c_float), ("roughness", C.c_float), ("anisotropic", C.c_float),
                 ("sheen", C.c_float), ("sheen_tint", C.c_float), ("clearcoat", C.c_float),
-                ("clearcoat_gloss", C.c_float)]
+                ("clearcoat_gloss", C.c_float), ("kr", C.c_float * 3), ("kt", C.c_float * 3), ("ior", C.c_float)]
 
 
 class TrSceneDesc(C.Structure):
@@ -123,7 +124,8 @@ def ptr(a: np.ndarray | None, ctype):
 
 @dataclass
 class Material:
-    """One tr_material. kind=TR_MAT_PHONG uses ka/kd/ks/ns; Disney12 the rest."""
+    """One tr_material. kind=TR_MAT_PHONG uses ka/kd/ks/ns; Disney12 base_color .. clearcoat_gloss;
+    TR_MAT_GLASS kr/kt/ior."""
     kind: int = TR_MAT_PHONG
     ka: tuple = (0.0, 0.0, 0.0)
     kd: tuple = (0.0, 0.0, 0.0)
@@ -140,6 +142,9 @@ class Material:
     sheen_tint: float = 0.0
     clearcoat: float = 0.0
     clearcoat_gloss: float = 0.0
+    kr: tuple = (0.0, 0.0, 0.0)
+    kt: tuple = (0.0, 0.0, 0.0)
+    ior: float = 1.0
 
     def to_c(self) -> TrMaterial:
         m = TrMaterial()
@@ -150,8 +155,10 @@ class Material:
         m.ns = self.ns
         m.base_color[:] = self.base_color
         for k in ("subsurface", "metallic", "specular", "specular_tint", "roughness", "anisotropic",
-                  "sheen", "sheen_tint", "clearcoat", "clearcoat_gloss"):
+                  "sheen", "sheen_tint", "clearcoat", "clearcoat_gloss", "ior"):
             setattr(m, k, getattr(self, k))
+        m.kr[:] = self.kr
+        m.kt[:] = self.kt
         return m
 
 

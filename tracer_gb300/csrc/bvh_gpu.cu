@@ -472,6 +472,8 @@ tr_status upload_device_built(tr_ctx* ctx) {
   sc.roots = ctx->d_roots.as<SceneRoot>();
   sc.num_scenes = (int)nsc;
   sc.max_lights = max_lights;
+  sc.has_glass = 0;
+  for (const DMat& m : hs.mats) sc.has_glass |= m.kind == MAT_GLASS;
   ctx->has_scene = true;
   return TR_OK;
 }

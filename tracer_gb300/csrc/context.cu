@@ -64,6 +64,12 @@ DMat derive_material(const tr_material& m) {
     d.diffuse_coef = mk3(diffuse.x / kPi, diffuse.y / kPi, diffuse.z / kPi);
     d.specular = spec;
     d.ns = m.ns;
+  } else if (m.kind == TR_MAT_GLASS) {
+    d.kind = MAT_GLASS;
+    d.kr = mk3(m.kr[0], m.kr[1], m.kr[2]);
+    d.kt_sqrt = mk3(std::sqrt(m.kt[0]), std::sqrt(m.kt[1]), std::sqrt(m.kt[2]));  // Glass::shading
+    d.ior = m.ior;
+    d.albedo = mk3(0.5f * (d.kr.x + d.kt_sqrt.x), 0.5f * (d.kr.y + d.kt_sqrt.y), 0.5f * (d.kr.z + d.kt_sqrt.z));
   } else {
     d.kind = MAT_DISNEY12;
     d.base = mk3(m.base_color[0], m.base_color[1], m.base_color[2]);
@@ -303,6 +309,8 @@ tr_status upload_device_tables(tr_ctx* ctx) {
   sc.roots = ctx->d_roots.as<SceneRoot>();
   sc.num_scenes = (int)nsc;
   sc.max_lights = max_lights;
+  sc.has_glass = 0;
+  for (const DMat& m : hs.mats) sc.has_glass |= m.kind == MAT_GLASS;
   ctx->has_scene = true;
   return TR_OK;
 }
@@ -477,7 +485,8 @@ static tr_status build_host_scene(tr_ctx* ctx, const tr_scene_desc* d, HostScene
     if (d->indices[i] < 0 || (uint32_t)d->indices[i] >= d->num_vertices)
       return set_err(ctx, TR_ERR_ARG, "triangle index out of range");
   for (uint32_t m = 0; m < d->num_materials; ++m)
-    if (d->materials[m].kind != TR_MAT_PHONG && d->materials[m].kind != TR_MAT_DISNEY12)
+    if (d->materials[m].kind != TR_MAT_PHONG && d->materials[m].kind != TR_MAT_DISNEY12 &&
+        d->materials[m].kind != TR_MAT_GLASS)
       return set_err(ctx, TR_ERR_ARG, "unknown material kind");
   for (uint32_t s = 0; s < d->num_spheres; ++s)
     if (!(d->sphere_radius[s] > 0.0f)) return set_err(ctx, TR_ERR_ARG, "invalid sphere radius");  // sphere.cpp:88-90

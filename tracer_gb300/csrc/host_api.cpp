@@ -406,6 +406,17 @@ RC<Material> create_phong_material(RC<const Texture2D> map_ka, RC<const Texture2
   return std::make_shared<Material>(m);
 }
 
+RC<Material> create_glass(RC<const Texture2D> map_kr, RC<const Texture2D> map_kt, RC<const Texture2D> map_ior) {
+  tr_material m{};
+  m.kind = TR_MAT_GLASS;
+  const Spectrum kr = tex(map_kr, "kr"), kt = tex(map_kt, "kt");
+  const float r[3] = {kr.r, kr.g, kr.b}, t[3] = {kt.r, kt.g, kt.b};
+  std::memcpy(m.kr, r, sizeof(r));
+  std::memcpy(m.kt, t, sizeof(t));
+  m.ior = tex_s(map_ior, "ior");
+  return std::make_shared<Material>(m);
+}
+
 RC<Material> create_disney_brdf(RC<const Texture2D> base_color, RC<const Texture2D> subsurface,
                                 RC<const Texture2D> metallic, RC<const Texture2D> specular,
                                 RC<const Texture2D> specular_tint, RC<const Texture2D> roughness,

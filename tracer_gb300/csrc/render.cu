@@ -51,17 +51,27 @@ enum : int {
   F_REC = 8,        // the previous vertex wrote a guiding record awaiting its radiance
   F_GCONT = 16,     // ...and its guided continuation is an MIS strategy of its direct lighting
   F_GX = 32,        // ...and so is a ray drawn from the mixture alone (in the MIS slot)
+  F_SPEC = 64,      // the continuation was sampled from a delta BSDF: emission it reaches counts
 };
+
+// PathTraceRenderer::max_specular_depth (src/renderer/path_trace_renderer.cpp:20):
+// delta samples that do not count toward the path depth
+constexpr int kMaxSpecularDepth = 20;
+
+// P1.w holds the path depth (low 16 bits) and the count of delta samples
+// that did not count toward it (high bits).
+__device__ __forceinline__ int path_depth(float w) { return __float_as_int(w) & 0xffff; }
+__device__ __forceinline__ int spec_depth(float w) { return __float_as_int(w) >> 16; }
 
 enum : int {  // counter slots
   C_EXT = 0,      // 2: extend queue sizes (double-buffered)
   C_ACT = 2,      // 2: live-slot list sizes
   C_SH = 4,       // shadow queue size
-  C_MAT = 5,      // 2: per-material hit queue sizes
-  C_NEE = 7,      // 2: per-material light-sample queue sizes
-  C_FEXT = 9,     // extend kernel's work-fetch position
-  C_FSH = 10,     // shadow kernel's work-fetch position
-  C_TB = 11,      // guiding training records written (whole render)
+  C_MAT = 5,      // 3: per-material hit queue sizes (Phong, Disney12, glass)
+  C_NEE = 8,      // 2: per-material light-sample queue sizes (glass has none)
+  C_FEXT = 10,    // extend kernel's work-fetch position
+  C_FSH = 11,     // shadow kernel's work-fetch position
+  C_TB = 12,      // guiding training records written (whole render)
   C_ERR = 15,     // traversal error word
 };
 
@@ -106,7 +116,7 @@ struct Launch {
   float4* SH;            // shadow: 3 per (slot, light): o|t_max, d, contrib|valid
   int* q_ext[2];
   int* q_act[2];
-  int* q_mat[2];
+  int* q_mat[kMatKinds];
   int* q_nee[2];
   int* q_sh;
   unsigned int* ctr;
@@ -517,9 +527,9 @@ __global__ void __launch_bounds__(128) k_logic(Launch P, int cur) {
       continue;
     }
     const DPrim& pr = P.sc.prims[pid];
-    if (__float_as_int(P.P1[slot].w) == 0 && pr.emissive) {
-      // emission seen by the camera ray: light_emit(isect, -ray.d); only
-      // triangles emit on this path
+    if ((path_depth(P.P1[slot].w) == 0 || (flags & F_SPEC)) && pr.emissive) {
+      // emission seen by the camera ray or after a delta sample:
+      // light_emit(isect, -ray.d); only triangles emit on this path
       const f3 gz = P.sc.tshade[pr.shape].gz;
       const float4 p1 = P.P1[slot], p2 = P.P2[slot];
       if (dot(gz, mk3(-p1.x, -p1.y, -p1.z)) > 0.0f) L = L + mulc(mk3(p2.x, p2.y, p2.z), pr.emission);
@@ -544,12 +554,15 @@ __global__ void __launch_bounds__(128) k_logic(Launch P, int cur) {
 template <int KIND>
 struct MatOps {
   static __device__ __forceinline__ BsdfSample sample(const Bsdf& b, f3 wo, float u, float v, float w) {
+    if (KIND == MAT_GLASS) return b.glass_sample(wo, u);
     return KIND == MAT_PHONG ? b.phong_sample_agg(wo, u, v, w) : b.disney_sample(wo, u, v, w);
   }
   static __device__ __forceinline__ f3 eval(const Bsdf& b, f3 wi, f3 wo) {
+    if (KIND == MAT_GLASS) return mk3(0.0f, 0.0f, 0.0f);
     return KIND == MAT_PHONG ? b.phong_eval_agg(wi, wo) : b.disney_eval(wi, wo);
   }
   static __device__ __forceinline__ float pdf(const Bsdf& b, f3 wi, f3 wo) {
+    if (KIND == MAT_GLASS) return 0.0f;
     return KIND == MAT_PHONG ? b.phong_pdf_agg(wi, wo) : b.disney_pdf(wi, wo);
   }
 };
@@ -658,7 +671,7 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
     unsigned long long st = P.rng[slot];
     const float4 p0 = P.P0[slot], p1 = P.P1[slot], p2 = P.P2[slot];
     const f3 ro = mk3(p0.x, p0.y, p0.z), rd = mk3(p1.x, p1.y, p1.z);
-    int depth = __float_as_int(p1.w);
+    int depth = path_depth(p1.w), sdepth = spec_depth(p1.w);
     f3 coef = mk3(p2.x, p2.y, p2.z);
     const float4 hit = P.HC[slot];
     Isect is;
@@ -831,10 +844,72 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
         }
       }
       P.P0[slot] = make_float4(no.x, no.y, no.z, __int_as_float(flags));
-      P.P1[slot] = make_float4(nd.x, nd.y, nd.z, __int_as_float(depth));
+      P.P1[slot] = make_float4(nd.x, nd.y, nd.z, __int_as_float(depth | sdepth << 16));
       P.q_ext[nxt][append(P.ctr + C_EXT + nxt)] = 2 * slot;
     }
     P.P2[slot] = make_float4(coef.x, coef.y, coef.z, p2.w);
+    P.q_act[nxt][append(P.ctr + C_ACT + nxt)] = slot;
+    P.rng[slot] = st;
+  }
+  count_add(P.stats, finished);
+}
+
+// A vertex on glass, a delta BSDF (src/material/glass.cpp:29-80): the body of
+// eval_pixel_li for a delta sample (src/renderer/path_trace_renderer.cpp:125-163).
+// No direct lighting (and no draws for it); up to kMaxSpecularDepth delta
+// samples of a path do not count toward its depth; the emission the next
+// ray reaches counts (F_SPEC, read by k_logic).
+__global__ void __launch_bounds__(128) k_glass(Launch P, int cur) {
+  const int nxt = cur ^ 1;
+  const unsigned int n = P.ctr[C_MAT + MAT_GLASS];
+  unsigned int finished = 0;
+  for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int slot = P.q_mat[MAT_GLASS][i];
+    unsigned long long st = P.rng[slot];
+    const float4 p0 = P.P0[slot], p1 = P.P1[slot], p2 = P.P2[slot];
+    int depth = path_depth(p1.w), sdepth = spec_depth(p1.w);
+    f3 coef = mk3(p2.x, p2.y, p2.z);
+    Isect is;
+    make_isect(P.sc, P.HC[slot], mk3(p0.x, p0.y, p0.z), mk3(p1.x, p1.y, p1.z), is);
+    Bsdf bsdf;
+    bsdf.m = P.sc.mats + P.sc.prims[is.prim].material;
+    bsdf.g = is.g;
+    bsdf.s = is.s;
+    const float u0 = Pcg::next(st);
+    Pcg::skip<2>(st);  // the rest of sample3()
+    const BsdfSample bs = bsdf.glass_sample(is.wo, u0);
+    bool term = black(bs.f) || bs.pdf < kEps;
+    if (!term) {
+      const bool counted = sdepth >= kMaxSpecularDepth;
+      if (!counted) ++sdepth;
+      coef = mulc(coef, divs(muls(bs.f, abs_cos(is.g.z, bs.wi)), bs.pdf));
+      term = !valid3(coef);
+      if (!term) {
+        if (counted) ++depth;
+        const JobDev& J = job_of(P, slot);
+        if (depth >= J.max_depth) {
+          term = true;
+        } else if (depth > J.min_depth) {
+          if (Pcg::next(st) > 0.9f) term = true;
+          else {
+            coef = divs(coef, 0.9f);
+            if (!valid3(coef)) term = true;
+          }
+        }
+      }
+    }
+    if (term) {
+      const float4 p3 = P.P3[slot];
+      finish_sample(P, slot, st, mk3(p3.x, p3.y, p3.z), nxt, finished);
+      P.rng[slot] = st;
+      continue;
+    }
+    const f3 no = is.eps_offset(bs.wi);
+    const f3 nd = normalize(normalize(bs.wi));
+    P.P0[slot] = make_float4(no.x, no.y, no.z, __int_as_float(F_SPEC));
+    P.P1[slot] = make_float4(nd.x, nd.y, nd.z, __int_as_float(depth | sdepth << 16));
+    P.P2[slot] = make_float4(coef.x, coef.y, coef.z, p2.w);
+    P.q_ext[nxt][append(P.ctr + C_EXT + nxt)] = 2 * slot;
     P.q_act[nxt][append(P.ctr + C_ACT + nxt)] = slot;
     P.rng[slot] = st;
   }
@@ -943,7 +1018,7 @@ tr_status reserve_render(tr_ctx* ctx, int n, int nl) {
                {&rb->M0, N * f4},           {&rb->M1, N * f4},          {&rb->M2, N * f4},
                {&rb->HC, N * f4},           {&rb->HM, N * f4},          {&rb->SC, N * 7 * f4},
                {&rb->NU, N * NL * 8},       {&rb->SH, N * NL * 3 * f4}, {&rb->acc, N * 32},
-               {&rb->q_ext, 2 * 2 * N * 4}, {&rb->q_act, 2 * N * 4},   {&rb->q_mat, 2 * N * 4},
+               {&rb->q_ext, 2 * 2 * N * 4}, {&rb->q_act, 2 * N * 4},   {&rb->q_mat, kMatKinds * N * 4},
                {&rb->q_nee, 2 * N * NL * 4}, {&rb->q_sh, N * NL * 4},  {&rb->ctr, 64},
                {&rb->stats, 64}};
   for (auto& nd : needs) {
@@ -1028,13 +1103,16 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
   if (njobs <= 0) return set_err(ctx, TR_ERR_ARG, "no jobs");
   long long total = 0;
-  long long max_iters = 0;  // every slot finishes within spp * (max_depth + 2) iterations
+  // every slot finishes within spp * (max_depth + 2) iterations, plus the
+  // delta samples that do not count toward the depth
+  long long max_iters = 0;
+  const int extra = ctx->dsc.has_glass ? kMaxSpecularDepth : 0;
   for (int k = 0; k < njobs; ++k) {
     tr_status v = validate_job(ctx, jobs[k]);
     if (v != TR_OK) return v;
     if (!jobs[k].film && njobs != 1) return set_err(ctx, TR_ERR_ARG, "batch jobs need device films");
     total += (long long)jobs[k].prm.width * jobs[k].prm.height;
-    max_iters = std::max(max_iters, (long long)jobs[k].prm.spp * (jobs[k].prm.max_depth + 2) + 4);
+    max_iters = std::max(max_iters, (long long)jobs[k].prm.spp * (jobs[k].prm.max_depth + 2 + extra) + 4);
   }
   if (total > (1ll << 28)) return set_err(ctx, TR_ERR_ARG, "batch too large");
   const int n = (int)total;
@@ -1081,9 +1159,9 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   for (int k = 0; k < 2; ++k) {
     P.q_ext[k] = rb->q_ext.as<int>() + (size_t)k * 2 * n;
     P.q_act[k] = rb->q_act.as<int>() + (size_t)k * n;
-    P.q_mat[k] = rb->q_mat.as<int>() + (size_t)k * n;
     P.q_nee[k] = rb->q_nee.as<int>() + (size_t)k * n * std::max(nl, 1);
   }
+  for (int k = 0; k < kMatKinds; ++k) P.q_mat[k] = rb->q_mat.as<int>() + (size_t)k * n;
   P.q_sh = rb->q_sh.as<int>();
   P.ctr = rb->ctr.as<unsigned int>();
   P.stats = rb->stats.as<unsigned long long>();
@@ -1191,7 +1269,7 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     // material and light-sample counts and the fetch positions
     cudaMemsetAsync(P.ctr + C_EXT + nxt, 0, 4, st);
     cudaMemsetAsync(P.ctr + C_ACT + nxt, 0, 4, st);
-    cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 7, st);  // C_SH, C_MAT x2, C_NEE x2, C_FEXT, C_FSH
+    cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 8, st);  // C_SH, C_MAT x3, C_NEE x2, C_FEXT, C_FSH
     mark();
     k_logic<<<grid, 128, 0, st>>>(P, cur);
     if (P.guide_alpha > 0.0f) {
@@ -1205,6 +1283,7 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     else k_material<MAT_PHONG><<<grid, 128, 0, st>>>(P, cur);
     mark();
     k_material<MAT_DISNEY12><<<grid, 128, 0, st>>>(P, cur);
+    if (P.sc.has_glass) k_glass<<<grid, 128, 0, st>>>(P, cur);  // timed with Disney12
     mark();
     k_nee<MAT_PHONG><<<grid, 128, 0, st>>>(P);
     mark();
@@ -1410,14 +1489,14 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   const size_t f4 = sizeof(float4);
   const size_t oP = L.take(5 * N * f4), oRng = L.take(N * 8), oM = L.take(3 * N * f4), oH = L.take(2 * N * f4),
                oSC = L.take(N * 7 * f4), oNU = L.take(N * NL * 8), oSH = L.take(N * NL * 3 * f4),
-               oQe = L.take(2 * 2 * N * 4), oQa = L.take(2 * N * 4), oQm = L.take(2 * N * 4),
+               oQe = L.take(2 * 2 * N * 4), oQa = L.take(2 * N * 4), oQm = L.take(kMatKinds * N * 4),
                oQn = L.take(2 * N * NL * 4), oQs = L.take(N * NL * 4), oCtr = L.take(64), oSt = L.take(64),
                oJob = L.take(sizeof(JobDev));
   if (npix > (1ll << 24) || L.off > kNoAllocScratchBytes) {
     char msg[256];
     std::snprintf(msg, sizeof(msg),
                   "film %dx%d with %d lights needs %zu bytes of scratch; tr_render_dev_noalloc has %zu "
-                  "(about 312 + 68 * lights bytes per pixel)",
+                  "(about 316 + 68 * lights bytes per pixel)",
                   prm->width, prm->height, nl, (size_t)L.off, kNoAllocScratchBytes);
     return set_err(ctx, TR_ERR_ARG, msg);
   }
@@ -1482,9 +1561,9 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   for (int k = 0; k < 2; ++k) {
     P.q_ext[k] = qe + (size_t)k * 2 * N;
     P.q_act[k] = qa + (size_t)k * N;
-    P.q_mat[k] = qm + (size_t)k * N;
     P.q_nee[k] = qn + (size_t)k * N * NL;
   }
+  for (int k = 0; k < kMatKinds; ++k) P.q_mat[k] = qm + (size_t)k * N;
   P.q_sh = reinterpret_cast<int*>(base + oQs);
   P.ctr = reinterpret_cast<unsigned int*>(base + oCtr);
   P.stats = reinterpret_cast<unsigned long long*>(base + oSt);
@@ -1503,18 +1582,21 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   NCHK(cudaMemsetAsync(P.stats, 0, 64, st));
   k_init<<<grid_init, 256, 0, st>>>(P);
   NCHK(cudaGetLastError());
-  // Every slot finishes within spp * (max_depth + 2) iterations; iterations
-  // past the drain find empty queues and return at once.
-  const long long iters = (long long)prm->spp * (prm->max_depth + 2) + 4;
+  // Every slot finishes within spp * (max_depth + 2) iterations (plus the
+  // delta samples that do not count toward the depth); iterations past the
+  // drain find empty queues and return at once.
+  const long long iters =
+      (long long)prm->spp * (prm->max_depth + 2 + (ctx->dsc.has_glass ? kMaxSpecularDepth : 0)) + 4;
   for (long long it = 0; it < iters; ++it) {
     const int cur = (int)(it & 1), nxt = cur ^ 1;
     k_extend<false><<<grid_ext, 128, 0, st>>>(P, cur);
     NCHK(cudaMemsetAsync(P.ctr + C_EXT + nxt, 0, 4, st));
     NCHK(cudaMemsetAsync(P.ctr + C_ACT + nxt, 0, 4, st));
-    NCHK(cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 7, st));
+    NCHK(cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 8, st));  // C_SH, C_MAT x3, C_NEE x2, C_FEXT, C_FSH
     k_logic<<<grid, 128, 0, st>>>(P, cur);
     k_material<MAT_PHONG><<<grid, 128, 0, st>>>(P, cur);
     k_material<MAT_DISNEY12><<<grid, 128, 0, st>>>(P, cur);
+    if (P.sc.has_glass) k_glass<<<grid, 128, 0, st>>>(P, cur);
     k_nee<MAT_PHONG><<<grid, 128, 0, st>>>(P);
     k_nee<MAT_DISNEY12><<<grid, 128, 0, st>>>(P);
     if (wide) k_shadow<false, true><<<grid_sh, 128, 0, st>>>(P);

@@ -78,10 +78,12 @@ struct DTriShade {
   int pad[3];
 };
 
-enum { MAT_PHONG = 0, MAT_DISNEY12 = 1 };
+enum { MAT_PHONG = 0, MAT_DISNEY12 = 1, MAT_GLASS = 2 };
+constexpr int kMatKinds = 3;
 
 // Phong: the AggregateBSDF<2> that Phong::shading builds (src/material/phong.cpp:29-70)
 // Disney12: the eleven parameters (src/material/disney_brdf.cpp:278-302)
+// Glass: GlassBSDF's colours and index of refraction
 struct DMat {
   int kind;
   float ns, w_diffuse, w_specular;
@@ -94,6 +96,9 @@ struct DMat {
   float subsurface, metallic, specular_s, specular_tint, roughness, anisotropic;
   float sheen, sheen_tint, clearcoat, clearcoat_gloss;
   f3 base;
+  // Glass (src/material/glass.cpp:117-140): reflect colour, sqrt(transmit colour), ior
+  f3 kr, kt_sqrt;
+  float ior;
 };
 
 // A diffuse area light on a triangle (src/light/diffuse_light.cpp:44-60)
@@ -130,6 +135,7 @@ struct DScene {
   const SceneRoot* roots;
   int num_scenes;
   int max_lights;  // most lights of one scene
+  int has_glass;   // some material is a delta BSDF (glass)
 };
 
 }  // namespace trg

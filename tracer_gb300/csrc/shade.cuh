@@ -173,8 +173,26 @@ __device__ __forceinline__ void make_isect(const DScene& sc, const float4 hit, f
 struct BsdfSample {
   f3 wi, f;
   float pdf;
+  bool delta = false;  // BSDFSampleResult::is_delta
   __device__ __forceinline__ bool valid() const { return pdf > 0.0f && !black(f); }  // core/bsdf.hpp:21-23
 };
+
+// dielectric_fresnel (src/utility/reflection.hpp:16-40)
+__device__ __forceinline__ float dielectric_fresnel(float eta_i, float eta_o, float cos_theta_i) {
+  if (cos_theta_i < 0.0f) {
+    const float t = eta_i;
+    eta_i = eta_o;
+    eta_o = t;
+    cos_theta_i = -cos_theta_i;
+  }
+  const float sin_theta_i = sqrtf(fmaxf(0.0f, 1.0f - cos_theta_i * cos_theta_i));
+  const float sin_theta_t = eta_o / eta_i * sin_theta_i;
+  if (sin_theta_t >= 1.0f) return 1.0f;
+  const float cos_theta_t = sqrtf(fmaxf(0.0f, 1.0f - sin_theta_t * sin_theta_t));
+  const float para = (eta_i * cos_theta_i - eta_o * cos_theta_t) / (eta_i * cos_theta_i + eta_o * cos_theta_t);
+  const float perp = (eta_o * cos_theta_i - eta_i * cos_theta_t) / (eta_o * cos_theta_i + eta_i * cos_theta_t);
+  return 0.5f * (para * para + perp * perp);
+}
 
 // microfacet helpers (src/material/utility/microfacet.cpp:7-134, microfacet.hpp:10-14)
 __device__ __forceinline__ float sqr(float x) { return x * x; }
@@ -558,13 +576,56 @@ struct Bsdf {
     return r;
   }
 
+  // ---- GlassBSDF (src/material/glass.cpp:11-99) with DielectricFresnelPoint(ior, 1) and
+  // TransportMode::Radiance: a delta BSDF (eval and pdf 0); u picks reflection with the
+  // Fresnel probability, else refraction (refract_dir, src/utility/reflection.hpp:43-51)
+  __device__ BsdfSample glass_sample(f3 wo, float u) const {
+    BsdfSample out;
+    out.pdf = 0.0f;
+    out.f = mk3(0.0f, 0.0f, 0.0f);
+    out.wi = out.f;
+    const f3 lwo = normalize(to_local(s, wo));
+    const f3 nor = lwo.z > 0.0f ? mk3(0.0f, 0.0f, 1.0f) : mk3(0.0f, 0.0f, -1.0f);
+    const float fr = dielectric_fresnel(m->ior, 1.0f, lwo.z);
+    if (u < fr) {
+      const f3 lwi = mk3(-lwo.x, -lwo.y, lwo.z);
+      const f3 wi = to_global(s, lwi);
+      const float q = fr / fabsf(lwi.z);
+      out.wi = wi;
+      out.f = muls(mk3(m->kr.x * q, m->kr.y * q, m->kr.z * q), normal_correct(g, s, wi));
+      out.pdf = fr;
+      out.delta = true;
+      return out;
+    }
+    const float eta_i = lwo.z > 0.0f ? 1.0f : m->ior, eta_t = lwo.z > 0.0f ? m->ior : 1.0f;
+    const float eta = eta_i / eta_t;
+    const float cos_i = fabsf(lwo.z);
+    const float sin_i2 = fmaxf(0.0f, 1.0f - cos_i * cos_i);
+    const float sin_t2 = eta * eta * sin_i2;
+    if (sin_t2 >= 1.0f) return out;  // total internal reflection: no sample
+    const float cos_t = sqrtf(1.0f - sin_t2);
+    const f3 lwi = normalize(scale(nor, eta * cos_i - cos_t) - scale(lwo, eta));
+    const f3 wi = to_global(s, lwi);
+    const float corr = eta * eta, az = fabsf(lwi.z);
+    const f3 f = mk3(((corr * m->kt_sqrt.x) * (1.0f - fr)) / az, ((corr * m->kt_sqrt.y) * (1.0f - fr)) / az,
+                     ((corr * m->kt_sqrt.z) * (1.0f - fr)) / az);
+    out.wi = wi;
+    out.f = muls(f, normal_correct(g, s, wi));
+    out.pdf = 1.0f - fr;
+    out.delta = true;
+    return out;
+  }
+
   __device__ __forceinline__ f3 eval(f3 wi, f3 wo) const {
+    if (m->kind == MAT_GLASS) return mk3(0.0f, 0.0f, 0.0f);
     return m->kind == MAT_PHONG ? phong_eval_agg(wi, wo) : disney_eval(wi, wo);
   }
   __device__ __forceinline__ float pdf(f3 wi, f3 wo) const {
+    if (m->kind == MAT_GLASS) return 0.0f;
     return m->kind == MAT_PHONG ? phong_pdf_agg(wi, wo) : disney_pdf(wi, wo);
   }
   __device__ __forceinline__ BsdfSample sample(f3 wo, float u, float v, float w) const {
+    if (m->kind == MAT_GLASS) return glass_sample(wo, u);
     return m->kind == MAT_PHONG ? phong_sample_agg(wo, u, v, w) : disney_sample(wo, u, v, w);
   }
 };
