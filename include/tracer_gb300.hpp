@@ -115,6 +115,31 @@ struct mesh_t {
   std::vector<int> indices;
   std::vector<int> materials;
 };
+// A Wavefront MTL material (src/utility/mesh_load.hpp:27-79): colours and
+// scalars as written, texture maps by file name.
+struct material_t {
+  std::string name;
+  real ambient[3] = {0, 0, 0}, diffuse[3] = {0, 0, 0}, specular[3] = {0, 0, 0}, transmittance[3] = {0, 0, 0},
+       emission[3] = {0, 0, 0};
+  real shininess = 1, ior = 1, dissolve = 1;
+  int illum = 0;
+  std::string map_ka, map_kd, map_ks, map_ns, map_bump, disp, map_d, refl;
+  real roughness = 0, metallic = 0, sheen = 0, clearcoat_thickness = 0, clearcoat_roughness = 0;
+  std::string map_pr, map_pm, map_ps, map_ke, norm;
+};
+struct model_t {
+  std::string name;
+  std::vector<mesh_t> mesh;
+  std::vector<material_t> material;
+};
+// load_model_from_file (src/utility/mesh_load.cpp:25-113), read by a
+// project-written Wavefront OBJ/MTL parser: one mesh per object/group with
+// faces, polygons fan-triangulated, vertices deduplicated by (position,
+// normal, uv) in first-use order, normals normalised, the material id of
+// every triangle (-1 without usemtl); mtllib files relative to the OBJ.
+// Faces need vertex normals, as the reference reads them unchecked.
+// Throws TracerError on a missing file or a malformed line.
+model_t load_model_from_file(const std::string& path);
 
 // ---- scene objects ----
 
