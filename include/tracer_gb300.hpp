@@ -173,6 +173,11 @@ RC<Material> create_disney_brdf(RC<const Texture2D> base_color, RC<const Texture
                                 RC<const Texture2D> clearcoat_gloss);
 // create_glass (src/factory/material.hpp:13-17, src/material/glass.cpp:145-154)
 RC<Material> create_glass(RC<const Texture2D> map_kr, RC<const Texture2D> map_kt, RC<const Texture2D> map_ior);
+// create_metal (src/factory/material.hpp:90-96, src/material/metal.cpp:68-76) with
+// no normal mapper; the painted conductor Fresnel is built as the reference
+// builds it from (color, eta, k)
+RC<Material> create_metal(RC<const Texture2D> color, RC<const Texture2D> eta, RC<const Texture2D> k,
+                          RC<const Texture2D> roughness, RC<const Texture2D> anisotropic);
 
 class Medium {
  public:

@@ -57,7 +57,7 @@ typedef struct tr_bvh_node32 {
   uint8_t pad;
 } tr_bvh_node32;
 
-enum { TR_MAT_PHONG = 0, TR_MAT_DISNEY12 = 1, TR_MAT_GLASS = 2 };
+enum { TR_MAT_PHONG = 0, TR_MAT_DISNEY12 = 1, TR_MAT_GLASS = 2, TR_MAT_METAL = 3 };
 
 /* Material record. Phong is create_phong_material(ka, kd, ks, ns)
  * (src/factory/material.hpp:19-24, src/material/phong.cpp:29-70); Disney12 is
@@ -76,6 +76,13 @@ typedef struct tr_material {
    * delta BSDF: Fresnel-weighted specular reflection (colour kr) or
    * refraction (colour sqrt(kt)) at index of refraction ior. */
   float kr[3], kt[3], ior;
+  /* Metal: create_metal(color, eta, k, roughness, anisotropic) with no normal
+   * map (src/material/metal.cpp:9-78): a GGX microfacet reflection with a
+   * painted conductor Fresnel; color, eta and k are RGB in create_metal's
+   * argument order (its hand-over to Metal's constructor and the Fresnel's
+   * parameter order are reproduced as the reference has them), roughness
+   * and anisotropic take the fields above. */
+  float color[3], eta[3], k[3];
 } tr_material;
 
 /* Flat scene description. It records what the reference factory calls build
@@ -307,7 +314,7 @@ tr_status tr_render_dev(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filt
  * event allocation. For callers that render previews inside a frame loop and
  * cannot take cudaFree's implicit device synchronisation, or that share the
  * GPU with a caching allocator holding the rest of its memory.
- *  - Limit: width * height * (316 + 68 * lights) bytes (plus alignment) must
+ *  - Limit: width * height * (316 + 72 * lights) bytes (plus alignment) must
  *    fit in 16 MiB, e.g. 128x128 with 8 lights; larger films return
  *    TR_ERR_ARG with the size needed.
  *  - The first call on a device looks up the array's address

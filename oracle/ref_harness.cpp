@@ -102,6 +102,9 @@ void* ref_scene_create(const tr_scene_desc* d) {
       s->materials.push_back(create_phong_material(ctex3(m.ka), ctex3(m.kd), ctex3(m.ks), ctex(m.ns)));
     } else if (m.kind == TR_MAT_GLASS) {
       s->materials.push_back(create_glass(ctex3(m.kr), ctex3(m.kt), ctex(m.ior)));
+    } else if (m.kind == TR_MAT_METAL) {
+      s->materials.push_back(create_metal(ctex3(m.color), ctex3(m.eta), ctex3(m.k), ctex(m.roughness),
+                                          ctex(m.anisotropic), newBox<NormalMapper>()));
     } else {
       s->materials.push_back(create_disney_brdf(
           ctex3(m.base_color), ctex(m.subsurface), ctex(m.metallic), ctex(m.specular),

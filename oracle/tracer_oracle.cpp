@@ -239,6 +239,16 @@ struct Mat {
   // transmit colour, index of refraction
   Sp kr, kt_sqrt;
   real ior;
+  // Metal::shading (material/metal.cpp:33-56): the painted conductor Fresnel
+  // as constructed there. create_metal(color, eta, k, ...) hands its
+  // arguments to Metal(color, k, eta, ...), so Metal's k is the caller's eta
+  // and its eta the caller's k; shading then builds
+  // PaintedConductorFresnelPoint(color, 1, eta, k), whose parameters are
+  // (eta_outside, eta_inside, k, paint). Net: eta_outside = color,
+  // eta_inside = 1, conductor k = the caller's k, paint = the caller's eta.
+  // GGX alphas (bxdf/microfacet_refl_bxdf.cpp:6-11); base holds the colour.
+  Sp f_eta2, f_etak2, f_paint;
+  real ax_m, ay_m;
 };
 struct Prim {
   int kind;  // 0 triangle, 1 sphere
@@ -764,6 +774,23 @@ struct BSDFSample {
   bool valid() const { return pdf > 0 && !f.black(); }  // core/bsdf.hpp:21-23
 };
 
+// ConductorFresnelPoint::evaluate (material/utility/fresnel_point.hpp:47-66), per channel
+inline real conductor_fresnel(real eta_2, real eta_k_2, real cos_theta_i) {
+  if (cos_theta_i <= 0) return 0;
+  const real cos2 = cos_theta_i * cos_theta_i;
+  const real sin2 = std::max(real(0), 1 - cos2);
+  const real t0 = eta_2 - eta_k_2 - sin2;
+  const real a2b2 = std::sqrt(t0 * t0 + real(4) * eta_2 * eta_k_2);
+  const real t1 = a2b2 + cos2;
+  const real a = std::sqrt(real(0.5) * (a2b2 + t0));
+  const real t2 = 2 * cos_theta_i * a;
+  const real rs = (t1 - t2) / (t1 + t2);
+  const real t3 = cos2 * a2b2 + sin2 * sin2;
+  const real t4 = t2 * sin2;
+  const real rp = rs * (t3 - t4) / (t3 + t4);
+  return real(0.5) * (rp + rs);
+}
+
 // dielectric_fresnel (utility/reflection.hpp:16-40)
 inline real dielectric_fresnel(real eta_i, real eta_o, real cos_theta_i) {
   if (cos_theta_i < 0) {
@@ -1101,14 +1128,110 @@ struct BSDF {
     out.delta = true;
     return out;
   }
+  // ---- Metal: AggregateBSDF<1> (material/aggregate_bsdf.hpp:36-118) of one
+  // GGXMicrofacetReflectionBXDF (bxdf/microfacet_refl_bxdf.cpp:13-78), weight 1
+  void ggx(V3 lwi, V3 lwo, Sp* eval, real* pdf) const {
+    const real cos_theta_i = lwi.z, cos_theta_o = lwo.z;
+    const V3 lwh = normalize(lwi + lwo);
+    const real cos_theta_d = dot(lwi, lwh);
+    const real phi_h = local_phi(lwh);
+    const real sin_phi_h = std::sin(phi_h), cos_phi_h = std::cos(phi_h);
+    const real cos_theta_h = lwh.z;
+    const real sin_theta_h = std::max<real>(0, std::sqrt(1 - cos_theta_h * cos_theta_h));
+    const real D = anisotropic_gtr2(sin_phi_h, cos_phi_h, sin_theta_h, cos_theta_h, m->ax_m, m->ay_m);
+    const real phi_i = local_phi(lwi), phi_o = local_phi(lwo);
+    const real sin_phi_i = std::sin(phi_i), cos_phi_i = std::cos(phi_i);
+    const real sin_phi_o = std::sin(phi_o), cos_phi_o = std::cos(phi_o);
+    const real tan_theta_i = local_tan_theta(lwi), tan_theta_o = local_tan_theta(lwo);
+    const real Gi = smith_anisotropic_gtr2(cos_phi_i, sin_phi_i, m->ax_m, m->ay_m, tan_theta_i);
+    const real Go = smith_anisotropic_gtr2(cos_phi_o, sin_phi_o, m->ax_m, m->ay_m, tan_theta_o);
+    if (eval) {
+      const real G = Gi * Go;
+      const real den = std::abs(4 * cos_theta_i * cos_theta_o);
+      Sp F;
+      F.r = m->f_paint.r * conductor_fresnel(m->f_eta2.r, m->f_etak2.r, cos_theta_d);
+      F.g = m->f_paint.g * conductor_fresnel(m->f_eta2.g, m->f_etak2.g, cos_theta_d);
+      F.b = m->f_paint.b * conductor_fresnel(m->f_eta2.b, m->f_etak2.b, cos_theta_d);
+      *eval = Sp(F.r * D * G / den, F.g * D * G / den, F.b * D * G / den);
+    }
+    if (pdf) *pdf = Go * D / (4 * cos_theta_o);
+  }
+  // microfacet::sample_anisotropic_gtr2_with_visible_normal (utility/microfacet.cpp:58-80)
+  V3 sample_vndf(V3 ve, real u, real v) const {
+    const real ax = m->ax_m, ay = m->ay_m;
+    const V3 vh = normalize(V3(ax * ve.x, ay * ve.y, ve.z));
+    const real lensq = vh.x * vh.x + vh.y * vh.y;
+    const V3 t1 = lensq > kEps ? divd(V3(-vh.y, vh.x, 0), std::sqrt(lensq)) : V3(1, 0, 0);
+    const V3 t2 = cross(vh, t1);
+    const real r = std::sqrt(u);
+    const real phi = 2 * kPi * v;
+    const real t_1 = r * std::cos(phi);
+    const real _t_2 = r * std::sin(phi);
+    const real sh = real(0.5) * (1 + vh.z);
+    const real t_2 = (1 - sh) * std::sqrt(1 - t_1 * t_1) + sh * _t_2;
+    const V3 nh = mulf(t1, t_1) + mulf(t2, t_2) + mulf(vh, std::sqrt(std::max(real(0), 1 - t_1 * t_1 - t_2 * t_2)));
+    return normalize(V3(ax * nh.x, ay * nh.y, std::max(real(0), nh.z)));
+  }
+  Sp metal_eval(V3 wi, V3 wo) const {
+    if (fringe(wi, wo)) return eval_fringe(wi, wo);
+    const V3 lwi = normalize(s.to_local(wi)), lwo = normalize(s.to_local(wo));
+    if (!lwi.z || !lwo.z) return Sp();
+    Sp r;
+    if (!(lwi.z <= 0 || lwo.z <= 0)) {
+      Sp e;
+      ggx(lwi, lwo, &e, nullptr);
+      r += e;
+    }
+    return r;
+  }
+  real metal_pdf(V3 wi, V3 wo) const {
+    if (fringe(wi, wo)) return pdf_fringe(wi, wo);
+    const V3 lwi = normalize(s.to_local(wi)), lwo = normalize(s.to_local(wo));
+    if (!lwi.z || !lwo.z) return 0;
+    real weight_sum = 0, pdf = 0;
+    weight_sum += 1;
+    real p = 0;
+    if (!(lwi.z <= 0 || lwo.z <= 0)) ggx(lwi, lwo, nullptr, &p);
+    pdf += 1 * p;
+    return weight_sum > 0 ? pdf / weight_sum : 0;
+  }
+  BSDFSample metal_sample(V3 wo, real u, real v, real w) const {
+    if (fringe(wo)) return sample_fringe(wo, u, v);
+    BSDFSample out;
+    const V3 lwo = normalize(s.to_local(wo));
+    if (!lwo.z) return out;
+    const real comp_sel = (u - real(0.001)) * 1;
+    if (!(comp_sel <= 1)) return out;
+    // GGXMicrofacetReflectionBXDF::sample with (v, w)
+    if (lwo.z <= 0) return out;
+    const V3 lwh = normalize(sample_vndf(lwo, v, w));
+    if (lwh.z <= 0) return out;
+    const V3 lwi0 = normalize(mulf(lwh, 2 * dot(lwo, lwh)) - lwo);
+    if (lwi0.z <= 0) return out;
+    Sp f;
+    real pdf = 0;
+    ggx(lwi0, lwo, &f, &pdf);
+    if (!(pdf > 0)) return out;  // BXDFSampleResult::is_valid (material/bxdf/bxdf.hpp:17-19)
+    const V3 lwi = normalize(lwi0);
+    pdf *= 1;
+    const V3 wi = s.to_global(lwi);
+    out.wi = wi;
+    out.f = f * normal_correct_factor(g, s, wi);
+    out.pdf = pdf;
+    return out;
+  }
+
   Sp eval(V3 wi, V3 wo) const {
+    if (m->kind == TR_MAT_METAL) return metal_eval(wi, wo);
     return m->kind == TR_MAT_PHONG ? phong_agg_eval(wi, wo) : (m->kind == TR_MAT_DISNEY12 ? disney_eval(wi, wo) : Sp());
   }
   real pdf(V3 wi, V3 wo) const {
+    if (m->kind == TR_MAT_METAL) return metal_pdf(wi, wo);
     return m->kind == TR_MAT_PHONG ? phong_agg_pdf(wi, wo) : (m->kind == TR_MAT_DISNEY12 ? disney_pdf(wi, wo) : 0);
   }
   BSDFSample sample(V3 wo, real u, real v, real w) const {
     if (m->kind == TR_MAT_GLASS) return glass_sample(wo, u);
+    if (m->kind == TR_MAT_METAL) return metal_sample(wo, u, v, w);
     return m->kind == TR_MAT_PHONG ? phong_agg_sample(wo, u, v, w) : disney_sample(wo, u, v, w);
   }
 };
@@ -1429,6 +1552,21 @@ void* orc_scene_create(const tr_scene_desc* d) {
       m.specular = spec;
       m.ns = src.ns;
       m.base = diffuse;
+    } else if (src.kind == TR_MAT_METAL) {
+      m.base = Sp(src.color[0], src.color[1], src.color[2]);
+      for (int c = 0; c < 3; ++c) {
+        // ConductorFresnelPoint(eta_outside = color, eta_inside = 1, k = the caller's k)
+        real e2 = real(1) / src.color[c];
+        e2 *= e2;
+        real ek2 = src.k[c] / src.color[c];
+        ek2 *= ek2;
+        (c == 0 ? m.f_eta2.r : c == 1 ? m.f_eta2.g : m.f_eta2.b) = e2;
+        (c == 0 ? m.f_etak2.r : c == 1 ? m.f_etak2.g : m.f_etak2.b) = ek2;
+        (c == 0 ? m.f_paint.r : c == 1 ? m.f_paint.g : m.f_paint.b) = src.eta[c];
+      }
+      const real aspect = src.anisotropic > 0 ? std::sqrt(1 - real(0.9) * src.anisotropic) : real(1);
+      m.ax_m = std::max(real(0.001), src.roughness * src.roughness / aspect);
+      m.ay_m = std::max(real(0.001), src.roughness * src.roughness * aspect);
     } else if (src.kind == TR_MAT_GLASS) {
       m.kr = Sp(src.kr[0], src.kr[1], src.kr[2]);
       m.kt_sqrt = Sp(std::sqrt(src.kt[0]), std::sqrt(src.kt[1]), std::sqrt(src.kt[2]));

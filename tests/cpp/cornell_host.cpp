@@ -76,12 +76,14 @@ bool throws(void (*fn)()) {
 
 int main(int argc, char** argv) {
   if (argc < 5) {
-    std::fprintf(stderr, "usage: %s out_prefix width height spp [render]\n", argv[0]);
+    std::fprintf(stderr, "usage: %s out_prefix width height spp [render|describe] [glass_metal]\n", argv[0]);
     return 2;
   }
   const std::string out = argv[1];
   const int W = std::atoi(argv[2]), H = std::atoi(argv[3]), spp = std::atoi(argv[4]);
   const bool render = argc > 5 && std::strcmp(argv[5], "render") == 0;
+  // the short box in metal and the tall one in glass
+  const bool glass_metal = argc > 6 && std::strcmp(argv[6], "glass_metal") == 0;
 
   // construction errors throw (src/shape/sphere.cpp:88-90)
   if (!throws([] { create_sphere(-1.0f, Transform()); }) ||
@@ -96,6 +98,9 @@ int main(int argc, char** argv) {
   auto white = create_phong_material(zero, konst(0.73f, 0.73f, 0.73f), zero, konst(1, 1, 1));
   auto red = create_phong_material(zero, konst(0.65f, 0.05f, 0.05f), zero, konst(1, 1, 1));
   auto green = create_phong_material(zero, konst(0.12f, 0.45f, 0.15f), zero, konst(1, 1, 1));
+  auto metal = create_metal(konst(0.95f, 0.64f, 0.54f), konst(0.2f, 0.92f, 1.1f), konst(3.9f, 2.45f, 2.14f),
+                            konst(0.35f, 0.35f, 0.35f), konst(0.4f, 0.4f, 0.4f));
+  auto glass = create_glass(konst(1, 1, 1), konst(1, 1, 1), konst(1.5f, 1.5f, 1.5f));
   auto vacuum = create_vacuum();
   const MediumInterface mi(vacuum);
 
@@ -116,9 +121,9 @@ int main(int argc, char** argv) {
   add(quad_mesh({1, -1, -1}, {1, -1, 1}, {1, 1, 1}, {1, 1, -1}, {-1, 0, 0}), id, green, black);       // right
   const float pi = 3.14159265358979f;
   add(cube_mesh(), translate({-0.35f, -0.7f, -0.3f}) * rotate_y(15.0f * pi / 180.0f) * scale(0.6f, 0.6f, 0.6f),
-      white, black);
+      glass_metal ? metal : white, black);
   add(cube_mesh(), translate({0.35f, -0.4f, 0.3f}) * rotate_y(-18.0f * pi / 180.0f) * scale(0.6f, 1.2f, 0.6f),
-      white, black);
+      glass_metal ? glass : white, black);
   add(quad_mesh({-0.25f, 0.99f, -0.25f}, {0.25f, 0.99f, -0.25f}, {0.25f, 0.99f, 0.25f}, {-0.25f, 0.99f, 0.25f},
                 {0, -1, 0}),
       id, white, Spectrum(17, 12, 4));

@@ -70,6 +70,21 @@ def test_cornell_glass(gpu, min_depth):
     assert abs(a.mean() - b.mean()) <= 0.01 * b.mean()
 
 
+@pytest.mark.parametrize("min_depth", [8, 2])
+def test_cornell_metal(gpu, min_depth):
+    """The short box in metal (anisotropic GGX, painted conductor Fresnel,
+    visible-normal sampling) with light sampling and MIS like the other
+    non-delta materials."""
+    sc, cam, filt, par = scenes.cornell(64, 64, 8, max_depth=8, min_depth=min_depth, metal=True)
+    orc = oracle.Oracle(sc, "port")
+    orc.set_camera(cam, filt)
+    ref = orc.render(par)
+    gpu.upload(sc)
+    out, stats = gpu.render(cam, filt, par)
+    assert stats.samples == 64 * 64 * 8
+    _compare(out, ref, 0.8)
+
+
 def test_cornell(gpu):
     sc, cam, filt, par = scenes.cornell(64, 64, 8)
     orc = oracle.Oracle(sc, "port")
@@ -114,13 +129,15 @@ def test_fp64_accumulation(gpu):
     assert np.allclose(out32, out64, rtol=1e-5, atol=1e-6)
 
 
-@pytest.mark.parametrize("maker", ["cornell", "disney", "glass"])
+@pytest.mark.parametrize("maker", ["cornell", "disney", "glass", "metal"])
 def test_replay_recorded_rays(gpu, maker):
     """Every trace the oracle's integrator makes, replayed on the GPU."""
     if maker == "cornell":
         sc, cam, filt, par = scenes.cornell(32, 32, 4)
     elif maker == "glass":
         sc, cam, filt, par = scenes.cornell(32, 32, 4, max_depth=8, min_depth=2, glass=True)
+    elif maker == "metal":
+        sc, cam, filt, par = scenes.cornell(32, 32, 4, max_depth=8, min_depth=2, glass=True, metal=True)
     else:
         sc, cam, filt, par = scenes.disney_grid(32, 32, 2)
     orc = oracle.Oracle(sc, "port")
@@ -190,7 +207,7 @@ def test_occluded_room_small(gpu):
     _compare(out, ref, 0.8)
 
 
-@pytest.mark.parametrize("maker", ["cornell", "room", "glass"])
+@pytest.mark.parametrize("maker", ["cornell", "room", "glass", "metal"])
 def test_converged_fp64_image_within_one_percent(gpu, maker):
     """The image bar: a 4096-spp render accumulated in FP64 on the GPU is
     within 1% mean relative error of the oracle's 4096-spp FP64 render of
@@ -201,6 +218,9 @@ def test_converged_fp64_image_within_one_percent(gpu, maker):
     elif maker == "glass":
         sc, cam, filt, _ = scenes.cornell(24, 24, 1, glass=True)
         par = scenes.make_params(24, 24, 4096, 8, 8)
+    elif maker == "metal":
+        sc, cam, filt, _ = scenes.cornell(24, 24, 1, metal=True)
+        par = scenes.make_params(24, 24, 4096, 5, 5)
     else:
         sc, cam, filt, _ = scenes.occluded_room(20, 16, 1, n_tris=5000)
         par = scenes.make_params(20, 16, 4096, 3, 10)

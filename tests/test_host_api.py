@@ -96,12 +96,33 @@ def test_factory_scene_description(program, tmp_path):
     assert abs(cam.film_aspect - 1.0) < 1e-7
 
 
+def test_factory_glass_and_metal_materials(program, tmp_path):
+    """create_metal and create_glass records as the renderer receives them."""
+    from tracer_gb300.abi import TR_MAT_GLASS, TR_MAT_METAL
+    out = str(tmp_path / "c")
+    r = subprocess.run([program, out, "16", "16", "1", "describe", "glass_metal"], check=True, capture_output=True,
+                       text=True)
+    assert "36 triangles, 2 lights, 5 materials" in r.stdout
+    sb, _ = _read_desc(out + ".desc")
+    kinds = [m.rec.kind for m in sb.materials]
+    metal = sb.materials[kinds.index(TR_MAT_METAL)].rec
+    glass = sb.materials[kinds.index(TR_MAT_GLASS)].rec
+    assert np.allclose(list(metal.color), [0.95, 0.64, 0.54]) and np.allclose(list(metal.k), [3.9, 2.45, 2.14])
+    assert np.allclose(list(metal.eta), [0.2, 0.92, 1.1])
+    assert abs(metal.roughness - 0.35) < 1e-7 and abs(metal.anisotropic - 0.4) < 1e-7
+    assert abs(glass.ior - 1.5) < 1e-7 and np.allclose(list(glass.kt), [1, 1, 1])
+    # the metal box is the short one, the glass box the tall one
+    assert sb.prim_material[10] == kinds.index(TR_MAT_METAL)
+    assert sb.prim_material[22] == kinds.index(TR_MAT_GLASS)
+
+
 @pytest.mark.gpu
-def test_factory_scene_renders_like_the_oracle(program, tmp_path):
+@pytest.mark.parametrize("variant", ["", "glass_metal"])
+def test_factory_scene_renders_like_the_oracle(program, tmp_path, variant):
     W, H, S = 48, 40, 4
     out = str(tmp_path / "c")
-    r = subprocess.run([program, out, str(W), str(H), str(S), "render"], check=True, capture_output=True,
-                       text=True)
+    r = subprocess.run([program, out, str(W), str(H), str(S), "render"] + ([variant] if variant else []),
+                       check=True, capture_output=True, text=True)
     assert f"{W * H * S} samples" in r.stdout
     sb, cam = _read_desc(out + ".desc")
     sums = np.fromfile(out + ".sums", np.float64).reshape(H, W, 4)
@@ -115,7 +136,12 @@ def test_factory_scene_renders_like_the_oracle(program, tmp_path):
     close = (rel.max(-1) <= 1e-5).mean()
     mre = float(np.mean(np.abs(a - b) / np.maximum(np.abs(b), 1e-3)))
     print(f"pixels within 1e-5: {close:.4f}  MRE {mre:.2e}")
-    assert close >= 0.9 and mre < 0.01
+    if variant:
+        # refraction amplifies last-bit differences of the transcendentals
+        # into other paths for a few samples: most pixels and the image mean agree
+        assert close >= 0.8 and abs(a.mean() - b.mean()) <= 0.01 * b.mean()
+    else:
+        assert close >= 0.9 and mre < 0.01
     # RenderTarget = sum / weight (Film::write_render_target)
     want = (sums[..., :3].astype(np.float32) / sums[..., 3:4].astype(np.float32))
     assert np.array_equal(rgb, want)

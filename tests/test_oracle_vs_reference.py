@@ -78,6 +78,17 @@ def test_glass_cornell(min_depth):
     assert np.array_equal(bits(port.render(par)), bits(ref.render(par)))
 
 
+@pytest.mark.parametrize("min_depth,glass", [(8, False), (2, False), (2, True)])
+def test_metal_cornell(min_depth, glass):
+    """Metal (an anisotropic GGX conductor with the painted Fresnel that
+    create_metal builds), alone and beside glass."""
+    sc, cam, filt, par = scenes.cornell(32, 24, 4, max_depth=8, min_depth=min_depth, glass=glass, metal=True)
+    port, ref = oracle.Oracle(sc, "port"), oracle.Oracle(sc, "reference")
+    port.set_camera(cam, filt)
+    ref.set_camera(cam, filt)
+    assert np.array_equal(bits(port.render(par)), bits(ref.render(par)))
+
+
 def test_make_ray():
     for o, d in (((0, 0, 0), (1, 2, 3)), ((1, -1, 0.5), (1e-9, 1, 0)), ((0, 0, 0), (-0.0, 0.0, -3))):
         a = oracle.make_ray("port", o, d, 0.0, 1.0)

@@ -23,6 +23,7 @@ TR_ERR_UNSUPPORTED = 8
 TR_MAT_PHONG = 0
 TR_MAT_DISNEY12 = 1
 TR_MAT_GLASS = 2
+TR_MAT_METAL = 3
 
 f32p = C.POINTER(C.c_float)
 f64p = C.POINTER(C.c_double)
@@ -55,7 +56,8 @@ class TrMaterial(C.Structure):
                 ("subsurface", C.c_float), ("metallic", C.c_float), ("specular", C.c_float),
                 ("specular_tint", C.c_float), ("roughness", C.c_float), ("anisotropic", C.c_float),
                 ("sheen", C.c_float), ("sheen_tint", C.c_float), ("clearcoat", C.c_float),
-                ("clearcoat_gloss", C.c_float), ("kr", C.c_float * 3), ("kt", C.c_float * 3), ("ior", C.c_float)]
+                ("clearcoat_gloss", C.c_float), ("kr", C.c_float * 3), ("kt", C.c_float * 3), ("ior", C.c_float),
+                ("color", C.c_float * 3), ("eta", C.c_float * 3), ("k", C.c_float * 3)]
 
 
 class TrSceneDesc(C.Structure):
@@ -125,7 +127,7 @@ def ptr(a: np.ndarray | None, ctype):
 @dataclass
 class Material:
     """One tr_material. kind=TR_MAT_PHONG uses ka/kd/ks/ns; Disney12 base_color .. clearcoat_gloss;
-    TR_MAT_GLASS kr/kt/ior."""
+    TR_MAT_GLASS kr/kt/ior; TR_MAT_METAL color/eta/k with roughness/anisotropic."""
     kind: int = TR_MAT_PHONG
     ka: tuple = (0.0, 0.0, 0.0)
     kd: tuple = (0.0, 0.0, 0.0)
@@ -145,6 +147,9 @@ class Material:
     kr: tuple = (0.0, 0.0, 0.0)
     kt: tuple = (0.0, 0.0, 0.0)
     ior: float = 1.0
+    color: tuple = (0.0, 0.0, 0.0)
+    eta: tuple = (0.0, 0.0, 0.0)
+    k: tuple = (0.0, 0.0, 0.0)
 
     def to_c(self) -> TrMaterial:
         m = TrMaterial()
@@ -159,6 +164,9 @@ class Material:
             setattr(m, k, getattr(self, k))
         m.kr[:] = self.kr
         m.kt[:] = self.kt
+        m.color[:] = self.color
+        m.eta[:] = self.eta
+        m.k[:] = self.k
         return m
 
 

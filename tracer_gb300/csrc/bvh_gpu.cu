@@ -473,7 +473,11 @@ tr_status upload_device_built(tr_ctx* ctx) {
   sc.num_scenes = (int)nsc;
   sc.max_lights = max_lights;
   sc.has_glass = 0;
-  for (const DMat& m : hs.mats) sc.has_glass |= m.kind == MAT_GLASS;
+  sc.has_metal = 0;
+  for (const DMat& m : hs.mats) {
+    sc.has_glass |= m.kind == MAT_GLASS;
+    sc.has_metal |= m.kind == MAT_METAL;
+  }
   ctx->has_scene = true;
   return TR_OK;
 }

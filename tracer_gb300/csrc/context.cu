@@ -64,6 +64,30 @@ DMat derive_material(const tr_material& m) {
     d.diffuse_coef = mk3(diffuse.x / kPi, diffuse.y / kPi, diffuse.z / kPi);
     d.specular = spec;
     d.ns = m.ns;
+  } else if (m.kind == TR_MAT_METAL) {
+    // create_metal(color, eta, k) hands over to Metal(color, k, eta), whose
+    // shading builds PaintedConductorFresnelPoint(color, 1, eta, k) with
+    // parameters (eta_outside, eta_inside, k, paint): eta_outside = color,
+    // eta_inside = 1, conductor k = the caller's k, paint = the caller's eta
+    d.kind = MAT_METAL;
+    d.base = mk3(m.color[0], m.color[1], m.color[2]);
+    d.albedo = d.base;  // AggregateBSDF<1>(..., color)
+    float e2[3], ek2[3];
+    for (int c = 0; c < 3; ++c) {
+      e2[c] = 1.0f / m.color[c];
+      e2[c] *= e2[c];
+      ek2[c] = m.k[c] / m.color[c];
+      ek2[c] *= ek2[c];
+    }
+    d.f_eta2 = mk3(e2[0], e2[1], e2[2]);
+    d.f_etak2 = mk3(ek2[0], ek2[1], ek2[2]);
+    d.f_paint = mk3(m.eta[0], m.eta[1], m.eta[2]);
+    d.roughness = m.roughness;
+    d.anisotropic = m.anisotropic;
+    // GGXMicrofacetReflectionBXDF (src/material/bxdf/microfacet_refl_bxdf.cpp:6-11)
+    const float aspect = m.anisotropic > 0.0f ? std::sqrt(1.0f - 0.9f * m.anisotropic) : 1.0f;
+    d.ax = smax(0.001f, m.roughness * m.roughness / aspect);
+    d.ay = smax(0.001f, m.roughness * m.roughness * aspect);
   } else if (m.kind == TR_MAT_GLASS) {
     d.kind = MAT_GLASS;
     d.kr = mk3(m.kr[0], m.kr[1], m.kr[2]);
@@ -310,7 +334,11 @@ tr_status upload_device_tables(tr_ctx* ctx) {
   sc.num_scenes = (int)nsc;
   sc.max_lights = max_lights;
   sc.has_glass = 0;
-  for (const DMat& m : hs.mats) sc.has_glass |= m.kind == MAT_GLASS;
+  sc.has_metal = 0;
+  for (const DMat& m : hs.mats) {
+    sc.has_glass |= m.kind == MAT_GLASS;
+    sc.has_metal |= m.kind == MAT_METAL;
+  }
   ctx->has_scene = true;
   return TR_OK;
 }
@@ -486,7 +514,7 @@ static tr_status build_host_scene(tr_ctx* ctx, const tr_scene_desc* d, HostScene
       return set_err(ctx, TR_ERR_ARG, "triangle index out of range");
   for (uint32_t m = 0; m < d->num_materials; ++m)
     if (d->materials[m].kind != TR_MAT_PHONG && d->materials[m].kind != TR_MAT_DISNEY12 &&
-        d->materials[m].kind != TR_MAT_GLASS)
+        d->materials[m].kind != TR_MAT_GLASS && d->materials[m].kind != TR_MAT_METAL)
       return set_err(ctx, TR_ERR_ARG, "unknown material kind");
   for (uint32_t s = 0; s < d->num_spheres; ++s)
     if (!(d->sphere_radius[s] > 0.0f)) return set_err(ctx, TR_ERR_ARG, "invalid sphere radius");  // sphere.cpp:88-90

@@ -417,6 +417,20 @@ RC<Material> create_glass(RC<const Texture2D> map_kr, RC<const Texture2D> map_kt
   return std::make_shared<Material>(m);
 }
 
+RC<Material> create_metal(RC<const Texture2D> color, RC<const Texture2D> eta, RC<const Texture2D> k,
+                          RC<const Texture2D> roughness, RC<const Texture2D> anisotropic) {
+  tr_material m{};
+  m.kind = TR_MAT_METAL;
+  const Spectrum c = tex(color, "color"), e = tex(eta, "eta"), kk = tex(k, "k");
+  const float cv[3] = {c.r, c.g, c.b}, ev[3] = {e.r, e.g, e.b}, kv[3] = {kk.r, kk.g, kk.b};
+  std::memcpy(m.color, cv, sizeof(cv));
+  std::memcpy(m.eta, ev, sizeof(ev));
+  std::memcpy(m.k, kv, sizeof(kv));
+  m.roughness = tex_s(roughness, "roughness");
+  m.anisotropic = tex_s(anisotropic, "anisotropic");
+  return std::make_shared<Material>(m);
+}
+
 RC<Material> create_disney_brdf(RC<const Texture2D> base_color, RC<const Texture2D> subsurface,
                                 RC<const Texture2D> metallic, RC<const Texture2D> specular,
                                 RC<const Texture2D> specular_tint, RC<const Texture2D> roughness,

@@ -63,15 +63,18 @@ constexpr int kMaxSpecularDepth = 20;
 __device__ __forceinline__ int path_depth(float w) { return __float_as_int(w) & 0xffff; }
 __device__ __forceinline__ int spec_depth(float w) { return __float_as_int(w) >> 16; }
 
+// light-sample queue of a material kind (glass has none)
+__host__ __device__ constexpr int nee_index(int kind) { return kind == MAT_METAL ? 2 : kind; }
+
 enum : int {  // counter slots
   C_EXT = 0,      // 2: extend queue sizes (double-buffered)
   C_ACT = 2,      // 2: live-slot list sizes
   C_SH = 4,       // shadow queue size
-  C_MAT = 5,      // 3: per-material hit queue sizes (Phong, Disney12, glass)
-  C_NEE = 8,      // 2: per-material light-sample queue sizes (glass has none)
-  C_FEXT = 10,    // extend kernel's work-fetch position
-  C_FSH = 11,     // shadow kernel's work-fetch position
-  C_TB = 12,      // guiding training records written (whole render)
+  C_MAT = 5,      // 4: per-material hit queue sizes (Phong, Disney12, glass, metal)
+  C_NEE = 9,      // 3: light-sample queue sizes (Phong, Disney12, metal; glass has none)
+  C_FEXT = 12,    // extend kernel's work-fetch position
+  C_FSH = 13,     // shadow kernel's work-fetch position
+  C_TB = 14,      // guiding training records written (whole render)
   C_ERR = 15,     // traversal error word
 };
 
@@ -117,7 +120,7 @@ struct Launch {
   int* q_ext[2];
   int* q_act[2];
   int* q_mat[kMatKinds];
-  int* q_nee[2];
+  int* q_nee[kNeeKinds];
   int* q_sh;
   unsigned int* ctr;
   unsigned long long* stats;  // samples, extend rays, shadow rays, shade items, visit counts (4-7)
@@ -555,14 +558,17 @@ template <int KIND>
 struct MatOps {
   static __device__ __forceinline__ BsdfSample sample(const Bsdf& b, f3 wo, float u, float v, float w) {
     if (KIND == MAT_GLASS) return b.glass_sample(wo, u);
+    if (KIND == MAT_METAL) return b.metal_sample(wo, u, v, w);
     return KIND == MAT_PHONG ? b.phong_sample_agg(wo, u, v, w) : b.disney_sample(wo, u, v, w);
   }
   static __device__ __forceinline__ f3 eval(const Bsdf& b, f3 wi, f3 wo) {
     if (KIND == MAT_GLASS) return mk3(0.0f, 0.0f, 0.0f);
+    if (KIND == MAT_METAL) return b.metal_eval(wi, wo);
     return KIND == MAT_PHONG ? b.phong_eval_agg(wi, wo) : b.disney_eval(wi, wo);
   }
   static __device__ __forceinline__ float pdf(const Bsdf& b, f3 wi, f3 wo) {
     if (KIND == MAT_GLASS) return 0.0f;
+    if (KIND == MAT_METAL) return b.metal_pdf(wi, wo);
     return KIND == MAT_PHONG ? b.phong_pdf_agg(wi, wo) : b.disney_pdf(wi, wo);
   }
 };
@@ -735,7 +741,7 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
       const float lu = Pcg::next(st), lv = Pcg::next(st);
       Pcg::skip<3>(st);
       P.NU[item] = make_float2(lu, lv);
-      P.q_nee[KIND][append(P.ctr + C_NEE + KIND)] = item;
+      P.q_nee[nee_index(KIND)][append(P.ctr + C_NEE + nee_index(KIND))] = item;
     }
     float4* sc = P.SC + 7 * (size_t)slot;
     sc[0] = make_float4(is.pos.x, is.pos.y, is.pos.z, __int_as_float(mat));
@@ -921,9 +927,9 @@ __global__ void __launch_bounds__(128) k_glass(Launch P, int cur) {
 // the contribution when it is blocked.
 template <int KIND>
 __global__ void __launch_bounds__(128) k_nee(Launch P) {
-  const unsigned int n = P.ctr[C_NEE + KIND];
+  const unsigned int n = P.ctr[C_NEE + nee_index(KIND)];
   for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int item = P.q_nee[KIND][i];
+    const int item = P.q_nee[nee_index(KIND)][i];
     const int slot = item / P.nl_max, l = item - slot * P.nl_max;
     const float4* sc = P.SC + 7 * (size_t)slot;
     const float4 a = sc[0], b = sc[1], c = sc[2], d = sc[3], e = sc[4], f = sc[5], g = sc[6];
@@ -1019,7 +1025,7 @@ tr_status reserve_render(tr_ctx* ctx, int n, int nl) {
                {&rb->HC, N * f4},           {&rb->HM, N * f4},          {&rb->SC, N * 7 * f4},
                {&rb->NU, N * NL * 8},       {&rb->SH, N * NL * 3 * f4}, {&rb->acc, N * 32},
                {&rb->q_ext, 2 * 2 * N * 4}, {&rb->q_act, 2 * N * 4},   {&rb->q_mat, kMatKinds * N * 4},
-               {&rb->q_nee, 2 * N * NL * 4}, {&rb->q_sh, N * NL * 4},  {&rb->ctr, 64},
+               {&rb->q_nee, kNeeKinds * N * NL * 4}, {&rb->q_sh, N * NL * 4},  {&rb->ctr, 64},
                {&rb->stats, 64}};
   for (auto& nd : needs) {
     cudaError_t e = nd.b->reserve(nd.bytes);
@@ -1159,8 +1165,8 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   for (int k = 0; k < 2; ++k) {
     P.q_ext[k] = rb->q_ext.as<int>() + (size_t)k * 2 * n;
     P.q_act[k] = rb->q_act.as<int>() + (size_t)k * n;
-    P.q_nee[k] = rb->q_nee.as<int>() + (size_t)k * n * std::max(nl, 1);
   }
+  for (int k = 0; k < kNeeKinds; ++k) P.q_nee[k] = rb->q_nee.as<int>() + (size_t)k * n * std::max(nl, 1);
   for (int k = 0; k < kMatKinds; ++k) P.q_mat[k] = rb->q_mat.as<int>() + (size_t)k * n;
   P.q_sh = rb->q_sh.as<int>();
   P.ctr = rb->ctr.as<unsigned int>();
@@ -1269,7 +1275,7 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     // material and light-sample counts and the fetch positions
     cudaMemsetAsync(P.ctr + C_EXT + nxt, 0, 4, st);
     cudaMemsetAsync(P.ctr + C_ACT + nxt, 0, 4, st);
-    cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 8, st);  // C_SH, C_MAT x3, C_NEE x2, C_FEXT, C_FSH
+    cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 10, st);  // C_SH, C_MAT x4, C_NEE x3, C_FEXT, C_FSH
     mark();
     k_logic<<<grid, 128, 0, st>>>(P, cur);
     if (P.guide_alpha > 0.0f) {
@@ -1284,10 +1290,12 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     mark();
     k_material<MAT_DISNEY12><<<grid, 128, 0, st>>>(P, cur);
     if (P.sc.has_glass) k_glass<<<grid, 128, 0, st>>>(P, cur);  // timed with Disney12
+    if (P.sc.has_metal) k_material<MAT_METAL><<<grid, 128, 0, st>>>(P, cur);
     mark();
     k_nee<MAT_PHONG><<<grid, 128, 0, st>>>(P);
     mark();
     k_nee<MAT_DISNEY12><<<grid, 128, 0, st>>>(P);
+    if (P.sc.has_metal) k_nee<MAT_METAL><<<grid, 128, 0, st>>>(P);  // timed with Disney12
     mark();
     if (count && wide) k_shadow<true, true><<<grid_sh, 128, 0, st>>>(P);
     else if (count) k_shadow<true><<<grid_sh, 128, 0, st>>>(P);
@@ -1490,13 +1498,13 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   const size_t oP = L.take(5 * N * f4), oRng = L.take(N * 8), oM = L.take(3 * N * f4), oH = L.take(2 * N * f4),
                oSC = L.take(N * 7 * f4), oNU = L.take(N * NL * 8), oSH = L.take(N * NL * 3 * f4),
                oQe = L.take(2 * 2 * N * 4), oQa = L.take(2 * N * 4), oQm = L.take(kMatKinds * N * 4),
-               oQn = L.take(2 * N * NL * 4), oQs = L.take(N * NL * 4), oCtr = L.take(64), oSt = L.take(64),
+               oQn = L.take(kNeeKinds * N * NL * 4), oQs = L.take(N * NL * 4), oCtr = L.take(64), oSt = L.take(64),
                oJob = L.take(sizeof(JobDev));
   if (npix > (1ll << 24) || L.off > kNoAllocScratchBytes) {
     char msg[256];
     std::snprintf(msg, sizeof(msg),
                   "film %dx%d with %d lights needs %zu bytes of scratch; tr_render_dev_noalloc has %zu "
-                  "(about 316 + 68 * lights bytes per pixel)",
+                  "(about 316 + 72 * lights bytes per pixel)",
                   prm->width, prm->height, nl, (size_t)L.off, kNoAllocScratchBytes);
     return set_err(ctx, TR_ERR_ARG, msg);
   }
@@ -1561,8 +1569,8 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   for (int k = 0; k < 2; ++k) {
     P.q_ext[k] = qe + (size_t)k * 2 * N;
     P.q_act[k] = qa + (size_t)k * N;
-    P.q_nee[k] = qn + (size_t)k * N * NL;
   }
+  for (int k = 0; k < kNeeKinds; ++k) P.q_nee[k] = qn + (size_t)k * N * NL;
   for (int k = 0; k < kMatKinds; ++k) P.q_mat[k] = qm + (size_t)k * N;
   P.q_sh = reinterpret_cast<int*>(base + oQs);
   P.ctr = reinterpret_cast<unsigned int*>(base + oCtr);
@@ -1592,13 +1600,15 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
     k_extend<false><<<grid_ext, 128, 0, st>>>(P, cur);
     NCHK(cudaMemsetAsync(P.ctr + C_EXT + nxt, 0, 4, st));
     NCHK(cudaMemsetAsync(P.ctr + C_ACT + nxt, 0, 4, st));
-    NCHK(cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 8, st));  // C_SH, C_MAT x3, C_NEE x2, C_FEXT, C_FSH
+    NCHK(cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 10, st));  // C_SH, C_MAT x4, C_NEE x3, C_FEXT, C_FSH
     k_logic<<<grid, 128, 0, st>>>(P, cur);
     k_material<MAT_PHONG><<<grid, 128, 0, st>>>(P, cur);
     k_material<MAT_DISNEY12><<<grid, 128, 0, st>>>(P, cur);
     if (P.sc.has_glass) k_glass<<<grid, 128, 0, st>>>(P, cur);
+    if (P.sc.has_metal) k_material<MAT_METAL><<<grid, 128, 0, st>>>(P, cur);
     k_nee<MAT_PHONG><<<grid, 128, 0, st>>>(P);
     k_nee<MAT_DISNEY12><<<grid, 128, 0, st>>>(P);
+    if (P.sc.has_metal) k_nee<MAT_METAL><<<grid, 128, 0, st>>>(P);
     if (wide) k_shadow<false, true><<<grid_sh, 128, 0, st>>>(P);
     else k_shadow<false><<<grid_sh, 128, 0, st>>>(P);
   }

@@ -78,8 +78,9 @@ struct DTriShade {
   int pad[3];
 };
 
-enum { MAT_PHONG = 0, MAT_DISNEY12 = 1, MAT_GLASS = 2 };
-constexpr int kMatKinds = 3;
+enum { MAT_PHONG = 0, MAT_DISNEY12 = 1, MAT_GLASS = 2, MAT_METAL = 3 };
+constexpr int kMatKinds = 4;
+constexpr int kNeeKinds = 3;  // kinds with light sampling: Phong, Disney12, metal (glass is a delta BSDF)
 
 // Phong: the AggregateBSDF<2> that Phong::shading builds (src/material/phong.cpp:29-70)
 // Disney12: the eleven parameters (src/material/disney_brdf.cpp:278-302)
@@ -99,6 +100,9 @@ struct DMat {
   // Glass (src/material/glass.cpp:117-140): reflect colour, sqrt(transmit colour), ior
   f3 kr, kt_sqrt;
   float ior;
+  // Metal (src/material/metal.cpp:33-56): painted conductor Fresnel constants
+  // (squared ratios and paint, per channel); ax, ay above hold its GGX alphas
+  f3 f_eta2, f_etak2, f_paint;
 };
 
 // A diffuse area light on a triangle (src/light/diffuse_light.cpp:44-60)
@@ -136,6 +140,7 @@ struct DScene {
   int num_scenes;
   int max_lights;  // most lights of one scene
   int has_glass;   // some material is a delta BSDF (glass)
+  int has_metal;   // some material is metal
 };
 
 }  // namespace trg

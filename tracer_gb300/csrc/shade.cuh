@@ -177,6 +177,23 @@ struct BsdfSample {
   __device__ __forceinline__ bool valid() const { return pdf > 0.0f && !black(f); }  // core/bsdf.hpp:21-23
 };
 
+// ConductorFresnelPoint::evaluate (src/material/utility/fresnel_point.hpp:47-66), one channel
+__device__ __forceinline__ float conductor_fresnel(float eta_2, float eta_k_2, float cos_theta_i) {
+  if (cos_theta_i <= 0.0f) return 0.0f;
+  const float cos2 = cos_theta_i * cos_theta_i;
+  const float sin2 = fmaxf(0.0f, 1.0f - cos2);
+  const float t0 = eta_2 - eta_k_2 - sin2;
+  const float a2b2 = sqrtf(t0 * t0 + 4.0f * eta_2 * eta_k_2);
+  const float t1 = a2b2 + cos2;
+  const float a = sqrtf(0.5f * (a2b2 + t0));
+  const float t2 = 2.0f * cos_theta_i * a;
+  const float rs = (t1 - t2) / (t1 + t2);
+  const float t3 = cos2 * a2b2 + sin2 * sin2;
+  const float t4 = t2 * sin2;
+  const float rp = rs * (t3 - t4) / (t3 + t4);
+  return 0.5f * (rp + rs);
+}
+
 // dielectric_fresnel (src/utility/reflection.hpp:16-40)
 __device__ __forceinline__ float dielectric_fresnel(float eta_i, float eta_o, float cos_theta_i) {
   if (cos_theta_i < 0.0f) {
@@ -616,16 +633,109 @@ struct Bsdf {
     return out;
   }
 
+  // ---- Metal: AggregateBSDF<1> (src/material/aggregate_bsdf.hpp:36-118) of one
+  // GGXMicrofacetReflectionBXDF (src/material/bxdf/microfacet_refl_bxdf.cpp:13-78), weight 1
+  __device__ void ggx(f3 lwi, f3 lwo, f3* eval, float* pdf) const {
+    const float cos_theta_i = lwi.z, cos_theta_o = lwo.z;
+    const f3 lwh = normalize(lwi + lwo);
+    const float cos_theta_d = dot(lwi, lwh);
+    float sin_phi_h, cos_phi_h, sin_phi_i, cos_phi_i, sin_phi_o, cos_phi_o;
+    sincosf(local_phi(lwh), &sin_phi_h, &cos_phi_h);
+    const float cos_theta_h = lwh.z;
+    float sin_theta_h = sqrtf(1.0f - cos_theta_h * cos_theta_h);
+    sin_theta_h = 0.0f < sin_theta_h ? sin_theta_h : 0.0f;  // std::max<real>(0, x)
+    const float D = anisotropic_gtr2(sin_phi_h, cos_phi_h, sin_theta_h, cos_theta_h, m->ax, m->ay);
+    sincosf(local_phi(lwi), &sin_phi_i, &cos_phi_i);
+    sincosf(local_phi(lwo), &sin_phi_o, &cos_phi_o);
+    const float Gi = smith_aniso_gtr2(cos_phi_i, sin_phi_i, m->ax, m->ay, local_tan_theta(lwi));
+    const float Go = smith_aniso_gtr2(cos_phi_o, sin_phi_o, m->ax, m->ay, local_tan_theta(lwo));
+    if (eval) {
+      const float G = Gi * Go;
+      const float den = fabsf(4.0f * cos_theta_i * cos_theta_o);
+      const float Fr = m->f_paint.x * conductor_fresnel(m->f_eta2.x, m->f_etak2.x, cos_theta_d);
+      const float Fg = m->f_paint.y * conductor_fresnel(m->f_eta2.y, m->f_etak2.y, cos_theta_d);
+      const float Fb = m->f_paint.z * conductor_fresnel(m->f_eta2.z, m->f_etak2.z, cos_theta_d);
+      *eval = mk3(Fr * D * G / den, Fg * D * G / den, Fb * D * G / den);
+    }
+    if (pdf) *pdf = Go * D / (4.0f * cos_theta_o);
+  }
+  // microfacet::sample_anisotropic_gtr2_with_visible_normal (src/material/utility/microfacet.cpp:58-80)
+  __device__ f3 sample_vndf(f3 ve, float u, float v) const {
+    const float ax = m->ax, ay = m->ay;
+    const f3 vh = normalize(mk3(ax * ve.x, ay * ve.y, ve.z));
+    const float lensq = vh.x * vh.x + vh.y * vh.y;
+    const f3 t1 = lensq > kEps ? divd(mk3(-vh.y, vh.x, 0.0f), (double)sqrtf(lensq)) : mk3(1.0f, 0.0f, 0.0f);
+    const f3 t2 = cross(vh, t1);
+    const float r = sqrtf(u);
+    float sp, cp;
+    sincosf(2.0f * kPi * v, &sp, &cp);
+    const float t_1 = r * cp;
+    const float t_2a = r * sp;
+    const float sh = 0.5f * (1.0f + vh.z);
+    const float t_2 = (1.0f - sh) * sqrtf(1.0f - t_1 * t_1) + sh * t_2a;
+    const float q = 1.0f - t_1 * t_1 - t_2 * t_2;
+    const f3 nh = scale(t1, t_1) + scale(t2, t_2) + scale(vh, sqrtf(0.0f < q ? q : 0.0f));
+    return normalize(mk3(ax * nh.x, ay * nh.y, 0.0f < nh.z ? nh.z : 0.0f));
+  }
+  __device__ f3 metal_eval(f3 wi, f3 wo) const {
+    if (fringe(wi) | fringe(wo)) return eval_fringe(wi, wo);
+    const f3 lwi = normalize(to_local(s, wi)), lwo = normalize(to_local(s, wo));
+    if (!lwi.z || !lwo.z) return mk3(0.0f, 0.0f, 0.0f);
+    f3 r = mk3(0.0f, 0.0f, 0.0f);
+    if (!(lwi.z <= 0.0f || lwo.z <= 0.0f)) {
+      f3 e;
+      ggx(lwi, lwo, &e, nullptr);
+      r = r + e;
+    }
+    return r;
+  }
+  __device__ float metal_pdf(f3 wi, f3 wo) const {
+    if (fringe(wi) | fringe(wo)) return pdf_fringe(wi, wo);
+    const f3 lwi = normalize(to_local(s, wi)), lwo = normalize(to_local(s, wo));
+    if (!lwi.z || !lwo.z) return 0.0f;
+    float p = 0.0f;
+    if (!(lwi.z <= 0.0f || lwo.z <= 0.0f)) ggx(lwi, lwo, nullptr, &p);
+    return (1.0f * p) / 1.0f;
+  }
+  __device__ BsdfSample metal_sample(f3 wo, float u, float v, float w) const {
+    if (fringe(wo)) return sample_fringe(wo, u, v);
+    BsdfSample out;
+    out.pdf = 0.0f;
+    out.f = mk3(0.0f, 0.0f, 0.0f);
+    out.wi = out.f;
+    const f3 lwo = normalize(to_local(s, wo));
+    if (!lwo.z) return out;
+    if (!((u - 0.001f) * 1.0f <= 1.0f)) return out;
+    if (lwo.z <= 0.0f) return out;
+    const f3 lwh = normalize(sample_vndf(lwo, v, w));
+    if (lwh.z <= 0.0f) return out;
+    const f3 lwi0 = normalize(scale(lwh, 2.0f * dot(lwo, lwh)) - lwo);
+    if (lwi0.z <= 0.0f) return out;
+    f3 f;
+    float pdf = 0.0f;
+    ggx(lwi0, lwo, &f, &pdf);
+    if (!(pdf > 0.0f)) return out;  // BXDFSampleResult::is_valid
+    const f3 lwi = normalize(lwi0);
+    const f3 wi = to_global(s, lwi);
+    out.wi = wi;
+    out.f = muls(f, normal_correct(g, s, wi));
+    out.pdf = pdf * 1.0f;
+    return out;
+  }
+
   __device__ __forceinline__ f3 eval(f3 wi, f3 wo) const {
     if (m->kind == MAT_GLASS) return mk3(0.0f, 0.0f, 0.0f);
+    if (m->kind == MAT_METAL) return metal_eval(wi, wo);
     return m->kind == MAT_PHONG ? phong_eval_agg(wi, wo) : disney_eval(wi, wo);
   }
   __device__ __forceinline__ float pdf(f3 wi, f3 wo) const {
     if (m->kind == MAT_GLASS) return 0.0f;
+    if (m->kind == MAT_METAL) return metal_pdf(wi, wo);
     return m->kind == MAT_PHONG ? phong_pdf_agg(wi, wo) : disney_pdf(wi, wo);
   }
   __device__ __forceinline__ BsdfSample sample(f3 wo, float u, float v, float w) const {
     if (m->kind == MAT_GLASS) return glass_sample(wo, u);
+    if (m->kind == MAT_METAL) return metal_sample(wo, u, v, w);
     return m->kind == MAT_PHONG ? phong_sample_agg(wo, u, v, w) : disney_sample(wo, u, v, w);
   }
 };

@@ -23,7 +23,7 @@ import math
 
 import numpy as np
 
-from .abi import (RAY_DTYPE, TR_MAT_DISNEY12, TR_MAT_GLASS, TR_MAT_PHONG, Material, SceneBuffers, make_camera,
+from .abi import (RAY_DTYPE, TR_MAT_DISNEY12, TR_MAT_GLASS, TR_MAT_METAL, TR_MAT_PHONG, Material, SceneBuffers, make_camera,
                   make_filter, make_params)
 
 F32_MAX = np.float32(np.finfo(np.float32).max)
@@ -208,12 +208,13 @@ def lambert(albedo) -> Material:
     return Material(kind=TR_MAT_PHONG, kd=tuple(albedo), ks=(0.0, 0.0, 0.0), ns=1.0)
 
 
-def cornell(width=256, height=256, spp=16, max_depth=5, min_depth=5, glass=False):
+def cornell(width=256, height=256, spp=16, max_depth=5, min_depth=5, glass=False, metal=False):
     """Cornell box [-1,1]^3 open at +z: 10 wall triangles, two boxes (12 each),
     a 0.5x0.5 ceiling light at y = 0.99 emitting (17,12,4): 36 triangles,
     2 lights. Pinhole camera at (0,0,3.5), 40 degree fov. min_depth >= max_depth
     disables Russian roulette. glass: the tall box is glass (kr = kt = 1,
-    ior 1.5), which takes paths through the specular branch."""
+    ior 1.5), which takes paths through the specular branch. metal: the short
+    box is a rough anisotropic metal (GGX with a painted conductor Fresnel)."""
     b = _Builder()
     white = b.material(lambert((0.73, 0.73, 0.73)))
     tall = b.material(Material(kind=TR_MAT_GLASS, kr=(1.0, 1.0, 1.0), kt=(1.0, 1.0, 1.0), ior=1.5)) if glass else white
@@ -224,7 +225,9 @@ def cornell(width=256, height=256, spp=16, max_depth=5, min_depth=5, glass=False
     b.quad((-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1), (0, 0, 1), white)    # back
     b.quad((-1, -1, -1), (-1, 1, -1), (-1, 1, 1), (-1, -1, 1), (1, 0, 0), red)      # left
     b.quad((1, -1, -1), (1, 1, -1), (1, 1, 1), (1, -1, 1), (-1, 0, 0), green)       # right
-    b.box((-0.35, -0.7, -0.3), (0.6, 0.6, 0.6), 15.0, white)
+    short = b.material(Material(kind=TR_MAT_METAL, color=(0.95, 0.64, 0.54), eta=(0.2, 0.92, 1.1), k=(3.9, 2.45, 2.14),
+                                roughness=0.35, anisotropic=0.4)) if metal else white
+    b.box((-0.35, -0.7, -0.3), (0.6, 0.6, 0.6), 15.0, short)
     b.box((0.35, -0.4, 0.3), (0.6, 1.2, 0.6), -18.0, tall)
     b.quad((-0.25, 0.99, -0.25), (0.25, 0.99, -0.25), (0.25, 0.99, 0.25), (-0.25, 0.99, 0.25), (0, -1, 0),
            white, emission=(17.0, 12.0, 4.0))
