@@ -111,6 +111,16 @@ typedef struct tr_scene_desc {
   uint32_t num_lights;
   const int32_t* light_prims;   /* primitive indices, in scene.lights order */
   int32_t max_leaf_prims;       /* create_bvh_accel argument (src/accelerator/bvh.cpp:315) */
+  /* Environment light: create_ibl_light(create_hdr_texture2d(image), world_to_light)
+   * (src/light/environment_light.cpp:14-84,196-203, src/texture/hdr_texture.cpp:9-37)
+   * with scene->environment_light set and the light appended to scene->lights
+   * after the area lights, as the reference's demo driver does
+   * (src/main.cpp:59-67). env_texels == NULL: no environment light. */
+  uint32_t env_width, env_height;
+  const float* env_texels;   /* 3 * env_width * env_height, linear RGB; texel (x, y) at 3 * (x + y * env_width),
+                                row y at v = y / (env_height - 1) (v = theta / pi) */
+  const float* env_to_light; /* 16, row-major world_to_light matrix */
+  const float* env_to_world; /* 16, row-major inverse of env_to_light (the Transform's inverse) */
 } tr_scene_desc;
 
 /* create_thin_lens_camera arguments (src/camera/thin_lens_camera.cpp:23-36). */

@@ -23,6 +23,7 @@
 #include <cstdint>
 #include <cstring>
 #include <limits>
+#include <memory>
 #include <thread>
 #include <vector>
 
@@ -313,12 +314,153 @@ struct Camera {
   real focal_distance, lens_radius, film_w, film_h;
 };
 
+// ------------------------------------------------------ environment light
+// Distribution1D (utility/distribution.hpp:12-79): piecewise-constant density
+// over [0, 1) with n cells.
+struct Dist1D {
+  std::vector<real> func, cdf;
+  real func_int = 0;
+  Dist1D() = default;
+  Dist1D(const real* f, int n) : func(f, f + n), cdf(n + 1, 0) {
+    for (int i = 0; i < n; i++) cdf[i + 1] = cdf[i] + func[i] / n;
+    func_int = cdf[n];
+    if (!func_int) {
+      for (int i = 1; i < n + 1; i++) cdf[i] = real(i) / n;
+    } else {
+      for (int i = 1; i < n + 1; i++) cdf[i] /= func_int;
+    }
+  }
+  int count() const { return (int)func.size(); }
+  // std::lower_bound over the reversed cdf with std::greater: the last index
+  // i whose cdf[i] is not above u (cdf is non-decreasing)
+  int last_not_above(real u) const {
+    int lo = 0, hi = (int)cdf.size();  // answer + 1 lies in [lo, hi]
+    while (lo < hi) {
+      const int mid = (lo + hi) / 2;
+      if (cdf[mid] > u) hi = mid;
+      else lo = mid + 1;
+    }
+    return lo - 1;
+  }
+  real sample_continuous(real u, real* pdf, int* off = nullptr) const {
+    int offset = std::clamp<int>(last_not_above(u), 0, (int)cdf.size() - 2);
+    if (off) *off = offset;
+    real du = u - cdf[offset];
+    if (offset + 1 < (int)cdf.size() && cdf[offset + 1] - cdf[offset] > 0) du /= cdf[offset + 1] - cdf[offset];
+    if (pdf) *pdf = (func_int > 0) ? func[offset] / func_int : 0;
+    return (offset + du) / count();
+  }
+};
+// Distribution2D (utility/distribution.hpp:81-111); its pdf multiplies by
+// the marginal integral, as the reference does.
+struct Dist2D {
+  std::vector<Dist1D> cond;
+  Dist1D marg;
+  void build(const real* data, int nu, int nv) {
+    cond.clear();
+    for (int v = 0; v < nv; v++) cond.emplace_back(&data[v * nu], nu);
+    std::vector<real> mf;
+    for (int v = 0; v < nv; v++) mf.push_back(cond[v].func_int);
+    marg = Dist1D(mf.data(), nv);
+  }
+  void sample_continuous(real u, real v, float* pdf, real& d0, real& d1) const {
+    float pdfs[2];
+    int iv;
+    d1 = marg.sample_continuous(v, &pdfs[1], &iv);
+    d0 = cond[iv].sample_continuous(u, &pdfs[0]);
+    *pdf = pdfs[0] * pdfs[1];
+  }
+  real pdf(real u, real v) const {
+    const int nu = cond[0].count(), nv = marg.count();
+    const int iu = std::clamp<int>((int)(u * nu), 0, nu - 1);
+    const int iv = std::clamp<int>((int)(v * nv), 0, nv - 1);
+    return cond[iv].func[iu] * marg.func_int;
+  }
+};
+// IBL over an HDRTexture2D (light/environment_light.cpp:14-193,
+// texture/hdr_texture.cpp:9-37, core/texture.hpp:57-95)
+struct Env {
+  int w = 0, h = 0;
+  std::vector<real> tex;      // 3 per texel, texel (x, y) at 3 * (x + y * w)
+  real to_light[16], to_world[16];
+  Dist2D dist;
+  V3 center;
+  real radius = 1;
+  Sp texel(int x, int y) const {
+    const real* t = &tex[3 * ((size_t)x + (size_t)y * w)];
+    return Sp(t[0], t[1], t[2]);
+  }
+  // Point3f * double (geometry.hpp:268-271): double product rounded to float
+  static Sp scaled(Sp c, double f) { return Sp((real)(f * c.r), (real)(f * c.g), (real)(f * c.b)); }
+  // Texture2D::evaluate with the repeat wrap, LinearSampler::Sample2D (utility/sampler.hpp:16-29)
+  Sp eval(real u_in, real v_in) const {
+    const real uw = std::clamp<real>(u_in - std::floor(u_in), 0, 1);
+    const real vw = std::clamp<real>(v_in - std::floor(v_in), 0, 1);
+    double u = std::clamp((double)uw, 0.0, 1.0) * (w - 1);
+    double v = std::clamp((double)vw, 0.0, 1.0) * (h - 1);
+    const int u0 = std::clamp(static_cast<int>(u), 0, w - 1), u1 = std::clamp(u0 + 1, 0, w - 1);
+    const int v0 = std::clamp(static_cast<int>(v), 0, h - 1), v1 = std::clamp(v0 + 1, 0, h - 1);
+    const double du = u - u0, dv = v - v0;
+    return scaled(scaled(texel(u0, v0), 1.0 - du) + scaled(texel(u1, v0), du), 1.0 - dv) +
+           scaled(scaled(texel(u0, v1), 1.0 - du) + scaled(texel(u1, v1), du), dv);
+  }
+  // the IBL constructor's sampling density: luminance times solid angle per
+  // cell of a grid of at most 360 x 180 (environment_light.cpp:39-81)
+  void build_distribution() {
+    const int nw = std::min(w, 360), nh = std::min(h, 180);
+    std::vector<real> img((size_t)nw * nh, 0);
+    for (int y = 0; y < nh; ++y) {
+      const real y0 = static_cast<real>(y) / nh, y1 = static_cast<real>(y + 1) / nh;
+      const real sy0 = y0 * h, sy1 = y1 * h;
+      const int yb = std::max<int>(0, (int)(std::floor(sy0) - 1));
+      const int ye = std::min<int>(h - 1, (int)(std::floor(sy1) + 1));
+      for (int x = 0; x < nw; ++x) {
+        const real x0 = static_cast<real>(x) / nw, x1 = static_cast<real>(x + 1) / nw;
+        const real sx0 = x0 * w, sx1 = x1 * w;
+        const int xb = std::max<int>(0, (int)(std::floor(sx0) - 1));
+        const int xe = std::min<int>(w - 1, (int)(std::floor(sx1) + 1));
+        real lum = 0;
+        for (int sy = yb; sy <= ye; ++sy)
+          for (int sx = xb; sx <= xe; ++sx) {
+            const real su = static_cast<real>(sx + 0.5) / w;
+            const real sv = static_cast<real>(sy + 0.5) / h;
+            lum += eval(su, sv).lum();
+          }
+        const real area = (real)std::abs(2 * kPi * (x1 - x0) * kPi * (y1 - y0) * std::sin(kPi * 0.5 * (y1 + y0)));
+        img[(size_t)x + (size_t)y * nw] = lum * area;
+      }
+    }
+    dist.build(img.data(), nw, nh);
+  }
+  // IBL::light_emit (environment_light.cpp:172-182)
+  Sp emit(V3 d) const {
+    V3 dir = normalize(d);
+    dir = normalize(xform_vec(to_light, dir));
+    const real phi = local_phi(dir);
+    const real theta = std::acos(std::clamp<real>(dir.z, -1, 1));
+    const real u = std::clamp<real>(phi / (2 * kPi), 0, 1);
+    const real v = std::clamp<real>(theta * kInvPi, 0, 1);
+    return eval(u, v);
+  }
+  // IBL::pdf (environment_light.cpp:184-191)
+  real pdf(V3 d) const {
+    const V3 wi = xform_vec(to_light, d);
+    const real theta = std::acos(std::clamp<real>(wi.z, -1, 1));
+    real phi = std::atan2(wi.y, wi.x);
+    phi = (phi < 0) ? (phi + 2 * kPi) : phi;
+    const real sin_theta = std::sin(theta);
+    if (sin_theta == 0) return 0;
+    return dist.pdf(phi * kInv2Pi, theta * kInvPi) / (2 * kPi * kPi * sin_theta);
+  }
+};
+
 struct Scene {
   std::vector<Tri> tris;
   std::vector<Sphere> spheres;
   std::vector<Mat> mats;
   std::vector<Prim> prims;
   std::vector<int> lights;       // primitive ids in scene.lights order
+  std::unique_ptr<Env> env;      // environment light (after the area lights in scene.lights)
   std::vector<Node> nodes;
   std::vector<int> order;        // leaf slot -> primitive id
   int max_leaf = 1;
@@ -1284,6 +1426,26 @@ inline Sp light_emit(const Scene& sc, int prim, const Isect& is, V3 w) {
   return dot(is.g.z, w) > 0 ? sc.prims[prim].emission : Sp(0);
 }
 
+// IBL::sample_li (light/environment_light.cpp:88-116): a direction from the
+// luminance distribution, its radiance and a point 2 world radii away.
+LightSample env_sample_li(const Env& env, V3 ref, real u, real v) {
+  LightSample out;
+  float map_pdf;
+  real su, sv;
+  env.dist.sample_continuous(u, v, &map_pdf, su, sv);
+  if (map_pdf == 0) return out;
+  const real theta = sv * kPi, phi = su * 2 * kPi;
+  const real cos_theta = std::cos(theta), sin_theta = std::sin(theta);
+  const real sin_phi = std::sin(phi), cos_phi = std::cos(phi);
+  V3 wi(sin_theta * cos_phi, sin_theta * sin_phi, cos_theta);
+  wi = normalize(xform_vec(env.to_world, wi));
+  if (sin_theta == 0) return out;
+  out.pdf = map_pdf / (2 * kPi * kPi * sin_theta);
+  out.radiance = env.emit(wi);
+  out.pos = ref + mulf(wi, 2 * env.radius);
+  return out;
+}
+
 // ---------------------------------------------------------- ray recording
 struct RayLog {
   std::vector<tr_ray> closest, any;
@@ -1343,6 +1505,25 @@ Sp sample_area_light(Tracer& tr, int light, const Isect& is, const BSDF& bsdf, S
   float weight = power_heuristic(ls.pdf, bpdf);
   return (f * weight) / ls.pdf;
 }
+// sample_environment_light (renderer/direct_illumination.cpp:73-106)
+Sp sample_env_light(Tracer& tr, const Isect& is, const BSDF& bsdf, Sampler& smp) {
+  const real u = smp.u(), v = smp.u();
+  smp.u(); smp.u(); smp.u();
+  LightSample ls = env_sample_li(*tr.sc.env, is.pos, u, v);
+  if (ls.radiance.black()) return Sp();
+  V3 to_light = ls.pos - is.pos;
+  double dist = length(to_light) - kEps;
+  if (dist <= kEps) return Sp();
+  to_light = normalize(to_light);
+  const Ray shadow = make_ray(is.pos, to_light, kEps, (real)dist);
+  if (tr.trace_any(shadow)) return Sp();
+  const Sp bf = bsdf.eval(to_light, is.wo);
+  if (bf.black()) return Sp();
+  const real bpdf = bsdf.pdf(to_light, is.wo);
+  const Sp f = (ls.radiance * bf) * abs_cos(to_light, is.g.z);
+  float weight = power_heuristic(ls.pdf, bpdf);
+  return (f * weight) / ls.pdf;
+}
 // sample_bsdf (renderer/direct_illumination.cpp:144-198)
 Sp sample_bsdf_mis(Tracer& tr, const Isect& is, const BSDF& bsdf, Sampler& smp) {
   const real u = smp.u(), v = smp.u(), w = smp.u();
@@ -1351,7 +1532,17 @@ Sp sample_bsdf_mis(Tracer& tr, const Isect& is, const BSDF& bsdf, Sampler& smp) 
   bs.wi = normalize(bs.wi);
   Ray ray = make_ray(is.eps_offset(bs.wi), bs.wi);
   Isect t;
-  if (!tr.trace_p(ray, t)) return Sp();
+  if (!tr.trace_p(ray, t)) {
+    // the environment light's share (direct_illumination.cpp:156-174)
+    if (!tr.sc.env) return Sp();
+    const Sp Le = tr.sc.env->emit(ray.d);
+    if (Le.black()) return Sp();
+    const Sp f = (Le * bs.f) * abs_cos(is.g.z, ray.d);
+    if (bs.delta) return f / bs.pdf;
+    const real lpdf = tr.sc.env->pdf(ray.d);
+    const real weight = power_heuristic(bs.pdf, lpdf);
+    return (f * weight) / bs.pdf;
+  }
   const Prim& pr = tr.sc.prims[t.prim];
   if (!pr.light) return Sp();
   Sp Le = light_emit(tr.sc, t.prim, t, t.wo);
@@ -1363,7 +1554,8 @@ Sp sample_bsdf_mis(Tracer& tr, const Isect& is, const BSDF& bsdf, Sampler& smp) 
 }
 
 // PathTraceRenderer::eval_pixel_li (renderer/path_trace_renderer.cpp:27-210)
-// for vacuum media and no environment light. A delta sample gets no direct
+// for vacuum media. A ray that leaves the scene at depth 0 or after a delta
+// sample adds the environment light's radiance (:66-81). A delta sample gets no direct
 // lighting, the emission its ray reaches counts, and up to
 // max_specular_depth (20, path_trace_renderer.cpp:20) of them do not count
 // toward the depth (:131-139).
@@ -1380,6 +1572,7 @@ Sp eval_li(Tracer& tr, Ray ray, Sampler& smp, int min_depth, int max_depth) {
     Isect is;
     bool found = tr.trace_p(ray, is);
     if ((depth == 0 || specular) && found && sc.prims[is.prim].light) L += coef * light_emit(sc, is.prim, is, -ray.d);
+    if ((depth == 0 || specular) && !found && sc.env) L += coef * sc.env->emit(ray.d);
     if (!found) break;
     BSDF bsdf{&sc.mats[sc.prims[is.prim].material], is.g, is.s};
     const real u = smp.u(), v = smp.u(), w = smp.u();
@@ -1393,6 +1586,7 @@ Sp eval_li(Tracer& tr, Ray ray, Sampler& smp, int min_depth, int max_depth) {
     if (!specular) {
       Sp direct;
       for (int li : sc.lights) direct += coef * sample_area_light(tr, li, is, bsdf, smp);
+      if (sc.env) direct += coef * sample_env_light(tr, is, bsdf, smp);
       direct += coef * sample_bsdf_mis(tr, is, bsdf, smp);
       L += direct * (real(1) / 1);
     }
@@ -1591,6 +1785,26 @@ void* orc_scene_create(const tr_scene_desc* d) {
   }
   for (uint32_t l = 0; l < d->num_lights; ++l) sc->lights.push_back(d->light_prims[l]);
   build_bvh(*sc);
+  if (d->env_texels && d->env_width > 0 && d->env_height > 0) {
+    auto env = std::make_unique<Env>();
+    env->w = (int)d->env_width;
+    env->h = (int)d->env_height;
+    env->tex.assign(d->env_texels, d->env_texels + 3 * (size_t)env->w * env->h);
+    std::memcpy(env->to_light, d->env_to_light, 64);
+    std::memcpy(env->to_world, d->env_to_world, 64);
+    env->build_distribution();
+    // EnvironmentLight::preprocess over the tree's root box (core/light.hpp:93-95,
+    // Bounds3::bounding_sphere, geometry.hpp:752-755)
+    if (!sc->nodes.empty()) {
+      const Bounds& b = sc->nodes[0].b;
+      const V3 sum = b.lo + b.hi;
+      env->center = V3((real)(0.5 * sum.x), (real)(0.5 * sum.y), (real)(0.5 * sum.z));
+      const bool inside = env->center.x >= b.lo.x && env->center.x <= b.hi.x && env->center.y >= b.lo.y &&
+                          env->center.y <= b.hi.y && env->center.z >= b.lo.z && env->center.z <= b.hi.z;
+      env->radius = inside ? (real)length(env->center - b.hi) : 0;
+    }
+    sc->env = std::move(env);
+  }
   return sc;
 }
 

@@ -89,6 +89,19 @@ def test_metal_cornell(min_depth, glass):
     assert np.array_equal(bits(port.render(par)), bits(ref.render(par)))
 
 
+@pytest.mark.parametrize("area_light,env_size,min_depth", [(True, (64, 32), 3), (False, (400, 200), 2),
+                                                             (True, (37, 19), 6)])
+def test_environment_light(area_light, env_size, min_depth):
+    """The IBL environment light: emission of escaping rays, its light
+    sample and the MIS ray's share, with its luminance distribution built
+    over the full map and over a downsampled 360 x 180 grid."""
+    sc, cam, filt, par = scenes.outdoor(32, 24, 4, min_depth=min_depth, env_size=env_size, area_light=area_light)
+    port, ref = oracle.Oracle(sc, "port"), oracle.Oracle(sc, "reference")
+    port.set_camera(cam, filt)
+    ref.set_camera(cam, filt)
+    assert np.array_equal(bits(port.render(par)), bits(ref.render(par)))
+
+
 def test_make_ray():
     for o, d in (((0, 0, 0), (1, 2, 3)), ((1, -1, 0.5), (1e-9, 1, 0)), ((0, 0, 0), (-0.0, 0.0, -3))):
         a = oracle.make_ray("port", o, d, 0.0, 1.0)

@@ -262,6 +262,59 @@ def disney_grid(width=1024, height=1024, spp=64, max_depth=8, min_depth=5, seed=
     return scene, cam, make_filter(0.5, 0.6), make_params(width, height, spp, min_depth, max_depth)
 
 
+def sky_map(width=64, height=32, sun=(0.55, 1.2), sun_radiance=300.0):
+    """A synthetic HDR environment map in the IBL's (u, v) = (phi / 2pi, theta / pi)
+    layout (row y at theta = pi * y / (height - 1)): a sky brightening toward
+    the horizon, a dim ground below it and a small sun disc of high radiance
+    centred at (theta, phi) = `sun`."""
+    y, x = np.mgrid[0:height, 0:width]
+    theta = np.pi * y / max(height - 1, 1)
+    phi = 2 * np.pi * x / max(width - 1, 1)
+    t = np.clip(theta / (np.pi / 2), 0, 1)[..., None]
+    sky = (1 - t) * np.array([0.25, 0.45, 0.9]) + t * np.array([0.9, 0.9, 1.0])
+    ground = np.array([0.18, 0.14, 0.1]) * np.ones_like(sky)
+    img = np.where((theta <= np.pi / 2)[..., None], sky, ground)
+    d = np.stack([np.sin(theta) * np.cos(phi), np.sin(theta) * np.sin(phi), np.cos(theta)], -1)
+    st, sp = sun
+    s = np.array([np.sin(st) * np.cos(sp), np.sin(st) * np.sin(sp), np.cos(st)])
+    img = img + np.where(((d @ s) > np.cos(0.12))[..., None], sun_radiance * np.array([1.0, 0.9, 0.75]), 0.0)
+    return img.astype(np.float32)
+
+
+def rotate_x(theta):
+    """rotate_x (src/utility/transform.cpp:139-145) in float: the matrix and its
+    transpose as the Transform's inverse, row-major."""
+    s, c = np.float32(math.sin(np.float32(theta))), np.float32(math.cos(np.float32(theta)))
+    m = np.array([1, 0, 0, 0, 0, c, -s, 0, 0, s, c, 0, 0, 0, 0, 1], dtype=np.float32)
+    return m, np.ascontiguousarray(m.reshape(4, 4).T).ravel()
+
+
+def outdoor(width=96, height=64, spp=8, max_depth=6, min_depth=3, env_size=(64, 32), area_light=True):
+    """An open scene under an environment light: a ground quad, Disney12,
+    metal, glass and Lambertian spheres, optionally one small area light; the
+    sky map of `sky_map` with world +y as the light's +z (world_to_light =
+    rotate_x(pi/2), as the reference's demo does)."""
+    b = _Builder()
+    ground = b.material(lambert((0.45, 0.42, 0.4)))
+    b.quad((-6, 0, -6), (6, 0, -6), (6, 0, 6), (-6, 0, 6), (0, 1, 0), ground)
+    if area_light:
+        b.quad((1.5, 3, -0.5), (2.5, 3, -0.5), (2.5, 3, 0.5), (1.5, 3, 0.5), (0, -1, 0), ground,
+               emission=(6.0, 6.0, 6.0))
+    mats = [b.material(Material(kind=TR_MAT_DISNEY12, base_color=(0.8, 0.3, 0.2), metallic=0.2, roughness=0.4,
+                                specular=0.5, clearcoat=0.5, clearcoat_gloss=0.7, sheen_tint=0.5)),
+            b.material(Material(kind=TR_MAT_METAL, color=(0.95, 0.64, 0.54), eta=(0.2, 0.92, 1.1),
+                                k=(3.9, 2.45, 2.14), roughness=0.25, anisotropic=0.0)),
+            b.material(Material(kind=TR_MAT_GLASS, kr=(1.0, 1.0, 1.0), kt=(1.0, 1.0, 1.0), ior=1.5)),
+            b.material(lambert((0.2, 0.5, 0.3)))]
+    for k, m in enumerate(mats):
+        b.sphere((-2.25 + 1.5 * k, 0.6, 0.0), 0.6, m)
+    scene = b.finish(max_leaf_prims=3)
+    scene.env_texels = sky_map(*env_size)
+    scene.env_to_light, scene.env_to_world = rotate_x(math.pi / 2)
+    cam = make_camera(width / height, (0, 1.6, 6.5), (0, 0.9, 0), (0, 1, 0), math.radians(50.0), 0.0, 1.0)
+    return scene, cam, make_filter(0.5, 0.6), make_params(width, height, spp, min_depth, max_depth)
+
+
 def traversal(n_tris=1 << 20, seed=0, max_leaf_prims=4):
     """n_tris triangles: centres uniform in [0,1]^3, each vertex the centre plus
     an edge vector uniform in [-0.01,0.01]^3. numpy PCG64(seed)."""
