@@ -196,6 +196,11 @@ class Light {
   virtual ~Light() = default;
 };
 class AreaLight : public Light {};
+// An environment light: create_ibl_light (src/factory/light.hpp:12-14).
+class EnvironmentLight : public Light {
+ public:
+  virtual ~EnvironmentLight() = default;
+};
 
 class Primitive {
  public:
@@ -238,6 +243,8 @@ struct SceneDesc {
   std::vector<float> prim_emission;
   std::vector<int32_t> light_prims;
   int32_t max_leaf_prims = 1;
+  uint32_t env_width = 0, env_height = 0;  // environment map (0 x 0: none)
+  std::vector<float> env_texels, env_to_light, env_to_world;
   tr_scene_desc view() const;
 };
 
@@ -248,6 +255,9 @@ class Scene {
   virtual RC<const Camera> get_camera() const noexcept = 0;
   virtual void prepare_to_render() = 0;
   Span<const Light*> lights;
+  // src/core/scene.hpp:31; when set, it is also the last entry of `lights`
+  // (as src/main.cpp:59-67 arranges)
+  RC<EnvironmentLight> environment_light;
   // GPU-path additions: the description prepare_to_render() assembled and a
   // counter that changes whenever it is rebuilt.
   virtual const SceneDesc& desc() const = 0;
@@ -272,6 +282,17 @@ class Image2D {
   int w_ = 0, h_ = 0;
   std::vector<T> data_;
 };
+
+using Color3f = Point3f;
+
+// create_hdr_texture2d (src/factory/texture.hpp:16, src/texture/hdr_texture.cpp:9-37):
+// bilinear lookups of a linear-RGB image, texel (x, y) at
+// (u, v) = (x / (width - 1), y / (height - 1)), coordinates wrapped by repeat.
+RC<Texture2D> create_hdr_texture2d(const RC<Image2D<Color3f>>& image);
+// create_ibl_light (src/light/environment_light.cpp:196-203): the texture
+// (an HDR texture, or a constant one) over the sphere of directions,
+// (u, v) = (phi / 2pi, theta / pi) in the light space of world_to_light.
+RC<EnvironmentLight> create_ibl_light(RC<const Texture2D> tex, const Transform& world_to_light);
 
 struct RenderTarget {
   Image2D<Spectrum> color;

@@ -1795,6 +1795,8 @@ void* orc_scene_create(const tr_scene_desc* d) {
     env->build_distribution();
     // EnvironmentLight::preprocess over the tree's root box (core/light.hpp:93-95,
     // Bounds3::bounding_sphere, geometry.hpp:752-755)
+    // (an empty tree's default box gives centre 0 and radius 0)
+    env->radius = 0;
     if (!sc->nodes.empty()) {
       const Bounds& b = sc->nodes[0].b;
       const V3 sum = b.lo + b.hi;

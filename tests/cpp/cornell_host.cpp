@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <string>
 
@@ -82,8 +83,9 @@ int main(int argc, char** argv) {
   const std::string out = argv[1];
   const int W = std::atoi(argv[2]), H = std::atoi(argv[3]), spp = std::atoi(argv[4]);
   const bool render = argc > 5 && std::strcmp(argv[5], "render") == 0;
-  // the short box in metal and the tall one in glass
-  const bool glass_metal = argc > 6 && std::strcmp(argv[6], "glass_metal") == 0;
+  // the short box in metal and the tall one in glass; an environment light
+  const bool glass_metal = argc > 6 && std::strstr(argv[6], "glass_metal") != nullptr;
+  const bool sky = argc > 6 && std::strstr(argv[6], "sky") != nullptr;
 
   // construction errors throw (src/shape/sphere.cpp:88-90)
   if (!throws([] { create_sphere(-1.0f, Transform()); }) ||
@@ -132,6 +134,19 @@ int main(int argc, char** argv) {
   bvh->build(std::move(primitives));
   auto scene = create_general_scene(bvh);
   scene->lights = area_lights;
+  if (sky) {
+    // a 32 x 16 map: a blue-to-white sky, a dark ground, a bright sun texel
+    auto img = std::make_shared<Image2D<Color3f>>(32, 16);
+    for (int y = 0; y < 16; ++y)
+      for (int x = 0; x < 32; ++x) {
+        const float t = std::min(1.0f, (float)y / 7.5f);
+        img->at(x, y) = y < 8 ? Color3f{0.25f + 0.65f * t, 0.45f + 0.45f * t, 0.9f + 0.1f * t}
+                              : Color3f{0.18f, 0.14f, 0.1f};
+      }
+    img->at(5, 3) = Color3f{120.0f, 110.0f, 90.0f};
+    scene->environment_light = create_ibl_light(create_hdr_texture2d(img), rotate_x(3.14159265358979f / 2));
+    scene->lights.push_back(scene->environment_light.get());
+  }
   scene->set_camera(create_thin_lens_camera((float)W / (float)H, {0, 0, 3.5f}, {0, 0, 0}, {0, 1, 0},
                                             40.0f * pi / 180.0f, 0.0f, 1.0f));
   scene->prepare_to_render();
@@ -153,6 +168,11 @@ int main(int argc, char** argv) {
   put(f, d.light_prims);
   std::fwrite(&d.max_leaf_prims, 4, 1, f);
   std::fwrite(&scene->get_camera()->rec, sizeof(tr_camera), 1, f);
+  std::fwrite(&d.env_width, 4, 1, f);
+  std::fwrite(&d.env_height, 4, 1, f);
+  put(f, d.env_texels);
+  put(f, d.env_to_light);
+  put(f, d.env_to_world);
   std::fclose(f);
   std::printf("scene: %zu triangles, %zu lights, %zu materials\n", d.indices.size() / 3, d.light_prims.size(),
               d.materials.size());

@@ -85,6 +85,28 @@ def test_cornell_metal(gpu, min_depth):
     _compare(out, ref, 0.8)
 
 
+@pytest.mark.parametrize("glass,area_light", [(False, True), (True, True), (False, False)])
+def test_outdoor_environment_light(gpu, glass, area_light):
+    """An open scene under the IBL environment light: escaping camera rays
+    and rays after delta samples see the map, every vertex samples it (after
+    the area light) and the MIS ray's escape is weighted against it."""
+    sc, cam, filt, par = scenes.outdoor(64, 48, 8, glass=glass, area_light=area_light)
+    orc = oracle.Oracle(sc, "port")
+    orc.set_camera(cam, filt)
+    ref = orc.render(par)
+    gpu.upload(sc)
+    out, stats = gpu.render(cam, filt, par)
+    assert stats.samples == 64 * 48 * 8
+    if not glass:
+        _compare(out, ref, 0.8)
+        return
+    a, b = _image(out.astype(np.float64)), _image(ref.astype(np.float64))
+    rel = (np.abs(a - b) / np.maximum(np.abs(b), 1e-6)).max(-1)
+    print(f"within 1e-5: {(rel <= 1e-5).mean():.4f}, image means {a.mean():.5f} {b.mean():.5f}")
+    assert (rel <= 1e-5).mean() >= 0.8
+    assert abs(a.mean() - b.mean()) <= 0.01 * b.mean()
+
+
 def test_cornell(gpu):
     sc, cam, filt, par = scenes.cornell(64, 64, 8)
     orc = oracle.Oracle(sc, "port")
@@ -129,7 +151,7 @@ def test_fp64_accumulation(gpu):
     assert np.allclose(out32, out64, rtol=1e-5, atol=1e-6)
 
 
-@pytest.mark.parametrize("maker", ["cornell", "disney", "glass", "metal"])
+@pytest.mark.parametrize("maker", ["cornell", "disney", "glass", "metal", "outdoor"])
 def test_replay_recorded_rays(gpu, maker):
     """Every trace the oracle's integrator makes, replayed on the GPU."""
     if maker == "cornell":
@@ -138,6 +160,8 @@ def test_replay_recorded_rays(gpu, maker):
         sc, cam, filt, par = scenes.cornell(32, 32, 4, max_depth=8, min_depth=2, glass=True)
     elif maker == "metal":
         sc, cam, filt, par = scenes.cornell(32, 32, 4, max_depth=8, min_depth=2, glass=True, metal=True)
+    elif maker == "outdoor":
+        sc, cam, filt, par = scenes.outdoor(32, 32, 4)
     else:
         sc, cam, filt, par = scenes.disney_grid(32, 32, 2)
     orc = oracle.Oracle(sc, "port")
@@ -207,7 +231,7 @@ def test_occluded_room_small(gpu):
     _compare(out, ref, 0.8)
 
 
-@pytest.mark.parametrize("maker", ["cornell", "room", "glass", "metal"])
+@pytest.mark.parametrize("maker", ["cornell", "room", "glass", "metal", "outdoor"])
 def test_converged_fp64_image_within_one_percent(gpu, maker):
     """The image bar: a 4096-spp render accumulated in FP64 on the GPU is
     within 1% mean relative error of the oracle's 4096-spp FP64 render of
@@ -221,6 +245,9 @@ def test_converged_fp64_image_within_one_percent(gpu, maker):
     elif maker == "metal":
         sc, cam, filt, _ = scenes.cornell(24, 24, 1, metal=True)
         par = scenes.make_params(24, 24, 4096, 5, 5)
+    elif maker == "outdoor":
+        sc, cam, filt, _ = scenes.outdoor(24, 16, 1, glass=False)
+        par = scenes.make_params(24, 16, 4096, 3, 6)
     else:
         sc, cam, filt, _ = scenes.occluded_room(20, 16, 1, n_tris=5000)
         par = scenes.make_params(20, 16, 4096, 3, 10)

@@ -63,9 +63,15 @@ def _read_desc(path):
     max_leaf = int(np.frombuffer(buf, np.int32, 1, off)[0])
     off += 4
     cam = TrCamera.from_buffer_copy(buf, off)
+    off += ctypes.sizeof(TrCamera)
+    ew, eh = (int(v) for v in np.frombuffer(buf, np.uint32, 2, off))
+    off += 8
+    tex, to_l, to_w = take(np.float32), take(np.float32), take(np.float32)
     sb = SceneBuffers(positions=pos, normals=nrm, uvs=uv, indices=idx, sphere_radius=sr, sphere_to_world=sw,
                       sphere_to_local=sl, materials=[_Raw(m) for m in mats], prim_shape=ps, prim_material=pm,
                       prim_emission=pe, light_prims=lp, max_leaf_prims=max_leaf)
+    if ew and eh:
+        sb.env_texels, sb.env_to_light, sb.env_to_world = tex.reshape(eh, ew, 3), to_l, to_w
     return sb, cam
 
 
@@ -116,8 +122,32 @@ def test_factory_glass_and_metal_materials(program, tmp_path):
     assert sb.prim_material[22] == kinds.index(TR_MAT_GLASS)
 
 
+def test_factory_environment_light(program, tmp_path):
+    """create_ibl_light over create_hdr_texture2d, set as the scene's
+    environment light and appended to its lights: the description carries the
+    map and the world_to_light transform, and the oracle and the reference
+    build render it alike."""
+    out = str(tmp_path / "c")
+    r = subprocess.run([program, out, "16", "16", "1", "describe", "sky"], check=True, capture_output=True,
+                       text=True)
+    assert "36 triangles, 2 lights" in r.stdout  # the area lights; the environment light is separate
+    sb, cam = _read_desc(out + ".desc")
+    assert sb.env_texels.shape == (16, 32, 3)
+    assert np.allclose(sb.env_texels[3, 5], [120, 110, 90])
+    to_l = sb.env_to_light.reshape(4, 4)
+    assert np.allclose(to_l @ [0, 1, 0, 0], [0, 0, 1, 0], atol=1e-6)  # world +y is the light's +z
+    assert np.array_equal(sb.env_to_world.reshape(4, 4), to_l.T)
+    if oracle.ref_available():
+        W, H = 16, 16
+        par = make_params(W, H, 2, 5, 5)
+        port, ref = oracle.Oracle(sb, "port"), oracle.Oracle(sb, "reference")
+        for o in (port, ref):
+            o.set_camera(cam, make_filter(0.5, 0.6))
+        assert np.array_equal(port.render(par).view(np.uint32), ref.render(par).view(np.uint32))
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("variant", ["", "glass_metal"])
+@pytest.mark.parametrize("variant", ["", "glass_metal", "sky"])
 def test_factory_scene_renders_like_the_oracle(program, tmp_path, variant):
     W, H, S = 48, 40, 4
     out = str(tmp_path / "c")

@@ -478,6 +478,8 @@ tr_status upload_device_built(tr_ctx* ctx) {
     sc.has_glass |= m.kind == MAT_GLASS;
     sc.has_metal |= m.kind == MAT_METAL;
   }
+  tr_status es = upload_envs(ctx);
+  if (es != TR_OK) return es;
   ctx->has_scene = true;
   return TR_OK;
 }

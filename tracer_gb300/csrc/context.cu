@@ -339,7 +339,70 @@ tr_status upload_device_tables(tr_ctx* ctx) {
     sc.has_glass |= m.kind == MAT_GLASS;
     sc.has_metal |= m.kind == MAT_METAL;
   }
+  tr_status es = upload_envs(ctx);
+  if (es != TR_OK) return es;
   ctx->has_scene = true;
+  return TR_OK;
+}
+
+tr_status upload_envs(tr_ctx* ctx) {
+  const std::vector<EnvHost>& envs = ctx->hs.envs;
+  DScene& sc = ctx->dsc;
+  sc.envs = nullptr;
+  sc.has_env = envs.empty() ? 0 : 1;
+  if (envs.empty()) return TR_OK;
+  // one pool of floats, every array starting on a 16-byte boundary
+  size_t total = 0;
+  auto take = [&](size_t n) {
+    const size_t at = total;
+    total += (n + 3) & ~size_t(3);
+    return at;
+  };
+  struct Off { size_t tex, cf, cc, ci, mc; };
+  std::vector<Off> off(envs.size());
+  for (size_t i = 0; i < envs.size(); ++i) {
+    const EnvHost& e = envs[i];
+    off[i] = {take(e.texels.size()), take(e.cond_func.size()), take(e.cond_cdf.size()), take(e.cond_int.size()),
+              take(e.marg_cdf.size())};
+  }
+  std::vector<float> pool(total, 0.0f);
+  for (size_t i = 0; i < envs.size(); ++i) {
+    const EnvHost& e = envs[i];
+    std::copy(e.texels.begin(), e.texels.end(), pool.begin() + (ptrdiff_t)off[i].tex);
+    std::copy(e.cond_func.begin(), e.cond_func.end(), pool.begin() + (ptrdiff_t)off[i].cf);
+    std::copy(e.cond_cdf.begin(), e.cond_cdf.end(), pool.begin() + (ptrdiff_t)off[i].cc);
+    std::copy(e.cond_int.begin(), e.cond_int.end(), pool.begin() + (ptrdiff_t)off[i].ci);
+    std::copy(e.marg_cdf.begin(), e.marg_cdf.end(), pool.begin() + (ptrdiff_t)off[i].mc);
+  }
+  TR_CUDA(ctx, ctx->d_env_pool.reserve(total * sizeof(float)));
+  TR_CUDA(ctx, cudaMemcpyAsync(ctx->d_env_pool.p, pool.data(), total * sizeof(float), cudaMemcpyHostToDevice,
+                               ctx->stream));
+  const float* base = ctx->d_env_pool.as<float>();
+  std::vector<DEnv> recs(envs.size());
+  for (size_t i = 0; i < envs.size(); ++i) {
+    const EnvHost& e = envs[i];
+    DEnv& r = recs[i];
+    std::memset(&r, 0, sizeof(r));
+    r.texels = reinterpret_cast<const float4*>(base + off[i].tex);
+    r.cond_func = base + off[i].cf;
+    r.cond_cdf = base + off[i].cc;
+    r.cond_int = base + off[i].ci;
+    r.marg_cdf = base + off[i].mc;
+    r.marg_int = e.marg_int;
+    r.w = e.w;
+    r.h = e.h;
+    r.nu = e.nu;
+    r.nv = e.nv;
+    std::memcpy(r.to_light, e.to_light, sizeof(r.to_light));
+    std::memcpy(r.to_world, e.to_world, sizeof(r.to_world));
+    std::memcpy(r.center, e.center, sizeof(r.center));
+    r.radius = e.radius;
+  }
+  TR_CUDA(ctx, ctx->d_envs.reserve(recs.size() * sizeof(DEnv)));
+  TR_CUDA(ctx, cudaMemcpyAsync(ctx->d_envs.p, recs.data(), recs.size() * sizeof(DEnv), cudaMemcpyHostToDevice,
+                               ctx->stream));
+  TR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  sc.envs = ctx->d_envs.as<DEnv>();
   return TR_OK;
 }
 
@@ -465,8 +528,9 @@ void tr_ctx_destroy(tr_ctx* ctx) {
   cudaStreamSynchronize(ctx->stream);
   release_render(ctx);
   release_guide(ctx);
-  for (DevBuf* b : {&ctx->d_nodes, &ctx->d_slots, &ctx->d_spheres, &ctx->d_prims, &ctx->d_tshade, &ctx->d_mats,
-                    &ctx->d_lights, &ctx->d_roots, &ctx->d_rays, &ctx->d_out0, &ctx->d_out1, &ctx->d_err})
+  for (DevBuf* b : {&ctx->d_nodes, &ctx->d_nodes4, &ctx->d_slots, &ctx->d_spheres, &ctx->d_prims, &ctx->d_tshade, &ctx->d_mats,
+                    &ctx->d_lights, &ctx->d_roots, &ctx->d_rays, &ctx->d_out0, &ctx->d_out1, &ctx->d_err,
+                    &ctx->d_env_pool, &ctx->d_envs})
     b->release();
   cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -634,7 +698,29 @@ static tr_status build_host_scene(tr_ctx* ctx, const tr_scene_desc* d, HostScene
     L.extent = fabsf(L.A.x) + fabsf(L.A.y) + fabsf(L.A.z) + fabsf(L.B.x) + fabsf(L.B.y) + fabsf(L.B.z) + fabsf(L.C.x) +
                fabsf(L.C.y) + fabsf(L.C.z) + 1.0f;
     L.prim = p;
+    L.env = -1;
     hs.lights.push_back(L);
+  }
+  if (d->env_texels) {
+    // the environment light follows the area lights in scene.lights; its
+    // bounding sphere is that of the tree's root box, the union of the
+    // primitive boxes
+    EnvHost env;
+    std::string why;
+    if (!build_env_tables(d, env, why)) return set_err(ctx, TR_ERR_ARG, why);
+    float rlo[3] = {kRealMax, kRealMax, kRealMax}, rhi[3] = {-kRealMax, -kRealMax, -kRealMax};
+    for (uint32_t p = 0; p < np; ++p)
+      for (int k = 0; k < 3; ++k) {
+        rlo[k] = smin(rlo[k], lo[3 * p + k]);
+        rhi[k] = smax(rhi[k], hi[3 * p + k]);
+      }
+    env_bounding_sphere(env, rlo, rhi, np == 0);
+    DLight L;
+    std::memset(&L, 0, sizeof(L));
+    L.prim = -1;
+    L.env = 0;
+    hs.lights.push_back(L);
+    hs.envs.push_back(std::move(env));
   }
   if (device_bvh) {  // the tree is built on the device at upload
     hs.device_bvh = true;
@@ -680,10 +766,13 @@ static void append_scene(HostScene& dst, const HostScene& src) {
   dst.tshade.insert(dst.tshade.end(), src.tshade.begin(), src.tshade.end());
   dst.spheres.insert(dst.spheres.end(), src.spheres.begin(), src.spheres.end());
   dst.mats.insert(dst.mats.end(), src.mats.begin(), src.mats.end());
+  const int env_base = (int)dst.envs.size();
   for (DLight l : src.lights) {
-    l.prim += (int)prim_base;
+    if (l.env >= 0) l.env += env_base;
+    else l.prim += (int)prim_base;
     dst.lights.push_back(l);
   }
+  dst.envs.insert(dst.envs.end(), src.envs.begin(), src.envs.end());
   dst.A.insert(dst.A.end(), src.A.begin(), src.A.end());
   dst.AB.insert(dst.AB.end(), src.AB.begin(), src.AB.end());
   dst.AC.insert(dst.AC.end(), src.AC.begin(), src.AC.end());

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "../../include/tracer_gpu.h"
+#include "env_light.h"
 #include "scene_types.h"
 
 namespace trg {
@@ -55,6 +56,8 @@ struct HostScene {
   // TR_BVH_DEVICE: no host tree; the primitive bounds (3 floats each) for the device build
   bool device_bvh = false;
   std::vector<float> blo, bhi;
+  // environment lights of the set (DLight::env indexes them)
+  std::vector<EnvHost> envs;
 };
 
 struct RenderBuffers;  // render.cu
@@ -70,6 +73,7 @@ struct tr_ctx {
   trg::DScene dsc{};
   trg::DevBuf d_nodes, d_nodes4, d_slots, d_spheres, d_prims, d_tshade, d_mats, d_lights, d_roots;
   trg::DevBuf d_rays, d_out0, d_out1, d_err;
+  trg::DevBuf d_env_pool, d_envs;  // environment lights: texels and tables, DEnv records
   std::atomic<int> cancel{0};
   trg::RenderBuffers* rb = nullptr;
   tr_tuning tune{20, 0, 16, 8, 2};
@@ -84,6 +88,8 @@ tr_status cuda_fail(tr_ctx* ctx, cudaError_t e, const char* what);
 tr_status set_err(tr_ctx* ctx, tr_status s, const std::string& msg);
 tr_status upload_device_tables(tr_ctx* ctx);
 tr_status upload_device_built(tr_ctx* ctx);  // bvh_gpu.cu: the TR_BVH_DEVICE path
+// Uploads the set's environment lights and sets the scene's envs / has_env.
+tr_status upload_envs(tr_ctx* ctx);
 // Grid of a persistent traversal kernel: SMs x resident blocks (tuned or as many as fit).
 int traversal_grid(const tr_ctx* ctx, const void* kernel);
 // Whether any-hit traversal walks the four-wide tree (tuning and scene allow it).

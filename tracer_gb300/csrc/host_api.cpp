@@ -7,6 +7,7 @@
 // vertices equal the ones the reference's create_triangle_mesh stores
 // (src/shape/triangle.cpp:216-236).
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <unordered_map>
@@ -233,6 +234,39 @@ void put_matrix(std::vector<float>& out, const Matrix4x4& m) {
     for (int j = 0; j < 4; ++j) out.push_back(m.m[i][j]);
 }
 
+// HDRTexture2D (src/texture/hdr_texture.cpp:9-37) behind Texture2D::evaluate
+// with the repeat wrap (src/core/texture.hpp:57-95) and LinearSampler::Sample2D
+// (src/utility/sampler.hpp:16-29).
+class HdrTexture : public Texture2D {
+ public:
+  explicit HdrTexture(RC<Image2D<Color3f>> img) : img_(std::move(img)) {}
+  Spectrum evaluate(const Point2f& uv) const override {
+    auto wrap = [](real x) { return std::clamp<real>(x - std::floor(x), 0, 1); };
+    const int w = img_->width(), h = img_->height();
+    const double u = std::clamp((double)wrap(uv.x), 0.0, 1.0) * (w - 1);
+    const double v = std::clamp((double)wrap(uv.y), 0.0, 1.0) * (h - 1);
+    const int u0 = std::clamp((int)u, 0, w - 1), u1 = std::clamp(u0 + 1, 0, w - 1);
+    const int v0 = std::clamp((int)v, 0, h - 1), v1 = std::clamp(v0 + 1, 0, h - 1);
+    const double du = u - u0, dv = v - v0;
+    auto mul = [](const Color3f& c, double f) { return Color3f{(real)(f * c.x), (real)(f * c.y), (real)(f * c.z)}; };
+    auto add = [](const Color3f& a, const Color3f& b) { return Color3f{a.x + b.x, a.y + b.y, a.z + b.z}; };
+    const Color3f r = add(mul(add(mul(img_->at(u0, v0), 1.0 - du), mul(img_->at(u1, v0), du)), 1.0 - dv),
+                          mul(add(mul(img_->at(u0, v1), 1.0 - du), mul(img_->at(u1, v1), du)), dv));
+    return Spectrum(r.x, r.y, r.z);
+  }
+  const Image2D<Color3f>& image() const { return *img_; }
+
+ private:
+  RC<Image2D<Color3f>> img_;
+};
+
+class IblLight : public EnvironmentLight {
+ public:
+  IblLight(RC<const Texture2D> tex, const Transform& t) : tex(std::move(tex)), world_to_light(t) {}
+  RC<const Texture2D> tex;
+  Transform world_to_light;
+};
+
 class GeneralScene : public Scene {
  public:
   explicit GeneralScene(RC<BvhAggregate> a) : accel_(std::move(a)) {}
@@ -283,10 +317,40 @@ class GeneralScene : public Scene {
       d.prim_emission.insert(d.prim_emission.end(), {gp->emission.r, gp->emission.g, gp->emission.b});
       light_index.emplace(&gp->light, (int)i);
     }
-    for (const Light* l : lights) {
+    for (size_t k = 0; k < lights.size(); ++k) {
+      const Light* l = lights[k];
+      if (dynamic_cast<const EnvironmentLight*>(l)) {
+        if (l != environment_light.get() || k + 1 != lights.size())
+          throw std::invalid_argument("an environment light must be the scene's environment_light and its last light");
+        continue;
+      }
       auto it = light_index.find(l);
       if (it == light_index.end()) throw std::invalid_argument("scene light is not a primitive of this scene");
       d.light_prims.push_back(it->second);
+    }
+    if (environment_light) {
+      if (lights.empty() || lights.back() != environment_light.get())
+        throw std::invalid_argument("the environment light must also be the last entry of scene->lights");
+      const auto* ibl = dynamic_cast<const IblLight*>(environment_light.get());
+      if (!ibl) throw std::invalid_argument("environment light not made by create_ibl_light");
+      if (const auto* ht = dynamic_cast<const HdrTexture*>(ibl->tex.get())) {
+        const Image2D<Color3f>& img = ht->image();
+        d.env_width = (uint32_t)img.width();
+        d.env_height = (uint32_t)img.height();
+        for (int y = 0; y < img.height(); ++y)
+          for (int x = 0; x < img.width(); ++x) {
+            const Color3f& c = img.at(x, y);
+            d.env_texels.insert(d.env_texels.end(), {c.x, c.y, c.z});
+          }
+      } else if (const auto* ct = dynamic_cast<const ConstantTexture*>(ibl->tex.get())) {
+        const Spectrum c = ct->evaluate(Point2f{0, 0});  // a constant map is a 1 x 1 image
+        d.env_width = d.env_height = 1;
+        d.env_texels = {c.r, c.g, c.b};
+      } else {
+        throw std::invalid_argument("environment light texture must be an HDR or constant texture");
+      }
+      put_matrix(d.env_to_light, ibl->world_to_light.matrix());
+      put_matrix(d.env_to_world, ibl->world_to_light.inverse_matrix());
     }
     desc_ = std::move(d);
     ++revision_;
@@ -371,6 +435,16 @@ class GpuRenderer : public GpuPathTraceRenderer {
 // ---------------------------------------------------------------- factories
 
 RC<Texture2D> create_constant_texture2d(const Spectrum& constant) { return std::make_shared<ConstantTexture>(constant); }
+
+RC<Texture2D> create_hdr_texture2d(const RC<Image2D<Color3f>>& image) {
+  if (!image || image->width() <= 0 || image->height() <= 0) throw std::invalid_argument("empty HDR image");
+  return std::make_shared<HdrTexture>(image);
+}
+
+RC<EnvironmentLight> create_ibl_light(RC<const Texture2D> tex, const Transform& world_to_light) {
+  if (!tex) throw std::invalid_argument("environment light without texture");
+  return std::make_shared<IblLight>(std::move(tex), world_to_light);
+}
 
 RC<Shape> create_sphere(real radius, const Transform& local_to_world) {
   if (radius <= 0) throw std::runtime_error("invalid sphere radius");  // src/shape/sphere.cpp:88-90
@@ -523,6 +597,13 @@ tr_scene_desc SceneDesc::view() const {
   d.num_lights = (uint32_t)light_prims.size();
   d.light_prims = light_prims.data();
   d.max_leaf_prims = max_leaf_prims;
+  if (env_width && env_height) {
+    d.env_width = env_width;
+    d.env_height = env_height;
+    d.env_texels = env_texels.data();
+    d.env_to_light = env_to_light.data();
+    d.env_to_world = env_to_world.data();
+  }
   return d;
 }
 

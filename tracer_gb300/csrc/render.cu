@@ -98,6 +98,7 @@ struct JobDev {
   unsigned int seed_base;
   int scene, slot_base;
   int light_base, nl;  // the scene's lights in DScene::lights
+  int env;             // the scene's environment light in DScene::envs (its last light), or -1
   float filter_radius, filter_alpha, filter_exp;
   int fp64;
   float4* film;  // film sums (float4 per pixel, or 2 x double2)
@@ -400,7 +401,19 @@ __global__ void __launch_bounds__(128) k_shadow(Launch P) {
 __device__ f3 mis_contribution(const Launch& P, int slot) {
   const float4 hit = P.HM[slot];
   const int pid = __float_as_int(hit.x);
-  if (pid < 0) return mk3(0.0f, 0.0f, 0.0f);
+  if (pid < 0) {
+    // the ray left the scene: the environment light's share (:156-174)
+    const int ei = job_of(P, slot).env;
+    if (ei < 0) return mk3(0.0f, 0.0f, 0.0f);
+    const DEnv& e = P.sc.envs[ei];
+    const float4 m0 = P.M0[slot], m1 = P.M1[slot], m2 = P.M2[slot];
+    const f3 d = mk3(m1.x, m1.y, m1.z);
+    const f3 Le = env_emit(e, d);
+    if (black(Le)) return mk3(0.0f, 0.0f, 0.0f);
+    const f3 f = muls(mulc(Le, mk3(m2.x, m2.y, m2.z)), m1.w);
+    const float w = power_heuristic(m0.w, env_pdf(e, d));
+    return divs(muls(f, w), m0.w);
+  }
   const DPrim& pr = P.sc.prims[pid];
   if (!pr.emissive) return mk3(0.0f, 0.0f, 0.0f);
   const float4 m0 = P.M0[slot], m1 = P.M1[slot], m2 = P.M2[slot];
@@ -523,6 +536,15 @@ __global__ void __launch_bounds__(128) k_logic(Launch P, int cur) {
     }
     const float4 hit = P.HC[slot];
     const int pid = __float_as_int(hit.x);
+    if (!(flags & F_TERMINATE) && pid < 0 && (path_depth(P.P1[slot].w) == 0 || (flags & F_SPEC))) {
+      // a camera ray or one after a delta sample left the scene: the
+      // environment light's radiance along it (path_trace_renderer.cpp:66-81)
+      const int ei = job_of(P, slot).env;
+      if (ei >= 0) {
+        const float4 p1 = P.P1[slot], p2 = P.P2[slot];
+        L = L + mulc(mk3(p2.x, p2.y, p2.z), env_emit(P.sc.envs[ei], mk3(p1.x, p1.y, p1.z)));
+      }
+    }
     if ((flags & F_TERMINATE) || pid < 0) {
       unsigned long long st = P.rng[slot];
       finish_sample(P, slot, st, L, nxt, finished);
@@ -946,6 +968,35 @@ __global__ void __launch_bounds__(128) k_nee(Launch P) {
     const DLight& lt = P.sc.lights[job_of(P, slot).light_base + l];
     float4* rec = P.SH + 3 * (size_t)item;
     bool ok = false;
+    if (lt.env >= 0) {
+      // sample_environment_light (src/renderer/direct_illumination.cpp:73-106)
+      f3 Le, lpos;
+      float lpdf;
+      if (env_sample(P.sc.envs[lt.env], pos, uv.x, uv.y, Le, lpdf, lpos) && !black(Le)) {
+        f3 to_light = lpos - pos;
+        bool too_close;
+        const float dist = dist_minus_eps(len2f(to_light), too_close);
+        if (!too_close) {
+          to_light = normalize(to_light);
+          const f3 bf = MatOps<KIND>::eval(bsdf, to_light, wo);
+          if (!black(bf)) {
+            const float bpdf = MatOps<KIND>::pdf(bsdf, to_light, wo);
+            const f3 fl = muls(mulc(Le, bf), abs_cos(to_light, bsdf.g.z));
+            const float w = power_heuristic(lpdf, bpdf);
+            const float4 p4 = P.P4[slot];
+            const f3 cc = mulc(mk3(p4.x, p4.y, p4.z), divs(muls(fl, w), lpdf));
+            const f3 sd = normalize(to_light);
+            rec[0] = make_float4(pos.x, pos.y, pos.z, dist);
+            rec[1] = make_float4(sd.x, sd.y, sd.z, 0.0f);
+            rec[2] = make_float4(cc.x, cc.y, cc.z, 1.0f);
+            P.q_sh[append(P.ctr + C_SH)] = item;
+            ok = true;
+          }
+        }
+      }
+      if (!ok) rec[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      continue;
+    }
     // Triangle::sample via UniformSampleTriangle (src/shape/triangle.cpp:61-97)
     const float su0 = sqrtf(uv.x);
     const float bx = 1.0f - su0, by = uv.y * su0;
@@ -1096,6 +1147,7 @@ static JobDev make_job_dev(tr_ctx* ctx, const JobSpec& j, int slot_base, void* f
   J.slot_base = slot_base;
   J.light_base = (int)ctx->hs.scene_light[j.scene];
   J.nl = (int)ctx->hs.scene_nlight[j.scene];
+  J.env = J.nl > 0 ? ctx->hs.lights[J.light_base + J.nl - 1].env : -1;
   J.filter_radius = j.filter.radius;
   J.filter_alpha = j.filter.alpha;
   J.filter_exp = std::exp(-j.filter.alpha * j.filter.radius * j.filter.radius);  // GaussianFilter ctor
@@ -1176,6 +1228,8 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     if (!(gp->alpha >= 0.0f && gp->alpha < 1.0f)) return set_err(ctx, TR_ERR_ARG, "guide alpha must be in [0, 1)");
     if (gp->alpha > 0.0f && (!ctx->guide || !ctx->guide->params.p))
       return set_err(ctx, TR_ERR_STATE, "guide model not initialised");
+    if (gp->alpha > 0.0f && ctx->dsc.has_env)
+      return set_err(ctx, TR_ERR_UNSUPPORTED, "guided sampling covers area lights only, not an environment light");
     for (int k = 0; k < 3; ++k) {
       if (!(gp->box_hi[k] > gp->box_lo[k])) return set_err(ctx, TR_ERR_ARG, "empty guide box");
       P.gbox_lo[k] = gp->box_lo[k];

@@ -113,7 +113,25 @@ struct DLight {
   float area_pdf; // 1 / surface_area()
   int prim;
   float extent;   // sum of |coordinates| of A, B, C plus 1 (scale of the back-side margin)
-  int pad;
+  int env;        // >= 0: the environment light DScene::envs[env] (prim is -1), else -1
+};
+
+// Environment light of one scene: the reference's IBL over an HDR texture
+// (src/light/environment_light.cpp:14-193). Tables built on the host with
+// the reference's arithmetic: the texels, the Distribution2D of its
+// luminance (rows of the conditional p(u | v), the marginal over v), the
+// rotation parts of world_to_light and its inverse, and the scene's
+// bounding sphere.
+struct DEnv {
+  const float4* texels;     // w x h, texel (x, y) at x + y * w
+  const float* cond_func;   // nv x nu
+  const float* cond_cdf;    // nv x (nu + 1)
+  const float* cond_int;    // nv (the marginal's function)
+  const float* marg_cdf;    // nv + 1
+  float marg_int;
+  int w, h, nu, nv;
+  float to_light[9], to_world[9];
+  float center[3], radius;
 };
 
 // Root of one scene of the uploaded set: its tree and its lights.
@@ -141,6 +159,8 @@ struct DScene {
   int max_lights;  // most lights of one scene
   int has_glass;   // some material is a delta BSDF (glass)
   int has_metal;   // some material is metal
+  const DEnv* envs;  // environment lights of the set (DLight::env indexes them)
+  int has_env;       // some scene has an environment light
 };
 
 }  // namespace trg

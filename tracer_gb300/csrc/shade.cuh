@@ -9,6 +9,7 @@
 // arithmetic (traversal, frames, normalisation) is exact.
 #pragma once
 
+#include "env_tex.cuh"
 #include "scene_types.h"
 
 namespace trg {
@@ -749,6 +750,85 @@ __device__ __forceinline__ float light_pdf_at(float area, f3 ref, f3 pos, f3 n) 
   const float abscos = fabsf(cos_x(n, p2ref));
   area *= abscos;
   return dist2 / area;
+}
+
+// ------------------------------------------------------- environment light
+// The vector part of a Transform (src/utility/transform.hpp:89-95), 3 x 3 row-major.
+__device__ __forceinline__ f3 rot3(const float* m, f3 v) {
+  return mk3(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[3] * v.x + m[4] * v.y + m[5] * v.z,
+             m[6] * v.x + m[7] * v.y + m[8] * v.z);
+}
+__device__ __forceinline__ float clamp_pm1(float z) { return z < -1.0f ? -1.0f : (1.0f < z ? 1.0f : z); }
+__device__ __forceinline__ float clamp01(float x) { return x < 0.0f ? 0.0f : (1.0f < x ? 1.0f : x); }
+
+// IBL::light_emit (src/light/environment_light.cpp:172-182): the map at
+// (phi / 2pi, theta / pi) of the direction in light space.
+__device__ __forceinline__ f3 env_emit(const DEnv& e, f3 d) {
+  f3 dir = normalize(d);
+  dir = normalize(rot3(e.to_light, dir));
+  const float phi = local_phi(dir);
+  const float theta = acosf(clamp_pm1(dir.z));
+  return env_tex_eval(e.texels, e.w, e.h, clamp01(phi / (2.0f * kPi)), clamp01(theta * kInvPi));
+}
+
+// Distribution1D::sample_continuous (src/utility/distribution.hpp:37-55):
+// the cell is the last index whose cdf is not above u (std::lower_bound over
+// the reversed cdf), the offset inside it linear.
+__device__ __forceinline__ float dist1d_sample(const float* __restrict__ func, const float* __restrict__ cdf, int n,
+                                               float func_int, float u, float& pdf, int& off) {
+  int lo = 0, hi = n + 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (cdf[mid] > u) hi = mid;
+    else lo = mid + 1;
+  }
+  int offset = lo - 1;
+  offset = offset < 0 ? 0 : (offset > n - 1 ? n - 1 : offset);
+  off = offset;
+  float du = u - cdf[offset];
+  if (cdf[offset + 1] - cdf[offset] > 0.0f) du /= cdf[offset + 1] - cdf[offset];
+  pdf = func_int > 0.0f ? func[offset] / func_int : 0.0f;
+  return ((float)offset + du) / (float)n;
+}
+
+// IBL::sample_li (src/light/environment_light.cpp:88-116) through
+// Distribution2D::sample_continuous (src/utility/distribution.hpp:95-102).
+// Returns false where the reference returns an empty sample.
+__device__ __forceinline__ bool env_sample(const DEnv& e, f3 ref, float u, float v, f3& radiance, float& pdf,
+                                           f3& pos) {
+  float p0, p1;
+  int iv, iu;
+  const float d1 = dist1d_sample(e.cond_int, e.marg_cdf, e.nv, e.marg_int, v, p1, iv);
+  const float d0 = dist1d_sample(e.cond_func + (size_t)iv * e.nu, e.cond_cdf + (size_t)iv * (e.nu + 1), e.nu,
+                                 e.cond_int[iv], u, p0, iu);
+  const float map_pdf = p0 * p1;
+  if (map_pdf == 0.0f) return false;
+  const float theta = d1 * kPi, phi = d0 * 2.0f * kPi;
+  const float cos_theta = cosf(theta), sin_theta = sinf(theta);
+  const float sin_phi = sinf(phi), cos_phi = cosf(phi);
+  f3 wi = mk3(sin_theta * cos_phi, sin_theta * sin_phi, cos_theta);
+  wi = normalize(rot3(e.to_world, wi));
+  if (sin_theta == 0.0f) return false;
+  pdf = map_pdf / (2.0f * kPi * kPi * sin_theta);
+  radiance = env_emit(e, wi);
+  pos = ref + scale(wi, 2.0f * e.radius);
+  return true;
+}
+
+// IBL::pdf (src/light/environment_light.cpp:184-191) with Distribution2D::pdf
+// (src/utility/distribution.hpp:103-107), which multiplies the conditional's
+// function by the marginal integral.
+__device__ __forceinline__ float env_pdf(const DEnv& e, f3 d) {
+  const f3 wi = rot3(e.to_light, d);
+  const float theta = acosf(clamp_pm1(wi.z));
+  float phi = atan2f(wi.y, wi.x);
+  phi = phi < 0.0f ? phi + 2.0f * kPi : phi;
+  const float sin_theta = sinf(theta);
+  if (sin_theta == 0.0f) return 0.0f;
+  int iu = (int)(phi * kInv2Pi * (float)e.nu), iv = (int)(theta * kInvPi * (float)e.nv);
+  iu = iu < 0 ? 0 : (iu > e.nu - 1 ? e.nu - 1 : iu);
+  iv = iv < 0 ? 0 : (iv > e.nv - 1 ? e.nv - 1 : iv);
+  return e.cond_func[(size_t)iv * e.nu + iu] * e.marg_int / (2.0f * kPi * kPi * sin_theta);
 }
 
 // ------------------------------------------------------------------ camera

@@ -289,9 +289,10 @@ def rotate_x(theta):
     return m, np.ascontiguousarray(m.reshape(4, 4).T).ravel()
 
 
-def outdoor(width=96, height=64, spp=8, max_depth=6, min_depth=3, env_size=(64, 32), area_light=True):
+def outdoor(width=96, height=64, spp=8, max_depth=6, min_depth=3, env_size=(64, 32), area_light=True, glass=True):
     """An open scene under an environment light: a ground quad, Disney12,
-    metal, glass and Lambertian spheres, optionally one small area light; the
+    metal, glass (Lambertian when `glass` is False) and Lambertian spheres,
+    optionally one small area light; the
     sky map of `sky_map` with world +y as the light's +z (world_to_light =
     rotate_x(pi/2), as the reference's demo does)."""
     b = _Builder()
@@ -304,7 +305,8 @@ def outdoor(width=96, height=64, spp=8, max_depth=6, min_depth=3, env_size=(64, 
                                 specular=0.5, clearcoat=0.5, clearcoat_gloss=0.7, sheen_tint=0.5)),
             b.material(Material(kind=TR_MAT_METAL, color=(0.95, 0.64, 0.54), eta=(0.2, 0.92, 1.1),
                                 k=(3.9, 2.45, 2.14), roughness=0.25, anisotropic=0.0)),
-            b.material(Material(kind=TR_MAT_GLASS, kr=(1.0, 1.0, 1.0), kt=(1.0, 1.0, 1.0), ior=1.5)),
+            b.material(Material(kind=TR_MAT_GLASS, kr=(1.0, 1.0, 1.0), kt=(1.0, 1.0, 1.0), ior=1.5) if glass
+                       else lambert((0.7, 0.7, 0.7))),
             b.material(lambert((0.2, 0.5, 0.3)))]
     for k, m in enumerate(mats):
         b.sphere((-2.25 + 1.5 * k, 0.6, 0.0), 0.6, m)
