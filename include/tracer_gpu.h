@@ -57,7 +57,7 @@ typedef struct tr_bvh_node32 {
   uint8_t pad;
 } tr_bvh_node32;
 
-enum { TR_MAT_PHONG = 0, TR_MAT_DISNEY12 = 1, TR_MAT_GLASS = 2, TR_MAT_METAL = 3 };
+enum { TR_MAT_PHONG = 0, TR_MAT_DISNEY12 = 1, TR_MAT_GLASS = 2, TR_MAT_METAL = 3, TR_MAT_DISNEY15 = 4 };
 
 /* Material record. Phong is create_phong_material(ka, kd, ks, ns)
  * (src/factory/material.hpp:19-24, src/material/phong.cpp:29-70); Disney12 is
@@ -83,6 +83,13 @@ typedef struct tr_material {
    * parameter order are reproduced as the reference has them), roughness
    * and anisotropic take the fields above. */
   float color[3], eta[3], k[3];
+  /* Disney 2015: create_disney(base_color, metallic, roughness, transmission,
+   * transmission_roughness, ior, specular_scale, specular_tint, anisotropic,
+   * sheen, sheen_tint, clearcoat, clearcoat_gloss) with no normal mapper and
+   * no BSSRDF (src/material/disney.cpp:541-677); the fields above hold
+   * base_color, metallic, roughness, specular_tint, anisotropic, sheen,
+   * sheen_tint, clearcoat, clearcoat_gloss and ior. */
+  float transmission, transmission_roughness, specular_scale[3];
 } tr_material;
 
 /* Flat scene description. It records what the reference factory calls build

@@ -23,6 +23,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "core/bssrdf.hpp"
 #include "core/camera.hpp"
 #include "core/light.hpp"
 #include "core/render.hpp"
@@ -104,6 +105,12 @@ void* ref_scene_create(const tr_scene_desc* d) {
       s->materials.push_back(create_phong_material(ctex3(m.ka), ctex3(m.kd), ctex3(m.ks), ctex(m.ns)));
     } else if (m.kind == TR_MAT_GLASS) {
       s->materials.push_back(create_glass(ctex3(m.kr), ctex3(m.kt), ctex(m.ior)));
+    } else if (m.kind == TR_MAT_DISNEY15) {
+      s->materials.push_back(create_disney(
+          ctex3(m.base_color), ctex(m.metallic), ctex(m.roughness), ctex(m.transmission),
+          ctex(m.transmission_roughness), ctex(m.ior), ctex3(m.specular_scale), ctex(m.specular_tint),
+          ctex(m.anisotropic), ctex(m.sheen), ctex(m.sheen_tint), ctex(m.clearcoat), ctex(m.clearcoat_gloss),
+          newBox<const NormalMapper>(nullptr), newRC<BSSRDFSurface>()));
     } else if (m.kind == TR_MAT_METAL) {
       s->materials.push_back(create_metal(ctex3(m.color), ctex3(m.eta), ctex3(m.k), ctex(m.roughness),
                                           ctex(m.anisotropic), newBox<NormalMapper>()));

@@ -115,6 +115,7 @@ inline Sp operator*(Sp a, real s) { return Sp(a.r * s, a.g * s, a.b * s); }
 inline Sp operator/(Sp a, real s) { return Sp(a.r / s, a.g / s, a.b / s); }
 inline Sp operator+(Sp a, real s) { return Sp(a.r + s, a.g + s, a.b + s); }
 inline void operator+=(Sp& a, Sp b) { a = a + b; }
+inline Sp operator-(Sp a, Sp b) { return Sp(a.r - b.r, a.g - b.g, a.b - b.b); }
 // geometry.hpp:989-993 mix() with a Spectrum pair and a float factor
 inline Sp mix(Sp l, Sp r, real f) { return l * (1 - f) + r * f; }
 inline real mixf(real l, real r, real f) { return (1 - f) * l + f * r; }
@@ -250,6 +251,12 @@ struct Mat {
   // GGX alphas (bxdf/microfacet_refl_bxdf.cpp:6-11); base holds the colour.
   Sp f_eta2, f_etak2, f_paint;
   real ax_m, ay_m;
+  // DisneyBSDF's constructor (material/disney.cpp:341-392), with base,
+  // metallic, roughness, specular_tint, anisotropic, sheen, sheen_tint and
+  // clearcoat above: tint colour, specular scale, transmission, IOR, the
+  // alphas, clearcoat roughness and the four sampling weights
+  Sp c_tint, spec_scale;
+  real transmission, ior15, ax15, ay15, trans_ax, trans_ay, cc_rough, w_diff, w_trans, w_spec, w_cc;
 };
 struct Prim {
   int kind;  // 0 triangle, 1 sphere
@@ -1363,17 +1370,216 @@ struct BSDF {
     return out;
   }
 
+  // ---- DisneyBSDF, the 2015 model (material/disney.cpp:14-537), radiance transport
+  static real gtr2_D(V3 lwh, real ax, real ay) {
+    const real phi_h = local_phi(lwh);
+    return anisotropic_gtr2(std::sin(phi_h), std::cos(phi_h), local_cos_to_sin(lwh.z), lwh.z, ax, ay);
+  }
+  static real smith_G(V3 lw, real ax, real ay) {
+    const real phi = local_phi(lw);
+    return smith_anisotropic_gtr2(std::cos(phi), std::sin(phi), ax, ay, local_tan_theta(lw));
+  }
+  static real schlick1(real R0, real c) { return R0 + (1 - R0) * one_minus_5(c); }
+  Sp d15_f_transmission(V3 lwi, V3 lwo) const {
+    const real cos_theta_i = lwi.z, cos_theta_o = lwo.z;
+    const real eta = cos_theta_o > 0 ? m->ior15 : 1 / m->ior15;
+    V3 lwh = normalize(lwo + mulf(lwi, eta));
+    if (lwh.z < 0) lwh = -lwh;
+    const real cos_theta_d = dot(lwo, lwh);
+    const real F = dielectric_fresnel(m->ior15, 1, cos_theta_d);
+    const real D = gtr2_D(lwh, m->trans_ax, m->trans_ay);
+    const real G = smith_G(lwi, m->trans_ax, m->trans_ay) * smith_G(lwo, m->trans_ax, m->trans_ay);
+    const real sdem = cos_theta_d + eta * dot(lwi, lwh);
+    const real corr = 1 / eta;
+    const Sp sqrtC(std::sqrt(m->base.r), std::sqrt(m->base.g), std::sqrt(m->base.b));
+    const real val = (1 - F) * D * G * eta * eta * dot(lwi, lwh) * dot(lwo, lwh) * corr * corr /
+                     (cos_theta_i * cos_theta_o * sdem * sdem);
+    const real trans_factor = cos_theta_o > 0 ? m->transmission : 1;
+    return sqrtC * ((1 - m->metallic) * trans_factor) * std::abs(val);
+  }
+  Sp d15_f_inner_reflection(V3 lwi, V3 lwo) const {
+    const V3 lwh = -normalize(lwi + lwo);
+    const real cos_theta_d = dot(lwo, lwh);
+    const real F = dielectric_fresnel(m->ior15, 1, cos_theta_d);
+    const real D = gtr2_D(lwh, m->trans_ax, m->trans_ay);
+    const real G = smith_G(lwi, m->trans_ax, m->trans_ay) * smith_G(lwo, m->trans_ax, m->trans_ay);
+    return m->base * m->transmission * std::abs(F * D * G / (4 * lwi.z * lwo.z));
+  }
+  Sp d15_f_diffuse(real ci, real co, real cd) const {
+    const Sp f_lambert = m->base / kPi;
+    const real FL = one_minus_5(ci), FV = one_minus_5(co);
+    const real RR = 2 * m->roughness * cd * cd;
+    const Sp retro = m->base / kPi * RR * (FL + FV + FL * FV * (RR - 1));
+    return f_lambert * (1 - real(0.5) * FL) * (1 - real(0.5) * FV) + retro;
+  }
+  Sp d15_f_sheen(real cd) const {
+    return mix(Sp(1), m->c_tint, m->sheen_tint) * (4 * m->sheen) * one_minus_5(cd);
+  }
+  Sp d15_f_specular(V3 lwi, V3 lwo) const {
+    const V3 lwh = normalize(lwi + lwo);
+    const real cd = dot(lwi, lwh);
+    const Sp Cspec = mix(mix(Sp(1), m->c_tint, m->specular_tint), m->base, m->metallic);
+    const Sp dielectric = Cspec * dielectric_fresnel(m->ior15, 1, cd);
+    const Sp conductor = Cspec + (Sp(1) - Cspec) * one_minus_5(cd);
+    const Sp F = mix(m->spec_scale * dielectric, conductor, m->metallic);
+    const real D = gtr2_D(lwh, m->ax15, m->ay15);
+    const real G = smith_G(lwi, m->ax15, m->ay15) * smith_G(lwo, m->ax15, m->ay15);
+    return F * D * G / std::abs(4 * lwi.z * lwo.z);
+  }
+  real d15_pdf_transmission(V3 lwi, V3 lwo) const {
+    const real eta = lwo.z > 0 ? m->ior15 : 1 / m->ior15;
+    V3 lwh = normalize(lwo + mulf(lwi, eta));
+    if (lwh.z < 0) lwh = -lwh;
+    if (((lwo.z > 0) != (dot(lwh, lwo) > 0)) || ((lwi.z > 0) != (dot(lwh, lwi) > 0))) return 0;
+    const real sdem = dot(lwo, lwh) + eta * dot(lwi, lwh);
+    const real dwh_to_dwi = eta * eta * dot(lwi, lwh) / (sdem * sdem);
+    const real D = gtr2_D(lwh, m->trans_ax, m->trans_ay);
+    return std::abs(dot(lwi, lwh) * D * dwh_to_dwi);
+  }
+  real d15_pdf_inner_reflection(V3 lwi, V3 lwo) const {
+    const V3 lwh = -normalize(lwi + lwo);
+    const real D = gtr2_D(lwh, m->trans_ax, m->trans_ay);
+    return std::abs(lwh.z * D / (4 * dot(lwi, lwh)));
+  }
+  void d15_pdf_spec_cc(V3 lwi, V3 lwo, real& ps, real& pc) const {
+    const V3 lwh = normalize(lwi + lwo);
+    const real cos_theta_h = lwh.z, sin_theta_h = local_cos_to_sin(cos_theta_h);
+    const real cd = dot(lwi, lwh);
+    const real cos_phi_o = std::cos(local_phi(lwo));
+    const real sin_phi_o = local_cos_to_sin(cos_phi_o);
+    const real spec_D = gtr2_D(lwh, m->ax15, m->ay15);
+    ps = smith_anisotropic_gtr2(cos_phi_o, sin_phi_o, m->ax15, m->ay15, local_tan_theta(lwo)) * spec_D / (4 * lwo.z);
+    pc = cos_theta_h * gtr1(sin_theta_h, cos_theta_h, m->cc_rough) / (4 * cd);
+  }
+  Sp d15_eval(V3 wi, V3 wo) const {
+    if (fringe(wi, wo)) return eval_fringe(wi, wo);
+    const V3 lwi = normalize(s.to_local(wi)), lwo = normalize(s.to_local(wo));
+    if (std::abs(lwi.z) < kEps || std::abs(lwo.z) < kEps) return Sp();
+    if (lwi.z * lwo.z < 0) {
+      if (m->transmission == 0) return Sp();
+      return d15_f_transmission(lwi, lwo) * normal_correct_factor(g, s, wi);
+    }
+    if (lwi.z < 0 && lwo.z < 0) {
+      if (m->transmission == 0) return Sp();
+      return d15_f_inner_reflection(lwi, lwo) * normal_correct_factor(g, s, wi);
+    }
+    const V3 lwh = normalize(lwi + lwo);
+    const real cd = dot(lwi, lwh);
+    Sp diffuse, sheen;
+    if (m->metallic < 1) {
+      diffuse = d15_f_diffuse(lwi.z, lwo.z, cd);
+      if (m->sheen > 0) sheen = d15_f_sheen(cd);
+    }
+    const Sp specular = d15_f_specular(lwi, lwo);
+    Sp clearcoat;
+    if (m->clearcoat > 0) {
+      const real ch = lwh.z, sh = local_cos_to_sin(ch);
+      const real D = gtr1(sh, ch, m->cc_rough);
+      const real F = schlick1(real(0.04), cd);
+      const real G = smith_gtr2(local_tan_theta(lwi), real(0.25)) * smith_gtr2(local_tan_theta(lwo), real(0.25));
+      clearcoat = Sp(m->clearcoat * D * F * G / std::abs(4 * lwi.z * lwo.z));
+    }
+    const Sp ret = (diffuse + sheen) * ((1 - m->metallic) * (1 - m->transmission)) + specular + clearcoat;
+    return ret * normal_correct_factor(g, s, wi);
+  }
+  real d15_pdf(V3 wi, V3 wo) const {
+    if (fringe(wi, wo)) return pdf_fringe(wi, wo);
+    const V3 lwi = normalize(s.to_local(wi)), lwo = normalize(s.to_local(wo));
+    if (std::abs(lwi.z) < kEps || std::abs(lwo.z) < kEps) return 0;
+    if (lwo.z < 0) {
+      if (m->transmission == 0) return 0;
+      real macro_F = std::clamp<real>(dielectric_fresnel(m->ior15, 1, lwo.z), real(0.1), real(0.9));
+      if (lwi.z > 0) return (1 - macro_F) * d15_pdf_transmission(lwi, lwo);
+      return macro_F * d15_pdf_inner_reflection(lwi, lwo);
+    }
+    if (lwi.z < 0) return m->w_trans * d15_pdf_transmission(lwi, lwo);
+    const real diffuse = cosine_pdf(lwi.z);
+    real ps, pc;
+    d15_pdf_spec_cc(lwi, lwo, ps, pc);
+    return m->w_diff * diffuse + m->w_spec * ps + m->w_cc * pc;
+  }
+  BSDFSample d15_sample(V3 wo, real u, real v, real w) const {
+    if (fringe(wo)) return sample_fringe(wo, u, v);
+    BSDFSample out;
+    const V3 lwo = normalize(s.to_local(wo));
+    if (std::abs(lwo.z) < kEps) return out;
+    if (lwo.z < 0 && m->transmission == 0) return out;
+    // the lobe choice (disney.cpp:471-488): the second test is not inside the
+    // first one's else, so a diffuse draw is always replaced by one of the
+    // other three lobes (the cosine sample has no side effects and is skipped)
+    real sel = u;
+    V3 lwi(0, 0, 0);
+    if (!(sel < m->w_diff)) sel -= m->w_diff;
+    {
+      if (sel < m->w_trans) {
+        // sample_transmission (disney.cpp:286-306)
+        const V3 lwh = sample_anisotropic_gtr2(m->trans_ax, m->trans_ay, v, w);
+        if (lwh.z > 0 && (lwo.z > 0) == (dot(lwh, lwo) > 0)) {
+          const real eta = lwo.z > 0 ? 1 / m->ior15 : m->ior15;
+          const V3 owh = dot(lwh, lwo) > 0 ? lwh : -lwh;
+          V3 t;
+          if (refract_dir(lwo, owh, eta, t)) {
+            const V3 tn = normalize(t);
+            if (!(tn.z * lwo.z > 0 || ((tn.z > 0) != (dot(lwh, tn) > 0)))) lwi = tn;
+          }
+        }
+      } else {
+        sel -= m->w_trans;
+        if (sel < m->w_spec) {
+          // sample_specular (disney.cpp:322-333)
+          const V3 lwh = normalize(sample_vndf15(lwo, v, w));
+          if (lwh.z > 0) {
+            const V3 t = normalize(mulf(lwh, 2 * dot(lwo, lwh)) - lwo);
+            if (t.z > 0) lwi = t;
+          }
+        } else {
+          // sample_clearcoat (disney.cpp:334-344)
+          const V3 lwh = sample_gtr1(m->cc_rough, v, w);
+          if (lwh.z > 0) {
+            const V3 t = normalize(mulf(lwh, 2 * dot(lwo, lwh)) - lwo);
+            if (t.z > 0) lwi = t;
+          }
+        }
+      }
+    }
+    if (!lwi.x && !lwi.y && !lwi.z) return out;
+    const V3 wi = s.to_global(lwi);
+    out.wi = wi;
+    out.f = d15_eval(wi, wo);
+    out.pdf = d15_pdf(wi, wo);
+    return out;
+  }
+  // microfacet::sample_anisotropic_gtr2_with_visible_normal with the 2015 alphas
+  V3 sample_vndf15(V3 ve, real u, real v) const {
+    const real ax = m->ax15, ay = m->ay15;
+    const V3 vh = normalize(V3(ax * ve.x, ay * ve.y, ve.z));
+    const real lensq = vh.x * vh.x + vh.y * vh.y;
+    const V3 t1 = lensq > kEps ? divd(V3(-vh.y, vh.x, 0), std::sqrt(lensq)) : V3(1, 0, 0);
+    const V3 t2 = cross(vh, t1);
+    const real r = std::sqrt(u);
+    const real phi = 2 * kPi * v;
+    const real t_1 = r * std::cos(phi);
+    const real _t_2 = r * std::sin(phi);
+    const real sh = real(0.5) * (1 + vh.z);
+    const real t_2 = (1 - sh) * std::sqrt(1 - t_1 * t_1) + sh * _t_2;
+    const V3 nh = mulf(t1, t_1) + mulf(t2, t_2) + mulf(vh, std::sqrt(std::max(real(0), 1 - t_1 * t_1 - t_2 * t_2)));
+    return normalize(V3(ax * nh.x, ay * nh.y, std::max(real(0), nh.z)));
+  }
+
   Sp eval(V3 wi, V3 wo) const {
+    if (m->kind == TR_MAT_DISNEY15) return d15_eval(wi, wo);
     if (m->kind == TR_MAT_METAL) return metal_eval(wi, wo);
     return m->kind == TR_MAT_PHONG ? phong_agg_eval(wi, wo) : (m->kind == TR_MAT_DISNEY12 ? disney_eval(wi, wo) : Sp());
   }
   real pdf(V3 wi, V3 wo) const {
+    if (m->kind == TR_MAT_DISNEY15) return d15_pdf(wi, wo);
     if (m->kind == TR_MAT_METAL) return metal_pdf(wi, wo);
     return m->kind == TR_MAT_PHONG ? phong_agg_pdf(wi, wo) : (m->kind == TR_MAT_DISNEY12 ? disney_pdf(wi, wo) : 0);
   }
   BSDFSample sample(V3 wo, real u, real v, real w) const {
     if (m->kind == TR_MAT_GLASS) return glass_sample(wo, u);
     if (m->kind == TR_MAT_METAL) return metal_sample(wo, u, v, w);
+    if (m->kind == TR_MAT_DISNEY15) return d15_sample(wo, u, v, w);
     return m->kind == TR_MAT_PHONG ? phong_agg_sample(wo, u, v, w) : disney_sample(wo, u, v, w);
   }
 };
@@ -1761,6 +1967,32 @@ void* orc_scene_create(const tr_scene_desc* d) {
       const real aspect = src.anisotropic > 0 ? std::sqrt(1 - real(0.9) * src.anisotropic) : real(1);
       m.ax_m = std::max(real(0.001), src.roughness * src.roughness / aspect);
       m.ay_m = std::max(real(0.001), src.roughness * src.roughness * aspect);
+    } else if (src.kind == TR_MAT_DISNEY15) {
+      // Disney::shading + DisneyBSDF's constructor (material/disney.cpp:341-392,616-651)
+      m.base = Sp(src.base_color[0], src.base_color[1], src.base_color[2]);
+      m.metallic = src.metallic; m.roughness = src.roughness; m.specular_tint = src.specular_tint;
+      m.anisotropic = src.anisotropic; m.sheen = src.sheen; m.sheen_tint = src.sheen_tint;
+      m.clearcoat = src.clearcoat;
+      m.spec_scale = Sp(src.specular_scale[0], src.specular_scale[1], src.specular_scale[2]);
+      m.transmission = src.transmission;
+      const real lum = m.base.lum();
+      m.c_tint = lum > 0 ? m.base / lum : Sp(1);
+      m.ior15 = std::max(real(1.01), src.ior);
+      const real aspect = src.anisotropic > 0 ? std::sqrt(1 - real(0.9) * src.anisotropic) : real(1);
+      m.ax15 = std::max(real(0.001), src.roughness * src.roughness / aspect);
+      m.ay15 = std::max(real(0.001), src.roughness * src.roughness * aspect);
+      const real tr = src.transmission_roughness;
+      m.trans_ax = std::max(real(0.001), tr * tr / aspect);
+      m.trans_ay = std::max(real(0.001), tr * tr * aspect);
+      real cr = mixf(real(0.1), real(0), src.clearcoat_gloss);
+      cr *= cr;
+      m.cc_rough = std::max(cr, real(0.0001));
+      const real A = std::clamp(m.base.lum() * (1 - m.metallic), real(0.3), real(0.7));
+      const real B = 1 - A;
+      m.w_diff = A * (1 - m.transmission);
+      m.w_trans = A * m.transmission;
+      m.w_spec = B * 2 / (2 + m.clearcoat);
+      m.w_cc = B * m.clearcoat / (2 + m.clearcoat);
     } else if (src.kind == TR_MAT_GLASS) {
       m.kr = Sp(src.kr[0], src.kr[1], src.kr[2]);
       m.kt_sqrt = Sp(std::sqrt(src.kt[0]), std::sqrt(src.kt[1]), std::sqrt(src.kt[2]));

@@ -102,6 +102,17 @@ def test_environment_light(area_light, env_size, min_depth):
     assert np.array_equal(bits(port.render(par)), bits(ref.render(par)))
 
 
+@pytest.mark.parametrize("env,min_depth", [(True, 3), (False, 8), (True, 1)])
+def test_disney15(env, min_depth):
+    """The 2015 Disney BSDF (create_disney): rough transmission and inner
+    reflection, the specular, sheen and clearcoat lobes and its lobe choice."""
+    sc, cam, filt, par = scenes.disney15_row(48, 24, 4, min_depth=min_depth, env=env)
+    port, ref = oracle.Oracle(sc, "port"), oracle.Oracle(sc, "reference")
+    port.set_camera(cam, filt)
+    ref.set_camera(cam, filt)
+    assert np.array_equal(bits(port.render(par)), bits(ref.render(par)))
+
+
 def test_make_ray():
     for o, d in (((0, 0, 0), (1, 2, 3)), ((1, -1, 0.5), (1e-9, 1, 0)), ((0, 0, 0), (-0.0, 0.0, -3))):
         a = oracle.make_ray("port", o, d, 0.0, 1.0)

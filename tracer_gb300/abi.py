@@ -24,6 +24,7 @@ TR_MAT_PHONG = 0
 TR_MAT_DISNEY12 = 1
 TR_MAT_GLASS = 2
 TR_MAT_METAL = 3
+TR_MAT_DISNEY15 = 4
 
 f32p = C.POINTER(C.c_float)
 f64p = C.POINTER(C.c_double)
@@ -57,7 +58,9 @@ class TrMaterial(C.Structure):
                 ("specular_tint", C.c_float), ("roughness", C.c_float), ("anisotropic", C.c_float),
                 ("sheen", C.c_float), ("sheen_tint", C.c_float), ("clearcoat", C.c_float),
                 ("clearcoat_gloss", C.c_float), ("kr", C.c_float * 3), ("kt", C.c_float * 3), ("ior", C.c_float),
-                ("color", C.c_float * 3), ("eta", C.c_float * 3), ("k", C.c_float * 3)]
+                ("color", C.c_float * 3), ("eta", C.c_float * 3), ("k", C.c_float * 3),
+                ("transmission", C.c_float), ("transmission_roughness", C.c_float),
+                ("specular_scale", C.c_float * 3)]
 
 
 class TrSceneDesc(C.Structure):
@@ -129,7 +132,9 @@ def ptr(a: np.ndarray | None, ctype):
 @dataclass
 class Material:
     """One tr_material. kind=TR_MAT_PHONG uses ka/kd/ks/ns; Disney12 base_color .. clearcoat_gloss;
-    TR_MAT_GLASS kr/kt/ior; TR_MAT_METAL color/eta/k with roughness/anisotropic."""
+    TR_MAT_GLASS kr/kt/ior; TR_MAT_METAL color/eta/k with roughness/anisotropic; TR_MAT_DISNEY15
+    base_color, metallic, roughness, transmission, transmission_roughness, ior, specular_scale,
+    specular_tint, anisotropic, sheen, sheen_tint, clearcoat, clearcoat_gloss."""
     kind: int = TR_MAT_PHONG
     ka: tuple = (0.0, 0.0, 0.0)
     kd: tuple = (0.0, 0.0, 0.0)
@@ -152,6 +157,9 @@ class Material:
     color: tuple = (0.0, 0.0, 0.0)
     eta: tuple = (0.0, 0.0, 0.0)
     k: tuple = (0.0, 0.0, 0.0)
+    transmission: float = 0.0
+    transmission_roughness: float = 0.0
+    specular_scale: tuple = (0.0, 0.0, 0.0)
 
     def to_c(self) -> TrMaterial:
         m = TrMaterial()
@@ -162,11 +170,13 @@ class Material:
         m.ns = self.ns
         m.base_color[:] = self.base_color
         for k in ("subsurface", "metallic", "specular", "specular_tint", "roughness", "anisotropic",
-                  "sheen", "sheen_tint", "clearcoat", "clearcoat_gloss", "ior"):
+                  "sheen", "sheen_tint", "clearcoat", "clearcoat_gloss", "ior", "transmission",
+                  "transmission_roughness"):
             setattr(m, k, getattr(self, k))
         m.kr[:] = self.kr
         m.kt[:] = self.kt
         m.color[:] = self.color
+        m.specular_scale[:] = self.specular_scale
         m.eta[:] = self.eta
         m.k[:] = self.k
         return m

@@ -474,9 +474,11 @@ tr_status upload_device_built(tr_ctx* ctx) {
   sc.max_lights = max_lights;
   sc.has_glass = 0;
   sc.has_metal = 0;
+  sc.has_disney15 = 0;
   for (const DMat& m : hs.mats) {
     sc.has_glass |= m.kind == MAT_GLASS;
     sc.has_metal |= m.kind == MAT_METAL;
+    sc.has_disney15 |= m.kind == MAT_DISNEY15;
   }
   tr_status es = upload_envs(ctx);
   if (es != TR_OK) return es;

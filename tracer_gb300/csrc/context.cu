@@ -88,6 +88,39 @@ DMat derive_material(const tr_material& m) {
     const float aspect = m.anisotropic > 0.0f ? std::sqrt(1.0f - 0.9f * m.anisotropic) : 1.0f;
     d.ax = smax(0.001f, m.roughness * m.roughness / aspect);
     d.ay = smax(0.001f, m.roughness * m.roughness * aspect);
+  } else if (m.kind == TR_MAT_DISNEY15) {
+    // Disney::shading and DisneyBSDF's constructor (src/material/disney.cpp:341-392,616-651)
+    d.kind = MAT_DISNEY15;
+    d.base = mk3(m.base_color[0], m.base_color[1], m.base_color[2]);
+    d.albedo = d.base;  // get_albedo(): C_
+    d.metallic = m.metallic;
+    d.roughness = m.roughness;
+    d.specular_tint = m.specular_tint;
+    d.anisotropic = m.anisotropic;
+    d.sheen = m.sheen;
+    d.sheen_tint = m.sheen_tint;
+    d.clearcoat = m.clearcoat;
+    d.spec_scale = mk3(m.specular_scale[0], m.specular_scale[1], m.specular_scale[2]);
+    d.transmission = m.transmission;
+    const float l = lum(d.base);  // to_tint
+    d.c_tint = l > 0.0f ? mk3(d.base.x / l, d.base.y / l, d.base.z / l) : mk3(1.0f, 1.0f, 1.0f);
+    d.ior = smax(1.01f, m.ior);
+    const float aspect = m.anisotropic > 0.0f ? std::sqrt(1.0f - 0.9f * m.anisotropic) : 1.0f;
+    d.ax = smax(0.001f, m.roughness * m.roughness / aspect);
+    d.ay = smax(0.001f, m.roughness * m.roughness * aspect);
+    const float tr = m.transmission_roughness;
+    d.trans_ax = smax(0.001f, tr * tr / aspect);
+    d.trans_ay = smax(0.001f, tr * tr * aspect);
+    float cr = (1.0f - m.clearcoat_gloss) * 0.1f + m.clearcoat_gloss * 0.0f;  // mix(0.1, 0, gloss)
+    cr *= cr;
+    d.cc_rough = smax(cr, 0.0001f);
+    float A = lum(d.base) * (1.0f - d.metallic);
+    A = A < 0.3f ? 0.3f : (0.7f < A ? 0.7f : A);
+    const float B = 1.0f - A;
+    d.w_diff15 = A * (1.0f - d.transmission);
+    d.w_trans = A * d.transmission;
+    d.w_spec15 = B * 2.0f / (2.0f + d.clearcoat);
+    d.w_cc = B * d.clearcoat / (2.0f + d.clearcoat);
   } else if (m.kind == TR_MAT_GLASS) {
     d.kind = MAT_GLASS;
     d.kr = mk3(m.kr[0], m.kr[1], m.kr[2]);
@@ -335,9 +368,11 @@ tr_status upload_device_tables(tr_ctx* ctx) {
   sc.max_lights = max_lights;
   sc.has_glass = 0;
   sc.has_metal = 0;
+  sc.has_disney15 = 0;
   for (const DMat& m : hs.mats) {
     sc.has_glass |= m.kind == MAT_GLASS;
     sc.has_metal |= m.kind == MAT_METAL;
+    sc.has_disney15 |= m.kind == MAT_DISNEY15;
   }
   tr_status es = upload_envs(ctx);
   if (es != TR_OK) return es;
@@ -578,7 +613,8 @@ static tr_status build_host_scene(tr_ctx* ctx, const tr_scene_desc* d, HostScene
       return set_err(ctx, TR_ERR_ARG, "triangle index out of range");
   for (uint32_t m = 0; m < d->num_materials; ++m)
     if (d->materials[m].kind != TR_MAT_PHONG && d->materials[m].kind != TR_MAT_DISNEY12 &&
-        d->materials[m].kind != TR_MAT_GLASS && d->materials[m].kind != TR_MAT_METAL)
+        d->materials[m].kind != TR_MAT_GLASS && d->materials[m].kind != TR_MAT_METAL &&
+        d->materials[m].kind != TR_MAT_DISNEY15)
       return set_err(ctx, TR_ERR_ARG, "unknown material kind");
   for (uint32_t s = 0; s < d->num_spheres; ++s)
     if (!(d->sphere_radius[s] > 0.0f)) return set_err(ctx, TR_ERR_ARG, "invalid sphere radius");  // sphere.cpp:88-90

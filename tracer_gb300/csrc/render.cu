@@ -64,19 +64,22 @@ __device__ __forceinline__ int path_depth(float w) { return __float_as_int(w) & 
 __device__ __forceinline__ int spec_depth(float w) { return __float_as_int(w) >> 16; }
 
 // light-sample queue of a material kind (glass has none)
-__host__ __device__ constexpr int nee_index(int kind) { return kind == MAT_METAL ? 2 : kind; }
+__host__ __device__ constexpr int nee_index(int kind) {
+  return kind == MAT_METAL ? 2 : (kind == MAT_DISNEY15 ? 3 : kind);
+}
 
 enum : int {  // counter slots
   C_EXT = 0,      // 2: extend queue sizes (double-buffered)
   C_ACT = 2,      // 2: live-slot list sizes
   C_SH = 4,       // shadow queue size
-  C_MAT = 5,      // 4: per-material hit queue sizes (Phong, Disney12, glass, metal)
-  C_NEE = 9,      // 3: light-sample queue sizes (Phong, Disney12, metal; glass has none)
-  C_FEXT = 12,    // extend kernel's work-fetch position
-  C_FSH = 13,     // shadow kernel's work-fetch position
-  C_TB = 14,      // guiding training records written (whole render)
-  C_ERR = 15,     // traversal error word
+  C_MAT = 5,      // 5: per-material hit queue sizes (Phong, Disney12, glass, metal, Disney15)
+  C_NEE = 10,     // 4: light-sample queue sizes (Phong, Disney12, metal, Disney15; glass has none)
+  C_FEXT = 14,    // extend kernel's work-fetch position
+  C_FSH = 15,     // shadow kernel's work-fetch position
+  C_TB = 16,      // guiding training records written (whole render)
+  C_ERR = 17,     // traversal error word
 };
+constexpr int kCtrWords = 32;  // the counter array
 
 struct RenderBuffers {
   int n = 0, nl = 0;
@@ -581,16 +584,19 @@ struct MatOps {
   static __device__ __forceinline__ BsdfSample sample(const Bsdf& b, f3 wo, float u, float v, float w) {
     if (KIND == MAT_GLASS) return b.glass_sample(wo, u);
     if (KIND == MAT_METAL) return b.metal_sample(wo, u, v, w);
+    if (KIND == MAT_DISNEY15) return b.d15_sample(wo, u, v, w);
     return KIND == MAT_PHONG ? b.phong_sample_agg(wo, u, v, w) : b.disney_sample(wo, u, v, w);
   }
   static __device__ __forceinline__ f3 eval(const Bsdf& b, f3 wi, f3 wo) {
     if (KIND == MAT_GLASS) return mk3(0.0f, 0.0f, 0.0f);
     if (KIND == MAT_METAL) return b.metal_eval(wi, wo);
+    if (KIND == MAT_DISNEY15) return b.d15_eval(wi, wo);
     return KIND == MAT_PHONG ? b.phong_eval_agg(wi, wo) : b.disney_eval(wi, wo);
   }
   static __device__ __forceinline__ float pdf(const Bsdf& b, f3 wi, f3 wo) {
     if (KIND == MAT_GLASS) return 0.0f;
     if (KIND == MAT_METAL) return b.metal_pdf(wi, wo);
+    if (KIND == MAT_DISNEY15) return b.d15_pdf(wi, wo);
     return KIND == MAT_PHONG ? b.phong_pdf_agg(wi, wo) : b.disney_pdf(wi, wo);
   }
 };
@@ -1076,7 +1082,7 @@ tr_status reserve_render(tr_ctx* ctx, int n, int nl) {
                {&rb->HC, N * f4},           {&rb->HM, N * f4},          {&rb->SC, N * 7 * f4},
                {&rb->NU, N * NL * 8},       {&rb->SH, N * NL * 3 * f4}, {&rb->acc, N * 32},
                {&rb->q_ext, 2 * 2 * N * 4}, {&rb->q_act, 2 * N * 4},   {&rb->q_mat, kMatKinds * N * 4},
-               {&rb->q_nee, kNeeKinds * N * NL * 4}, {&rb->q_sh, N * NL * 4},  {&rb->ctr, 64},
+               {&rb->q_nee, kNeeKinds * N * NL * 4}, {&rb->q_sh, N * NL * 4},  {&rb->ctr, kCtrWords * 4},
                {&rb->stats, 64}};
   for (auto& nd : needs) {
     cudaError_t e = nd.b->reserve(nd.bytes);
@@ -1301,7 +1307,7 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   } while (0)
   for (int k = 0; k < njobs; ++k)
     RCHK(cudaMemsetAsync(jd[k].film, 0, (size_t)jd[k].W * jd[k].H * (jd[k].fp64 ? 32 : 16), st));
-  RCHK(cudaMemsetAsync(P.ctr, 0, 64, st));
+  RCHK(cudaMemsetAsync(P.ctr, 0, kCtrWords * 4, st));
   RCHK(cudaMemsetAsync(P.stats, 0, 64, st));
   RCHK(cudaEventRecord(e0, st));
   k_init<<<grid_init, 256, 0, st>>>(P);
@@ -1329,7 +1335,7 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     // material and light-sample counts and the fetch positions
     cudaMemsetAsync(P.ctr + C_EXT + nxt, 0, 4, st);
     cudaMemsetAsync(P.ctr + C_ACT + nxt, 0, 4, st);
-    cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 10, st);  // C_SH, C_MAT x4, C_NEE x3, C_FEXT, C_FSH
+    cudaMemsetAsync(P.ctr + C_SH, 0, 4 * (C_FSH + 1 - C_SH), st);  // C_SH, C_MAT, C_NEE, C_FEXT, C_FSH
     mark();
     k_logic<<<grid, 128, 0, st>>>(P, cur);
     if (P.guide_alpha > 0.0f) {
@@ -1345,11 +1351,13 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     k_material<MAT_DISNEY12><<<grid, 128, 0, st>>>(P, cur);
     if (P.sc.has_glass) k_glass<<<grid, 128, 0, st>>>(P, cur);  // timed with Disney12
     if (P.sc.has_metal) k_material<MAT_METAL><<<grid, 128, 0, st>>>(P, cur);
+    if (P.sc.has_disney15) k_material<MAT_DISNEY15><<<grid, 128, 0, st>>>(P, cur);
     mark();
     k_nee<MAT_PHONG><<<grid, 128, 0, st>>>(P);
     mark();
     k_nee<MAT_DISNEY12><<<grid, 128, 0, st>>>(P);
     if (P.sc.has_metal) k_nee<MAT_METAL><<<grid, 128, 0, st>>>(P);  // timed with Disney12
+    if (P.sc.has_disney15) k_nee<MAT_DISNEY15><<<grid, 128, 0, st>>>(P);
     mark();
     if (count && wide) k_shadow<true, true><<<grid_sh, 128, 0, st>>>(P);
     else if (count) k_shadow<true><<<grid_sh, 128, 0, st>>>(P);
@@ -1418,7 +1426,7 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   RCHK(cudaEventSynchronize(e1));
   unsigned long long hs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   RCHK(cudaMemcpy(hs, P.stats, sizeof(hs), cudaMemcpyDeviceToHost));
-  unsigned int ctrs[16];
+  unsigned int ctrs[kCtrWords];
   RCHK(cudaMemcpy(ctrs, P.ctr, sizeof(ctrs), cudaMemcpyDeviceToHost));
   // event k of an iteration's 9 precedes kernel k; stage of each interval
   static const int kStageOf[8] = {TR_STAGE_EXTEND,          TR_STAGE_RESET,     TR_STAGE_LOGIC,
@@ -1552,7 +1560,7 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   const size_t oP = L.take(5 * N * f4), oRng = L.take(N * 8), oM = L.take(3 * N * f4), oH = L.take(2 * N * f4),
                oSC = L.take(N * 7 * f4), oNU = L.take(N * NL * 8), oSH = L.take(N * NL * 3 * f4),
                oQe = L.take(2 * 2 * N * 4), oQa = L.take(2 * N * 4), oQm = L.take(kMatKinds * N * 4),
-               oQn = L.take(kNeeKinds * N * NL * 4), oQs = L.take(N * NL * 4), oCtr = L.take(64), oSt = L.take(64),
+               oQn = L.take(kNeeKinds * N * NL * 4), oQs = L.take(N * NL * 4), oCtr = L.take(kCtrWords * 4), oSt = L.take(64),
                oJob = L.take(sizeof(JobDev));
   if (npix > (1ll << 24) || L.off > kNoAllocScratchBytes) {
     char msg[256];
@@ -1640,7 +1648,7 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   // the counters, statistics and film start at zero on every call; the
   // rest of the scratch is written before it is read
   NCHK(cudaMemsetAsync(d_rgbw, 0, (size_t)n * 16, st));
-  NCHK(cudaMemsetAsync(P.ctr, 0, 64, st));
+  NCHK(cudaMemsetAsync(P.ctr, 0, kCtrWords * 4, st));
   NCHK(cudaMemsetAsync(P.stats, 0, 64, st));
   k_init<<<grid_init, 256, 0, st>>>(P);
   NCHK(cudaGetLastError());
@@ -1654,22 +1662,24 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
     k_extend<false><<<grid_ext, 128, 0, st>>>(P, cur);
     NCHK(cudaMemsetAsync(P.ctr + C_EXT + nxt, 0, 4, st));
     NCHK(cudaMemsetAsync(P.ctr + C_ACT + nxt, 0, 4, st));
-    NCHK(cudaMemsetAsync(P.ctr + C_SH, 0, 4 * 10, st));  // C_SH, C_MAT x4, C_NEE x3, C_FEXT, C_FSH
+    NCHK(cudaMemsetAsync(P.ctr + C_SH, 0, 4 * (C_FSH + 1 - C_SH), st));  // C_SH, C_MAT, C_NEE, C_FEXT, C_FSH
     k_logic<<<grid, 128, 0, st>>>(P, cur);
     k_material<MAT_PHONG><<<grid, 128, 0, st>>>(P, cur);
     k_material<MAT_DISNEY12><<<grid, 128, 0, st>>>(P, cur);
     if (P.sc.has_glass) k_glass<<<grid, 128, 0, st>>>(P, cur);
     if (P.sc.has_metal) k_material<MAT_METAL><<<grid, 128, 0, st>>>(P, cur);
+    if (P.sc.has_disney15) k_material<MAT_DISNEY15><<<grid, 128, 0, st>>>(P, cur);
     k_nee<MAT_PHONG><<<grid, 128, 0, st>>>(P);
     k_nee<MAT_DISNEY12><<<grid, 128, 0, st>>>(P);
     if (P.sc.has_metal) k_nee<MAT_METAL><<<grid, 128, 0, st>>>(P);
+    if (P.sc.has_disney15) k_nee<MAT_DISNEY15><<<grid, 128, 0, st>>>(P);
     if (wide) k_shadow<false, true><<<grid_sh, 128, 0, st>>>(P);
     else k_shadow<false><<<grid_sh, 128, 0, st>>>(P);
   }
   NCHK(cudaGetLastError());
   NCHK(cudaStreamSynchronize(st));
   unsigned long long hs[8];
-  unsigned int ctrs[16];
+  unsigned int ctrs[kCtrWords];
   NCHK(cudaMemcpy(hs, P.stats, sizeof(hs), cudaMemcpyDeviceToHost));
   NCHK(cudaMemcpy(ctrs, P.ctr, sizeof(ctrs), cudaMemcpyDeviceToHost));
 #undef NCHK

@@ -78,9 +78,10 @@ struct DTriShade {
   int pad[3];
 };
 
-enum { MAT_PHONG = 0, MAT_DISNEY12 = 1, MAT_GLASS = 2, MAT_METAL = 3 };
-constexpr int kMatKinds = 4;
-constexpr int kNeeKinds = 3;  // kinds with light sampling: Phong, Disney12, metal (glass is a delta BSDF)
+enum { MAT_PHONG = 0, MAT_DISNEY12 = 1, MAT_GLASS = 2, MAT_METAL = 3, MAT_DISNEY15 = 4 };
+constexpr int kMatKinds = 5;
+// kinds with light sampling: Phong, Disney12, metal, Disney15 (glass is a delta BSDF)
+constexpr int kNeeKinds = 4;
 
 // Phong: the AggregateBSDF<2> that Phong::shading builds (src/material/phong.cpp:29-70)
 // Disney12: the eleven parameters (src/material/disney_brdf.cpp:278-302)
@@ -103,6 +104,12 @@ struct DMat {
   // Metal (src/material/metal.cpp:33-56): painted conductor Fresnel constants
   // (squared ratios and paint, per channel); ax, ay above hold its GGX alphas
   f3 f_eta2, f_etak2, f_paint;
+  // Disney15 (src/material/disney.cpp:341-392): tint colour, specular scale,
+  // transmission, the transmission alphas, clearcoat roughness and the lobe
+  // weights; base, metallic, roughness, specular_tint, sheen, sheen_tint and
+  // clearcoat above, ax, ay its specular alphas, ior its IOR (at least 1.01)
+  f3 c_tint, spec_scale;
+  float transmission, trans_ax, trans_ay, cc_rough, w_diff15, w_trans, w_spec15, w_cc;
 };
 
 // A diffuse area light on a triangle (src/light/diffuse_light.cpp:44-60)
@@ -159,6 +166,7 @@ struct DScene {
   int max_lights;  // most lights of one scene
   int has_glass;   // some material is a delta BSDF (glass)
   int has_metal;   // some material is metal
+  int has_disney15;  // some material is the 2015 Disney BSDF
   const DEnv* envs;  // environment lights of the set (DLight::env indexes them)
   int has_env;       // some scene has an environment light
 };

@@ -661,8 +661,8 @@ struct Bsdf {
     if (pdf) *pdf = Go * D / (4.0f * cos_theta_o);
   }
   // microfacet::sample_anisotropic_gtr2_with_visible_normal (src/material/utility/microfacet.cpp:58-80)
-  __device__ f3 sample_vndf(f3 ve, float u, float v) const {
-    const float ax = m->ax, ay = m->ay;
+  __device__ f3 sample_vndf(f3 ve, float u, float v) const { return sample_vndf_a(ve, u, v, m->ax, m->ay); }
+  static __device__ f3 sample_vndf_a(f3 ve, float u, float v, float ax, float ay) {
     const f3 vh = normalize(mk3(ax * ve.x, ay * ve.y, ve.z));
     const float lensq = vh.x * vh.x + vh.y * vh.y;
     const f3 t1 = lensq > kEps ? divd(mk3(-vh.y, vh.x, 0.0f), (double)sqrtf(lensq)) : mk3(1.0f, 0.0f, 0.0f);
@@ -724,19 +724,191 @@ struct Bsdf {
     return out;
   }
 
+  // ---- DisneyBSDF, the 2015 model (src/material/disney.cpp:14-537), radiance transport
+  static __device__ __forceinline__ float d15_D(f3 lwh, float ax, float ay) {
+    float sp, cp;
+    sincosf(local_phi(lwh), &sp, &cp);
+    return anisotropic_gtr2(sp, cp, local_cos_to_sin(lwh.z), lwh.z, ax, ay);
+  }
+  static __device__ __forceinline__ float d15_G1(f3 lw, float ax, float ay) {
+    float sp, cp;
+    sincosf(local_phi(lw), &sp, &cp);
+    return smith_aniso_gtr2(cp, sp, ax, ay, local_tan_theta(lw));
+  }
+  __device__ f3 d15_f_transmission(f3 lwi, f3 lwo) const {
+    const float eta = lwo.z > 0.0f ? m->ior : 1.0f / m->ior;
+    f3 lwh = normalize(lwo + scale(lwi, eta));
+    if (lwh.z < 0.0f) lwh = -lwh;
+    const float cd = dot(lwo, lwh);
+    const float F = dielectric_fresnel(m->ior, 1.0f, cd);
+    const float D = d15_D(lwh, m->trans_ax, m->trans_ay);
+    const float G = d15_G1(lwi, m->trans_ax, m->trans_ay) * d15_G1(lwo, m->trans_ax, m->trans_ay);
+    const float sdem = cd + eta * dot(lwi, lwh);
+    const float corr = 1.0f / eta;
+    const float val = (1.0f - F) * D * G * eta * eta * dot(lwi, lwh) * dot(lwo, lwh) * corr * corr /
+                      (lwi.z * lwo.z * sdem * sdem);
+    const float k = (1.0f - m->metallic) * (lwo.z > 0.0f ? m->transmission : 1.0f);
+    const float av = fabsf(val);
+    return mk3(k * sqrtf(m->base.x) * av, k * sqrtf(m->base.y) * av, k * sqrtf(m->base.z) * av);
+  }
+  __device__ f3 d15_f_inner_reflection(f3 lwi, f3 lwo) const {
+    const f3 lwh = -normalize(lwi + lwo);
+    const float F = dielectric_fresnel(m->ior, 1.0f, dot(lwo, lwh));
+    const float D = d15_D(lwh, m->trans_ax, m->trans_ay);
+    const float G = d15_G1(lwi, m->trans_ax, m->trans_ay) * d15_G1(lwo, m->trans_ax, m->trans_ay);
+    return muls(muls(m->base, m->transmission), fabsf(F * D * G / (4.0f * lwi.z * lwo.z)));
+  }
+  __device__ f3 d15_f_specular(f3 lwi, f3 lwo) const {
+    const f3 lwh = normalize(lwi + lwo);
+    const float cd = dot(lwi, lwh);
+    const f3 one = mk3(1.0f, 1.0f, 1.0f);
+    const f3 Cspec = mix3(mix3(one, m->c_tint, m->specular_tint), m->base, m->metallic);
+    const f3 diel = muls(Cspec, dielectric_fresnel(m->ior, 1.0f, cd));
+    const f3 cond = Cspec + muls(one - Cspec, one_minus_5(cd));
+    const f3 F = mix3(mulc(m->spec_scale, diel), cond, m->metallic);
+    const float D = d15_D(lwh, m->ax, m->ay);
+    const float G = d15_G1(lwi, m->ax, m->ay) * d15_G1(lwo, m->ax, m->ay);
+    return divs(muls(muls(F, D), G), fabsf(4.0f * lwi.z * lwo.z));
+  }
+  __device__ float d15_pdf_transmission(f3 lwi, f3 lwo) const {
+    const float eta = lwo.z > 0.0f ? m->ior : 1.0f / m->ior;
+    f3 lwh = normalize(lwo + scale(lwi, eta));
+    if (lwh.z < 0.0f) lwh = -lwh;
+    if (((lwo.z > 0.0f) != (dot(lwh, lwo) > 0.0f)) || ((lwi.z > 0.0f) != (dot(lwh, lwi) > 0.0f))) return 0.0f;
+    const float sdem = dot(lwo, lwh) + eta * dot(lwi, lwh);
+    const float dwh_to_dwi = eta * eta * dot(lwi, lwh) / (sdem * sdem);
+    const float D = d15_D(lwh, m->trans_ax, m->trans_ay);
+    return fabsf(dot(lwi, lwh) * D * dwh_to_dwi);
+  }
+  __device__ float d15_pdf_inner_reflection(f3 lwi, f3 lwo) const {
+    const f3 lwh = -normalize(lwi + lwo);
+    const float D = d15_D(lwh, m->trans_ax, m->trans_ay);
+    return fabsf(lwh.z * D / (4.0f * dot(lwi, lwh)));
+  }
+  __device__ f3 d15_eval(f3 wi, f3 wo) const {
+    if (fringe(wi) | fringe(wo)) return eval_fringe(wi, wo);
+    const f3 lwi = normalize(to_local(s, wi)), lwo = normalize(to_local(s, wo));
+    if (fabsf(lwi.z) < kEps || fabsf(lwo.z) < kEps) return mk3(0.0f, 0.0f, 0.0f);
+    if (lwi.z * lwo.z < 0.0f) {
+      if (m->transmission == 0.0f) return mk3(0.0f, 0.0f, 0.0f);
+      return muls(d15_f_transmission(lwi, lwo), normal_correct(g, s, wi));
+    }
+    if (lwi.z < 0.0f && lwo.z < 0.0f) {
+      if (m->transmission == 0.0f) return mk3(0.0f, 0.0f, 0.0f);
+      return muls(d15_f_inner_reflection(lwi, lwo), normal_correct(g, s, wi));
+    }
+    const f3 lwh = normalize(lwi + lwo);
+    const float cd = dot(lwi, lwh);
+    f3 diffuse = mk3(0.0f, 0.0f, 0.0f), sheen = diffuse, clearcoat = diffuse;
+    if (m->metallic < 1.0f) {
+      // f_diffuse: Lambert with the retro-reflection term
+      const float FL = one_minus_5(lwi.z), FV = one_minus_5(lwo.z);
+      const float RR = 2.0f * m->roughness * cd * cd;
+      const f3 lam = divs(m->base, kPi);
+      const f3 retro = muls(muls(divs(m->base, kPi), RR), FL + FV + FL * FV * (RR - 1.0f));
+      diffuse = muls(muls(lam, 1.0f - 0.5f * FL), 1.0f - 0.5f * FV) + retro;
+      if (m->sheen > 0.0f)
+        sheen = muls(muls(mix3(mk3(1.0f, 1.0f, 1.0f), m->c_tint, m->sheen_tint), 4.0f * m->sheen), one_minus_5(cd));
+    }
+    const f3 specular = d15_f_specular(lwi, lwo);
+    if (m->clearcoat > 0.0f) {
+      const float ch = lwh.z, sh = local_cos_to_sin(ch);
+      const float D = gtr1(sh, ch, m->cc_rough);
+      const float F = 0.04f + (1.0f - 0.04f) * one_minus_5(cd);
+      const float G = smith_gtr2(local_tan_theta(lwi), 0.25f) * smith_gtr2(local_tan_theta(lwo), 0.25f);
+      const float c = m->clearcoat * D * F * G / fabsf(4.0f * lwi.z * lwo.z);
+      clearcoat = mk3(c, c, c);
+    }
+    const f3 ret = muls(diffuse + sheen, (1.0f - m->metallic) * (1.0f - m->transmission)) + specular + clearcoat;
+    return muls(ret, normal_correct(g, s, wi));
+  }
+  __device__ float d15_pdf(f3 wi, f3 wo) const {
+    if (fringe(wi) | fringe(wo)) return pdf_fringe(wi, wo);
+    const f3 lwi = normalize(to_local(s, wi)), lwo = normalize(to_local(s, wo));
+    if (fabsf(lwi.z) < kEps || fabsf(lwo.z) < kEps) return 0.0f;
+    if (lwo.z < 0.0f) {
+      if (m->transmission == 0.0f) return 0.0f;
+      float F = dielectric_fresnel(m->ior, 1.0f, lwo.z);
+      F = F < 0.1f ? 0.1f : (0.9f < F ? 0.9f : F);
+      if (lwi.z > 0.0f) return (1.0f - F) * d15_pdf_transmission(lwi, lwo);
+      return F * d15_pdf_inner_reflection(lwi, lwo);
+    }
+    if (lwi.z < 0.0f) return m->w_trans * d15_pdf_transmission(lwi, lwo);
+    // pdf_specular_clearcoat (disney.cpp:250-281): sin(phi_o) from cos(phi_o)
+    const f3 lwh = normalize(lwi + lwo);
+    const float ch = lwh.z, sh = local_cos_to_sin(ch);
+    const float cd = dot(lwi, lwh);
+    const float cos_phi_o = cosf(local_phi(lwo));
+    const float sin_phi_o = local_cos_to_sin(cos_phi_o);
+    const float ps = smith_aniso_gtr2(cos_phi_o, sin_phi_o, m->ax, m->ay, local_tan_theta(lwo)) *
+                     d15_D(lwh, m->ax, m->ay) / (4.0f * lwo.z);
+    const float pc = ch * gtr1(sh, ch, m->cc_rough) / (4.0f * cd);
+    return m->w_diff15 * cosine_pdf(lwi.z) + m->w_spec15 * ps + m->w_cc * pc;
+  }
+  __device__ BsdfSample d15_sample(f3 wo, float u, float v, float w) const {
+    if (fringe(wo)) return sample_fringe(wo, u, v);
+    BsdfSample out;
+    out.pdf = 0.0f;
+    out.f = mk3(0.0f, 0.0f, 0.0f);
+    out.wi = out.f;
+    const f3 lwo = normalize(to_local(s, wo));
+    if (fabsf(lwo.z) < kEps) return out;
+    if (lwo.z < 0.0f && m->transmission == 0.0f) return out;
+    // the lobe choice (disney.cpp:471-488): the second test is not inside the
+    // first one's else, so a diffuse draw is always replaced by one of the
+    // other three lobes (the cosine sample has no side effects and is skipped)
+    float sel = u;
+    if (!(sel < m->w_diff15)) sel -= m->w_diff15;
+    f3 lwi = mk3(0.0f, 0.0f, 0.0f);
+    if (sel < m->w_trans) {
+      const f3 lwh = sample_aniso_gtr2(m->trans_ax, m->trans_ay, v, w);
+      if (lwh.z > 0.0f && (lwo.z > 0.0f) == (dot(lwh, lwo) > 0.0f)) {
+        // refract_dir (src/utility/reflection.hpp:43-51) about the facet normal
+        const float eta = lwo.z > 0.0f ? 1.0f / m->ior : m->ior;
+        const f3 owh = dot(lwh, lwo) > 0.0f ? lwh : -lwh;
+        const float ci = fabsf(lwo.z);
+        const float st2 = eta * eta * fmaxf(0.0f, 1.0f - ci * ci);
+        if (st2 < 1.0f) {
+          const f3 t = normalize(scale(owh, eta * ci - sqrtf(1.0f - st2)) - scale(lwo, eta));
+          if (!(t.z * lwo.z > 0.0f || ((t.z > 0.0f) != (dot(lwh, t) > 0.0f)))) lwi = t;
+        }
+      }
+    } else if (sel -= m->w_trans, sel < m->w_spec15) {
+      const f3 lwh = normalize(sample_vndf_a(lwo, v, w, m->ax, m->ay));
+      if (lwh.z > 0.0f) {
+        const f3 t = normalize(scale(lwh, 2.0f * dot(lwo, lwh)) - lwo);
+        if (t.z > 0.0f) lwi = t;
+      }
+    } else {
+      const f3 lwh = sample_gtr1(m->cc_rough, v, w);
+      if (lwh.z > 0.0f) {
+        const f3 t = normalize(scale(lwh, 2.0f * dot(lwo, lwh)) - lwo);
+        if (t.z > 0.0f) lwi = t;
+      }
+    }
+    if (lwi.x == 0.0f && lwi.y == 0.0f && lwi.z == 0.0f) return out;
+    out.wi = to_global(s, lwi);
+    out.f = d15_eval(out.wi, wo);
+    out.pdf = d15_pdf(out.wi, wo);
+    return out;
+  }
+
   __device__ __forceinline__ f3 eval(f3 wi, f3 wo) const {
     if (m->kind == MAT_GLASS) return mk3(0.0f, 0.0f, 0.0f);
     if (m->kind == MAT_METAL) return metal_eval(wi, wo);
+    if (m->kind == MAT_DISNEY15) return d15_eval(wi, wo);
     return m->kind == MAT_PHONG ? phong_eval_agg(wi, wo) : disney_eval(wi, wo);
   }
   __device__ __forceinline__ float pdf(f3 wi, f3 wo) const {
     if (m->kind == MAT_GLASS) return 0.0f;
     if (m->kind == MAT_METAL) return metal_pdf(wi, wo);
+    if (m->kind == MAT_DISNEY15) return d15_pdf(wi, wo);
     return m->kind == MAT_PHONG ? phong_pdf_agg(wi, wo) : disney_pdf(wi, wo);
   }
   __device__ __forceinline__ BsdfSample sample(f3 wo, float u, float v, float w) const {
     if (m->kind == MAT_GLASS) return glass_sample(wo, u);
     if (m->kind == MAT_METAL) return metal_sample(wo, u, v, w);
+    if (m->kind == MAT_DISNEY15) return d15_sample(wo, u, v, w);
     return m->kind == MAT_PHONG ? phong_sample_agg(wo, u, v, w) : disney_sample(wo, u, v, w);
   }
 };

@@ -23,7 +23,7 @@ import math
 
 import numpy as np
 
-from .abi import (RAY_DTYPE, TR_MAT_DISNEY12, TR_MAT_GLASS, TR_MAT_METAL, TR_MAT_PHONG, Material, SceneBuffers, make_camera,
+from .abi import (RAY_DTYPE, TR_MAT_DISNEY12, TR_MAT_DISNEY15, TR_MAT_GLASS, TR_MAT_METAL, TR_MAT_PHONG, Material, SceneBuffers, make_camera,
                   make_filter, make_params)
 
 F32_MAX = np.float32(np.finfo(np.float32).max)
@@ -314,6 +314,35 @@ def outdoor(width=96, height=64, spp=8, max_depth=6, min_depth=3, env_size=(64, 
     scene.env_texels = sky_map(*env_size)
     scene.env_to_light, scene.env_to_world = rotate_x(math.pi / 2)
     cam = make_camera(width / height, (0, 1.6, 6.5), (0, 0.9, 0), (0, 1, 0), math.radians(50.0), 0.0, 1.0)
+    return scene, cam, make_filter(0.5, 0.6), make_params(width, height, spp, min_depth, max_depth)
+
+
+def disney15_row(width=96, height=48, spp=8, max_depth=6, min_depth=3, env=True):
+    """Five spheres of the 2015 Disney BSDF (create_disney) on a ground quad
+    under a small area light and (by default) the sky map: a rough
+    dielectric, a metal, a clearcoated sheen layer, a rough transmitter and a
+    smooth anisotropic transmitter."""
+    b = _Builder()
+    ground = b.material(lambert((0.45, 0.42, 0.4)))
+    b.quad((-6, 0, -6), (6, 0, -6), (6, 0, 6), (-6, 0, 6), (0, 1, 0), ground)
+    b.quad((-0.5, 3, -0.5), (0.5, 3, -0.5), (0.5, 3, 0.5), (-0.5, 3, 0.5), (0, -1, 0), ground,
+           emission=(8.0, 8.0, 8.0))
+    params = [dict(base_color=(0.8, 0.3, 0.2), roughness=0.5, specular_scale=(1.0, 1.0, 1.0), ior=1.5),
+              dict(base_color=(0.9, 0.7, 0.4), metallic=0.9, roughness=0.3, anisotropic=0.5, ior=1.5),
+              dict(base_color=(0.2, 0.4, 0.8), roughness=0.6, sheen=0.8, sheen_tint=0.5, clearcoat=0.7,
+                   clearcoat_gloss=0.6, specular_tint=0.3, specular_scale=(0.5, 0.5, 0.5), ior=1.4),
+              dict(base_color=(0.9, 0.9, 0.9), roughness=0.2, transmission=0.8, transmission_roughness=0.3,
+                   specular_scale=(1.0, 1.0, 1.0), ior=1.5),
+              dict(base_color=(0.7, 0.9, 0.7), roughness=0.1, transmission=0.5, transmission_roughness=0.05,
+                   anisotropic=0.6, metallic=0.1, ior=1.33)]
+    for k, p in enumerate(params):
+        m = b.material(Material(kind=TR_MAT_DISNEY15, **p))
+        b.sphere((-3.0 + 1.5 * k, 0.6, 0.0), 0.6, m)
+    scene = b.finish(max_leaf_prims=3)
+    if env:
+        scene.env_texels = sky_map(64, 32)
+        scene.env_to_light, scene.env_to_world = rotate_x(math.pi / 2)
+    cam = make_camera(width / height, (0, 1.8, 7.0), (0, 0.7, 0), (0, 1, 0), math.radians(50.0), 0.0, 1.0)
     return scene, cam, make_filter(0.5, 0.6), make_params(width, height, spp, min_depth, max_depth)
 
 
