@@ -173,6 +173,15 @@ RC<Material> create_disney_brdf(RC<const Texture2D> base_color, RC<const Texture
                                 RC<const Texture2D> clearcoat_gloss);
 // create_glass (src/factory/material.hpp:13-17, src/material/glass.cpp:145-154)
 RC<Material> create_glass(RC<const Texture2D> map_kr, RC<const Texture2D> map_kt, RC<const Texture2D> map_ior);
+// create_disney, the 2015 Disney BSDF (src/factory/material.hpp:37-53,
+// src/material/disney.cpp:541-677), with no normal mapper and no BSSRDF
+RC<Material> create_disney(RC<const Texture2D> base_color, RC<const Texture2D> metallic,
+                           RC<const Texture2D> roughness, RC<const Texture2D> transmission,
+                           RC<const Texture2D> transmission_roughness, RC<const Texture2D> ior,
+                           RC<const Texture2D> specular_scale, RC<const Texture2D> specular_tint,
+                           RC<const Texture2D> anisotropic, RC<const Texture2D> sheen,
+                           RC<const Texture2D> sheen_tint, RC<const Texture2D> clearcoat,
+                           RC<const Texture2D> clearcoat_gloss);
 // create_metal (src/factory/material.hpp:90-96, src/material/metal.cpp:68-76) with
 // no normal mapper; the painted conductor Fresnel is built as the reference
 // builds it from (color, eta, k)

@@ -86,6 +86,7 @@ int main(int argc, char** argv) {
   // the short box in metal and the tall one in glass; an environment light
   const bool glass_metal = argc > 6 && std::strstr(argv[6], "glass_metal") != nullptr;
   const bool sky = argc > 6 && std::strstr(argv[6], "sky") != nullptr;
+  const bool d15 = argc > 6 && std::strstr(argv[6], "disney15") != nullptr;
 
   // construction errors throw (src/shape/sphere.cpp:88-90)
   if (!throws([] { create_sphere(-1.0f, Transform()); }) ||
@@ -103,6 +104,13 @@ int main(int argc, char** argv) {
   auto metal = create_metal(konst(0.95f, 0.64f, 0.54f), konst(0.2f, 0.92f, 1.1f), konst(3.9f, 2.45f, 2.14f),
                             konst(0.35f, 0.35f, 0.35f), konst(0.4f, 0.4f, 0.4f));
   auto glass = create_glass(konst(1, 1, 1), konst(1, 1, 1), konst(1.5f, 1.5f, 1.5f));
+  // 2015 Disney: a rough transmitter and an anisotropic, clearcoated metal
+  auto d15_trans = create_disney(konst(0.9f, 0.9f, 0.9f), konst(0, 0, 0), konst(0.2f, 0.2f, 0.2f),
+                                 konst(0.8f, 0.8f, 0.8f), konst(0.3f, 0.3f, 0.3f), konst(1.5f, 1.5f, 1.5f),
+                                 konst(1, 1, 1), zero, zero, zero, zero, zero, zero);
+  auto d15_metal = create_disney(konst(0.9f, 0.7f, 0.4f), konst(0.9f, 0.9f, 0.9f), konst(0.3f, 0.3f, 0.3f), zero,
+                                 zero, konst(1.5f, 1.5f, 1.5f), zero, konst(0.2f, 0.2f, 0.2f), konst(0.5f, 0.5f, 0.5f),
+                                 zero, zero, konst(0.6f, 0.6f, 0.6f), konst(0.5f, 0.5f, 0.5f));
   auto vacuum = create_vacuum();
   const MediumInterface mi(vacuum);
 
@@ -123,9 +131,9 @@ int main(int argc, char** argv) {
   add(quad_mesh({1, -1, -1}, {1, -1, 1}, {1, 1, 1}, {1, 1, -1}, {-1, 0, 0}), id, green, black);       // right
   const float pi = 3.14159265358979f;
   add(cube_mesh(), translate({-0.35f, -0.7f, -0.3f}) * rotate_y(15.0f * pi / 180.0f) * scale(0.6f, 0.6f, 0.6f),
-      glass_metal ? metal : white, black);
+      glass_metal ? metal : (d15 ? d15_metal : white), black);
   add(cube_mesh(), translate({0.35f, -0.4f, 0.3f}) * rotate_y(-18.0f * pi / 180.0f) * scale(0.6f, 1.2f, 0.6f),
-      glass_metal ? glass : white, black);
+      glass_metal ? glass : (d15 ? d15_trans : white), black);
   add(quad_mesh({-0.25f, 0.99f, -0.25f}, {0.25f, 0.99f, -0.25f}, {0.25f, 0.99f, 0.25f}, {-0.25f, 0.99f, 0.25f},
                 {0, -1, 0}),
       id, white, Spectrum(17, 12, 4));

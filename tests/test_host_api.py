@@ -122,6 +122,26 @@ def test_factory_glass_and_metal_materials(program, tmp_path):
     assert sb.prim_material[22] == kinds.index(TR_MAT_GLASS)
 
 
+def test_factory_disney15(program, tmp_path):
+    """create_disney records the 2015 Disney parameters; the oracle and the
+    reference build render the factory scene alike."""
+    from tracer_gb300.abi import TR_MAT_DISNEY15
+    out = str(tmp_path / "c")
+    subprocess.run([program, out, "16", "16", "1", "describe", "disney15"], check=True, capture_output=True, text=True)
+    sb, cam = _read_desc(out + ".desc")
+    recs = [m.rec for m in sb.materials if m.rec.kind == TR_MAT_DISNEY15]
+    assert len(recs) == 2
+    trans = [r for r in recs if r.transmission > 0][0]
+    assert abs(trans.transmission - 0.8) < 1e-7 and abs(trans.transmission_roughness - 0.3) < 1e-7
+    assert abs(trans.ior - 1.5) < 1e-7 and np.allclose(list(trans.specular_scale), [1, 1, 1])
+    if oracle.ref_available():
+        par = make_params(16, 16, 2, 5, 5)
+        port, ref = oracle.Oracle(sb, "port"), oracle.Oracle(sb, "reference")
+        for o in (port, ref):
+            o.set_camera(cam, make_filter(0.5, 0.6))
+        assert np.array_equal(port.render(par).view(np.uint32), ref.render(par).view(np.uint32))
+
+
 def test_factory_environment_light(program, tmp_path):
     """create_ibl_light over create_hdr_texture2d, set as the scene's
     environment light and appended to its lights: the description carries the
@@ -147,7 +167,7 @@ def test_factory_environment_light(program, tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("variant", ["", "glass_metal", "sky"])
+@pytest.mark.parametrize("variant", ["", "glass_metal", "sky", "disney15"])
 def test_factory_scene_renders_like_the_oracle(program, tmp_path, variant):
     W, H, S = 48, 40, 4
     out = str(tmp_path / "c")

@@ -491,6 +491,33 @@ RC<Material> create_glass(RC<const Texture2D> map_kr, RC<const Texture2D> map_kt
   return std::make_shared<Material>(m);
 }
 
+RC<Material> create_disney(RC<const Texture2D> base_color, RC<const Texture2D> metallic,
+                           RC<const Texture2D> roughness, RC<const Texture2D> transmission,
+                           RC<const Texture2D> transmission_roughness, RC<const Texture2D> ior,
+                           RC<const Texture2D> specular_scale, RC<const Texture2D> specular_tint,
+                           RC<const Texture2D> anisotropic, RC<const Texture2D> sheen,
+                           RC<const Texture2D> sheen_tint, RC<const Texture2D> clearcoat,
+                           RC<const Texture2D> clearcoat_gloss) {
+  tr_material m{};
+  m.kind = TR_MAT_DISNEY15;
+  const Spectrum bc = tex(base_color, "base_color"), ss = tex(specular_scale, "specular_scale");
+  const float b3[3] = {bc.r, bc.g, bc.b}, s3[3] = {ss.r, ss.g, ss.b};
+  std::memcpy(m.base_color, b3, sizeof(b3));
+  std::memcpy(m.specular_scale, s3, sizeof(s3));
+  m.metallic = tex_s(metallic, "metallic");
+  m.roughness = tex_s(roughness, "roughness");
+  m.transmission = tex_s(transmission, "transmission");
+  m.transmission_roughness = tex_s(transmission_roughness, "transmission_roughness");
+  m.ior = tex_s(ior, "ior");
+  m.specular_tint = tex_s(specular_tint, "specular_tint");
+  m.anisotropic = tex_s(anisotropic, "anisotropic");
+  m.sheen = tex_s(sheen, "sheen");
+  m.sheen_tint = tex_s(sheen_tint, "sheen_tint");
+  m.clearcoat = tex_s(clearcoat, "clearcoat");
+  m.clearcoat_gloss = tex_s(clearcoat_gloss, "clearcoat_gloss");
+  return std::make_shared<Material>(m);
+}
+
 RC<Material> create_metal(RC<const Texture2D> color, RC<const Texture2D> eta, RC<const Texture2D> k,
                           RC<const Texture2D> roughness, RC<const Texture2D> anisotropic) {
   tr_material m{};
