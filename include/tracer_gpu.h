@@ -331,7 +331,7 @@ tr_status tr_render_dev(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filt
  * event allocation. For callers that render previews inside a frame loop and
  * cannot take cudaFree's implicit device synchronisation, or that share the
  * GPU with a caching allocator holding the rest of its memory.
- *  - Limit: width * height * (316 + 72 * lights) bytes (plus alignment) must
+ *  - Limit: width * height * (324 + 76 * lights) bytes (plus alignment) must
  *    fit in 16 MiB, e.g. 128x128 with 8 lights; larger films return
  *    TR_ERR_ARG with the size needed.
  *  - The first call on a device looks up the array's address

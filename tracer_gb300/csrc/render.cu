@@ -1566,7 +1566,7 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
     char msg[256];
     std::snprintf(msg, sizeof(msg),
                   "film %dx%d with %d lights needs %zu bytes of scratch; tr_render_dev_noalloc has %zu "
-                  "(about 316 + 72 * lights bytes per pixel)",
+                  "(about 324 + 76 * lights bytes per pixel)",
                   prm->width, prm->height, nl, (size_t)L.off, kNoAllocScratchBytes);
     return set_err(ctx, TR_ERR_ARG, msg);
   }
