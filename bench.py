@@ -805,7 +805,7 @@ def run_ours(args):
         "config": {"workload": label, "width": W, "height": H, "spp": par.spp, "max_depth": par.max_depth,
                    "min_depth": par.min_depth, "lights": nl, "primitives": int(len(sc.prim_shape)),
                    "parallelism": f"replicas x{world}",
-                   "l2": f"path state and queues ({W * H * (312 + 68 * max(nl, 1)) / 1e6:.0f} MB) exceed L2; "
+                   "l2": f"path state and queues ({W * H * (324 + 76 * max(nl, 1)) / 1e6:.0f} MB) exceed L2; "
                          "a 256 MiB buffer is written between timed steps"},
         "value_is": "camera samples per second of the plain GPU path tracer (time-to-1% relMSE under "
                     "'convergence')",
