@@ -307,6 +307,37 @@ struct RenderTarget {
   Image2D<Spectrum> color;
 };
 
+// ---- image files (src/utility/image_file.hpp:12-45), read and written by
+// project code in place of the reference's stb dependency ----
+
+struct Color3b {
+  uint8_t x = 0, y = 0, z = 0;
+};
+// Radiance HDR: the header, "-Y height +X width", RGBE scanlines (row 0 first).
+void write_image_to_hdr(const Image2D<Spectrum>& image, const std::string& filename);
+// 8-bit RGB PNG (row 0 first).
+void write_image_to_png(const Image2D<Color3b>& image, const std::string& filename);
+// A Radiance HDR file (flat or run-length scanlines, "-Y height +X width"),
+// row 0 = the first scanline, RGBE decoded as byte * 2^(exponent - 136).
+RC<Image2D<Color3f>> load_hdr_from_file(const std::string& filename);
+// create_texture2d_from_file (src/utility/image_file.cpp:168-178): ".hdr"
+// files become HDR textures. The 8-bit formats (.png, .jpg, .jpeg) have no
+// reader here and throw TracerError(TR_ERR_UNSUPPORTED); other extensions
+// throw TR_ERR_ARG, as the reference throws for them.
+RC<const Texture2D> create_texture2d_from_file(const std::string& filename);
+// The textures of an MTL material (src/utility/image_file.hpp:23-45).
+struct MaterialTexture {
+  RC<Texture2D> map_ka, map_kd, map_ks, map_kt, ior, map_ns, map_bump, disp, map_d, refl;
+  RC<Texture2D> map_pr, map_pm, map_ps, map_ke, norm;
+  bool has_emission = false;
+  bool as_glass = false;
+};
+// create_texture_from_file (src/utility/image_file.cpp:136-166): a constant
+// texture of the MTL value where no map is named, else the map file scaled
+// by the value (1 where the value is black); emission flags has_emission; an
+// ior above 1 makes the material glass with kt = ks (1 where ks is black).
+MaterialTexture create_texture_from_file(const material_t& material);
+
 class Film {
  public:
   Film(const Point2i& res, const RC<Filter>& filter) : resolution(res), filter(filter) {}

@@ -148,6 +148,9 @@ class ConstantTexture : public Texture2D {
 
 Spectrum tex(const RC<const Texture2D>& t, const char* what) {
   if (!t) throw std::invalid_argument(std::string("null texture: ") + what);
+  // the device materials take one value per parameter
+  if (!dynamic_cast<const ConstantTexture*>(t.get()))
+    throw TracerError(TR_ERR_UNSUPPORTED, std::string("image textures on materials are outside the GPU path: ") + what);
   return t->evaluate(Point2f{});
 }
 
