@@ -1,5 +1,6 @@
-"""Batched rendering of a scene set: every job's film equals the film of the
-same render done alone, and CUDA-graph replay changes nothing."""
+"""Batched rendering of a scene set (with an environment light, glass, metal
+and Disney 2015 scenes among area-lit ones): every job's film equals the
+film of the same render done alone, and CUDA-graph replay changes nothing."""
 import numpy as np
 import pytest
 
@@ -14,7 +15,9 @@ def _set():
          scenes.make_params(24, 20, 8, 1, 7, seed_base=39))
     c = scenes.disney_grid(32, 24, 2)
     d = scenes.occluded_room(48, 36, 4, n_tris=5000)
-    return [a, b, c, d]
+    e = scenes.outdoor(32, 24, 4)  # environment light, glass and metal
+    f = scenes.disney15_row(32, 16, 2, env=False)
+    return [a, b, c, d, e, f]
 
 
 def test_batch_equals_single_renders(gpu):
@@ -30,12 +33,12 @@ def test_batch_equals_single_renders(gpu):
     torch.cuda.synchronize()
     # scenes in another order than the set, one scene twice
     extra = torch.zeros_like(films[0])
-    jobs = [(k, items[k][1], items[k][2], items[k][3], films[k].data_ptr()) for k in (2, 0, 3, 1)]
+    jobs = [(k, items[k][1], items[k][2], items[k][3], films[k].data_ptr()) for k in (2, 5, 0, 4, 3, 1)]
     jobs.append((0, items[0][1], items[0][2], items[0][3], extra.data_ptr()))
     torch.cuda.synchronize()
     st = gpu.render_batch_dev(jobs)
     assert st.samples == sum(s for _, s in singles) + singles[0][1]
-    for k in range(4):
+    for k in range(len(items)):
         got = films[k].cpu().numpy()
         assert np.array_equal(got.view(np.uint32), singles[k][0].view(np.uint32)), k
     assert np.array_equal(extra.cpu().numpy().view(np.uint32), singles[0][0].view(np.uint32))
