@@ -563,9 +563,9 @@ void tr_ctx_destroy(tr_ctx* ctx) {
   cudaStreamSynchronize(ctx->stream);
   release_render(ctx);
   release_guide(ctx);
-  for (DevBuf* b : {&ctx->d_nodes, &ctx->d_nodes4, &ctx->d_slots, &ctx->d_spheres, &ctx->d_prims, &ctx->d_tshade, &ctx->d_mats,
-                    &ctx->d_lights, &ctx->d_roots, &ctx->d_rays, &ctx->d_out0, &ctx->d_out1, &ctx->d_err,
-                    &ctx->d_env_pool, &ctx->d_envs})
+  for (DevBuf* b : {&ctx->d_nodes, &ctx->d_nodes4, &ctx->d_slots, &ctx->d_spheres, &ctx->d_prims, &ctx->d_tshade,
+                    &ctx->d_mats, &ctx->d_lights, &ctx->d_roots, &ctx->d_rays, &ctx->d_out0, &ctx->d_out1,
+                    &ctx->d_err, &ctx->d_env_pool, &ctx->d_envs})
     b->release();
   cudaStreamDestroy(ctx->stream);
   delete ctx;

@@ -1560,7 +1560,8 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   const size_t oP = L.take(5 * N * f4), oRng = L.take(N * 8), oM = L.take(3 * N * f4), oH = L.take(2 * N * f4),
                oSC = L.take(N * 7 * f4), oNU = L.take(N * NL * 8), oSH = L.take(N * NL * 3 * f4),
                oQe = L.take(2 * 2 * N * 4), oQa = L.take(2 * N * 4), oQm = L.take(kMatKinds * N * 4),
-               oQn = L.take(kNeeKinds * N * NL * 4), oQs = L.take(N * NL * 4), oCtr = L.take(kCtrWords * 4), oSt = L.take(64),
+               oQn = L.take(kNeeKinds * N * NL * 4), oQs = L.take(N * NL * 4), oCtr = L.take(kCtrWords * 4),
+               oSt = L.take(64),
                oJob = L.take(sizeof(JobDev));
   if (npix > (1ll << 24) || L.off > kNoAllocScratchBytes) {
     char msg[256];
