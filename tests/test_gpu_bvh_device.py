@@ -64,7 +64,8 @@ def test_device_tree_hits_equal_the_oracle(gpu, case):
     assert ((p1 >= 0) == (p0 >= 0)).mean() >= 0.999
 
 
-@pytest.mark.parametrize("make", [lambda: scenes.cornell(64, 64, 4), lambda: scenes.occluded_room(64, 48, 4, n_tris=20000)])
+@pytest.mark.parametrize("make", [lambda: scenes.cornell(64, 64, 4), lambda: scenes.occluded_room(64, 48, 4, n_tris=20000),
+                                  lambda: scenes.outdoor(64, 48, 4, glass=False)])
 def test_device_tree_renders_the_same_image(gpu, make):
     sc, cam, filt, par = make()
     gpu.upload(sc)

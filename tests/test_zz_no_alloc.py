@@ -30,9 +30,13 @@ def _cases():
     sc = scenes.random_scene(0, n_tris=60, n_spheres=8)
     yield ("random", sc, scenes.random_camera(48, 40, 0), scenes.make_filter(0.5, 0.6),
            scenes.make_params(48, 40, 4, 1, 7, seed_base=5))
+    sc, cam, filt, par = scenes.outdoor(48, 32, 4)  # environment light, glass, metal
+    yield "outdoor", sc, cam, filt, par
+    sc, cam, filt, par = scenes.disney15_row(48, 24, 4)
+    yield "disney15", sc, cam, filt, par
 
 
-@pytest.mark.parametrize("case", [0, 1])
+@pytest.mark.parametrize("case", [0, 1, 2, 3])
 def test_noalloc_matches_render_dev_on_consecutive_calls(gpu, case):
     import torch
     name, sc, cam, filt, par = list(_cases())[case]
