@@ -254,6 +254,7 @@ struct SceneDesc {
   int32_t max_leaf_prims = 1;
   uint32_t env_width = 0, env_height = 0;  // environment map (0 x 0: none)
   std::vector<float> env_texels, env_to_light, env_to_world;
+  std::vector<uint8_t> env_texels8;  // an 8-bit map instead of env_texels
   tr_scene_desc view() const;
 };
 
@@ -299,7 +300,7 @@ using Color3f = Point3f;
 // (u, v) = (x / (width - 1), y / (height - 1)), coordinates wrapped by repeat.
 RC<Texture2D> create_hdr_texture2d(const RC<Image2D<Color3f>>& image);
 // create_ibl_light (src/light/environment_light.cpp:196-203): the texture
-// (an HDR texture, or a constant one) over the sphere of directions,
+// (an HDR, 8-bit image or constant texture) over the sphere of directions,
 // (u, v) = (phi / 2pi, theta / pi) in the light space of world_to_light.
 RC<EnvironmentLight> create_ibl_light(RC<const Texture2D> tex, const Transform& world_to_light);
 
@@ -317,13 +318,20 @@ struct Color3b {
 void write_image_to_hdr(const Image2D<Spectrum>& image, const std::string& filename);
 // 8-bit RGB PNG (row 0 first).
 void write_image_to_png(const Image2D<Color3b>& image, const std::string& filename);
+// An 8-bit PNG (grey, RGB, palette or RGBA; not interlaced), rows flipped
+// so that the file's last row is row 0, as load_image_from_file
+// (src/utility/image_file.cpp:26-58) loads it; grey+alpha is refused.
+RC<Image2D<Color3b>> load_image_from_file(const std::string& filename);
+// create_image_texture2d (src/texture/image_texture2d.cpp:9-37): bilinear
+// lookups in byte arithmetic (each weighted texel truncated to a byte), / 255.
+RC<Texture2D> create_image_texture2d(const RC<Image2D<Color3b>>& image);
 // A Radiance HDR file (flat or run-length scanlines, "-Y height +X width"),
 // row 0 = the first scanline, RGBE decoded as byte * 2^(exponent - 136).
 RC<Image2D<Color3f>> load_hdr_from_file(const std::string& filename);
 // create_texture2d_from_file (src/utility/image_file.cpp:168-178): ".hdr"
-// files become HDR textures. The 8-bit formats (.png, .jpg, .jpeg) have no
-// reader here and throw TracerError(TR_ERR_UNSUPPORTED); other extensions
-// throw TR_ERR_ARG, as the reference throws for them.
+// files become HDR textures, ".png" files image textures. JPEG has no reader
+// here and throws TracerError(TR_ERR_UNSUPPORTED); other extensions throw
+// TR_ERR_ARG, as the reference throws for them.
 RC<const Texture2D> create_texture2d_from_file(const std::string& filename);
 // The textures of an MTL material (src/utility/image_file.hpp:23-45).
 struct MaterialTexture {

@@ -122,12 +122,17 @@ typedef struct tr_scene_desc {
    * (src/light/environment_light.cpp:14-84,196-203, src/texture/hdr_texture.cpp:9-37)
    * with scene->environment_light set and the light appended to scene->lights
    * after the area lights, as the reference's demo driver does
-   * (src/main.cpp:59-67). env_texels == NULL: no environment light. */
+   * (src/main.cpp:59-67). env_texels and env_texels8 NULL: no environment light. */
   uint32_t env_width, env_height;
   const float* env_texels;   /* 3 * env_width * env_height, linear RGB; texel (x, y) at 3 * (x + y * env_width),
                                 row y at v = y / (env_height - 1) (v = theta / pi) */
   const float* env_to_light; /* 16, row-major world_to_light matrix */
   const float* env_to_world; /* 16, row-major inverse of env_to_light (the Transform's inverse) */
+  /* An 8-bit map instead of env_texels: create_image_texture2d(image)
+   * (src/texture/image_texture2d.cpp:9-37), 3 bytes per texel in the same
+   * layout, looked up with the reference's byte arithmetic and divided by
+   * 255. Used when env_texels is NULL and this is not. */
+  const uint8_t* env_texels8;
 } tr_scene_desc;
 
 /* create_thin_lens_camera arguments (src/camera/thin_lens_camera.cpp:23-36). */

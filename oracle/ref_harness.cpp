@@ -152,16 +152,27 @@ void* ref_scene_create(const tr_scene_desc* d) {
   s->scene = create_general_scene(s->bvh);
   for (uint32_t l = 0; l < d->num_lights; ++l)
     s->scene->lights.push_back(s->prims[d->light_prims[l]]->as_area_light());
-  if (d->env_texels && d->env_width > 0 && d->env_height > 0) {
-    // the demo driver's environment light (src/main.cpp:59-67) over an HDR image
-    auto img = newRC<Image2D<Color3f>>((int)d->env_width, (int)d->env_height);
-    for (uint32_t y = 0; y < d->env_height; ++y)
-      for (uint32_t x = 0; x < d->env_width; ++x) {
-        const float* t = d->env_texels + 3 * ((size_t)x + (size_t)y * d->env_width);
-        img->at((int)x, (int)y) = Color3f(t[0], t[1], t[2]);
-      }
-    auto ibl = create_ibl_light(create_hdr_texture2d(img),
-                                Transform(to_matrix(d->env_to_light), to_matrix(d->env_to_world)));
+  if ((d->env_texels || d->env_texels8) && d->env_width > 0 && d->env_height > 0) {
+    // the demo driver's environment light (src/main.cpp:59-67) over an HDR or 8-bit image
+    RC<Texture2D> tex;
+    if (d->env_texels) {
+      auto img = newRC<Image2D<Color3f>>((int)d->env_width, (int)d->env_height);
+      for (uint32_t y = 0; y < d->env_height; ++y)
+        for (uint32_t x = 0; x < d->env_width; ++x) {
+          const float* t = d->env_texels + 3 * ((size_t)x + (size_t)y * d->env_width);
+          img->at((int)x, (int)y) = Color3f(t[0], t[1], t[2]);
+        }
+      tex = create_hdr_texture2d(img);
+    } else {
+      auto img = newRC<Image2D<Color3b>>((int)d->env_width, (int)d->env_height);
+      for (uint32_t y = 0; y < d->env_height; ++y)
+        for (uint32_t x = 0; x < d->env_width; ++x) {
+          const uint8_t* t = d->env_texels8 + 3 * ((size_t)x + (size_t)y * d->env_width);
+          img->at((int)x, (int)y) = Color3b(t[0], t[1], t[2]);
+        }
+      tex = create_image_texture2d(img);
+    }
+    auto ibl = create_ibl_light(tex, Transform(to_matrix(d->env_to_light), to_matrix(d->env_to_world)));
     s->scene->environment_light = ibl;
     s->scene->lights.push_back(ibl.get());
   }

@@ -389,6 +389,7 @@ struct Dist2D {
 struct Env {
   int w = 0, h = 0;
   std::vector<real> tex;      // 3 per texel, texel (x, y) at 3 * (x + y * w)
+  std::vector<uint8_t> tex8;  // an 8-bit map (ImageTexture2D) instead, same layout
   real to_light[16], to_world[16];
   Dist2D dist;
   V3 center;
@@ -400,6 +401,16 @@ struct Env {
   // Point3f * double (geometry.hpp:268-271): double product rounded to float
   static Sp scaled(Sp c, double f) { return Sp((real)(f * c.r), (real)(f * c.g), (real)(f * c.b)); }
   // Texture2D::evaluate with the repeat wrap, LinearSampler::Sample2D (utility/sampler.hpp:16-29)
+  // Point3<uint8_t>: each product with a double truncates to a byte, sums are bytes
+  struct B3 {
+    uint8_t x, y, z;
+  };
+  B3 texel8(int x, int y) const {
+    const uint8_t* t = &tex8[3 * ((size_t)x + (size_t)y * w)];
+    return B3{t[0], t[1], t[2]};
+  }
+  static B3 scaled8(B3 c, double f) { return B3{(uint8_t)(f * c.x), (uint8_t)(f * c.y), (uint8_t)(f * c.z)}; }
+  static B3 add8(B3 a, B3 b) { return B3{(uint8_t)(a.x + b.x), (uint8_t)(a.y + b.y), (uint8_t)(a.z + b.z)}; }
   Sp eval(real u_in, real v_in) const {
     const real uw = std::clamp<real>(u_in - std::floor(u_in), 0, 1);
     const real vw = std::clamp<real>(v_in - std::floor(v_in), 0, 1);
@@ -408,6 +419,12 @@ struct Env {
     const int u0 = std::clamp(static_cast<int>(u), 0, w - 1), u1 = std::clamp(u0 + 1, 0, w - 1);
     const int v0 = std::clamp(static_cast<int>(v), 0, h - 1), v1 = std::clamp(v0 + 1, 0, h - 1);
     const double du = u - u0, dv = v - v0;
+    if (!tex8.empty()) {
+      // ImageTexture2D::evaluate_impl (texture/image_texture2d.cpp:26-30): bytes / 255
+      const B3 c = add8(scaled8(add8(scaled8(texel8(u0, v0), 1.0 - du), scaled8(texel8(u1, v0), du)), 1.0 - dv),
+                        scaled8(add8(scaled8(texel8(u0, v1), 1.0 - du), scaled8(texel8(u1, v1), du)), dv));
+      return Sp(c.x / real(255.0), c.y / real(255.0), c.z / real(255.0));
+    }
     return scaled(scaled(texel(u0, v0), 1.0 - du) + scaled(texel(u1, v0), du), 1.0 - dv) +
            scaled(scaled(texel(u0, v1), 1.0 - du) + scaled(texel(u1, v1), du), dv);
   }
@@ -2017,11 +2034,12 @@ void* orc_scene_create(const tr_scene_desc* d) {
   }
   for (uint32_t l = 0; l < d->num_lights; ++l) sc->lights.push_back(d->light_prims[l]);
   build_bvh(*sc);
-  if (d->env_texels && d->env_width > 0 && d->env_height > 0) {
+  if ((d->env_texels || d->env_texels8) && d->env_width > 0 && d->env_height > 0) {
     auto env = std::make_unique<Env>();
     env->w = (int)d->env_width;
     env->h = (int)d->env_height;
-    env->tex.assign(d->env_texels, d->env_texels + 3 * (size_t)env->w * env->h);
+    if (d->env_texels) env->tex.assign(d->env_texels, d->env_texels + 3 * (size_t)env->w * env->h);
+    else env->tex8.assign(d->env_texels8, d->env_texels8 + 3 * (size_t)env->w * env->h);
     std::memcpy(env->to_light, d->env_to_light, 64);
     std::memcpy(env->to_world, d->env_to_world, 64);
     env->build_distribution();

@@ -1,5 +1,6 @@
 // Drives the image-file helpers of the C++ host API for tests/test_image_file.py:
 //   image_file load <file.hdr>       prints "size w h" and every pixel
+//   image_file png <file.png>        the same for load_image_from_file (bytes)
 //   image_file write <file.hdr> w h  writes a w x h test pattern with write_image_to_hdr
 //   image_file tex <file>            create_texture2d_from_file, one lookup
 //   image_file mtl <file.obj>        prints create_texture_from_file for each material
@@ -22,6 +23,14 @@ int main(int argc, char** argv) {
         for (int x = 0; x < img->width(); ++x) {
           const Color3f& c = img->at(x, y);
           std::printf("%.9g %.9g %.9g\n", c.x, c.y, c.z);
+        }
+    } else if (cmd == "png") {
+      auto img = load_image_from_file(path);
+      std::printf("size %d %d\n", img->width(), img->height());
+      for (int y = 0; y < img->height(); ++y)
+        for (int x = 0; x < img->width(); ++x) {
+          const Color3b& c = img->at(x, y);
+          std::printf("%d %d %d\n", c.x, c.y, c.z);
         }
     } else if (cmd == "write" && argc >= 5) {
       const int w = std::atoi(argv[3]), h = std::atoi(argv[4]);

@@ -85,12 +85,14 @@ def test_cornell_metal(gpu, min_depth):
     _compare(out, ref, 0.8)
 
 
-@pytest.mark.parametrize("glass,area_light", [(False, True), (True, True), (False, False)])
-def test_outdoor_environment_light(gpu, glass, area_light):
+@pytest.mark.parametrize("glass,area_light,env_8bit", [(False, True, False), (True, True, False),
+                                                      (False, False, False), (False, True, True)])
+def test_outdoor_environment_light(gpu, glass, area_light, env_8bit):
     """An open scene under the IBL environment light: escaping camera rays
     and rays after delta samples see the map, every vertex samples it (after
-    the area light) and the MIS ray's escape is weighted against it."""
-    sc, cam, filt, par = scenes.outdoor(64, 48, 8, glass=glass, area_light=area_light)
+    the area light) and the MIS ray's escape is weighted against it; the map
+    as HDR floats or as 8-bit texels (ImageTexture2D's byte arithmetic)."""
+    sc, cam, filt, par = scenes.outdoor(64, 48, 8, glass=glass, area_light=area_light, env_8bit=env_8bit)
     orc = oracle.Oracle(sc, "port")
     orc.set_camera(cam, filt)
     ref = orc.render(par)

@@ -3,7 +3,9 @@ C++ host API: the Radiance HDR reader on files written here (flat and
 run-length scanlines), write/read round trips, create_texture2d_from_file's
 format rules and create_texture_from_file on MTL materials."""
 import os
+import struct
 import subprocess
+import zlib
 
 import numpy as np
 import pytest
@@ -93,10 +95,10 @@ def test_write_then_load_round_trip(program, tmp_path):
     assert np.allclose(px, want, rtol=0, atol=want.max(-1, keepdims=True) / 128)
 
 
-@pytest.mark.parametrize("name,status", [("x.png", TR_ERR_UNSUPPORTED), ("x.jpg", TR_ERR_UNSUPPORTED),
+@pytest.mark.parametrize("name,status", [("missing.png", TR_ERR_ARG), ("x.jpg", TR_ERR_UNSUPPORTED),
                                          ("x.tga", TR_ERR_ARG), ("noext", TR_ERR_ARG), ("missing.hdr", TR_ERR_ARG)])
 def test_texture_file_rules(program, tmp_path, name, status):
-    """create_texture2d_from_file: .hdr read, 8-bit formats unsupported here,
+    """create_texture2d_from_file: .hdr and .png read, JPEG unsupported here,
     other extensions rejected as the reference rejects them."""
     r = subprocess.run([program, "tex", str(tmp_path / name)], capture_output=True, text=True)
     assert r.returncode == 1 and r.stdout.startswith(f"error {status}"), r.stdout
@@ -138,8 +140,129 @@ def test_material_textures(program, tmp_path):
     assert m[3:6] == ["0.5", "0.5", "0.5"]  # the map (1.0) scaled by Kd
 
 
-def test_material_with_png_map_is_unsupported(program, tmp_path):
+def _png(rows, ctype, palette=None, filters=None):
+    """A PNG of 8-bit rows (list of byte arrays, top first), zlib-compressed,
+    each row encoded with the given filter type (0-4) as ISO/IEC 15948 defines."""
+    ch = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
+    h, w = len(rows), len(rows[0]) // ch
+    raw, prev = bytearray(), bytes(len(rows[0]))
+    for y, row in enumerate(rows):
+        ft = (filters or [0])[y % len(filters or [0])]
+        out = bytearray()
+        for i, v in enumerate(row):
+            a = row[i - ch] if i >= ch else 0
+            b = prev[i]
+            c = prev[i - ch] if i >= ch else 0
+            if ft == 0:
+                pr = 0
+            elif ft == 1:
+                pr = a
+            elif ft == 2:
+                pr = b
+            elif ft == 3:
+                pr = (a + b) >> 1
+            else:
+                p = a + b - c
+                pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
+                pr = a if pa <= pb and pa <= pc else (b if pb <= pc else c)
+            out.append((v - pr) & 255)
+        raw += bytes([ft]) + out
+        prev = bytes(row)
+
+    def chunk(t, d):
+        return struct.pack(">I", len(d)) + t + d + struct.pack(">I", zlib.crc32(t + d) & 0xffffffff)
+    png = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, ctype, 0, 0, 0))
+    if palette is not None:
+        png += chunk(b"PLTE", bytes(palette))
+    # two IDAT chunks, the second one empty-ish: the stream spans chunks
+    z = zlib.compress(bytes(raw), 9)
+    return png + chunk(b"IDAT", z[:len(z) // 2]) + chunk(b"IDAT", z[len(z) // 2:]) + chunk(b"IEND", b"")
+
+
+def _load_png(program, path):
+    r = subprocess.run([program, "png", str(path)], capture_output=True, text=True)
+    lines = r.stdout.splitlines()
+    if r.returncode != 0:
+        return None, lines
+    w, h = (int(v) for v in lines[0].split()[1:])
+    return np.array([[int(v) for v in ln.split()] for ln in lines[1:]], np.uint8).reshape(h, w, 3), lines
+
+
+@pytest.mark.parametrize("ctype", [0, 2, 3, 6])
+def test_load_png(program, tmp_path, ctype):
+    """Grey, RGB, palette and RGBA PNGs with every filter type and a
+    dynamic-Huffman zlib stream; rows come back flipped (the file's last row
+    is row 0), grey expanded to RGB, alpha dropped."""
+    rng = np.random.default_rng(ctype)
+    h, w = 7, 23
+    ch = {0: 1, 2: 3, 3: 1, 6: 4}[ctype]
+    smooth = (np.add.outer(np.arange(h) * 9, np.arange(w * ch) * 3) % 256).astype(np.uint8)
+    data = np.where(rng.random((h, w * ch)) < 0.3, rng.integers(0, 256, (h, w * ch)), smooth).astype(np.uint8)
+    palette = rng.integers(0, 256, 3 * 256).astype(np.uint8) if ctype == 3 else None
+    p = tmp_path / "a.png"
+    p.write_bytes(_png([bytes(r) for r in data], ctype, palette, filters=[0, 1, 2, 3, 4]))
+    got, lines = _load_png(program, p)
+    assert got is not None, lines
+    px = data.reshape(h, w, ch)
+    if ctype == 0:
+        want = np.repeat(px, 3, axis=2)
+    elif ctype == 3:
+        want = palette.reshape(256, 3)[px[..., 0]]
+    else:
+        want = px[..., :3]
+    assert np.array_equal(got, want[::-1])
+
+
+def test_png_refusals(program, tmp_path):
+    p = tmp_path / "ga.png"
+    p.write_bytes(_png([bytes(8)] * 2, 4))
+    r = subprocess.run([program, "png", str(p)], capture_output=True, text=True)
+    assert r.returncode == 1 and "component" in r.stdout  # grey+alpha, as the reference refuses it
+    p = tmp_path / "bad.png"
+    p.write_bytes(_png([bytes(range(12))] * 3, 2)[:-30])  # truncated
+    r = subprocess.run([program, "png", str(p)], capture_output=True, text=True)
+    assert r.returncode == 1
+
+
+def _lerp8(img, u, v):
+    """ImageTexture2D's byte lookup: each weighted texel truncated to a byte, / 255."""
+    h, w = img.shape[:2]
+    u = min(max(np.float32(u) - np.floor(np.float32(u)), 0), 1) * (w - 1)
+    v = min(max(np.float32(v) - np.floor(np.float32(v)), 0), 1) * (h - 1)
+    u0, v0 = int(u), int(v)
+    u1, v1 = min(u0 + 1, w - 1), min(v0 + 1, h - 1)
+    du, dv = u - u0, v - v0
+    t = lambda x, f: (np.floor(f * x.astype(np.float64))).astype(np.int64) & 255
+    top = (t(img[v0, u0], 1 - du) + t(img[v0, u1], du)) & 255
+    bot = (t(img[v1, u0], 1 - du) + t(img[v1, u1], du)) & 255
+    return (((t(top, 1 - dv) + t(bot, dv)) & 255).astype(np.float32) / np.float32(255)).astype(np.float32)
+
+
+def test_png_texture_lookup(program, tmp_path):
+    img = np.random.default_rng(3).integers(0, 256, (5, 9, 3), dtype=np.uint8)
+    p = tmp_path / "t.png"
+    p.write_bytes(_png([bytes(r) for r in img.reshape(5, 27)], 2))
+    r = subprocess.run([program, "tex", str(p)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout
+    got = np.array([float(v) for v in r.stdout.split()[1:]], np.float32)
+    assert np.array_equal(got, _lerp8(img[::-1], 0.25, 0.5))
+
+
+def test_material_with_png_map(program, tmp_path):
+    """An 8-bit map of an MTL material: bytes / 255 raised to 2.2, back to
+    bytes, times Kd, each step truncating to a byte."""
+    p = tmp_path / "wall.png"
+    p.write_bytes(_png([bytes([200, 100, 50] * 4)] * 3, 2))
     (tmp_path / "s.obj").write_text("mtllib s.mtl\nv 0 0 0\nv 1 0 0\nv 0 1 0\nvn 0 0 1\nf 1//1 2//1 3//1\n")
-    (tmp_path / "s.mtl").write_text("newmtl wall\nKd 0.7 0.6 0.5\nmap_Kd wall.png\n")
+    (tmp_path / "s.mtl").write_text(f"newmtl wall\nKd 0.5 0.5 0.5\nmap_Kd {p}\n")
     r = subprocess.run([program, "mtl", str(tmp_path / "s.obj")], capture_output=True, text=True)
-    assert r.returncode == 1 and r.stdout.startswith(f"error {TR_ERR_UNSUPPORTED}")
+    assert r.returncode == 0, r.stdout
+    kd = np.array([float(v) for v in r.stdout.split()[3:6]], np.float32)
+    texel = []
+    for b in (200, 100, 50):
+        g = int(np.float32(np.float32(b) / np.float32(255)) ** np.float32(2.2) * np.float32(255))
+        texel.append(int(g * np.float32(0.5)))
+    # the program looks the texture up at (0.5, 0.5): halfway between texels,
+    # where the byte arithmetic can lose one level
+    want = _lerp8(np.tile(np.array(texel, np.uint8), (3, 4, 1)), 0.5, 0.5)
+    assert np.allclose(kd, want, rtol=0, atol=1e-6), (kd, want)

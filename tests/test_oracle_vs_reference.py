@@ -102,6 +102,18 @@ def test_environment_light(area_light, env_size, min_depth):
     assert np.array_equal(bits(port.render(par)), bits(ref.render(par)))
 
 
+@pytest.mark.parametrize("min_depth", [3, 1])
+def test_environment_light_8bit(min_depth):
+    """An environment light over an 8-bit map (ImageTexture2D): its byte
+    arithmetic (each weighted texel truncated to a byte) in the lookups and in
+    the luminance distribution."""
+    sc, cam, filt, par = scenes.outdoor(32, 24, 4, min_depth=min_depth, env_8bit=True, env_size=(53, 27))
+    port, ref = oracle.Oracle(sc, "port"), oracle.Oracle(sc, "reference")
+    port.set_camera(cam, filt)
+    ref.set_camera(cam, filt)
+    assert np.array_equal(bits(port.render(par)), bits(ref.render(par)))
+
+
 @pytest.mark.parametrize("env,min_depth", [(True, 3), (False, 8), (True, 1)])
 def test_disney15(env, min_depth):
     """The 2015 Disney BSDF (create_disney): rough transmission and inner

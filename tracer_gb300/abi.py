@@ -74,7 +74,7 @@ class TrSceneDesc(C.Structure):
                 ("num_lights", C.c_uint32), ("light_prims", i32p),
                 ("max_leaf_prims", C.c_int32),
                 ("env_width", C.c_uint32), ("env_height", C.c_uint32), ("env_texels", f32p),
-                ("env_to_light", f32p), ("env_to_world", f32p)]
+                ("env_to_light", f32p), ("env_to_world", f32p), ("env_texels8", C.POINTER(C.c_uint8))]
 
 
 class TrCamera(C.Structure):
@@ -199,6 +199,7 @@ class SceneBuffers:
     light_prims: np.ndarray          # (L,) i32
     max_leaf_prims: int = 3
     env_texels: np.ndarray | None = None    # (H,W,3) f32 environment map, row y at v = y / (H - 1)
+    env_texels8: np.ndarray | None = None   # (H,W,3) u8 map (ImageTexture2D) used instead when set
     env_to_light: np.ndarray | None = None  # (16,) f32 world_to_light; identity when None
     env_to_world: np.ndarray | None = None  # (16,) f32 its inverse
     _keep: list = field(default_factory=list, repr=False)
@@ -232,16 +233,21 @@ class SceneBuffers:
         d.num_lights = len(arrs["light_prims"])
         d.light_prims = ptr(arrs["light_prims"], C.c_int32)
         d.max_leaf_prims = int(self.max_leaf_prims)
-        if self.env_texels is not None:
-            tex = np.ascontiguousarray(self.env_texels, dtype=np.float32)
+        if self.env_texels is not None or self.env_texels8 is not None:
+            ldr = self.env_texels is None
+            tex = np.ascontiguousarray(self.env_texels8 if ldr else self.env_texels,
+                                       dtype=np.uint8 if ldr else np.float32)
             if tex.ndim != 3 or tex.shape[2] != 3:
-                raise ValueError("env_texels must be (height, width, 3)")
+                raise ValueError("environment texels must be (height, width, 3)")
             eye = np.eye(4, dtype=np.float32).ravel()
             to_l = np.ascontiguousarray(eye if self.env_to_light is None else self.env_to_light, dtype=np.float32)
             to_w = np.ascontiguousarray(eye if self.env_to_world is None else self.env_to_world, dtype=np.float32)
             self._keep += [tex, to_l, to_w]
             d.env_height, d.env_width = tex.shape[0], tex.shape[1]
-            d.env_texels = ptr(tex, C.c_float)
+            if ldr:
+                d.env_texels8 = tex.ctypes.data_as(C.POINTER(C.c_uint8))
+            else:
+                d.env_texels = ptr(tex, C.c_float)
             d.env_to_light = ptr(to_l, C.c_float)
             d.env_to_world = ptr(to_w, C.c_float)
         return d

@@ -393,17 +393,18 @@ tr_status upload_envs(tr_ctx* ctx) {
     total += (n + 3) & ~size_t(3);
     return at;
   };
-  struct Off { size_t tex, cf, cc, ci, mc; };
+  struct Off { size_t tex, tex8, cf, cc, ci, mc; };
   std::vector<Off> off(envs.size());
   for (size_t i = 0; i < envs.size(); ++i) {
     const EnvHost& e = envs[i];
-    off[i] = {take(e.texels.size()), take(e.cond_func.size()), take(e.cond_cdf.size()), take(e.cond_int.size()),
-              take(e.marg_cdf.size())};
+    off[i] = {take(e.texels.size()), take(e.texels8.size() / 4), take(e.cond_func.size()),
+              take(e.cond_cdf.size()), take(e.cond_int.size()), take(e.marg_cdf.size())};
   }
   std::vector<float> pool(total, 0.0f);
   for (size_t i = 0; i < envs.size(); ++i) {
     const EnvHost& e = envs[i];
     std::copy(e.texels.begin(), e.texels.end(), pool.begin() + (ptrdiff_t)off[i].tex);
+    if (!e.texels8.empty()) std::memcpy(pool.data() + off[i].tex8, e.texels8.data(), e.texels8.size());
     std::copy(e.cond_func.begin(), e.cond_func.end(), pool.begin() + (ptrdiff_t)off[i].cf);
     std::copy(e.cond_cdf.begin(), e.cond_cdf.end(), pool.begin() + (ptrdiff_t)off[i].cc);
     std::copy(e.cond_int.begin(), e.cond_int.end(), pool.begin() + (ptrdiff_t)off[i].ci);
@@ -418,7 +419,8 @@ tr_status upload_envs(tr_ctx* ctx) {
     const EnvHost& e = envs[i];
     DEnv& r = recs[i];
     std::memset(&r, 0, sizeof(r));
-    r.texels = reinterpret_cast<const float4*>(base + off[i].tex);
+    r.texels = e.texels.empty() ? nullptr : reinterpret_cast<const float4*>(base + off[i].tex);
+    r.texels8 = e.texels8.empty() ? nullptr : reinterpret_cast<const uchar4*>(base + off[i].tex8);
     r.cond_func = base + off[i].cf;
     r.cond_cdf = base + off[i].cc;
     r.cond_int = base + off[i].ci;
@@ -737,7 +739,7 @@ static tr_status build_host_scene(tr_ctx* ctx, const tr_scene_desc* d, HostScene
     L.env = -1;
     hs.lights.push_back(L);
   }
-  if (d->env_texels) {
+  if (d->env_texels || d->env_texels8) {
     // the environment light follows the area lights in scene.lights; its
     // bounding sphere is that of the tree's root box, the union of the
     // primitive boxes

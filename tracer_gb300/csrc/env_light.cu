@@ -30,7 +30,7 @@ float build_1d(const float* f, int n, float* cdf) {
 }  // namespace
 
 bool build_env_tables(const tr_scene_desc* d, EnvHost& env, std::string& err) {
-  if (!d->env_texels) return true;
+  if (!d->env_texels && !d->env_texels8) return true;
   if (d->env_width == 0 || d->env_height == 0 || d->env_width > 65536 || d->env_height > 65536) {
     err = "environment map size out of range";
     return false;
@@ -42,12 +42,22 @@ bool build_env_tables(const tr_scene_desc* d, EnvHost& env, std::string& err) {
   const int w = (int)d->env_width, h = (int)d->env_height;
   env.w = w;
   env.h = h;
-  env.texels.resize(4 * (size_t)w * h);
-  for (size_t i = 0; i < (size_t)w * h; ++i) {
-    env.texels[4 * i] = d->env_texels[3 * i];
-    env.texels[4 * i + 1] = d->env_texels[3 * i + 1];
-    env.texels[4 * i + 2] = d->env_texels[3 * i + 2];
-    env.texels[4 * i + 3] = 0.0f;
+  if (d->env_texels) {
+    env.texels.resize(4 * (size_t)w * h);
+    for (size_t i = 0; i < (size_t)w * h; ++i) {
+      env.texels[4 * i] = d->env_texels[3 * i];
+      env.texels[4 * i + 1] = d->env_texels[3 * i + 1];
+      env.texels[4 * i + 2] = d->env_texels[3 * i + 2];
+      env.texels[4 * i + 3] = 0.0f;
+    }
+  } else {
+    env.texels8.resize(4 * (size_t)w * h);
+    for (size_t i = 0; i < (size_t)w * h; ++i) {
+      env.texels8[4 * i] = d->env_texels8[3 * i];
+      env.texels8[4 * i + 1] = d->env_texels8[3 * i + 1];
+      env.texels8[4 * i + 2] = d->env_texels8[3 * i + 2];
+      env.texels8[4 * i + 3] = 0;
+    }
   }
   for (int r = 0; r < 3; ++r)
     for (int c = 0; c < 3; ++c) {
@@ -55,6 +65,8 @@ bool build_env_tables(const tr_scene_desc* d, EnvHost& env, std::string& err) {
       env.to_world[3 * r + c] = d->env_to_world[4 * r + c];
     }
   const float4* tex = reinterpret_cast<const float4*>(env.texels.data());
+  const uchar4* tex8 = reinterpret_cast<const uchar4*>(env.texels8.data());
+  const bool ldr = !env.texels8.empty();
   // luminance x solid angle per cell of the (at most) 360 x 180 grid; each
   // cell sums the luminance of the texel centres it covers plus a one-texel
   // border
@@ -75,7 +87,8 @@ bool build_env_tables(const tr_scene_desc* d, EnvHost& env, std::string& err) {
       float lum = 0.0f;
       for (int sy = yb; sy <= ye; ++sy)
         for (int sx = xb; sx <= xe; ++sx) {
-          const f3 c = env_tex_eval(tex, w, h, (float)(sx + 0.5) / w, (float)(sy + 0.5) / h);
+          const float su = (float)(sx + 0.5) / w, sv = (float)(sy + 0.5) / h;
+          const f3 c = ldr ? env_tex_eval8(tex8, w, h, su, sv) : env_tex_eval(tex, w, h, su, sv);
           lum += 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z;
         }
       // d_omega = sin(theta) d_theta d_phi over the cell, the sine in double

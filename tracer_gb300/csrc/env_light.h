@@ -17,6 +17,7 @@ struct EnvHost {
   int w = 0, h = 0;              // texture size
   int nu = 0, nv = 0;            // distribution grid: min(w, 360) x min(h, 180)
   std::vector<float> texels;     // 4 per texel (r, g, b, 0), texel (x, y) at 4 * (x + y * w)
+  std::vector<uint8_t> texels8;  // an 8-bit map instead: 4 bytes per texel (r, g, b, 0)
   std::vector<float> cond_func;  // nv rows of nu: the conditional densities p(u | v) before normalisation
   std::vector<float> cond_cdf;   // nv rows of nu + 1
   std::vector<float> cond_int;   // nv: each row's integral (the marginal's function)

@@ -40,4 +40,32 @@ TR_HD f3 env_tex_eval(const float4* tex, int w, int h, float u_in, float v_in) {
              (float)(ev * tb) + (float)(dv * bb));
 }
 
+// ImageTexture2D::evaluate_impl (src/texture/image_texture2d.cpp:26-30) over
+// Image2D<Color3b>: the same bilinear weights, but each weighted texel is a
+// Point3<uint8_t> (the double product truncated to a byte) and the sums are
+// bytes; the result is divided by 255.
+TR_HD f3 env_tex_eval8(const uchar4* tex, int w, int h, float u_in, float v_in) {
+  float uw = u_in - floorf(u_in), vw = v_in - floorf(v_in);
+  uw = uw < 0.0f ? 0.0f : (1.0f < uw ? 1.0f : uw);
+  vw = vw < 0.0f ? 0.0f : (1.0f < vw ? 1.0f : vw);
+  double u = (double)uw, v = (double)vw;
+  u = (u < 0.0 ? 0.0 : (1.0 < u ? 1.0 : u)) * (double)(w - 1);
+  v = (v < 0.0 ? 0.0 : (1.0 < v ? 1.0 : v)) * (double)(h - 1);
+  int u0 = (int)u, v0 = (int)v;
+  u0 = u0 < 0 ? 0 : (u0 > w - 1 ? w - 1 : u0);
+  v0 = v0 < 0 ? 0 : (v0 > h - 1 ? h - 1 : v0);
+  const int u1 = u0 + 1 > w - 1 ? w - 1 : u0 + 1;
+  const int v1 = v0 + 1 > h - 1 ? h - 1 : v0 + 1;
+  const double du = u - u0, dv = v - v0;
+  const double eu = 1.0 - du, ev = 1.0 - dv;
+  const uchar4 a = tex[u0 + (size_t)v0 * w], b = tex[u1 + (size_t)v0 * w];
+  const uchar4 c = tex[u0 + (size_t)v1 * w], d = tex[u1 + (size_t)v1 * w];
+  auto by = [](double f, int x) { return (int)(f * (double)x) & 0xff; };
+  auto ch = [&](int ta, int tb, int tc, int td) {
+    const int top = (by(eu, ta) + by(du, tb)) & 0xff, bot = (by(eu, tc) + by(du, td)) & 0xff;
+    return (float)((by(ev, top) + by(dv, bot)) & 0xff) / 255.0f;
+  };
+  return mk3(ch(a.x, b.x, c.x, d.x), ch(a.y, b.y, c.y, d.y), ch(a.z, b.z, c.z, d.z));
+}
+
 }  // namespace trg

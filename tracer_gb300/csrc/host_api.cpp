@@ -263,6 +263,35 @@ class HdrTexture : public Texture2D {
   RC<Image2D<Color3f>> img_;
 };
 
+// ImageTexture2D (src/texture/image_texture2d.cpp:9-37): the same lookup over
+// bytes, each weighted texel truncated to a byte (Point3<uint8_t>), / 255.
+class ImageTexture : public Texture2D {
+ public:
+  explicit ImageTexture(RC<Image2D<Color3b>> img) : img_(std::move(img)) {}
+  Spectrum evaluate(const Point2f& uv) const override {
+    auto wrap = [](real x) { return std::clamp<real>(x - std::floor(x), 0, 1); };
+    const int w = img_->width(), h = img_->height();
+    const double u = std::clamp((double)wrap(uv.x), 0.0, 1.0) * (w - 1);
+    const double v = std::clamp((double)wrap(uv.y), 0.0, 1.0) * (h - 1);
+    const int u0 = std::clamp((int)u, 0, w - 1), u1 = std::clamp(u0 + 1, 0, w - 1);
+    const int v0 = std::clamp((int)v, 0, h - 1), v1 = std::clamp(v0 + 1, 0, h - 1);
+    const double du = u - u0, dv = v - v0;
+    auto mul = [](const Color3b& c, double f) {
+      return Color3b{(uint8_t)(f * c.x), (uint8_t)(f * c.y), (uint8_t)(f * c.z)};
+    };
+    auto add = [](const Color3b& a, const Color3b& b) {
+      return Color3b{(uint8_t)(a.x + b.x), (uint8_t)(a.y + b.y), (uint8_t)(a.z + b.z)};
+    };
+    const Color3b r = add(mul(add(mul(img_->at(u0, v0), 1.0 - du), mul(img_->at(u1, v0), du)), 1.0 - dv),
+                          mul(add(mul(img_->at(u0, v1), 1.0 - du), mul(img_->at(u1, v1), du)), dv));
+    return Spectrum(r.x / real(255.0), r.y / real(255.0), r.z / real(255.0));
+  }
+  const Image2D<Color3b>& image() const { return *img_; }
+
+ private:
+  RC<Image2D<Color3b>> img_;
+};
+
 class IblLight : public EnvironmentLight {
  public:
   IblLight(RC<const Texture2D> tex, const Transform& t) : tex(std::move(tex)), world_to_light(t) {}
@@ -345,12 +374,21 @@ class GeneralScene : public Scene {
             const Color3f& c = img.at(x, y);
             d.env_texels.insert(d.env_texels.end(), {c.x, c.y, c.z});
           }
+      } else if (const auto* it = dynamic_cast<const ImageTexture*>(ibl->tex.get())) {
+        const Image2D<Color3b>& img = it->image();
+        d.env_width = (uint32_t)img.width();
+        d.env_height = (uint32_t)img.height();
+        for (int y = 0; y < img.height(); ++y)
+          for (int x = 0; x < img.width(); ++x) {
+            const Color3b& c = img.at(x, y);
+            d.env_texels8.insert(d.env_texels8.end(), {c.x, c.y, c.z});
+          }
       } else if (const auto* ct = dynamic_cast<const ConstantTexture*>(ibl->tex.get())) {
         const Spectrum c = ct->evaluate(Point2f{0, 0});  // a constant map is a 1 x 1 image
         d.env_width = d.env_height = 1;
         d.env_texels = {c.r, c.g, c.b};
       } else {
-        throw std::invalid_argument("environment light texture must be an HDR or constant texture");
+        throw std::invalid_argument("environment light texture must be an HDR, 8-bit image or constant texture");
       }
       put_matrix(d.env_to_light, ibl->world_to_light.matrix());
       put_matrix(d.env_to_world, ibl->world_to_light.inverse_matrix());
@@ -442,6 +480,11 @@ RC<Texture2D> create_constant_texture2d(const Spectrum& constant) { return std::
 RC<Texture2D> create_hdr_texture2d(const RC<Image2D<Color3f>>& image) {
   if (!image || image->width() <= 0 || image->height() <= 0) throw std::invalid_argument("empty HDR image");
   return std::make_shared<HdrTexture>(image);
+}
+
+RC<Texture2D> create_image_texture2d(const RC<Image2D<Color3b>>& image) {
+  if (!image || image->width() <= 0 || image->height() <= 0) throw std::invalid_argument("empty image");
+  return std::make_shared<ImageTexture>(image);
 }
 
 RC<EnvironmentLight> create_ibl_light(RC<const Texture2D> tex, const Transform& world_to_light) {
@@ -630,7 +673,8 @@ tr_scene_desc SceneDesc::view() const {
   if (env_width && env_height) {
     d.env_width = env_width;
     d.env_height = env_height;
-    d.env_texels = env_texels.data();
+    d.env_texels = env_texels.empty() ? nullptr : env_texels.data();
+    d.env_texels8 = env_texels8.empty() ? nullptr : env_texels8.data();
     d.env_to_light = env_to_light.data();
     d.env_to_world = env_to_world.data();
   }

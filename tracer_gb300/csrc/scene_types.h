@@ -131,6 +131,7 @@ struct DLight {
 // bounding sphere.
 struct DEnv {
   const float4* texels;     // w x h, texel (x, y) at x + y * w
+  const uchar4* texels8;    // an 8-bit map instead (texels is then null)
   const float* cond_func;   // nv x nu
   const float* cond_cdf;    // nv x (nu + 1)
   const float* cond_int;    // nv (the marginal's function)

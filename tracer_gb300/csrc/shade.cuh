@@ -940,7 +940,8 @@ __device__ __forceinline__ f3 env_emit(const DEnv& e, f3 d) {
   dir = normalize(rot3(e.to_light, dir));
   const float phi = local_phi(dir);
   const float theta = acosf(clamp_pm1(dir.z));
-  return env_tex_eval(e.texels, e.w, e.h, clamp01(phi / (2.0f * kPi)), clamp01(theta * kInvPi));
+  const float u = clamp01(phi / (2.0f * kPi)), v = clamp01(theta * kInvPi);
+  return e.texels8 ? env_tex_eval8(e.texels8, e.w, e.h, u, v) : env_tex_eval(e.texels, e.w, e.h, u, v);
 }
 
 // Distribution1D::sample_continuous (src/utility/distribution.hpp:37-55):

@@ -289,7 +289,8 @@ def rotate_x(theta):
     return m, np.ascontiguousarray(m.reshape(4, 4).T).ravel()
 
 
-def outdoor(width=96, height=64, spp=8, max_depth=6, min_depth=3, env_size=(64, 32), area_light=True, glass=True):
+def outdoor(width=96, height=64, spp=8, max_depth=6, min_depth=3, env_size=(64, 32), area_light=True, glass=True,
+            env_8bit=False):
     """An open scene under an environment light: a ground quad, Disney12,
     metal, glass (Lambertian when `glass` is False) and Lambertian spheres,
     optionally one small area light; the
@@ -311,7 +312,10 @@ def outdoor(width=96, height=64, spp=8, max_depth=6, min_depth=3, env_size=(64, 
     for k, m in enumerate(mats):
         b.sphere((-2.25 + 1.5 * k, 0.6, 0.0), 0.6, m)
     scene = b.finish(max_leaf_prims=3)
-    scene.env_texels = sky_map(*env_size)
+    if env_8bit:  # the map as 8-bit values (an ImageTexture2D), the sun at full scale
+        scene.env_texels8 = np.clip(sky_map(*env_size, sun_radiance=1.0) * 255.0, 0, 255).astype(np.uint8)
+    else:
+        scene.env_texels = sky_map(*env_size)
     scene.env_to_light, scene.env_to_world = rotate_x(math.pi / 2)
     cam = make_camera(width / height, (0, 1.6, 6.5), (0, 0.9, 0), (0, 1, 0), math.radians(50.0), 0.0, 1.0)
     return scene, cam, make_filter(0.5, 0.6), make_params(width, height, spp, min_depth, max_depth)
