@@ -218,10 +218,21 @@ def test_png_refusals(program, tmp_path):
     p.write_bytes(_png([bytes(8)] * 2, 4))
     r = subprocess.run([program, "png", str(p)], capture_output=True, text=True)
     assert r.returncode == 1 and "component" in r.stdout  # grey+alpha, as the reference refuses it
-    p = tmp_path / "bad.png"
-    p.write_bytes(_png([bytes(range(12))] * 3, 2)[:-30])  # truncated
+    good = _png([bytes(range(12))] * 3, 2)
+    for cut in (30, 2, 3):  # truncated inside the data, and with only part of the last chunk header left
+        p = tmp_path / f"bad{cut}.png"
+        p.write_bytes(good[:-cut] if cut == 30 else good[:-12] + good[-12:-12 + 8 + cut])
+        r = subprocess.run([program, "png", str(p)], capture_output=True, text=True)
+        assert r.returncode in (0, 1) and ("error" in r.stdout or r.stdout.startswith("size")), r.stdout
+    # image data that inflates past the image's size is refused
+    big = bytearray(_png([bytes(12)] * 3, 2))
+    z = zlib.compress(bytes(100000))
+    idat = struct.pack(">I", len(z)) + b"IDAT" + z + struct.pack(">I", zlib.crc32(b"IDAT" + z) & 0xffffffff)
+    at = big.index(b"IDAT") - 4
+    p = tmp_path / "bomb.png"
+    p.write_bytes(bytes(big[:at]) + idat + b"\0\0\0\0IEND\xaeB`\x82")
     r = subprocess.run([program, "png", str(p)], capture_output=True, text=True)
-    assert r.returncode == 1
+    assert r.returncode == 1 and "longer than the image" in r.stdout, r.stdout
 
 
 def _lerp8(img, u, v):

@@ -89,7 +89,8 @@ struct Huffman {
   }
 };
 
-std::vector<uint8_t> inflate_zlib(const uint8_t* data, size_t n) {
+// Inflates a zlib stream of at most `limit` output bytes.
+std::vector<uint8_t> inflate_zlib(const uint8_t* data, size_t n, size_t limit) {
   if (n < 2 || (data[0] & 0x0f) != 8 || ((data[0] << 8) | data[1]) % 31 != 0 || (data[1] & 0x20))
     throw TracerError(TR_ERR_ARG, "bad zlib header");
   // RFC 1951 section 3.2.5: base values and extra bits of lengths 257..285 and distances 0..29
@@ -114,6 +115,7 @@ std::vector<uint8_t> inflate_zlib(const uint8_t* data, size_t n) {
       const uint32_t len = br.p[br.pos] | (br.p[br.pos + 1] << 8), nlen = br.p[br.pos + 2] | (br.p[br.pos + 3] << 8);
       br.pos += 4;
       if ((len ^ 0xffffu) != nlen || br.n - br.pos < len) throw TracerError(TR_ERR_ARG, "bad stored block");
+      if (out.size() + len > limit) throw TracerError(TR_ERR_ARG, "deflate stream longer than the image");
       out.insert(out.end(), br.p + br.pos, br.p + br.pos + len);
       br.pos += len;
       continue;
@@ -158,6 +160,7 @@ std::vector<uint8_t> inflate_zlib(const uint8_t* data, size_t n) {
     }
     for (;;) {
       const int sym = lit.decode(br);
+      if (out.size() >= limit && sym != 256) throw TracerError(TR_ERR_ARG, "deflate stream longer than the image");
       if (sym < 256) {
         out.push_back((uint8_t)sym);
       } else if (sym == 256) {
@@ -170,6 +173,7 @@ std::vector<uint8_t> inflate_zlib(const uint8_t* data, size_t n) {
         if (di >= 30) throw TracerError(TR_ERR_ARG, "bad distance symbol");
         const size_t d = (size_t)kDistBase[di] + br.bits(kDistExtra[di]);
         if (d > out.size()) throw TracerError(TR_ERR_ARG, "distance beyond the output");
+        if (out.size() + len > limit) throw TracerError(TR_ERR_ARG, "deflate stream longer than the image");
         for (int k = 0; k < len; ++k) out.push_back(out[out.size() - d]);
       }
     }
@@ -194,7 +198,7 @@ std::vector<uint8_t> decode_png(const std::vector<uint8_t>& f, int& w, int& h, i
   while (pos + 8 <= f.size()) {
     const uint32_t len = be32(&f[pos]);
     const std::string type(reinterpret_cast<const char*>(&f[pos + 4]), 4);
-    if (f.size() - pos - 12 < len) throw TracerError(TR_ERR_ARG, "truncated PNG chunk");
+    if (f.size() - pos < 12 || f.size() - pos - 12 < len) throw TracerError(TR_ERR_ARG, "truncated PNG chunk");
     const uint8_t* d = &f[pos + 8];
     if (type == "IHDR") {
       if (len < 13) throw TracerError(TR_ERR_ARG, "bad IHDR");
@@ -212,14 +216,15 @@ std::vector<uint8_t> decode_png(const std::vector<uint8_t>& f, int& w, int& h, i
     }
     pos += 12 + len;
   }
-  if (w <= 0 || h <= 0 || w > (1 << 16) || h > (1 << 16)) throw TracerError(TR_ERR_ARG, "bad PNG size");
+  if (w <= 0 || h <= 0 || w > (1 << 16) || h > (1 << 16) || (size_t)w * h > (size_t(1) << 28))
+    throw TracerError(TR_ERR_ARG, "bad PNG size");
   if (depth != 8) throw TracerError(TR_ERR_UNSUPPORTED, "PNG bit depth other than 8");
   if (interlace) throw TracerError(TR_ERR_UNSUPPORTED, "interlaced PNG");
   const int ch = ctype == 0 ? 1 : ctype == 2 ? 3 : ctype == 3 ? 1 : ctype == 4 ? 2 : ctype == 6 ? 4 : 0;
   if (!ch) throw TracerError(TR_ERR_ARG, "bad PNG colour type");
   if (ctype == 3 && plte.size() < 3) throw TracerError(TR_ERR_ARG, "palette PNG without PLTE");
-  const std::vector<uint8_t> raw = inflate_zlib(idat.data(), idat.size());
   const size_t stride = (size_t)w * ch;
+  const std::vector<uint8_t> raw = inflate_zlib(idat.data(), idat.size(), (stride + 1) * h);
   if (raw.size() < (stride + 1) * h) throw TracerError(TR_ERR_ARG, "short PNG image data");
   std::vector<uint8_t> px(stride * h);
   for (int y = 0; y < h; ++y) {
@@ -345,7 +350,8 @@ RC<Image2D<Color3f>> load_hdr_from_file(const std::string& filename) {
     const std::string res = line();
     char ya[3] = {0}, xa[3] = {0};
     if (std::sscanf(res.c_str(), "%2s %d %2s %d", ya, &h, xa, &w) != 4 || std::strcmp(ya, "-Y") != 0 ||
-        std::strcmp(xa, "+X") != 0 || w <= 0 || h <= 0 || w > (1 << 16) || h > (1 << 16))
+        std::strcmp(xa, "+X") != 0 || w <= 0 || h <= 0 || w > (1 << 16) || h > (1 << 16) ||
+        (size_t)w * h > (size_t(1) << 28))
       throw TracerError(TR_ERR_UNSUPPORTED, "HDR resolution line '" + res + "' (only -Y h +X w): " + filename);
   }
   auto img = std::make_shared<Image2D<Color3f>>(w, h);
