@@ -58,6 +58,28 @@ def test_guided_estimator_keeps_the_plain_expectation(gpu):
     assert rel.max() < 0.08
 
 
+def test_guided_estimator_keeps_the_plain_expectation_under_an_environment_light(gpu):
+    """The same with the sky map and an area light: the environment light's
+    sample, the continuation and the mixture ray leaving the scene are MIS
+    strategies of its direct lighting (weighted with the density the light
+    sample is drawn with, the plain sampler's share with the reference's own
+    IBL::pdf), so the guided image keeps the plain image's expectation."""
+    sc, cam, filt, _ = scenes.outdoor(32, 32, 1, glass=False)
+    gpu.upload(sc)
+    gpu.guide_init(seed=5)
+    par = scenes.make_params(32, 32, 1024, 3, 6, seed_base=1)
+    plain, _ = gpu.render(cam, filt, par, fp64=True)
+    par_g = scenes.make_params(32, 32, 1024, 3, 6, seed_base=7_000_000)
+    guided, st = _film(gpu, cam, filt, par_g, make_guide(0.5, (-6, -1, -6), (6, 4, 6)))
+    assert st.samples == 32 * 32 * 1024
+    a = _image(plain).reshape(4, 8, 4, 8, 3).mean((1, 3))
+    b = _image(guided).reshape(4, 8, 4, 8, 3).mean((1, 3))
+    rel = np.abs(a - b) / np.maximum(a, 1e-3)
+    print(f"block means: max rel diff {rel.max():.4f}, image mean plain {a.mean():.5f} guided {b.mean():.5f}")
+    assert abs(a.mean() - b.mean()) <= 0.01 * a.mean()
+    assert rel.max() < 0.08
+
+
 def test_training_on_render_records(gpu):
     sc, cam, filt, par = scenes.occluded_room(64, 48, 8, n_tris=20000)
     gpu.upload(sc)

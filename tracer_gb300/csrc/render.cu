@@ -441,9 +441,11 @@ __device__ __forceinline__ float mis_w(float a, float b) { return a > 0.0f ? pow
 // eval and pdf, sample_bsdf with the sampler's own integrand and density,
 // src/renderer/direct_illumination.cpp:35-71,144-198). fe, pb: eval and pdf
 // at w; fs, ps: the plain sampler's integrand and density at w; lpdf: the
-// light's solid-angle density at w.
-__device__ __forceinline__ f3 direct_integrand(f3 fe, float pb, f3 fs, float ps, float lpdf) {
-  return muls(fe, mis_w(lpdf, pb)) + muls(fs, mis_w(ps, lpdf));
+// light's solid-angle density at w; lq: the light density the reference's
+// sample_bsdf weighs against (lpdf for area lights, IBL::pdf for the
+// environment light, :156-174).
+__device__ __forceinline__ f3 direct_integrand(f3 fe, float pb, f3 fs, float ps, float lpdf, float lq) {
+  return muls(fe, mis_w(lpdf, pb)) + muls(fs, mis_w(ps, lq));
 }
 
 // Emission reached by a ray of a guided vertex that is one of its MIS
@@ -456,17 +458,30 @@ __device__ __forceinline__ f3 direct_integrand(f3 fe, float pb, f3 fs, float ps,
 __device__ f3 guided_strategy_emission(const Launch& P, int slot, float4 hit, f3 o, f3 d, float pr, float po, f3 fe,
                                        float pb, float ps, float nc, float cosv) {
   const int pid = __float_as_int(hit.x);
-  if (pid < 0) return mk3(0.0f, 0.0f, 0.0f);
-  const DPrim& pr_ = P.sc.prims[pid];
-  if (!pr_.emissive) return mk3(0.0f, 0.0f, 0.0f);
-  const f3 gz = P.sc.tshade[pr_.shape].gz;
-  if (!(dot(gz, -d) > 0.0f)) return mk3(0.0f, 0.0f, 0.0f);
-  const float lpdf = light_pdf_at(pr_.area, o, o + scale(d, hit.y), gz);
+  f3 Le;
+  float lpdf, lq;
+  if (pid < 0) {  // left the scene: the environment light, if any
+    const int ei = job_of(P, slot).env;
+    if (ei < 0) return mk3(0.0f, 0.0f, 0.0f);
+    const DEnv& e = P.sc.envs[ei];
+    Le = env_emit(e, d);
+    if (black(Le)) return mk3(0.0f, 0.0f, 0.0f);
+    lpdf = env_sample_density(e, d);
+    lq = env_pdf(e, d);
+  } else {
+    const DPrim& pr_ = P.sc.prims[pid];
+    if (!pr_.emissive) return mk3(0.0f, 0.0f, 0.0f);
+    const f3 gz = P.sc.tshade[pr_.shape].gz;
+    if (!(dot(gz, -d) > 0.0f)) return mk3(0.0f, 0.0f, 0.0f);
+    Le = pr_.emission;
+    lpdf = light_pdf_at(pr_.area, o, o + scale(d, hit.y), gz);
+    lq = lpdf;
+  }
   const int mat = __float_as_int(P.SC[7 * (size_t)slot].w);
   const f3 fs = ps > 0.0f ? muls(P.sc.mats[mat].diffuse_coef, nc) : mk3(0.0f, 0.0f, 0.0f);
-  const f3 g = direct_integrand(fe, pb, fs, ps, lpdf);
+  const f3 g = direct_integrand(fe, pb, fs, ps, lpdf, lq);
   const float w = pr * pr / (pr * pr + lpdf * lpdf + po * po);
-  return muls(mulc(pr_.emission, g), cosv * w / pr);
+  return muls(mulc(Le, g), cosv * w / pr);
 }
 
 // The strategy in the MIS slot (M0-M2, normal correction and |cos| in the
@@ -492,7 +507,11 @@ __device__ f3 guided_continuation_emission(const Launch& P, int slot) {
 // part of the radiance that arrived along it, and so of the training target.
 __device__ __forceinline__ f3 continuation_emission(const Launch& P, int slot, float4 hit) {
   const int pid = __float_as_int(hit.x);
-  if (pid < 0) return mk3(0.0f, 0.0f, 0.0f);
+  if (pid < 0) {
+    const int ei = job_of(P, slot).env;
+    const float4 p1 = P.P1[slot];
+    return ei < 0 ? mk3(0.0f, 0.0f, 0.0f) : env_emit(P.sc.envs[ei], mk3(p1.x, p1.y, p1.z));
+  }
   const DPrim& pr = P.sc.prims[pid];
   if (!pr.emissive) return mk3(0.0f, 0.0f, 0.0f);
   const float4 p1 = P.P1[slot];
@@ -672,11 +691,11 @@ __device__ __noinline__ void guided_mixture_ray(const Launch& P, const Bsdf& bsd
 // same direct-lighting integral as the reference's pair of strategies.
 // Returns that integrand times |cos| per unit emission, times the weight.
 __device__ __noinline__ f3 guided_nee_factor(const Launch& P, const Bsdf& bsdf, f3 wo, f3 wl, int row, bool three,
-                                             float lpdf) {
+                                             float lpdf, float lq) {
   const Mixture mx{P.gout + (size_t)row * kMixFloats};
   const float ps = lambert_plain_pdf(bsdf, wo, wl);
   const f3 fs = ps > 0.0f ? muls(bsdf.m->diffuse_coef, normal_correct(bsdf.g, bsdf.s, wl)) : mk3(0.0f, 0.0f, 0.0f);
-  const f3 g = direct_integrand(bsdf.phong_eval_agg(wl, wo), bsdf.phong_pdf_agg(wl, wo), fs, ps, lpdf);
+  const f3 g = direct_integrand(bsdf.phong_eval_agg(wl, wo), bsdf.phong_pdf_agg(wl, wo), fs, ps, lpdf, lq);
   const float pm = mx.pdf(wl);
   const float pg = P.guide_alpha * pm + (1.0f - P.guide_alpha) * ps;
   const float po = three ? pm : 0.0f;
@@ -984,13 +1003,26 @@ __global__ void __launch_bounds__(128) k_nee(Launch P) {
         const float dist = dist_minus_eps(len2f(to_light), too_close);
         if (!too_close) {
           to_light = normalize(to_light);
-          const f3 bf = MatOps<KIND>::eval(bsdf, to_light, wo);
-          if (!black(bf)) {
-            const float bpdf = MatOps<KIND>::pdf(bsdf, to_light, wo);
-            const f3 fl = muls(mulc(Le, bf), abs_cos(to_light, bsdf.g.z));
-            const float w = power_heuristic(lpdf, bpdf);
-            const float4 p4 = P.P4[slot];
-            const f3 cc = mulc(mk3(p4.x, p4.y, p4.z), divs(muls(fl, w), lpdf));
+          const int gcode = __float_as_int(g.y);  // guided vertex: network row (bit 30: three strategies), else -1
+          const float4 p4 = P.P4[slot];
+          f3 cc = mk3(0.0f, 0.0f, 0.0f);
+          bool trace = false;
+          if (KIND == MAT_PHONG && gcode >= 0) {
+            const f3 fw = guided_nee_factor(P, bsdf, wo, to_light, gcode & 0x3fffffff, (gcode >> 30) & 1, lpdf,
+                                            env_pdf(P.sc.envs[lt.env], normalize(to_light)));
+            trace = !black(fw);
+            cc = mulc(mk3(p4.x, p4.y, p4.z), divs(mulc(Le, fw), lpdf));
+          } else {
+            const f3 bf = MatOps<KIND>::eval(bsdf, to_light, wo);
+            trace = !black(bf);
+            if (trace) {
+              const float bpdf = MatOps<KIND>::pdf(bsdf, to_light, wo);
+              const f3 fl = muls(mulc(Le, bf), abs_cos(to_light, bsdf.g.z));
+              const float w = power_heuristic(lpdf, bpdf);
+              cc = mulc(mk3(p4.x, p4.y, p4.z), divs(muls(fl, w), lpdf));
+            }
+          }
+          if (trace) {
             const f3 sd = normalize(to_light);
             rec[0] = make_float4(pos.x, pos.y, pos.z, dist);
             rec[1] = make_float4(sd.x, sd.y, sd.z, 0.0f);
@@ -1023,7 +1055,7 @@ __global__ void __launch_bounds__(128) k_nee(Launch P) {
           bool trace = false;
           const float4 p4 = P.P4[slot];
           if (KIND == MAT_PHONG && grow >= 0) {
-            const f3 fw = guided_nee_factor(P, bsdf, wo, to_light, grow, (gcode >> 30) & 1, lpdf);
+            const f3 fw = guided_nee_factor(P, bsdf, wo, to_light, grow, (gcode >> 30) & 1, lpdf, lpdf);
             trace = !black(fw);
             cc = mulc(mk3(p4.x, p4.y, p4.z), divs(mulc(lt.emission, fw), lpdf));
           } else {
@@ -1234,8 +1266,6 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     if (!(gp->alpha >= 0.0f && gp->alpha < 1.0f)) return set_err(ctx, TR_ERR_ARG, "guide alpha must be in [0, 1)");
     if (gp->alpha > 0.0f && (!ctx->guide || !ctx->guide->params.p))
       return set_err(ctx, TR_ERR_STATE, "guide model not initialised");
-    if (gp->alpha > 0.0f && ctx->dsc.has_env)
-      return set_err(ctx, TR_ERR_UNSUPPORTED, "guided sampling covers area lights only, not an environment light");
     for (int k = 0; k < 3; ++k) {
       if (!(gp->box_hi[k] > gp->box_lo[k])) return set_err(ctx, TR_ERR_ARG, "empty guide box");
       P.gbox_lo[k] = gp->box_lo[k];

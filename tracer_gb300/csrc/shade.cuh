@@ -988,6 +988,22 @@ __device__ __forceinline__ bool env_sample(const DEnv& e, f3 ref, float u, float
   return true;
 }
 
+// The density env_sample draws direction d with, per solid angle:
+// func(u, v) / marginal integral / (2 pi^2 sin theta). (IBL::pdf below is
+// the reference's weight, which multiplies by the integral instead; the
+// guided estimator's MIS weights need the density itself.)
+__device__ __forceinline__ float env_sample_density(const DEnv& e, f3 d) {
+  const f3 wi = normalize(rot3(e.to_light, d));
+  const float theta = acosf(clamp_pm1(wi.z));
+  const float sin_theta = sinf(theta);
+  if (!(sin_theta > 0.0f) || !(e.marg_int > 0.0f)) return 0.0f;
+  const float phi = local_phi(wi);
+  int iu = (int)(phi * kInv2Pi * (float)e.nu), iv = (int)(theta * kInvPi * (float)e.nv);
+  iu = iu < 0 ? 0 : (iu > e.nu - 1 ? e.nu - 1 : iu);
+  iv = iv < 0 ? 0 : (iv > e.nv - 1 ? e.nv - 1 : iv);
+  return e.cond_func[(size_t)iv * e.nu + iu] / e.marg_int / (2.0f * kPi * kPi * sin_theta);
+}
+
 // IBL::pdf (src/light/environment_light.cpp:184-191) with Distribution2D::pdf
 // (src/utility/distribution.hpp:103-107), which multiplies the conditional's
 // function by the marginal integral.
