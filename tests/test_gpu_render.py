@@ -109,6 +109,25 @@ def test_outdoor_environment_light(gpu, glass, area_light, env_8bit):
     assert abs(a.mean() - b.mean()) <= 0.01 * b.mean()
 
 
+@pytest.mark.parametrize("case", ["sky", "black", "1x1", "black_with_geometry"])
+def test_environment_light_edge_cases(gpu, case):
+    """No geometry, an all-black map and a 1 x 1 map on the device."""
+    if case == "black_with_geometry":
+        sc, cam, filt, par = scenes.outdoor(24, 16, 2)
+        sc.env_texels = np.zeros((8, 16, 3), np.float32)
+    else:
+        tex = {"sky": scenes.sky_map(16, 8), "black": np.zeros((8, 16, 3), np.float32),
+               "1x1": np.full((1, 1, 3), 2.0, np.float32)}[case]
+        sc, cam, filt, par = scenes.env_only(tex)
+    orc = oracle.Oracle(sc, "port")
+    orc.set_camera(cam, filt)
+    ref = orc.render(par)
+    gpu.upload(sc)
+    out, stats = gpu.render(cam, filt, par)
+    assert stats.samples == par.width * par.height * par.spp
+    _compare(out, ref, 0.99)
+
+
 @pytest.mark.parametrize("env,min_depth", [(True, 3), (False, 8)])
 def test_disney15_row(gpu, env, min_depth):
     """The 2015 Disney BSDF (create_disney): rough transmission, inner

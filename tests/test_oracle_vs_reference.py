@@ -102,6 +102,23 @@ def test_environment_light(area_light, env_size, min_depth):
     assert np.array_equal(bits(port.render(par)), bits(ref.render(par)))
 
 
+@pytest.mark.parametrize("case", ["sky", "black", "1x1", "black_with_geometry"])
+def test_environment_light_edge_cases(case):
+    """No geometry (every ray leaves at once), an all-black map (a uniform
+    distribution whose samples are all empty) and a 1 x 1 map."""
+    if case == "black_with_geometry":
+        sc, cam, filt, par = scenes.outdoor(24, 16, 2)
+        sc.env_texels = np.zeros((8, 16, 3), np.float32)
+    else:
+        tex = {"sky": scenes.sky_map(16, 8), "black": np.zeros((8, 16, 3), np.float32),
+               "1x1": np.full((1, 1, 3), 2.0, np.float32)}[case]
+        sc, cam, filt, par = scenes.env_only(tex)
+    port, ref = oracle.Oracle(sc, "port"), oracle.Oracle(sc, "reference")
+    port.set_camera(cam, filt)
+    ref.set_camera(cam, filt)
+    assert np.array_equal(bits(port.render(par)), bits(ref.render(par)))
+
+
 @pytest.mark.parametrize("min_depth", [3, 1])
 def test_environment_light_8bit(min_depth):
     """An environment light over an 8-bit map (ImageTexture2D): its byte

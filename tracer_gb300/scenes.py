@@ -321,6 +321,21 @@ def outdoor(width=96, height=64, spp=8, max_depth=6, min_depth=3, env_size=(64, 
     return scene, cam, make_filter(0.5, 0.6), make_params(width, height, spp, min_depth, max_depth)
 
 
+def env_only(texels, width=16, height=16, spp=2):
+    """No geometry at all, only an environment light over `texels` (H, W, 3):
+    every camera ray leaves the scene at once."""
+    sb = SceneBuffers(positions=np.zeros((0, 3), np.float32), normals=np.zeros((0, 3), np.float32),
+                      uvs=np.zeros((0, 2), np.float32), indices=np.zeros((0, 3), np.int32),
+                      sphere_radius=np.zeros(0, np.float32), sphere_to_world=np.zeros((0, 16), np.float32),
+                      sphere_to_local=np.zeros((0, 16), np.float32), materials=[lambert((0.5, 0.5, 0.5))],
+                      prim_shape=np.zeros(0, np.int32), prim_material=np.zeros(0, np.int32),
+                      prim_emission=np.zeros((0, 3), np.float32), light_prims=np.zeros(0, np.int32))
+    sb.env_texels = np.asarray(texels, np.float32)
+    sb.env_to_light, sb.env_to_world = rotate_x(math.pi / 2)
+    cam = make_camera(width / height, (0, 1, 5), (0, 0, 0), (0, 1, 0), math.radians(60.0), 0.0, 1.0)
+    return sb, cam, make_filter(0.5, 0.6), make_params(width, height, spp, 3, 5)
+
+
 def disney15_row(width=96, height=48, spp=8, max_depth=6, min_depth=3, env=True):
     """Five spheres of the 2015 Disney BSDF (create_disney) on a ground quad
     under a small area light and (by default) the sky map: a rough
