@@ -59,6 +59,18 @@ typedef struct tr_bvh_node32 {
 
 enum { TR_MAT_PHONG = 0, TR_MAT_DISNEY12 = 1, TR_MAT_GLASS = 2, TR_MAT_METAL = 3, TR_MAT_DISNEY15 = 4 };
 
+/* An image texture: create_hdr_texture2d (float texels) or
+ * create_image_texture2d (8-bit texels) (src/texture/hdr_texture.cpp,
+ * src/texture/image_texture2d.cpp), looked up at the hit's uv with the
+ * repeat wrap and the reference's bilinear arithmetic. Exactly one of
+ * texels and texels8 is non-NULL; texel (x, y) at 3 * (x + y * width),
+ * row y at v = y / (height - 1). */
+typedef struct tr_texture {
+  uint32_t width, height;
+  const float* texels;
+  const uint8_t* texels8;
+} tr_texture;
+
 /* Material record. Phong is create_phong_material(ka, kd, ks, ns)
  * (src/factory/material.hpp:19-24, src/material/phong.cpp:29-70); Disney12 is
  * create_disney_brdf (src/material/disney_brdf.cpp:278-344). Constant textures
@@ -90,6 +102,10 @@ typedef struct tr_material {
    * base_color, metallic, roughness, specular_tint, anisotropic, sheen,
    * sheen_tint, clearcoat, clearcoat_gloss and ior. */
   float transmission, transmission_roughness, specular_scale[3];
+  /* Phong maps: 0 = the constant ka, kd, ks, ns above; k = the scene's
+   * textures[k - 1], evaluated at the hit's uv (ns takes its red channel,
+   * Texture2D::evaluate_s). */
+  uint32_t tex_ka, tex_kd, tex_ks, tex_ns;
 } tr_material;
 
 /* Flat scene description. It records what the reference factory calls build
@@ -133,6 +149,9 @@ typedef struct tr_scene_desc {
    * layout, looked up with the reference's byte arithmetic and divided by
    * 255. Used when env_texels is NULL and this is not. */
   const uint8_t* env_texels8;
+  /* image textures referenced by the materials' tex_* fields */
+  uint32_t num_textures;
+  const tr_texture* textures;
 } tr_scene_desc;
 
 /* create_thin_lens_camera arguments (src/camera/thin_lens_camera.cpp:23-36). */

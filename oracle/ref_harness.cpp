@@ -99,10 +99,34 @@ void* ref_scene_create(const tr_scene_desc* d) {
   mi.inside = vacuum;
   mi.outside = vacuum;
 
+  // image textures of the materials (create_hdr_texture2d / create_image_texture2d)
+  std::vector<RC<Texture2D>> textures;
+  for (uint32_t k = 0; k < d->num_textures; ++k) {
+    const tr_texture& t = d->textures[k];
+    if (t.texels) {
+      auto img = newRC<Image2D<Color3f>>((int)t.width, (int)t.height);
+      for (uint32_t y = 0; y < t.height; ++y)
+        for (uint32_t x = 0; x < t.width; ++x) {
+          const float* p = t.texels + 3 * ((size_t)x + (size_t)y * t.width);
+          img->at((int)x, (int)y) = Color3f(p[0], p[1], p[2]);
+        }
+      textures.push_back(create_hdr_texture2d(img));
+    } else {
+      auto img = newRC<Image2D<Color3b>>((int)t.width, (int)t.height);
+      for (uint32_t y = 0; y < t.height; ++y)
+        for (uint32_t x = 0; x < t.width; ++x) {
+          const uint8_t* p = t.texels8 + 3 * ((size_t)x + (size_t)y * t.width);
+          img->at((int)x, (int)y) = Color3b(p[0], p[1], p[2]);
+        }
+      textures.push_back(create_image_texture2d(img));
+    }
+  }
+  auto map = [&](uint32_t k, RC<Texture2D> constant) { return k ? textures[k - 1] : constant; };
   for (uint32_t i = 0; i < d->num_materials; ++i) {
     const tr_material& m = d->materials[i];
     if (m.kind == TR_MAT_PHONG) {
-      s->materials.push_back(create_phong_material(ctex3(m.ka), ctex3(m.kd), ctex3(m.ks), ctex(m.ns)));
+      s->materials.push_back(create_phong_material(map(m.tex_ka, ctex3(m.ka)), map(m.tex_kd, ctex3(m.kd)),
+                                                   map(m.tex_ks, ctex3(m.ks)), map(m.tex_ns, ctex(m.ns))));
     } else if (m.kind == TR_MAT_GLASS) {
       s->materials.push_back(create_glass(ctex3(m.kr), ctex3(m.kt), ctex(m.ior)));
     } else if (m.kind == TR_MAT_DISNEY15) {

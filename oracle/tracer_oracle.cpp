@@ -257,6 +257,10 @@ struct Mat {
   // alphas, clearcoat roughness and the four sampling weights
   Sp c_tint, spec_scale;
   real transmission, ior15, ax15, ay15, trans_ax, trans_ay, cc_rough, w_diff, w_trans, w_spec, w_cc;
+  // Phong maps (0: the constants; k: the scene's textures[k - 1]) and the constants
+  int tex_ka = 0, tex_kd = 0, tex_ks = 0, tex_ns = 0;
+  Sp kd_c, ks_c;
+  real ns_c = 1;
 };
 struct Prim {
   int kind;  // 0 triangle, 1 sphere
@@ -386,14 +390,11 @@ struct Dist2D {
 };
 // IBL over an HDRTexture2D (light/environment_light.cpp:14-193,
 // texture/hdr_texture.cpp:9-37, core/texture.hpp:57-95)
-struct Env {
+// HDRTexture2D / ImageTexture2D behind Texture2D::evaluate
+struct Tex {
   int w = 0, h = 0;
   std::vector<real> tex;      // 3 per texel, texel (x, y) at 3 * (x + y * w)
   std::vector<uint8_t> tex8;  // an 8-bit map (ImageTexture2D) instead, same layout
-  real to_light[16], to_world[16];
-  Dist2D dist;
-  V3 center;
-  real radius = 1;
   Sp texel(int x, int y) const {
     const real* t = &tex[3 * ((size_t)x + (size_t)y * w)];
     return Sp(t[0], t[1], t[2]);
@@ -428,6 +429,12 @@ struct Env {
     return scaled(scaled(texel(u0, v0), 1.0 - du) + scaled(texel(u1, v0), du), 1.0 - dv) +
            scaled(scaled(texel(u0, v1), 1.0 - du) + scaled(texel(u1, v1), du), dv);
   }
+};
+struct Env : Tex {
+  real to_light[16], to_world[16];
+  Dist2D dist;
+  V3 center;
+  real radius = 1;
   // the IBL constructor's sampling density: luminance times solid angle per
   // cell of a grid of at most 360 x 180 (environment_light.cpp:39-81)
   void build_distribution() {
@@ -485,6 +492,7 @@ struct Scene {
   std::vector<Prim> prims;
   std::vector<int> lights;       // primitive ids in scene.lights order
   std::unique_ptr<Env> env;      // environment light (after the area lights in scene.lights)
+  std::vector<Tex> textures;     // image textures of the materials
   std::vector<Node> nodes;
   std::vector<int> order;        // leaf slot -> primitive id
   int max_leaf = 1;
@@ -1669,6 +1677,37 @@ LightSample env_sample_li(const Env& env, V3 ref, real u, real v) {
   return out;
 }
 
+// Phong::shading's set-up (material/phong.cpp:29-70) from kd, ks and ns.
+inline void phong_setup(Mat& m, Sp diffuse, Sp spec, real ns) {
+  real dem = 1;
+  dem = std::max(dem, diffuse.r + spec.r);
+  dem = std::max(dem, diffuse.g + spec.g);
+  dem = std::max(dem, diffuse.b + spec.b);
+  diffuse = diffuse / dem;
+  spec = spec / dem;
+  real dl = diffuse.lum(), sl = spec.lum();
+  real wd = (dl + sl > kEps) ? dl / (dl + sl) : real(0.5);
+  m.w_diffuse = wd;
+  m.w_specular = 1 - wd;
+  m.albedo = diffuse + spec;
+  m.diffuse_coef = diffuse / kPi;
+  m.specular = spec;
+  m.ns = ns;
+  m.base = diffuse;
+}
+// The material at a hit: a Phong material with maps evaluates them at the
+// hit's uv (Texture2D::evaluate, evaluate_s) and sets up again.
+inline const Mat& material_at(const Scene& sc, int mi, const Isect& is, Mat& scratch) {
+  const Mat& m = sc.mats[mi];
+  if (m.kind != TR_MAT_PHONG || !(m.tex_kd | m.tex_ks | m.tex_ns)) return m;
+  scratch = m;
+  const Sp kd = m.tex_kd ? sc.textures[m.tex_kd - 1].eval(is.uv[0], is.uv[1]) : m.kd_c;
+  const Sp ks = m.tex_ks ? sc.textures[m.tex_ks - 1].eval(is.uv[0], is.uv[1]) : m.ks_c;
+  const real ns = m.tex_ns ? sc.textures[m.tex_ns - 1].eval(is.uv[0], is.uv[1]).r : m.ns_c;
+  phong_setup(scratch, kd, ks, ns);
+  return scratch;
+}
+
 // ---------------------------------------------------------- ray recording
 struct RayLog {
   std::vector<tr_ray> closest, any;
@@ -1797,7 +1836,8 @@ Sp eval_li(Tracer& tr, Ray ray, Sampler& smp, int min_depth, int max_depth) {
     if ((depth == 0 || specular) && found && sc.prims[is.prim].light) L += coef * light_emit(sc, is.prim, is, -ray.d);
     if ((depth == 0 || specular) && !found && sc.env) L += coef * sc.env->emit(ray.d);
     if (!found) break;
-    BSDF bsdf{&sc.mats[sc.prims[is.prim].material], is.g, is.s};
+    Mat hit_mat;
+    BSDF bsdf{&material_at(sc, sc.prims[is.prim].material, is, hit_mat), is.g, is.s};
     const real u = smp.u(), v = smp.u(), w = smp.u();
     BSDFSample bs = bsdf.sample(is.wo, u, v, w);
     if (bs.f.black() || bs.pdf < kEps) break;
@@ -1953,22 +1993,14 @@ void* orc_scene_create(const tr_scene_desc* d) {
     Mat& m = sc->mats[i];
     m.kind = src.kind;
     if (src.kind == TR_MAT_PHONG) {
-      Sp diffuse(src.kd[0], src.kd[1], src.kd[2]), spec(src.ks[0], src.ks[1], src.ks[2]);
-      real dem = 1;
-      dem = std::max(dem, diffuse.r + spec.r);
-      dem = std::max(dem, diffuse.g + spec.g);
-      dem = std::max(dem, diffuse.b + spec.b);
-      diffuse = diffuse / dem;
-      spec = spec / dem;
-      real dl = diffuse.lum(), sl = spec.lum();
-      real wd = (dl + sl > kEps) ? dl / (dl + sl) : real(0.5);
-      m.w_diffuse = wd;
-      m.w_specular = 1 - wd;
-      m.albedo = diffuse + spec;
-      m.diffuse_coef = diffuse / kPi;
-      m.specular = spec;
-      m.ns = src.ns;
-      m.base = diffuse;
+      m.kd_c = Sp(src.kd[0], src.kd[1], src.kd[2]);
+      m.ks_c = Sp(src.ks[0], src.ks[1], src.ks[2]);
+      m.ns_c = src.ns;
+      m.tex_ka = (int)src.tex_ka;
+      m.tex_kd = (int)src.tex_kd;
+      m.tex_ks = (int)src.tex_ks;
+      m.tex_ns = (int)src.tex_ns;
+      phong_setup(m, m.kd_c, m.ks_c, m.ns_c);
     } else if (src.kind == TR_MAT_METAL) {
       m.base = Sp(src.color[0], src.color[1], src.color[2]);
       for (int c = 0; c < 3; ++c) {
@@ -2033,6 +2065,15 @@ void* orc_scene_create(const tr_scene_desc* d) {
     pr.light = !pr.emission.black();
   }
   for (uint32_t l = 0; l < d->num_lights; ++l) sc->lights.push_back(d->light_prims[l]);
+  for (uint32_t k = 0; k < d->num_textures; ++k) {
+    const tr_texture& t = d->textures[k];
+    Tex x;
+    x.w = (int)t.width;
+    x.h = (int)t.height;
+    if (t.texels) x.tex.assign(t.texels, t.texels + 3 * (size_t)x.w * x.h);
+    else x.tex8.assign(t.texels8, t.texels8 + 3 * (size_t)x.w * x.h);
+    sc->textures.push_back(std::move(x));
+  }
   build_bvh(*sc);
   if ((d->env_texels || d->env_texels8) && d->env_width > 0 && d->env_height > 0) {
     auto env = std::make_unique<Env>();

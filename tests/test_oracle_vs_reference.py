@@ -102,6 +102,21 @@ def test_environment_light(area_light, env_size, min_depth):
     assert np.array_equal(bits(port.render(par)), bits(ref.render(par)))
 
 
+@pytest.mark.parametrize("maker", ["cornell", "outdoor"])
+def test_phong_image_textures(maker):
+    """Phong materials with image maps (8-bit and float kd, float ks and ns)
+    looked up at the hit's uv: barycentric on triangles, (phi, theta) on a
+    sphere."""
+    if maker == "cornell":
+        sc, cam, filt, par = scenes.cornell(32, 32, 4, textured=True)
+    else:
+        sc, cam, filt, par = scenes.outdoor(32, 24, 4, textured=True, glass=False)
+    port, ref = oracle.Oracle(sc, "port"), oracle.Oracle(sc, "reference")
+    port.set_camera(cam, filt)
+    ref.set_camera(cam, filt)
+    assert np.array_equal(bits(port.render(par)), bits(ref.render(par)))
+
+
 @pytest.mark.parametrize("case", ["sky", "black", "1x1", "black_with_geometry"])
 def test_environment_light_edge_cases(case):
     """No geometry (every ray leaves at once), an all-black map (a uniform

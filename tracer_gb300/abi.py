@@ -60,7 +60,13 @@ class TrMaterial(C.Structure):
                 ("clearcoat_gloss", C.c_float), ("kr", C.c_float * 3), ("kt", C.c_float * 3), ("ior", C.c_float),
                 ("color", C.c_float * 3), ("eta", C.c_float * 3), ("k", C.c_float * 3),
                 ("transmission", C.c_float), ("transmission_roughness", C.c_float),
-                ("specular_scale", C.c_float * 3)]
+                ("specular_scale", C.c_float * 3),
+                ("tex_ka", C.c_uint32), ("tex_kd", C.c_uint32), ("tex_ks", C.c_uint32), ("tex_ns", C.c_uint32)]
+
+
+class TrTexture(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("texels", f32p),
+                ("texels8", C.POINTER(C.c_uint8))]
 
 
 class TrSceneDesc(C.Structure):
@@ -74,7 +80,8 @@ class TrSceneDesc(C.Structure):
                 ("num_lights", C.c_uint32), ("light_prims", i32p),
                 ("max_leaf_prims", C.c_int32),
                 ("env_width", C.c_uint32), ("env_height", C.c_uint32), ("env_texels", f32p),
-                ("env_to_light", f32p), ("env_to_world", f32p), ("env_texels8", C.POINTER(C.c_uint8))]
+                ("env_to_light", f32p), ("env_to_world", f32p), ("env_texels8", C.POINTER(C.c_uint8)),
+                ("num_textures", C.c_uint32), ("textures", C.POINTER(TrTexture))]
 
 
 class TrCamera(C.Structure):
@@ -160,6 +167,10 @@ class Material:
     transmission: float = 0.0
     transmission_roughness: float = 0.0
     specular_scale: tuple = (0.0, 0.0, 0.0)
+    tex_ka: int = 0  # Phong maps: 0 the constant, k the scene's textures[k - 1]
+    tex_kd: int = 0
+    tex_ks: int = 0
+    tex_ns: int = 0
 
     def to_c(self) -> TrMaterial:
         m = TrMaterial()
@@ -177,6 +188,7 @@ class Material:
         m.kt[:] = self.kt
         m.color[:] = self.color
         m.specular_scale[:] = self.specular_scale
+        m.tex_ka, m.tex_kd, m.tex_ks, m.tex_ns = self.tex_ka, self.tex_kd, self.tex_ks, self.tex_ns
         m.eta[:] = self.eta
         m.k[:] = self.k
         return m
@@ -200,6 +212,7 @@ class SceneBuffers:
     max_leaf_prims: int = 3
     env_texels: np.ndarray | None = None    # (H,W,3) f32 environment map, row y at v = y / (H - 1)
     env_texels8: np.ndarray | None = None   # (H,W,3) u8 map (ImageTexture2D) used instead when set
+    textures: list = field(default_factory=list)  # (H,W,3) f32 (HDR) or u8 (8-bit) images for tex_* fields
     env_to_light: np.ndarray | None = None  # (16,) f32 world_to_light; identity when None
     env_to_world: np.ndarray | None = None  # (16,) f32 its inverse
     _keep: list = field(default_factory=list, repr=False)
@@ -233,6 +246,22 @@ class SceneBuffers:
         d.num_lights = len(arrs["light_prims"])
         d.light_prims = ptr(arrs["light_prims"], C.c_int32)
         d.max_leaf_prims = int(self.max_leaf_prims)
+        if self.textures:
+            recs = (TrTexture * len(self.textures))()
+            for i, img in enumerate(self.textures):
+                eight = np.asarray(img).dtype == np.uint8
+                arr = np.ascontiguousarray(img, dtype=np.uint8 if eight else np.float32)
+                if arr.ndim != 3 or arr.shape[2] != 3:
+                    raise ValueError("textures must be (height, width, 3)")
+                self._keep.append(arr)
+                recs[i].height, recs[i].width = arr.shape[0], arr.shape[1]
+                if eight:
+                    recs[i].texels8 = arr.ctypes.data_as(C.POINTER(C.c_uint8))
+                else:
+                    recs[i].texels = ptr(arr, C.c_float)
+            self._keep.append(recs)
+            d.num_textures = len(self.textures)
+            d.textures = C.cast(recs, C.POINTER(TrTexture))
         if self.env_texels is not None or self.env_texels8 is not None:
             ldr = self.env_texels is None
             tex = np.ascontiguousarray(self.env_texels8 if ldr else self.env_texels,

@@ -208,21 +208,40 @@ def lambert(albedo) -> Material:
     return Material(kind=TR_MAT_PHONG, kd=tuple(albedo), ks=(0.0, 0.0, 0.0), ns=1.0)
 
 
-def cornell(width=256, height=256, spp=16, max_depth=5, min_depth=5, glass=False, metal=False):
+def checker(n=16, cells=4, c0=(0.8, 0.8, 0.8), c1=(0.1, 0.3, 0.7), eight_bit=True):
+    """An n x n checkerboard texture of `cells` x `cells` squares, 8-bit or float."""
+    y, x = np.mgrid[0:n, 0:n]
+    odd = ((x * cells // n + y * cells // n) % 2 == 1)[..., None]
+    img = np.where(odd, np.array(c1), np.array(c0))
+    return (img * 255.0).astype(np.uint8) if eight_bit else img.astype(np.float32)
+
+
+def cornell(width=256, height=256, spp=16, max_depth=5, min_depth=5, glass=False, metal=False, textured=False):
     """Cornell box [-1,1]^3 open at +z: 10 wall triangles, two boxes (12 each),
     a 0.5x0.5 ceiling light at y = 0.99 emitting (17,12,4): 36 triangles,
     2 lights. Pinhole camera at (0,0,3.5), 40 degree fov. min_depth >= max_depth
     disables Russian roulette. glass: the tall box is glass (kr = kt = 1,
     ior 1.5), which takes paths through the specular branch. metal: the short
-    box is a rough anisotropic metal (GGX with a painted conductor Fresnel)."""
+    box is a rough anisotropic metal (GGX with a painted conductor Fresnel).
+    textured: the floor's kd is an 8-bit checkerboard, the back wall's kd, ks
+    and ns float maps (Phong with image textures)."""
     b = _Builder()
     white = b.material(lambert((0.73, 0.73, 0.73)))
+    floor, back = white, white
+    textures = []
+    if textured:
+        textures = [checker(16, 4), checker(12, 3, (0.9, 0.2, 0.1), (0.2, 0.8, 0.3), eight_bit=False),
+                    np.full((4, 4, 3), 0.15, np.float32),
+                    np.linspace(5.0, 60.0, 8 * 8 * 3, dtype=np.float32).reshape(8, 8, 3)]
+        floor = b.material(Material(kind=TR_MAT_PHONG, kd=(0.73, 0.73, 0.73), ns=1.0, tex_kd=1))
+        back = b.material(Material(kind=TR_MAT_PHONG, kd=(0.5, 0.5, 0.5), ks=(0.1, 0.1, 0.1), ns=10.0,
+                                   tex_kd=2, tex_ks=3, tex_ns=4))
     tall = b.material(Material(kind=TR_MAT_GLASS, kr=(1.0, 1.0, 1.0), kt=(1.0, 1.0, 1.0), ior=1.5)) if glass else white
     red = b.material(lambert((0.65, 0.05, 0.05)))
     green = b.material(lambert((0.12, 0.45, 0.15)))
-    b.quad((-1, -1, -1), (1, -1, -1), (1, -1, 1), (-1, -1, 1), (0, 1, 0), white)    # floor
+    b.quad((-1, -1, -1), (1, -1, -1), (1, -1, 1), (-1, -1, 1), (0, 1, 0), floor)    # floor
     b.quad((-1, 1, -1), (1, 1, -1), (1, 1, 1), (-1, 1, 1), (0, -1, 0), white)       # ceiling
-    b.quad((-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1), (0, 0, 1), white)    # back
+    b.quad((-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1), (0, 0, 1), back)     # back
     b.quad((-1, -1, -1), (-1, 1, -1), (-1, 1, 1), (-1, -1, 1), (1, 0, 0), red)      # left
     b.quad((1, -1, -1), (1, 1, -1), (1, 1, 1), (1, -1, 1), (-1, 0, 0), green)       # right
     short = b.material(Material(kind=TR_MAT_METAL, color=(0.95, 0.64, 0.54), eta=(0.2, 0.92, 1.1), k=(3.9, 2.45, 2.14),
@@ -232,6 +251,7 @@ def cornell(width=256, height=256, spp=16, max_depth=5, min_depth=5, glass=False
     b.quad((-0.25, 0.99, -0.25), (0.25, 0.99, -0.25), (0.25, 0.99, 0.25), (-0.25, 0.99, 0.25), (0, -1, 0),
            white, emission=(17.0, 12.0, 4.0))
     scene = b.finish(max_leaf_prims=3)
+    scene.textures = textures
     cam = make_camera(width / height, (0, 0, 3.5), (0, 0, 0), (0, 1, 0), math.radians(40.0), 0.0, 1.0)
     return scene, cam, make_filter(0.5, 0.6), make_params(width, height, spp, min_depth, max_depth)
 
@@ -290,7 +310,7 @@ def rotate_x(theta):
 
 
 def outdoor(width=96, height=64, spp=8, max_depth=6, min_depth=3, env_size=(64, 32), area_light=True, glass=True,
-            env_8bit=False):
+            env_8bit=False, textured=False):
     """An open scene under an environment light: a ground quad, Disney12,
     metal, glass (Lambertian when `glass` is False) and Lambertian spheres,
     optionally one small area light; the
@@ -308,10 +328,12 @@ def outdoor(width=96, height=64, spp=8, max_depth=6, min_depth=3, env_size=(64, 
                                 k=(3.9, 2.45, 2.14), roughness=0.25, anisotropic=0.0)),
             b.material(Material(kind=TR_MAT_GLASS, kr=(1.0, 1.0, 1.0), kt=(1.0, 1.0, 1.0), ior=1.5) if glass
                        else lambert((0.7, 0.7, 0.7))),
-            b.material(lambert((0.2, 0.5, 0.3)))]
+            b.material(Material(kind=TR_MAT_PHONG, kd=(0.2, 0.5, 0.3), ns=1.0, tex_kd=1 if textured else 0))]
     for k, m in enumerate(mats):
         b.sphere((-2.25 + 1.5 * k, 0.6, 0.0), 0.6, m)
     scene = b.finish(max_leaf_prims=3)
+    if textured:  # the last sphere's kd: a checkerboard over its (phi, theta) uv
+        scene.textures = [checker(32, 8, (0.9, 0.9, 0.2), (0.1, 0.2, 0.6))]
     if env_8bit:  # the map as 8-bit values (an ImageTexture2D), the sun at full scale
         scene.env_texels8 = np.clip(sky_map(*env_size, sun_radiance=1.0) * 255.0, 0, 255).astype(np.uint8)
     else:
