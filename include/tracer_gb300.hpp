@@ -162,6 +162,8 @@ class Material {
  public:
   explicit Material(const tr_material& m) : rec(m) {}
   tr_material rec;
+  // Phong's image maps (ka, kd, ks, ns; null where the map is a constant)
+  RC<const Texture2D> maps[4];
 };
 RC<Material> create_phong_material(RC<const Texture2D> map_ka, RC<const Texture2D> map_kd,
                                    RC<const Texture2D> map_ks, RC<const Texture2D> map_ns);
@@ -255,7 +257,16 @@ struct SceneDesc {
   uint32_t env_width = 0, env_height = 0;  // environment map (0 x 0: none)
   std::vector<float> env_texels, env_to_light, env_to_world;
   std::vector<uint8_t> env_texels8;  // an 8-bit map instead of env_texels
+  struct TextureData {
+    uint32_t width = 0, height = 0;
+    std::vector<float> texels;     // 3 per texel (HDR)
+    std::vector<uint8_t> texels8;  // or 3 bytes per texel (8-bit)
+  };
+  std::vector<TextureData> textures;  // the materials' image maps (tr_material::tex_* - 1)
   tr_scene_desc view() const;
+
+ private:
+  mutable std::vector<tr_texture> texture_recs_;
 };
 
 class Scene {

@@ -87,6 +87,7 @@ int main(int argc, char** argv) {
   const bool glass_metal = argc > 6 && std::strstr(argv[6], "glass_metal") != nullptr;
   const bool sky = argc > 6 && std::strstr(argv[6], "sky") != nullptr;
   const bool d15 = argc > 6 && std::strstr(argv[6], "disney15") != nullptr;
+  const bool textured = argc > 6 && std::strstr(argv[6], "textured") != nullptr;
 
   // construction errors throw (src/shape/sphere.cpp:88-90)
   if (!throws([] { create_sphere(-1.0f, Transform()); }) ||
@@ -111,6 +112,12 @@ int main(int argc, char** argv) {
   auto d15_metal = create_disney(konst(0.9f, 0.7f, 0.4f), konst(0.9f, 0.9f, 0.9f), konst(0.3f, 0.3f, 0.3f), zero,
                                  zero, konst(1.5f, 1.5f, 1.5f), zero, konst(0.2f, 0.2f, 0.2f), konst(0.5f, 0.5f, 0.5f),
                                  zero, zero, konst(0.6f, 0.6f, 0.6f), konst(0.5f, 0.5f, 0.5f));
+  // an 8-bit checkerboard kd for the floor (create_image_texture2d)
+  auto board = std::make_shared<Image2D<Color3b>>(8, 8);
+  for (int y = 0; y < 8; ++y)
+    for (int x = 0; x < 8; ++x)
+      board->at(x, y) = ((x / 2 + y / 2) % 2) ? Color3b{30, 80, 200} : Color3b{220, 210, 190};
+  auto floor_mat = textured ? create_phong_material(zero, create_image_texture2d(board), zero, konst(1, 1, 1)) : white;
   auto vacuum = create_vacuum();
   const MediumInterface mi(vacuum);
 
@@ -124,7 +131,7 @@ int main(int argc, char** argv) {
   };
   const Transform id;
   const Spectrum black;
-  add(quad_mesh({-1, -1, -1}, {-1, -1, 1}, {1, -1, 1}, {1, -1, -1}, {0, 1, 0}), id, white, black);    // floor
+  add(quad_mesh({-1, -1, -1}, {-1, -1, 1}, {1, -1, 1}, {1, -1, -1}, {0, 1, 0}), id, floor_mat, black);  // floor
   add(quad_mesh({-1, 1, -1}, {1, 1, -1}, {1, 1, 1}, {-1, 1, 1}, {0, -1, 0}), id, white, black);       // ceiling
   add(quad_mesh({-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1}, {0, 0, 1}), id, white, black);    // back
   add(quad_mesh({-1, -1, -1}, {-1, 1, -1}, {-1, 1, 1}, {-1, -1, 1}, {1, 0, 0}), id, red, black);      // left
@@ -181,6 +188,14 @@ int main(int argc, char** argv) {
   put(f, d.env_texels);
   put(f, d.env_to_light);
   put(f, d.env_to_world);
+  const uint32_t ntex = (uint32_t)d.textures.size();
+  std::fwrite(&ntex, 4, 1, f);
+  for (const auto& t : d.textures) {
+    std::fwrite(&t.width, 4, 1, f);
+    std::fwrite(&t.height, 4, 1, f);
+    put(f, t.texels);
+    put(f, t.texels8);
+  }
   std::fclose(f);
   std::printf("scene: %zu triangles, %zu lights, %zu materials\n", d.indices.size() / 3, d.light_prims.size(),
               d.materials.size());

@@ -17,7 +17,9 @@ def _set():
     d = scenes.occluded_room(48, 36, 4, n_tris=5000)
     e = scenes.outdoor(32, 24, 4)  # environment light, glass and metal
     f = scenes.disney15_row(32, 16, 2, env=False)
-    return [a, b, c, d, e, f]
+    g = scenes.outdoor(24, 16, 2, glass=False, textured=True)  # image maps (texture indices offset in the set)
+    h = scenes.cornell(24, 24, 2, textured=True)
+    return [a, b, c, d, e, f, g, h]
 
 
 def test_batch_equals_single_renders(gpu):
@@ -33,7 +35,7 @@ def test_batch_equals_single_renders(gpu):
     torch.cuda.synchronize()
     # scenes in another order than the set, one scene twice
     extra = torch.zeros_like(films[0])
-    jobs = [(k, items[k][1], items[k][2], items[k][3], films[k].data_ptr()) for k in (2, 5, 0, 4, 3, 1)]
+    jobs = [(k, items[k][1], items[k][2], items[k][3], films[k].data_ptr()) for k in (2, 5, 7, 0, 4, 3, 6, 1)]
     jobs.append((0, items[0][1], items[0][2], items[0][3], extra.data_ptr()))
     torch.cuda.synchronize()
     st = gpu.render_batch_dev(jobs)

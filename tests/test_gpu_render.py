@@ -109,6 +109,23 @@ def test_outdoor_environment_light(gpu, glass, area_light, env_8bit):
     assert abs(a.mean() - b.mean()) <= 0.01 * b.mean()
 
 
+@pytest.mark.parametrize("maker", ["cornell", "outdoor"])
+def test_phong_image_textures(gpu, maker):
+    """Phong materials with image maps (8-bit and float kd, float ks and ns)
+    at the hit's uv: barycentric on triangles, (phi, theta) on a sphere."""
+    if maker == "cornell":
+        sc, cam, filt, par = scenes.cornell(64, 64, 8, textured=True)
+    else:
+        sc, cam, filt, par = scenes.outdoor(64, 48, 8, textured=True, glass=False)
+    orc = oracle.Oracle(sc, "port")
+    orc.set_camera(cam, filt)
+    ref = orc.render(par)
+    gpu.upload(sc)
+    out, stats = gpu.render(cam, filt, par)
+    assert stats.samples == par.width * par.height * par.spp
+    _compare(out, ref, 0.95)
+
+
 @pytest.mark.parametrize("case", ["sky", "black", "1x1", "black_with_geometry"])
 def test_environment_light_edge_cases(gpu, case):
     """No geometry, an all-black map and a 1 x 1 map on the device."""
@@ -187,7 +204,7 @@ def test_fp64_accumulation(gpu):
     assert np.allclose(out32, out64, rtol=1e-5, atol=1e-6)
 
 
-@pytest.mark.parametrize("maker", ["cornell", "disney", "glass", "metal", "outdoor", "disney15"])
+@pytest.mark.parametrize("maker", ["cornell", "disney", "glass", "metal", "outdoor", "disney15", "textured"])
 def test_replay_recorded_rays(gpu, maker):
     """Every trace the oracle's integrator makes, replayed on the GPU."""
     if maker == "cornell":
@@ -200,6 +217,8 @@ def test_replay_recorded_rays(gpu, maker):
         sc, cam, filt, par = scenes.outdoor(32, 32, 4)
     elif maker == "disney15":
         sc, cam, filt, par = scenes.disney15_row(32, 32, 4)
+    elif maker == "textured":
+        sc, cam, filt, par = scenes.cornell(32, 32, 4, textured=True)
     else:
         sc, cam, filt, par = scenes.disney_grid(32, 32, 2)
     orc = oracle.Oracle(sc, "port")

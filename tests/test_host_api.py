@@ -72,6 +72,13 @@ def _read_desc(path):
                       prim_emission=pe, light_prims=lp, max_leaf_prims=max_leaf)
     if ew and eh:
         sb.env_texels, sb.env_to_light, sb.env_to_world = tex.reshape(eh, ew, 3), to_l, to_w
+    ntex = int(np.frombuffer(buf, np.uint32, 1, off)[0])
+    off += 4
+    for _ in range(ntex):
+        tw, th = (int(v) for v in np.frombuffer(buf, np.uint32, 2, off))
+        off += 8
+        f, b = take(np.float32), take(np.uint8)
+        sb.textures.append(f.reshape(th, tw, 3) if f.size else b.reshape(th, tw, 3))
     return sb, cam
 
 
@@ -122,6 +129,24 @@ def test_factory_glass_and_metal_materials(program, tmp_path):
     assert sb.prim_material[22] == kinds.index(TR_MAT_GLASS)
 
 
+def test_factory_phong_image_map(program, tmp_path):
+    """create_phong_material with an image map: the description carries the
+    image as a texture and the material refers to it; the oracle and the
+    reference build render it alike."""
+    out = str(tmp_path / "c")
+    subprocess.run([program, out, "16", "16", "1", "describe", "textured"], check=True, capture_output=True, text=True)
+    sb, cam = _read_desc(out + ".desc")
+    assert len(sb.textures) == 1 and sb.textures[0].shape == (8, 8, 3) and sb.textures[0].dtype == np.uint8
+    floor = sb.materials[sb.prim_material[0]].rec
+    assert floor.tex_kd == 1 and floor.tex_ks == 0 and floor.tex_ns == 0
+    if oracle.ref_available():
+        par = make_params(16, 16, 2, 5, 5)
+        port, ref = oracle.Oracle(sb, "port"), oracle.Oracle(sb, "reference")
+        for o in (port, ref):
+            o.set_camera(cam, make_filter(0.5, 0.6))
+        assert np.array_equal(port.render(par).view(np.uint32), ref.render(par).view(np.uint32))
+
+
 def test_factory_disney15(program, tmp_path):
     """create_disney records the 2015 Disney parameters; the oracle and the
     reference build render the factory scene alike."""
@@ -167,7 +192,7 @@ def test_factory_environment_light(program, tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("variant", ["", "glass_metal", "sky", "disney15"])
+@pytest.mark.parametrize("variant", ["", "glass_metal", "sky", "disney15", "textured"])
 def test_factory_scene_renders_like_the_oracle(program, tmp_path, variant):
     W, H, S = 48, 40, 4
     out = str(tmp_path / "c")

@@ -61,6 +61,17 @@ def test_noalloc_matches_render_dev_on_consecutive_calls(gpu, case):
         np.testing.assert_allclose(got, want, rtol=RTOL, atol=0)
 
 
+def test_noalloc_rejects_image_maps(gpu):
+    """Materials with image maps need per-slot set-ups the static scratch has no room for."""
+    import torch
+    from tracer_gb300.abi import TR_ERR_UNSUPPORTED
+    sc, cam, filt, par = scenes.cornell(16, 16, 1, textured=True)
+    gpu.upload(sc)
+    out = torch.zeros((16, 16, 4), dtype=torch.float32, device="cuda:0")
+    torch.cuda.synchronize()
+    assert _noalloc(gpu)(gpu.h, C.byref(cam), C.byref(filt), C.byref(par), out.data_ptr(), None) == TR_ERR_UNSUPPORTED
+
+
 def test_noalloc_rejects_oversize_film(gpu):
     import torch
     sc, cam, filt, par = scenes.cornell(1024, 1024, 1)

@@ -482,6 +482,8 @@ tr_status upload_device_built(tr_ctx* ctx) {
   }
   tr_status es = upload_envs(ctx);
   if (es != TR_OK) return es;
+  es = upload_textures(ctx);
+  if (es != TR_OK) return es;
   ctx->has_scene = true;
   return TR_OK;
 }

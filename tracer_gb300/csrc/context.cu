@@ -49,21 +49,13 @@ DMat derive_material(const tr_material& m) {
   std::memset(&d, 0, sizeof(d));
   if (m.kind == TR_MAT_PHONG) {
     d.kind = MAT_PHONG;
-    f3 diffuse = mk3(m.kd[0], m.kd[1], m.kd[2]), spec = mk3(m.ks[0], m.ks[1], m.ks[2]);
-    float dem = 1.0f;
-    dem = smax(dem, diffuse.x + spec.x);
-    dem = smax(dem, diffuse.y + spec.y);
-    dem = smax(dem, diffuse.z + spec.z);
-    diffuse = mk3(diffuse.x / dem, diffuse.y / dem, diffuse.z / dem);
-    spec = mk3(spec.x / dem, spec.y / dem, spec.z / dem);
-    const float dl = lum(diffuse), sl = lum(spec);
-    const float wd = (dl + sl > kEps) ? dl / (dl + sl) : 0.5f;
-    d.w_diffuse = wd;
-    d.w_specular = 1.0f - wd;
-    d.albedo = diffuse + spec;
-    d.diffuse_coef = mk3(diffuse.x / kPi, diffuse.y / kPi, diffuse.z / kPi);
-    d.specular = spec;
-    d.ns = m.ns;
+    d.kd_c = mk3(m.kd[0], m.kd[1], m.kd[2]);
+    d.ks_c = mk3(m.ks[0], m.ks[1], m.ks[2]);
+    d.ns_c = m.ns;
+    d.tex_kd = (int)m.tex_kd;
+    d.tex_ks = (int)m.tex_ks;
+    d.tex_ns = (int)m.tex_ns;
+    phong_setup(d, d.kd_c, d.ks_c, d.ns_c);  // the constants; a hit with maps sets up again
   } else if (m.kind == TR_MAT_METAL) {
     // create_metal(color, eta, k) hands over to Metal(color, k, eta), whose
     // shading builds PaintedConductorFresnelPoint(color, 1, eta, k) with
@@ -376,7 +368,48 @@ tr_status upload_device_tables(tr_ctx* ctx) {
   }
   tr_status es = upload_envs(ctx);
   if (es != TR_OK) return es;
+  es = upload_textures(ctx);
+  if (es != TR_OK) return es;
   ctx->has_scene = true;
+  return TR_OK;
+}
+
+tr_status upload_textures(tr_ctx* ctx) {
+  const std::vector<HostScene::Tex>& tx = ctx->hs.textures;
+  DScene& sc = ctx->dsc;
+  sc.textures = nullptr;
+  sc.has_textures = 0;
+  for (const DMat& m : ctx->hs.mats)
+    if (m.kind == MAT_PHONG && (m.tex_kd | m.tex_ks | m.tex_ns)) sc.has_textures = 1;
+  if (tx.empty()) return TR_OK;
+  // one pool, 16 bytes per float texel and 4 per byte texel, every map 16-byte aligned
+  size_t total = 0;
+  std::vector<size_t> off(tx.size());
+  for (size_t i = 0; i < tx.size(); ++i) {
+    off[i] = total;
+    const size_t bytes = tx[i].texels.empty() ? tx[i].texels8.size() : tx[i].texels.size() * sizeof(float);
+    total += (bytes + 15) & ~size_t(15);
+  }
+  std::vector<uint8_t> pool(total, 0);
+  for (size_t i = 0; i < tx.size(); ++i) {
+    if (!tx[i].texels.empty()) std::memcpy(pool.data() + off[i], tx[i].texels.data(), tx[i].texels.size() * 4);
+    else std::memcpy(pool.data() + off[i], tx[i].texels8.data(), tx[i].texels8.size());
+  }
+  TR_CUDA(ctx, ctx->d_tex_pool.reserve(total));
+  TR_CUDA(ctx, cudaMemcpyAsync(ctx->d_tex_pool.p, pool.data(), total, cudaMemcpyHostToDevice, ctx->stream));
+  const uint8_t* base = ctx->d_tex_pool.as<uint8_t>();
+  std::vector<DTex> recs(tx.size());
+  for (size_t i = 0; i < tx.size(); ++i) {
+    recs[i].texels = tx[i].texels.empty() ? nullptr : reinterpret_cast<const float4*>(base + off[i]);
+    recs[i].texels8 = tx[i].texels8.empty() ? nullptr : reinterpret_cast<const uchar4*>(base + off[i]);
+    recs[i].w = tx[i].w;
+    recs[i].h = tx[i].h;
+  }
+  TR_CUDA(ctx, ctx->d_texs.reserve(recs.size() * sizeof(DTex)));
+  TR_CUDA(ctx, cudaMemcpyAsync(ctx->d_texs.p, recs.data(), recs.size() * sizeof(DTex), cudaMemcpyHostToDevice,
+                               ctx->stream));
+  TR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  sc.textures = ctx->d_texs.as<DTex>();
   return TR_OK;
 }
 
@@ -567,7 +600,7 @@ void tr_ctx_destroy(tr_ctx* ctx) {
   release_guide(ctx);
   for (DevBuf* b : {&ctx->d_nodes, &ctx->d_nodes4, &ctx->d_slots, &ctx->d_spheres, &ctx->d_prims, &ctx->d_tshade,
                     &ctx->d_mats, &ctx->d_lights, &ctx->d_roots, &ctx->d_rays, &ctx->d_out0, &ctx->d_out1,
-                    &ctx->d_err, &ctx->d_env_pool, &ctx->d_envs})
+                    &ctx->d_err, &ctx->d_env_pool, &ctx->d_envs, &ctx->d_tex_pool, &ctx->d_texs})
     b->release();
   cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -663,6 +696,12 @@ static tr_status build_host_scene(tr_ctx* ctx, const tr_scene_desc* d, HostScene
     ts.nA = nA;
     ts.dn1 = nB - nA;
     ts.dn2 = nC - nA;
+    ts.uvA[0] = uA[0];
+    ts.uvA[1] = uA[1];
+    ts.duv1[0] = m00;
+    ts.duv1[1] = m01;
+    ts.duv2[0] = m10;
+    ts.duv2[1] = m11;
     const float det = m00 * m11 - m01 * m10;
     ts.det_nonzero = det ? 1 : 0;
     if (det) {
@@ -682,7 +721,34 @@ static tr_status build_host_scene(tr_ctx* ctx, const tr_scene_desc* d, HostScene
     const float ratio = (float)lengthd(xform_vec(S.m, mk3(1.0f, 0.0f, 0.0f)));  // transformed_shape.hpp:13-15
     sph_wr[s] = ratio * S.radius;
   }
-  for (uint32_t m = 0; m < d->num_materials; ++m) hs.mats.push_back(derive_material(d->materials[m]));
+  if (d->num_textures && !d->textures) return set_err(ctx, TR_ERR_ARG, "textures missing");
+  for (uint32_t m = 0; m < d->num_materials; ++m) {
+    const tr_material& tm = d->materials[m];
+    if (tm.kind == TR_MAT_PHONG &&
+        (tm.tex_ka > d->num_textures || tm.tex_kd > d->num_textures || tm.tex_ks > d->num_textures ||
+         tm.tex_ns > d->num_textures))
+      return set_err(ctx, TR_ERR_ARG, "material names a missing texture");
+    hs.mats.push_back(derive_material(tm));
+  }
+  for (uint32_t k = 0; k < d->num_textures; ++k) {
+    const tr_texture& t = d->textures[k];
+    if (t.width == 0 || t.height == 0 || t.width > 65536 || t.height > 65536 || (!t.texels == !t.texels8))
+      return set_err(ctx, TR_ERR_ARG, "invalid texture " + std::to_string(k));
+    HostScene::Tex x;
+    x.w = (int)t.width;
+    x.h = (int)t.height;
+    const size_t n = (size_t)x.w * x.h;
+    if (t.texels) {
+      x.texels.resize(4 * n);
+      for (size_t i = 0; i < n; ++i)
+        for (int c = 0; c < 4; ++c) x.texels[4 * i + c] = c < 3 ? t.texels[3 * i + c] : 0.0f;
+    } else {
+      x.texels8.resize(4 * n);
+      for (size_t i = 0; i < n; ++i)
+        for (int c = 0; c < 4; ++c) x.texels8[4 * i + c] = c < 3 ? t.texels8[3 * i + c] : 0;
+    }
+    hs.textures.push_back(std::move(x));
+  }
   hs.prims.resize(np);
   std::vector<float> lo(3 * (size_t)np), hi(3 * (size_t)np);
   for (uint32_t p = 0; p < np; ++p) {
@@ -803,7 +869,16 @@ static void append_scene(HostScene& dst, const HostScene& src) {
   }
   dst.tshade.insert(dst.tshade.end(), src.tshade.begin(), src.tshade.end());
   dst.spheres.insert(dst.spheres.end(), src.spheres.begin(), src.spheres.end());
-  dst.mats.insert(dst.mats.end(), src.mats.begin(), src.mats.end());
+  const int tex_base = (int)dst.textures.size();
+  for (DMat m : src.mats) {
+    if (m.kind == MAT_PHONG) {
+      if (m.tex_kd) m.tex_kd += tex_base;
+      if (m.tex_ks) m.tex_ks += tex_base;
+      if (m.tex_ns) m.tex_ns += tex_base;
+    }
+    dst.mats.push_back(m);
+  }
+  dst.textures.insert(dst.textures.end(), src.textures.begin(), src.textures.end());
   const int env_base = (int)dst.envs.size();
   for (DLight l : src.lights) {
     if (l.env >= 0) l.env += env_base;

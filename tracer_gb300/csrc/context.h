@@ -58,6 +58,13 @@ struct HostScene {
   std::vector<float> blo, bhi;
   // environment lights of the set (DLight::env indexes them)
   std::vector<EnvHost> envs;
+  // image textures of the materials, 4 floats or 4 bytes per texel
+  struct Tex {
+    int w = 0, h = 0;
+    std::vector<float> texels;
+    std::vector<uint8_t> texels8;
+  };
+  std::vector<Tex> textures;
 };
 
 struct RenderBuffers;  // render.cu
@@ -74,6 +81,7 @@ struct tr_ctx {
   trg::DevBuf d_nodes, d_nodes4, d_slots, d_spheres, d_prims, d_tshade, d_mats, d_lights, d_roots;
   trg::DevBuf d_rays, d_out0, d_out1, d_err;
   trg::DevBuf d_env_pool, d_envs;  // environment lights: texels and tables, DEnv records
+  trg::DevBuf d_tex_pool, d_texs;  // material textures: texels, DTex records
   std::atomic<int> cancel{0};
   trg::RenderBuffers* rb = nullptr;
   tr_tuning tune{20, 0, 16, 8, 2};
@@ -90,6 +98,8 @@ tr_status upload_device_tables(tr_ctx* ctx);
 tr_status upload_device_built(tr_ctx* ctx);  // bvh_gpu.cu: the TR_BVH_DEVICE path
 // Uploads the set's environment lights and sets the scene's envs / has_env.
 tr_status upload_envs(tr_ctx* ctx);
+// Uploads the set's material textures and sets the scene's textures / has_textures.
+tr_status upload_textures(tr_ctx* ctx);
 // Grid of a persistent traversal kernel: SMs x resident blocks (tuned or as many as fit).
 int traversal_grid(const tr_ctx* ctx, const void* kernel);
 // Whether any-hit traversal walks the four-wide tree (tuning and scene allow it).

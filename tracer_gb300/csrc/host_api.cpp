@@ -311,6 +311,7 @@ class GeneralScene : public Scene {
     std::unordered_map<const MeshData*, int> mesh_base;
     std::unordered_map<const Material*, int> mat_index;
     std::unordered_map<const Light*, int> light_index;
+    std::unordered_map<const Texture2D*, uint32_t> tex_index;
     for (size_t i = 0; i < accel_->prims.size(); ++i) {
       const auto* gp = dynamic_cast<const GeometricPrimitive*>(accel_->prims[i].get());
       if (!gp) throw std::invalid_argument("primitive not made by create_geometric_primitive");
@@ -318,7 +319,39 @@ class GeneralScene : public Scene {
       auto mi = mat_index.find(gp->material.get());
       if (mi == mat_index.end()) {
         mi = mat_index.emplace(gp->material.get(), (int)d.materials.size()).first;
-        d.materials.push_back(gp->material->rec);
+        tr_material rec = gp->material->rec;
+        uint32_t* slots[4] = {&rec.tex_ka, &rec.tex_kd, &rec.tex_ks, &rec.tex_ns};
+        for (int k = 0; k < 4; ++k) {
+          const Texture2D* t = gp->material->maps[k].get();
+          if (!t) continue;
+          auto ti = tex_index.find(t);
+          if (ti == tex_index.end()) {
+            SceneDesc::TextureData td;
+            if (const auto* ht = dynamic_cast<const HdrTexture*>(t)) {
+              const Image2D<Color3f>& img = ht->image();
+              td.width = (uint32_t)img.width();
+              td.height = (uint32_t)img.height();
+              for (int y = 0; y < img.height(); ++y)
+                for (int x = 0; x < img.width(); ++x) {
+                  const Color3f& c = img.at(x, y);
+                  td.texels.insert(td.texels.end(), {c.x, c.y, c.z});
+                }
+            } else {
+              const Image2D<Color3b>& img = static_cast<const ImageTexture*>(t)->image();
+              td.width = (uint32_t)img.width();
+              td.height = (uint32_t)img.height();
+              for (int y = 0; y < img.height(); ++y)
+                for (int x = 0; x < img.width(); ++x) {
+                  const Color3b& c = img.at(x, y);
+                  td.texels8.insert(td.texels8.end(), {c.x, c.y, c.z});
+                }
+            }
+            ti = tex_index.emplace(t, (uint32_t)d.textures.size() + 1).first;
+            d.textures.push_back(std::move(td));
+          }
+          *slots[k] = ti->second;
+        }
+        d.materials.push_back(rec);
       }
       if (const auto* ts = dynamic_cast<const TriangleShape*>(gp->shape.get())) {
         auto mb = mesh_base.find(ts->mesh.get());
@@ -517,13 +550,26 @@ RC<Material> create_phong_material(RC<const Texture2D> map_ka, RC<const Texture2
                                    RC<const Texture2D> map_ks, RC<const Texture2D> map_ns) {
   tr_material m{};
   m.kind = TR_MAT_PHONG;
-  const Spectrum ka = tex(map_ka, "ka"), kd = tex(map_kd, "kd"), ks = tex(map_ks, "ks");
-  const float a[3] = {ka.r, ka.g, ka.b}, d[3] = {kd.r, kd.g, kd.b}, s[3] = {ks.r, ks.g, ks.b};
+  // constants are recorded as values, image maps as textures of the material
+  const RC<const Texture2D> in[4] = {map_ka, map_kd, map_ks, map_ns};
+  const char* names[4] = {"ka", "kd", "ks", "ns"};
+  Spectrum v[4];
+  RC<const Texture2D> maps[4];
+  for (int k = 0; k < 4; ++k) {
+    if (!in[k]) throw std::invalid_argument(std::string("null texture: ") + names[k]);
+    if (dynamic_cast<const HdrTexture*>(in[k].get()) || dynamic_cast<const ImageTexture*>(in[k].get()))
+      maps[k] = in[k];
+    else
+      v[k] = tex(in[k], names[k]);
+  }
+  const float a[3] = {v[0].r, v[0].g, v[0].b}, d[3] = {v[1].r, v[1].g, v[1].b}, s[3] = {v[2].r, v[2].g, v[2].b};
   std::memcpy(m.ka, a, sizeof(a));
   std::memcpy(m.kd, d, sizeof(d));
   std::memcpy(m.ks, s, sizeof(s));
-  m.ns = tex_s(map_ns, "ns");
-  return std::make_shared<Material>(m);
+  m.ns = v[3].r;
+  auto mat = std::make_shared<Material>(m);
+  for (int k = 0; k < 4; ++k) mat->maps[k] = maps[k];
+  return mat;
 }
 
 RC<Material> create_glass(RC<const Texture2D> map_kr, RC<const Texture2D> map_kt, RC<const Texture2D> map_ior) {
@@ -670,6 +716,15 @@ tr_scene_desc SceneDesc::view() const {
   d.num_lights = (uint32_t)light_prims.size();
   d.light_prims = light_prims.data();
   d.max_leaf_prims = max_leaf_prims;
+  texture_recs_.resize(textures.size());
+  for (size_t k = 0; k < textures.size(); ++k) {
+    texture_recs_[k].width = textures[k].width;
+    texture_recs_[k].height = textures[k].height;
+    texture_recs_[k].texels = textures[k].texels.empty() ? nullptr : textures[k].texels.data();
+    texture_recs_[k].texels8 = textures[k].texels8.empty() ? nullptr : textures[k].texels8.data();
+  }
+  d.num_textures = (uint32_t)textures.size();
+  d.textures = texture_recs_.empty() ? nullptr : texture_recs_.data();
   if (env_width && env_height) {
     d.env_width = env_width;
     d.env_height = env_height;

@@ -80,6 +80,9 @@ enum : int {  // counter slots
   C_ERR = 17,     // traversal error word
 };
 constexpr int kCtrWords = 32;  // the counter array
+// Material code in the shading context: the material index, or with this bit
+// set the slot's own set-up in Launch::MT (a Phong material with maps).
+constexpr int kMatScratch = 1 << 30;
 
 struct RenderBuffers {
   int n = 0, nl = 0;
@@ -87,6 +90,7 @@ struct RenderBuffers {
       stats;
   DevBuf VR, NV, gfeat, gout, tb;  // path guiding: vertex records, network rows, training records
   DevBuf GX;                        // path guiding: the continuation's MIS data (4 float4 per slot)
+  DevBuf MT;                        // Phong set-ups at hits with image maps (one DMat per slot)
   DevBuf jobs;                      // JobDev table of the current render
   unsigned int tb_count = 0, tb_cap = 0;  // training records of the last guided render
   unsigned int* h_active = nullptr;  // pinned: live-slot count per check
@@ -121,6 +125,7 @@ struct Launch {
                          // also holds the guided vertex's network row, normal correction and |cos|)
   float2* NU;            // light-sample draws per (slot, light)
   float4* SH;            // shadow: 3 per (slot, light): o|t_max, d, contrib|valid
+  DMat* MT;              // per slot: the Phong set-up at a hit with image maps (null without maps)
   int* q_ext[2];
   int* q_act[2];
   int* q_mat[kMatKinds];
@@ -477,8 +482,9 @@ __device__ f3 guided_strategy_emission(const Launch& P, int slot, float4 hit, f3
     lpdf = light_pdf_at(pr_.area, o, o + scale(d, hit.y), gz);
     lq = lpdf;
   }
-  const int mat = __float_as_int(P.SC[7 * (size_t)slot].w);
-  const f3 fs = ps > 0.0f ? muls(P.sc.mats[mat].diffuse_coef, nc) : mk3(0.0f, 0.0f, 0.0f);
+  const int mcode = __float_as_int(P.SC[7 * (size_t)slot].w);
+  const DMat& mat = (mcode & kMatScratch) ? P.MT[slot] : P.sc.mats[mcode];
+  const f3 fs = ps > 0.0f ? muls(mat.diffuse_coef, nc) : mk3(0.0f, 0.0f, 0.0f);
   const f3 g = direct_integrand(fe, pb, fs, ps, lpdf, lq);
   const float w = pr * pr / (pr * pr + lpdf * lpdf + po * po);
   return muls(mulc(Le, g), cosv * w / pr);
@@ -729,9 +735,16 @@ __global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
     const float4 hit = P.HC[slot];
     Isect is;
     make_isect(P.sc, hit, ro, rd, is);
-    const int mat = P.sc.prims[is.prim].material;
+    int mat = P.sc.prims[is.prim].material;
     Bsdf bsdf;
     bsdf.m = P.sc.mats + mat;
+    if (KIND == MAT_PHONG && P.MT && (bsdf.m->tex_kd | bsdf.m->tex_ks | bsdf.m->tex_ns)) {
+      float u, v;
+      hit_uv(P.sc, hit, ro, rd, u, v);
+      phong_at(P.sc, *bsdf.m, u, v, P.MT + slot);
+      bsdf.m = P.MT + slot;
+      mat |= kMatScratch;
+    }
     bsdf.g = is.g;
     bsdf.s = is.s;
     const float u0 = Pcg::next(st), u1 = Pcg::next(st), u2 = Pcg::next(st);
@@ -982,7 +995,8 @@ __global__ void __launch_bounds__(128) k_nee(Launch P) {
     const float4 a = sc[0], b = sc[1], c = sc[2], d = sc[3], e = sc[4], f = sc[5], g = sc[6];
     const f3 pos = mk3(a.x, a.y, a.z), wo = mk3(b.x, b.y, b.z);
     Bsdf bsdf;
-    bsdf.m = P.sc.mats + __float_as_int(a.w);
+    const int mcode = __float_as_int(a.w);
+    bsdf.m = (mcode & kMatScratch) ? P.MT + slot : P.sc.mats + mcode;
     bsdf.g.x = mk3(b.w, c.x, c.y);
     bsdf.g.y = mk3(c.z, c.w, d.x);
     bsdf.g.z = mk3(d.y, d.z, d.w);
@@ -1089,7 +1103,7 @@ void release_render(tr_ctx* ctx) {
   for (DevBuf* b : {&rb->P0, &rb->P1, &rb->P2, &rb->P3, &rb->P4, &rb->rng, &rb->M0, &rb->M1, &rb->M2, &rb->HC,
                     &rb->HM, &rb->SC, &rb->NU, &rb->SH, &rb->acc, &rb->q_ext, &rb->q_act, &rb->q_mat, &rb->q_nee,
                     &rb->q_sh, &rb->ctr, &rb->stats, &rb->VR, &rb->NV, &rb->gfeat, &rb->gout, &rb->tb, &rb->jobs,
-                    &rb->GX})
+                    &rb->GX, &rb->MT})
     b->release();
   if (rb->h_active) cudaFreeHost(rb->h_active);
   for (cudaEvent_t e : rb->ev_pool) cudaEventDestroy(e);
@@ -1252,6 +1266,12 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   P.SC = rb->SC.as<float4>();
   P.NU = rb->NU.as<float2>();
   P.SH = rb->SH.as<float4>();
+  P.MT = nullptr;
+  if (ctx->dsc.has_textures) {
+    cudaError_t e = rb->MT.reserve((size_t)n * sizeof(DMat));
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "per-slot material set-ups");
+    P.MT = rb->MT.as<DMat>();
+  }
   for (int k = 0; k < 2; ++k) {
     P.q_ext[k] = rb->q_ext.as<int>() + (size_t)k * 2 * n;
     P.q_act[k] = rb->q_act.as<int>() + (size_t)k * n;
@@ -1580,6 +1600,8 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
     return set_err(ctx, TR_ERR_UNSUPPORTED, "direct_light_sample_num must be 1 on the GPU path");
   if (!(filter->radius > 0.0f) || filter->radius > 16.0f) return set_err(ctx, TR_ERR_ARG, "invalid filter radius");
   if (ctx->device < 0 || ctx->device >= kMaxDevices) return set_err(ctx, TR_ERR_ARG, "device ordinal out of range");
+  if (ctx->dsc.has_textures)  // their per-slot material set-ups have no room in the static scratch
+    return set_err(ctx, TR_ERR_UNSUPPORTED, "tr_render_dev_noalloc does not take materials with image maps");
   const long long npix = (long long)prm->width * prm->height;
   const int nl = ctx->dsc.max_lights;
   const size_t NL = (size_t)std::max(nl, 1);

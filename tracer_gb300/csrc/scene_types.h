@@ -75,7 +75,16 @@ struct DTriShade {
   f3 nA, dn1, dn2;  // normalised vertex normal A, nB - nA, nC - nA
   f3 dndu0, dndv0;  // compute_ss_ts(nB-nA, nC-nA, uv...) when its determinant != 0
   int det_nonzero;
-  int pad[3];
+  float uvA[2], duv1[2], duv2[2];  // uvA, uvB - uvA, uvC - uvA (the hit's uv, triangle.cpp:186)
+  int pad;
+};
+
+// An image texture (HDRTexture2D or ImageTexture2D): w x h texels, texel
+// (x, y) at x + y * w; exactly one of the two pointers is set.
+struct DTex {
+  const float4* texels;
+  const uchar4* texels8;
+  int w, h;
 };
 
 enum { MAT_PHONG = 0, MAT_DISNEY12 = 1, MAT_GLASS = 2, MAT_METAL = 3, MAT_DISNEY15 = 4 };
@@ -110,7 +119,31 @@ struct DMat {
   // clearcoat above, ax, ay its specular alphas, ior its IOR (at least 1.01)
   f3 c_tint, spec_scale;
   float transmission, trans_ax, trans_ay, cc_rough, w_diff15, w_trans, w_spec15, w_cc;
+  // Phong maps (0: the constants below; k: DScene::textures[k - 1]) and the constants
+  int tex_kd, tex_ks, tex_ns;
+  f3 kd_c, ks_c;
+  float ns_c;
 };
+
+// Phong::shading's set-up (src/material/phong.cpp:29-70): kd and ks scaled
+// down so that no channel sums above 1, lobe weights by luminance.
+TR_HD void phong_setup(DMat& d, f3 diffuse, f3 spec, float ns) {
+  float dem = 1.0f;
+  dem = (dem < diffuse.x + spec.x) ? diffuse.x + spec.x : dem;
+  dem = (dem < diffuse.y + spec.y) ? diffuse.y + spec.y : dem;
+  dem = (dem < diffuse.z + spec.z) ? diffuse.z + spec.z : dem;
+  diffuse = mk3(diffuse.x / dem, diffuse.y / dem, diffuse.z / dem);
+  spec = mk3(spec.x / dem, spec.y / dem, spec.z / dem);
+  const float dl = 0.2126f * diffuse.x + 0.7152f * diffuse.y + 0.0722f * diffuse.z;
+  const float sl = 0.2126f * spec.x + 0.7152f * spec.y + 0.0722f * spec.z;
+  const float wd = (dl + sl > kEps) ? dl / (dl + sl) : 0.5f;
+  d.w_diffuse = wd;
+  d.w_specular = 1.0f - wd;
+  d.albedo = diffuse + spec;
+  d.diffuse_coef = mk3(diffuse.x / kPi, diffuse.y / kPi, diffuse.z / kPi);
+  d.specular = spec;
+  d.ns = ns;
+}
 
 // A diffuse area light on a triangle (src/light/diffuse_light.cpp:44-60)
 struct DLight {
@@ -170,6 +203,8 @@ struct DScene {
   int has_disney15;  // some material is the 2015 Disney BSDF
   const DEnv* envs;  // environment lights of the set (DLight::env indexes them)
   int has_env;       // some scene has an environment light
+  const DTex* textures;  // image textures of the set's materials
+  int has_textures;      // some material has an image map
 };
 
 }  // namespace trg

@@ -160,6 +160,53 @@ __device__ __forceinline__ void sphere_isect(const DSphere& S, f3 o, f3 d, float
   is.wo = xform_vec(S.m, -ld);
 }
 
+// The hit's uv, formed only for materials with image maps: the barycentric
+// blend of Triangle::intersect_p (src/shape/triangle.cpp:186) or
+// sphere::local_geometry_uv_and_coord (src/shape/sphere.cpp:48-56) at the
+// local hit point.
+static __device__ __noinline__ void hit_uv(const DScene& sc, const float4 hit, f3 o, f3 d, float& u, float& v) {
+  const DPrim& p = sc.prims[__float_as_int(hit.x)];
+  if (p.kind == PRIM_TRIANGLE) {
+    const DTriShade& ts = sc.tshade[p.shape];
+    u = ts.uvA[0] + hit.z * ts.duv1[0] + hit.w * ts.duv2[0];
+    v = ts.uvA[1] + hit.z * ts.duv1[1] + hit.w * ts.duv2[1];
+    return;
+  }
+  const DSphere& S = sc.spheres[p.shape];
+  const f3 lo = xform_point(S.inv, o);
+  const f3 ld = normalize(xform_vec(S.inv, d));
+  const f3 q = lo + scale(ld, hit.y);
+  float phi = (!q.x && !q.y) ? 0.0f : atan2f(q.y, q.x);
+  if (phi < 0.0f) phi += 2.0f * kPi;
+  float st = q.z / S.radius;
+  st = st < -1.0f ? -1.0f : (1.0f < st ? 1.0f : st);
+  u = 0.5f * kInvPi * phi;
+  v = kInvPi * asinf(st) + 0.5f;
+}
+
+// Texture2D::evaluate of an image texture (HDR or 8-bit) at (u, v).
+__device__ __forceinline__ f3 tex_eval(const DTex& t, float u, float v) {
+  return t.texels8 ? env_tex_eval8(t.texels8, t.w, t.h, u, v) : env_tex_eval(t.texels, t.w, t.h, u, v);
+}
+
+// Phong::shading with maps: kd, ks and ns (its red channel) at the hit's uv,
+// then the same set-up as for constants, written to `out`.
+static __device__ __noinline__ void phong_at(const DScene& sc, const DMat& m, float u, float v, DMat* out) {
+  const f3 kd = m.tex_kd ? tex_eval(sc.textures[m.tex_kd - 1], u, v) : m.kd_c;
+  const f3 ks = m.tex_ks ? tex_eval(sc.textures[m.tex_ks - 1], u, v) : m.ks_c;
+  const float ns = m.tex_ns ? tex_eval(sc.textures[m.tex_ns - 1], u, v).x : m.ns_c;
+  DMat d;
+  d.kind = MAT_PHONG;
+  phong_setup(d, kd, ks, ns);
+  out->kind = d.kind;
+  out->ns = d.ns;
+  out->w_diffuse = d.w_diffuse;
+  out->w_specular = d.w_specular;
+  out->diffuse_coef = d.diffuse_coef;
+  out->specular = d.specular;
+  out->albedo = d.albedo;
+}
+
 __device__ __forceinline__ void make_isect(const DScene& sc, const float4 hit, f3 o, f3 d, Isect& is) {
   const int pid = __float_as_int(hit.x);
   const DPrim& p = sc.prims[pid];
