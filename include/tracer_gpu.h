@@ -358,6 +358,8 @@ tr_status tr_render_dev(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filt
  *  - Limit: width * height * (324 + 76 * lights) bytes (plus alignment) must
  *    fit in 16 MiB, e.g. 128x128 with 8 lights; larger films return
  *    TR_ERR_ARG with the size needed.
+ *  - Scenes whose materials have image maps return TR_ERR_UNSUPPORTED (their
+ *    per-pixel material set-ups do not fit the array).
  *  - The first call on a device looks up the array's address
  *    (cudaGetSymbolAddress), which can load the module; make that call
  *    before any stream capture.
