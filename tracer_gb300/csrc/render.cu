@@ -985,7 +985,7 @@ __global__ void __launch_bounds__(128) k_glass(Launch P, int cur) {
 // sample_area_light (src/renderer/direct_illumination.cpp:35-71) for one
 // (vertex, light) pair: the shadow ray is traced by k_shadow, which zeroes
 // the contribution when it is blocked.
-template <int KIND>
+template <int KIND, bool MAPS = false>  // MAPS: Phong hits may carry per-slot set-ups
 __global__ void __launch_bounds__(128) k_nee(Launch P) {
   const unsigned int n = P.ctr[C_NEE + nee_index(KIND)];
   for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -996,7 +996,7 @@ __global__ void __launch_bounds__(128) k_nee(Launch P) {
     const f3 pos = mk3(a.x, a.y, a.z), wo = mk3(b.x, b.y, b.z);
     Bsdf bsdf;
     const int mcode = __float_as_int(a.w);
-    bsdf.m = (mcode & kMatScratch) ? P.MT + slot : P.sc.mats + mcode;
+    bsdf.m = (MAPS && (mcode & kMatScratch)) ? P.MT + slot : P.sc.mats + mcode;
     bsdf.g.x = mk3(b.w, c.x, c.y);
     bsdf.g.y = mk3(c.z, c.w, d.x);
     bsdf.g.z = mk3(d.y, d.z, d.w);
@@ -1403,7 +1403,8 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     if (P.sc.has_metal) k_material<MAT_METAL><<<grid, 128, 0, st>>>(P, cur);
     if (P.sc.has_disney15) k_material<MAT_DISNEY15><<<grid, 128, 0, st>>>(P, cur);
     mark();
-    k_nee<MAT_PHONG><<<grid, 128, 0, st>>>(P);
+    if (P.MT) k_nee<MAT_PHONG, true><<<grid, 128, 0, st>>>(P);
+    else k_nee<MAT_PHONG><<<grid, 128, 0, st>>>(P);
     mark();
     k_nee<MAT_DISNEY12><<<grid, 128, 0, st>>>(P);
     if (P.sc.has_metal) k_nee<MAT_METAL><<<grid, 128, 0, st>>>(P);  // timed with Disney12
