@@ -982,11 +982,60 @@ __global__ void __launch_bounds__(128) k_glass(Launch P, int cur) {
   count_add(P.stats, finished);
 }
 
+// sample_environment_light (src/renderer/direct_illumination.cpp:73-106) for
+// one (vertex, environment light) item; false: no shadow ray. gcode: the
+// guided vertex's network row (bit 30: three strategies), else -1.
+template <int KIND>
+__device__ __noinline__ bool nee_env_item(const Launch& P, int item, int slot, int env, f3 pos, f3 wo,
+                                          const Bsdf& bsdf, float2 uv, int gcode, float4* rec) {
+  bool ok = false;
+  // sample_environment_light (src/renderer/direct_illumination.cpp:73-106)
+  f3 Le, lpos;
+  float lpdf;
+  if (env_sample(P.sc.envs[env], pos, uv.x, uv.y, Le, lpdf, lpos) && !black(Le)) {
+    f3 to_light = lpos - pos;
+    bool too_close;
+    const float dist = dist_minus_eps(len2f(to_light), too_close);
+    if (!too_close) {
+      to_light = normalize(to_light);
+      const float4 p4 = P.P4[slot];
+      f3 cc = mk3(0.0f, 0.0f, 0.0f);
+      bool trace = false;
+      if (KIND == MAT_PHONG && gcode >= 0) {
+        const f3 fw = guided_nee_factor(P, bsdf, wo, to_light, gcode & 0x3fffffff, (gcode >> 30) & 1, lpdf,
+                                        env_pdf(P.sc.envs[env], normalize(to_light)));
+        trace = !black(fw);
+        cc = mulc(mk3(p4.x, p4.y, p4.z), divs(mulc(Le, fw), lpdf));
+      } else {
+        const f3 bf = MatOps<KIND>::eval(bsdf, to_light, wo);
+        trace = !black(bf);
+        if (trace) {
+          const float bpdf = MatOps<KIND>::pdf(bsdf, to_light, wo);
+          const f3 fl = muls(mulc(Le, bf), abs_cos(to_light, bsdf.g.z));
+          const float w = power_heuristic(lpdf, bpdf);
+          cc = mulc(mk3(p4.x, p4.y, p4.z), divs(muls(fl, w), lpdf));
+        }
+      }
+      if (trace) {
+        const f3 sd = normalize(to_light);
+        rec[0] = make_float4(pos.x, pos.y, pos.z, dist);
+        rec[1] = make_float4(sd.x, sd.y, sd.z, 0.0f);
+        rec[2] = make_float4(cc.x, cc.y, cc.z, 1.0f);
+        P.q_sh[append(P.ctr + C_SH)] = item;
+        ok = true;
+      }
+    }
+  }
+  return ok;
+}
+
 // sample_area_light (src/renderer/direct_illumination.cpp:35-71) for one
 // (vertex, light) pair: the shadow ray is traced by k_shadow, which zeroes
 // the contribution when it is blocked.
+// Six resident blocks per SM (80 registers, a few bytes of spill) measured
+// faster than the five its free allocation (91 registers) allows.
 template <int KIND, bool MAPS = false>  // MAPS: Phong hits may carry per-slot set-ups
-__global__ void __launch_bounds__(128) k_nee(Launch P) {
+__global__ void __launch_bounds__(128, 6) k_nee(Launch P) {
   const unsigned int n = P.ctr[C_NEE + nee_index(KIND)];
   for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int item = P.q_nee[nee_index(KIND)][i];
@@ -1007,46 +1056,9 @@ __global__ void __launch_bounds__(128) k_nee(Launch P) {
     const DLight& lt = P.sc.lights[job_of(P, slot).light_base + l];
     float4* rec = P.SH + 3 * (size_t)item;
     bool ok = false;
-    if (lt.env >= 0) {
-      // sample_environment_light (src/renderer/direct_illumination.cpp:73-106)
-      f3 Le, lpos;
-      float lpdf;
-      if (env_sample(P.sc.envs[lt.env], pos, uv.x, uv.y, Le, lpdf, lpos) && !black(Le)) {
-        f3 to_light = lpos - pos;
-        bool too_close;
-        const float dist = dist_minus_eps(len2f(to_light), too_close);
-        if (!too_close) {
-          to_light = normalize(to_light);
-          const int gcode = __float_as_int(g.y);  // guided vertex: network row (bit 30: three strategies), else -1
-          const float4 p4 = P.P4[slot];
-          f3 cc = mk3(0.0f, 0.0f, 0.0f);
-          bool trace = false;
-          if (KIND == MAT_PHONG && gcode >= 0) {
-            const f3 fw = guided_nee_factor(P, bsdf, wo, to_light, gcode & 0x3fffffff, (gcode >> 30) & 1, lpdf,
-                                            env_pdf(P.sc.envs[lt.env], normalize(to_light)));
-            trace = !black(fw);
-            cc = mulc(mk3(p4.x, p4.y, p4.z), divs(mulc(Le, fw), lpdf));
-          } else {
-            const f3 bf = MatOps<KIND>::eval(bsdf, to_light, wo);
-            trace = !black(bf);
-            if (trace) {
-              const float bpdf = MatOps<KIND>::pdf(bsdf, to_light, wo);
-              const f3 fl = muls(mulc(Le, bf), abs_cos(to_light, bsdf.g.z));
-              const float w = power_heuristic(lpdf, bpdf);
-              cc = mulc(mk3(p4.x, p4.y, p4.z), divs(muls(fl, w), lpdf));
-            }
-          }
-          if (trace) {
-            const f3 sd = normalize(to_light);
-            rec[0] = make_float4(pos.x, pos.y, pos.z, dist);
-            rec[1] = make_float4(sd.x, sd.y, sd.z, 0.0f);
-            rec[2] = make_float4(cc.x, cc.y, cc.z, 1.0f);
-            P.q_sh[append(P.ctr + C_SH)] = item;
-            ok = true;
-          }
-        }
-      }
-      if (!ok) rec[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (lt.env >= 0) {  // out of line: its registers would otherwise count for every item
+      if (!nee_env_item<KIND>(P, item, slot, lt.env, pos, wo, bsdf, uv, __float_as_int(g.y), rec))
+        rec[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       continue;
     }
     // Triangle::sample via UniformSampleTriangle (src/shape/triangle.cpp:61-97)
