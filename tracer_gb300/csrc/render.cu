@@ -720,8 +720,11 @@ __device__ __noinline__ BsdfSample sample_bsdf_shared(const Bsdf& b, f3 wo, floa
 // One path vertex on a material of kind KIND: the body of eval_pixel_li
 // from the BSDF sample to the next continuation ray
 // (src/renderer/path_trace_renderer.cpp:125-163).
+// Resident blocks per SM, measured on the room: Phong runs faster at five
+// (96 registers, little spill) than at eight (64 registers, ~200 bytes of
+// spill), Disney12 the other way round.
 template <int KIND, bool GUIDED = false>
-__global__ void __launch_bounds__(128) k_material(Launch P, int cur) {
+__global__ void __launch_bounds__(128, KIND == MAT_DISNEY12 ? 8 : 5) k_material(Launch P, int cur) {
   const int nxt = cur ^ 1;
   const unsigned int n = P.ctr[C_MAT + KIND];
   unsigned int finished = 0;
