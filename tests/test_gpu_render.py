@@ -160,6 +160,28 @@ def test_disney15_row(gpu, env, min_depth):
     _compare(out, ref, 0.95)
 
 
+@pytest.mark.parametrize("seed", [0, 1])
+def test_mixed_random_scenes(gpu, seed):
+    """Random scenes with every material kind and the environment light:
+    most pixels agree within 1e-5 (refraction can send a few samples along
+    other paths after a last-bit difference) and the image mean within 1%."""
+    sc = scenes.mixed_scene(seed)
+    cam = scenes.random_camera(64, 48, seed)
+    par = scenes.make_params(64, 48, 8, 2, 7, seed_base=seed * 31)
+    filt = scenes.make_filter(0.5, 0.6)
+    orc = oracle.Oracle(sc, "port")
+    orc.set_camera(cam, filt)
+    ref = orc.render(par)
+    gpu.upload(sc)
+    out, stats = gpu.render(cam, filt, par)
+    assert stats.samples == 64 * 48 * 8
+    a, b = _image(out.astype(np.float64)), _image(ref.astype(np.float64))
+    rel = (np.abs(a - b) / np.maximum(np.abs(b), 1e-6)).max(-1)
+    print(f"within 1e-5: {(rel <= 1e-5).mean():.4f}, image means {a.mean():.5f} {b.mean():.5f}")
+    assert (rel <= 1e-5).mean() >= 0.8
+    assert abs(a.mean() - b.mean()) <= 0.01 * b.mean()
+
+
 def test_cornell(gpu):
     sc, cam, filt, par = scenes.cornell(64, 64, 8)
     orc = oracle.Oracle(sc, "port")

@@ -157,6 +157,22 @@ def test_disney15(env, min_depth):
     assert np.array_equal(bits(port.render(par)), bits(ref.render(par)))
 
 
+@pytest.mark.parametrize("seed", range(6))
+@pytest.mark.parametrize("env", [True, False])
+def test_mixed_random_scenes(seed, env):
+    """Random triangles and spheres with materials of every kind (Phong with
+    and without image maps, Disney12, Disney 2015, glass, metal), Russian
+    roulette from depth 2, with and without the environment light."""
+    sc = scenes.mixed_scene(seed, env=env)
+    cam = scenes.random_camera(32, 24, seed)
+    par = scenes.make_params(32, 24, 4, 2, 7, seed_base=seed * 31)
+    filt = scenes.make_filter(0.5, 0.6)
+    port, ref = oracle.Oracle(sc, "port"), oracle.Oracle(sc, "reference")
+    port.set_camera(cam, filt)
+    ref.set_camera(cam, filt)
+    assert np.array_equal(bits(port.render(par)), bits(ref.render(par)))
+
+
 def test_make_ray():
     for o, d in (((0, 0, 0), (1, 2, 3)), ((1, -1, 0.5), (1e-9, 1, 0)), ((0, 0, 0), (-0.0, 0.0, -3))):
         a = oracle.make_ray("port", o, d, 0.0, 1.0)

@@ -470,6 +470,49 @@ def random_scene(seed=0, n_tris=64, n_spheres=8, n_lights=2, disney_frac=0.5, ma
     return scene
 
 
+def mixed_scene(seed=0, n_tris=80, n_spheres=10, env=True):
+    """random_scene's geometry with materials of every kind drawn at random:
+    Phong (some with 8-bit or float image maps), Disney12, Disney 2015,
+    glass and metal; with the sky map as an environment light when `env`."""
+    sc = random_scene(seed, n_tris=n_tris, n_spheres=n_spheres)
+    rng = np.random.default_rng(1000 + seed)
+    sc.textures = [checker(8, 2), checker(6, 3, (0.9, 0.4, 0.1), (0.1, 0.1, 0.9), eight_bit=False),
+                   np.linspace(2.0, 40.0, 4 * 4 * 3, dtype=np.float32).reshape(4, 4, 3)]
+    mats = []
+    for k in range(len(sc.materials)):
+        if k == 0:  # the floor and the lights keep theirs
+            mats.append(sc.materials[0])
+            continue
+        kind = int(rng.integers(0, 6))
+        p = rng.random(14)
+        if kind == 0:
+            mats.append(Material(kind=TR_MAT_PHONG, kd=tuple(0.2 + 0.7 * p[0:3]), ks=tuple(0.3 * p[3:6]),
+                                 ns=float(1 + 40 * p[6]), tex_kd=int(rng.integers(0, 3)),
+                                 tex_ns=3 if p[7] < 0.5 else 0))
+        elif kind == 1:
+            mats.append(Material(kind=TR_MAT_DISNEY12, base_color=tuple(p[0:3]), metallic=p[3], roughness=p[4],
+                                 specular=p[5], specular_tint=p[6], sheen=p[7], clearcoat=p[8],
+                                 clearcoat_gloss=p[9], anisotropic=p[10], subsurface=p[11], sheen_tint=0.5))
+        elif kind == 2:
+            mats.append(Material(kind=TR_MAT_DISNEY15, base_color=tuple(p[0:3]), metallic=p[3], roughness=p[4],
+                                 transmission=p[5], transmission_roughness=p[6], ior=1.2 + p[7],
+                                 specular_scale=tuple(p[8:11]), specular_tint=p[11], anisotropic=p[12],
+                                 sheen=p[13], clearcoat=p[0] * p[1], clearcoat_gloss=p[2]))
+        elif kind == 3:
+            mats.append(Material(kind=TR_MAT_GLASS, kr=tuple(0.5 + 0.5 * p[0:3]), kt=tuple(0.5 + 0.5 * p[3:6]),
+                                 ior=1.2 + 0.6 * p[6]))
+        elif kind == 4:
+            mats.append(Material(kind=TR_MAT_METAL, color=tuple(0.3 + 0.7 * p[0:3]), eta=tuple(0.1 + p[3:6]),
+                                 k=tuple(1 + 3 * p[6:9]), roughness=0.05 + 0.6 * p[9], anisotropic=p[10]))
+        else:
+            mats.append(Material(kind=TR_MAT_PHONG, kd=tuple(0.2 + 0.7 * p[0:3]), ns=1.0))
+    sc.materials = mats
+    if env:
+        sc.env_texels = sky_map(32, 16)
+        sc.env_to_light, sc.env_to_world = rotate_x(math.pi / 2)
+    return sc
+
+
 def random_camera(width, height, seed=0):
     rng = np.random.default_rng(seed + 1000)
     pos = (float(rng.uniform(-1, 1)), float(rng.uniform(0.0, 1.5)), float(4 + rng.uniform(0, 1)))
