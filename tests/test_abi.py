@@ -40,6 +40,37 @@ def test_struct_layouts():
     assert ctypes.sizeof(TrMaterial) == 4 * 49  # + glass kr, kt, ior; metal color, eta, k; Disney 2015; maps
 
 
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirror against the C compiler's layout of include/tracer_gpu.h:
+    sizes and the offsets of the fields added last."""
+    import subprocess
+    from tracer_gb300.abi import TrFilter, TrTexture
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "layout.c"
+    fields = {"tr_scene_desc": ["env_width", "env_texels", "env_to_world", "env_texels8", "num_textures",
+                                "textures", "max_leaf_prims"],
+              "tr_material": ["k", "transmission", "specular_scale", "tex_ka", "tex_ns"],
+              "tr_texture": ["texels", "texels8"], "tr_camera": ["focal_dist"], "tr_filter": ["alpha"],
+              "tr_render_params": ["flags"]}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "tracer_gpu.h"', "int main(void) {"]
+    for t, fs in fields.items():
+        lines.append(f'  printf("{t} %zu\\n", sizeof({t}));')
+        for f in fs:
+            lines.append(f'  printf("{t}.{f} %zu\\n", offsetof({t}, {f}));')
+    lines += ["  return 0;", "}"]
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", f"-I{os.path.join(root, 'include')}", str(src), "-o", str(exe)], check=True)
+    got = dict(ln.split() for ln in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                    check=True).stdout.splitlines())
+    py = {"tr_scene_desc": TrSceneDesc, "tr_material": TrMaterial, "tr_texture": TrTexture, "tr_camera": TrCamera,
+          "tr_filter": TrFilter, "tr_render_params": TrRenderParams}
+    for t, fs in fields.items():
+        assert int(got[t]) == ctypes.sizeof(py[t]), t
+        for f in fs:
+            assert int(got[f"{t}.{f}"]) == getattr(py[t], f).offset, (t, f)
+
+
 def test_make_ray_matches_reference_semantics():
     from tracer_gb300 import scenes
     from tracer_gb300.native import make_ray
