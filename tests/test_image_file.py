@@ -140,7 +140,7 @@ def test_material_textures(program, tmp_path):
     assert m[3:6] == ["0.5", "0.5", "0.5"]  # the map (1.0) scaled by Kd
 
 
-def _png(rows, ctype, palette=None, filters=None):
+def _png(rows, ctype, palette=None, filters=None, level=9):
     """A PNG of 8-bit rows (list of byte arrays, top first), zlib-compressed,
     each row encoded with the given filter type (0-4) as ISO/IEC 15948 defines."""
     ch = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
@@ -175,7 +175,7 @@ def _png(rows, ctype, palette=None, filters=None):
     if palette is not None:
         png += chunk(b"PLTE", bytes(palette))
     # two IDAT chunks, the second one empty-ish: the stream spans chunks
-    z = zlib.compress(bytes(raw), 9)
+    z = zlib.compress(bytes(raw), level)
     return png + chunk(b"IDAT", z[:len(z) // 2]) + chunk(b"IDAT", z[len(z) // 2:]) + chunk(b"IEND", b"")
 
 
@@ -188,11 +188,12 @@ def _load_png(program, path):
     return np.array([[int(v) for v in ln.split()] for ln in lines[1:]], np.uint8).reshape(h, w, 3), lines
 
 
+@pytest.mark.parametrize("level", [0, 1, 9])
 @pytest.mark.parametrize("ctype", [0, 2, 3, 6])
-def test_load_png(program, tmp_path, ctype):
-    """Grey, RGB, palette and RGBA PNGs with every filter type and a
-    dynamic-Huffman zlib stream; rows come back flipped (the file's last row
-    is row 0), grey expanded to RGB, alpha dropped."""
+def test_load_png(program, tmp_path, ctype, level):
+    """Grey, RGB, palette and RGBA PNGs with every filter type, as stored,
+    fixed- and dynamic-Huffman zlib streams (levels 0, 1, 9); rows come back
+    flipped (the file's last row is row 0), grey expanded to RGB, alpha dropped."""
     rng = np.random.default_rng(ctype)
     h, w = 7, 23
     ch = {0: 1, 2: 3, 3: 1, 6: 4}[ctype]
@@ -200,7 +201,7 @@ def test_load_png(program, tmp_path, ctype):
     data = np.where(rng.random((h, w * ch)) < 0.3, rng.integers(0, 256, (h, w * ch)), smooth).astype(np.uint8)
     palette = rng.integers(0, 256, 3 * 256).astype(np.uint8) if ctype == 3 else None
     p = tmp_path / "a.png"
-    p.write_bytes(_png([bytes(r) for r in data], ctype, palette, filters=[0, 1, 2, 3, 4]))
+    p.write_bytes(_png([bytes(r) for r in data], ctype, palette, filters=[0, 1, 2, 3, 4], level=level))
     got, lines = _load_png(program, p)
     assert got is not None, lines
     px = data.reshape(h, w, ch)
