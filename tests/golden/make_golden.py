@@ -88,6 +88,20 @@ def main():
                         **render("cornell", lambda: scenes.cornell(32, 32, 4)))
     np.savez_compressed(os.path.join(OUT, "disney_grid_32x32_2spp.npz"),
                         **render("disney", lambda: scenes.disney_grid(32, 32, 2, min_depth=3)))
+    # the rows beyond the configured scenes: glass and metal, Disney 2015, the
+    # environment light (HDR and 8-bit maps) and Phong image maps
+    np.savez_compressed(os.path.join(OUT, "cornell_glass_metal_24x24_2spp.npz"),
+                        **render("glass_metal", lambda: scenes.cornell(24, 24, 2, max_depth=8, min_depth=2,
+                                                                        glass=True, metal=True)))
+    np.savez_compressed(os.path.join(OUT, "disney15_row_32x16_2spp.npz"),
+                        **render("disney15", lambda: scenes.disney15_row(32, 16, 2, env=False)))
+    np.savez_compressed(os.path.join(OUT, "outdoor_env_24x16_2spp.npz"),
+                        **render("outdoor", lambda: scenes.outdoor(24, 16, 2, env_size=(32, 16))))
+    np.savez_compressed(os.path.join(OUT, "outdoor_env8_textured_24x16_2spp.npz"),
+                        **render("outdoor8", lambda: scenes.outdoor(24, 16, 2, env_size=(32, 16), env_8bit=True,
+                                                                     textured=True, glass=False)))
+    np.savez_compressed(os.path.join(OUT, "cornell_textured_24x24_2spp.npz"),
+                        **render("textured", lambda: scenes.cornell(24, 24, 2, textured=True)))
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))

@@ -520,7 +520,10 @@ def random_camera(width, height, seed=0):
 
 
 _MAT_FIELDS = ("ka", "kd", "ks", "ns", "base_color", "subsurface", "metallic", "specular", "specular_tint",
-               "roughness", "anisotropic", "sheen", "sheen_tint", "clearcoat", "clearcoat_gloss")
+               "roughness", "anisotropic", "sheen", "sheen_tint", "clearcoat", "clearcoat_gloss",
+               # added later: fixtures packed before them have shorter rows and keep the defaults
+               "kr", "kt", "ior", "color", "eta", "k", "transmission", "transmission_roughness", "specular_scale",
+               "tex_ka", "tex_kd", "tex_ks", "tex_ns")
 
 
 def pack_scene(s: SceneBuffers, prefix: str = "") -> dict:
@@ -537,6 +540,11 @@ def pack_scene(s: SceneBuffers, prefix: str = "") -> dict:
            "sphere_to_local": s.sphere_to_local, "materials": np.asarray(mats, np.float32),
            "prim_shape": s.prim_shape, "prim_material": s.prim_material, "prim_emission": s.prim_emission,
            "light_prims": s.light_prims, "max_leaf_prims": np.int32(s.max_leaf_prims)}
+    if s.env_texels is not None or s.env_texels8 is not None:
+        out["env_texels"] = s.env_texels if s.env_texels is not None else s.env_texels8
+        out["env_to_light"], out["env_to_world"] = s.env_to_light, s.env_to_world
+    for k, t in enumerate(s.textures):
+        out[f"texture{k}"] = t
     return {prefix + k: np.asarray(v) for k, v in out.items()}
 
 
@@ -546,19 +554,34 @@ def unpack_scene(d, prefix: str = "") -> SceneBuffers:
         m = Material(kind=int(row[0]))
         i = 1
         for f in _MAT_FIELDS:
-            if isinstance(getattr(m, f), tuple):
+            if i >= len(row):
+                break
+            cur = getattr(m, f)
+            if isinstance(cur, tuple):
                 setattr(m, f, tuple(float(x) for x in row[i:i + 3]))
                 i += 3
             else:
-                setattr(m, f, float(row[i]))
+                setattr(m, f, int(row[i]) if isinstance(cur, int) and f.startswith("tex_") else float(row[i]))
                 i += 1
         mats.append(m)
     g = lambda k: np.asarray(d[prefix + k])
-    return SceneBuffers(positions=g("positions"), normals=g("normals"), uvs=g("uvs"), indices=g("indices"),
-                        sphere_radius=g("sphere_radius"), sphere_to_world=g("sphere_to_world"),
-                        sphere_to_local=g("sphere_to_local"), materials=mats, prim_shape=g("prim_shape"),
-                        prim_material=g("prim_material"), prim_emission=g("prim_emission"),
-                        light_prims=g("light_prims"), max_leaf_prims=int(g("max_leaf_prims")))
+    sb = SceneBuffers(positions=g("positions"), normals=g("normals"), uvs=g("uvs"), indices=g("indices"),
+                      sphere_radius=g("sphere_radius"), sphere_to_world=g("sphere_to_world"),
+                      sphere_to_local=g("sphere_to_local"), materials=mats, prim_shape=g("prim_shape"),
+                      prim_material=g("prim_material"), prim_emission=g("prim_emission"),
+                      light_prims=g("light_prims"), max_leaf_prims=int(g("max_leaf_prims")))
+    if prefix + "env_texels" in d:
+        env = g("env_texels")
+        if env.dtype == np.uint8:
+            sb.env_texels8 = env
+        else:
+            sb.env_texels = env
+        sb.env_to_light, sb.env_to_world = g("env_to_light"), g("env_to_world")
+    k = 0
+    while prefix + f"texture{k}" in d:
+        sb.textures.append(g(f"texture{k}"))
+        k += 1
+    return sb
 
 
 def pack_view(cam, filt, par, prefix: str = "") -> dict:
