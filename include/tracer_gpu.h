@@ -180,7 +180,7 @@ typedef struct tr_render_params {
   int32_t height;
   int32_t spp;
   int32_t min_depth;
-  int32_t max_depth;
+  int32_t max_depth;                /* 0 .. 65515 (larger: TR_ERR_ARG) */
   int32_t direct_light_sample_num; /* must be 1 on the GPU path */
   uint32_t seed_base;
   uint32_t flags; /* TR_RENDER_* bits below */
@@ -368,8 +368,11 @@ tr_status tr_render_dev(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filt
  *  - The array is shared by every context on a device: calls that overlap
  *    in time on one device (two contexts, two threads) race and corrupt
  *    each other's results. Calls on one context run in order.
- *  - Blocks until done; runs a fixed number of wavefront iterations, so
- *    tr_cancel does not stop it; stats->device_ms and stage_ms stay 0. */
+ *  - Blocks until done. Every 16 wavefront iterations it copies the
+ *    live-path count into a host stack variable (a synchronous pageable
+ *    copy) and stops once every path has ended, or with TR_ERR_CANCELLED
+ *    after tr_cancel; stats->device_ms and stage_ms stay 0.
+ *  - Restores the caller's current device before returning. */
 tr_status tr_render_dev_noalloc(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter,
                                 const tr_render_params* params, float* d_rgbw, tr_stats* stats);
 

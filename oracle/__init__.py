@@ -25,7 +25,8 @@ from tracer_gb300.abi import (NODE_DTYPE, RAY_DTYPE, TrCamera, TrFilter, TrRay, 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libtracer_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libtracer_ref.so")
-REF_ROOT = os.environ.get("TRACER_REF_ROOT", "/root/reference")
+# the reference checkout: a sibling of this repository unless TRACER_REF_ROOT says otherwise
+REF_ROOT = os.environ.get("TRACER_REF_ROOT", os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 
 def build_port() -> str:

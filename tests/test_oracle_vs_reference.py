@@ -178,3 +178,36 @@ def test_make_ray():
         a = oracle.make_ray("port", o, d, 0.0, 1.0)
         b = oracle.make_ray("reference", o, d, 0.0, 1.0)
         assert bytes(a) == bytes(b)
+
+
+def test_thin_lens_camera():
+    """ThinLensCamera with a lens (src/camera/thin_lens_camera.cpp:40-59):
+    the lens sample, the focal plane at focal_dist and look_at's frame."""
+    sc, _, filt, par = scenes.cornell(40, 32, 4)
+    cam = scenes.make_camera(40 / 32, (0.3, 0.2, 3.5), (0, -0.2, 0), (0, 1, 0), np.radians(40.0), 0.12, 3.1)
+    port, ref = oracle.Oracle(sc, "port"), oracle.Oracle(sc, "reference")
+    port.set_camera(cam, filt)
+    ref.set_camera(cam, filt)
+    a, b = port.render(par), ref.render(par)
+    assert np.array_equal(bits(a), bits(b))
+    # the lens matters: the same scene through a pinhole gives another film
+    pin = scenes.make_camera(40 / 32, (0.3, 0.2, 3.5), (0, -0.2, 0), (0, 1, 0), np.radians(40.0), 0.0, 3.1)
+    port.set_camera(pin, filt)
+    assert not np.array_equal(bits(port.render(par)), bits(a))
+
+
+def test_traversal_workload_full_size():
+    """The traversal workload at its configured size: the port's BVH over
+    1,048,576 triangles is the reference build's node for node, and a
+    quarter of the 4M closest-hit and shadow rays give the same results."""
+    sc = scenes.traversal(1 << 20, seed=0)
+    port, ref = oracle.Oracle(sc, "port"), oracle.Oracle(sc, "reference")
+    n0, o0 = port.bvh()
+    n1, o1 = ref.bvh()
+    assert np.array_equal(n0, n1) and np.array_equal(o0, o1)
+    rays = scenes.traversal_rays(1 << 22, seed=0)[::4]
+    p0, t0 = port.trace_closest(rays)
+    p1, t1 = ref.trace_closest(rays)
+    assert np.array_equal(p0, p1) and np.array_equal(bits(t0), bits(t1))
+    srays = scenes.traversal_rays(1 << 22, seed=0, shadow=True)[::4]
+    assert np.array_equal(port.trace_any(srays), ref.trace_any(srays))

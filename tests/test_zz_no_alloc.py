@@ -51,8 +51,12 @@ def test_noalloc_matches_render_dev_on_consecutive_calls(gpu, case):
         out = torch.full((H, W, 4), float("nan"), dtype=torch.float32, device="cuda:0")
         torch.cuda.synchronize()  # the fill runs on torch's stream, the render on the context's
         st = TrStats()
+        free_before = torch.cuda.mem_get_info(0)[0]
         s = f(gpu.h, C.byref(cam), C.byref(filt), C.byref(par), out.data_ptr(), C.byref(st))
         assert s == 0, gpu.L.tr_ctx_last_error(gpu.h).decode()
+        if call == 1:
+            # after a first call (module and symbol set-up) the call takes no device memory
+            assert torch.cuda.mem_get_info(0)[0] == free_before
         got = out.cpu().numpy()
         assert st.samples == st_ref.samples == W * H * par.spp
         assert st.extend_rays == st_ref.extend_rays and st.shadow_rays == st_ref.shadow_rays
@@ -90,3 +94,18 @@ def test_noalloc_rejects_oversize_film(gpu):
     st = TrStats()
     assert f(gpu.h, C.byref(cam), C.byref(filt), C.byref(small), out.data_ptr(), C.byref(st)) == 0
     assert st.samples == 32 * 32 * 2
+
+
+def test_noalloc_rejects_depth_beyond_16_bits(gpu):
+    """The path depth is kept in 16 bits: max_depth above 65515 is an
+    argument error for both render entry points, before any device work."""
+    import torch
+    sc, cam, filt, _ = scenes.cornell(8, 8, 1)
+    gpu.upload(sc)
+    out = torch.zeros((8, 8, 4), dtype=torch.float32, device="cuda:0")
+    torch.cuda.synchronize()
+    deep = scenes.make_params(8, 8, 1, 70000, 70000)
+    assert _noalloc(gpu)(gpu.h, C.byref(cam), C.byref(filt), C.byref(deep), out.data_ptr(), None) == TR_ERR_ARG
+    assert "65515" in gpu.L.tr_ctx_last_error(gpu.h).decode()
+    with pytest.raises(Exception):
+        gpu.render_dev(cam, filt, deep, out.data_ptr())

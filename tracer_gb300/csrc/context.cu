@@ -576,7 +576,8 @@ tr_status tr_ctx_create(tr_ctx** out, int device) {
     cudaGetLastError();
     return TR_ERR_CUDA;
   }
-  if (cudaSetDevice(device) != cudaSuccess) return TR_ERR_CUDA;
+  trg::DeviceScope scope(device);
+  if (scope.status != cudaSuccess) return TR_ERR_CUDA;
   tr_ctx* ctx = new tr_ctx();
   ctx->device = device;
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -594,7 +595,7 @@ tr_status tr_ctx_create(tr_ctx** out, int device) {
 
 void tr_ctx_destroy(tr_ctx* ctx) {
   if (!ctx) return;
-  cudaSetDevice(ctx->device);
+  trg::DeviceScope scope(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   release_render(ctx);
   release_guide(ctx);
@@ -898,7 +899,7 @@ tr_status tr_scene_upload(tr_ctx* ctx, const tr_scene_desc* d) {
 
 tr_status tr_scene_set_upload(tr_ctx* ctx, const tr_scene_desc* descs, uint32_t n) {
   if (!ctx || !descs || n == 0 || n > 65536) return TR_ERR_ARG;
-  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  TR_DEVICE_SCOPE(ctx);
   ctx->has_scene = false;
   const bool device_bvh = ctx->bvh_builder == TR_BVH_DEVICE;
   // each scene's tables and tree on its own host thread
@@ -978,7 +979,7 @@ tr_status tr_bvh_upload(tr_ctx* ctx, const tr_bvh_node32* nodes, size_t num_node
   if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
   if (ctx->hs.device_bvh) return set_err(ctx, TR_ERR_STATE, "the BVH was built on the device (TR_BVH_DEVICE)");
   if (ctx->hs.scene_node.size() != 1) return set_err(ctx, TR_ERR_STATE, "tr_bvh_upload replaces the tree of a single scene");
-  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  TR_DEVICE_SCOPE(ctx);
   std::vector<tr_bvh_node32> keep_nodes = ctx->hs.nodes;
   std::vector<uint32_t> keep_order = ctx->hs.order;
   ctx->hs.nodes.assign(nodes, nodes + num_nodes);
@@ -1049,7 +1050,7 @@ tr_status tr_trace_count_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, int32_
   if (((uintptr_t)d_rays & 15u) != 0) return set_err(ctx, TR_ERR_ARG, "ray buffer must be 16-byte aligned");
   *boxes = *prims = 0;
   if (n == 0) return TR_OK;
-  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  TR_DEVICE_SCOPE(ctx);
   // scratch: the words after the error word and the fetch position
   unsigned long long* counts = reinterpret_cast<unsigned long long*>(ctx->d_err.as<char>() + 16);
   TR_CUDA(ctx, cudaMemsetAsync(ctx->d_err.as<int>() + 1, 0, sizeof(int), ctx->stream));
@@ -1078,7 +1079,7 @@ tr_status tr_trace_closest(tr_ctx* ctx, const tr_ray* rays, size_t n, int32_t* p
   if (!ctx || (n && (!rays || !prim || !t))) return TR_ERR_ARG;
   if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
   if (n == 0) return TR_OK;
-  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  TR_DEVICE_SCOPE(ctx);
   TR_CUDA(ctx, ctx->d_rays.reserve(n * sizeof(tr_ray)));
   TR_CUDA(ctx, ctx->d_out0.reserve(n * sizeof(int32_t)));
   TR_CUDA(ctx, ctx->d_out1.reserve(n * sizeof(float)));
@@ -1094,7 +1095,7 @@ tr_status tr_trace_any(tr_ctx* ctx, const tr_ray* rays, size_t n, uint8_t* hit) 
   if (!ctx || (n && (!rays || !hit))) return TR_ERR_ARG;
   if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
   if (n == 0) return TR_OK;
-  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  TR_DEVICE_SCOPE(ctx);
   TR_CUDA(ctx, ctx->d_rays.reserve(n * sizeof(tr_ray)));
   TR_CUDA(ctx, ctx->d_out0.reserve(n));
   TR_CUDA(ctx, cudaMemcpyAsync(ctx->d_rays.p, rays, n * sizeof(tr_ray), cudaMemcpyHostToDevice, ctx->stream));

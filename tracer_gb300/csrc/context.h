@@ -108,6 +108,37 @@ void release_render(tr_ctx* ctx);
 void release_guide(tr_ctx* ctx);
 }  // namespace trg
 
+namespace trg {
+// Makes a device current for the duration of a C ABI call and gives the
+// caller's current device back when the call returns.
+struct DeviceScope {
+  int prev = -1;
+  cudaError_t status = cudaSuccess;
+  explicit DeviceScope(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+      cudaGetLastError();
+      prev = -1;
+    }
+    if (prev != dev) status = cudaSetDevice(dev);
+  }
+  ~DeviceScope() {
+    int now = -1;
+    if (prev >= 0 && cudaGetDevice(&now) == cudaSuccess && now != prev) cudaSetDevice(prev);
+  }
+  DeviceScope(const DeviceScope&) = delete;
+  DeviceScope& operator=(const DeviceScope&) = delete;
+};
+}  // namespace trg
+
+// The context's device for the rest of the enclosing C ABI function (the
+// caller's device is restored on return); returns the error if it cannot be
+// made current.
+#define TR_DEVICE_SCOPE(ctx)                                                          \
+  trg::DeviceScope dev_scope_((ctx)->device);                                         \
+  do {                                                                                \
+    if (dev_scope_.status != cudaSuccess) return trg::cuda_fail((ctx), dev_scope_.status, "cudaSetDevice"); \
+  } while (0)
+
 // Returns from the enclosing C ABI function with the context's error when a
 // CUDA runtime call fails.
 #define TR_CUDA(ctx, call)                                          \

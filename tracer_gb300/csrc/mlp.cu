@@ -671,7 +671,7 @@ extern "C" {
 
 tr_status tr_guide_init(tr_ctx* ctx, uint64_t seed) {
   if (!ctx) return TR_ERR_ARG;
-  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  TR_DEVICE_SCOPE(ctx);
   tr_status s = guide_reserve(ctx);
   if (s != TR_OK) return s;
   // uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) for weights and biases
@@ -690,7 +690,7 @@ tr_status tr_guide_init(tr_ctx* ctx, uint64_t seed) {
 
 tr_status tr_guide_set_params(tr_ctx* ctx, const float* params, size_t n) {
   if (!ctx || !params || n != (size_t)mlp::kParams) return TR_ERR_ARG;
-  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  TR_DEVICE_SCOPE(ctx);
   tr_status s = guide_reserve(ctx);
   if (s != TR_OK) return s;
   TR_CUDA(ctx, cudaMemcpyAsync(ctx->guide->params.p, params, n * 4, cudaMemcpyHostToDevice, ctx->stream));
@@ -705,7 +705,7 @@ tr_status tr_guide_set_params(tr_ctx* ctx, const float* params, size_t n) {
 tr_status tr_guide_get_params(tr_ctx* ctx, float* params, size_t n) {
   if (!ctx || !params || n != (size_t)mlp::kParams) return TR_ERR_ARG;
   if (!ctx->guide || !ctx->guide->params.p) return set_err(ctx, TR_ERR_STATE, "guide model not initialised");
-  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  TR_DEVICE_SCOPE(ctx);
   TR_CUDA(ctx, cudaMemcpyAsync(params, ctx->guide->params.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
   TR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return TR_OK;
@@ -716,7 +716,7 @@ tr_status tr_guide_forward_dev(tr_ctx* ctx, const float* d_in, size_t n, float* 
   if (!ctx->guide || !ctx->guide->params.p) return set_err(ctx, TR_ERR_STATE, "guide model not initialised");
   if (n > (1u << 30)) return set_err(ctx, TR_ERR_ARG, "too many rows");
   if (n == 0) return TR_OK;
-  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  TR_DEVICE_SCOPE(ctx);
   tr_status s = guide_forward(ctx, d_in, (int)n, d_out, nullptr);
   return s != TR_OK ? s : guide_check(ctx);
 }
@@ -725,7 +725,7 @@ tr_status tr_guide_backward_dev(tr_ctx* ctx, const float* d_in, const float* d_d
   if (!ctx || !d_grads || (n && (!d_in || !d_dout))) return TR_ERR_ARG;
   if (!ctx->guide || !ctx->guide->params.p) return set_err(ctx, TR_ERR_STATE, "guide model not initialised");
   if (n > (1u << 26)) return set_err(ctx, TR_ERR_ARG, "too many rows");
-  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  TR_DEVICE_SCOPE(ctx);
   if (n == 0) {
     TR_CUDA(ctx, cudaMemsetAsync(d_grads, 0, mlp::kParams * 4, ctx->stream));
     return guide_check(ctx);
@@ -739,7 +739,7 @@ tr_status tr_guide_loss_dev(tr_ctx* ctx, const float* d_in, const float* d_dir, 
   if (!ctx || !loss || !d_dout || n == 0 || !d_in || !d_dir || !d_weight) return TR_ERR_ARG;
   if (!ctx->guide || !ctx->guide->params.p) return set_err(ctx, TR_ERR_STATE, "guide model not initialised");
   if (n > (1u << 26)) return set_err(ctx, TR_ERR_ARG, "too many rows");
-  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  TR_DEVICE_SCOPE(ctx);
   tr_status s = guide_loss(ctx, d_in, d_dir, d_weight, (int)n);
   if (s != TR_OK) return s;
   TR_CUDA(ctx, cudaMemcpyAsync(d_dout, ctx->guide->dout.p, n * mlp::kOut * 4, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -752,7 +752,7 @@ tr_status tr_guide_train_step_dev(tr_ctx* ctx, const float* d_in, const float* d
   if (!ctx || n == 0 || !d_in || !d_dir || !d_weight || !(lr > 0.0f)) return TR_ERR_ARG;
   if (!ctx->guide || !ctx->guide->params.p) return set_err(ctx, TR_ERR_STATE, "guide model not initialised");
   if (n > (1u << 26)) return set_err(ctx, TR_ERR_ARG, "too many rows");
-  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  TR_DEVICE_SCOPE(ctx);
   tr_status s = guide_train_step(ctx, d_in, d_dir, d_weight, (int)n, lr);
   if (s != TR_OK) return s;
   float l = 0.0f;

@@ -105,7 +105,7 @@ extern "C" tr_status tr_film_resolve_dev(tr_ctx* ctx, const float* d_rgbw, const
   if (pixels == 0) return TR_OK;
   if (!post::aligned(d_rgbw ? (const void*)d_rgbw : (const void*)d_rgbw64, 16))
     return set_err(ctx, TR_ERR_ARG, "film buffer must be 16-byte aligned");
-  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  TR_DEVICE_SCOPE(ctx);
   post::k_resolve<<<post::grid(ctx, pixels), 256, 0, ctx->stream>>>(
       reinterpret_cast<const float4*>(d_rgbw), reinterpret_cast<const double2*>(d_rgbw64), pixels, d_rgb);
   TR_CUDA(ctx, cudaGetLastError());
@@ -116,7 +116,7 @@ extern "C" tr_status tr_aces_tone_map_dev(tr_ctx* ctx, float* d_rgb, size_t pixe
   if (!ctx || (pixels && !d_rgb)) return TR_ERR_ARG;
   if (pixels == 0) return TR_OK;
   if (exposure < 0.0f) exposure = 1.0f;  // ACESToneMapper's constructor resets an invalid exposure
-  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  TR_DEVICE_SCOPE(ctx);
   post::k_aces<<<post::grid(ctx, 3 * pixels), 256, 0, ctx->stream>>>(d_rgb, 3 * pixels, exposure);
   TR_CUDA(ctx, cudaGetLastError());
   return TR_OK;
@@ -126,7 +126,7 @@ extern "C" tr_status tr_gamma_correct_dev(tr_ctx* ctx, float* d_rgb, size_t pixe
   if (!ctx || (pixels && !d_rgb)) return TR_ERR_ARG;
   if (pixels == 0) return TR_OK;
   if (!(gamma > 0.0f)) gamma = 1.0f;  // GammaCorrector's constructor resets an invalid gamma
-  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  TR_DEVICE_SCOPE(ctx);
   post::k_gamma<<<post::grid(ctx, 3 * pixels), 256, 0, ctx->stream>>>(d_rgb, 3 * pixels, gamma);
   TR_CUDA(ctx, cudaGetLastError());
   return TR_OK;
@@ -136,7 +136,7 @@ extern "C" tr_status tr_to_rgb8_dev(tr_ctx* ctx, const float* d_rgb, size_t pixe
                                     uint8_t* d_rgb8) {
   if (!ctx || (pixels && (!d_rgb || !d_rgb8))) return TR_ERR_ARG;
   if (pixels == 0) return TR_OK;
-  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  TR_DEVICE_SCOPE(ctx);
   post::k_rgb8<<<post::grid(ctx, 3 * pixels), 256, 0, ctx->stream>>>(d_rgb, 3 * pixels, inv_gamma, d_rgb8);
   TR_CUDA(ctx, cudaGetLastError());
   return TR_OK;
@@ -146,7 +146,7 @@ extern "C" tr_status tr_to_rgbe_dev(tr_ctx* ctx, const float* d_rgb, size_t pixe
   if (!ctx || (pixels && (!d_rgb || !d_rgbe))) return TR_ERR_ARG;
   if (pixels == 0) return TR_OK;
   if (!post::aligned(d_rgbe, 4)) return set_err(ctx, TR_ERR_ARG, "RGBE buffer must be 4-byte aligned");
-  TR_CUDA(ctx, cudaSetDevice(ctx->device));
+  TR_DEVICE_SCOPE(ctx);
   post::k_rgbe<<<post::grid(ctx, pixels), 256, 0, ctx->stream>>>(d_rgb, pixels, reinterpret_cast<uchar4*>(d_rgbe));
   TR_CUDA(ctx, cudaGetLastError());
   return TR_OK;

@@ -59,7 +59,9 @@ enum : int {
 constexpr int kMaxSpecularDepth = 20;
 
 // P1.w holds the path depth (low 16 bits) and the count of delta samples
-// that did not count toward it (high bits).
+// that did not count toward it (high bits). The depth must stay below 2^16
+// with the uncounted delta samples on top: larger max_depth is rejected.
+constexpr int kMaxPathDepth = 0xffff - kMaxSpecularDepth;
 __device__ __forceinline__ int path_depth(float w) { return __float_as_int(w) & 0xffff; }
 __device__ __forceinline__ int spec_depth(float w) { return __float_as_int(w) >> 16; }
 
@@ -1192,6 +1194,8 @@ static tr_status validate_job(tr_ctx* ctx, const JobSpec& j) {
   if (j.scene < 0 || j.scene >= ctx->dsc.num_scenes) return set_err(ctx, TR_ERR_ARG, "scene index out of range");
   if (prm->width <= 0 || prm->height <= 0 || prm->spp <= 0 || prm->max_depth < 0)
     return set_err(ctx, TR_ERR_ARG, "invalid render size, spp or depth");
+  if (prm->max_depth > kMaxPathDepth)
+    return set_err(ctx, TR_ERR_ARG, "max_depth above 65515 (the path depth is kept in 16 bits)");
   if ((long long)prm->width * prm->height > (1ll << 28)) return set_err(ctx, TR_ERR_ARG, "film too large");
   if (prm->direct_light_sample_num != 1)
     return set_err(ctx, TR_ERR_UNSUPPORTED, "direct_light_sample_num must be 1 on the GPU path");
@@ -1237,7 +1241,7 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     if (v != TR_OK) return v;
     if (!jobs[k].film && njobs != 1) return set_err(ctx, TR_ERR_ARG, "batch jobs need device films");
     total += (long long)jobs[k].prm.width * jobs[k].prm.height;
-    max_iters = std::max(max_iters, (long long)jobs[k].prm.spp * (jobs[k].prm.max_depth + 2 + extra) + 4);
+    max_iters = std::max(max_iters, (long long)jobs[k].prm.spp * ((long long)jobs[k].prm.max_depth + 2 + extra) + 4);
   }
   if (total > (1ll << 28)) return set_err(ctx, TR_ERR_ARG, "batch too large");
   const int n = (int)total;
@@ -1336,7 +1340,10 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   }
 
   int sms = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  {
+    const cudaError_t ae = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (ae != cudaSuccess) return cuda_fail(ctx, ae, "cudaDeviceGetAttribute(multiprocessor count)");
+  }
   if (sms <= 0) sms = 1;
   const int grid = sms * ctx->tune.shade_blocks_per_sm, grid_init = sms * 8;
   const int grid_ext = traversal_grid(ctx, (const void*)k_extend<false>);
@@ -1558,7 +1565,7 @@ extern "C" {
 tr_status tr_render_dev(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter, const tr_render_params* params,
                         float* d_rgbw, double* d_rgbw64, tr_stats* stats) {
   if (!ctx || !cam || !filter || !params || ((d_rgbw == nullptr) == (d_rgbw64 == nullptr))) return TR_ERR_ARG;
-  cudaSetDevice(ctx->device);
+  TR_DEVICE_SCOPE(ctx);
   void* out = d_rgbw ? (void*)d_rgbw : (void*)d_rgbw64;
   if (((uintptr_t)out & 15u) != 0) return set_err(ctx, TR_ERR_ARG, "film buffer must be 16-byte aligned");
   return render_impl(ctx, cam, filter, params, out, d_rgbw64 != nullptr, stats);
@@ -1567,7 +1574,7 @@ tr_status tr_render_dev(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filt
 tr_status tr_render(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter, const tr_render_params* params,
                     float* rgbw, double* rgbw64, tr_stats* stats) {
   if (!ctx || !cam || !filter || !params || ((rgbw == nullptr) == (rgbw64 == nullptr))) return TR_ERR_ARG;
-  cudaSetDevice(ctx->device);
+  TR_DEVICE_SCOPE(ctx);
   tr_status s = render_impl(ctx, cam, filter, params, nullptr, rgbw64 != nullptr, stats);
   if (s != TR_OK) return s;
   const size_t n = (size_t)params->width * params->height;
@@ -1612,6 +1619,8 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   if (!ctx->has_scene) return set_err(ctx, TR_ERR_STATE, "no scene uploaded");
   if (prm->width <= 0 || prm->height <= 0 || prm->spp <= 0 || prm->max_depth < 0)
     return set_err(ctx, TR_ERR_ARG, "invalid render size, spp or depth");
+  if (prm->max_depth > kMaxPathDepth)
+    return set_err(ctx, TR_ERR_ARG, "max_depth above 65515 (the path depth is kept in 16 bits)");
   if (prm->direct_light_sample_num != 1)
     return set_err(ctx, TR_ERR_UNSUPPORTED, "direct_light_sample_num must be 1 on the GPU path");
   if (!(filter->radius > 0.0f) || filter->radius > 16.0f) return set_err(ctx, TR_ERR_ARG, "invalid filter radius");
@@ -1708,7 +1717,10 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   P.stats = reinterpret_cast<unsigned long long*>(base + oSt);
 
   int sms = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  {
+    const cudaError_t ae = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (ae != cudaSuccess) return cuda_fail(ctx, ae, "cudaDeviceGetAttribute(multiprocessor count)");
+  }
   if (sms <= 0) sms = 1;
   const int grid = sms * ctx->tune.shade_blocks_per_sm, grid_init = sms * 8;
   const int grid_ext = traversal_grid(ctx, (const void*)k_extend<false>);
@@ -1722,11 +1734,18 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   k_init<<<grid_init, 256, 0, st>>>(P);
   NCHK(cudaGetLastError());
   // Every slot finishes within spp * (max_depth + 2) iterations (plus the
-  // delta samples that do not count toward the depth); iterations past the
-  // drain find empty queues and return at once.
+  // delta samples that do not count toward the depth): that bound is the
+  // ceiling. Every kDrainCheck iterations the live-slot count is copied into
+  // a host stack variable (a pageable copy: nothing is allocated), and the
+  // loop stops once the wavefront has drained or tr_cancel was called.
   const long long iters =
-      (long long)prm->spp * (prm->max_depth + 2 + (ctx->dsc.has_glass ? kMaxSpecularDepth : 0)) + 4;
-  for (long long it = 0; it < iters; ++it) {
+      (long long)prm->spp * ((long long)prm->max_depth + 2 + (ctx->dsc.has_glass ? kMaxSpecularDepth : 0)) + 4;
+  constexpr int kDrainCheck = 16;  // even: the count read is the list the next iteration starts from
+  ctx->cancel.store(0);
+  long long it = 0;
+  unsigned int live = 1;
+  bool cancelled = false;
+  while (it < iters && live != 0 && !cancelled) {
     const int cur = (int)(it & 1), nxt = cur ^ 1;
     k_extend<false><<<grid_ext, 128, 0, st>>>(P, cur);
     NCHK(cudaMemsetAsync(P.ctr + C_EXT + nxt, 0, 4, st));
@@ -1744,6 +1763,13 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
     if (P.sc.has_disney15) k_nee<MAT_DISNEY15><<<grid, 128, 0, st>>>(P);
     if (wide) k_shadow<false, true><<<grid_sh, 128, 0, st>>>(P);
     else k_shadow<false><<<grid_sh, 128, 0, st>>>(P);
+    ++it;
+    if (it % kDrainCheck == 0 || it == iters) {
+      NCHK(cudaGetLastError());
+      NCHK(cudaMemcpyAsync(&live, P.ctr + C_ACT + (int)(it & 1), 4, cudaMemcpyDeviceToHost, st));
+      NCHK(cudaStreamSynchronize(st));
+      cancelled = ctx->cancel.load() != 0;
+    }
   }
   NCHK(cudaGetLastError());
   NCHK(cudaStreamSynchronize(st));
@@ -1758,10 +1784,11 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
     stats->extend_rays = hs[1];
     stats->shadow_rays = hs[2];
     stats->shade_items = hs[3];
-    stats->iterations = (uint64_t)iters;
+    stats->iterations = (uint64_t)it;
   }
   if (ctrs[C_ERR] != 0) return set_err(ctx, TR_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
-  if (ctrs[C_ACT + (int)(iters & 1)] != 0)
+  if (cancelled) return set_err(ctx, TR_ERR_CANCELLED, "render cancelled");
+  if (ctrs[C_ACT + (int)(it & 1)] != 0)
     return set_err(ctx, TR_ERR_TIMEOUT, "wavefront did not drain within its iteration bound");
   return TR_OK;
 }
@@ -1770,8 +1797,7 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
 
 extern "C" tr_status tr_render_batch_dev(tr_ctx* ctx, const tr_batch_job* jobs, uint32_t n, tr_stats* stats) {
   if (!ctx || !jobs || n == 0 || n > (1u << 20)) return TR_ERR_ARG;
-  cudaError_t e = cudaSetDevice(ctx->device);
-  if (e != cudaSuccess) return trg::cuda_fail(ctx, e, "cudaSetDevice");
+  TR_DEVICE_SCOPE(ctx);
   std::vector<trg::JobSpec> spec(n);
   for (uint32_t k = 0; k < n; ++k) {
     if (!jobs[k].d_rgbw) return trg::set_err(ctx, TR_ERR_ARG, "batch job without a film");
@@ -1851,8 +1877,8 @@ extern "C" tr_status tr_render_guided_dev(tr_ctx* ctx, const tr_camera* cam, con
                                           const tr_render_params* params, const tr_guide_params* guide,
                                           float* d_rgbw, double* d_rgbw64, tr_stats* stats) {
   if (!ctx || !cam || !filter || !params || !guide || ((d_rgbw == nullptr) == (d_rgbw64 == nullptr))) return TR_ERR_ARG;
-  cudaError_t e = cudaSetDevice(ctx->device);
-  if (e != cudaSuccess) return trg::cuda_fail(ctx, e, "cudaSetDevice");
+  TR_DEVICE_SCOPE(ctx);
+  cudaError_t e;
   void* out = d_rgbw ? (void*)d_rgbw : (void*)d_rgbw64;
   if (((uintptr_t)out & 15u) != 0) return trg::set_err(ctx, TR_ERR_ARG, "film buffer must be 16-byte aligned");
   return trg::render_impl(ctx, cam, filter, params, out, d_rgbw64 != nullptr, stats, guide);
@@ -1863,8 +1889,8 @@ extern "C" tr_status tr_guide_train_on_records(tr_ctx* ctx, int32_t steps, uint3
   if (!ctx || steps < 0 || batch == 0 || batch > (1u << 22) || !(lr > 0.0f)) return TR_ERR_ARG;
   if (!ctx->guide || !ctx->guide->params.p) return trg::set_err(ctx, TR_ERR_STATE, "guide model not initialised");
   if (!ctx->rb || ctx->rb->tb_count == 0) return trg::set_err(ctx, TR_ERR_STATE, "no training records");
-  cudaError_t e = cudaSetDevice(ctx->device);
-  if (e != cudaSuccess) return trg::cuda_fail(ctx, e, "cudaSetDevice");
+  TR_DEVICE_SCOPE(ctx);
+  cudaError_t e;
   trg::RenderBuffers* rb = ctx->rb;
   const float* in = rb->tb.as<float>();
   const float* dir = in + (size_t)rb->tb_cap * 7;
@@ -1885,7 +1911,6 @@ extern "C" tr_status tr_render_dev_noalloc(tr_ctx* ctx, const tr_camera* cam, co
                                            const tr_render_params* params, float* d_rgbw, tr_stats* stats) {
   if (!ctx || !cam || !filter || !params || !d_rgbw) return TR_ERR_ARG;
   if (((uintptr_t)d_rgbw & 15u) != 0) return trg::set_err(ctx, TR_ERR_ARG, "film buffer must be 16-byte aligned");
-  cudaError_t e = cudaSetDevice(ctx->device);
-  if (e != cudaSuccess) return trg::cuda_fail(ctx, e, "cudaSetDevice");
+  TR_DEVICE_SCOPE(ctx);
   return trg::render_noalloc_impl(ctx, cam, filter, params, d_rgbw, stats);
 }

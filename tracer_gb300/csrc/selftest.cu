@@ -122,7 +122,7 @@ using namespace trg;
 
 extern "C" tr_status tr_selftest(tr_ctx* ctx, int which, uint64_t n, uint64_t seed, uint64_t* mismatches) {
   if (!ctx || !mismatches || which < 0 || which > 7) return TR_ERR_ARG;
-  cudaSetDevice(ctx->device);
+  TR_DEVICE_SCOPE(ctx);
   unsigned long long* d_bad = nullptr;
   cudaError_t e = cudaMalloc(&d_bad, sizeof(unsigned long long));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "selftest counter");
