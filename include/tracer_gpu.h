@@ -256,13 +256,23 @@ tr_status tr_synchronize(tr_ctx* ctx);
  *    primitive tests before an early exit and the visit counts differ.
  *    Closest-hit traversal always keeps the reference's binary order (it
  *    decides which of two equal-distance primitives is reported). A scene
- *    whose collapsed tree could overflow the traversal stack uses width 2. */
+ *    whose collapsed tree could overflow the traversal stack uses width 2.
+ *  - ray_bin_bits (0..5): before each traversal launch of a render, its
+ *    queue of rays is regrouped by direction octant and the origin's cell in
+ *    a 2^b x 2^b x 2^b grid over the scene box (0: queue order). Each ray's
+ *    result is unchanged; warps walk more alike paths.
+ *  - treelet_nodes (0..1024): the top of the closest-hit tree (this many
+ *    child-pair nodes, breadth first from the root) is staged in shared
+ *    memory by every block of the traversal kernels (0: all nodes are read
+ *    from global memory). */
 typedef struct tr_tuning {
   int32_t trav_refill_lanes;
   int32_t trav_blocks_per_sm;
   int32_t shade_blocks_per_sm;
   int32_t graph_iterations;
   int32_t any_node_width;
+  int32_t ray_bin_bits;
+  int32_t treelet_nodes;
 } tr_tuning;
 tr_status tr_ctx_set_tuning(tr_ctx* ctx, const tr_tuning* t);
 tr_status tr_ctx_get_tuning(const tr_ctx* ctx, tr_tuning* t);

@@ -25,7 +25,8 @@ class tuned:
     """Context manager: the GPU context's launch tuning with some fields
     changed, restored afterwards (the `gpu` fixture is shared)."""
 
-    FIELDS = ("trav_refill_lanes", "trav_blocks_per_sm", "shade_blocks_per_sm", "graph_iterations", "any_node_width")
+    FIELDS = ("trav_refill_lanes", "trav_blocks_per_sm", "shade_blocks_per_sm", "graph_iterations", "any_node_width",
+              "ray_bin_bits", "treelet_nodes")
 
     def __init__(self, gpu, **fields):
         self.gpu, self.fields = gpu, fields
@@ -40,4 +41,4 @@ class tuned:
 
     def _apply(self, v):
         self.gpu.set_tuning(v["trav_refill_lanes"], v["trav_blocks_per_sm"], v["shade_blocks_per_sm"],
-                            v["graph_iterations"], v["any_node_width"])
+                            v["graph_iterations"], v["any_node_width"], v["ray_bin_bits"], v["treelet_nodes"])

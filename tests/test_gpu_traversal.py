@@ -195,3 +195,34 @@ def test_four_wide_any_hit_equals_the_oracle(gpu, case):
         got = gpu.trace_any(rays)
     print(case, "occluded", int(want.sum()), "of", len(rays))
     assert np.array_equal(want, got)
+
+
+@pytest.mark.parametrize("bits,treelet", [(3, 0), (0, 64), (4, 256), (5, 1024), (2, 1)])
+def test_binning_and_treelet_keep_results(gpu, bits, treelet):
+    """Ray binning (the queue visited in octant/cell order) and the
+    shared-memory treelet (the top of the tree read from shared memory)
+    change only the order of work and where nodes are read from: hits stay
+    bit-exact, on random scenes with spheres, the traversal workload and the
+    occluded room."""
+    from conftest import tuned
+    rng = np.random.default_rng(bits * 100 + treelet)
+    cases = [(scenes.random_scene(bits, n_tris=300, n_spheres=20), _random_rays(rng, 20000),
+              _random_rays(rng, 20000, shadow=True)),
+             (scenes.traversal(1 << 15, seed=2), scenes.traversal_rays(1 << 15, seed=2),
+              scenes.traversal_rays(1 << 15, seed=2, shadow=True))]
+    room = scenes.occluded_room(32, 24, 1, n_tris=30000)[0]
+    o = rng.uniform([-3.9, 0.1, -2.9], [3.9, 3.9, 2.9], (20000, 3)).astype(np.float32)
+    tgt = rng.uniform([4.5, 0.5, -1.5], [7.5, 3.5, 1.5], (20000, 3)).astype(np.float32)
+    cases.append((room, scenes.make_rays(o, rng.normal(size=(20000, 3)).astype(np.float32), 0.0, scenes.F32_MAX),
+                  scenes.make_rays(o, tgt - o, 0.0, np.linalg.norm(tgt - o, axis=1).astype(np.float32) * 0.999)))
+    for sc, rays, srays in cases:
+        orc = oracle.Oracle(sc, "port")
+        p0, t0 = orc.trace_closest(rays)
+        h0 = orc.trace_any(srays)
+        gpu.upload(sc)
+        with tuned(gpu, ray_bin_bits=bits, treelet_nodes=treelet):
+            for width in (2, 4):
+                with tuned(gpu, any_node_width=width):
+                    p1, t1 = gpu.trace_closest(rays)
+                    assert np.array_equal(p0, p1) and _same_bits(t0, t1)
+                    assert np.array_equal(h0, gpu.trace_any(srays))

@@ -463,6 +463,10 @@ tr_status upload_device_built(tr_ctx* ctx) {
   DScene& sc = ctx->dsc;
   sc.nodes = ctx->d_nodes.as<DNode>();
   sc.nodes4 = nullptr;
+  sc.treelet = nullptr;  // no host copy of the device-built tree to stage from
+  sc.treelet_n = 0;
+  hs.dnodes.clear();
+  hs.root0 = -1;
   sc.slots = ctx->d_slots.as<float4>();
   sc.spheres = ctx->d_spheres.as<DSphere>();
   sc.prims = ctx->d_prims.as<DPrim>();

@@ -17,6 +17,7 @@
 #include <string>
 #include <vector>
 
+#include "binning.cuh"
 #include "bvh_build.h"
 #include "context.h"
 #include "traverse.cuh"
@@ -345,10 +346,14 @@ tr_status upload_device_tables(tr_ctx* ctx) {
   ctx->any4_stack = stack4;
   TR_CUDA(ctx, put(ctx->d_roots, roots.data(), roots.size() * sizeof(SceneRoot)));
   TR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  hs.root0 = nsc == 1 && roots[0].kind == 1 ? roots[0].offset : -1;
+  hs.dnodes = std::move(dn);
 
   DScene& sc = ctx->dsc;
   sc.nodes = ctx->d_nodes.as<DNode>();
   sc.nodes4 = wide ? ctx->d_nodes4.as<DNode4>() : nullptr;
+  sc.treelet = nullptr;
+  sc.treelet_n = 0;
   sc.slots = ctx->d_slots.as<float4>();
   sc.spheres = ctx->d_spheres.as<DSphere>();
   sc.prims = ctx->d_prims.as<DPrim>();
@@ -370,8 +375,54 @@ tr_status upload_device_tables(tr_ctx* ctx) {
   if (es != TR_OK) return es;
   es = upload_textures(ctx);
   if (es != TR_OK) return es;
+  es = upload_treelet(ctx);
+  if (es != TR_OK) return es;
   ctx->has_scene = true;
   return TR_OK;
+}
+
+tr_status upload_treelet(tr_ctx* ctx) {
+  DScene& sc = ctx->dsc;
+  sc.treelet = nullptr;
+  sc.treelet_n = 0;
+  const HostScene& hs = ctx->hs;
+  const int want = ctx->tune.treelet_nodes;
+  if (want <= 0 || hs.root0 < 0 || hs.dnodes.size() >= (size_t)kTreeletRef) return TR_OK;
+  // breadth first from the root: node `order[i]` becomes treelet node i
+  std::vector<int> order{hs.root0};
+  std::vector<int> at(hs.dnodes.size(), -1);
+  at[hs.root0] = 0;
+  for (size_t h = 0; h < order.size(); ++h) {
+    const DNode& d = hs.dnodes[order[h]];
+    const unsigned cc = (unsigned)d.d.z;
+    const int child[2] = {d.d.x, d.d.y};
+    const bool interior[2] = {(cc & 0xffffu) == 0, (cc >> 16) == 0};
+    for (int c = 0; c < 2; ++c)
+      if (interior[c] && (int)order.size() < want) {
+        at[child[c]] = (int)order.size();
+        order.push_back(child[c]);
+      }
+  }
+  std::vector<DNode> tl(order.size());
+  for (size_t i = 0; i < order.size(); ++i) {
+    DNode d = hs.dnodes[order[i]];
+    const unsigned cc = (unsigned)d.d.z;
+    if ((cc & 0xffffu) == 0 && at[d.d.x] >= 0) d.d.x = kTreeletRef | at[d.d.x];
+    if ((cc >> 16) == 0 && at[d.d.y] >= 0) d.d.y = kTreeletRef | at[d.d.y];
+    tl[i] = d;
+  }
+  TR_CUDA(ctx, ctx->d_treelet.reserve(tl.size() * sizeof(DNode)));
+  TR_CUDA(ctx, cudaMemcpyAsync(ctx->d_treelet.p, tl.data(), tl.size() * sizeof(DNode), cudaMemcpyHostToDevice,
+                               ctx->stream));
+  TR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  sc.treelet = ctx->d_treelet.as<DNode>();
+  sc.treelet_n = (int)tl.size();
+  return TR_OK;
+}
+
+cudaError_t allow_dynamic_smem(const void* kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
 tr_status upload_textures(tr_ctx* ctx) {
@@ -484,16 +535,19 @@ struct BatchJob {
   int32_t* prim;  // closest: prim id and t (prim, tout); any: hit flags (hit); all null: no output
   float* tout;
   uint8_t* hit;
+  const int* perm;  // ray binning: work item i is ray perm[i] (null: ray i)
   __device__ __forceinline__ unsigned int count() const { return n; }
-  __device__ __forceinline__ void load(unsigned int i, f3& o, f3& d, float& t_min, float& t_max, int& scene) const {
+  __device__ __forceinline__ void load(unsigned int w, f3& o, f3& d, float& t_min, float& t_max, int& scene) const {
     scene = 0;
+    const unsigned int i = perm ? (unsigned int)perm[w] : w;
     const float4 r0 = __ldg(rays + 2 * (size_t)i), r1 = __ldg(rays + 2 * (size_t)i + 1);
     o = mk3(r0.x, r0.y, r0.z);
     d = mk3(r0.w, r1.x, r1.y);
     t_min = r1.z;
     t_max = r1.w;
   }
-  __device__ __forceinline__ void store(unsigned int i, const Hit& h, float t_max, bool occluded) const {
+  __device__ __forceinline__ void store(unsigned int w, const Hit& h, float t_max, bool occluded) const {
+    const unsigned int i = perm ? (unsigned int)perm[w] : w;
     if (prim) {
       prim[i] = h.prim;
       tout[i] = t_max;
@@ -503,20 +557,34 @@ struct BatchJob {
   }
 };
 
+// The caller's ray array as a source of ray binning (binning.cuh).
+struct BatchSrc {
+  const float4* rays;
+  unsigned int n;
+  __device__ __forceinline__ unsigned int count() const { return n; }
+  __device__ __forceinline__ int item(unsigned int i) const { return (int)i; }
+  __device__ __forceinline__ void ray(unsigned int i, f3& o, f3& d, int& scene) const {
+    scene = 0;
+    const float4 r0 = __ldg(rays + 2 * (size_t)i), r1 = __ldg(rays + 2 * (size_t)i + 1);
+    o = mk3(r0.x, r0.y, r0.z);
+    d = mk3(r0.w, r1.x, r1.y);
+  }
+};
+
 template <bool ANY, bool WIDE = false>
 __global__ void __launch_bounds__(128) k_trace_batch(DScene sc, BatchJob job, unsigned int* fetch, int* err,
-                                                    int refill) {
+                                                    int refill, int tl_n) {
   VisitCount vc;
-  persistent_traverse<ANY, false, WIDE>(sc, job, fetch, err, vc, refill);
+  persistent_traverse<ANY, false, WIDE>(sc, job, fetch, err, vc, refill, tl_n);
 }
 
 // The same traversal counting boxes and primitives tested (all lanes leave
 // the persistent loop together, so the warp reduction sees every lane).
 template <bool ANY, bool WIDE = false>
 __global__ void __launch_bounds__(128) k_trace_count(DScene sc, BatchJob job, unsigned int* fetch, int* err,
-                                                    int refill, unsigned long long* counts) {
+                                                    int refill, unsigned long long* counts, int tl_n) {
   VisitCount vc;
-  persistent_traverse<ANY, true, WIDE>(sc, job, fetch, err, vc, refill);
+  persistent_traverse<ANY, true, WIDE>(sc, job, fetch, err, vc, refill, tl_n);
   const unsigned int b = __reduce_add_sync(0xffffffffu, vc.boxes), p = __reduce_add_sync(0xffffffffu, vc.prims);
   if ((threadIdx.x & 31u) == 0) {
     atomicAdd(counts, (unsigned long long)b);
@@ -524,17 +592,61 @@ __global__ void __launch_bounds__(128) k_trace_count(DScene sc, BatchJob job, un
   }
 }
 
-int traversal_grid(const tr_ctx* ctx, const void* kernel) {
+int traversal_grid(const tr_ctx* ctx, const void* kernel, size_t smem) {
   int sms = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess) {
+    cudaGetLastError();
+    sms = 1;
+  }
   int per_sm = ctx->tune.trav_blocks_per_sm;
   if (per_sm <= 0) {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0) != cudaSuccess || per_sm <= 0) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, smem) != cudaSuccess || per_sm <= 0) {
       cudaGetLastError();
       per_sm = 4;
     }
   }
   return std::max(sms, 1) * per_sm;
+}
+
+// Launches the persistent traversal of `job` (counts: the counting kernel,
+// which adds boxes and primitives tested there) on the context stream: the
+// tuned grid, the shared-memory treelet for binary walks, and -- with
+// ray_bin_bits -- the rays visited in binned order.
+template <bool ANY, bool WIDE>
+tr_status launch_trace(tr_ctx* ctx, BatchJob& job, unsigned long long* counts) {
+  cudaStream_t st = ctx->stream;
+  unsigned int* fetch = reinterpret_cast<unsigned int*>(ctx->d_err.as<int>() + 1);
+  TR_CUDA(ctx, cudaMemsetAsync(fetch, 0, sizeof(int), st));  // work-fetch position
+  const int bits = ctx->tune.ray_bin_bits;
+  if (bits > 0) {
+    const int nb = 1 << (3 + 3 * bits);
+    TR_CUDA(ctx, ctx->d_perm.reserve((size_t)job.n * 4));
+    TR_CUDA(ctx, ctx->d_bin_key.reserve((size_t)job.n * 4));
+    TR_CUDA(ctx, ctx->d_bin_cnt.reserve((size_t)nb * 4));
+    unsigned int* cnt = ctx->d_bin_cnt.as<unsigned int>();
+    unsigned int* keys = ctx->d_bin_key.as<unsigned int>();
+    int sms = 1;
+    TR_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    const BatchSrc src{job.rays, job.n};
+    TR_CUDA(ctx, cudaMemsetAsync(cnt, 0, (size_t)nb * 4, st));
+    k_bin_count<<<sms * 8, 128, 0, st>>>(src, ctx->dsc, cnt, keys, bits);
+    k_bin_scan<<<1, kBinScanThreads, 0, st>>>(cnt, nb);
+    k_bin_scatter<<<sms * 8, 128, 0, st>>>(src, cnt, keys, ctx->d_perm.as<int>());
+    job.perm = ctx->d_perm.as<int>();
+  }
+  const int tl = WIDE ? 0 : treelet_nodes(ctx);
+  const size_t smem = (size_t)tl * sizeof(DNode);
+  const void* k = counts ? (const void*)k_trace_count<ANY, WIDE> : (const void*)k_trace_batch<ANY, WIDE>;
+  TR_CUDA(ctx, allow_dynamic_smem(k, smem));
+  const int grid = traversal_grid(ctx, k, smem);
+  if (counts)
+    k_trace_count<ANY, WIDE><<<grid, 128, smem, st>>>(ctx->dsc, job, fetch, ctx->d_err.as<int>(),
+                                                      ctx->tune.trav_refill_lanes, counts, tl);
+  else
+    k_trace_batch<ANY, WIDE><<<grid, 128, smem, st>>>(ctx->dsc, job, fetch, ctx->d_err.as<int>(),
+                                                      ctx->tune.trav_refill_lanes, tl);
+  TR_CUDA(ctx, cudaGetLastError());
+  return TR_OK;
 }
 
 }  // namespace trg
@@ -601,7 +713,8 @@ void tr_ctx_destroy(tr_ctx* ctx) {
   release_guide(ctx);
   for (DevBuf* b : {&ctx->d_nodes, &ctx->d_nodes4, &ctx->d_slots, &ctx->d_spheres, &ctx->d_prims, &ctx->d_tshade,
                     &ctx->d_mats, &ctx->d_lights, &ctx->d_roots, &ctx->d_rays, &ctx->d_out0, &ctx->d_out1,
-                    &ctx->d_err, &ctx->d_env_pool, &ctx->d_envs, &ctx->d_tex_pool, &ctx->d_texs})
+                    &ctx->d_err, &ctx->d_env_pool, &ctx->d_envs, &ctx->d_tex_pool, &ctx->d_texs, &ctx->d_treelet,
+                    &ctx->d_perm, &ctx->d_bin_key, &ctx->d_bin_cnt})
     b->release();
   cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -614,9 +727,15 @@ tr_status tr_ctx_set_tuning(tr_ctx* ctx, const tr_tuning* t) {
   if (!ctx || !t) return TR_ERR_ARG;
   if (t->trav_refill_lanes < 1 || t->trav_refill_lanes > 32 || t->trav_blocks_per_sm < 0 ||
       t->trav_blocks_per_sm > 64 || t->shade_blocks_per_sm < 1 || t->shade_blocks_per_sm > 64 ||
-      t->graph_iterations < 0 || t->graph_iterations > 64 || (t->any_node_width != 2 && t->any_node_width != 4))
+      t->graph_iterations < 0 || t->graph_iterations > 64 || (t->any_node_width != 2 && t->any_node_width != 4) ||
+      t->ray_bin_bits < 0 || t->ray_bin_bits > kBinBitsMax || t->treelet_nodes < 0 || t->treelet_nodes > kTreeletMax)
     return set_err(ctx, TR_ERR_ARG, "tuning out of range");
+  const bool restage = t->treelet_nodes != ctx->tune.treelet_nodes;
   ctx->tune = *t;
+  if (restage && ctx->has_scene) {
+    TR_DEVICE_SCOPE(ctx);
+    return upload_treelet(ctx);
+  }
   return TR_OK;
 }
 
@@ -1014,13 +1133,9 @@ tr_status tr_trace_closest_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, int3
   if (n == 0) return TR_OK;
   if (n > 0x7fffffffull) return set_err(ctx, TR_ERR_ARG, "too many rays");
   if (((uintptr_t)d_rays & 15u) != 0) return set_err(ctx, TR_ERR_ARG, "ray buffer must be 16-byte aligned");
-  TR_CUDA(ctx, cudaMemsetAsync(ctx->d_err.as<int>() + 1, 0, sizeof(int), ctx->stream));  // fetch position
-  const BatchJob job{reinterpret_cast<const float4*>(d_rays), (unsigned int)n, d_prim, d_t, nullptr};
-  k_trace_batch<false><<<traversal_grid(ctx, (const void*)k_trace_batch<false>), 128, 0, ctx->stream>>>(
-      ctx->dsc, job, reinterpret_cast<unsigned int*>(ctx->d_err.as<int>() + 1), ctx->d_err.as<int>(),
-      ctx->tune.trav_refill_lanes);
-  TR_CUDA(ctx, cudaGetLastError());
-  return TR_OK;
+  TR_DEVICE_SCOPE(ctx);
+  BatchJob job{reinterpret_cast<const float4*>(d_rays), (unsigned int)n, d_prim, d_t, nullptr, nullptr};
+  return launch_trace<false, false>(ctx, job, nullptr);
 }
 
 tr_status tr_trace_any_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, uint8_t* d_hit) {
@@ -1029,17 +1144,10 @@ tr_status tr_trace_any_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, uint8_t*
   if (n == 0) return TR_OK;
   if (n > 0x7fffffffull) return set_err(ctx, TR_ERR_ARG, "too many rays");
   if (((uintptr_t)d_rays & 15u) != 0) return set_err(ctx, TR_ERR_ARG, "ray buffer must be 16-byte aligned");
-  TR_CUDA(ctx, cudaMemsetAsync(ctx->d_err.as<int>() + 1, 0, sizeof(int), ctx->stream));  // fetch position
-  const BatchJob job{reinterpret_cast<const float4*>(d_rays), (unsigned int)n, nullptr, nullptr, d_hit};
-  unsigned int* fetch = reinterpret_cast<unsigned int*>(ctx->d_err.as<int>() + 1);
-  if (any_wide(ctx))
-    k_trace_batch<true, true><<<traversal_grid(ctx, (const void*)k_trace_batch<true, true>), 128, 0, ctx->stream>>>(
-        ctx->dsc, job, fetch, ctx->d_err.as<int>(), ctx->tune.trav_refill_lanes);
-  else
-    k_trace_batch<true><<<traversal_grid(ctx, (const void*)k_trace_batch<true>), 128, 0, ctx->stream>>>(
-        ctx->dsc, job, fetch, ctx->d_err.as<int>(), ctx->tune.trav_refill_lanes);
-  TR_CUDA(ctx, cudaGetLastError());
-  return TR_OK;
+  TR_DEVICE_SCOPE(ctx);
+  BatchJob job{reinterpret_cast<const float4*>(d_rays), (unsigned int)n, nullptr, nullptr, d_hit, nullptr};
+  if (any_wide(ctx)) return launch_trace<true, true>(ctx, job, nullptr);
+  return launch_trace<true, false>(ctx, job, nullptr);
 }
 
 tr_status tr_trace_count_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, int32_t any, uint64_t* boxes,
@@ -1055,18 +1163,12 @@ tr_status tr_trace_count_dev(tr_ctx* ctx, const tr_ray* d_rays, size_t n, int32_
   unsigned long long* counts = reinterpret_cast<unsigned long long*>(ctx->d_err.as<char>() + 16);
   TR_CUDA(ctx, cudaMemsetAsync(ctx->d_err.as<int>() + 1, 0, sizeof(int), ctx->stream));
   TR_CUDA(ctx, cudaMemsetAsync(counts, 0, 16, ctx->stream));
-  const BatchJob job{reinterpret_cast<const float4*>(d_rays), (unsigned int)n, nullptr, nullptr, nullptr};
-  unsigned int* fetch = reinterpret_cast<unsigned int*>(ctx->d_err.as<int>() + 1);
-  if (any && any_wide(ctx))
-    k_trace_count<true, true><<<traversal_grid(ctx, (const void*)k_trace_count<true, true>), 128, 0, ctx->stream>>>(
-        ctx->dsc, job, fetch, ctx->d_err.as<int>(), ctx->tune.trav_refill_lanes, counts);
-  else if (any)
-    k_trace_count<true><<<traversal_grid(ctx, (const void*)k_trace_count<true>), 128, 0, ctx->stream>>>(
-        ctx->dsc, job, fetch, ctx->d_err.as<int>(), ctx->tune.trav_refill_lanes, counts);
-  else
-    k_trace_count<false><<<traversal_grid(ctx, (const void*)k_trace_count<false>), 128, 0, ctx->stream>>>(
-        ctx->dsc, job, fetch, ctx->d_err.as<int>(), ctx->tune.trav_refill_lanes, counts);
-  TR_CUDA(ctx, cudaGetLastError());
+  BatchJob job{reinterpret_cast<const float4*>(d_rays), (unsigned int)n, nullptr, nullptr, nullptr, nullptr};
+  tr_status ls;
+  if (any && any_wide(ctx)) ls = launch_trace<true, true>(ctx, job, counts);
+  else if (any) ls = launch_trace<true, false>(ctx, job, counts);
+  else ls = launch_trace<false, false>(ctx, job, counts);
+  if (ls != TR_OK) return ls;
   unsigned long long h[2];
   TR_CUDA(ctx, cudaMemcpyAsync(h, counts, 16, cudaMemcpyDeviceToHost, ctx->stream));
   tr_status s = check_err_word(ctx);

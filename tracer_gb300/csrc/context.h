@@ -65,6 +65,10 @@ struct HostScene {
     std::vector<uint8_t> texels8;
   };
   std::vector<Tex> textures;
+  // the child-pair nodes as uploaded and scene 0's root among them (-1: the
+  // root is a leaf, or the tree was built on the device)
+  std::vector<DNode> dnodes;
+  int root0 = -1;
 };
 
 struct RenderBuffers;  // render.cu
@@ -82,9 +86,11 @@ struct tr_ctx {
   trg::DevBuf d_rays, d_out0, d_out1, d_err;
   trg::DevBuf d_env_pool, d_envs;  // environment lights: texels and tables, DEnv records
   trg::DevBuf d_tex_pool, d_texs;  // material textures: texels, DTex records
+  trg::DevBuf d_treelet;           // the shared-memory treelet (DScene::treelet)
+  trg::DevBuf d_perm, d_bin_key, d_bin_cnt;  // ray binning of tr_trace_*: order, keys, bin counts
   std::atomic<int> cancel{0};
   trg::RenderBuffers* rb = nullptr;
-  tr_tuning tune{20, 0, 16, 8, 2};
+  tr_tuning tune{20, 0, 16, 8, 2, 0, 0};
   int bvh_builder = TR_BVH_REFERENCE;
   size_t any4_nodes = 0;  // four-wide any-hit tree of the uploaded set (0: not available)
   int any4_stack = 0;     // its traversal stack bound
@@ -100,8 +106,15 @@ tr_status upload_device_built(tr_ctx* ctx);  // bvh_gpu.cu: the TR_BVH_DEVICE pa
 tr_status upload_envs(tr_ctx* ctx);
 // Uploads the set's material textures and sets the scene's textures / has_textures.
 tr_status upload_textures(tr_ctx* ctx);
-// Grid of a persistent traversal kernel: SMs x resident blocks (tuned or as many as fit).
-int traversal_grid(const tr_ctx* ctx, const void* kernel);
+// Grid of a persistent traversal kernel: SMs x resident blocks (tuned or as
+// many as fit with `smem` bytes of dynamic shared memory per block).
+int traversal_grid(const tr_ctx* ctx, const void* kernel, size_t smem = 0);
+// Builds and uploads the shared-memory treelet for the tuned node count.
+tr_status upload_treelet(tr_ctx* ctx);
+// Nodes of the treelet the traversal kernels stage (0: none).
+inline int treelet_nodes(const tr_ctx* ctx) { return ctx->tune.treelet_nodes > 0 ? ctx->dsc.treelet_n : 0; }
+// Lets `kernel` take `bytes` of dynamic shared memory (above the 48 KiB default).
+cudaError_t allow_dynamic_smem(const void* kernel, size_t bytes);
 // Whether any-hit traversal walks the four-wide tree (tuning and scene allow it).
 inline bool any_wide(const tr_ctx* ctx) { return ctx->tune.any_node_width == 4 && ctx->dsc.nodes4 != nullptr; }
 void release_render(tr_ctx* ctx);

@@ -39,6 +39,7 @@
 #include "context.h"
 #include "mixture.cuh"
 #include "mlp.h"
+#include "binning.cuh"
 #include "shade.cuh"
 #include "traverse.cuh"
 
@@ -94,6 +95,7 @@ struct RenderBuffers {
   DevBuf GX;                        // path guiding: the continuation's MIS data (4 float4 per slot)
   DevBuf MT;                        // Phong set-ups at hits with image maps (one DMat per slot)
   DevBuf jobs;                      // JobDev table of the current render
+  DevBuf q_srt, bin_key, bin_cnt;   // ray binning: the reordered queue, keys, bin counts
   unsigned int tb_count = 0, tb_cap = 0;  // training records of the last guided render
   unsigned int* h_active = nullptr;  // pinned: live-slot count per check
   std::vector<cudaEvent_t> ev_pool;  // reused by stage timing
@@ -119,6 +121,7 @@ struct Launch {
   int njobs, nslots;
   int nl_max;  // stride of the per-(slot, light) records
   int refill;  // traversal lane-refill threshold (tr_tuning)
+  int tl_n;    // treelet nodes the binary traversal kernels stage (their launches give tl_n * 64 bytes)
   float4 *P0, *P1, *P2, *P3, *P4;  // cont o|flags, cont d|depth, coef|sample, L|px, coef_prev|py
   unsigned long long* rng;
   float4 *M0, *M1, *M2;  // mis o|bsdf_pdf, mis d|abs_cos, bsdf_f (guided: o|p_guided, d|p_bsdf, f_eval|p_plain)
@@ -133,6 +136,11 @@ struct Launch {
   int* q_mat[kMatKinds];
   int* q_nee[kNeeKinds];
   int* q_sh;
+  // ray binning (bin_bits > 0): the extend or shadow queue reordered by ray
+  // key, read by the traversal kernels instead of the queue
+  int bin_bits;
+  int* q_srt;
+  unsigned int *bin_key, *bin_cnt;
   unsigned int* ctr;
   unsigned long long* stats;  // samples, extend rays, shadow rays, shade items, visit counts (4-7)
   // path guiding (alpha > 0: sample Lambertian continuations from the network's mixture;
@@ -344,9 +352,11 @@ __global__ void __launch_bounds__(256) k_init(Launch P) {
 struct ExtendJob {
   const Launch& P;
   int cur;
+  const int* q;  // the queue, or its binned order
+  __device__ ExtendJob(const Launch& P_, int cur_) : P(P_), cur(cur_), q(P_.bin_bits ? P_.q_srt : P_.q_ext[cur_]) {}
   __device__ __forceinline__ unsigned int count() const { return P.ctr[C_EXT + cur]; }
   __device__ __forceinline__ void load(unsigned int i, f3& o, f3& d, float& t_min, float& t_max, int& scene) const {
-    const int e = P.q_ext[cur][i];
+    const int e = q[i];
     const int slot = e >> 1;
     scene = job_of(P, slot).scene;
     const float4 a = (e & 1) ? P.M0[slot] : P.P0[slot];
@@ -357,7 +367,7 @@ struct ExtendJob {
     t_max = kRealMax;
   }
   __device__ __forceinline__ void store(unsigned int i, const Hit& h, float, bool) const {
-    const int e = P.q_ext[cur][i];
+    const int e = q[i];
     const float4 rec = make_float4(__int_as_float(h.prim), h.t_attr, h.alpha, h.beta);
     if (e & 1) P.HM[e >> 1] = rec;
     else P.HC[e >> 1] = rec;
@@ -367,9 +377,11 @@ struct ExtendJob {
 // Work items of the shadow kernel: shadow records o|t_max, d, contrib|valid.
 struct ShadowJob {
   const Launch& P;
+  const int* q;  // the queue, or its binned order
+  __device__ explicit ShadowJob(const Launch& P_) : P(P_), q(P_.bin_bits ? P_.q_srt : P_.q_sh) {}
   __device__ __forceinline__ unsigned int count() const { return P.ctr[C_SH]; }
   __device__ __forceinline__ void load(unsigned int i, f3& o, f3& d, float& t_min, float& t_max, int& scene) const {
-    const int r = P.q_sh[i];
+    const int r = q[i];
     scene = job_of(P, r / P.nl_max).scene;
     const float4 a = P.SH[3 * r], b = P.SH[3 * r + 1];
     o = mk3(a.x, a.y, a.z);
@@ -378,16 +390,46 @@ struct ShadowJob {
     t_max = a.w;
   }
   __device__ __forceinline__ void store(unsigned int i, const Hit&, float, bool occluded) const {
-    if (occluded) P.SH[3 * P.q_sh[i] + 2].w = 0.0f;
+    if (occluded) P.SH[3 * q[i] + 2].w = 0.0f;
+  }
+};
+
+// The two queues as sources of ray binning (binning.cuh): entries in queue
+// order with their rays.
+struct ExtendSrc {
+  Launch P;
+  int cur;
+  __device__ __forceinline__ unsigned int count() const { return P.ctr[C_EXT + cur]; }
+  __device__ __forceinline__ int item(unsigned int i) const { return P.q_ext[cur][i]; }
+  __device__ __forceinline__ void ray(unsigned int i, f3& o, f3& d, int& scene) const {
+    const int e = P.q_ext[cur][i];
+    const int slot = e >> 1;
+    scene = job_of(P, slot).scene;
+    const float4 a = (e & 1) ? P.M0[slot] : P.P0[slot];
+    const float4 b = (e & 1) ? P.M1[slot] : P.P1[slot];
+    o = mk3(a.x, a.y, a.z);
+    d = mk3(b.x, b.y, b.z);
+  }
+};
+struct ShadowSrc {
+  Launch P;
+  __device__ __forceinline__ unsigned int count() const { return P.ctr[C_SH]; }
+  __device__ __forceinline__ int item(unsigned int i) const { return P.q_sh[i]; }
+  __device__ __forceinline__ void ray(unsigned int i, f3& o, f3& d, int& scene) const {
+    const int r = P.q_sh[i];
+    scene = job_of(P, r / P.nl_max).scene;
+    const float4 a = P.SH[3 * r], b = P.SH[3 * r + 1];
+    o = mk3(a.x, a.y, a.z);
+    d = mk3(b.x, b.y, b.z);
   }
 };
 
 template <bool COUNT>
 __global__ void __launch_bounds__(128) k_extend(Launch P, int cur) {
-  ExtendJob job{P, cur};
+  ExtendJob job(P, cur);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.stats + 1, (unsigned long long)job.count());
   VisitCount vc;
-  persistent_traverse<false, COUNT>(P.sc, job, P.ctr + C_FEXT, (int*)(P.ctr + C_ERR), vc, P.refill);
+  persistent_traverse<false, COUNT>(P.sc, job, P.ctr + C_FEXT, (int*)(P.ctr + C_ERR), vc, P.refill, P.tl_n);
   if (COUNT) {
     count_add(P.stats + 4, vc.boxes);
     count_add(P.stats + 5, vc.prims);
@@ -396,10 +438,10 @@ __global__ void __launch_bounds__(128) k_extend(Launch P, int cur) {
 
 template <bool COUNT, bool WIDE = false>
 __global__ void __launch_bounds__(128) k_shadow(Launch P) {
-  ShadowJob job{P};
+  ShadowJob job(P);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.stats + 2, (unsigned long long)job.count());
   VisitCount vc;
-  persistent_traverse<true, COUNT, WIDE>(P.sc, job, P.ctr + C_FSH, (int*)(P.ctr + C_ERR), vc, P.refill);
+  persistent_traverse<true, COUNT, WIDE>(P.sc, job, P.ctr + C_FSH, (int*)(P.ctr + C_ERR), vc, P.refill, P.tl_n);
   if (COUNT) {
     count_add(P.stats + 6, vc.boxes);
     count_add(P.stats + 7, vc.prims);
@@ -1120,7 +1162,7 @@ void release_render(tr_ctx* ctx) {
   for (DevBuf* b : {&rb->P0, &rb->P1, &rb->P2, &rb->P3, &rb->P4, &rb->rng, &rb->M0, &rb->M1, &rb->M2, &rb->HC,
                     &rb->HM, &rb->SC, &rb->NU, &rb->SH, &rb->acc, &rb->q_ext, &rb->q_act, &rb->q_mat, &rb->q_nee,
                     &rb->q_sh, &rb->ctr, &rb->stats, &rb->VR, &rb->NV, &rb->gfeat, &rb->gout, &rb->tb, &rb->jobs,
-                    &rb->GX, &rb->MT})
+                    &rb->GX, &rb->MT, &rb->q_srt, &rb->bin_key, &rb->bin_cnt})
     b->release();
   if (rb->h_active) cudaFreeHost(rb->h_active);
   for (cudaEvent_t e : rb->ev_pool) cudaEventDestroy(e);
@@ -1300,6 +1342,17 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   P.q_sh = rb->q_sh.as<int>();
   P.ctr = rb->ctr.as<unsigned int>();
   P.stats = rb->stats.as<unsigned long long>();
+  P.bin_bits = ctx->tune.ray_bin_bits;
+  if (P.bin_bits) {
+    const size_t cap = std::max((size_t)2 * n, (size_t)n * std::max(nl, 1));
+    cudaError_t e;
+    if ((e = rb->q_srt.reserve(cap * 4)) != cudaSuccess || (e = rb->bin_key.reserve(cap * 4)) != cudaSuccess ||
+        (e = rb->bin_cnt.reserve((size_t)4 << (3 + 3 * P.bin_bits))) != cudaSuccess)
+      return cuda_fail(ctx, e, "ray binning buffers");
+    P.q_srt = rb->q_srt.as<int>();
+    P.bin_key = rb->bin_key.as<unsigned int>();
+    P.bin_cnt = rb->bin_cnt.as<unsigned int>();
+  }
   if (gp) {
     if (njobs != 1) return set_err(ctx, TR_ERR_ARG, "guided rendering takes one job");
     if (!(gp->alpha >= 0.0f && gp->alpha < 1.0f)) return set_err(ctx, TR_ERR_ARG, "guide alpha must be in [0, 1)");
@@ -1346,9 +1399,19 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   }
   if (sms <= 0) sms = 1;
   const int grid = sms * ctx->tune.shade_blocks_per_sm, grid_init = sms * 8;
-  const int grid_ext = traversal_grid(ctx, (const void*)k_extend<false>);
+  // the treelet staged by the binary traversal kernels
+  P.tl_n = treelet_nodes(ctx);
+  const size_t tl_smem = (size_t)P.tl_n * sizeof(DNode);
+  for (const void* k : {(const void*)k_extend<false>, (const void*)k_extend<true>, (const void*)k_shadow<false>,
+                        (const void*)k_shadow<true>}) {
+    const cudaError_t ae = allow_dynamic_smem(k, tl_smem);
+    if (ae != cudaSuccess) return cuda_fail(ctx, ae, "traversal shared memory");
+  }
+  const int grid_ext = traversal_grid(ctx, (const void*)k_extend<false>, tl_smem);
   const bool wide = any_wide(ctx);
-  const int grid_sh = traversal_grid(ctx, wide ? (const void*)k_shadow<false, true> : (const void*)k_shadow<false>);
+  const size_t sh_smem = wide ? 0 : tl_smem;
+  const int grid_sh =
+      traversal_grid(ctx, wide ? (const void*)k_shadow<false, true> : (const void*)k_shadow<false>, sh_smem);
   P.refill = ctx->tune.trav_refill_lanes;
 
   ctx->cancel.store(0);
@@ -1397,11 +1460,18 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     cudaEventRecord(ev[nev++], st);
   };
   // one wavefront iteration; returns the first launch error
+  const int bin_nb = P.bin_bits ? 1 << (3 + 3 * P.bin_bits) : 0;
   auto iteration = [&](int cur) -> tr_status {
     const int nxt = cur ^ 1;
     mark();
-    if (count) k_extend<true><<<grid_ext, 128, 0, st>>>(P, cur);
-    else k_extend<false><<<grid_ext, 128, 0, st>>>(P, cur);
+    if (P.bin_bits) {  // the extend queue in ray-key order (counted with the extend stage)
+      cudaMemsetAsync(P.bin_cnt, 0, (size_t)bin_nb * 4, st);
+      k_bin_count<<<grid, 128, 0, st>>>(ExtendSrc{P, cur}, P.sc, P.bin_cnt, P.bin_key, P.bin_bits);
+      k_bin_scan<<<1, kBinScanThreads, 0, st>>>(P.bin_cnt, bin_nb);
+      k_bin_scatter<<<grid, 128, 0, st>>>(ExtendSrc{P, cur}, P.bin_cnt, P.bin_key, P.q_srt);
+    }
+    if (count) k_extend<true><<<grid_ext, 128, tl_smem, st>>>(P, cur);
+    else k_extend<false><<<grid_ext, 128, tl_smem, st>>>(P, cur);
     mark();
     // next iteration's extend and live counts; this iteration's shadow,
     // material and light-sample counts and the fetch positions
@@ -1432,10 +1502,16 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     if (P.sc.has_metal) k_nee<MAT_METAL><<<grid, 128, 0, st>>>(P);  // timed with Disney12
     if (P.sc.has_disney15) k_nee<MAT_DISNEY15><<<grid, 128, 0, st>>>(P);
     mark();
+    if (P.bin_bits) {  // the shadow queue in ray-key order (counted with the shadow stage)
+      cudaMemsetAsync(P.bin_cnt, 0, (size_t)bin_nb * 4, st);
+      k_bin_count<<<grid, 128, 0, st>>>(ShadowSrc{P}, P.sc, P.bin_cnt, P.bin_key, P.bin_bits);
+      k_bin_scan<<<1, kBinScanThreads, 0, st>>>(P.bin_cnt, bin_nb);
+      k_bin_scatter<<<grid, 128, 0, st>>>(ShadowSrc{P}, P.bin_cnt, P.bin_key, P.q_srt);
+    }
     if (count && wide) k_shadow<true, true><<<grid_sh, 128, 0, st>>>(P);
-    else if (count) k_shadow<true><<<grid_sh, 128, 0, st>>>(P);
+    else if (count) k_shadow<true><<<grid_sh, 128, sh_smem, st>>>(P);
     else if (wide) k_shadow<false, true><<<grid_sh, 128, 0, st>>>(P);
-    else k_shadow<false><<<grid_sh, 128, 0, st>>>(P);
+    else k_shadow<false><<<grid_sh, 128, sh_smem, st>>>(P);
     mark();
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? TR_OK : cuda_fail(ctx, e, "wavefront launch");
@@ -1836,15 +1912,21 @@ extern "C" tr_status tr_autotune(tr_ctx* ctx, const tr_batch_job* jobs, uint32_t
   };
   // coordinate descent over the discrete settings
   static const int kBlocks[] = {0, 4, 6, 8}, kRefill[] = {12, 20, 28}, kShade[] = {8, 16, 32},
-                   kGraph[] = {0, 4, 8, 16}, kWidth[] = {2, 4};
+                   kGraph[] = {0, 4, 8, 16}, kWidth[] = {2, 4}, kBins[] = {0, 3, 4}, kTreelet[] = {0, 64, 256};
   tr_tuning cur = ctx->tune;
   double cur_ms = 0.0;
   tr_status s = time_once(cur, cur_ms);
   if (s != TR_OK) return s;
   for (int pass = 0; pass < 2; ++pass) {
     bool improved = false;
-    for (int dim = 0; dim < 5; ++dim) {
-      const int* vals = dim == 0 ? kBlocks : dim == 1 ? kRefill : dim == 2 ? kShade : dim == 3 ? kGraph : kWidth;
+    for (int dim = 0; dim < 7; ++dim) {
+      const int* vals = dim == 0   ? kBlocks
+                        : dim == 1 ? kRefill
+                        : dim == 2 ? kShade
+                        : dim == 3 ? kGraph
+                        : dim == 4 ? kWidth
+                        : dim == 5 ? kBins
+                                   : kTreelet;
       const int nv = dim == 0 || dim == 3 ? 4 : dim == 4 ? 2 : 3;
       for (int k = 0; k < nv; ++k) {
         tr_tuning t = cur;
@@ -1852,7 +1934,9 @@ extern "C" tr_status tr_autotune(tr_ctx* ctx, const tr_batch_job* jobs, uint32_t
                      : dim == 1 ? &t.trav_refill_lanes
                      : dim == 2 ? &t.shade_blocks_per_sm
                      : dim == 3 ? &t.graph_iterations
-                                : &t.any_node_width;
+                     : dim == 4 ? &t.any_node_width
+                     : dim == 5 ? &t.ray_bin_bits
+                                : &t.treelet_nodes;
         if (*field == vals[k]) continue;
         *field = vals[k];
         double ms = 0.0;

@@ -34,6 +34,14 @@ struct alignas(16) int4 {
 
 namespace trg {
 
+// Launch-tuning limits (tr_tuning): ray-binning grid bits per axis, and the
+// child-pair nodes of the shared-memory treelet.
+constexpr int kBinBitsMax = 5;
+constexpr int kTreeletMax = 1024;
+// A child reference with this bit set names a node of the shared-memory
+// treelet (its index in the low bits) instead of a DNode in global memory.
+constexpr int kTreeletRef = 1 << 25;
+
 struct alignas(16) DNode {
   float4 a;  // L.lo.x L.lo.y L.lo.z L.hi.x
   float4 b;  // L.hi.y L.hi.z R.lo.x R.lo.y
@@ -205,6 +213,11 @@ struct DScene {
   int has_env;       // some scene has an environment light
   const DTex* textures;  // image textures of the set's materials
   int has_textures;      // some material has an image map
+  // Top of scene 0's child-pair tree, breadth first from the root, for
+  // staging in shared memory (single-scene sets only): copies of DNodes whose
+  // references to other treelet nodes are kTreeletRef | treelet index.
+  const DNode* treelet;
+  int treelet_n;  // nodes in it (0: none)
 };
 
 }  // namespace trg

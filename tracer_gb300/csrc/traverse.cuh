@@ -38,6 +38,23 @@ struct Hit {
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 
+// The shared-memory treelet (DScene::treelet, staged by each block of a
+// traversal kernel into its dynamic shared memory). Float4 k of treelet node j
+// sits at 4 * j + (k ^ ((j >> 1) & 3)): eight lanes reading the same field of
+// eight consecutive nodes then hit eight different bank groups (without the
+// swizzle a 64-byte node stride leaves only two).
+extern __shared__ float4 trav_smem[];
+
+__device__ __forceinline__ int treelet_slot(int j, int k) { return 4 * j + (k ^ ((j >> 1) & 3)); }
+
+// Copies the first n treelet nodes into shared memory; every thread of the
+// block calls it once, before any traversal.
+__device__ __forceinline__ void stage_treelet(const DScene& sc, int n) {
+  const float4* src = reinterpret_cast<const float4*>(sc.treelet);
+  for (int i = threadIdx.x; i < 4 * n; i += blockDim.x) trav_smem[treelet_slot(i >> 2, i & 3)] = __ldg(src + i);
+  __syncthreads();
+}
+
 // Slab test with the reference's arithmetic. Returns the t_max-independent
 // part ("pass"), and tmin for the "tMin < ray.t_max" part.
 // Written without branches (the reference's early returns become flags;
@@ -199,8 +216,9 @@ struct TravLane {
 
   // Starts a ray in scene `scene` of the set; returns false when it misses
   // the root box (done at once).
+  // tl: the block staged scene 0's treelet (its root is treelet node 0).
   __device__ __forceinline__ bool start(const DScene& sc, int scene, f3 o_, f3 d_, float tmin_, float tmax_,
-                                        VisitCount& vc) {
+                                        VisitCount& vc, bool tl) {
     o = o_;
     d = d_;
     t_min = tmin_;
@@ -222,6 +240,7 @@ struct TravLane {
     if (!box_pass(R.lo[0], R.lo[1], R.lo[2], R.hi[0], R.hi[1], R.hi[2], o, inv, n0, n1, n2, tmin) || !(tmin < t_max))
       return false;
     cur = WIDE && R.kind == 1 ? R.offset4 : R.offset;
+    if (!WIDE && tl && scene == 0 && R.kind == 1) cur = kTreeletRef;
     cnt = R.kind == 2 ? R.count : 0;
     return true;
   }
@@ -244,9 +263,20 @@ struct TravLane {
 
   // One child-pair visit at interior node `cur`; returns false when done.
   __device__ __forceinline__ bool interior(const DScene& sc, int* err, VisitCount& vc) {
-    const float4* np = reinterpret_cast<const float4*>(sc.nodes + cur);
-    const float4 a = ldg4(np), b = ldg4(np + 1), c = ldg4(np + 2);
-    const float4 dd = ldg4(np + 3);
+    float4 a, b, c, dd;
+    if (cur & kTreeletRef) {
+      const int j = cur & (kTreeletRef - 1);
+      a = trav_smem[treelet_slot(j, 0)];
+      b = trav_smem[treelet_slot(j, 1)];
+      c = trav_smem[treelet_slot(j, 2)];
+      dd = trav_smem[treelet_slot(j, 3)];
+    } else {
+      const float4* np = reinterpret_cast<const float4*>(sc.nodes + cur);
+      a = ldg4(np);
+      b = ldg4(np + 1);
+      c = ldg4(np + 2);
+      dd = ldg4(np + 3);
+    }
     if (COUNT) vc.boxes += 2;
     float tl, tr;
     const bool hl = box_pass(a.x, a.y, a.z, a.w, b.x, b.y, o, inv, n0, n1, n2, tl) && tl < t_max;
@@ -380,9 +410,14 @@ struct TravLane {
 // Job: unsigned count() const;
 //      void load(unsigned i, f3& o, f3& d, float& t_min, float& t_max, int& scene);
 //      void store(unsigned i, const Hit& h, float t_max, bool occluded).
+// tl_n: treelet nodes to stage in shared memory (the launch gives the block
+// at least tl_n * 64 bytes of dynamic shared memory; 0: none). The four-wide
+// walk does not use the treelet.
 template <bool ANY, bool COUNT, bool WIDE = false, class Job>
 __device__ __forceinline__ void persistent_traverse(const DScene& sc, Job& job, unsigned int* fetch, int* err,
-                                                    VisitCount& vc, int refill) {
+                                                    VisitCount& vc, int refill, int tl_n = 0) {
+  const bool tl = !WIDE && tl_n > 0;
+  if (tl) stage_treelet(sc, tl_n);
   const unsigned int n = job.count();
   const unsigned int lane = threadIdx.x & 31u;
   const unsigned int below = (1u << lane) - 1u;
@@ -403,7 +438,7 @@ __device__ __forceinline__ void persistent_traverse(const DScene& sc, Job& job, 
           float tmin, tmax;
           int scene;
           job.load(item, o, d, tmin, tmax, scene);
-          live = L.start(sc, scene, o, d, tmin, tmax, vc);
+          live = L.start(sc, scene, o, d, tmin, tmax, vc, tl);
           if (!live) job.store(item, L.h, L.t_max, false);
         } else {
           exhausted = true;

@@ -225,8 +225,13 @@ class GpuContext:
 
     def set_tuning(self, refill: int | None = None, trav_blocks_per_sm: int | None = None,
                    shade_blocks_per_sm: int | None = None, graph_iterations: int | None = None,
-                   any_node_width: int | None = None) -> None:
+                   any_node_width: int | None = None, ray_bin_bits: int | None = None,
+                   treelet_nodes: int | None = None) -> None:
         t = self.tuning()
+        if ray_bin_bits is not None:
+            t.ray_bin_bits = ray_bin_bits
+        if treelet_nodes is not None:
+            t.treelet_nodes = treelet_nodes
         if any_node_width is not None:
             t.any_node_width = any_node_width
         if graph_iterations is not None:
