@@ -217,6 +217,7 @@ typedef struct tr_stats {
   uint64_t any_boxes;     /*   boxes tested by shadow rays */
   uint64_t any_prims;     /*   primitives tested by shadow rays */
   uint64_t guide_records; /* guided renders: training records kept */
+  uint64_t occluder_hits; /* shadow rays answered by their slot's remembered occluder (tr_tuning.occluder_cache) */
 } tr_stats;
 
 const char* tr_status_string(tr_status s);
@@ -257,14 +258,21 @@ tr_status tr_synchronize(tr_ctx* ctx);
  *    Closest-hit traversal always keeps the reference's binary order (it
  *    decides which of two equal-distance primitives is reported). A scene
  *    whose collapsed tree could overflow the traversal stack uses width 2.
- *  - ray_bin_bits (0..5): before each traversal launch of a render, its
- *    queue of rays is regrouped by direction octant and the origin's cell in
- *    a 2^b x 2^b x 2^b grid over the scene box (0: queue order). Each ray's
- *    result is unchanged; warps walk more alike paths.
+ *  - ray_bin_bits (0..5): before traversal of a render's extension rays
+ *    and of the rays given to tr_trace_*, the rays are regrouped by
+ *    direction octant and the origin's cell in a 2^b x 2^b x 2^b grid over
+ *    the scene box (0: given order). Each ray's result is unchanged; warps
+ *    walk more alike paths. A render's shadow rays keep their queue order.
  *  - treelet_nodes (0..1024): the top of the closest-hit tree (this many
  *    child-pair nodes, breadth first from the root) is staged in shared
  *    memory by every block of the traversal kernels (0: all nodes are read
- *    from global memory). */
+ *    from global memory).
+ *  - occluder_cache (0 or 1): a render remembers, per pixel slot and light,
+ *    the primitive that last blocked its shadow ray, and tests it (after its
+ *    BVH leaf's box) before walking the tree. The slab test passes a box
+ *    whenever it passes a box inside it, so a ray that passes the leaf's box
+ *    passes every box above it: the reference's any-hit walk reaches that
+ *    primitive, and a hit there gives the walk's answer. */
 typedef struct tr_tuning {
   int32_t trav_refill_lanes;
   int32_t trav_blocks_per_sm;
@@ -273,6 +281,7 @@ typedef struct tr_tuning {
   int32_t any_node_width;
   int32_t ray_bin_bits;
   int32_t treelet_nodes;
+  int32_t occluder_cache;
 } tr_tuning;
 tr_status tr_ctx_set_tuning(tr_ctx* ctx, const tr_tuning* t);
 tr_status tr_ctx_get_tuning(const tr_ctx* ctx, tr_tuning* t);

@@ -283,17 +283,19 @@ def test_visit_counts_match_oracle(gpu):
 
 def test_tuning_does_not_change_results(gpu):
     """Launch tuning (grid sizes, lane refill threshold, any-hit node
-    width, ray binning, the shared-memory treelet) never changes the film."""
+    width, ray binning, the shared-memory treelet, the occluder cache)
+    never changes the film."""
     from conftest import tuned
     for make in (lambda: scenes.disney_grid(48, 32, 2), lambda: scenes.occluded_room(48, 32, 2, n_tris=20000)):
         sc, cam, filt, par = make()
         gpu.upload(sc)
         with tuned(gpu, any_node_width=2):
             base, _ = gpu.render(cam, filt, par)
-        for refill, tb, sb, w, bits, tl in ((1, 1, 1, 2, 0, 0), (32, 3, 40, 4, 3, 0), (7, 0, 9, 4, 0, 256),
-                                            (20, 0, 16, 4, 0, 0), (20, 0, 16, 2, 4, 64), (12, 0, 8, 2, 5, 1024)):
+        for refill, tb, sb, w, bits, tl, oc in ((1, 1, 1, 2, 0, 0, 0), (32, 3, 40, 4, 3, 0, 1), (7, 0, 9, 4, 0, 256, 0),
+                                                (20, 0, 16, 4, 0, 0, 1), (20, 0, 16, 2, 4, 64, 1),
+                                                (12, 0, 8, 2, 5, 1024, 0)):
             with tuned(gpu, trav_refill_lanes=refill, trav_blocks_per_sm=tb, shade_blocks_per_sm=sb,
-                       any_node_width=w, ray_bin_bits=bits, treelet_nodes=tl):
+                       any_node_width=w, ray_bin_bits=bits, treelet_nodes=tl, occluder_cache=oc):
                 out, _ = gpu.render(cam, filt, par)
             assert np.array_equal(out.view(np.uint32), base.view(np.uint32))
 

@@ -110,7 +110,8 @@ class TrStats(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("extend_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
                 ("shade_items", C.c_uint64), ("iterations", C.c_uint64), ("device_ms", C.c_double),
                 ("stage_ms", C.c_double * 8), ("closest_boxes", C.c_uint64), ("closest_prims", C.c_uint64),
-                ("any_boxes", C.c_uint64), ("any_prims", C.c_uint64), ("guide_records", C.c_uint64)]
+                ("any_boxes", C.c_uint64), ("any_prims", C.c_uint64), ("guide_records", C.c_uint64),
+                ("occluder_hits", C.c_uint64)]
 
 
 class TrGuideParams(C.Structure):
@@ -121,7 +122,8 @@ class TrGuideParams(C.Structure):
 class TrTuning(C.Structure):
     _fields_ = [("trav_refill_lanes", C.c_int32), ("trav_blocks_per_sm", C.c_int32),
                 ("shade_blocks_per_sm", C.c_int32), ("graph_iterations", C.c_int32),
-                ("any_node_width", C.c_int32), ("ray_bin_bits", C.c_int32), ("treelet_nodes", C.c_int32)]
+                ("any_node_width", C.c_int32), ("ray_bin_bits", C.c_int32), ("treelet_nodes", C.c_int32),
+                ("occluder_cache", C.c_int32)]
 
 
 class TrBatchJob(C.Structure):

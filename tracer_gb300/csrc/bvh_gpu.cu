@@ -465,6 +465,7 @@ tr_status upload_device_built(tr_ctx* ctx) {
   sc.nodes4 = nullptr;
   sc.treelet = nullptr;  // no host copy of the device-built tree to stage from
   sc.treelet_n = 0;
+  sc.slot_leaf = nullptr;  // nor the leaf of every slot: no occluder cache
   hs.dnodes.clear();
   hs.root0 = -1;
   sc.slots = ctx->d_slots.as<float4>();

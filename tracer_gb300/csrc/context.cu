@@ -292,8 +292,19 @@ tr_status upload_device_tables(tr_ctx* ctx) {
     if (bytes) return cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
     return cudaSuccess;
   };
+  // where each slot's leaf box is stored (the occluder cache tests it)
+  std::vector<int> slot_leaf(hs.order.size(), -1);
+  for (size_t i = 0; i < nn; ++i) {
+    const tr_bvh_node32& n = hs.nodes[i];
+    if (n.count > 0) continue;
+    const tr_bvh_node32* kids[2] = {&hs.nodes[i + 1], &hs.nodes[n.offset]};
+    for (int side = 0; side < 2; ++side)
+      if (kids[side]->count > 0)
+        for (int s = 0; s < kids[side]->count; ++s) slot_leaf[(size_t)kids[side]->offset + s] = 2 * dix[i] + side;
+  }
   TR_CUDA(ctx, put(ctx->d_nodes, dn.data(), dn.size() * sizeof(DNode)));
   TR_CUDA(ctx, put(ctx->d_slots, slots.data(), slots.size() * sizeof(float4)));
+  TR_CUDA(ctx, put(ctx->d_slot_leaf, slot_leaf.data(), slot_leaf.size() * sizeof(int)));
   TR_CUDA(ctx, put(ctx->d_spheres, hs.spheres.data(), hs.spheres.size() * sizeof(DSphere)));
   TR_CUDA(ctx, put(ctx->d_prims, hs.prims.data(), hs.prims.size() * sizeof(DPrim)));
   TR_CUDA(ctx, put(ctx->d_tshade, hs.tshade.data(), hs.tshade.size() * sizeof(DTriShade)));
@@ -355,6 +366,7 @@ tr_status upload_device_tables(tr_ctx* ctx) {
   sc.treelet = nullptr;
   sc.treelet_n = 0;
   sc.slots = ctx->d_slots.as<float4>();
+  sc.slot_leaf = ctx->d_slot_leaf.as<int>();
   sc.spheres = ctx->d_spheres.as<DSphere>();
   sc.prims = ctx->d_prims.as<DPrim>();
   sc.tshade = ctx->d_tshade.as<DTriShade>();
@@ -537,6 +549,7 @@ struct BatchJob {
   uint8_t* hit;
   const int* perm;  // ray binning: work item i is ray perm[i] (null: ray i)
   __device__ __forceinline__ unsigned int count() const { return n; }
+  __device__ __forceinline__ int cached(unsigned int) const { return -1; }
   __device__ __forceinline__ void load(unsigned int w, f3& o, f3& d, float& t_min, float& t_max, int& scene) const {
     scene = 0;
     const unsigned int i = perm ? (unsigned int)perm[w] : w;
@@ -714,7 +727,7 @@ void tr_ctx_destroy(tr_ctx* ctx) {
   for (DevBuf* b : {&ctx->d_nodes, &ctx->d_nodes4, &ctx->d_slots, &ctx->d_spheres, &ctx->d_prims, &ctx->d_tshade,
                     &ctx->d_mats, &ctx->d_lights, &ctx->d_roots, &ctx->d_rays, &ctx->d_out0, &ctx->d_out1,
                     &ctx->d_err, &ctx->d_env_pool, &ctx->d_envs, &ctx->d_tex_pool, &ctx->d_texs, &ctx->d_treelet,
-                    &ctx->d_perm, &ctx->d_bin_key, &ctx->d_bin_cnt})
+                    &ctx->d_perm, &ctx->d_bin_key, &ctx->d_bin_cnt, &ctx->d_slot_leaf})
     b->release();
   cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -728,7 +741,8 @@ tr_status tr_ctx_set_tuning(tr_ctx* ctx, const tr_tuning* t) {
   if (t->trav_refill_lanes < 1 || t->trav_refill_lanes > 32 || t->trav_blocks_per_sm < 0 ||
       t->trav_blocks_per_sm > 64 || t->shade_blocks_per_sm < 1 || t->shade_blocks_per_sm > 64 ||
       t->graph_iterations < 0 || t->graph_iterations > 64 || (t->any_node_width != 2 && t->any_node_width != 4) ||
-      t->ray_bin_bits < 0 || t->ray_bin_bits > kBinBitsMax || t->treelet_nodes < 0 || t->treelet_nodes > kTreeletMax)
+      t->ray_bin_bits < 0 || t->ray_bin_bits > kBinBitsMax || t->treelet_nodes < 0 || t->treelet_nodes > kTreeletMax ||
+      (t->occluder_cache != 0 && t->occluder_cache != 1))
     return set_err(ctx, TR_ERR_ARG, "tuning out of range");
   const bool restage = t->treelet_nodes != ctx->tune.treelet_nodes;
   ctx->tune = *t;

@@ -83,6 +83,9 @@ enum : int {  // counter slots
   C_ERR = 17,     // traversal error word
 };
 constexpr int kCtrWords = 32;  // the counter array
+// Statistics words: samples, extend rays, shadow rays, shade items, visit
+// counts (4-7), occluder-cache hits (8).
+constexpr int kStatWords = 16;
 // Material code in the shading context: the material index, or with this bit
 // set the slot's own set-up in Launch::MT (a Phong material with maps).
 constexpr int kMatScratch = 1 << 30;
@@ -96,6 +99,7 @@ struct RenderBuffers {
   DevBuf MT;                        // Phong set-ups at hits with image maps (one DMat per slot)
   DevBuf jobs;                      // JobDev table of the current render
   DevBuf q_srt, bin_key, bin_cnt;   // ray binning: the reordered queue, keys, bin counts
+  DevBuf OC;                        // occluder cache, one int per (slot, light)
   unsigned int tb_count = 0, tb_cap = 0;  // training records of the last guided render
   unsigned int* h_active = nullptr;  // pinned: live-slot count per check
   std::vector<cudaEvent_t> ev_pool;  // reused by stage timing
@@ -141,6 +145,9 @@ struct Launch {
   int bin_bits;
   int* q_srt;
   unsigned int *bin_key, *bin_cnt;
+  // occluder cache (null: off): per (slot, light) item, the slot that last
+  // blocked its shadow ray, or -1
+  int* OC;
   unsigned int* ctr;
   unsigned long long* stats;  // samples, extend rays, shadow rays, shade items, visit counts (4-7)
   // path guiding (alpha > 0: sample Lambertian continuations from the network's mixture;
@@ -355,6 +362,7 @@ struct ExtendJob {
   const int* q;  // the queue, or its binned order
   __device__ ExtendJob(const Launch& P_, int cur_) : P(P_), cur(cur_), q(P_.bin_bits ? P_.q_srt : P_.q_ext[cur_]) {}
   __device__ __forceinline__ unsigned int count() const { return P.ctr[C_EXT + cur]; }
+  __device__ __forceinline__ int cached(unsigned int) const { return -1; }
   __device__ __forceinline__ void load(unsigned int i, f3& o, f3& d, float& t_min, float& t_max, int& scene) const {
     const int e = q[i];
     const int slot = e >> 1;
@@ -377,9 +385,11 @@ struct ExtendJob {
 // Work items of the shadow kernel: shadow records o|t_max, d, contrib|valid.
 struct ShadowJob {
   const Launch& P;
-  const int* q;  // the queue, or its binned order
-  __device__ explicit ShadowJob(const Launch& P_) : P(P_), q(P_.bin_bits ? P_.q_srt : P_.q_sh) {}
+  const int* q;  // the queue (shadow rays keep queue order: a vertex's rays to every light are adjacent)
+  __device__ explicit ShadowJob(const Launch& P_) : P(P_), q(P_.q_sh) {}
   __device__ __forceinline__ unsigned int count() const { return P.ctr[C_SH]; }
+  // the slot that last blocked this (pixel slot, light) item's shadow ray
+  __device__ __forceinline__ int cached(unsigned int i) const { return P.OC ? P.OC[q[i]] : -1; }
   __device__ __forceinline__ void load(unsigned int i, f3& o, f3& d, float& t_min, float& t_max, int& scene) const {
     const int r = q[i];
     scene = job_of(P, r / P.nl_max).scene;
@@ -389,13 +399,18 @@ struct ShadowJob {
     t_min = kEps;
     t_max = a.w;
   }
-  __device__ __forceinline__ void store(unsigned int i, const Hit&, float, bool occluded) const {
-    if (occluded) P.SH[3 * q[i] + 2].w = 0.0f;
+  __device__ __forceinline__ void store(unsigned int i, const Hit& h, float, bool occluded) const {
+    if (occluded) {
+      P.SH[3 * q[i] + 2].w = 0.0f;
+      if (P.OC) P.OC[q[i]] = h.prim;
+    }
   }
 };
 
-// The two queues as sources of ray binning (binning.cuh): entries in queue
-// order with their rays.
+// The extend queue as a source of ray binning (binning.cuh): entries in
+// queue order with their rays. (The shadow queue is not binned: k_nee appends
+// a vertex's rays to all lights next to each other, an order binning loses;
+// measured slower on the occluded room.)
 struct ExtendSrc {
   Launch P;
   int cur;
@@ -407,18 +422,6 @@ struct ExtendSrc {
     scene = job_of(P, slot).scene;
     const float4 a = (e & 1) ? P.M0[slot] : P.P0[slot];
     const float4 b = (e & 1) ? P.M1[slot] : P.P1[slot];
-    o = mk3(a.x, a.y, a.z);
-    d = mk3(b.x, b.y, b.z);
-  }
-};
-struct ShadowSrc {
-  Launch P;
-  __device__ __forceinline__ unsigned int count() const { return P.ctr[C_SH]; }
-  __device__ __forceinline__ int item(unsigned int i) const { return P.q_sh[i]; }
-  __device__ __forceinline__ void ray(unsigned int i, f3& o, f3& d, int& scene) const {
-    const int r = P.q_sh[i];
-    scene = job_of(P, r / P.nl_max).scene;
-    const float4 a = P.SH[3 * r], b = P.SH[3 * r + 1];
     o = mk3(a.x, a.y, a.z);
     d = mk3(b.x, b.y, b.z);
   }
@@ -442,6 +445,7 @@ __global__ void __launch_bounds__(128) k_shadow(Launch P) {
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.stats + 2, (unsigned long long)job.count());
   VisitCount vc;
   persistent_traverse<true, COUNT, WIDE>(P.sc, job, P.ctr + C_FSH, (int*)(P.ctr + C_ERR), vc, P.refill, P.tl_n);
+  if (P.OC) count_add(P.stats + 8, vc.cache_hits);
   if (COUNT) {
     count_add(P.stats + 6, vc.boxes);
     count_add(P.stats + 7, vc.prims);
@@ -1162,7 +1166,7 @@ void release_render(tr_ctx* ctx) {
   for (DevBuf* b : {&rb->P0, &rb->P1, &rb->P2, &rb->P3, &rb->P4, &rb->rng, &rb->M0, &rb->M1, &rb->M2, &rb->HC,
                     &rb->HM, &rb->SC, &rb->NU, &rb->SH, &rb->acc, &rb->q_ext, &rb->q_act, &rb->q_mat, &rb->q_nee,
                     &rb->q_sh, &rb->ctr, &rb->stats, &rb->VR, &rb->NV, &rb->gfeat, &rb->gout, &rb->tb, &rb->jobs,
-                    &rb->GX, &rb->MT, &rb->q_srt, &rb->bin_key, &rb->bin_cnt})
+                    &rb->GX, &rb->MT, &rb->q_srt, &rb->bin_key, &rb->bin_cnt, &rb->OC})
     b->release();
   if (rb->h_active) cudaFreeHost(rb->h_active);
   for (cudaEvent_t e : rb->ev_pool) cudaEventDestroy(e);
@@ -1188,7 +1192,7 @@ tr_status reserve_render(tr_ctx* ctx, int n, int nl) {
                {&rb->NU, N * NL * 8},       {&rb->SH, N * NL * 3 * f4}, {&rb->acc, N * 32},
                {&rb->q_ext, 2 * 2 * N * 4}, {&rb->q_act, 2 * N * 4},   {&rb->q_mat, kMatKinds * N * 4},
                {&rb->q_nee, kNeeKinds * N * NL * 4}, {&rb->q_sh, N * NL * 4},  {&rb->ctr, kCtrWords * 4},
-               {&rb->stats, 64}};
+               {&rb->stats, kStatWords * 8}};
   for (auto& nd : needs) {
     cudaError_t e = nd.b->reserve(nd.bytes);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "render buffer allocation");
@@ -1342,9 +1346,16 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   P.q_sh = rb->q_sh.as<int>();
   P.ctr = rb->ctr.as<unsigned int>();
   P.stats = rb->stats.as<unsigned long long>();
+  P.OC = nullptr;
+  if (ctx->tune.occluder_cache && ctx->dsc.slot_leaf && !(flags & TR_RENDER_COUNT_VISITS)) {
+    // (a counting render keeps the reference's walks: its visit counts are the oracle's)
+    const cudaError_t e = rb->OC.reserve((size_t)n * std::max(nl, 1) * 4);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "occluder cache");
+    P.OC = rb->OC.as<int>();
+  }
   P.bin_bits = ctx->tune.ray_bin_bits;
   if (P.bin_bits) {
-    const size_t cap = std::max((size_t)2 * n, (size_t)n * std::max(nl, 1));
+    const size_t cap = (size_t)2 * n;
     cudaError_t e;
     if ((e = rb->q_srt.reserve(cap * 4)) != cudaSuccess || (e = rb->bin_key.reserve(cap * 4)) != cudaSuccess ||
         (e = rb->bin_cnt.reserve((size_t)4 << (3 + 3 * P.bin_bits))) != cudaSuccess)
@@ -1443,7 +1454,8 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   for (int k = 0; k < njobs; ++k)
     RCHK(cudaMemsetAsync(jd[k].film, 0, (size_t)jd[k].W * jd[k].H * (jd[k].fp64 ? 32 : 16), st));
   RCHK(cudaMemsetAsync(P.ctr, 0, kCtrWords * 4, st));
-  RCHK(cudaMemsetAsync(P.stats, 0, 64, st));
+  RCHK(cudaMemsetAsync(P.stats, 0, kStatWords * 8, st));
+  if (P.OC) RCHK(cudaMemsetAsync(P.OC, 0xff, (size_t)n * P.nl_max * 4, st));
   RCHK(cudaEventRecord(e0, st));
   k_init<<<grid_init, 256, 0, st>>>(P);
   RCHK(cudaGetLastError());
@@ -1502,12 +1514,6 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     if (P.sc.has_metal) k_nee<MAT_METAL><<<grid, 128, 0, st>>>(P);  // timed with Disney12
     if (P.sc.has_disney15) k_nee<MAT_DISNEY15><<<grid, 128, 0, st>>>(P);
     mark();
-    if (P.bin_bits) {  // the shadow queue in ray-key order (counted with the shadow stage)
-      cudaMemsetAsync(P.bin_cnt, 0, (size_t)bin_nb * 4, st);
-      k_bin_count<<<grid, 128, 0, st>>>(ShadowSrc{P}, P.sc, P.bin_cnt, P.bin_key, P.bin_bits);
-      k_bin_scan<<<1, kBinScanThreads, 0, st>>>(P.bin_cnt, bin_nb);
-      k_bin_scatter<<<grid, 128, 0, st>>>(ShadowSrc{P}, P.bin_cnt, P.bin_key, P.q_srt);
-    }
     if (count && wide) k_shadow<true, true><<<grid_sh, 128, 0, st>>>(P);
     else if (count) k_shadow<true><<<grid_sh, 128, sh_smem, st>>>(P);
     else if (wide) k_shadow<false, true><<<grid_sh, 128, 0, st>>>(P);
@@ -1573,7 +1579,7 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   }
   RCHK(cudaEventRecord(e1, st));
   RCHK(cudaEventSynchronize(e1));
-  unsigned long long hs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  unsigned long long hs[kStatWords] = {};
   RCHK(cudaMemcpy(hs, P.stats, sizeof(hs), cudaMemcpyDeviceToHost));
   unsigned int ctrs[kCtrWords];
   RCHK(cudaMemcpy(ctrs, P.ctr, sizeof(ctrs), cudaMemcpyDeviceToHost));
@@ -1615,6 +1621,7 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     stats->any_boxes = hs[6];
     stats->any_prims = hs[7];
     stats->guide_records = rb->tb_count;
+    stats->occluder_hits = hs[8];
   }
   return result;
 #undef RCHK
@@ -1714,7 +1721,7 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
                oSC = L.take(N * 7 * f4), oNU = L.take(N * NL * 8), oSH = L.take(N * NL * 3 * f4),
                oQe = L.take(2 * 2 * N * 4), oQa = L.take(2 * N * 4), oQm = L.take(kMatKinds * N * 4),
                oQn = L.take(kNeeKinds * N * NL * 4), oQs = L.take(N * NL * 4), oCtr = L.take(kCtrWords * 4),
-               oSt = L.take(64),
+               oSt = L.take(kStatWords * 8),
                oJob = L.take(sizeof(JobDev));
   if (npix > (1ll << 24) || L.off > kNoAllocScratchBytes) {
     char msg[256];
@@ -1806,7 +1813,7 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   // rest of the scratch is written before it is read
   NCHK(cudaMemsetAsync(d_rgbw, 0, (size_t)n * 16, st));
   NCHK(cudaMemsetAsync(P.ctr, 0, kCtrWords * 4, st));
-  NCHK(cudaMemsetAsync(P.stats, 0, 64, st));
+  NCHK(cudaMemsetAsync(P.stats, 0, kStatWords * 8, st));
   k_init<<<grid_init, 256, 0, st>>>(P);
   NCHK(cudaGetLastError());
   // Every slot finishes within spp * (max_depth + 2) iterations (plus the
@@ -1849,7 +1856,7 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   }
   NCHK(cudaGetLastError());
   NCHK(cudaStreamSynchronize(st));
-  unsigned long long hs[8];
+  unsigned long long hs[kStatWords];
   unsigned int ctrs[kCtrWords];
   NCHK(cudaMemcpy(hs, P.stats, sizeof(hs), cudaMemcpyDeviceToHost));
   NCHK(cudaMemcpy(ctrs, P.ctr, sizeof(ctrs), cudaMemcpyDeviceToHost));

@@ -218,6 +218,9 @@ struct DScene {
   // references to other treelet nodes are kTreeletRef | treelet index.
   const DNode* treelet;
   int treelet_n;  // nodes in it (0: none)
+  // Per slot: 2 * (its leaf's parent DNode) + (1 if the leaf is the right
+  // child); -1 where the leaf is a scene's root. Null for device-built trees.
+  const int* slot_leaf;
 };
 
 }  // namespace trg

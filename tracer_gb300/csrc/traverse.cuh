@@ -127,6 +127,7 @@ __device__ __forceinline__ bool sphere_roots(f3 lo, f3 ld, float radius, float& 
 // units of the traversal's algorithmic-bytes figure).
 struct VisitCount {
   unsigned int boxes = 0, prims = 0;
+  unsigned int cache_hits = 0;  // any-hit rays answered by a remembered occluder
 };
 
 template <bool ANY, bool COUNT = false>
@@ -171,6 +172,41 @@ struct Traversal {
   }
 
 };
+
+// Any hit through a remembered occluder: slot s, tested after the box of its
+// BVH leaf (stored in the leaf's parent node). The slab test passes a box
+// whenever it passes a box inside it (rounding is monotone, a child's box
+// lies in its parent's, and the NaN cases of a slab plane through the origin
+// act like the parent's infinities), and the culling bound t_max is fixed for
+// any hits; so a ray that passes the leaf's box passes every box above it,
+// the reference's walk reaches the slot, and a hit there is the walk's answer
+// (occluded). A miss here says nothing: the walk follows.
+__device__ __forceinline__ bool occluded_by_slot(const DScene& sc, int scene, int s, f3 o, f3 d, float t_min,
+                                                 float t_max) {
+  const int lp = __ldg(sc.slot_leaf + s);
+  float lx, ly, lz, hx, hy, hz;
+  if (lp >= 0) {
+    const float4* np = reinterpret_cast<const float4*>(sc.nodes + (lp >> 1));
+    const float4 b = ldg4(np + 1);
+    if (lp & 1) {
+      const float4 c = ldg4(np + 2);
+      lx = b.z; ly = b.w; lz = c.x; hx = c.y; hy = c.z; hz = c.w;
+    } else {
+      const float4 a = ldg4(np);
+      lx = a.x; ly = a.y; lz = a.z; hx = a.w; hy = b.x; hz = b.y;
+    }
+  } else {
+    const SceneRoot& R = sc.roots[scene];
+    lx = R.lo[0]; ly = R.lo[1]; lz = R.lo[2]; hx = R.hi[0]; hy = R.hi[1]; hz = R.hi[2];
+  }
+  const f3 inv = mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+  float tmin;
+  if (!box_pass(lx, ly, lz, hx, hy, hz, o, inv, inv.x < 0.0f, inv.y < 0.0f, inv.z < 0.0f, tmin) || !(tmin < t_max))
+    return false;
+  Hit h;
+  float tm = t_max;
+  return Traversal<true>::test_slot(sc, s, o, d, t_min, tm, h);
+}
 
 // ---------------------------------------------------------------------------
 // Persistent traversal with dynamic fetch. Each lane runs the same per-ray
@@ -343,6 +379,7 @@ struct TravLane {
       if (COUNT) ++vc.prims;
       if (Traversal<ANY, COUNT>::test_slot(sc, pl + i, o, d, t_min, t_max, h)) {
         occluded = true;
+        h.prim = pl + i;  // any hit: the occluding slot
         return false;
       }
     }
@@ -400,6 +437,7 @@ struct TravLane {
       if (COUNT) ++vc.prims;
       if (Traversal<ANY, COUNT>::test_slot(sc, cur + i, o, d, t_min, t_max, h)) {
         occluded = true;
+        h.prim = cur + i;  // any hit: the occluding slot
         return false;
       }
     }
@@ -409,7 +447,9 @@ struct TravLane {
 
 // Job: unsigned count() const;
 //      void load(unsigned i, f3& o, f3& d, float& t_min, float& t_max, int& scene);
+//      int cached(unsigned i) const;  any hits: a slot to test first (occluded_by_slot), or -1
 //      void store(unsigned i, const Hit& h, float t_max, bool occluded).
+// For an occluded any-hit ray h.prim is the occluding slot.
 // tl_n: treelet nodes to stage in shared memory (the launch gives the block
 // at least tl_n * 64 bytes of dynamic shared memory; 0: none). The four-wide
 // walk does not use the treelet.
@@ -438,8 +478,16 @@ __device__ __forceinline__ void persistent_traverse(const DScene& sc, Job& job, 
           float tmin, tmax;
           int scene;
           job.load(item, o, d, tmin, tmax, scene);
-          live = L.start(sc, scene, o, d, tmin, tmax, vc, tl);
-          if (!live) job.store(item, L.h, L.t_max, false);
+          const int cs = ANY ? job.cached(item) : -1;
+          if (ANY && cs >= 0 && occluded_by_slot(sc, scene, cs, o, d, tmin, tmax)) {
+            ++vc.cache_hits;
+            L.h.prim = cs;
+            job.store(item, L.h, tmax, true);
+            live = false;
+          } else {
+            live = L.start(sc, scene, o, d, tmin, tmax, vc, tl);
+            if (!live) job.store(item, L.h, L.t_max, false);
+          }
         } else {
           exhausted = true;
         }
