@@ -534,7 +534,9 @@ def run_batch(args):
         "gpu_launches": int(sum(1 + 7 * s.iterations for s in stats)),
         "autotune": {"trav_refill_lanes": tuning.trav_refill_lanes, "trav_blocks_per_sm": tuning.trav_blocks_per_sm,
                      "shade_blocks_per_sm": tuning.shade_blocks_per_sm, "graph_iterations": tuning.graph_iterations,
-                     "any_node_width": tuning.any_node_width, "probe_ms": round(probe_ms, 2),
+                     "any_node_width": tuning.any_node_width, "ray_bin_bits": tuning.ray_bin_bits,
+                     "treelet_nodes": tuning.treelet_nodes, "occluder_cache": tuning.occluder_cache,
+                     "probe_ms": round(probe_ms, 2),
                      "tune_s": round(tune_s, 1)},
         "setup_s": {"generate": round(gen_s, 1), "upload_and_bvh": round(upload_s, 1)},
         "device_bvh": {"upload_and_bvh_s": round(dev_upload_s, 2), "msamples_per_s": round(dev_rate, 1),
