@@ -531,7 +531,7 @@ def run_batch(args):
                    "l2": "path state of all jobs exceeds L2; a 256 MiB buffer is written between timed steps"},
         "value_is": "camera samples per second over the whole batch (one tr_render_batch_dev call per step)",
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 64 * 200, "d2h_bytes_per_step": d2h},
-        "gpu_launches": int(sum(1 + 7 * s.iterations for s in stats)),
+        "gpu_launches": int(sum(launches_of(s) for s in stats)),
         "autotune": {"trav_refill_lanes": tuning.trav_refill_lanes, "trav_blocks_per_sm": tuning.trav_blocks_per_sm,
                      "shade_blocks_per_sm": tuning.shade_blocks_per_sm, "graph_iterations": tuning.graph_iterations,
                      "any_node_width": tuning.any_node_width, "ray_bin_bits": tuning.ray_bin_bits,
@@ -683,6 +683,21 @@ def _flagged(par, flags):
     return p
 
 
+def launches_of(st) -> int:
+    """Kernels one render launched: the persistent kernel's single launch
+    (iterations 1), else k_init and 7 kernels per wavefront iteration."""
+    return 1 if st.iterations == 1 else 1 + 7 * st.iterations
+
+
+def apply_tuning(ctx, spec: str | None) -> dict:
+    """--tuning key=value,...: tr_tuning fields set on the context."""
+    if not spec:
+        return {}
+    kv = {k.strip(): int(v) for k, v in (p.split("=") for p in spec.split(",") if p)}
+    ctx.set_tuning(**{("refill" if k == "trav_refill_lanes" else k): v for k, v in kv.items()})
+    return kv
+
+
 def run_ours(args):
     import torch
     from tracer_gb300.native import GpuContext
@@ -693,6 +708,7 @@ def run_ours(args):
     label, sc, cam, filt, par = workload(args.workload, args.size)
     ctx = GpuContext(local)
     ctx.upload(sc)
+    tuning = apply_tuning(ctx, args.tuning)
     nl = len(sc.light_prims)
     W, H = par.width, par.height
     stream = torch.cuda.ExternalStream(ctx.stream, device=local)
@@ -808,11 +824,13 @@ def run_ours(args):
                    "min_depth": par.min_depth, "lights": nl, "primitives": int(len(sc.prim_shape)),
                    "parallelism": f"replicas x{world}",
                    "l2": f"path state and queues ({W * H * (324 + 76 * max(nl, 1)) / 1e6:.0f} MB) exceed L2; "
-                         "a 256 MiB buffer is written between timed steps"},
+                         "a 256 MiB buffer is written between timed steps",
+                   "render_mode": "persistent kernel (one launch per render)" if stats[0].iterations == 1
+                   else "wavefront", **({"tuning": tuning} if tuning else {})},
         "value_is": "camera samples per second of the plain GPU path tracer (time-to-1% relMSE under "
                     "'convergence')",
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": W * H * 16},
-        "gpu_launches": int(sum(1 + 7 * s.iterations for s in stats)),
+        "gpu_launches": int(sum(launches_of(s) for s in stats)),
         "roofline": roof,
         "rays": {"extend": staged.extend_rays, "shadow": staged.shadow_rays,
                  "mrays_per_s": rays / (ms / args.steps / 1e3) / 1e6,
@@ -845,6 +863,7 @@ def main():
     ap.add_argument("--no-convergence", action="store_true", help="skip the time-to-1%% relMSE leg")
     ap.add_argument("--size", default=None, help="WxHxSPP override (profiling captures)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tuning", default=None, help="tr_tuning fields, e.g. render_mode=2,ray_bin_bits=0")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -272,7 +272,16 @@ tr_status tr_synchronize(tr_ctx* ctx);
  *    BVH leaf's box) before walking the tree. The slab test passes a box
  *    whenever it passes a box inside it, so a ray that passes the leaf's box
  *    passes every box above it: the reference's any-hit walk reaches that
- *    primitive, and a hit there gives the walk's answer. */
+ *    primitive, and a hit there gives the walk's answer.
+ *  - render_mode: TR_RENDER_MODE_WAVEFRONT runs a render (or a batch) as
+ *    the wavefront, about ten launches per path vertex over compacted queues;
+ *    TR_RENDER_MODE_PERSISTENT as one launch of the persistent kernel, each
+ *    thread running a pixel's samples with the path state in registers (the
+ *    launch and the film zeroing captured into a CUDA graph when
+ *    graph_iterations > 0); TR_RENDER_MODE_AUTO picks the persistent kernel
+ *    for renders of at most 2^18 pixels. Guided and instrumented renders
+ *    (TR_RENDER_TIME_STAGES, TR_RENDER_COUNT_VISITS) and scenes with more
+ *    than 16 lights always use the wavefront. Films are identical. */
 typedef struct tr_tuning {
   int32_t trav_refill_lanes;
   int32_t trav_blocks_per_sm;
@@ -282,7 +291,9 @@ typedef struct tr_tuning {
   int32_t ray_bin_bits;
   int32_t treelet_nodes;
   int32_t occluder_cache;
+  int32_t render_mode;
 } tr_tuning;
+enum { TR_RENDER_MODE_AUTO = 0, TR_RENDER_MODE_WAVEFRONT = 1, TR_RENDER_MODE_PERSISTENT = 2 };
 tr_status tr_ctx_set_tuning(tr_ctx* ctx, const tr_tuning* t);
 tr_status tr_ctx_get_tuning(const tr_ctx* ctx, tr_tuning* t);
 

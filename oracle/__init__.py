@@ -25,6 +25,7 @@ from tracer_gb300.abi import (NODE_DTYPE, RAY_DTYPE, TrCamera, TrFilter, TrRay, 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libtracer_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libtracer_ref.so")
+REF_SO_O0 = os.path.join(HERE, "_ref", "O0", "libtracer_ref.so")  # the as-shipped -O0 build (CPU-baseline record)
 # the reference checkout: a sibling of this repository unless TRACER_REF_ROOT says otherwise
 REF_ROOT = os.environ.get("TRACER_REF_ROOT", os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
@@ -64,7 +65,7 @@ def _load(kind: str) -> C.CDLL:
         lib = C.CDLL(PORT_SO)
         pre = "orc_"
     else:
-        lib = C.CDLL(REF_SO)
+        lib = C.CDLL(REF_SO_O0 if kind == "reference-O0" else REF_SO)
         pre = "ref_"
     vp, sz = C.c_void_p, C.c_size_t
     f32p, i32p, u32p, u8p = (C.POINTER(C.c_float), C.POINTER(C.c_int32), C.POINTER(C.c_uint32),
@@ -197,7 +198,7 @@ class Oracle:
 
     def render_stock_seconds(self, params: TrRenderParams, workers: int = 0):
         """Reference build only: time of the stock create_pt_renderer render()."""
-        assert self.kind == "reference"
+        assert self.kind.startswith("reference")
         return self.lib.ref_render_stock(self.h, C.byref(params), workers, None)
 
     def render_log(self, params: TrRenderParams, pix0: int, pix1: int):

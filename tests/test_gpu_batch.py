@@ -61,7 +61,8 @@ def test_graph_replay_changes_nothing(gpu):
             assert np.array_equal(o.view(np.uint32), outs[0].view(np.uint32))
     finally:
         gpu.set_tuning(old.trav_refill_lanes, old.trav_blocks_per_sm, old.shade_blocks_per_sm, old.graph_iterations,
-                       old.any_node_width, old.ray_bin_bits, old.treelet_nodes, old.occluder_cache)
+                       old.any_node_width, old.ray_bin_bits, old.treelet_nodes, old.occluder_cache,
+                       old.render_mode)
 
 
 def test_scene_set_traversal_uses_scene_zero(gpu):
@@ -98,4 +99,5 @@ def test_autotune_picks_a_valid_tuning_and_keeps_results(gpu):
             assert np.array_equal(b.view(np.uint32), f.cpu().numpy().view(np.uint32))
     finally:
         gpu.set_tuning(old.trav_refill_lanes, old.trav_blocks_per_sm, old.shade_blocks_per_sm, old.graph_iterations,
-                       old.any_node_width, old.ray_bin_bits, old.treelet_nodes, old.occluder_cache)
+                       old.any_node_width, old.ray_bin_bits, old.treelet_nodes, old.occluder_cache,
+                       old.render_mode)

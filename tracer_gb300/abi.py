@@ -119,11 +119,14 @@ class TrGuideParams(C.Structure):
                 ("max_records", C.c_uint32)]
 
 
+TR_RENDER_MODE_AUTO, TR_RENDER_MODE_WAVEFRONT, TR_RENDER_MODE_PERSISTENT = 0, 1, 2
+
+
 class TrTuning(C.Structure):
     _fields_ = [("trav_refill_lanes", C.c_int32), ("trav_blocks_per_sm", C.c_int32),
                 ("shade_blocks_per_sm", C.c_int32), ("graph_iterations", C.c_int32),
                 ("any_node_width", C.c_int32), ("ray_bin_bits", C.c_int32), ("treelet_nodes", C.c_int32),
-                ("occluder_cache", C.c_int32)]
+                ("occluder_cache", C.c_int32), ("render_mode", C.c_int32)]
 
 
 class TrBatchJob(C.Structure):

@@ -24,7 +24,7 @@ CU_FLAGS = ["-O3", "-std=c++17", *ARCH, "-lineinfo", "--fmad=false", "-Xptxas", 
             "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", f"-I{INCLUDE}"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", f"-I{INCLUDE}"]
 
-CU_SOURCES = ["context.cu", "render.cu", "selftest.cu", "mlp.cu", "bvh_gpu.cu", "post.cu", "env_light.cu"]
+CU_SOURCES = ["context.cu", "render.cu", "mega.cu", "selftest.cu", "mlp.cu", "bvh_gpu.cu", "post.cu", "env_light.cu"]
 CXX_SOURCES = ["bvh_build.cpp", "host_api.cpp", "image_out.cpp", "obj_load.cpp", "image_file.cpp"]
 
 

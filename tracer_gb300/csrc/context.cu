@@ -742,7 +742,8 @@ tr_status tr_ctx_set_tuning(tr_ctx* ctx, const tr_tuning* t) {
       t->trav_blocks_per_sm > 64 || t->shade_blocks_per_sm < 1 || t->shade_blocks_per_sm > 64 ||
       t->graph_iterations < 0 || t->graph_iterations > 64 || (t->any_node_width != 2 && t->any_node_width != 4) ||
       t->ray_bin_bits < 0 || t->ray_bin_bits > kBinBitsMax || t->treelet_nodes < 0 || t->treelet_nodes > kTreeletMax ||
-      (t->occluder_cache != 0 && t->occluder_cache != 1))
+      (t->occluder_cache != 0 && t->occluder_cache != 1) || t->render_mode < TR_RENDER_MODE_AUTO ||
+      t->render_mode > TR_RENDER_MODE_PERSISTENT)
     return set_err(ctx, TR_ERR_ARG, "tuning out of range");
   const bool restage = t->treelet_nodes != ctx->tune.treelet_nodes;
   ctx->tune = *t;

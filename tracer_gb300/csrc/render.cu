@@ -40,6 +40,8 @@
 #include "mixture.cuh"
 #include "mlp.h"
 #include "binning.cuh"
+#include "mega.h"
+#include "render_common.cuh"
 #include "shade.cuh"
 #include "traverse.cuh"
 
@@ -54,17 +56,6 @@ enum : int {
   F_GX = 32,        // ...and so is a ray drawn from the mixture alone (in the MIS slot)
   F_SPEC = 64,      // the continuation was sampled from a delta BSDF: emission it reaches counts
 };
-
-// PathTraceRenderer::max_specular_depth (src/renderer/path_trace_renderer.cpp:20):
-// delta samples that do not count toward the path depth
-constexpr int kMaxSpecularDepth = 20;
-
-// P1.w holds the path depth (low 16 bits) and the count of delta samples
-// that did not count toward it (high bits). The depth must stay below 2^16
-// with the uncounted delta samples on top: larger max_depth is rejected.
-constexpr int kMaxPathDepth = 0xffff - kMaxSpecularDepth;
-__device__ __forceinline__ int path_depth(float w) { return __float_as_int(w) & 0xffff; }
-__device__ __forceinline__ int spec_depth(float w) { return __float_as_int(w) >> 16; }
 
 // light-sample queue of a material kind (glass has none)
 __host__ __device__ constexpr int nee_index(int kind) {
@@ -86,6 +77,8 @@ constexpr int kCtrWords = 32;  // the counter array
 // Statistics words: samples, extend rays, shadow rays, shade items, visit
 // counts (4-7), occluder-cache hits (8).
 constexpr int kStatWords = 16;
+// render_mode auto: renders of at most this many pixels use the persistent kernel
+constexpr long long kMegaAutoSlots = 1 << 18;
 // Material code in the shading context: the material index, or with this bit
 // set the slot's own set-up in Launch::MT (a Phong material with maps).
 constexpr int kMatScratch = 1 << 30;
@@ -103,20 +96,6 @@ struct RenderBuffers {
   unsigned int tb_count = 0, tb_cap = 0;  // training records of the last guided render
   unsigned int* h_active = nullptr;  // pinned: live-slot count per check
   std::vector<cudaEvent_t> ev_pool;  // reused by stage timing
-};
-
-// One render of a batch: a scene of the set seen through a camera onto a
-// film. Its path slots are slot_base .. slot_base + W * H - 1, one per pixel.
-struct JobDev {
-  Cam cam;
-  int W, H, spp, min_depth, max_depth;
-  unsigned int seed_base;
-  int scene, slot_base;
-  int light_base, nl;  // the scene's lights in DScene::lights
-  int env;             // the scene's environment light in DScene::envs (its last light), or -1
-  float filter_radius, filter_alpha, filter_exp;
-  int fp64;
-  float4* film;  // film sums (float4 per pixel, or 2 x double2)
 };
 
 struct Launch {
@@ -164,16 +143,8 @@ struct Launch {
   unsigned int tb_cap;
 };
 
-// The job a path slot belongs to (slot bases ascend with the job index).
-__device__ __forceinline__ const JobDev& job_of(const Launch& P, int slot) {
-  int lo = 0, hi = P.njobs - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (P.jobs[mid].slot_base <= slot) lo = mid;
-    else hi = mid - 1;
-  }
-  return P.jobs[lo];
-}
+// The job a path slot belongs to.
+__device__ __forceinline__ const JobDev& job_of(const Launch& P, int slot) { return job_of(P.jobs, P.njobs, slot); }
 
 // Network inputs of a vertex: position in the scene box mapped to [-1, 1],
 // outgoing direction, roughness.
@@ -209,62 +180,6 @@ __device__ __forceinline__ void count_add(unsigned long long* c, unsigned int v)
   const unsigned int peers = __match_any_sync(active, (unsigned long long)c);
   const unsigned int s = __reduce_add_sync(peers, v);
   if ((int)(threadIdx.x & 31u) == __ffs(peers) - 1 && s) atomicAdd(c, (unsigned long long)s);
-}
-
-// Film::Tile::add_sample (src/core/render.hpp:37-57). With radius <= 0.5 a
-// sample reaches only its own pixel with non-zero weight (neighbours get
-// exactly 0), so the slot owns its pixel and adds in sample order.
-__device__ __forceinline__ void film_add(const JobDev& J, int slot, float px, float py, f3 L) {
-  const int pix = slot - J.slot_base;
-  const int x = pix % J.W, y = pix / J.W;
-  if (J.filter_radius <= 0.5f) {
-    const float ox = px - ((float)x + 0.5f), oy = py - ((float)y + 0.5f);  // exact for W, H < 2^23
-    const float fw = gaussian(J.filter_alpha, ox, J.filter_exp) * gaussian(J.filter_alpha, oy, J.filter_exp);
-    const f3 c = muls(muls(L, fw), 1.0f);
-    if (J.fp64) {
-      double2* a = reinterpret_cast<double2*>(J.film) + 2 * pix;
-      double2 a0 = a[0], a1 = a[1];
-      a0.x += c.x;
-      a0.y += c.y;
-      a1.x += c.z;
-      a1.y += fw;
-      a[0] = a0;
-      a[1] = a1;
-    } else {
-      float4 a = J.film[pix];
-      a.x += c.x;
-      a.y += c.y;
-      a.z += c.z;
-      a.w += fw;
-      J.film[pix] = a;
-    }
-    return;
-  }
-  // wider filters: scatter with atomics (order of additions not fixed)
-  const float r = J.filter_radius;
-  const float dx = px - 0.5f, dy = py - 0.5f;
-  const int x0 = max((int)ceilf(dx - r), 0), y0 = max((int)ceilf(dy - r), 0);
-  const int x1 = min((int)floorf(dx + r) + 1, J.W), y1 = min((int)floorf(dy + r) + 1, J.H);
-  for (int yy = y0; yy < y1; ++yy)
-    for (int xx = x0; xx < x1; ++xx) {
-      const float ox = px - ((float)xx + 0.5f), oy = py - ((float)yy + 0.5f);
-      const float fw = gaussian(J.filter_alpha, ox, J.filter_exp) * gaussian(J.filter_alpha, oy, J.filter_exp);
-      const f3 c = muls(muls(L, fw), 1.0f);
-      const int o = yy * J.W + xx;
-      if (J.fp64) {
-        double* a = reinterpret_cast<double*>(J.film) + 4 * o;
-        atomicAdd(a, (double)c.x);
-        atomicAdd(a + 1, (double)c.y);
-        atomicAdd(a + 2, (double)c.z);
-        atomicAdd(a + 3, (double)fw);
-      } else {
-        float* a = reinterpret_cast<float*>(J.film) + 4 * o;
-        atomicAdd(a, c.x);
-        atomicAdd(a + 1, c.y);
-        atomicAdd(a + 2, c.z);
-        atomicAdd(a + 3, fw);
-      }
-    }
 }
 
 // Starts the slot's next camera sample, finishing samples that Russian
@@ -1434,6 +1349,22 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   cudaGraphExec_t gexec = nullptr;
   const bool timed = (flags & TR_RENDER_TIME_STAGES) != 0;
   const bool count = (flags & TR_RENDER_COUNT_VISITS) != 0;
+  // the persistent kernel (tr_tuning.render_mode) for plain renders whose
+  // scenes have at most kMegaLights lights; by default for renders of at most
+  // kMegaAutoSlots pixels, which the wavefront's launches cannot fill the GPU with
+  bool mega = false;
+  unsigned mmask = 0;
+  int mgrid = 0;
+  if (!gp && !timed && !count && nl <= kMegaLights && ctx->tune.render_mode != TR_RENDER_MODE_WAVEFRONT) {
+    mega = ctx->tune.render_mode == TR_RENDER_MODE_PERSISTENT || (long long)n <= kMegaAutoSlots;
+    if (mega) {
+      bool d12 = false;
+      for (const DMat& m : ctx->hs.mats) d12 |= m.kind == MAT_DISNEY12;
+      mmask = mega_kernel_mask(ctx->dsc, d12);
+      const long long want = ((long long)n + kMegaThreads - 1) / kMegaThreads;
+      mgrid = (int)std::min<long long>(want, (long long)sms * mega_blocks_per_sm(mmask));
+    }
+  }
   std::vector<cudaEvent_t>& ev = rb->ev_pool;
   size_t nev = 0;
   auto cleanup = [&]() {
@@ -1451,6 +1382,61 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
       return cuda_fail(ctx, e_, #call); \
     }                                   \
   } while (0)
+  if (mega) {
+    // The persistent kernel: every sample of every job in one launch. With
+    // graphs enabled, the zeroing of the films and counters and the launch
+    // are captured into one CUDA graph and replayed as one launch.
+    MegaLaunch M;
+    M.sc = P.sc;
+    M.jobs = P.jobs;
+    M.njobs = njobs;
+    M.nslots = n;
+    M.nl_max = nl;
+    M.occluder_cache = ctx->tune.occluder_cache;
+    M.fetch = P.ctr + C_FEXT;
+    M.err = (int*)(P.ctr + C_ERR);
+    M.stats = P.stats;
+    const bool use_graph = ctx->tune.graph_iterations > 0;
+    RCHK(cudaEventRecord(e0, st));
+    if (use_graph) RCHK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t le = cudaSuccess;
+    for (int k = 0; k < njobs && le == cudaSuccess; ++k)
+      le = cudaMemsetAsync(jd[k].film, 0, (size_t)jd[k].W * jd[k].H * (jd[k].fp64 ? 32 : 16), st);
+    if (le == cudaSuccess) le = cudaMemsetAsync(P.ctr, 0, kCtrWords * 4, st);
+    if (le == cudaSuccess) le = cudaMemsetAsync(P.stats, 0, kStatWords * 8, st);
+    if (le == cudaSuccess) le = launch_mega(M, mmask, mgrid, st);
+    if (use_graph) {
+      const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+      if (le == cudaSuccess) le = ce;
+      if (le == cudaSuccess) le = cudaGraphInstantiate(&gexec, graph, 0);
+      if (le == cudaSuccess) le = cudaGraphLaunch(gexec, st);
+    }
+    RCHK(le);
+    RCHK(cudaEventRecord(e1, st));
+    RCHK(cudaEventSynchronize(e1));
+    unsigned long long hs[kStatWords] = {};
+    RCHK(cudaMemcpy(hs, P.stats, sizeof(hs), cudaMemcpyDeviceToHost));
+    unsigned int ctrs[kCtrWords];
+    RCHK(cudaMemcpy(ctrs, P.ctr, sizeof(ctrs), cudaMemcpyDeviceToHost));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cleanup();
+    tr_status result = TR_OK;
+    if (ctrs[C_ERR] & 1u) result = set_err(ctx, TR_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
+    else if (ctrs[C_ERR] & 2u) result = set_err(ctx, TR_ERR_TIMEOUT, "a path slot ran past its vertex bound");
+    rb->tb_count = 0;
+    if (stats) {
+      std::memset(stats, 0, sizeof(*stats));
+      stats->samples = hs[0];
+      stats->extend_rays = hs[1];
+      stats->shadow_rays = hs[2];
+      stats->shade_items = hs[3];
+      stats->iterations = 1;
+      stats->device_ms = ms;
+      stats->occluder_hits = hs[8];
+    }
+    return result;
+  }
   for (int k = 0; k < njobs; ++k)
     RCHK(cudaMemsetAsync(jd[k].film, 0, (size_t)jd[k].W * jd[k].H * (jd[k].fp64 ? 32 : 16), st));
   RCHK(cudaMemsetAsync(P.ctr, 0, kCtrWords * 4, st));
@@ -1917,35 +1903,31 @@ extern "C" tr_status tr_autotune(tr_ctx* ctx, const tr_batch_job* jobs, uint32_t
     ms = v[1];
     return TR_OK;
   };
-  // coordinate descent over the discrete settings
-  static const int kBlocks[] = {0, 4, 6, 8}, kRefill[] = {12, 20, 28}, kShade[] = {8, 16, 32},
-                   kGraph[] = {0, 4, 8, 16}, kWidth[] = {2, 4}, kBins[] = {0, 3, 4}, kTreelet[] = {0, 64, 256};
+  // coordinate descent over the discrete settings, the execution model first
+  static const int kMode[] = {TR_RENDER_MODE_WAVEFRONT, TR_RENDER_MODE_PERSISTENT}, kBlocks[] = {0, 4, 6, 8},
+                   kRefill[] = {12, 20, 28}, kShade[] = {8, 16, 32}, kGraph[] = {0, 4, 8, 16}, kWidth[] = {2, 4},
+                   kBins[] = {0, 3, 4}, kTreelet[] = {0, 64, 256}, kCache[] = {0, 1};
+  struct Dim {
+    int32_t tr_tuning::*field;
+    const int* vals;
+    int nv;
+  };
+  static const Dim kDims[] = {{&tr_tuning::render_mode, kMode, 2},        {&tr_tuning::trav_blocks_per_sm, kBlocks, 4},
+                              {&tr_tuning::trav_refill_lanes, kRefill, 3}, {&tr_tuning::shade_blocks_per_sm, kShade, 3},
+                              {&tr_tuning::graph_iterations, kGraph, 4},   {&tr_tuning::any_node_width, kWidth, 2},
+                              {&tr_tuning::ray_bin_bits, kBins, 3},        {&tr_tuning::treelet_nodes, kTreelet, 3},
+                              {&tr_tuning::occluder_cache, kCache, 2}};
   tr_tuning cur = ctx->tune;
   double cur_ms = 0.0;
   tr_status s = time_once(cur, cur_ms);
   if (s != TR_OK) return s;
   for (int pass = 0; pass < 2; ++pass) {
     bool improved = false;
-    for (int dim = 0; dim < 7; ++dim) {
-      const int* vals = dim == 0   ? kBlocks
-                        : dim == 1 ? kRefill
-                        : dim == 2 ? kShade
-                        : dim == 3 ? kGraph
-                        : dim == 4 ? kWidth
-                        : dim == 5 ? kBins
-                                   : kTreelet;
-      const int nv = dim == 0 || dim == 3 ? 4 : dim == 4 ? 2 : 3;
-      for (int k = 0; k < nv; ++k) {
+    for (const Dim& dim : kDims) {
+      for (int k = 0; k < dim.nv; ++k) {
         tr_tuning t = cur;
-        int* field = dim == 0   ? &t.trav_blocks_per_sm
-                     : dim == 1 ? &t.trav_refill_lanes
-                     : dim == 2 ? &t.shade_blocks_per_sm
-                     : dim == 3 ? &t.graph_iterations
-                     : dim == 4 ? &t.any_node_width
-                     : dim == 5 ? &t.ray_bin_bits
-                                : &t.treelet_nodes;
-        if (*field == vals[k]) continue;
-        *field = vals[k];
+        if (t.*dim.field == dim.vals[k]) continue;
+        t.*dim.field = dim.vals[k];
         double ms = 0.0;
         s = time_once(t, ms);
         if (s != TR_OK) return s;

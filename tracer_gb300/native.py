@@ -226,8 +226,11 @@ class GpuContext:
     def set_tuning(self, refill: int | None = None, trav_blocks_per_sm: int | None = None,
                    shade_blocks_per_sm: int | None = None, graph_iterations: int | None = None,
                    any_node_width: int | None = None, ray_bin_bits: int | None = None,
-                   treelet_nodes: int | None = None, occluder_cache: int | None = None) -> None:
+                   treelet_nodes: int | None = None, occluder_cache: int | None = None,
+                   render_mode: int | None = None) -> None:
         t = self.tuning()
+        if render_mode is not None:
+            t.render_mode = render_mode
         if occluder_cache is not None:
             t.occluder_cache = occluder_cache
         if ray_bin_bits is not None:
