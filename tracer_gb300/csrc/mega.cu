@@ -36,14 +36,23 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 
+// What a trace gives back: the hit record (any hit: the occluding slot in
+// prim) and whether the ray is occluded.
+struct Traced {
+  Hit h;
+  bool occluded;
+};
+
 // Closest hit (ANY = false) or occlusion (ANY = true) of every lane's ray,
 // the 32 lanes walking together: the speculative while-while of
 // persistent_traverse without its refill. Lanes with `active` false take no
-// part in the walk; every lane of the warp must call it.
-// Out of line: one copy serves the extension and the MIS ray.
+// part in the walk; every lane of the warp must call it. Out of line: one
+// copy serves the extension and the MIS ray; the walk's state is local to the
+// call (registers, its stack in local memory).
 template <bool ANY>
-__device__ __noinline__ void warp_trace(const DScene& sc, TravLane<ANY, false>& L, bool active, int scene, f3 o,
-                                        f3 d, float tmin, float tmax, int* err) {
+__device__ __noinline__ Traced warp_trace(const DScene& sc, bool active, int scene, f3 o, f3 d, float tmin,
+                                          float tmax, int* err) {
+  TravLane<ANY, false> L;
   VisitCount vc;
   bool live = active && L.start(sc, scene, o, d, tmin, tmax, vc, false);
   if (!active) {
@@ -65,6 +74,7 @@ __device__ __noinline__ void warp_trace(const DScene& sc, TravLane<ANY, false>& 
     if (live) live = L.postponed_leaf(sc, vc);
     if (!__any_sync(kFull, live)) break;
   }
+  return Traced{L.h, L.occluded};
 }
 
 // Material dispatch limited to the kinds of the instantiation (the sampler
@@ -157,8 +167,6 @@ template <unsigned MASK>
 __global__ void __launch_bounds__(kMegaThreads, 2) k_mega(MegaLaunch P) {
   const DScene& sc = P.sc;
   const int lane = (int)(threadIdx.x & 31u);
-  TravLane<false, false> TC;
-  TravLane<true, false> TA;
   Path p;
   p.slot = -1;
   p.has_ray = false;
@@ -201,7 +209,7 @@ __global__ void __launch_bounds__(kMegaThreads, 2) k_mega(MegaLaunch P) {
 
     // ---- extend: closest hit of the continuation or camera ray (k_extend)
     const int scene = p.has_ray ? p.J->scene : 0;
-    warp_trace<false>(sc, TC, p.has_ray, scene, p.o, p.d, 0.0f, kRealMax, P.err);
+    const Traced ext = warp_trace<false>(sc, p.has_ray, scene, p.o, p.d, 0.0f, kRealMax, P.err);
     n_ext += p.has_ray;
 
     // ---- vertex (k_logic, then k_material / k_glass)
@@ -219,8 +227,8 @@ __global__ void __launch_bounds__(kMegaThreads, 2) k_mega(MegaLaunch P) {
         p.has_ray = false;
         p.slot = -1;
       } else {
-        const int pid = TC.h.prim;
-        const float4 hit = make_float4(__int_as_float(pid), TC.h.t_attr, TC.h.alpha, TC.h.beta);
+        const int pid = ext.h.prim;
+        const float4 hit = make_float4(__int_as_float(pid), ext.h.t_attr, ext.h.alpha, ext.h.beta);
         if (pid < 0) {
           // a camera ray or one after a delta sample left the scene: the
           // environment light's radiance along it (path_trace_renderer.cpp:66-81)
@@ -419,10 +427,10 @@ __global__ void __launch_bounds__(kMegaThreads, 2) k_mega(MegaLaunch P) {
       }
       n_sh += trace;
       if (__any_sync(kFull, walk)) {
-        warp_trace<true>(sc, TA, walk, walk ? p.J->scene : 0, so, sd, kEps, dist, P.err);
-        if (walk && TA.occluded) {
+        const Traced sh = warp_trace<true>(sc, walk, walk ? p.J->scene : 0, so, sd, kEps, dist, P.err);
+        if (walk && sh.occluded) {
           blocked = true;
-          oc[l] = TA.h.prim;
+          oc[l] = sh.h.prim;
         }
       }
       if (trace && !blocked) direct = direct + cc;
@@ -431,10 +439,10 @@ __global__ void __launch_bounds__(kMegaThreads, 2) k_mega(MegaLaunch P) {
     // ---- mis: the BSDF-sampled ray's emission, weighted against the light
     //      (mis_contribution of render.cu, direct_illumination.cpp:144-198)
     if (__any_sync(kFull, mis)) {
-      warp_trace<false>(sc, TC, mis, mis ? p.J->scene : 0, mo, md, 0.0f, kRealMax, P.err);
+      const Traced mh = warp_trace<false>(sc, mis, mis ? p.J->scene : 0, mo, md, 0.0f, kRealMax, P.err);
       n_ext += mis;
       if (mis) {
-        const int pid = TC.h.prim;
+        const int pid = mh.h.prim;
         f3 c = mk3(0.0f, 0.0f, 0.0f);
         if (pid < 0) {
           const int ei = p.J->env;
@@ -453,7 +461,7 @@ __global__ void __launch_bounds__(kMegaThreads, 2) k_mega(MegaLaunch P) {
             const f3 gz = sc.tshade[pr.shape].gz;
             if (dot(gz, -md) > 0.0f) {
               const f3 f = muls(mulc(pr.emission, mf), mcos);
-              const f3 pos = mo + scale(md, TC.h.t_attr);
+              const f3 pos = mo + scale(md, mh.h.t_attr);
               const float lpdf = light_pdf_at(pr.area, mo, pos, gz);
               const float w = power_heuristic(mpdf, lpdf);
               c = divs(muls(f, w), mpdf);
