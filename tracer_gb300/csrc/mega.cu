@@ -164,7 +164,7 @@ __device__ __forceinline__ void finish_sample(Path& p) {
 }
 
 template <unsigned MASK>
-__global__ void __launch_bounds__(kMegaThreads, 2) k_mega(MegaLaunch P) {
+__global__ void __launch_bounds__(kMegaThreads, 1) k_mega(MegaLaunch P) {
   const DScene& sc = P.sc;
   const int lane = (int)(threadIdx.x & 31u);
   Path p;
@@ -205,13 +205,16 @@ __global__ void __launch_bounds__(kMegaThreads, 2) k_mega(MegaLaunch P) {
         }
       }
     }
-    if (__all_sync(kFull, done)) break;
+    // the block goes through the phases together (one phase's code in the
+    // instruction cache at a time); it ends when all its lanes are done
+    if (!__syncthreads_or(!done)) break;
 
     // ---- extend: closest hit of the continuation or camera ray (k_extend)
     const int scene = p.has_ray ? p.J->scene : 0;
     const Traced ext = warp_trace<false>(sc, p.has_ray, scene, p.o, p.d, 0.0f, kRealMax, P.err);
     n_ext += p.has_ray;
 
+    __syncthreads();
     // ---- vertex (k_logic, then k_material / k_glass)
     bool vertex = false, term = false, mis = false;
     int kind = 0, mcode = 0;
@@ -350,6 +353,7 @@ __global__ void __launch_bounds__(kMegaThreads, 2) k_mega(MegaLaunch P) {
       }
     }
 
+    __syncthreads();
     // ---- lights: the light sample and its shadow ray per light (k_nee, k_shadow)
     f3 direct = mk3(0.0f, 0.0f, 0.0f);
     Bsdf bsdf;
@@ -436,6 +440,7 @@ __global__ void __launch_bounds__(kMegaThreads, 2) k_mega(MegaLaunch P) {
       if (trace && !blocked) direct = direct + cc;
     }
 
+    __syncthreads();
     // ---- mis: the BSDF-sampled ray's emission, weighted against the light
     //      (mis_contribution of render.cu, direct_illumination.cpp:144-198)
     if (__any_sync(kFull, mis)) {
