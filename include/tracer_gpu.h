@@ -279,7 +279,7 @@ tr_status tr_synchronize(tr_ctx* ctx);
  *    thread running a pixel's samples with the path state in registers (the
  *    launch and the film zeroing captured into a CUDA graph when
  *    graph_iterations > 0); TR_RENDER_MODE_AUTO picks the persistent kernel
- *    for renders of at most 2^18 pixels. Guided and instrumented renders
+ *    for renders of at most 2^17 pixels. Guided and instrumented renders
  *    (TR_RENDER_TIME_STAGES, TR_RENDER_COUNT_VISITS) and scenes with more
  *    than 16 lights always use the wavefront. Films are identical. */
 typedef struct tr_tuning {

@@ -41,6 +41,6 @@ unsigned mega_kernel_mask(const DScene& sc, bool has_disney12);
 cudaError_t launch_mega(const MegaLaunch& P, unsigned mask, int grid, cudaStream_t st);
 // Resident blocks per SM of that instantiation.
 int mega_blocks_per_sm(unsigned mask);
-constexpr int kMegaThreads = 256;
+constexpr int kMegaThreads = 512;
 
 }  // namespace trg

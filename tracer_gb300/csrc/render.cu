@@ -78,7 +78,7 @@ constexpr int kCtrWords = 32;  // the counter array
 // counts (4-7), occluder-cache hits (8).
 constexpr int kStatWords = 16;
 // render_mode auto: renders of at most this many pixels use the persistent kernel
-constexpr long long kMegaAutoSlots = 1 << 18;
+constexpr long long kMegaAutoSlots = 1 << 17;
 // Material code in the shading context: the material index, or with this bit
 // set the slot's own set-up in Launch::MT (a Phong material with maps).
 constexpr int kMatScratch = 1 << 30;
