@@ -367,7 +367,7 @@ def run_reference(args):
         line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(args.steps, 1),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic (seeded procedural scenes)", "config": {"workload": label},
+                "data": "synthetic (seeded procedural scenes)", "config": batch_config(args.gpus),
                 "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                                  "sample": f"{nrows} rows per step of one of the batch's first four jobs in turn, "
                                            "CPU restatement of the reference (oracle/tracer_oracle.cpp)"},
@@ -394,7 +394,7 @@ def run_reference(args):
                 "value": value, "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": 1e3 * dt / max(args.steps, 1), "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded random triangles and rays)",
-                "config": {"workload": label},
+                "config": traversal_config(args.gpus),
                 "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
                                  "sample": f"{m} closest-hit and {m} shadow rays per step, CPU restatement of "
                                            "BVHAccel::intersect_p / intersect (oracle/tracer_oracle.cpp)"},
@@ -420,8 +420,7 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded procedural scene)",
-            "config": {"workload": label, "width": par.width, "height": par.height, "spp": par.spp,
-                       "max_depth": par.max_depth, "min_depth": par.min_depth},
+            "config": frame_config(label, sc, par, args.gpus),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{nrows} rows spread over the frame per step at {par.spp} spp, "
                                        "CPU restatement of the reference (oracle/tracer_oracle.cpp)"},
@@ -526,9 +525,8 @@ def run_batch(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (64 seeded procedural scenes, no dataset)",
-        "config": {"workload": "batch_64_scenes_10k_2M_tris_mixed_res_spp_depth6", "scenes": 64, "triangles": tris,
-                   "samples_per_step": int(stats[0].samples), "parallelism": f"replicas x{world}",
-                   "l2": "path state of all jobs exceeds L2; a 256 MiB buffer is written between timed steps"},
+        "config": batch_config(world),
+        "workload_detail": {"triangles": tris, "samples_per_step": int(stats[0].samples)},
         "value_is": "camera samples per second over the whole batch (one tr_render_batch_dev call per step)",
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 64 * 200, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(sum(launches_of(s) for s in stats)),
@@ -652,9 +650,7 @@ def run_traversal(args):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded random triangles and rays, no dataset)",
-        "config": {"workload": "traversal_1M_tris_leaf4_4M_closest_4M_shadow_rays", "triangles": n_tris,
-                   "rays_per_step": 2 * n_rays, "parallelism": f"replicas x{world}",
-                   "l2": "a 256 MiB buffer is written before each timed step (nodes + slots ~ 90 MB, rays 256 MB)"},
+        "config": traversal_config(world),
         "e2e": {"value": e2e, "unit": "Mrays/s", "h2d_bytes_per_step": 2 * 32 * n_rays,
                 "d2h_bytes_per_step": n_rays * 8 + n_rays},
         "gpu_launches": 2 * args.steps,
@@ -681,6 +677,32 @@ def _flagged(par, flags):
     ctypes.memmove(ctypes.byref(p), ctypes.byref(par), ctypes.sizeof(p))
     p.flags = flags
     return p
+
+
+def frame_config(label, sc, par, gpus) -> dict:
+    """The workload of a frame bench: identical in both arms' JSON lines."""
+    nl = int(len(sc.light_prims))
+    W, H = par.width, par.height
+    return {"workload": label, "width": W, "height": H, "spp": par.spp, "max_depth": par.max_depth,
+            "min_depth": par.min_depth, "lights": nl, "primitives": int(len(sc.prim_shape)),
+            "parallelism": f"replicas x{gpus}",
+            "l2": f"path state and queues ({W * H * (324 + 76 * max(nl, 1)) / 1e6:.0f} MB) exceed L2; "
+                  "a 256 MiB buffer is written between timed steps"}
+
+
+BATCH_LABEL = "batch_64_scenes_10k_2M_tris_mixed_res_spp_depth6"
+TRAVERSAL_LABEL = "traversal_1M_tris_leaf4_4M_closest_4M_shadow_rays"
+
+
+def batch_config(gpus) -> dict:
+    return {"workload": BATCH_LABEL, "scenes": 64, "parallelism": f"replicas x{gpus}",
+            "l2": "path state of all jobs exceeds L2; a 256 MiB buffer is written between timed steps"}
+
+
+def traversal_config(gpus) -> dict:
+    return {"workload": TRAVERSAL_LABEL, "triangles": 1 << 20, "rays_per_step": 2 << 22,
+            "parallelism": f"replicas x{gpus}",
+            "l2": "a 256 MiB buffer is written before each timed step (nodes + slots ~ 90 MB, rays 256 MB)"}
 
 
 def launches_of(st) -> int:
@@ -820,13 +842,9 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene, no dataset)",
-        "config": {"workload": label, "width": W, "height": H, "spp": par.spp, "max_depth": par.max_depth,
-                   "min_depth": par.min_depth, "lights": nl, "primitives": int(len(sc.prim_shape)),
-                   "parallelism": f"replicas x{world}",
-                   "l2": f"path state and queues ({W * H * (324 + 76 * max(nl, 1)) / 1e6:.0f} MB) exceed L2; "
-                         "a 256 MiB buffer is written between timed steps",
-                   "render_mode": "persistent kernel (one launch per render)" if stats[0].iterations == 1
-                   else "wavefront", **({"tuning": tuning} if tuning else {})},
+        "config": frame_config(label, sc, par, world),
+        "render_mode": "persistent kernel (one launch per render)" if stats[0].iterations == 1 else "wavefront",
+        **({"tuning": tuning} if tuning else {}),
         "value_is": "camera samples per second of the plain GPU path tracer (time-to-1% relMSE under "
                     "'convergence')",
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": W * H * 16},
