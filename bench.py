@@ -13,7 +13,7 @@ camera samples per second over exactly K steps (CUDA events on the
 renderer's stream, synchronised on both sides, maximum over ranks); `e2e`
 repeats the measurement through the C ABI's host-buffer entry point
 (tr_render), which copies the film back every step. `convergence` times the
-plain and the guided path tracer to 1% relMSE against a 2048-spp FP64
+plain and the guided path tracer to 1% relMSE against a 4096-spp FP64
 reference of the same scene at 1024x768.
 
 --impl reference times the reference algorithm on the host cores instead:
@@ -123,8 +123,9 @@ def _image(acc: np.ndarray) -> np.ndarray:
 GUIDE_BOX = {"occluded_room": ((-4.0, 0.0, -3.0), (4.0, 4.0, 3.0))}
 
 
-def convergence(ctx, name: str, size=(1024, 768), ref_spp=2048, pass_spp=8, max_spp=768, target=0.01,
-                alpha=0.25, train_steps=24, warm_steps=200, batch=65536, lr=1e-3, record_every=8):
+def convergence(ctx, name: str, size=(1024, 768), ref_spp=4096, pass_spp=8, max_spp=768, target=0.01,
+                alpha=0.25, train_steps=24, warm_steps=200, batch=65536, lr=1e-3, record_every=8,
+                light_grid=(32, 16, 24), light_bins=8, light_share=0.2):
     """Time for the plain and the guided GPU path tracer to reach `target`
     relMSE against a converged reference of the same scene. The reference
     is ref_spp samples per pixel accumulated in double. Each run adds
@@ -139,7 +140,12 @@ def convergence(ctx, name: str, size=(1024, 768), ref_spp=2048, pass_spp=8, max_
     (`warm_steps` more after the first pass; online training is inside the
     timed region). If a training
     loss is not finite the network is re-initialised and the next pass
-    renders plainly (the plain path is the fallback)."""
+    renders plainly (the plain path is the fallback). The guided run also
+    learns its light samples: every pass draws each area light's point from
+    the light table (`light_grid` cells over the guide box, `light_bins`^2
+    cells of the light's sample square, `light_share` of the uniform density
+    mixed in) and records its unoccluded light samples, and the table is
+    rebuilt from all passes so far after each pass."""
     from tracer_gb300.abi import make_guide
     W, H = size
     _, sc, cam, filt, par = workload(name, f"{W}x{H}x{pass_spp}")
@@ -159,13 +165,16 @@ def convergence(ctx, name: str, size=(1024, 768), ref_spp=2048, pass_spp=8, max_
         use_alpha = 0.0
         if guided:
             ctx.guide_init(seed=0)
+            ctx.guide_light_init(light_grid, light_bins)
         for k in range(max_spp // pass_spp):
             p = scenes.make_params(W, H, pass_spp, par.min_depth, par.max_depth, seed_base=1 + k * W * H)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             if guided:
-                ctx.render_guided_dev(cam, filt, p, make_guide(use_alpha, *box, record=record_every),
+                ctx.render_guided_dev(cam, filt, p, make_guide(use_alpha, *box, record=record_every,
+                                                               light_guide=True, light_record=True),
                                       film.data_ptr(), fp64=True)
+                ctx.guide_light_update(light_share)
                 loss = ctx.guide_train_on_records(train_steps + (warm_steps if k == 0 else 0), batch, lr, seed=k)
                 if np.isfinite(loss):
                     use_alpha = alpha
@@ -191,6 +200,7 @@ def convergence(ctx, name: str, size=(1024, 768), ref_spp=2048, pass_spp=8, max_
         if guided:
             res.update({"alpha": alpha, "train_steps_per_pass": train_steps, "warm_steps": warm_steps, "batch": batch,
                         "lr": lr, "record_every": record_every,
+                        "light_table": {"grid": list(light_grid), "bins": light_bins, "uniform_share": light_share},
                         "mean_loss_per_pass": losses[:8] + (["..."] if len(losses) > 9 else []) + losses[-1:]})
         return res
 

@@ -507,14 +507,40 @@ tr_status tr_guide_train_step_dev(tr_ctx* ctx, const float* d_in, const float* d
  * samples of a pixel (sample index % n == 0) also become training records
  * (network input, direction, incident-radiance estimate / pdf), up to
  * max_records (0: 4M), for tr_guide_train_on_records. The random stream
- * differs from the plain renderer's when alpha > 0. */
+ * differs from the plain renderer's when alpha > 0.
+ * Learned light sampling (light_guide = 1, after tr_guide_light_init): the
+ * point on each area light is drawn from the context's light table instead
+ * of uniformly -- per cell of a grid over the guide box and per light, a
+ * distribution over bins x bins cells of the light's sample square, mixed
+ * with the uniform one -- and the light sample's estimate is divided by that
+ * density over the uniform one. The MIS weights stay the reference's, so
+ * the estimate's expectation is unchanged and the image converges to the
+ * plain renderer's. With light_record = 1 the unoccluded light samples of
+ * the render are added to the table's statistics (tr_guide_light_update
+ * turns them into the distributions of later renders). The light sample
+ * uses the reference's two draws (the first picks the bin and its remainder
+ * the position in it), so no draw is added to the random stream. */
 typedef struct tr_guide_params {
   float alpha;
   float box_lo[3]; /* scene box of the position inputs */
   float box_hi[3];
   int32_t record;   /* 0: no records; n > 0: record every n-th sample of a pixel */
   uint32_t max_records;
+  int32_t light_guide;  /* 1: area-light samples from the light table */
+  int32_t light_record; /* 1: unoccluded light samples update the table's statistics (needs light_guide) */
 } tr_guide_params;
+/* Light table of learned light sampling: grid[0] x grid[1] x grid[2] cells
+ * over the box of later guided renders' tr_guide_params, every light of the
+ * uploaded scene (a single scene), bins x bins cells of its sample square
+ * (bins 1..16; at most 2^26 entries). Statistics start at zero and the
+ * distributions uniform. No reference counterpart. */
+tr_status tr_guide_light_init(tr_ctx* ctx, const int32_t grid[3], int32_t bins);
+/* Turns the recorded statistics into the distributions: per (cell, light)
+ * uniform_share / bins^2 + (1 - uniform_share) * (the bin's share of the
+ * recorded estimates), uniform where nothing was recorded;
+ * 0 < uniform_share <= 1. Statistics keep accumulating. No reference
+ * counterpart. */
+tr_status tr_guide_light_update(tr_ctx* ctx, float uniform_share);
 tr_status tr_render_guided_dev(tr_ctx* ctx, const tr_camera* cam, const tr_filter* filter,
                                const tr_render_params* params, const tr_guide_params* guide,
                                float* d_rgbw, double* d_rgbw64, tr_stats* stats);

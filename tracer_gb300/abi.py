@@ -116,7 +116,7 @@ class TrStats(C.Structure):
 
 class TrGuideParams(C.Structure):
     _fields_ = [("alpha", C.c_float), ("box_lo", C.c_float * 3), ("box_hi", C.c_float * 3), ("record", C.c_int32),
-                ("max_records", C.c_uint32)]
+                ("max_records", C.c_uint32), ("light_guide", C.c_int32), ("light_record", C.c_int32)]
 
 
 TR_RENDER_MODE_AUTO, TR_RENDER_MODE_WAVEFRONT, TR_RENDER_MODE_PERSISTENT = 0, 1, 2
@@ -306,9 +306,13 @@ def make_filter(radius=0.5, alpha=0.6) -> TrFilter:
     return f
 
 
-def make_guide(alpha: float, box_lo, box_hi, record: bool | int = False, max_records: int = 0) -> "TrGuideParams":
-    """record: False/0 none, True/1 every sample, n the first of every n samples of a pixel."""
+def make_guide(alpha: float, box_lo, box_hi, record: bool | int = False, max_records: int = 0,
+               light_guide: bool = False, light_record: bool = False) -> "TrGuideParams":
+    """record: False/0 none, True/1 every sample, n the first of every n samples of a pixel;
+    light_guide / light_record: learned light sampling from / statistics into the light table."""
     g = TrGuideParams()
+    g.light_guide = int(light_guide)
+    g.light_record = int(light_record)
     g.alpha = alpha
     g.box_lo[:] = box_lo
     g.box_hi[:] = box_hi

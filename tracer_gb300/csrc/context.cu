@@ -727,7 +727,8 @@ void tr_ctx_destroy(tr_ctx* ctx) {
   for (DevBuf* b : {&ctx->d_nodes, &ctx->d_nodes4, &ctx->d_slots, &ctx->d_spheres, &ctx->d_prims, &ctx->d_tshade,
                     &ctx->d_mats, &ctx->d_lights, &ctx->d_roots, &ctx->d_rays, &ctx->d_out0, &ctx->d_out1,
                     &ctx->d_err, &ctx->d_env_pool, &ctx->d_envs, &ctx->d_tex_pool, &ctx->d_texs, &ctx->d_treelet,
-                    &ctx->d_perm, &ctx->d_bin_key, &ctx->d_bin_cnt, &ctx->d_slot_leaf})
+                    &ctx->d_perm, &ctx->d_bin_key, &ctx->d_bin_cnt, &ctx->d_slot_leaf, &ctx->d_lg_acc,
+                    &ctx->d_lg_cdf})
     b->release();
   cudaStreamDestroy(ctx->stream);
   delete ctx;

@@ -88,6 +88,11 @@ struct tr_ctx {
   trg::DevBuf d_tex_pool, d_texs;  // material textures: texels, DTex records
   trg::DevBuf d_treelet;           // the shared-memory treelet (DScene::treelet)
   trg::DevBuf d_slot_leaf;         // DScene::slot_leaf
+  // learned light sampling: per (grid cell, light) the statistics and the
+  // sampling distribution (cumulative) over bins x bins sample-square cells
+  trg::DevBuf d_lg_acc, d_lg_cdf;
+  int lg_grid[3] = {0, 0, 0};
+  int lg_bins = 0, lg_nl = 0;
   trg::DevBuf d_perm, d_bin_key, d_bin_cnt;  // ray binning of tr_trace_*: order, keys, bin counts
   std::atomic<int> cancel{0};
   trg::RenderBuffers* rb = nullptr;

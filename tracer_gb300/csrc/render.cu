@@ -141,7 +141,52 @@ struct Launch {
   int* NV;       // records of the slot's current sample
   float *tb_in, *tb_dir, *tb_w;
   unsigned int tb_cap;
+  // learned light sampling (lg_cdf null: the reference's uniform light
+  // sample): per (cell of lg_grid over the guide box, light) the cumulative
+  // distribution over lg_bins x lg_bins cells of the light's sample square;
+  // lg_acc non-null: unoccluded light samples add to its statistics
+  const float* lg_cdf;
+  float* lg_acc;
+  int lg_grid[3], lg_bins;
 };
+
+// The light-table entry of position `pos` and light l: the cell of the grid
+// over the guide box (clamped) times the lights plus l, times bins^2 floats.
+__device__ __forceinline__ size_t lg_table(const Launch& P, f3 pos, int l) {
+  const float q[3] = {pos.x, pos.y, pos.z};
+  int c[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    // gbox_scale maps the box to [0, 2]
+    const float u = (q[k] - P.gbox_lo[k]) * P.gbox_scale[k] * 0.5f * (float)P.lg_grid[k];
+    c[k] = (int)fminf(fmaxf(u, 0.0f), (float)(P.lg_grid[k] - 1));
+  }
+  const int cell = (c[2] * P.lg_grid[1] + c[1]) * P.lg_grid[0] + c[0];
+  return ((size_t)cell * P.nl_max + l) * (size_t)(P.lg_bins * P.lg_bins);
+}
+
+// A learned light sample: the bin by the first draw's inverse CDF, the
+// position inside the bin from that draw's remainder and the second draw.
+// Returns the point in the light's sample square, the bin, and the ratio of
+// the uniform density to the table's there.
+__device__ __forceinline__ float2 lg_sample(const Launch& P, size_t tab, float2 uv, int& bin, float& ratio) {
+  const float* cdf = P.lg_cdf + tab;
+  const int nb = P.lg_bins * P.lg_bins;
+  int lo = 0, hi = nb - 1;  // the first bin whose cumulative value is above u (the last is exactly 1)
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (cdf[mid] > uv.x) hi = mid;
+    else lo = mid + 1;
+  }
+  bin = lo;
+  const float c0 = lo ? cdf[lo - 1] : 0.0f;
+  const float pm = cdf[lo] - c0;
+  float r = pm > 0.0f ? (uv.x - c0) / pm : 0.5f;
+  r = fminf(fmaxf(r, 0.0f), 0.99999994f);
+  ratio = 1.0f / (pm * (float)nb);
+  const int bx = lo % P.lg_bins, by = lo / P.lg_bins;
+  return make_float2(((float)bx + r) / (float)P.lg_bins, ((float)by + uv.y) / (float)P.lg_bins);
+}
 
 // The job a path slot belongs to.
 __device__ __forceinline__ const JobDev& job_of(const Launch& P, int slot) { return job_of(P.jobs, P.njobs, slot); }
@@ -507,6 +552,16 @@ __global__ void __launch_bounds__(128) k_logic(Launch P, int cur) {
       for (int l = 0; l < nl; ++l) {
         const float4 c = P.SH[3 * (slot * P.nl_max + l) + 2];
         if (c.w != 0.0f) direct = direct + mk3(c.x, c.y, c.z);
+        if (P.lg_acc && c.w != 0.0f) {
+          // an unoccluded learned light sample: its estimate into the
+          // statistics of its (cell, light) bin (environment-light items
+          // carry no estimate)
+          const float v = P.SH[3 * (slot * P.nl_max + l) + 1].w;
+          if (v > 0.0f && v < 1e30f) {
+            const float4 s0 = P.SC[7 * (size_t)slot];
+            atomicAdd(P.lg_acc + lg_table(P, mk3(s0.x, s0.y, s0.z), l) + ((int)c.w - 1), v);
+          }
+        }
       }
       if (flags & F_MIS) direct = direct + mulc(mk3(p4.x, p4.y, p4.z), mis_contribution(P, slot));
       if (flags & (F_GCONT | F_GX)) {
@@ -1027,9 +1082,14 @@ __global__ void __launch_bounds__(128, 6) k_nee(Launch P) {
         rec[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       continue;
     }
-    // Triangle::sample via UniformSampleTriangle (src/shape/triangle.cpp:61-97)
-    const float su0 = sqrtf(uv.x);
-    const float bx = 1.0f - su0, by = uv.y * su0;
+    // Triangle::sample via UniformSampleTriangle (src/shape/triangle.cpp:61-97),
+    // at the light table's point of the sample square when it is learned
+    float2 su = uv;
+    int lbin = 0;
+    float lratio = 1.0f;
+    if (P.lg_cdf) su = lg_sample(P, lg_table(P, pos, l), uv, lbin, lratio);
+    const float su0 = sqrtf(su.x);
+    const float bx = 1.0f - su0, by = su.y * su0;
     const f3 lpos = scale(lt.A, bx) + scale(lt.B, by) + scale(lt.C, 1.0f - bx - by);
     const f3 sp2ref = pos - lpos;
     if (dot(lt.gz, sp2ref) > 0.0f) {
@@ -1046,10 +1106,14 @@ __global__ void __launch_bounds__(128, 6) k_nee(Launch P) {
           f3 cc = mk3(0.0f, 0.0f, 0.0f);          // contribution before the shadow test
           bool trace = false;
           const float4 p4 = P.P4[slot];
+          // the estimate per unit path throughput; a learned light sample's
+          // is divided by the table's density over the uniform one (the MIS
+          // weights stay those of the uniform sample)
+          f3 inner = mk3(0.0f, 0.0f, 0.0f);
           if (KIND == MAT_PHONG && grow >= 0) {
             const f3 fw = guided_nee_factor(P, bsdf, wo, to_light, grow, (gcode >> 30) & 1, lpdf, lpdf);
             trace = !black(fw);
-            cc = mulc(mk3(p4.x, p4.y, p4.z), divs(mulc(lt.emission, fw), lpdf));
+            inner = divs(mulc(lt.emission, fw), lpdf);
           } else {
             const f3 bf = MatOps<KIND>::eval(bsdf, to_light, wo);
             trace = !black(bf);
@@ -1057,14 +1121,17 @@ __global__ void __launch_bounds__(128, 6) k_nee(Launch P) {
               const float bpdf = MatOps<KIND>::pdf(bsdf, to_light, wo);
               const f3 fl = muls(mulc(lt.emission, bf), abs_cos(to_light, bsdf.g.z));
               const float w = power_heuristic(lpdf, bpdf);
-              cc = mulc(mk3(p4.x, p4.y, p4.z), divs(muls(fl, w), lpdf));
+              inner = divs(muls(fl, w), lpdf);
             }
           }
+          if (P.lg_cdf) inner = muls(inner, lratio);
+          cc = mulc(mk3(p4.x, p4.y, p4.z), inner);
           if (trace) {
             const f3 sd = normalize(to_light);
             rec[0] = make_float4(pos.x, pos.y, pos.z, dist);
-            rec[1] = make_float4(sd.x, sd.y, sd.z, 0.0f);
-            rec[2] = make_float4(cc.x, cc.y, cc.z, 1.0f);
+            // statistics of the light table: the estimate's luminance, the bin + 1
+            rec[1] = make_float4(sd.x, sd.y, sd.z, P.lg_acc ? lum(inner) : 0.0f);
+            rec[2] = make_float4(cc.x, cc.y, cc.z, P.lg_acc ? (float)(lbin + 1) : 1.0f);
             P.q_sh[append(P.ctr + C_SH)] = item;
             ok = true;
           }
@@ -1292,6 +1359,16 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     P.guide_alpha = gp->alpha;
     if (gp->record < 0) return set_err(ctx, TR_ERR_ARG, "guide record stride must be >= 0");
     P.guide_record = gp->record;
+    if (gp->light_record && !gp->light_guide)
+      return set_err(ctx, TR_ERR_ARG, "light_record needs light_guide (the statistics are kept per table bin)");
+    if (gp->light_guide) {
+      if (!ctx->d_lg_cdf.p || ctx->lg_nl != std::max(nl, 1))
+        return set_err(ctx, TR_ERR_STATE, "light table not initialised for this scene (tr_guide_light_init)");
+      P.lg_cdf = ctx->d_lg_cdf.as<float>();
+      P.lg_acc = gp->light_record ? ctx->d_lg_acc.as<float>() : nullptr;
+      for (int k = 0; k < 3; ++k) P.lg_grid[k] = ctx->lg_grid[k];
+      P.lg_bins = ctx->lg_bins;
+    }
     P.maxd = std::max(jobs[0].prm.max_depth, 1);
     const size_t N = (size_t)n;
     const unsigned int cap = gp->max_records ? gp->max_records : (4u << 20);
@@ -1955,6 +2032,71 @@ extern "C" tr_status tr_render_guided_dev(tr_ctx* ctx, const tr_camera* cam, con
   void* out = d_rgbw ? (void*)d_rgbw : (void*)d_rgbw64;
   if (((uintptr_t)out & 15u) != 0) return trg::set_err(ctx, TR_ERR_ARG, "film buffer must be 16-byte aligned");
   return trg::render_impl(ctx, cam, filter, params, out, d_rgbw64 != nullptr, stats, guide);
+}
+
+namespace trg {
+
+// The light table's sampling distributions from its statistics: per
+// (cell, light) group of nb bins, share / nb + (1 - share) * the bin's part
+// of the group's recorded estimates (uniform where none), as a cumulative
+// distribution ending at exactly 1.
+__global__ void __launch_bounds__(128) k_lg_update(const float* __restrict__ acc, float* __restrict__ cdf,
+                                                   size_t groups, int nb, float share) {
+  for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < groups; g += (size_t)gridDim.x * blockDim.x) {
+    const float* a = acc + g * nb;
+    float* c = cdf + g * nb;
+    double tot = 0.0;
+    for (int b = 0; b < nb; ++b) tot += a[b];
+    const double u = (double)share / nb;
+    double run = 0.0;
+    for (int b = 0; b < nb; ++b) {
+      run += u + (tot > 0.0 ? (1.0 - share) * (double)a[b] / tot : (1.0 - share) / nb);
+      c[b] = (float)run;
+    }
+    for (int b = 0; b < nb; ++b) c[b] = (float)((double)c[b] / run);
+    c[nb - 1] = 1.0f;
+  }
+}
+
+}  // namespace trg
+
+extern "C" tr_status tr_guide_light_init(tr_ctx* ctx, const int32_t grid[3], int32_t bins) {
+  if (!ctx || !grid || bins < 1 || bins > 16) return TR_ERR_ARG;
+  if (!ctx->has_scene) return trg::set_err(ctx, TR_ERR_STATE, "no scene uploaded");
+  if (ctx->dsc.num_scenes != 1) return trg::set_err(ctx, TR_ERR_ARG, "the light table takes a single scene");
+  long long cells = 1;
+  for (int k = 0; k < 3; ++k) {
+    if (grid[k] < 1 || grid[k] > 1024) return trg::set_err(ctx, TR_ERR_ARG, "light-table grid out of range");
+    cells *= grid[k];
+  }
+  const int nl = std::max(ctx->dsc.max_lights, 1);
+  const long long n = cells * nl * bins * bins;
+  if (n > (1ll << 26)) return trg::set_err(ctx, TR_ERR_ARG, "light table above 2^26 entries");
+  TR_DEVICE_SCOPE(ctx);
+  TR_CUDA(ctx, ctx->d_lg_acc.reserve((size_t)n * 4));
+  TR_CUDA(ctx, ctx->d_lg_cdf.reserve((size_t)n * 4));
+  TR_CUDA(ctx, cudaMemsetAsync(ctx->d_lg_acc.p, 0, (size_t)n * 4, ctx->stream));
+  for (int k = 0; k < 3; ++k) ctx->lg_grid[k] = grid[k];
+  ctx->lg_bins = bins;
+  ctx->lg_nl = nl;
+  trg::k_lg_update<<<1024, 128, 0, ctx->stream>>>(ctx->d_lg_acc.as<float>(), ctx->d_lg_cdf.as<float>(),
+                                                 (size_t)(n / (bins * bins)), bins * bins, 1.0f);
+  TR_CUDA(ctx, cudaGetLastError());
+  TR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return TR_OK;
+}
+
+extern "C" tr_status tr_guide_light_update(tr_ctx* ctx, float uniform_share) {
+  if (!ctx || !(uniform_share > 0.0f && uniform_share <= 1.0f)) return TR_ERR_ARG;
+  if (!ctx->d_lg_cdf.p || ctx->lg_bins <= 0) return trg::set_err(ctx, TR_ERR_STATE, "light table not initialised");
+  TR_DEVICE_SCOPE(ctx);
+  const int nb = ctx->lg_bins * ctx->lg_bins;
+  const size_t groups = (size_t)ctx->lg_grid[0] * ctx->lg_grid[1] * ctx->lg_grid[2] * ctx->lg_nl;
+  trg::k_lg_update<<<1024, 128, 0, ctx->stream>>>(ctx->d_lg_acc.as<float>(), ctx->d_lg_cdf.as<float>(), groups, nb,
+                                                 uniform_share);
+  TR_CUDA(ctx, cudaGetLastError());
+  TR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return TR_OK;
 }
 
 extern "C" tr_status tr_guide_train_on_records(tr_ctx* ctx, int32_t steps, uint32_t batch, float lr, uint64_t seed,

@@ -105,6 +105,10 @@ def lib() -> C.CDLL:
                                        C.POINTER(TrGuideParams), C.c_void_p, C.c_void_p, C.POINTER(TrStats)]
     L.tr_guide_train_on_records.restype = st
     L.tr_guide_train_on_records.argtypes = [vp, C.c_int32, C.c_uint32, C.c_float, C.c_uint64, C.POINTER(C.c_float)]
+    L.tr_guide_light_init.restype = st
+    L.tr_guide_light_init.argtypes = [vp, C.POINTER(C.c_int32), C.c_int32]
+    L.tr_guide_light_update.restype = st
+    L.tr_guide_light_update.argtypes = [vp, C.c_float]
     L.tr_scene_set_upload.restype = st
     L.tr_scene_set_upload.argtypes = [vp, C.POINTER(TrSceneDesc), C.c_uint32]
     L.tr_render_batch_dev.restype = st
@@ -324,6 +328,15 @@ class GpuContext:
         loss = C.c_float()
         self._check(self.L.tr_guide_train_on_records(self.h, steps, batch, lr, seed, C.byref(loss)))
         return loss.value
+
+    def guide_light_init(self, grid=(32, 16, 24), bins: int = 8) -> None:
+        """Light table of learned light sampling (statistics zero, distributions uniform)."""
+        g = (C.c_int32 * 3)(*grid)
+        self._check(self.L.tr_guide_light_init(self.h, g, bins))
+
+    def guide_light_update(self, uniform_share: float = 0.2) -> None:
+        """Recorded light-sample statistics -> the table's sampling distributions."""
+        self._check(self.L.tr_guide_light_update(self.h, uniform_share))
 
     def upload_set(self, scenes) -> None:
         """Uploads a scene set (list of SceneBuffers) for batched rendering."""
