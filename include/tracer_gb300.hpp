@@ -14,7 +14,8 @@
 // the reference (src/shape/sphere.cpp:88-90); render errors throw TracerError
 // carrying the C ABI's status.
 //
-// Constant textures only (create_constant_texture2d); the vacuum medium only.
+// Constant textures and image maps (HDR or 8-bit) as material arguments; the
+// vacuum medium only.
 #pragma once
 
 #include <cstdint>
@@ -162,8 +163,10 @@ class Material {
  public:
   explicit Material(const tr_material& m) : rec(m) {}
   tr_material rec;
-  // Phong's image maps (ka, kd, ks, ns; null where the map is a constant)
-  RC<const Texture2D> maps[4];
+  // image maps of the factory's arguments in their order (Phong: ka, kd, ks,
+  // ns; the other kinds as tr_material.tex_param lists them); null where the
+  // argument is a constant
+  RC<const Texture2D> maps[13];
 };
 RC<Material> create_phong_material(RC<const Texture2D> map_ka, RC<const Texture2D> map_kd,
                                    RC<const Texture2D> map_ks, RC<const Texture2D> map_ns);

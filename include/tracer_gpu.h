@@ -106,6 +106,19 @@ typedef struct tr_material {
    * textures[k - 1], evaluated at the hit's uv (ns takes its red channel,
    * Texture2D::evaluate_s). */
   uint32_t tex_ka, tex_kd, tex_ks, tex_ns;
+  /* Maps of the other kinds, one per factory argument in the factory's
+   * order (0 = the constant field above, k = textures[k - 1] at the hit's
+   * uv; scalar arguments take the red channel, as the materials' shading
+   * does with Texture2D::evaluate_s):
+   *   glass    kr, kt, ior                                (src/material/glass.cpp:117-140)
+   *   metal    color, eta, k, roughness, anisotropic      (src/material/metal.cpp:33-56)
+   *   Disney15 base_color, metallic, roughness, transmission, transmission_roughness,
+   *            ior, specular_scale, specular_tint, anisotropic, sheen, sheen_tint,
+   *            clearcoat, clearcoat_gloss                  (src/material/disney.cpp:604-639)
+   *   Disney12 base_color, subsurface, metallic, specular, specular_tint, roughness,
+   *            anisotropic, sheen, sheen_tint, clearcoat, clearcoat_gloss
+   *                                                        (src/material/disney_brdf.cpp:278-302) */
+  uint32_t tex_param[13];
 } tr_material;
 
 /* Flat scene description. It records what the reference factory calls build

@@ -128,21 +128,28 @@ void* ref_scene_create(const tr_scene_desc* d) {
       s->materials.push_back(create_phong_material(map(m.tex_ka, ctex3(m.ka)), map(m.tex_kd, ctex3(m.kd)),
                                                    map(m.tex_ks, ctex3(m.ks)), map(m.tex_ns, ctex(m.ns))));
     } else if (m.kind == TR_MAT_GLASS) {
-      s->materials.push_back(create_glass(ctex3(m.kr), ctex3(m.kt), ctex(m.ior)));
+      const uint32_t* t = m.tex_param;  // the factory's arguments: image maps or constants
+      s->materials.push_back(create_glass(map(t[0], ctex3(m.kr)), map(t[1], ctex3(m.kt)), map(t[2], ctex(m.ior))));
     } else if (m.kind == TR_MAT_DISNEY15) {
+      const uint32_t* t = m.tex_param;
       s->materials.push_back(create_disney(
-          ctex3(m.base_color), ctex(m.metallic), ctex(m.roughness), ctex(m.transmission),
-          ctex(m.transmission_roughness), ctex(m.ior), ctex3(m.specular_scale), ctex(m.specular_tint),
-          ctex(m.anisotropic), ctex(m.sheen), ctex(m.sheen_tint), ctex(m.clearcoat), ctex(m.clearcoat_gloss),
-          newBox<const NormalMapper>(nullptr), newRC<BSSRDFSurface>()));
+          map(t[0], ctex3(m.base_color)), map(t[1], ctex(m.metallic)), map(t[2], ctex(m.roughness)),
+          map(t[3], ctex(m.transmission)), map(t[4], ctex(m.transmission_roughness)), map(t[5], ctex(m.ior)),
+          map(t[6], ctex3(m.specular_scale)), map(t[7], ctex(m.specular_tint)), map(t[8], ctex(m.anisotropic)),
+          map(t[9], ctex(m.sheen)), map(t[10], ctex(m.sheen_tint)), map(t[11], ctex(m.clearcoat)),
+          map(t[12], ctex(m.clearcoat_gloss)), newBox<const NormalMapper>(nullptr), newRC<BSSRDFSurface>()));
     } else if (m.kind == TR_MAT_METAL) {
-      s->materials.push_back(create_metal(ctex3(m.color), ctex3(m.eta), ctex3(m.k), ctex(m.roughness),
-                                          ctex(m.anisotropic), newBox<NormalMapper>()));
+      const uint32_t* t = m.tex_param;
+      s->materials.push_back(create_metal(map(t[0], ctex3(m.color)), map(t[1], ctex3(m.eta)), map(t[2], ctex3(m.k)),
+                                          map(t[3], ctex(m.roughness)), map(t[4], ctex(m.anisotropic)),
+                                          newBox<NormalMapper>()));
     } else {
+      const uint32_t* t = m.tex_param;
       s->materials.push_back(create_disney_brdf(
-          ctex3(m.base_color), ctex(m.subsurface), ctex(m.metallic), ctex(m.specular),
-          ctex(m.specular_tint), ctex(m.roughness), ctex(m.anisotropic), ctex(m.sheen),
-          ctex(m.sheen_tint), ctex(m.clearcoat), ctex(m.clearcoat_gloss)));
+          map(t[0], ctex3(m.base_color)), map(t[1], ctex(m.subsurface)), map(t[2], ctex(m.metallic)),
+          map(t[3], ctex(m.specular)), map(t[4], ctex(m.specular_tint)), map(t[5], ctex(m.roughness)),
+          map(t[6], ctex(m.anisotropic)), map(t[7], ctex(m.sheen)), map(t[8], ctex(m.sheen_tint)),
+          map(t[9], ctex(m.clearcoat)), map(t[10], ctex(m.clearcoat_gloss))));
     }
   }
 

@@ -261,6 +261,8 @@ struct Mat {
   int tex_ka = 0, tex_kd = 0, tex_ks = 0, tex_ns = 0;
   Sp kd_c, ks_c;
   real ns_c = 1;
+  // another kind with image maps (tr_material.tex_param): set up again at each hit
+  bool maps = false;
 };
 struct Prim {
   int kind;  // 0 triangle, 1 sphere
@@ -489,6 +491,7 @@ struct Scene {
   std::vector<Tri> tris;
   std::vector<Sphere> spheres;
   std::vector<Mat> mats;
+  std::vector<tr_material> msrc;  // the materials' factory arguments and maps
   std::vector<Prim> prims;
   std::vector<int> lights;       // primitive ids in scene.lights order
   std::unique_ptr<Env> env;      // environment light (after the area lights in scene.lights)
@@ -1695,10 +1698,134 @@ inline void phong_setup(Mat& m, Sp diffuse, Sp spec, real ns) {
   m.ns = ns;
   m.base = diffuse;
 }
-// The material at a hit: a Phong material with maps evaluates them at the
-// hit's uv (Texture2D::evaluate, evaluate_s) and sets up again.
+// A material's set-up from its factory arguments (the shading functions'
+// per-hit work that depends on the arguments only; see Mat).
+static Mat make_mat(const tr_material& src) {
+  Mat m;
+  m.kind = src.kind;
+  if (src.kind == TR_MAT_PHONG) {
+    m.kd_c = Sp(src.kd[0], src.kd[1], src.kd[2]);
+    m.ks_c = Sp(src.ks[0], src.ks[1], src.ks[2]);
+    m.ns_c = src.ns;
+    m.tex_ka = (int)src.tex_ka;
+    m.tex_kd = (int)src.tex_kd;
+    m.tex_ks = (int)src.tex_ks;
+    m.tex_ns = (int)src.tex_ns;
+    phong_setup(m, m.kd_c, m.ks_c, m.ns_c);
+  } else if (src.kind == TR_MAT_METAL) {
+    m.base = Sp(src.color[0], src.color[1], src.color[2]);
+    for (int c = 0; c < 3; ++c) {
+      // ConductorFresnelPoint(eta_outside = color, eta_inside = 1, k = the caller's k)
+      real e2 = real(1) / src.color[c];
+      e2 *= e2;
+      real ek2 = src.k[c] / src.color[c];
+      ek2 *= ek2;
+      (c == 0 ? m.f_eta2.r : c == 1 ? m.f_eta2.g : m.f_eta2.b) = e2;
+      (c == 0 ? m.f_etak2.r : c == 1 ? m.f_etak2.g : m.f_etak2.b) = ek2;
+      (c == 0 ? m.f_paint.r : c == 1 ? m.f_paint.g : m.f_paint.b) = src.eta[c];
+    }
+    const real aspect = src.anisotropic > 0 ? std::sqrt(1 - real(0.9) * src.anisotropic) : real(1);
+    m.ax_m = std::max(real(0.001), src.roughness * src.roughness / aspect);
+    m.ay_m = std::max(real(0.001), src.roughness * src.roughness * aspect);
+  } else if (src.kind == TR_MAT_DISNEY15) {
+    // Disney::shading + DisneyBSDF's constructor (material/disney.cpp:341-392,616-651)
+    m.base = Sp(src.base_color[0], src.base_color[1], src.base_color[2]);
+    m.metallic = src.metallic; m.roughness = src.roughness; m.specular_tint = src.specular_tint;
+    m.anisotropic = src.anisotropic; m.sheen = src.sheen; m.sheen_tint = src.sheen_tint;
+    m.clearcoat = src.clearcoat;
+    m.spec_scale = Sp(src.specular_scale[0], src.specular_scale[1], src.specular_scale[2]);
+    m.transmission = src.transmission;
+    const real lum = m.base.lum();
+    m.c_tint = lum > 0 ? m.base / lum : Sp(1);
+    m.ior15 = std::max(real(1.01), src.ior);
+    const real aspect = src.anisotropic > 0 ? std::sqrt(1 - real(0.9) * src.anisotropic) : real(1);
+    m.ax15 = std::max(real(0.001), src.roughness * src.roughness / aspect);
+    m.ay15 = std::max(real(0.001), src.roughness * src.roughness * aspect);
+    const real tr = src.transmission_roughness;
+    m.trans_ax = std::max(real(0.001), tr * tr / aspect);
+    m.trans_ay = std::max(real(0.001), tr * tr * aspect);
+    real cr = mixf(real(0.1), real(0), src.clearcoat_gloss);
+    cr *= cr;
+    m.cc_rough = std::max(cr, real(0.0001));
+    const real A = std::clamp(m.base.lum() * (1 - m.metallic), real(0.3), real(0.7));
+    const real B = 1 - A;
+    m.w_diff = A * (1 - m.transmission);
+    m.w_trans = A * m.transmission;
+    m.w_spec = B * 2 / (2 + m.clearcoat);
+    m.w_cc = B * m.clearcoat / (2 + m.clearcoat);
+  } else if (src.kind == TR_MAT_GLASS) {
+    m.kr = Sp(src.kr[0], src.kr[1], src.kr[2]);
+    m.kt_sqrt = Sp(std::sqrt(src.kt[0]), std::sqrt(src.kt[1]), std::sqrt(src.kt[2]));
+    m.ior = src.ior;
+  } else {
+    m.base = Sp(src.base_color[0], src.base_color[1], src.base_color[2]);
+    m.subsurface = src.subsurface; m.metallic = src.metallic; m.specular_s = src.specular;
+    m.specular_tint = src.specular_tint; m.roughness = src.roughness; m.anisotropic = src.anisotropic;
+    m.sheen = src.sheen; m.sheen_tint = src.sheen_tint; m.clearcoat = src.clearcoat;
+    m.clearcoat_gloss = src.clearcoat_gloss;
+  }
+
+  return m;
+}
+
+
+// Factory arguments a kind's tex_param maps: glass (kr, kt, ior), metal
+// (color, eta, k, roughness, anisotropic), Disney 2015 (13), Disney 2012 (11).
+inline int mapped_args(int kind) {
+  switch (kind) {
+    case TR_MAT_GLASS: return 3;
+    case TR_MAT_METAL: return 5;
+    case TR_MAT_DISNEY15: return 13;
+    case TR_MAT_DISNEY12: return 11;
+    default: return 0;
+  }
+}
+
+// The factory arguments at a hit: every mapped argument replaced by its map
+// at the hit's uv -- Texture2D::evaluate for colours, evaluate_s (the red
+// channel) for scalars, as Glass::shading, Metal::shading, Disney::shading and
+// Disney12::shading call them (material/glass.cpp:117-140, metal.cpp:33-56,
+// disney.cpp:604-639, disney_brdf.cpp:278-302).
+inline tr_material mapped_args_at(const Scene& sc, tr_material m, const Isect& is) {
+  auto col = [&](int i, float* dst) {
+    if (!m.tex_param[i]) return;
+    const Sp c = sc.textures[m.tex_param[i] - 1].eval(is.uv[0], is.uv[1]);
+    dst[0] = c.r; dst[1] = c.g; dst[2] = c.b;
+  };
+  auto scl = [&](int i, float& dst) {
+    if (m.tex_param[i]) dst = sc.textures[m.tex_param[i] - 1].eval(is.uv[0], is.uv[1]).r;
+  };
+  switch (m.kind) {
+    case TR_MAT_GLASS:
+      col(0, m.kr); col(1, m.kt); scl(2, m.ior);
+      break;
+    case TR_MAT_METAL:
+      col(0, m.color); col(1, m.eta); col(2, m.k); scl(3, m.roughness); scl(4, m.anisotropic);
+      break;
+    case TR_MAT_DISNEY15:
+      col(0, m.base_color); scl(1, m.metallic); scl(2, m.roughness); scl(3, m.transmission);
+      scl(4, m.transmission_roughness); scl(5, m.ior); col(6, m.specular_scale); scl(7, m.specular_tint);
+      scl(8, m.anisotropic); scl(9, m.sheen); scl(10, m.sheen_tint); scl(11, m.clearcoat);
+      scl(12, m.clearcoat_gloss);
+      break;
+    case TR_MAT_DISNEY12:
+      col(0, m.base_color); scl(1, m.subsurface); scl(2, m.metallic); scl(3, m.specular);
+      scl(4, m.specular_tint); scl(5, m.roughness); scl(6, m.anisotropic); scl(7, m.sheen);
+      scl(8, m.sheen_tint); scl(9, m.clearcoat); scl(10, m.clearcoat_gloss);
+      break;
+  }
+  return m;
+}
+
+// The material at a hit: a material with image maps evaluates them at the
+// hit's uv and sets up again -- Phong from its own maps (Texture2D::evaluate,
+// evaluate_s), the other kinds through their mapped factory arguments.
 inline const Mat& material_at(const Scene& sc, int mi, const Isect& is, Mat& scratch) {
   const Mat& m = sc.mats[mi];
+  if (m.maps) {
+    scratch = make_mat(mapped_args_at(sc, sc.msrc[mi], is));
+    return scratch;
+  }
   if (m.kind != TR_MAT_PHONG || !(m.tex_kd | m.tex_ks | m.tex_ns)) return m;
   scratch = m;
   const Sp kd = m.tex_kd ? sc.textures[m.tex_kd - 1].eval(is.uv[0], is.uv[1]) : m.kd_c;
@@ -1988,71 +2115,11 @@ void* orc_scene_create(const tr_scene_desc* d) {
     S.world_radius = ratio * S.radius;
   }
   sc->mats.resize(d->num_materials);
+  sc->msrc.assign(d->materials, d->materials + d->num_materials);
   for (uint32_t i = 0; i < d->num_materials; ++i) {
+    sc->mats[i] = make_mat(d->materials[i]);
     const tr_material& src = d->materials[i];
-    Mat& m = sc->mats[i];
-    m.kind = src.kind;
-    if (src.kind == TR_MAT_PHONG) {
-      m.kd_c = Sp(src.kd[0], src.kd[1], src.kd[2]);
-      m.ks_c = Sp(src.ks[0], src.ks[1], src.ks[2]);
-      m.ns_c = src.ns;
-      m.tex_ka = (int)src.tex_ka;
-      m.tex_kd = (int)src.tex_kd;
-      m.tex_ks = (int)src.tex_ks;
-      m.tex_ns = (int)src.tex_ns;
-      phong_setup(m, m.kd_c, m.ks_c, m.ns_c);
-    } else if (src.kind == TR_MAT_METAL) {
-      m.base = Sp(src.color[0], src.color[1], src.color[2]);
-      for (int c = 0; c < 3; ++c) {
-        // ConductorFresnelPoint(eta_outside = color, eta_inside = 1, k = the caller's k)
-        real e2 = real(1) / src.color[c];
-        e2 *= e2;
-        real ek2 = src.k[c] / src.color[c];
-        ek2 *= ek2;
-        (c == 0 ? m.f_eta2.r : c == 1 ? m.f_eta2.g : m.f_eta2.b) = e2;
-        (c == 0 ? m.f_etak2.r : c == 1 ? m.f_etak2.g : m.f_etak2.b) = ek2;
-        (c == 0 ? m.f_paint.r : c == 1 ? m.f_paint.g : m.f_paint.b) = src.eta[c];
-      }
-      const real aspect = src.anisotropic > 0 ? std::sqrt(1 - real(0.9) * src.anisotropic) : real(1);
-      m.ax_m = std::max(real(0.001), src.roughness * src.roughness / aspect);
-      m.ay_m = std::max(real(0.001), src.roughness * src.roughness * aspect);
-    } else if (src.kind == TR_MAT_DISNEY15) {
-      // Disney::shading + DisneyBSDF's constructor (material/disney.cpp:341-392,616-651)
-      m.base = Sp(src.base_color[0], src.base_color[1], src.base_color[2]);
-      m.metallic = src.metallic; m.roughness = src.roughness; m.specular_tint = src.specular_tint;
-      m.anisotropic = src.anisotropic; m.sheen = src.sheen; m.sheen_tint = src.sheen_tint;
-      m.clearcoat = src.clearcoat;
-      m.spec_scale = Sp(src.specular_scale[0], src.specular_scale[1], src.specular_scale[2]);
-      m.transmission = src.transmission;
-      const real lum = m.base.lum();
-      m.c_tint = lum > 0 ? m.base / lum : Sp(1);
-      m.ior15 = std::max(real(1.01), src.ior);
-      const real aspect = src.anisotropic > 0 ? std::sqrt(1 - real(0.9) * src.anisotropic) : real(1);
-      m.ax15 = std::max(real(0.001), src.roughness * src.roughness / aspect);
-      m.ay15 = std::max(real(0.001), src.roughness * src.roughness * aspect);
-      const real tr = src.transmission_roughness;
-      m.trans_ax = std::max(real(0.001), tr * tr / aspect);
-      m.trans_ay = std::max(real(0.001), tr * tr * aspect);
-      real cr = mixf(real(0.1), real(0), src.clearcoat_gloss);
-      cr *= cr;
-      m.cc_rough = std::max(cr, real(0.0001));
-      const real A = std::clamp(m.base.lum() * (1 - m.metallic), real(0.3), real(0.7));
-      const real B = 1 - A;
-      m.w_diff = A * (1 - m.transmission);
-      m.w_trans = A * m.transmission;
-      m.w_spec = B * 2 / (2 + m.clearcoat);
-      m.w_cc = B * m.clearcoat / (2 + m.clearcoat);
-    } else if (src.kind == TR_MAT_GLASS) {
-      m.kr = Sp(src.kr[0], src.kr[1], src.kr[2]);
-      m.kt_sqrt = Sp(std::sqrt(src.kt[0]), std::sqrt(src.kt[1]), std::sqrt(src.kt[2]));
-      m.ior = src.ior;
-    } else {
-      m.base = Sp(src.base_color[0], src.base_color[1], src.base_color[2]);
-      m.subsurface = src.subsurface; m.metallic = src.metallic; m.specular_s = src.specular;
-      m.specular_tint = src.specular_tint; m.roughness = src.roughness; m.anisotropic = src.anisotropic;
-      m.sheen = src.sheen; m.sheen_tint = src.sheen_tint; m.clearcoat = src.clearcoat;
-      m.clearcoat_gloss = src.clearcoat_gloss;
-    }
+    for (int k = 0; k < mapped_args(src.kind); ++k) sc->mats[i].maps |= src.tex_param[k] != 0;
   }
   sc->prims.resize(d->num_prims);
   for (uint32_t p = 0; p < d->num_prims; ++p) {

@@ -78,6 +78,11 @@ def render(name, maker):
     return d
 
 
+def mapped():
+    """Image maps on glass, metal, Disney 2015 and Disney12 arguments."""
+    return render("mapped", lambda: scenes.mapped_materials(32, 16, 2))
+
+
 def main():
     if not oracle.ref_available():
         oracle.build_ref()
@@ -102,6 +107,7 @@ def main():
                                                                      textured=True, glass=False)))
     np.savez_compressed(os.path.join(OUT, "cornell_textured_24x24_2spp.npz"),
                         **render("textured", lambda: scenes.cornell(24, 24, 2, textured=True)))
+    np.savez_compressed(os.path.join(OUT, "mapped_materials_32x16_2spp.npz"), **mapped())
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))

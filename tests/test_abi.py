@@ -37,7 +37,7 @@ def test_struct_layouts():
     assert NODE_DTYPE.itemsize == 32
     assert ctypes.sizeof(TrCamera) == 4 * 13
     assert ctypes.sizeof(TrRenderParams) == 4 * 8
-    assert ctypes.sizeof(TrMaterial) == 4 * 49  # + glass kr, kt, ior; metal color, eta, k; Disney 2015; maps
+    assert ctypes.sizeof(TrMaterial) == 4 * 62  # + glass kr, kt, ior; metal color, eta, k; Disney 2015; maps
 
 
 def test_struct_layouts_match_the_header(tmp_path):

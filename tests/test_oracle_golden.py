@@ -63,7 +63,7 @@ def test_mixed_scene_render_and_trace():
 @pytest.mark.parametrize("name", ["cornell_32x32_4spp.npz", "disney_grid_32x32_2spp.npz",
                                   "cornell_glass_metal_24x24_2spp.npz", "disney15_row_32x16_2spp.npz",
                                   "outdoor_env_24x16_2spp.npz", "outdoor_env8_textured_24x16_2spp.npz",
-                                  "cornell_textured_24x24_2spp.npz"])
+                                  "cornell_textured_24x24_2spp.npz", "mapped_materials_32x16_2spp.npz"])
 def test_renders(name):
     g = load(name)
     sc = scenes.unpack_scene(g)

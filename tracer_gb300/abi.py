@@ -61,7 +61,8 @@ class TrMaterial(C.Structure):
                 ("color", C.c_float * 3), ("eta", C.c_float * 3), ("k", C.c_float * 3),
                 ("transmission", C.c_float), ("transmission_roughness", C.c_float),
                 ("specular_scale", C.c_float * 3),
-                ("tex_ka", C.c_uint32), ("tex_kd", C.c_uint32), ("tex_ks", C.c_uint32), ("tex_ns", C.c_uint32)]
+                ("tex_ka", C.c_uint32), ("tex_kd", C.c_uint32), ("tex_ks", C.c_uint32), ("tex_ns", C.c_uint32),
+                ("tex_param", C.c_uint32 * 13)]
 
 
 class TrTexture(C.Structure):
@@ -176,6 +177,8 @@ class Material:
     tex_kd: int = 0
     tex_ks: int = 0
     tex_ns: int = 0
+    # maps of the other kinds, per factory argument in the factory's order (tr_material.tex_param)
+    tex_param: tuple = (0,) * 13
 
     def to_c(self) -> TrMaterial:
         m = TrMaterial()
@@ -196,6 +199,8 @@ class Material:
         m.tex_ka, m.tex_kd, m.tex_ks, m.tex_ns = self.tex_ka, self.tex_kd, self.tex_ks, self.tex_ns
         m.eta[:] = self.eta
         m.k[:] = self.k
+        for i, t in enumerate(self.tex_param):
+            m.tex_param[i] = t
         return m
 
 

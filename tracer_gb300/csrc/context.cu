@@ -20,6 +20,7 @@
 #include "binning.cuh"
 #include "bvh_build.h"
 #include "context.h"
+#include "mat_setup.cuh"
 #include "traverse.cuh"
 
 namespace trg {
@@ -41,109 +42,6 @@ tr_status cuda_fail(tr_ctx* ctx, cudaError_t e, const char* what) {
 namespace {
 
 const float kIdentity[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
-
-// Color3::lum (src/core/spectrum.hpp:94-96)
-inline float lum(f3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
-
-DMat derive_material(const tr_material& m) {
-  DMat d;
-  std::memset(&d, 0, sizeof(d));
-  if (m.kind == TR_MAT_PHONG) {
-    d.kind = MAT_PHONG;
-    d.kd_c = mk3(m.kd[0], m.kd[1], m.kd[2]);
-    d.ks_c = mk3(m.ks[0], m.ks[1], m.ks[2]);
-    d.ns_c = m.ns;
-    d.tex_kd = (int)m.tex_kd;
-    d.tex_ks = (int)m.tex_ks;
-    d.tex_ns = (int)m.tex_ns;
-    phong_setup(d, d.kd_c, d.ks_c, d.ns_c);  // the constants; a hit with maps sets up again
-  } else if (m.kind == TR_MAT_METAL) {
-    // create_metal(color, eta, k) hands over to Metal(color, k, eta), whose
-    // shading builds PaintedConductorFresnelPoint(color, 1, eta, k) with
-    // parameters (eta_outside, eta_inside, k, paint): eta_outside = color,
-    // eta_inside = 1, conductor k = the caller's k, paint = the caller's eta
-    d.kind = MAT_METAL;
-    d.base = mk3(m.color[0], m.color[1], m.color[2]);
-    d.albedo = d.base;  // AggregateBSDF<1>(..., color)
-    float e2[3], ek2[3];
-    for (int c = 0; c < 3; ++c) {
-      e2[c] = 1.0f / m.color[c];
-      e2[c] *= e2[c];
-      ek2[c] = m.k[c] / m.color[c];
-      ek2[c] *= ek2[c];
-    }
-    d.f_eta2 = mk3(e2[0], e2[1], e2[2]);
-    d.f_etak2 = mk3(ek2[0], ek2[1], ek2[2]);
-    d.f_paint = mk3(m.eta[0], m.eta[1], m.eta[2]);
-    d.roughness = m.roughness;
-    d.anisotropic = m.anisotropic;
-    // GGXMicrofacetReflectionBXDF (src/material/bxdf/microfacet_refl_bxdf.cpp:6-11)
-    const float aspect = m.anisotropic > 0.0f ? std::sqrt(1.0f - 0.9f * m.anisotropic) : 1.0f;
-    d.ax = smax(0.001f, m.roughness * m.roughness / aspect);
-    d.ay = smax(0.001f, m.roughness * m.roughness * aspect);
-  } else if (m.kind == TR_MAT_DISNEY15) {
-    // Disney::shading and DisneyBSDF's constructor (src/material/disney.cpp:341-392,616-651)
-    d.kind = MAT_DISNEY15;
-    d.base = mk3(m.base_color[0], m.base_color[1], m.base_color[2]);
-    d.albedo = d.base;  // get_albedo(): C_
-    d.metallic = m.metallic;
-    d.roughness = m.roughness;
-    d.specular_tint = m.specular_tint;
-    d.anisotropic = m.anisotropic;
-    d.sheen = m.sheen;
-    d.sheen_tint = m.sheen_tint;
-    d.clearcoat = m.clearcoat;
-    d.spec_scale = mk3(m.specular_scale[0], m.specular_scale[1], m.specular_scale[2]);
-    d.transmission = m.transmission;
-    const float l = lum(d.base);  // to_tint
-    d.c_tint = l > 0.0f ? mk3(d.base.x / l, d.base.y / l, d.base.z / l) : mk3(1.0f, 1.0f, 1.0f);
-    d.ior = smax(1.01f, m.ior);
-    const float aspect = m.anisotropic > 0.0f ? std::sqrt(1.0f - 0.9f * m.anisotropic) : 1.0f;
-    d.ax = smax(0.001f, m.roughness * m.roughness / aspect);
-    d.ay = smax(0.001f, m.roughness * m.roughness * aspect);
-    const float tr = m.transmission_roughness;
-    d.trans_ax = smax(0.001f, tr * tr / aspect);
-    d.trans_ay = smax(0.001f, tr * tr * aspect);
-    float cr = (1.0f - m.clearcoat_gloss) * 0.1f + m.clearcoat_gloss * 0.0f;  // mix(0.1, 0, gloss)
-    cr *= cr;
-    d.cc_rough = smax(cr, 0.0001f);
-    float A = lum(d.base) * (1.0f - d.metallic);
-    A = A < 0.3f ? 0.3f : (0.7f < A ? 0.7f : A);
-    const float B = 1.0f - A;
-    d.w_diff15 = A * (1.0f - d.transmission);
-    d.w_trans = A * d.transmission;
-    d.w_spec15 = B * 2.0f / (2.0f + d.clearcoat);
-    d.w_cc = B * d.clearcoat / (2.0f + d.clearcoat);
-  } else if (m.kind == TR_MAT_GLASS) {
-    d.kind = MAT_GLASS;
-    d.kr = mk3(m.kr[0], m.kr[1], m.kr[2]);
-    d.kt_sqrt = mk3(std::sqrt(m.kt[0]), std::sqrt(m.kt[1]), std::sqrt(m.kt[2]));  // Glass::shading
-    d.ior = m.ior;
-    d.albedo = mk3(0.5f * (d.kr.x + d.kt_sqrt.x), 0.5f * (d.kr.y + d.kt_sqrt.y), 0.5f * (d.kr.z + d.kt_sqrt.z));
-  } else {
-    d.kind = MAT_DISNEY12;
-    d.base = mk3(m.base_color[0], m.base_color[1], m.base_color[2]);
-    d.albedo = d.base;
-    d.subsurface = m.subsurface;
-    d.metallic = m.metallic;
-    d.specular_s = m.specular;
-    d.specular_tint = m.specular_tint;
-    d.roughness = m.roughness;
-    d.anisotropic = m.anisotropic;
-    d.sheen = m.sheen;
-    d.sheen_tint = m.sheen_tint;
-    d.clearcoat = m.clearcoat;
-    d.clearcoat_gloss = m.clearcoat_gloss;
-    // DisneyBRDF's per-call constants (src/material/disney_brdf.cpp:81-83,142-151,188-193)
-    const float aspect = (float)std::sqrt(1.0 - (double)m.anisotropic * 0.9);
-    d.ax = smax(0.001f, m.roughness * m.roughness / aspect);
-    d.ay = smax(0.001f, m.roughness * m.roughness * aspect);
-    d.p_diffuse = smin(0.8f, 1.0f - m.metallic);
-    d.p_spec_sample = (float)(1.0 / (1.0 + 0.5 * (double)m.clearcoat) * (double)(1.0f - d.p_diffuse));
-    d.p_spec_pdf = (float)(1.0 / (1.0 + 0.5 * (double)m.clearcoat));
-  }
-  return d;
-}
 
 inline float as_float(int i) {
   float f;
@@ -441,10 +339,18 @@ tr_status upload_textures(tr_ctx* ctx) {
   const std::vector<HostScene::Tex>& tx = ctx->hs.textures;
   DScene& sc = ctx->dsc;
   sc.textures = nullptr;
+  sc.msrc = nullptr;
   sc.has_textures = 0;
   for (const DMat& m : ctx->hs.mats)
-    if (m.kind == MAT_PHONG && (m.tex_kd | m.tex_ks | m.tex_ns)) sc.has_textures = 1;
+    if (m.tex_any) sc.has_textures = 1;
   if (tx.empty()) return TR_OK;
+  if (sc.has_textures) {
+    // the factory arguments of every material, for the set-ups at hits with maps
+    TR_CUDA(ctx, ctx->d_msrc.reserve(ctx->hs.msrc.size() * sizeof(tr_material)));
+    TR_CUDA(ctx, cudaMemcpyAsync(ctx->d_msrc.p, ctx->hs.msrc.data(), ctx->hs.msrc.size() * sizeof(tr_material),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    sc.msrc = ctx->d_msrc.as<tr_material>();
+  }
   // one pool, 16 bytes per float texel and 4 per byte texel, every map 16-byte aligned
   size_t total = 0;
   std::vector<size_t> off(tx.size());
@@ -728,7 +634,7 @@ void tr_ctx_destroy(tr_ctx* ctx) {
                     &ctx->d_mats, &ctx->d_lights, &ctx->d_roots, &ctx->d_rays, &ctx->d_out0, &ctx->d_out1,
                     &ctx->d_err, &ctx->d_env_pool, &ctx->d_envs, &ctx->d_tex_pool, &ctx->d_texs, &ctx->d_treelet,
                     &ctx->d_perm, &ctx->d_bin_key, &ctx->d_bin_cnt, &ctx->d_slot_leaf, &ctx->d_lg_acc,
-                    &ctx->d_lg_cdf})
+                    &ctx->d_lg_cdf, &ctx->d_msrc})
     b->release();
   cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -864,7 +770,17 @@ static tr_status build_host_scene(tr_ctx* ctx, const tr_scene_desc* d, HostScene
         (tm.tex_ka > d->num_textures || tm.tex_kd > d->num_textures || tm.tex_ks > d->num_textures ||
          tm.tex_ns > d->num_textures))
       return set_err(ctx, TR_ERR_ARG, "material names a missing texture");
-    hs.mats.push_back(derive_material(tm));
+    bool maps = tm.kind == TR_MAT_PHONG && (tm.tex_kd | tm.tex_ks | tm.tex_ns);
+    for (int k = 0; k < mapped_params(tm.kind); ++k) {
+      if (tm.tex_param[k] > d->num_textures) return set_err(ctx, TR_ERR_ARG, "material names a missing texture");
+      maps |= tm.tex_param[k] != 0;
+    }
+    DMat dm = derive_material(tm);
+    dm.tex_any = maps ? 1 : 0;
+    hs.mats.push_back(dm);
+    tr_material src = tm;
+    for (int k = mapped_params(tm.kind); k < 13; ++k) src.tex_param[k] = 0;
+    hs.msrc.push_back(src);
   }
   for (uint32_t k = 0; k < d->num_textures; ++k) {
     const tr_texture& t = d->textures[k];
@@ -1013,6 +929,11 @@ static void append_scene(HostScene& dst, const HostScene& src) {
       if (m.tex_ns) m.tex_ns += tex_base;
     }
     dst.mats.push_back(m);
+  }
+  for (tr_material m : src.msrc) {
+    for (uint32_t& t : m.tex_param)
+      if (t) t += (uint32_t)tex_base;
+    dst.msrc.push_back(m);
   }
   dst.textures.insert(dst.textures.end(), src.textures.begin(), src.textures.end());
   const int env_base = (int)dst.envs.size();

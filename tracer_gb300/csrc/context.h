@@ -69,6 +69,9 @@ struct HostScene {
   // root is a leaf, or the tree was built on the device)
   std::vector<DNode> dnodes;
   int root0 = -1;
+  // every material's factory arguments and maps (the device re-derives the
+  // set-up of a material with maps at each of its hits)
+  std::vector<tr_material> msrc;
 };
 
 struct RenderBuffers;  // render.cu
@@ -91,6 +94,7 @@ struct tr_ctx {
   // learned light sampling: per (grid cell, light) the statistics and the
   // sampling distribution (cumulative) over bins x bins sample-square cells
   trg::DevBuf d_lg_acc, d_lg_cdf;
+  trg::DevBuf d_msrc;  // DScene::msrc
   int lg_grid[3] = {0, 0, 0};
   int lg_bins = 0, lg_nl = 0;
   trg::DevBuf d_perm, d_bin_key, d_bin_cnt;  // ray binning of tr_trace_*: order, keys, bin counts

@@ -148,13 +148,10 @@ class ConstantTexture : public Texture2D {
 
 Spectrum tex(const RC<const Texture2D>& t, const char* what) {
   if (!t) throw std::invalid_argument(std::string("null texture: ") + what);
-  // the device materials take one value per parameter
   if (!dynamic_cast<const ConstantTexture*>(t.get()))
-    throw TracerError(TR_ERR_UNSUPPORTED, std::string("image textures on materials are outside the GPU path: ") + what);
+    throw TracerError(TR_ERR_UNSUPPORTED, std::string("texture kind outside the GPU path: ") + what);
   return t->evaluate(Point2f{});
 }
-
-real tex_s(const RC<const Texture2D>& t, const char* what) { return tex(t, what).r; }
 
 // ---------------------------------------------------------------- shapes
 
@@ -292,6 +289,33 @@ class ImageTexture : public Texture2D {
   RC<Image2D<Color3b>> img_;
 };
 
+bool is_image(const Texture2D* t) {
+  return dynamic_cast<const HdrTexture*>(t) || dynamic_cast<const ImageTexture*>(t);
+}
+
+// A factory argument: a constant texture gives its value; an image texture
+// (HDR or 8-bit) is kept as map `slot` of the material and evaluated at each
+// hit's uv (the constant field stays zero).
+struct Args {
+  RC<const Texture2D> maps[13];
+  Spectrum col(const RC<const Texture2D>& t, const char* what, int slot) {
+    if (!t) throw std::invalid_argument(std::string("null texture: ") + what);
+    if (is_image(t.get())) {
+      maps[slot] = t;
+      return Spectrum(0);
+    }
+    if (!dynamic_cast<const ConstantTexture*>(t.get()))
+      throw TracerError(TR_ERR_UNSUPPORTED, std::string("texture kind outside the GPU path: ") + what);
+    return t->evaluate(Point2f{});
+  }
+  real scl(const RC<const Texture2D>& t, const char* what, int slot) { return col(t, what, slot).r; }
+  RC<Material> make(const tr_material& m) {
+    auto mat = std::make_shared<Material>(m);
+    for (int k = 0; k < 13; ++k) mat->maps[k] = maps[k];
+    return mat;
+  }
+};
+
 class IblLight : public EnvironmentLight {
  public:
   IblLight(RC<const Texture2D> tex, const Transform& t) : tex(std::move(tex)), world_to_light(t) {}
@@ -320,8 +344,11 @@ class GeneralScene : public Scene {
       if (mi == mat_index.end()) {
         mi = mat_index.emplace(gp->material.get(), (int)d.materials.size()).first;
         tr_material rec = gp->material->rec;
-        uint32_t* slots[4] = {&rec.tex_ka, &rec.tex_kd, &rec.tex_ks, &rec.tex_ns};
-        for (int k = 0; k < 4; ++k) {
+        uint32_t* slots[13];
+        const int nslots = rec.kind == TR_MAT_PHONG ? 4 : 13;
+        uint32_t* phong[4] = {&rec.tex_ka, &rec.tex_kd, &rec.tex_ks, &rec.tex_ns};
+        for (int k = 0; k < nslots; ++k) slots[k] = rec.kind == TR_MAT_PHONG ? phong[k] : &rec.tex_param[k];
+        for (int k = 0; k < nslots; ++k) {
           const Texture2D* t = gp->material->maps[k].get();
           if (!t) continue;
           auto ti = tex_index.find(t);
@@ -575,12 +602,13 @@ RC<Material> create_phong_material(RC<const Texture2D> map_ka, RC<const Texture2
 RC<Material> create_glass(RC<const Texture2D> map_kr, RC<const Texture2D> map_kt, RC<const Texture2D> map_ior) {
   tr_material m{};
   m.kind = TR_MAT_GLASS;
-  const Spectrum kr = tex(map_kr, "kr"), kt = tex(map_kt, "kt");
+  Args a;
+  const Spectrum kr = a.col(map_kr, "kr", 0), kt = a.col(map_kt, "kt", 1);
   const float r[3] = {kr.r, kr.g, kr.b}, t[3] = {kt.r, kt.g, kt.b};
   std::memcpy(m.kr, r, sizeof(r));
   std::memcpy(m.kt, t, sizeof(t));
-  m.ior = tex_s(map_ior, "ior");
-  return std::make_shared<Material>(m);
+  m.ior = a.scl(map_ior, "ior", 2);
+  return a.make(m);
 }
 
 RC<Material> create_disney(RC<const Texture2D> base_color, RC<const Texture2D> metallic,
@@ -592,36 +620,38 @@ RC<Material> create_disney(RC<const Texture2D> base_color, RC<const Texture2D> m
                            RC<const Texture2D> clearcoat_gloss) {
   tr_material m{};
   m.kind = TR_MAT_DISNEY15;
-  const Spectrum bc = tex(base_color, "base_color"), ss = tex(specular_scale, "specular_scale");
+  Args a;
+  const Spectrum bc = a.col(base_color, "base_color", 0), ss = a.col(specular_scale, "specular_scale", 6);
   const float b3[3] = {bc.r, bc.g, bc.b}, s3[3] = {ss.r, ss.g, ss.b};
   std::memcpy(m.base_color, b3, sizeof(b3));
   std::memcpy(m.specular_scale, s3, sizeof(s3));
-  m.metallic = tex_s(metallic, "metallic");
-  m.roughness = tex_s(roughness, "roughness");
-  m.transmission = tex_s(transmission, "transmission");
-  m.transmission_roughness = tex_s(transmission_roughness, "transmission_roughness");
-  m.ior = tex_s(ior, "ior");
-  m.specular_tint = tex_s(specular_tint, "specular_tint");
-  m.anisotropic = tex_s(anisotropic, "anisotropic");
-  m.sheen = tex_s(sheen, "sheen");
-  m.sheen_tint = tex_s(sheen_tint, "sheen_tint");
-  m.clearcoat = tex_s(clearcoat, "clearcoat");
-  m.clearcoat_gloss = tex_s(clearcoat_gloss, "clearcoat_gloss");
-  return std::make_shared<Material>(m);
+  m.metallic = a.scl(metallic, "metallic", 1);
+  m.roughness = a.scl(roughness, "roughness", 2);
+  m.transmission = a.scl(transmission, "transmission", 3);
+  m.transmission_roughness = a.scl(transmission_roughness, "transmission_roughness", 4);
+  m.ior = a.scl(ior, "ior", 5);
+  m.specular_tint = a.scl(specular_tint, "specular_tint", 7);
+  m.anisotropic = a.scl(anisotropic, "anisotropic", 8);
+  m.sheen = a.scl(sheen, "sheen", 9);
+  m.sheen_tint = a.scl(sheen_tint, "sheen_tint", 10);
+  m.clearcoat = a.scl(clearcoat, "clearcoat", 11);
+  m.clearcoat_gloss = a.scl(clearcoat_gloss, "clearcoat_gloss", 12);
+  return a.make(m);
 }
 
 RC<Material> create_metal(RC<const Texture2D> color, RC<const Texture2D> eta, RC<const Texture2D> k,
                           RC<const Texture2D> roughness, RC<const Texture2D> anisotropic) {
   tr_material m{};
   m.kind = TR_MAT_METAL;
-  const Spectrum c = tex(color, "color"), e = tex(eta, "eta"), kk = tex(k, "k");
+  Args a;
+  const Spectrum c = a.col(color, "color", 0), e = a.col(eta, "eta", 1), kk = a.col(k, "k", 2);
   const float cv[3] = {c.r, c.g, c.b}, ev[3] = {e.r, e.g, e.b}, kv[3] = {kk.r, kk.g, kk.b};
   std::memcpy(m.color, cv, sizeof(cv));
   std::memcpy(m.eta, ev, sizeof(ev));
   std::memcpy(m.k, kv, sizeof(kv));
-  m.roughness = tex_s(roughness, "roughness");
-  m.anisotropic = tex_s(anisotropic, "anisotropic");
-  return std::make_shared<Material>(m);
+  m.roughness = a.scl(roughness, "roughness", 3);
+  m.anisotropic = a.scl(anisotropic, "anisotropic", 4);
+  return a.make(m);
 }
 
 RC<Material> create_disney_brdf(RC<const Texture2D> base_color, RC<const Texture2D> subsurface,
@@ -632,21 +662,22 @@ RC<Material> create_disney_brdf(RC<const Texture2D> base_color, RC<const Texture
                                 RC<const Texture2D> clearcoat_gloss) {
   tr_material m{};
   m.kind = TR_MAT_DISNEY12;
-  const Spectrum bc = tex(base_color, "base_color");
+  Args a;
+  const Spectrum bc = a.col(base_color, "base_color", 0);
   m.base_color[0] = bc.r;
   m.base_color[1] = bc.g;
   m.base_color[2] = bc.b;
-  m.subsurface = tex_s(subsurface, "subsurface");
-  m.metallic = tex_s(metallic, "metallic");
-  m.specular = tex_s(specular, "specular");
-  m.specular_tint = tex_s(specular_tint, "specular_tint");
-  m.roughness = tex_s(roughness, "roughness");
-  m.anisotropic = tex_s(anisotropic, "anisotropic");
-  m.sheen = tex_s(sheen, "sheen");
-  m.sheen_tint = tex_s(sheen_tint, "sheen_tint");
-  m.clearcoat = tex_s(clearcoat, "clearcoat");
-  m.clearcoat_gloss = tex_s(clearcoat_gloss, "clearcoat_gloss");
-  return std::make_shared<Material>(m);
+  m.subsurface = a.scl(subsurface, "subsurface", 1);
+  m.metallic = a.scl(metallic, "metallic", 2);
+  m.specular = a.scl(specular, "specular", 3);
+  m.specular_tint = a.scl(specular_tint, "specular_tint", 4);
+  m.roughness = a.scl(roughness, "roughness", 5);
+  m.anisotropic = a.scl(anisotropic, "anisotropic", 6);
+  m.sheen = a.scl(sheen, "sheen", 7);
+  m.sheen_tint = a.scl(sheen_tint, "sheen_tint", 8);
+  m.clearcoat = a.scl(clearcoat, "clearcoat", 9);
+  m.clearcoat_gloss = a.scl(clearcoat_gloss, "clearcoat_gloss", 10);
+  return a.make(m);
 }
 
 RC<Medium> create_vacuum() { return std::make_shared<VacuumMedium>(); }

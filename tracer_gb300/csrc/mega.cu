@@ -250,10 +250,10 @@ __global__ void __launch_bounds__(kMegaThreads, 1) k_mega(MegaLaunch P) {
           Bsdf bsdf;
           mcode = pr.material;
           bsdf.m = sc.mats + mcode;
-          if ((MASK & MK_MAPS) && kind == MAT_PHONG && (bsdf.m->tex_kd | bsdf.m->tex_ks | bsdf.m->tex_ns)) {
+          if ((MASK & MK_MAPS) && bsdf.m->tex_any) {  // image maps: the material at this hit's uv
             float u, v;
             hit_uv(sc, hit, p.o, p.d, u, v);
-            phong_at(sc, *bsdf.m, u, v, &tmat);
+            material_at(sc, pr.material, u, v, &tmat);
             bsdf.m = &tmat;
             mcode = -1;
           }

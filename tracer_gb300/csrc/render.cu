@@ -759,10 +759,11 @@ __global__ void __launch_bounds__(128, KIND == MAT_DISNEY12 ? 8 : 5) k_material(
     int mat = P.sc.prims[is.prim].material;
     Bsdf bsdf;
     bsdf.m = P.sc.mats + mat;
-    if (KIND == MAT_PHONG && P.MT && (bsdf.m->tex_kd | bsdf.m->tex_ks | bsdf.m->tex_ns)) {
+    if (P.MT && bsdf.m->tex_any) {
+      // image maps: the material set up at this hit's uv, in the slot's record
       float u, v;
       hit_uv(P.sc, hit, ro, rd, u, v);
-      phong_at(P.sc, *bsdf.m, u, v, P.MT + slot);
+      material_at(P.sc, mat, u, v, P.MT + slot);
       bsdf.m = P.MT + slot;
       mat |= kMatScratch;
     }
@@ -960,6 +961,12 @@ __global__ void __launch_bounds__(128) k_glass(Launch P, int cur) {
     make_isect(P.sc, P.HC[slot], mk3(p0.x, p0.y, p0.z), mk3(p1.x, p1.y, p1.z), is);
     Bsdf bsdf;
     bsdf.m = P.sc.mats + P.sc.prims[is.prim].material;
+    if (P.MT && bsdf.m->tex_any) {  // image maps: the material at this hit's uv
+      float u, v;
+      hit_uv(P.sc, P.HC[slot], mk3(p0.x, p0.y, p0.z), mk3(p1.x, p1.y, p1.z), u, v);
+      material_at(P.sc, P.sc.prims[is.prim].material, u, v, P.MT + slot);
+      bsdf.m = P.MT + slot;
+    }
     bsdf.g = is.g;
     bsdf.s = is.s;
     const float u0 = Pcg::next(st);
@@ -1055,7 +1062,7 @@ __device__ __noinline__ bool nee_env_item(const Launch& P, int item, int slot, i
 // the contribution when it is blocked.
 // Six resident blocks per SM (80 registers, a few bytes of spill) measured
 // faster than the five its free allocation (91 registers) allows.
-template <int KIND, bool MAPS = false>  // MAPS: Phong hits may carry per-slot set-ups
+template <int KIND, bool MAPS = false>  // MAPS: hits of materials with image maps carry per-slot set-ups
 __global__ void __launch_bounds__(128, 6) k_nee(Launch P) {
   const unsigned int n = P.ctr[C_NEE + nee_index(KIND)];
   for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -1573,9 +1580,17 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     if (P.MT) k_nee<MAT_PHONG, true><<<grid, 128, 0, st>>>(P);
     else k_nee<MAT_PHONG><<<grid, 128, 0, st>>>(P);
     mark();
-    k_nee<MAT_DISNEY12><<<grid, 128, 0, st>>>(P);
-    if (P.sc.has_metal) k_nee<MAT_METAL><<<grid, 128, 0, st>>>(P);  // timed with Disney12
-    if (P.sc.has_disney15) k_nee<MAT_DISNEY15><<<grid, 128, 0, st>>>(P);
+    // (MAPS instantiations: hits of materials with image maps read the slot's set-up)
+    if (P.MT) k_nee<MAT_DISNEY12, true><<<grid, 128, 0, st>>>(P);
+    else k_nee<MAT_DISNEY12><<<grid, 128, 0, st>>>(P);
+    if (P.sc.has_metal) {  // timed with Disney12
+      if (P.MT) k_nee<MAT_METAL, true><<<grid, 128, 0, st>>>(P);
+      else k_nee<MAT_METAL><<<grid, 128, 0, st>>>(P);
+    }
+    if (P.sc.has_disney15) {
+      if (P.MT) k_nee<MAT_DISNEY15, true><<<grid, 128, 0, st>>>(P);
+      else k_nee<MAT_DISNEY15><<<grid, 128, 0, st>>>(P);
+    }
     mark();
     if (count && wide) k_shadow<true, true><<<grid_sh, 128, 0, st>>>(P);
     else if (count) k_shadow<true><<<grid_sh, 128, sh_smem, st>>>(P);

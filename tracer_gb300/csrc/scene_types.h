@@ -32,6 +32,8 @@ struct alignas(16) int4 {
 };
 #endif
 
+struct tr_material;  // the C ABI's material record (tracer_gpu.h)
+
 namespace trg {
 
 // Launch-tuning limits (tr_tuning): ray-binning grid bits per axis, and the
@@ -131,6 +133,9 @@ struct DMat {
   int tex_kd, tex_ks, tex_ns;
   f3 kd_c, ks_c;
   float ns_c;
+  // some argument of the material is an image map: a hit sets the material
+  // up from DScene::msrc at its uv (0 in such per-hit set-ups)
+  int tex_any;
 };
 
 // Phong::shading's set-up (src/material/phong.cpp:29-70): kd and ks scaled
@@ -221,6 +226,9 @@ struct DScene {
   // Per slot: 2 * (its leaf's parent DNode) + (1 if the leaf is the right
   // child); -1 where the leaf is a scene's root. Null for device-built trees.
   const int* slot_leaf;
+  // The materials' factory arguments and maps, by material index (only for
+  // sets with image maps; null otherwise)
+  const tr_material* msrc;
 };
 
 }  // namespace trg

@@ -10,6 +10,7 @@
 #pragma once
 
 #include "env_tex.cuh"
+#include "mat_setup.cuh"
 #include "scene_types.h"
 
 namespace trg {
@@ -205,6 +206,21 @@ static __device__ __noinline__ void phong_at(const DScene& sc, const DMat& m, fl
   out->diffuse_coef = d.diffuse_coef;
   out->specular = d.specular;
   out->albedo = d.albedo;
+}
+
+// The set-up of a material with image maps at a hit's (u, v): Phong's maps
+// through phong_at; the other kinds' mapped arguments evaluated from
+// DScene::msrc, then the same set-up as for constants (derive_material).
+static __device__ __noinline__ void material_at(const DScene& sc, int mi, float u, float v, DMat* out) {
+  const DMat& m = sc.mats[mi];
+  if (m.kind == MAT_PHONG) {
+    phong_at(sc, m, u, v, out);
+    return;
+  }
+  tr_material src = sc.msrc[mi];
+  apply_maps(src, [&](int t) { return tex_eval(sc.textures[t], u, v); });
+  *out = derive_material(src);
+  out->tex_any = 0;
 }
 
 __device__ __forceinline__ void make_isect(const DScene& sc, const float4 hit, f3 o, f3 d, Isect& is) {

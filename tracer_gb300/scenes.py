@@ -387,6 +387,48 @@ def disney15_row(width=96, height=48, spp=8, max_depth=6, min_depth=3, env=True)
     return scene, cam, make_filter(0.5, 0.6), make_params(width, height, spp, min_depth, max_depth)
 
 
+def mapped_materials(width=96, height=48, spp=8, max_depth=6, min_depth=3, env=True):
+    """Image maps on every material kind that takes them: a ground of
+    Disney12 with a base-colour checker and a roughness ramp; spheres of
+    metal (colour and roughness maps), Disney 2015 (base colour, roughness,
+    transmission and sheen maps), glass (kr map and an ior map) and Disney12
+    (base colour, metallic, clearcoat maps) beside a constant Phong sphere,
+    under a small area light and (by default) the sky map. Maps are 8-bit
+    checkers and float ramps (create_image_texture2d, create_hdr_texture2d)."""
+    b = _Builder()
+    ramp = np.linspace(0.05, 0.95, 8 * 4 * 3, dtype=np.float32).reshape(4, 8, 3)
+    ior_map = np.linspace(1.2, 1.8, 6 * 6 * 3, dtype=np.float32).reshape(6, 6, 3)
+    textures = [checker(16, 4),                                                        # 1: 8-bit colours
+                ramp,                                                                  # 2: float ramp
+                checker(8, 2, (0.9, 0.9, 0.9), (0.1, 0.1, 0.1), eight_bit=False),      # 3: float 0.9/0.1
+                ior_map,                                                               # 4: float 1.2..1.8
+                checker(12, 3, (0.95, 0.64, 0.54), (0.3, 0.7, 0.9))]                   # 5: 8-bit colours
+    ground = b.material(Material(kind=TR_MAT_DISNEY12, base_color=(0.5, 0.5, 0.5), roughness=0.5, specular=0.5,
+                                 tex_param=(1, 0, 0, 0, 0, 2) + (0,) * 7))
+    b.quad((-6, 0, -6), (6, 0, -6), (6, 0, 6), (-6, 0, 6), (0, 1, 0), ground)
+    light = b.material(lambert((0.5, 0.5, 0.5)))
+    b.quad((-0.5, 3, -0.5), (0.5, 3, -0.5), (0.5, 3, 0.5), (-0.5, 3, 0.5), (0, -1, 0), light,
+           emission=(8.0, 8.0, 8.0))
+    mats = [Material(kind=TR_MAT_METAL, color=(0.95, 0.64, 0.54), eta=(0.2, 0.92, 1.1), k=(3.9, 2.45, 2.14),
+                     roughness=0.3, anisotropic=0.3, tex_param=(5, 0, 0, 2, 0) + (0,) * 8),
+            Material(kind=TR_MAT_DISNEY15, base_color=(0.8, 0.3, 0.2), roughness=0.5, specular_scale=(1.0, 1.0, 1.0),
+                     ior=1.5, tex_param=(1, 0, 2, 3, 0, 0, 0, 0, 0, 2, 0, 0, 0)),
+            Material(kind=TR_MAT_GLASS, kr=(1.0, 1.0, 1.0), kt=(1.0, 1.0, 1.0), ior=1.5,
+                     tex_param=(5, 0, 4) + (0,) * 10),
+            Material(kind=TR_MAT_DISNEY12, base_color=(0.2, 0.4, 0.8), roughness=0.4, specular=0.5, clearcoat=0.3,
+                     clearcoat_gloss=0.5, tex_param=(5, 0, 3, 0, 0, 0, 0, 0, 0, 2, 0) + (0, 0)),
+            lambert((0.6, 0.6, 0.2))]
+    for k, m in enumerate(mats):
+        b.sphere((-3.0 + 1.5 * k, 0.6, 0.0), 0.6, b.material(m))
+    scene = b.finish(max_leaf_prims=3)
+    scene.textures = textures
+    if env:
+        scene.env_texels = sky_map(64, 32)
+        scene.env_to_light, scene.env_to_world = rotate_x(math.pi / 2)
+    cam = make_camera(width / height, (0, 1.8, 7.0), (0, 0.7, 0), (0, 1, 0), math.radians(50.0), 0.0, 1.0)
+    return scene, cam, make_filter(0.5, 0.6), make_params(width, height, spp, min_depth, max_depth)
+
+
 def traversal(n_tris=1 << 20, seed=0, max_leaf_prims=4):
     """n_tris triangles: centres uniform in [0,1]^3, each vertex the centre plus
     an edge vector uniform in [-0.01,0.01]^3. numpy PCG64(seed)."""
@@ -523,7 +565,7 @@ _MAT_FIELDS = ("ka", "kd", "ks", "ns", "base_color", "subsurface", "metallic", "
                "roughness", "anisotropic", "sheen", "sheen_tint", "clearcoat", "clearcoat_gloss",
                # added later: fixtures packed before them have shorter rows and keep the defaults
                "kr", "kt", "ior", "color", "eta", "k", "transmission", "transmission_roughness", "specular_scale",
-               "tex_ka", "tex_kd", "tex_ks", "tex_ns")
+               "tex_ka", "tex_kd", "tex_ks", "tex_ns", "tex_param")
 
 
 def pack_scene(s: SceneBuffers, prefix: str = "") -> dict:
@@ -558,8 +600,10 @@ def unpack_scene(d, prefix: str = "") -> SceneBuffers:
                 break
             cur = getattr(m, f)
             if isinstance(cur, tuple):
-                setattr(m, f, tuple(float(x) for x in row[i:i + 3]))
-                i += 3
+                n = len(cur)
+                cast = int if f == "tex_param" else float
+                setattr(m, f, tuple(cast(x) for x in row[i:i + n]))
+                i += n
             else:
                 setattr(m, f, int(row[i]) if isinstance(cur, int) and f.startswith("tex_") else float(row[i]))
                 i += 1
