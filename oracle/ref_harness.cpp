@@ -435,3 +435,46 @@ void ref_post_process(float* rgb, int w, int h, int kind, float param) {
     }
 }
 }
+
+// ---------------------------------------------------------------- images
+// The reference's 8-bit image reader (load_image_from_file, src/utility/
+// image_file.cpp:26-58, over its vendored stb_image: format found from the
+// file's bytes, rows flipped, 1 and 4 channels to RGB) and the vendored
+// stb_image_write encoders its image_file.cpp compiles, which make the
+// reader-test files (JPEG, TGA, BMP) here.
+#include "utility/image_file.hpp"
+#include <stb_image_write.h>
+
+extern "C" {
+
+// Reads `path` with the reference's reader; rgb (3 * w * h bytes) may be null
+// to ask for the size. Returns 0, or -1 when the reference throws.
+int ref_load_image(const char* path, int* w, int* h, uint8_t* rgb) {
+  try {
+    auto img = load_image_from_file(path);
+    *w = img->width();
+    *h = img->height();
+    if (rgb)
+      for (int y = 0; y < *h; ++y)
+        for (int x = 0; x < *w; ++x) {
+          const Color3b& c = img->at(x, y);
+          uint8_t* o = rgb + 3 * ((size_t)y * *w + x);
+          o[0] = c.x; o[1] = c.y; o[2] = c.z;
+        }
+    return 0;
+  } catch (...) {
+    return -1;
+  }
+}
+
+// kind: 0 JPEG (quality q), 1 TGA (run-length encoded unless q == 0), 2 BMP.
+int ref_write_image(const char* path, int kind, int w, int h, int comp, const uint8_t* px, int q) {
+  if (kind == 0) return stbi_write_jpg(path, w, h, comp, px, q);
+  if (kind == 1) {
+    stbi_write_tga_with_rle = q != 0;
+    return stbi_write_tga(path, w, h, comp, px);
+  }
+  return stbi_write_bmp(path, w, h, comp, px);
+}
+
+}  // extern "C"

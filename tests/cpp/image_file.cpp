@@ -1,6 +1,6 @@
 // Drives the image-file helpers of the C++ host API for tests/test_image_file.py:
 //   image_file load <file.hdr>       prints "size w h" and every pixel
-//   image_file png <file.png>        the same for load_image_from_file (bytes)
+//   image_file png <file>            the same for load_image_from_file (bytes; PNG, JPEG, BMP or TGA)
 //   image_file write <file.hdr> w h  writes a w x h test pattern with write_image_to_hdr
 //   image_file tex <file>            create_texture2d_from_file, one lookup
 //   image_file mtl <file.obj>        prints create_texture_from_file for each material

@@ -78,6 +78,68 @@ def render(name, maker):
     return d
 
 
+def image_cases():
+    """(name, file bytes) of the 8-bit image reader's cases: files from the
+    reference's own encoders (stb_image_write's JPEG at three qualities and
+    grey, TGA raw and run-length, BMP) and from tests/jpeg_writer.py (the JPEG
+    layouts those encoders never write: 4:2:2, 4:4:0, 4:1:1, mixed sampling,
+    restart intervals, one scan per component, RGB component ids, grey with
+    2x2 sampling, a 3x5 image)."""
+    import ctypes as C
+    import tempfile
+    sys.path.insert(0, os.path.dirname(OUT))
+    from jpeg_writer import write_jpeg
+    lib = C.CDLL(oracle.REF_SO)
+    rng = np.random.default_rng(11)
+    yy, xx = np.mgrid[0:45, 0:61]
+    img = np.stack([xx * 4, yy * 5, (xx * yy) % 256], -1).clip(0, 255).astype(np.uint8)
+    img[10:20, 10:30] = (rng.random((10, 20, 3)) * 255).astype(np.uint8)
+    cases = []
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, kind, src, q in (("stb_q50.jpg", 0, img, 50), ("stb_q85.jpg", 0, img, 85), ("stb_q95.jpg", 0, img, 95),
+                                   ("stb_grey.jpg", 0, img[..., :1], 80), ("stb_rle.tga", 1, img, 1),
+                                   ("stb_raw_rgba.tga", 1, np.dstack([img, img[..., :1]]), 0),
+                                   ("stb_grey.tga", 1, img[..., 1:2], 1), ("stb.bmp", 2, img, 0),
+                                   ("stb_rgba.bmp", 2, np.dstack([img, img[..., :1]]), 0)):
+            p = os.path.join(tmp, name)
+            src = np.ascontiguousarray(src)
+            h, w, c = src.shape
+            assert lib.ref_write_image(p.encode(), kind, w, h, c, src.ctypes.data_as(C.c_void_p), q) == 1
+            cases.append((name, open(p, "rb").read()))
+    for name, kw, src in (("w_422.jpg", dict(sampling=((2, 1), (1, 1), (1, 1))), img),
+                          ("w_440.jpg", dict(sampling=((1, 2), (1, 1), (1, 1))), img),
+                          ("w_411.jpg", dict(sampling=((4, 1), (1, 1), (1, 1))), img),
+                          ("w_mixed.jpg", dict(sampling=((2, 2), (2, 1), (1, 2))), img),
+                          ("w_restart.jpg", dict(restart=3), img),
+                          ("w_scans_422_restart.jpg", dict(sampling=((2, 1), (1, 1), (1, 1)), interleaved=False,
+                                                           restart=5), img),
+                          ("w_rgb_ids.jpg", dict(sampling=((1, 1), (1, 1), (1, 1)), ids=(82, 71, 66)), img),
+                          ("w_grey_22.jpg", dict(sampling=((2, 2),)), img[..., 1]),
+                          ("w_tiny.jpg", dict(), img[:3, :5])):
+        cases.append((name, write_jpeg(src, **kw)))
+    return cases
+
+
+def image_files():
+    """The reader's cases with the reference's decodes (load_image_from_file)."""
+    import ctypes as C
+    import tempfile
+    lib = C.CDLL(oracle.REF_SO)
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for k, (name, data) in enumerate(image_cases()):
+            p = os.path.join(tmp, name)
+            open(p, "wb").write(data)
+            w, h = C.c_int(), C.c_int()
+            assert lib.ref_load_image(p.encode(), C.byref(w), C.byref(h), None) == 0, name
+            px = np.zeros((h.value, w.value, 3), np.uint8)
+            lib.ref_load_image(p.encode(), C.byref(w), C.byref(h), px.ctypes.data_as(C.c_void_p))
+            out[f"name{k}"] = np.array(name)
+            out[f"file{k}"] = np.frombuffer(data, np.uint8)
+            out[f"rgb{k}"] = px
+    return out
+
+
 def mapped():
     """Image maps on glass, metal, Disney 2015 and Disney12 arguments."""
     return render("mapped", lambda: scenes.mapped_materials(32, 16, 2))
@@ -108,6 +170,7 @@ def main():
     np.savez_compressed(os.path.join(OUT, "cornell_textured_24x24_2spp.npz"),
                         **render("textured", lambda: scenes.cornell(24, 24, 2, textured=True)))
     np.savez_compressed(os.path.join(OUT, "mapped_materials_32x16_2spp.npz"), **mapped())
+    np.savez_compressed(os.path.join(OUT, "image_files.npz"), **image_files())
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))

@@ -95,11 +95,14 @@ def test_write_then_load_round_trip(program, tmp_path):
     assert np.allclose(px, want, rtol=0, atol=want.max(-1, keepdims=True) / 128)
 
 
-@pytest.mark.parametrize("name,status", [("missing.png", TR_ERR_ARG), ("x.jpg", TR_ERR_UNSUPPORTED),
-                                         ("x.tga", TR_ERR_ARG), ("noext", TR_ERR_ARG), ("missing.hdr", TR_ERR_ARG)])
+@pytest.mark.parametrize("name,status", [("missing.png", TR_ERR_ARG), ("missing.jpg", TR_ERR_ARG),
+                                         ("x.tga", TR_ERR_ARG), ("x.bmp", TR_ERR_ARG), ("noext", TR_ERR_ARG),
+                                         ("missing.hdr", TR_ERR_ARG)])
 def test_texture_file_rules(program, tmp_path, name, status):
-    """create_texture2d_from_file: .hdr and .png read, JPEG unsupported here,
-    other extensions rejected as the reference rejects them."""
+    """create_texture2d_from_file: .hdr, .png and .jpg/.jpeg read (a missing
+    file is an argument error); other extensions -- .tga and .bmp too, which
+    the reference's is_float_image rejects -- refused as the reference refuses
+    them."""
     r = subprocess.run([program, "tex", str(tmp_path / name)], capture_output=True, text=True)
     assert r.returncode == 1 and r.stdout.startswith(f"error {status}"), r.stdout
 

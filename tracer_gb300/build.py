@@ -25,7 +25,7 @@ CU_FLAGS = ["-O3", "-std=c++17", *ARCH, "-lineinfo", "--fmad=false", "-Xptxas", 
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", f"-I{INCLUDE}"]
 
 CU_SOURCES = ["context.cu", "render.cu", "mega.cu", "selftest.cu", "mlp.cu", "bvh_gpu.cu", "post.cu", "env_light.cu"]
-CXX_SOURCES = ["bvh_build.cpp", "host_api.cpp", "image_out.cpp", "obj_load.cpp", "image_file.cpp"]
+CXX_SOURCES = ["bvh_build.cpp", "host_api.cpp", "image_out.cpp", "obj_load.cpp", "image_file.cpp", "image_formats.cpp"]
 
 
 def nvcc() -> str:

@@ -3,6 +3,7 @@
 // Radiance HDR reader (G. Ward's RGBE format: a text header, the resolution
 // line, then flat or run-length scanlines), and the MTL-to-texture mapping
 // of create_texture_from_file.
+#include "image_formats.h"
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -271,7 +272,7 @@ RC<Texture2D> texture_of(const std::string& name, real r, real g, real b) {
   if (name.empty()) return create_constant_texture2d(Spectrum(r, g, b));
   if (!r && !g && !b) r = g = b = 1;
   const std::string ext = extension(name);
-  if (ext == ".png") {
+  if (ext == ".png" || ext == ".jpg" || ext == ".jpeg") {
     // 8-bit maps: bytes / 255 raised to 2.2, back to bytes, times the scale
     // (each step truncating to a byte, as Point3<uint8_t> does)
     auto img = load_image_from_file(name);
@@ -286,11 +287,10 @@ RC<Texture2D> texture_of(const std::string& name, real r, real g, real b) {
       }
     return create_image_texture2d(img);
   }
-  if (ext != ".hdr") {
-    if (ext == ".jpg" || ext == ".jpeg")
-      throw TracerError(TR_ERR_UNSUPPORTED, "JPEG files have no reader here (convert to .png or .hdr): " + name);
-    throw TracerError(TR_ERR_ARG, "unsupported image format: " + name);
-  }
+  // is_float_image (src/utility/image_file.cpp:83-98): ".jpg", ".jpeg" and
+  // ".png" are 8-bit, ".hdr" float, everything else (".bmp" too: the
+  // reference compares with "bmp", without the dot) is refused
+  if (ext != ".hdr") throw TracerError(TR_ERR_ARG, "unsupported image format: " + name);
   auto img = load_hdr_from_file(name);
   for (int y = 0; y < img->height(); ++y)
     for (int x = 0; x < img->width(); ++x) {
@@ -392,16 +392,18 @@ RC<Image2D<Color3f>> load_hdr_from_file(const std::string& filename) {
 }
 
 RC<Image2D<Color3b>> load_image_from_file(const std::string& filename) {
-  const std::string ext = extension(filename);
-  if (ext != ".png")
-    throw TracerError(TR_ERR_UNSUPPORTED, "8-bit images are read from PNG files only: " + filename);
   std::ifstream f(filename, std::ios::binary);
   if (!f) throw TracerError(TR_ERR_ARG, "load image failed: " + filename);
   const std::vector<uint8_t> buf((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
   int w = 0, h = 0, comp = 0;
   std::vector<uint8_t> px;
   try {
-    px = decode_png(buf, w, h, comp);
+    // the format from the file's bytes, as stb_image finds it
+    if (buf.size() >= 8 && std::memcmp(buf.data(), "\x89PNG\r\n\x1a\n", 8) == 0) px = decode_png(buf, w, h, comp);
+    else if (tracer_files::is_jpeg(buf)) px = tracer_files::decode_jpeg(buf, w, h, comp);
+    else if (tracer_files::is_bmp(buf)) px = tracer_files::decode_bmp(buf, w, h, comp);
+    else if (tracer_files::is_tga(buf)) px = tracer_files::decode_tga(buf, w, h, comp);
+    else throw TracerError(TR_ERR_ARG, "unknown image format");
   } catch (const TracerError& e) {
     throw TracerError(e.status, std::string(e.what()) + ": " + filename);
   }
@@ -420,9 +422,7 @@ RC<Image2D<Color3b>> load_image_from_file(const std::string& filename) {
 RC<const Texture2D> create_texture2d_from_file(const std::string& filename) {
   const std::string ext = extension(filename);
   if (ext == ".hdr") return create_hdr_texture2d(load_hdr_from_file(filename));
-  if (ext == ".png") return create_image_texture2d(load_image_from_file(filename));
-  if (ext == ".jpg" || ext == ".jpeg")
-    throw TracerError(TR_ERR_UNSUPPORTED, "JPEG files have no reader here (convert to .png or .hdr): " + filename);
+  if (ext == ".png" || ext == ".jpg" || ext == ".jpeg") return create_image_texture2d(load_image_from_file(filename));
   throw TracerError(TR_ERR_ARG, "unsupported image format: " + filename);
 }
 
