@@ -80,6 +80,20 @@ KERNEL_NAMES = {"extend": "k_extend", "logic": "k_logic", "material_phong": "k_m
                 "shadow": "k_shadow"}
 
 
+def dram_bound(traffic_per_launch: float, launch_ms: float, peak_gbs: float) -> dict:
+    """What bounds a kernel, from its measured DRAM bytes per launch: the
+    DRAM bandwidth those bytes take over the launch's duration, as a fraction
+    of the HBM peak. The tree walks read a few percent of HBM bandwidth (L1
+    and L2 serve most node and triangle reads) and stall on dependent loads:
+    they are latency-bound, and the algorithmic fraction beside it says how
+    many bytes the walk touches, not what limits it."""
+    gbs = traffic_per_launch / (launch_ms / 1e3) / 1e9
+    frac = gbs / peak_gbs
+    return {"bound": "hbm" if frac >= 0.5 else "latency", "dram_gbs": gbs, "dram_frac": frac,
+            "frac_is": "algorithmic bytes / launch time / HBM peak; dram_frac: measured DRAM bytes / launch "
+                       "time / HBM peak"}
+
+
 def traffic_per_unit(stage: str):
     """DRAM bytes per work item of a kernel from a committed ncu summary, or None."""
     try:
@@ -162,6 +176,7 @@ def convergence(ctx, name: str, size=(1024, 768), ref_spp=4096, pass_spp=8, max_
         film = torch.zeros((H, W, 4), dtype=torch.float64, device=f"cuda:{torch.cuda.current_device()}")
         acc = np.zeros((H, W, 4), np.float64)
         spent, curve, reached, losses = 0.0, [], None, []
+        train_s = 0.0
         use_alpha = 0.0
         if guided:
             ctx.guide_init(seed=0)
@@ -175,7 +190,9 @@ def convergence(ctx, name: str, size=(1024, 768), ref_spp=4096, pass_spp=8, max_
                                                                light_guide=True, light_record=True),
                                       film.data_ptr(), fp64=True)
                 ctx.guide_light_update(light_share)
+                t1 = time.perf_counter()
                 loss = ctx.guide_train_on_records(train_steps + (warm_steps if k == 0 else 0), batch, lr, seed=k)
+                train_s += time.perf_counter() - t1
                 if np.isfinite(loss):
                     use_alpha = alpha
                 else:
@@ -199,7 +216,7 @@ def convergence(ctx, name: str, size=(1024, 768), ref_spp=4096, pass_spp=8, max_
                "relmse_curve_spp_s_relmse": curve}
         if guided:
             res.update({"alpha": alpha, "train_steps_per_pass": train_steps, "warm_steps": warm_steps, "batch": batch,
-                        "lr": lr, "record_every": record_every,
+                        "lr": lr, "record_every": record_every, "train_s": round(train_s, 4),
                         "light_table": {"grid": list(light_grid), "bins": light_bins, "uniform_share": light_share},
                         "mean_loss_per_pass": losses[:8] + (["..."] if len(losses) > 9 else []) + losses[-1:]})
         return res
@@ -839,6 +856,7 @@ def run_ours(args):
         if tr is not None:
             roof["traffic"] = tr["bytes_per_unit"] * dom_items / max(iters, 1)
             roof["traffic_source"] = tr["source"]
+            roof.update(dram_bound(roof["traffic"], roof["avg_launch_ms"], peak))
     else:
         roof.update({"achieved": None, "frac": None})
     conv = None

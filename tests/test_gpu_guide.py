@@ -191,3 +191,107 @@ def test_training_learns_a_direction_field(gpu):
     print("loss", [round(v, 3) for v in losses[::30]], "uniform", round(math.log(4 * math.pi), 3))
     assert all(np.isfinite(losses))
     assert np.mean(losses[-20:]) < math.log(4 * math.pi) - 1.0
+
+
+def _batch(rng, n, zero_weights=0):
+    x = rng.normal(0, 1, (n, 7)).astype(np.float32)
+    d = rng.normal(0, 1, (n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    w = rng.exponential(1.0, n).astype(np.float32)
+    w[:zero_weights] = 0.0
+    return x, d, w
+
+
+def _torch_grad(p, x, d, w):
+    import torch
+    layers = torch_params(p, True)
+    loss = mixture_nll(torch_net(layers, torch.tensor(x)), torch.tensor(d), torch.tensor(w))
+    loss.backward()
+    return loss.item(), flat_grads(layers)
+
+
+def _step(gpu, x, d, w, lr):
+    import torch
+    dx, ddir, dw = (torch.tensor(a, device="cuda:0") for a in (x, d, w))
+    torch.cuda.synchronize()
+    return gpu.guide_train_step_dev(dx.data_ptr(), ddir.data_ptr(), dw.data_ptr(), len(x), lr)
+
+
+@pytest.mark.parametrize("n", [77, 3000, 65536])
+def test_fused_training_step_against_torch(gpu, n):
+    """One Adam step through the fused kernels (forward, loss and backward in
+    one tcgen05 launch, Adam and the weight images in a second): the loss is
+    torch's, and Adam's first step moves every parameter by lr against the
+    sign of torch's fp32 gradient (m / sqrt(v) = g / |g| after one step)."""
+    rng = np.random.default_rng(n)
+    gpu.guide_init(seed=4)
+    p = gpu.guide_params()
+    x, d, w = _batch(rng, n, zero_weights=min(20, n // 4))
+    want_loss, g = _torch_grad(p, x, d, w)
+    lr = 1e-4
+    loss = _step(gpu, x, d, w, lr)
+    delta = gpu.guide_params().astype(np.float64) - p
+    print(f"n={n} loss gpu {loss:.6f} torch {want_loss:.6f}")
+    assert abs(loss - want_loss) <= 1e-3 * abs(want_loss)
+    o = 0
+    for i, (kin, kout) in enumerate(LAYERS):
+        for name, size in (("W", kin * kout), ("b", kout)):
+            gg, dd = g[o:o + size], delta[o:o + size]
+            big = np.abs(gg) > 2e-2 * np.abs(gg).max()
+            agree = (np.sign(dd[big]) == -np.sign(gg[big])).mean()
+            print(f"  layer {i} {name}: {big.sum()} significant gradients, sign agreement {agree:.4f}")
+            assert agree >= 0.99, (i, name, agree)
+            assert np.abs(np.abs(dd[big]) - lr).max() <= 0.05 * lr
+            o += size
+    # the packed images follow the parameters: a forward pass matches torch on the new parameters
+    import torch
+    p1 = gpu.guide_params()
+    xs = x[:256]
+    dxs = torch.tensor(xs, device="cuda:0")
+    out = torch.zeros((len(xs), 40), device="cuda:0")
+    torch.cuda.synchronize()
+    gpu.guide_forward_dev(dxs.data_ptr(), len(xs), out.data_ptr())
+    want = torch_forward(p1, xs)
+    assert np.abs(out.cpu().numpy() - want).max() <= TOL * np.abs(want).max()
+
+
+def test_fused_training_step_gradient_magnitudes(gpu):
+    """Two Adam steps on two batches: the second update is
+    -lr (0.09 g_a + 0.1 g_b) / 0.19 / sqrt((0.000999 g_a^2 + 0.001 g_b^2) / 0.001999),
+    which depends on the ratio of the two batches' gradients per parameter,
+    so it checks gradient magnitudes, not only signs (lr small enough that
+    the first step does not move the second gradient)."""
+    rng = np.random.default_rng(21)
+    gpu.guide_init(seed=6)
+    p = gpu.guide_params()
+    xa, da, wa = _batch(rng, 4000)
+    xb, db, wb = _batch(rng, 2500)
+    _, ga = _torch_grad(p, xa, da, wa)
+    _, gb = _torch_grad(p, xb, db, wb)
+    lr = 1e-6
+    _step(gpu, xa, da, wa, lr)
+    p1 = gpu.guide_params().astype(np.float64)
+    _step(gpu, xb, db, wb, lr)
+    delta = gpu.guide_params().astype(np.float64) - p1
+    ga, gb = ga.astype(np.float64), gb.astype(np.float64)
+    want = -lr * ((0.09 * ga + 0.1 * gb) / 0.19) / np.sqrt((0.000999 * ga ** 2 + 0.001 * gb ** 2) / 0.001999)
+    sig = np.maximum(np.abs(ga), np.abs(gb)) > 5e-2 * np.maximum(np.abs(ga).max(), np.abs(gb).max())
+    err = np.abs(delta - want)[sig] / lr
+    print(f"{sig.sum()} parameters; |update - expected| / lr: median {np.median(err):.4f}, "
+          f"99th percentile {np.percentile(err, 99):.4f}")
+    # fp32 parameters near 0.1-1 resolve an update of 1e-6 to ~1e-7 / 1e-6
+    assert np.percentile(err, 95) <= 0.1
+
+
+def test_fused_training_step_is_deterministic(gpu):
+    """The gradient partials of the CTAs are summed in a fixed order: the same
+    step from the same state gives bit-identical parameters."""
+    rng = np.random.default_rng(3)
+    x, d, w = _batch(rng, 20000)
+    outs = []
+    for _ in range(2):
+        gpu.guide_init(seed=8)
+        for _ in range(3):
+            _step(gpu, x, d, w, 1e-3)
+        outs.append(gpu.guide_params())
+    assert np.array_equal(outs[0].view(np.uint32), outs[1].view(np.uint32))

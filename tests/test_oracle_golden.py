@@ -3,8 +3,17 @@ own sources (tests/golden/make_golden.py). Bit-exact: the oracle repeats the
 reference's arithmetic operation by operation, including libstdc++'s
 partition/nth_element in the BVH build and glibc's libm.
 
-This is what pins the oracle on machines without the reference checkout."""
+This is what pins the oracle on machines without the reference checkout.
+
+The fixtures were made on x86-64. glibc's float acosf, asinf, tanf and
+atan2f are other implementations on aarch64 and differ from x86-64's in the
+last bit for about 0.1-1% of inputs (measured on the GB300 machine's Grace
+cores), and the sign of a generated NaN is the machine's. So on x86-64 every
+film is bit-exact; elsewhere a film whose scene reaches those functions
+(environment-light lookups, Disney sampling) must be bit-exact on at least
+98% of its pixels and within 1e-5 relative on all of them."""
 import os
+import platform
 
 import numpy as np
 import pytest
@@ -24,15 +33,23 @@ def bits(a):
     return np.ascontiguousarray(a).view(np.uint32)
 
 
+def same_bits(got, want):
+    """Bit-equal, except that a NaN matches any NaN: the sign of the NaN that
+    0/0 or inf - inf produces is the machine's (x86 sets it, Arm does not)."""
+    got, want = np.ascontiguousarray(got, np.float32), np.ascontiguousarray(want, np.float32)
+    nan = np.isnan(want)
+    return bool(np.array_equal(np.isnan(got), nan) and np.array_equal(bits(got)[~nan], bits(want)[~nan]))
+
+
 def test_units():
     g = load("units.npz")
     n = len(g["a"])
     assert np.array_equal(bits(oracle.unit("port", "cross", g["a"], g["b"], out_shape=(n, 3), n=n)), bits(g["cross"]))
-    assert np.array_equal(bits(oracle.unit("port", "normalize", g["a"], out_shape=(n, 3), n=n)), bits(g["normalize"]))
+    assert same_bits(oracle.unit("port", "normalize", g["a"], out_shape=(n, 3), n=n), g["normalize"])
     for s, row in zip(g["seeds"], g["pcg"]):
         assert np.array_equal(bits(oracle.pcg_uniform("port", int(s), len(row))), bits(row))
     # numpy restatement used to build rays and normals
-    assert np.array_equal(bits(scenes.ref_normalize(g["a"])), bits(g["normalize"]))
+    assert same_bits(scenes.ref_normalize(g["a"]), g["normalize"])
 
 
 def test_traversal():
@@ -57,7 +74,7 @@ def test_mixed_scene_render_and_trace():
     prim, t = orc.trace_closest(g["rays"].view(RAY_DTYPE))
     assert np.array_equal(prim, g["prim"]) and np.array_equal(bits(t), bits(g["t"]))
     orc.set_camera(cam, filt)
-    assert np.array_equal(bits(orc.render(par)), bits(g["rgbw"]))
+    assert_film(orc.render(par), g["rgbw"])
 
 
 @pytest.mark.parametrize("name", ["cornell_32x32_4spp.npz", "disney_grid_32x32_2spp.npz",
@@ -70,4 +87,17 @@ def test_renders(name):
     cam, filt, par = scenes.unpack_view(g)
     orc = oracle.Oracle(sc, "port")
     orc.set_camera(cam, filt)
-    assert np.array_equal(bits(orc.render(par)), bits(g["rgbw"]))
+    assert_film(orc.render(par), g["rgbw"])
+
+
+def assert_film(got, want):
+    if platform.machine() in ("x86_64", "AMD64"):
+        assert np.array_equal(bits(got), bits(want))
+        return
+    exact = (bits(got) == bits(want)).all(-1).mean()
+    a, b = got.astype(np.float64), want.astype(np.float64)
+    ia = a[..., :3] / np.maximum(a[..., 3:4], 1e-30)
+    ib = b[..., :3] / np.maximum(b[..., 3:4], 1e-30)
+    rel = (np.abs(ia - ib) / np.maximum(np.abs(ib), 1e-6)).max()
+    print(f"{platform.machine()}: {exact:.4f} of the pixels bit-exact, max relative difference {rel:.2e}")
+    assert exact >= 0.98 and rel <= 1e-5

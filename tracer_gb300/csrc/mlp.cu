@@ -391,53 +391,57 @@ __device__ __forceinline__ float vmf_log_norm(float kappa) {
   return logf(kappa) - 1.8378770664093453f - log1pf(-expf(-2.0f * kappa));
 }
 
+// log p(omega | z) of one row, and d[0..39] = the gradient of -wi log p
+// w.r.t. the row's 40 network outputs z.
+__device__ __forceinline__ float row_nll_grad(const float* z, float3 om, float wi, float* d) {
+  float a_max = -INFINITY;
+  for (int j = 0; j < kLobes; ++j) a_max = fmaxf(a_max, z[5 * j]);
+  float esum = 0.0f, lq[kLobes], pi[kLobes];
+  for (int j = 0; j < kLobes; ++j) {
+    pi[j] = expf(z[5 * j] - a_max);
+    esum += pi[j];
+  }
+  float lmax = -INFINITY;
+  Lobe L[kLobes];
+  for (int j = 0; j < kLobes; ++j) {
+    pi[j] /= esum;
+    const float s = fminf(fmaxf(z[5 * j + 1], TR_GUIDE_LOG_KAPPA_MIN), TR_GUIDE_LOG_KAPPA_MAX);
+    const float kappa = expf(s);
+    const float3 m = make_float3(z[5 * j + 2], z[5 * j + 3], z[5 * j + 4]);
+    const float mlen = sqrtf(m.x * m.x + m.y * m.y + m.z * m.z) + 1e-6f;
+    const float3 mu = make_float3(m.x / mlen, m.y / mlen, m.z / mlen);
+    const float c = mu.x * om.x + mu.y * om.y + mu.z * om.z;
+    L[j] = Lobe{pi[j], kappa, mlen, c, mu};
+    lq[j] = logf(fmaxf(pi[j], 1e-30f)) + vmf_log_norm(kappa) + kappa * (c - 1.0f);
+    lmax = fmaxf(lmax, lq[j]);
+  }
+  float qs = 0.0f;
+  for (int j = 0; j < kLobes; ++j) qs += expf(lq[j] - lmax);
+  const float logp = lmax + logf(qs);
+  for (int j = 0; j < kLobes; ++j) {
+    const float q = expf(lq[j] - logp);  // responsibility
+    const Lobe& b = L[j];
+    d[5 * j] = -wi * (q - b.pi);
+    const float s = z[5 * j + 1];
+    const float e2 = expf(-2.0f * b.kappa);
+    const float dlogk = 1.0f - 2.0f * b.kappa * e2 / fmaxf(-expm1f(-2.0f * b.kappa), 1e-30f) + b.kappa * (b.c - 1.0f);
+    d[5 * j + 1] = (s > TR_GUIDE_LOG_KAPPA_MIN && s < TR_GUIDE_LOG_KAPPA_MAX) ? -wi * q * dlogk : 0.0f;
+    const float f = -wi * q * b.kappa / b.mlen;
+    d[5 * j + 2] = f * (om.x - b.c * b.mu.x);
+    d[5 * j + 3] = f * (om.y - b.c * b.mu.y);
+    d[5 * j + 4] = f * (om.z - b.c * b.mu.z);
+  }
+  return logp;
+}
+
 __global__ void k_loss(const float* __restrict__ out, const float* __restrict__ dir, const float* __restrict__ w,
                        int n, const float* __restrict__ wsum, float* __restrict__ dout, float* __restrict__ loss) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   float li = 0.0f;
   if (i < n) {
-    const float* z = out + (size_t)i * kOut;
     const float3 om = make_float3(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]);
     const float wi = w[i] / fmaxf(*wsum, 1e-30f);
-    float a_max = -INFINITY;
-    for (int j = 0; j < kLobes; ++j) a_max = fmaxf(a_max, z[5 * j]);
-    float esum = 0.0f, lq[kLobes], pi[kLobes];
-    for (int j = 0; j < kLobes; ++j) {
-      pi[j] = expf(z[5 * j] - a_max);
-      esum += pi[j];
-    }
-    float lmax = -INFINITY;
-    Lobe L[kLobes];
-    for (int j = 0; j < kLobes; ++j) {
-      pi[j] /= esum;
-      const float s = fminf(fmaxf(z[5 * j + 1], TR_GUIDE_LOG_KAPPA_MIN), TR_GUIDE_LOG_KAPPA_MAX);
-      const float kappa = expf(s);
-      const float3 m = make_float3(z[5 * j + 2], z[5 * j + 3], z[5 * j + 4]);
-      const float mlen = sqrtf(m.x * m.x + m.y * m.y + m.z * m.z) + 1e-6f;
-      const float3 mu = make_float3(m.x / mlen, m.y / mlen, m.z / mlen);
-      const float c = mu.x * om.x + mu.y * om.y + mu.z * om.z;
-      L[j] = Lobe{pi[j], kappa, mlen, c, mu};
-      lq[j] = logf(fmaxf(pi[j], 1e-30f)) + vmf_log_norm(kappa) + kappa * (c - 1.0f);
-      lmax = fmaxf(lmax, lq[j]);
-    }
-    float qs = 0.0f;
-    for (int j = 0; j < kLobes; ++j) qs += expf(lq[j] - lmax);
-    const float logp = lmax + logf(qs);
-    li = -wi * logp;
-    float* d = dout + (size_t)i * kOut;
-    for (int j = 0; j < kLobes; ++j) {
-      const float q = expf(lq[j] - logp);  // responsibility
-      const Lobe& b = L[j];
-      d[5 * j] = -wi * (q - b.pi);
-      const float s = z[5 * j + 1];
-      const float e2 = expf(-2.0f * b.kappa);
-      const float dlogk = 1.0f - 2.0f * b.kappa * e2 / fmaxf(-expm1f(-2.0f * b.kappa), 1e-30f) + b.kappa * (b.c - 1.0f);
-      d[5 * j + 1] = (s > TR_GUIDE_LOG_KAPPA_MIN && s < TR_GUIDE_LOG_KAPPA_MAX) ? -wi * q * dlogk : 0.0f;
-      const float f = -wi * q * b.kappa / b.mlen;
-      d[5 * j + 2] = f * (om.x - b.c * b.mu.x);
-      d[5 * j + 3] = f * (om.y - b.c * b.mu.y);
-      d[5 * j + 4] = f * (om.z - b.c * b.mu.z);
-    }
+    li = -wi * row_nll_grad(out + (size_t)i * kOut, om, wi, dout + (size_t)i * kOut);
   }
   // block sum of the loss
   for (int o = 16; o > 0; o >>= 1) li += __shfl_xor_sync(0xffffffffu, li, o);
@@ -461,6 +465,364 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
   m[i] = mi;
   v[i] = vi;
   p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + 1e-8f);
+}
+
+// ------------------------------------------------------------ fused training step
+//
+// One Adam step on a batch is two launches: k_train and k_update.
+//
+// k_train does the batch's forward pass, loss and backward pass on the
+// tensor cores. CTAs (one per SM, 128 threads, all 512 TMEM columns) walk
+// 128-row tiles. A tile's rows are gathered from the record arrays; each
+// layer's input is kept in shared memory twice, as the forward MMA's A
+// operand and transposed (in_l^T) as the B operand of the weight-gradient
+// MMA; the last layer's epilogue evaluates the loss and its gradient; the
+// backward chain is the one of k_backward, with the ReLU masks held in
+// registers. Weight gradients accumulate in TMEM over the CTA's tiles and are
+// written once per CTA as a partial sum (no atomics).
+//
+// k_update sums the partials in a fixed order (the step is deterministic),
+// takes the Adam step and writes the updated fp16 weights and fp32 biases
+// into both packed images in place.
+//
+// Loss weighting: loss = sum_i -w_i log p_i / sum_i w_i. The rows carry
+// s * w_i into the fp16 gradient chain, s = N / (64 W) for the weight sum W
+// of N rows (the whole record set, or the batch), so the per-row values sit
+// in fp16's normal range; k_update divides by s * sum_i w_i.
+
+constexpr uint32_t kTWt = 34048;                           // transposed weights, kWtBytes
+constexpr uint32_t kTA = kTWt + kWtBytes;                  // forward A operand / backward dZ (128 x 64)
+constexpr uint32_t kTDzT = kTA + kTile * kHid * 2;         // dZ^T (128 x 128)
+constexpr uint32_t kTIn = kTDzT + 128 * kTile * 2;         // in_l^T, l = 0..4
+__host__ __device__ constexpr uint32_t tin_off(int l) {
+  return l == 0 ? kTIn : kTIn + (uint32_t)kInPad * kTile * 2 + (uint32_t)(l - 1) * 80u * kTile * 2;
+}
+constexpr uint32_t kTRed = tin_off(4) + 80u * kTile * 2;   // block-reduction scratch
+constexpr uint32_t kTMbar = kTRed + 64;
+constexpr uint32_t kTSlot = kTMbar + 8;
+constexpr uint32_t kTSmemBytes = kTSlot + 8;
+static_assert(kPackedBytes <= kTWt && kTWt % 128 == 0 && kTA % 128 == 0 && kTIn % 128 == 0, "k_train layout");
+static_assert(kTSmemBytes <= 227 * 1024, "k_train shared memory");
+constexpr int kPartStride = kParams + 16;  // per-CTA partial: gradients, then weight sum and loss sum
+constexpr int kWsumParts = 128;            // blocks of k_wsum
+constexpr float kRowScale = 1.0f / 64.0f;
+
+// The batch's row i: a record index drawn by a hash of (seed, i).
+__device__ __forceinline__ unsigned int batch_record(unsigned long long seed, unsigned int i, unsigned int count) {
+  unsigned long long h = seed * 0x9E3779B97F4A7C15ull + i * 0xBF58476D1CE4E5B9ull + 0x94D049BB133111EBull;
+  h ^= h >> 31;
+  h *= 0xD6E8FEB86659FD93ull;
+  h ^= h >> 32;
+  return (unsigned int)(h % count);
+}
+
+// Per-block sums of w[0..n) in a fixed order (kWsumParts blocks of 256).
+__global__ void k_wsum(const float* __restrict__ w, unsigned int n, float* __restrict__ parts) {
+  __shared__ float red[256];
+  float s = 0.0f;
+  for (unsigned int i = blockIdx.x * 256u + threadIdx.x; i < n; i += kWsumParts * 256u) s += w[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) parts[blockIdx.x] = red[0];
+}
+
+// The row scale s = nrows / (64 W) from k_wsum's partial sums, in a fixed order.
+__global__ void k_scale(const float* __restrict__ parts, float nrows, float* __restrict__ scale) {
+  __shared__ float red[kWsumParts];
+  red[threadIdx.x] = parts[threadIdx.x];
+  __syncthreads();
+  for (int o = kWsumParts / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *scale = nrows * kRowScale / fmaxf(red[0], 1e-30f);
+}
+
+__device__ __forceinline__ __half sat_half(float v) {
+  return __float2half_rn(fminf(fmaxf(v, -65504.0f), 65504.0f));
+}
+
+// rec_in: count x 7, rec_dir: count x 3, rec_w: count. gather != 0: row i of
+// the batch is record batch_record(seed, i, count); else record i.
+// part: gridDim.x x kPartStride floats.
+__global__ void __launch_bounds__(128, 1)
+    k_train(const uint8_t* __restrict__ img, const uint8_t* __restrict__ img_t, const float* __restrict__ rin,
+            const float* __restrict__ rdir, const float* __restrict__ rw, unsigned int count, int n,
+            unsigned long long seed, int gather, const float* __restrict__ scale, float* __restrict__ part,
+            int* err) {
+  extern __shared__ __align__(1024) uint8_t sm[];
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int i = tid; i < (int)(kPackedBytes / 16); i += blockDim.x)
+    reinterpret_cast<int4*>(sm)[i] = reinterpret_cast<const int4*>(img)[i];
+  for (int i = tid; i < (int)(kWtBytes / 16); i += blockDim.x)
+    reinterpret_cast<int4*>(sm + kTWt)[i] = reinterpret_cast<const int4*>(img_t)[i];
+  // operands start zero: padding rows and columns are never written again
+  for (int i = tid; i < (int)((kTRed - kTA) / 16); i += blockDim.x)
+    reinterpret_cast<int4*>(sm + kTA)[i] = make_int4(0, 0, 0, 0);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + kTMbar);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(sm + kTSlot);
+  if (tid == 0) tc05::mbar_init(mbar, 1);
+  if (warp == 0) tc05::tmem_alloc(slot, 512);
+  tc05::fence_before();
+  __syncthreads();
+  tc05::fence_after();
+  const uint32_t tmem = *slot;
+  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+  const float* bias = reinterpret_cast<const float*>(sm + kBiasOff);
+  uint8_t* A = sm + kTA;
+  uint8_t* DzT = sm + kTDzT;
+  const uint32_t w_addr = tc05::smem_u32(sm), wt_addr = tc05::smem_u32(sm + kTWt), a_addr = tc05::smem_u32(A),
+                 dzt_addr = tc05::smem_u32(DzT);
+  const float s = *scale;
+  float w_acc = 0.0f, l_acc = 0.0f;
+  uint32_t phase = 0;
+  bool ok = true;
+  int tiles_done = 0;
+  const int ntiles = (n + kTile - 1) / kTile;
+  for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+    const int i = t * kTile + tid;
+    const bool live = i < n;
+    float x[kIn], om[3], w = 0.0f;
+    {
+      const unsigned int j = live ? (gather ? batch_record(seed, (unsigned int)i, count) : (unsigned int)i) : 0u;
+#pragma unroll
+      for (int k = 0; k < kIn; ++k) x[k] = live ? rin[(size_t)j * kIn + k] : 0.0f;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) om[k] = live ? rdir[(size_t)j * 3 + k] : 0.0f;
+      if (live) w = rw[j];
+    }
+    {  // layer 0's input: the A operand (zero-padded to 16) and in_0^T (ones row at 7 for the bias)
+      __align__(16) __half h[16];
+#pragma unroll
+      for (int k = 0; k < 16; ++k) h[k] = __float2half_rn(k < kIn ? x[k] : 0.0f);
+      *reinterpret_cast<int4*>(A + tc05::core_off(tid, 0, kInPad)) = *reinterpret_cast<const int4*>(h);
+      *reinterpret_cast<int4*>(A + tc05::core_off(tid, 8, kInPad)) = *reinterpret_cast<const int4*>(h + 8);
+#pragma unroll
+      for (int k = 0; k < 16; ++k)
+        st_half(sm + tin_off(0), tc05::core_off(k, tid, kTile), k < kIn ? x[k] : (k == kIn && live ? 1.0f : 0.0f));
+    }
+    uint32_t mask[4][2];  // ReLU masks of this row's hidden units (h > 0 in fp16)
+    tc05::fence_proxy_async();
+    __syncthreads();
+    // ---- forward
+    for (int l = 0; l < kLayers && ok; ++l) {
+      const int K = layer_k(l), N = layer_n(l);
+      if (tid == 0) {
+        tc05::fence_after();
+        const uint32_t sbo = (uint32_t)(K / 8) * 128u;
+        for (int kk = 0; kk < K / 16; ++kk)
+          tc05::mma_f16(tmem, tc05::smem_desc(a_addr + kk * 256u, 128u, sbo),
+                        tc05::smem_desc(w_addr + w_off(l) + kk * 256u, 128u, sbo),
+                        tc05::idesc_f16_f32(128, (uint32_t)N), kk > 0 ? 1u : 0u);
+        tc05::commit(mbar);
+      }
+      const bool got = tc05::mbar_wait(mbar, phase);
+      ok = __syncthreads_and(got) != 0;
+      if (!ok) break;
+      phase ^= 1u;
+      tc05::fence_after();
+      if (l < kLayers - 1) {
+        uint8_t* inT = sm + tin_off(l + 1);
+        mask[l][0] = mask[l][1] = 0u;
+#pragma unroll
+        for (int c0 = 0; c0 < kHid; c0 += 16) {
+          float v[16];
+          tc05::tmem_ld16(tmem + lane_base + (uint32_t)c0, v);
+          __align__(16) __half h[16];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            h[j] = __float2half_rn(fmaxf(v[j] + bias[l * 64 + c0 + j], 0.0f));
+            if (__half2float(h[j]) > 0.0f) mask[l][c0 >> 5] |= 1u << ((c0 + j) & 31);
+            *reinterpret_cast<__half*>(inT + tc05::core_off(c0 + j, tid, kTile)) = h[j];
+          }
+          *reinterpret_cast<int4*>(A + tc05::core_off(tid, c0, kHid)) = *reinterpret_cast<const int4*>(h);
+          *reinterpret_cast<int4*>(A + tc05::core_off(tid, c0 + 8, kHid)) = *reinterpret_cast<const int4*>(h + 8);
+        }
+        st_half(inT, tc05::core_off(kHid, tid, kTile), live ? 1.0f : 0.0f);
+      } else {
+        // loss and its gradient w.r.t. the outputs: dZ_4 into dZ (K = 48) and dZ^T
+        float z[kOutPad];
+#pragma unroll
+        for (int c = 0; c < kOutPad / 16; ++c) {
+          float v[16];
+          tc05::tmem_ld16(tmem + lane_base + (uint32_t)(16 * c), v);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) z[16 * c + j] = 16 * c + j < kOut ? v[j] + bias[256 + 16 * c + j] : 0.0f;
+        }
+        float d[kOut];
+        if (live) {
+          const float logp = row_nll_grad(z, make_float3(om[0], om[1], om[2]), w * s, d);
+          w_acc += w;
+          l_acc -= w * logp;
+        } else {
+#pragma unroll
+          for (int c = 0; c < kOut; ++c) d[c] = 0.0f;
+        }
+#pragma unroll
+        for (int c = 0; c < kOutPad; ++c)
+          *reinterpret_cast<__half*>(A + tc05::core_off(tid, c, kOutPad)) = sat_half(c < kOut ? d[c] : 0.0f);
+#pragma unroll
+        for (int c = 0; c < kHid; ++c)
+          *reinterpret_cast<__half*>(DzT + tc05::core_off(c, tid, kTile)) = sat_half(c < kOut ? d[c] : 0.0f);
+      }
+      tc05::fence_before();
+      tc05::fence_proxy_async();
+      __syncthreads();
+    }
+    // ---- backward: dW_l (+)= dZ_l^T in_l, dH = dZ_l W_l, dZ_{l-1} = dH * mask
+    for (int l = kLayers - 1; l >= 0 && ok; --l) {
+      if (tid == 0) {
+        tc05::fence_after();
+        const uint32_t acc0 = tiles_done > 0 ? 1u : 0u;
+        for (int kk = 0; kk < kTile / 16; ++kk)
+          tc05::mma_f16(tmem + bk_col(l), tc05::smem_desc(dzt_addr + kk * 256u, 128u, 2048u),
+                        tc05::smem_desc(tc05::smem_u32(sm + tin_off(l)) + kk * 256u, 128u, 2048u),
+                        tc05::idesc_f16_f32(128, bk_n(l)), (acc0 || kk > 0) ? 1u : 0u);
+        if (l > 0) {
+          const int KK = layer_n(l);
+          const uint32_t sbo = (uint32_t)(KK / 8) * 128u;
+          for (int kk = 0; kk < KK / 16; ++kk)
+            tc05::mma_f16(tmem, tc05::smem_desc(a_addr + kk * 256u, 128u, sbo),
+                          tc05::smem_desc(wt_addr + wt_off(l) + kk * 256u, 128u, sbo), tc05::idesc_f16_f32(128, 64),
+                          kk > 0 ? 1u : 0u);
+        }
+        tc05::commit(mbar);
+      }
+      const bool got = tc05::mbar_wait(mbar, phase);
+      ok = __syncthreads_and(got) != 0;
+      if (!ok) break;
+      phase ^= 1u;
+      if (l == 0) break;
+      tc05::fence_after();
+#pragma unroll
+      for (int c0 = 0; c0 < kHid; c0 += 16) {
+        float v[16];
+        tc05::tmem_ld16(tmem + lane_base + (uint32_t)c0, v);
+        __align__(16) __half h[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int c = c0 + j;
+          h[j] = sat_half((mask[l - 1][c >> 5] >> (c & 31)) & 1u ? v[j] : 0.0f);
+          *reinterpret_cast<__half*>(DzT + tc05::core_off(c, tid, kTile)) = h[j];
+        }
+        *reinterpret_cast<int4*>(A + tc05::core_off(tid, c0, kHid)) = *reinterpret_cast<const int4*>(h);
+        *reinterpret_cast<int4*>(A + tc05::core_off(tid, c0 + 8, kHid)) = *reinterpret_cast<const int4*>(h + 8);
+      }
+      tc05::fence_before();
+      tc05::fence_proxy_async();
+      __syncthreads();
+    }
+    ++tiles_done;
+  }
+  if (!ok) {
+    if (tid == 0) atomicOr(err, 1);
+    tc05::mbar_wait(mbar, phase);  // the same phase, bounded: let an MMA still in flight finish
+  }
+  __syncthreads();
+  tc05::fence_after();
+  // this CTA's partial: weight gradients from TMEM lanes 0..63 (one output unit per lane)
+  float* mine = part + (size_t)blockIdx.x * kPartStride;
+  if (warp < 2) {
+    const int o = tid;
+    for (int l = 0; l < kLayers; ++l) {
+      const int N = bk_n(l), kin = layer_kin(l);
+      for (int c0 = 0; c0 < N; c0 += 16) {
+        float v[16];
+        tc05::tmem_ld16(tmem + lane_base + bk_col(l) + (uint32_t)c0, v);
+        if (o < layer_nout(l)) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int k = c0 + j;
+            const float g = (ok && tiles_done > 0) ? v[j] : 0.0f;
+            if (k < kin) mine[param_w(l) + o * kin + k] = g;
+            else if (k == kin) mine[param_b(l) + o] = g;
+          }
+        }
+      }
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    w_acc += __shfl_xor_sync(0xffffffffu, w_acc, off);
+    l_acc += __shfl_xor_sync(0xffffffffu, l_acc, off);
+  }
+  float* red = reinterpret_cast<float*>(sm + kTRed);
+  if ((tid & 31) == 0) {
+    red[2 * warp] = w_acc;
+    red[2 * warp + 1] = l_acc;
+  }
+  tc05::fence_before();
+  __syncthreads();
+  if (tid == 0) {
+    mine[kParams] = (red[0] + red[2]) + (red[4] + red[6]);
+    mine[kParams + 1] = (red[1] + red[3]) + (red[5] + red[7]);
+  }
+  if (warp == 0) {
+    tc05::tmem_dealloc(tmem, 512);
+    tc05::tmem_relinquish();
+  }
+}
+
+// Sums the nparts partials (32 parameters x 8 partial slices per block),
+// takes the Adam step, and writes the new weight (or bias) into the forward
+// image and, for layers 1..4, the transposed image. loss_out (optional)
+// receives the batch loss.
+__global__ void __launch_bounds__(256)
+    k_update(const float* __restrict__ part, int nparts, const float* __restrict__ scale,
+             float* __restrict__ p, float* __restrict__ m, float* __restrict__ v, float lr, float c1, float c2,
+             uint8_t* __restrict__ img, uint8_t* __restrict__ img_t, float* __restrict__ loss_out) {
+  __shared__ float red[8][33];
+  __shared__ float tot[8][2];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i = blockIdx.x * 32 + tx;
+  float g = 0.0f, ws = 0.0f, ls = 0.0f;
+  for (int c = ty; c < nparts; c += 8) {
+    const float* pc = part + (size_t)c * kPartStride;
+    if (i < kParams) g += pc[i];
+    if (tx == 0) {
+      ws += pc[kParams];
+      ls += pc[kParams + 1];
+    }
+  }
+  red[ty][tx] = g;
+  if (tx == 0) {
+    tot[ty][0] = ws;
+    tot[ty][1] = ls;
+  }
+  __syncthreads();
+  if (ty != 0 || i >= kParams) return;
+  g = 0.0f;
+  ws = 0.0f;
+  ls = 0.0f;
+#pragma unroll
+  for (int y = 0; y < 8; ++y) {
+    g += red[y][tx];
+    ws += tot[y][0];
+    ls += tot[y][1];
+  }
+  if (loss_out && i == 0) *loss_out = ls / fmaxf(ws, 1e-30f);
+  const float denom = *scale * ws;
+  g = denom > 1e-30f ? g / denom : 0.0f;
+  const float mi = 0.9f * m[i] + 0.1f * g;
+  const float vi = 0.999f * v[i] + 0.001f * g * g;
+  m[i] = mi;
+  v[i] = vi;
+  const float pi = p[i] - lr * (mi / c1) / (sqrtf(vi / c2) + 1e-8f);
+  p[i] = pi;
+  int l = kLayers - 1;
+  while (l > 0 && i < param_w(l)) --l;
+  const int kin = layer_kin(l), e = i - param_w(l);
+  if (e < layer_nout(l) * kin) {
+    const int o = e / kin, k = e % kin;
+    *reinterpret_cast<__half*>(img + w_off(l) + tc05::core_off(o, k, layer_k(l))) = __float2half_rn(pi);
+    if (l > 0) *reinterpret_cast<__half*>(img_t + wt_off(l) + tc05::core_off(k, o, layer_n(l))) = __float2half_rn(pi);
+  } else {
+    const int o = e - layer_nout(l) * kin;
+    reinterpret_cast<float*>(img + kBiasOff)[l < kLayers - 1 ? l * 64 + o : 256 + o] = pi;
+  }
 }
 
 }  // namespace mlp
@@ -487,12 +849,15 @@ tr_status guide_reserve(tr_ctx* ctx) {
   for (auto pr : {std::make_pair(&g->params, (size_t)mlp::kParams * 4), std::make_pair(&g->img, (size_t)mlp::kPackedBytes),
                   std::make_pair(&g->img_t, (size_t)mlp::kWtBytes), std::make_pair(&g->grads, (size_t)mlp::kParams * 4),
                   std::make_pair(&g->adam_m, (size_t)mlp::kParams * 4),
-                  std::make_pair(&g->adam_v, (size_t)mlp::kParams * 4), std::make_pair(&g->scal, (size_t)64)})
+                  std::make_pair(&g->adam_v, (size_t)mlp::kParams * 4),
+                  std::make_pair(&g->scal, (size_t)(16 + mlp::kWsumParts) * 4)})
     if ((e = pr.first->reserve(pr.second)) != cudaSuccess) return cuda_fail(ctx, e, "guide model allocation");
   if (!g->attr_set) {
     if ((e = cudaFuncSetAttribute(mlp::k_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::kSmemBytes)) !=
             cudaSuccess ||
         (e = cudaFuncSetAttribute(mlp::k_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::kBSmemBytes)) !=
+            cudaSuccess ||
+        (e = cudaFuncSetAttribute(mlp::k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, mlp::kTSmemBytes)) !=
             cudaSuccess)
       return cuda_fail(ctx, e, "guide kernels' shared memory");
     g->attr_set = true;
@@ -544,41 +909,56 @@ tr_status guide_forward_rows_on_device(tr_ctx* ctx, const float* d_in, const uns
   return e == cudaSuccess ? TR_OK : cuda_fail(ctx, e, "k_forward");
 }
 
-// Random batch of training records: rows idx = hash(seed, i) % count.
-__global__ void k_gather(const float* __restrict__ in, const float* __restrict__ dir, const float* __restrict__ w,
-                         unsigned int count, unsigned int batch, unsigned long long seed, float* __restrict__ bin,
-                         float* __restrict__ bdir, float* __restrict__ bw) {
-  const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= batch) return;
-  unsigned long long h = seed * 0x9E3779B97F4A7C15ull + i * 0xBF58476D1CE4E5B9ull + 0x94D049BB133111EBull;
-  h ^= h >> 31;
-  h *= 0xD6E8FEB86659FD93ull;
-  h ^= h >> 32;
-  const unsigned int j = (unsigned int)(h % count);
-  for (int k = 0; k < mlp::kIn; ++k) bin[(size_t)i * mlp::kIn + k] = in[(size_t)j * mlp::kIn + k];
-  for (int k = 0; k < 3; ++k) bdir[(size_t)i * 3 + k] = dir[(size_t)j * 3 + k];
-  bw[i] = w[j];
+// The row scale of a training pass or step (scal[2]) from the weights w[0..n).
+static tr_status guide_scale(tr_ctx* ctx, const float* w, unsigned int n) {
+  float* scal = ctx->guide->scal.as<float>();
+  mlp::k_wsum<<<mlp::kWsumParts, 256, 0, ctx->stream>>>(w, n, scal + 16);
+  mlp::k_scale<<<1, mlp::kWsumParts, 0, ctx->stream>>>(scal + 16, (float)n, scal + 2);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? TR_OK : cuda_fail(ctx, e, "guide weight sum");
+}
+
+// One Adam step on n rows (gather: drawn from `count` records by seed), two
+// launches: k_train, k_update. The batch loss lands in *d_loss (device).
+static tr_status guide_fused_step(tr_ctx* ctx, const float* in, const float* dir, const float* w, unsigned int count,
+                                  int n, int gather, unsigned long long seed, float lr, float* d_loss) {
+  GuideModel* g = ctx->guide;
+  const int grid = guide_grid(ctx, n, 1);
+  cudaError_t e;
+  if ((e = g->part.reserve((size_t)grid * mlp::kPartStride * 4)) != cudaSuccess)
+    return cuda_fail(ctx, e, "guide gradient partials");
+  const float* scale = g->scal.as<float>() + 2;
+  mlp::k_train<<<grid, 128, mlp::kTSmemBytes, ctx->stream>>>(g->img.as<uint8_t>(), g->img_t.as<uint8_t>(), in, dir, w,
+                                                              count, n, seed, gather, scale, g->part.as<float>(),
+                                                              ctx->d_err.as<int>() + 2);
+  ++g->step;
+  const float c1 = 1.0f - std::pow(0.9f, (float)g->step), c2 = 1.0f - std::pow(0.999f, (float)g->step);
+  mlp::k_update<<<(mlp::kParams + 31) / 32, dim3(32, 8), 0, ctx->stream>>>(
+      g->part.as<float>(), grid, scale, g->params.as<float>(), g->adam_m.as<float>(), g->adam_v.as<float>(), lr, c1,
+      c2, g->img.as<uint8_t>(), g->img_t.as<uint8_t>(), d_loss);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? TR_OK : cuda_fail(ctx, e, "guide training step");
 }
 
 tr_status guide_train_on(tr_ctx* ctx, const float* rec_in, const float* rec_dir, const float* rec_w, unsigned int count,
                          int steps, unsigned int batch, float lr, unsigned long long seed, float* mean_loss) {
   GuideModel* g = ctx->guide;
   cudaError_t e;
-  if ((e = g->batch.reserve((size_t)batch * 11 * 4)) != cudaSuccess) return cuda_fail(ctx, e, "training batch");
-  float* bin = g->batch.as<float>();
-  float* bdir = bin + (size_t)batch * 7;
-  float* bw = bdir + (size_t)batch * 3;
-  double sum = 0.0;
+  if ((e = g->losses.reserve((size_t)std::max(steps, 1) * 4)) != cudaSuccess)
+    return cuda_fail(ctx, e, "training losses");
+  tr_status st = guide_scale(ctx, rec_w, count);
+  if (st != TR_OK) return st;
   for (int s = 0; s < steps; ++s) {
-    k_gather<<<(batch + 255) / 256, 256, 0, ctx->stream>>>(rec_in, rec_dir, rec_w, count, batch,
-                                                            seed * 1000003ull + (unsigned long long)s, bin, bdir, bw);
-    tr_status st = guide_train_step(ctx, bin, bdir, bw, (int)batch, lr);
+    st = guide_fused_step(ctx, rec_in, rec_dir, rec_w, count, (int)batch, 1, seed * 1000003ull + (unsigned long long)s,
+                          lr, g->losses.as<float>() + s);
     if (st != TR_OK) return st;
-    float l = 0.0f;
-    TR_CUDA(ctx, cudaMemcpyAsync(&l, g->scal.as<float>() + 1, 4, cudaMemcpyDeviceToHost, ctx->stream));
-    TR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    sum += l;
   }
+  std::vector<float> l((size_t)steps);
+  if (steps)
+    TR_CUDA(ctx, cudaMemcpyAsync(l.data(), g->losses.p, (size_t)steps * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  TR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  double sum = 0.0;
+  for (float v : l) sum += v;
   if (mean_loss) *mean_loss = steps ? (float)(sum / steps) : 0.0f;
   return TR_OK;
 }
@@ -624,21 +1004,9 @@ static tr_status guide_loss(tr_ctx* ctx, const float* d_in, const float* d_dir, 
 }
 
 tr_status guide_train_step(tr_ctx* ctx, const float* d_in, const float* d_dir, const float* d_w, int n, float lr) {
-  tr_status s = guide_loss(ctx, d_in, d_dir, d_w, n);
+  tr_status s = guide_scale(ctx, d_w, (unsigned int)n);
   if (s != TR_OK) return s;
-  GuideModel* g = ctx->guide;
-  TR_CUDA(ctx, cudaMemsetAsync(g->grads.p, 0, mlp::kParams * 4, ctx->stream));
-  mlp::k_backward<<<guide_grid(ctx, n, 1), 128, mlp::kBSmemBytes, ctx->stream>>>(
-      g->img_t.as<uint8_t>(), d_in, g->acts.as<__half>(), g->dout.as<float>(), n, g->grads.as<float>(),
-      ctx->d_err.as<int>() + 2);
-  ++g->step;
-  const float c1 = 1.0f - std::pow(0.9f, (float)g->step), c2 = 1.0f - std::pow(0.999f, (float)g->step);
-  mlp::k_adam<<<(mlp::kParams + 255) / 256, 256, 0, ctx->stream>>>(g->params.as<float>(), g->grads.as<float>(),
-                                                                    g->adam_m.as<float>(), g->adam_v.as<float>(), lr,
-                                                                    c1, c2);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "guide training step");
-  return guide_pack(ctx);
+  return guide_fused_step(ctx, d_in, d_dir, d_w, (unsigned int)n, n, 0, 0ull, lr, ctx->guide->scal.as<float>() + 1);
 }
 
 // Synchronises and turns a timed-out tensor-core wait into an error.
@@ -657,7 +1025,7 @@ void release_guide(tr_ctx* ctx) {
   if (!ctx->guide) return;
   GuideModel* g = ctx->guide;
   for (DevBuf* b : {&g->params, &g->img, &g->img_t, &g->grads, &g->adam_m, &g->adam_v, &g->acts, &g->out, &g->dout,
-                    &g->scal, &g->batch})
+                    &g->scal, &g->part, &g->losses})
     b->release();
   delete g;
   ctx->guide = nullptr;

@@ -25,8 +25,10 @@ struct GuideModel {
   DevBuf img;     // fp16 weights in the forward MMA layout + fp32 biases
   DevBuf img_t;   // fp16 transposed weights of layers 1..4 (backward)
   DevBuf grads, adam_m, adam_v;
-  DevBuf acts, out, dout, scal;  // training workspace (grown on demand)
-  DevBuf batch;                  // gathered training batch (in, dir, weight)
+  DevBuf acts, out, dout;        // workspace of the unfused entry points (grown on demand)
+  DevBuf scal;                   // [1] loss, [2] row scale, [16..] weight partial sums
+  DevBuf part;                   // per-CTA gradient partials of the fused training step
+  DevBuf losses;                 // per-step batch losses of a training pass
   int64_t step = 0;              // Adam steps taken
   bool attr_set = false;
 };
