@@ -77,7 +77,7 @@ def kernel_bytes(stage: str, nl: int, boxes_per_ray=0.0, prims_per_ray=0.0) -> f
 
 KERNEL_NAMES = {"extend": "k_extend", "logic": "k_logic", "material_phong": "k_material<0>",
                 "material_disney": "k_material<1>", "nee_phong": "k_nee<0>", "nee_disney": "k_nee<1>",
-                "shadow": "k_shadow"}
+                "shadow": "k_shadow", "bin": "k_bin_count + k_bin_scan + k_bin_scatter"}
 
 
 def dram_bound(traffic_per_launch: float, launch_ms: float, peak_gbs: float) -> dict:
@@ -530,7 +530,7 @@ def run_batch(args):
         ctx.close()
         return 0
     stage_ms = dict(zip(STAGE_NAMES, staged.stage_ms))
-    dom = max((k for k in STAGE_NAMES if k != "reset"), key=lambda k: stage_ms[k])
+    dom = max((k for k in STAGE_NAMES if k not in ("reset", "bin")), key=lambda k: stage_ms[k])
     tris = int(sum(len(it[0].indices) for it in items))
     # the same set with the device BVH builder (outside the timed region):
     # upload time and rendering rate over its trees
@@ -834,7 +834,7 @@ def run_ours(args):
     stage_ms = dict(zip(STAGE_NAMES, staged.stage_ms))
     iters = staged.iterations
     items = {"extend": staged.extend_rays, "shadow": staged.shadow_rays, "logic": staged.shade_items}
-    kernels = [k for k in STAGE_NAMES if k != "reset" and stage_ms[k] > 0]
+    kernels = [k for k in STAGE_NAMES if k not in ("reset", "bin") and stage_ms[k] > 0]
     dom = max(kernels, key=lambda k: stage_ms[k])
     per = {}
     if staged.extend_rays:

@@ -214,7 +214,8 @@ enum {
   TR_STAGE_NEE_DISNEY = 5,      /* same, Disney12 */
   TR_STAGE_SHADOW = 6,          /* any hit of shadow rays */
   TR_STAGE_RESET = 7,           /* queue-counter resets */
-  TR_NUM_STAGES = 8
+  TR_STAGE_BIN = 8,             /* ray binning before the closest hit (tr_tuning.ray_bin_bits) */
+  TR_NUM_STAGES = 9
 };
 
 typedef struct tr_stats {
@@ -224,7 +225,7 @@ typedef struct tr_stats {
   uint64_t shade_items;  /* path vertices processed by the shade stage */
   uint64_t iterations;   /* wavefront iterations run */
   double device_ms;      /* device time of the render, CUDA events */
-  double stage_ms[8];    /* per kernel, TR_STAGE_* order (with TR_RENDER_TIME_STAGES) */
+  double stage_ms[9];    /* per kernel, TR_STAGE_* order (with TR_RENDER_TIME_STAGES) */
   uint64_t closest_boxes; /* with TR_RENDER_COUNT_VISITS: boxes tested by closest-hit rays */
   uint64_t closest_prims; /*   primitives tested by closest-hit rays */
   uint64_t any_boxes;     /*   boxes tested by shadow rays */

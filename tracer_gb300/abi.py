@@ -104,13 +104,13 @@ class TrRenderParams(C.Structure):
 TR_RENDER_TIME_STAGES = 1
 TR_RENDER_COUNT_VISITS = 2
 STAGE_NAMES = ["extend", "logic", "material_phong", "material_disney", "nee_phong", "nee_disney", "shadow",
-               "reset"]
+               "reset", "bin"]
 
 
 class TrStats(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("extend_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
                 ("shade_items", C.c_uint64), ("iterations", C.c_uint64), ("device_ms", C.c_double),
-                ("stage_ms", C.c_double * 8), ("closest_boxes", C.c_uint64), ("closest_prims", C.c_uint64),
+                ("stage_ms", C.c_double * 9), ("closest_boxes", C.c_uint64), ("closest_prims", C.c_uint64),
                 ("any_boxes", C.c_uint64), ("any_prims", C.c_uint64), ("guide_records", C.c_uint64),
                 ("occluder_hits", C.c_uint64)]
 

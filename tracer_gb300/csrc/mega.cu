@@ -513,10 +513,10 @@ unsigned mega_kernel_mask(const DScene& sc, bool has_disney12) {
   return has_disney12 ? kMaskPD : kMaskPhong;
 }
 
-cudaError_t launch_mega(const MegaLaunch& P, unsigned mask, int grid, cudaStream_t st) {
-  if (mask == kMaskPhong) k_mega<kMaskPhong><<<grid, kMegaThreads, 0, st>>>(P);
-  else if (mask == kMaskPD) k_mega<kMaskPD><<<grid, kMegaThreads, 0, st>>>(P);
-  else k_mega<kMaskAll><<<grid, kMegaThreads, 0, st>>>(P);
+cudaError_t launch_mega(const MegaLaunch& P, unsigned mask, int grid, int threads, cudaStream_t st) {
+  if (mask == kMaskPhong) k_mega<kMaskPhong><<<grid, threads, 0, st>>>(P);
+  else if (mask == kMaskPD) k_mega<kMaskPD><<<grid, threads, 0, st>>>(P);
+  else k_mega<kMaskAll><<<grid, threads, 0, st>>>(P);
   return cudaGetLastError();
 }
 

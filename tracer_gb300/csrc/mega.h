@@ -37,8 +37,8 @@ struct MegaLaunch {
 // The smallest instantiation covering a scene set (MK_* bits).
 unsigned mega_kernel_mask(const DScene& sc, bool has_disney12);
 // Launches the persistent kernel of instantiation `mask` (grid blocks of
-// kMegaThreads threads) on `st`.
-cudaError_t launch_mega(const MegaLaunch& P, unsigned mask, int grid, cudaStream_t st);
+// `threads` threads, at most kMegaThreads, a multiple of 32) on `st`.
+cudaError_t launch_mega(const MegaLaunch& P, unsigned mask, int grid, int threads, cudaStream_t st);
 // Resident blocks per SM of that instantiation.
 int mega_blocks_per_sm(unsigned mask);
 constexpr int kMegaThreads = 512;

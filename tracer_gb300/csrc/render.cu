@@ -1438,13 +1438,16 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   // kMegaAutoSlots pixels, which the wavefront's launches cannot fill the GPU with
   bool mega = false;
   unsigned mmask = 0;
-  int mgrid = 0;
+  int mgrid = 0, mthreads = kMegaThreads;
   if (!gp && !timed && !count && nl <= kMegaLights && ctx->tune.render_mode != TR_RENDER_MODE_WAVEFRONT) {
     mega = ctx->tune.render_mode == TR_RENDER_MODE_PERSISTENT || (long long)n <= kMegaAutoSlots;
     if (mega) {
       bool d12 = false;
       for (const DMat& m : ctx->hs.mats) d12 |= m.kind == MAT_DISNEY12;
       mmask = mega_kernel_mask(ctx->dsc, d12);
+      // full 512-thread blocks even when fewer than the SMs: spreading a
+      // 65k-pixel render over all 152 SMs in 448-thread blocks was slower
+      // (70.7 against 75.7 Msamples/s on the Cornell box)
       const long long want = ((long long)n + kMegaThreads - 1) / kMegaThreads;
       mgrid = (int)std::min<long long>(want, (long long)sms * mega_blocks_per_sm(mmask));
     }
@@ -1488,7 +1491,7 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
       le = cudaMemsetAsync(jd[k].film, 0, (size_t)jd[k].W * jd[k].H * (jd[k].fp64 ? 32 : 16), st);
     if (le == cudaSuccess) le = cudaMemsetAsync(P.ctr, 0, kCtrWords * 4, st);
     if (le == cudaSuccess) le = cudaMemsetAsync(P.stats, 0, kStatWords * 8, st);
-    if (le == cudaSuccess) le = launch_mega(M, mmask, mgrid, st);
+    if (le == cudaSuccess) le = launch_mega(M, mmask, mgrid, mthreads, st);
     if (use_graph) {
       const cudaError_t ce = cudaStreamEndCapture(st, &graph);
       if (le == cudaSuccess) le = ce;
@@ -1546,12 +1549,13 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   auto iteration = [&](int cur) -> tr_status {
     const int nxt = cur ^ 1;
     mark();
-    if (P.bin_bits) {  // the extend queue in ray-key order (counted with the extend stage)
+    if (P.bin_bits) {  // the extend queue in ray-key order
       cudaMemsetAsync(P.bin_cnt, 0, (size_t)bin_nb * 4, st);
       k_bin_count<<<grid, 128, 0, st>>>(ExtendSrc{P, cur}, P.sc, P.bin_cnt, P.bin_key, P.bin_bits);
       k_bin_scan<<<1, kBinScanThreads, 0, st>>>(P.bin_cnt, bin_nb);
       k_bin_scatter<<<grid, 128, 0, st>>>(ExtendSrc{P, cur}, P.bin_cnt, P.bin_key, P.q_srt);
     }
+    mark();
     if (count) k_extend<true><<<grid_ext, 128, tl_smem, st>>>(P, cur);
     else k_extend<false><<<grid_ext, 128, tl_smem, st>>>(P, cur);
     mark();
@@ -1661,13 +1665,13 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   RCHK(cudaMemcpy(hs, P.stats, sizeof(hs), cudaMemcpyDeviceToHost));
   unsigned int ctrs[kCtrWords];
   RCHK(cudaMemcpy(ctrs, P.ctr, sizeof(ctrs), cudaMemcpyDeviceToHost));
-  // event k of an iteration's 9 precedes kernel k; stage of each interval
-  static const int kStageOf[8] = {TR_STAGE_EXTEND,          TR_STAGE_RESET,     TR_STAGE_LOGIC,
-                                  TR_STAGE_MATERIAL_PHONG,  TR_STAGE_MATERIAL_DISNEY,
-                                  TR_STAGE_NEE_PHONG,       TR_STAGE_NEE_DISNEY, TR_STAGE_SHADOW};
+  // event k of an iteration's 10 precedes kernel group k; stage of each interval
+  static const int kStageOf[9] = {TR_STAGE_BIN,       TR_STAGE_EXTEND,          TR_STAGE_RESET,
+                                  TR_STAGE_LOGIC,     TR_STAGE_MATERIAL_PHONG,  TR_STAGE_MATERIAL_DISNEY,
+                                  TR_STAGE_NEE_PHONG, TR_STAGE_NEE_DISNEY,      TR_STAGE_SHADOW};
   double stage[TR_NUM_STAGES] = {};
-  for (size_t k = 0; k + 9 <= nev; k += 9)
-    for (int j = 0; j < 8; ++j) {
+  for (size_t k = 0; k + 10 <= nev; k += 10)
+    for (int j = 0; j < 9; ++j) {
       float a = 0.0f;
       cudaEventElapsedTime(&a, ev[k + j], ev[k + j + 1]);
       stage[kStageOf[j]] += a;
