@@ -472,7 +472,7 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
 // One Adam step on a batch is two launches: k_train and k_update.
 //
 // k_train does the batch's forward pass, loss and backward pass on the
-// tensor cores. CTAs (one per SM, 128 threads, all 512 TMEM columns) walk
+// tensor cores. CTAs (one per SM, 256 threads, all 512 TMEM columns) walk
 // 128-row tiles. A tile's rows are gathered from the record arrays; each
 // layer's input is kept in shared memory twice, as the forward MMA's A
 // operand and transposed (in_l^T) as the B operand of the weight-gradient
@@ -506,6 +506,8 @@ static_assert(kTSmemBytes <= 227 * 1024, "k_train shared memory");
 constexpr int kPartStride = kParams + 16;  // per-CTA partial: gradients, then weight sum and loss sum
 constexpr int kWsumParts = 128;            // blocks of k_wsum
 constexpr float kRowScale = 1.0f / 64.0f;
+constexpr int kTrainThreads = 256;         // k_train: two warps per TMEM lane quarter
+static_assert(kTRed + 8 * kTrainThreads / 32 <= kTMbar, "k_train reduction scratch");
 
 // The batch's row i: a record index drawn by a hash of (seed, i).
 __device__ __forceinline__ unsigned int batch_record(unsigned long long seed, unsigned int i, unsigned int count) {
@@ -549,13 +551,21 @@ __device__ __forceinline__ __half sat_half(float v) {
 // rec_in: count x 7, rec_dir: count x 3, rec_w: count. gather != 0: row i of
 // the batch is record batch_record(seed, i, count); else record i.
 // part: gridDim.x x kPartStride floats.
-__global__ void __launch_bounds__(128, 1)
+//
+// Eight warps: warp w reads TMEM lanes 32 (w % 4) .. + 31, so threads t and
+// t + 128 own the same tile row; in the epilogues of the hidden layers and of
+// the backward chain each of the two takes half of the row's 64 columns
+// (grp = w / 4). The loss epilogue, which needs a whole output row, runs on
+// the first four warps.
+__global__ void __launch_bounds__(kTrainThreads, 1)
     k_train(const uint8_t* __restrict__ img, const uint8_t* __restrict__ img_t, const float* __restrict__ rin,
             const float* __restrict__ rdir, const float* __restrict__ rw, unsigned int count, int n,
             unsigned long long seed, int gather, const float* __restrict__ scale, float* __restrict__ part,
             int* err) {
   extern __shared__ __align__(1024) uint8_t sm[];
   const int tid = threadIdx.x, warp = tid >> 5;
+  const int grp = warp >> 2;                         // column half of the epilogues
+  const int r = ((warp & 3) << 5) | (tid & 31);      // this thread's tile row (TMEM lane)
   for (int i = tid; i < (int)(kPackedBytes / 16); i += blockDim.x)
     reinterpret_cast<int4*>(sm)[i] = reinterpret_cast<const int4*>(img)[i];
   for (int i = tid; i < (int)(kWtBytes / 16); i += blockDim.x)
@@ -571,7 +581,7 @@ __global__ void __launch_bounds__(128, 1)
   __syncthreads();
   tc05::fence_after();
   const uint32_t tmem = *slot;
-  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+  const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
   const float* bias = reinterpret_cast<const float*>(sm + kBiasOff);
   uint8_t* A = sm + kTA;
   uint8_t* DzT = sm + kTDzT;
@@ -584,7 +594,7 @@ __global__ void __launch_bounds__(128, 1)
   int tiles_done = 0;
   const int ntiles = (n + kTile - 1) / kTile;
   for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-    const int i = t * kTile + tid;
+    const int i = t * kTile + r;
     const bool live = i < n;
     float x[kIn], om[3], w = 0.0f;
     {
@@ -595,17 +605,20 @@ __global__ void __launch_bounds__(128, 1)
       for (int k = 0; k < 3; ++k) om[k] = live ? rdir[(size_t)j * 3 + k] : 0.0f;
       if (live) w = rw[j];
     }
-    {  // layer 0's input: the A operand (zero-padded to 16) and in_0^T (ones row at 7 for the bias)
+    // layer 0's input: the A operand (zero-padded to 16; first four warps) and
+    // in_0^T (ones row at 7 for the bias; last four)
+    if (grp == 0) {
       __align__(16) __half h[16];
 #pragma unroll
       for (int k = 0; k < 16; ++k) h[k] = __float2half_rn(k < kIn ? x[k] : 0.0f);
-      *reinterpret_cast<int4*>(A + tc05::core_off(tid, 0, kInPad)) = *reinterpret_cast<const int4*>(h);
-      *reinterpret_cast<int4*>(A + tc05::core_off(tid, 8, kInPad)) = *reinterpret_cast<const int4*>(h + 8);
+      *reinterpret_cast<int4*>(A + tc05::core_off(r, 0, kInPad)) = *reinterpret_cast<const int4*>(h);
+      *reinterpret_cast<int4*>(A + tc05::core_off(r, 8, kInPad)) = *reinterpret_cast<const int4*>(h + 8);
+    } else {
 #pragma unroll
       for (int k = 0; k < 16; ++k)
-        st_half(sm + tin_off(0), tc05::core_off(k, tid, kTile), k < kIn ? x[k] : (k == kIn && live ? 1.0f : 0.0f));
+        st_half(sm + tin_off(0), tc05::core_off(k, r, kTile), k < kIn ? x[k] : (k == kIn && live ? 1.0f : 0.0f));
     }
-    uint32_t mask[4][2];  // ReLU masks of this row's hidden units (h > 0 in fp16)
+    uint32_t mask[4];  // ReLU masks (h > 0 in fp16) of this thread's 32 hidden units per layer
     tc05::fence_proxy_async();
     __syncthreads();
     // ---- forward
@@ -627,23 +640,25 @@ __global__ void __launch_bounds__(128, 1)
       tc05::fence_after();
       if (l < kLayers - 1) {
         uint8_t* inT = sm + tin_off(l + 1);
-        mask[l][0] = mask[l][1] = 0u;
+        uint32_t mk = 0u;
 #pragma unroll
-        for (int c0 = 0; c0 < kHid; c0 += 16) {
+        for (int hf = 0; hf < 2; ++hf) {
+          const int c0 = 32 * grp + 16 * hf;
           float v[16];
           tc05::tmem_ld16(tmem + lane_base + (uint32_t)c0, v);
           __align__(16) __half h[16];
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             h[j] = __float2half_rn(fmaxf(v[j] + bias[l * 64 + c0 + j], 0.0f));
-            if (__half2float(h[j]) > 0.0f) mask[l][c0 >> 5] |= 1u << ((c0 + j) & 31);
-            *reinterpret_cast<__half*>(inT + tc05::core_off(c0 + j, tid, kTile)) = h[j];
+            if (__half2float(h[j]) > 0.0f) mk |= 1u << (16 * hf + j);
+            *reinterpret_cast<__half*>(inT + tc05::core_off(c0 + j, r, kTile)) = h[j];
           }
-          *reinterpret_cast<int4*>(A + tc05::core_off(tid, c0, kHid)) = *reinterpret_cast<const int4*>(h);
-          *reinterpret_cast<int4*>(A + tc05::core_off(tid, c0 + 8, kHid)) = *reinterpret_cast<const int4*>(h + 8);
+          *reinterpret_cast<int4*>(A + tc05::core_off(r, c0, kHid)) = *reinterpret_cast<const int4*>(h);
+          *reinterpret_cast<int4*>(A + tc05::core_off(r, c0 + 8, kHid)) = *reinterpret_cast<const int4*>(h + 8);
         }
-        st_half(inT, tc05::core_off(kHid, tid, kTile), live ? 1.0f : 0.0f);
-      } else {
+        mask[l] = mk;
+        if (grp == 1) st_half(inT, tc05::core_off(kHid, r, kTile), live ? 1.0f : 0.0f);
+      } else if (grp == 0) {
         // loss and its gradient w.r.t. the outputs: dZ_4 into dZ (K = 48) and dZ^T
         float z[kOutPad];
 #pragma unroll
@@ -664,10 +679,10 @@ __global__ void __launch_bounds__(128, 1)
         }
 #pragma unroll
         for (int c = 0; c < kOutPad; ++c)
-          *reinterpret_cast<__half*>(A + tc05::core_off(tid, c, kOutPad)) = sat_half(c < kOut ? d[c] : 0.0f);
+          *reinterpret_cast<__half*>(A + tc05::core_off(r, c, kOutPad)) = sat_half(c < kOut ? d[c] : 0.0f);
 #pragma unroll
         for (int c = 0; c < kHid; ++c)
-          *reinterpret_cast<__half*>(DzT + tc05::core_off(c, tid, kTile)) = sat_half(c < kOut ? d[c] : 0.0f);
+          *reinterpret_cast<__half*>(DzT + tc05::core_off(c, r, kTile)) = sat_half(c < kOut ? d[c] : 0.0f);
       }
       tc05::fence_before();
       tc05::fence_proxy_async();
@@ -698,19 +713,20 @@ __global__ void __launch_bounds__(128, 1)
       phase ^= 1u;
       if (l == 0) break;
       tc05::fence_after();
+      const uint32_t mk = mask[l - 1];
 #pragma unroll
-      for (int c0 = 0; c0 < kHid; c0 += 16) {
+      for (int hf = 0; hf < 2; ++hf) {
+        const int c0 = 32 * grp + 16 * hf;
         float v[16];
         tc05::tmem_ld16(tmem + lane_base + (uint32_t)c0, v);
         __align__(16) __half h[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-          const int c = c0 + j;
-          h[j] = sat_half((mask[l - 1][c >> 5] >> (c & 31)) & 1u ? v[j] : 0.0f);
-          *reinterpret_cast<__half*>(DzT + tc05::core_off(c, tid, kTile)) = h[j];
+          h[j] = sat_half((mk >> (16 * hf + j)) & 1u ? v[j] : 0.0f);
+          *reinterpret_cast<__half*>(DzT + tc05::core_off(c0 + j, r, kTile)) = h[j];
         }
-        *reinterpret_cast<int4*>(A + tc05::core_off(tid, c0, kHid)) = *reinterpret_cast<const int4*>(h);
-        *reinterpret_cast<int4*>(A + tc05::core_off(tid, c0 + 8, kHid)) = *reinterpret_cast<const int4*>(h + 8);
+        *reinterpret_cast<int4*>(A + tc05::core_off(r, c0, kHid)) = *reinterpret_cast<const int4*>(h);
+        *reinterpret_cast<int4*>(A + tc05::core_off(r, c0 + 8, kHid)) = *reinterpret_cast<const int4*>(h + 8);
       }
       tc05::fence_before();
       tc05::fence_proxy_async();
@@ -724,13 +740,15 @@ __global__ void __launch_bounds__(128, 1)
   }
   __syncthreads();
   tc05::fence_after();
-  // this CTA's partial: weight gradients from TMEM lanes 0..63 (one output unit per lane)
+  // this CTA's partial: weight gradients from TMEM lanes 0..63 (one output
+  // unit per lane; warps 0, 1, 4, 5), the two column halves' 16-column
+  // chunks alternating
   float* mine = part + (size_t)blockIdx.x * kPartStride;
-  if (warp < 2) {
-    const int o = tid;
+  if ((warp & 3) < 2) {
+    const int o = r;
     for (int l = 0; l < kLayers; ++l) {
       const int N = bk_n(l), kin = layer_kin(l);
-      for (int c0 = 0; c0 < N; c0 += 16) {
+      for (int c0 = 16 * grp; c0 < N; c0 += 32) {
         float v[16];
         tc05::tmem_ld16(tmem + lane_base + bk_col(l) + (uint32_t)c0, v);
         if (o < layer_nout(l)) {
@@ -757,8 +775,13 @@ __global__ void __launch_bounds__(128, 1)
   tc05::fence_before();
   __syncthreads();
   if (tid == 0) {
-    mine[kParams] = (red[0] + red[2]) + (red[4] + red[6]);
-    mine[kParams + 1] = (red[1] + red[3]) + (red[5] + red[7]);
+    float ws = 0.0f, ls = 0.0f;
+    for (int k = 0; k < kTrainThreads / 32; ++k) {
+      ws += red[2 * k];
+      ls += red[2 * k + 1];
+    }
+    mine[kParams] = ws;
+    mine[kParams + 1] = ls;
   }
   if (warp == 0) {
     tc05::tmem_dealloc(tmem, 512);
@@ -928,7 +951,7 @@ static tr_status guide_fused_step(tr_ctx* ctx, const float* in, const float* dir
   if ((e = g->part.reserve((size_t)grid * mlp::kPartStride * 4)) != cudaSuccess)
     return cuda_fail(ctx, e, "guide gradient partials");
   const float* scale = g->scal.as<float>() + 2;
-  mlp::k_train<<<grid, 128, mlp::kTSmemBytes, ctx->stream>>>(g->img.as<uint8_t>(), g->img_t.as<uint8_t>(), in, dir, w,
+  mlp::k_train<<<grid, mlp::kTrainThreads, mlp::kTSmemBytes, ctx->stream>>>(g->img.as<uint8_t>(), g->img_t.as<uint8_t>(), in, dir, w,
                                                               count, n, seed, gather, scale, g->part.as<float>(),
                                                               ctx->d_err.as<int>() + 2);
   ++g->step;
