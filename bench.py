@@ -904,7 +904,8 @@ def run_ours(args):
                  "boxes_per_extend_ray": per.get("extend", (None, None))[0],
                  "prims_per_extend_ray": per.get("extend", (None, None))[1],
                  "boxes_per_shadow_ray": per.get("shadow", (None, None))[0],
-                 "prims_per_shadow_ray": per.get("shadow", (None, None))[1]},
+                 "prims_per_shadow_ray": per.get("shadow", (None, None))[1],
+                 "shadow_rays_answered_by_occluder_cache": staged.occluder_hits},
         "stage_ms": {k: round(v, 3) for k, v in stage_ms.items()},
         "clocks": clocks.summary(c0, c1),
     }

@@ -25,16 +25,22 @@ def _cases():
 
 
 @pytest.mark.parametrize("case", range(6))
-def test_occluder_cache_keeps_the_film(gpu, case):
+@pytest.mark.parametrize("mode", ["wavefront", "persistent"])
+def test_occluder_cache_keeps_the_film(gpu, case, mode):
+    """Both execution models: the wavefront's k_shadow (binary and four-wide
+    any-hit trees) and the persistent kernel's per-lane cache."""
     from conftest import tuned
+    from tracer_gb300.abi import TR_RENDER_MODE_PERSISTENT, TR_RENDER_MODE_WAVEFRONT
+    rm = TR_RENDER_MODE_WAVEFRONT if mode == "wavefront" else TR_RENDER_MODE_PERSISTENT
     name, (sc, cam, filt, par) = list(_cases())[case]
     gpu.upload(sc)
-    with tuned(gpu, occluder_cache=0):
+    with tuned(gpu, occluder_cache=0, render_mode=rm):
         off, st0 = gpu.render(cam, filt, par)
-    for width in (2, 4):
-        with tuned(gpu, occluder_cache=1, any_node_width=width):
+    for width in ((2, 4) if mode == "wavefront" else (2,)):
+        with tuned(gpu, occluder_cache=1, any_node_width=width, render_mode=rm):
             on, st1 = gpu.render(cam, filt, par)
-        print(f"{name} width {width}: shadow rays {st1.shadow_rays}, answered by the cache {st1.occluder_hits}")
+        assert (st1.iterations == 1) == (mode == "persistent")
+        print(f"{name} {mode} width {width}: shadow rays {st1.shadow_rays}, answered by the cache {st1.occluder_hits}")
         assert st0.occluder_hits == 0
         assert st1.shadow_rays == st0.shadow_rays
         assert np.array_equal(on.view(np.uint32), off.view(np.uint32))
