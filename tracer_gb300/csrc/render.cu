@@ -72,6 +72,7 @@ enum : int {  // counter slots
   C_FSH = 15,     // shadow kernel's work-fetch position
   C_TB = 16,      // guiding training records written (whole render)
   C_ERR = 17,     // traversal error word
+  C_ORD = 18,     // live slots written in slot order (this iteration)
 };
 constexpr int kCtrWords = 32;  // the counter array
 // Statistics words: samples, extend rays, shadow rays, shade items, visit
@@ -93,6 +94,7 @@ struct RenderBuffers {
   DevBuf jobs;                      // JobDev table of the current render
   DevBuf q_srt, bin_key, bin_cnt;   // ray binning: the reordered queue, keys, bin counts
   DevBuf OC;                        // occluder cache, one int per (slot, light)
+  DevBuf q_ord, act_flag;           // the live-slot list in slot order, per-slot marks
   unsigned int tb_count = 0, tb_cap = 0;  // training records of the last guided render
   unsigned int* h_active = nullptr;  // pinned: live-slot count per check
   std::vector<cudaEvent_t> ev_pool;  // reused by stage timing
@@ -127,6 +129,9 @@ struct Launch {
   // occluder cache (null: off): per (slot, light) item, the slot that last
   // blocked its shadow ray, or -1
   int* OC;
+  // the live-slot list in slot order (null: k_logic reads the list as appended)
+  int* q_ord;
+  unsigned char* act_flag;
   unsigned int* ctr;
   unsigned long long* stats;  // samples, extend rays, shadow rays, shade items, visit counts (4-7)
   // path guiding (alpha > 0: sample Lambertian continuations from the network's mixture;
@@ -533,13 +538,53 @@ __device__ __forceinline__ f3 continuation_emission(const Launch& P, int slot, f
   return pr.emission;
 }
 
+// Marks the slots of the live-slot list, which is in append order.
+__global__ void __launch_bounds__(256) k_act_mark(Launch P, int cur) {
+  const unsigned int n = P.ctr[C_ACT + cur];
+  for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    P.act_flag[P.q_act[cur][i]] = 1;
+}
+
+// The marked slots in slot order within each 256-slot range (the ranges in
+// the order their blocks reach the counter), marks cleared. k_logic then
+// reads the path state of consecutive slots together, and the queues it
+// fills, so the kernels after it, follow slot order too; the order of work
+// changes no result.
+__global__ void __launch_bounds__(256) k_act_order(Launch P) {
+  __shared__ unsigned int wsum[8];
+  __shared__ unsigned int base;
+  const int lane = (int)(threadIdx.x & 31u), warp = (int)(threadIdx.x >> 5);
+  for (unsigned int b0 = blockIdx.x * 256u; b0 < (unsigned int)P.nslots; b0 += gridDim.x * 256u) {
+    const unsigned int s = b0 + threadIdx.x;
+    const bool live = s < (unsigned int)P.nslots && P.act_flag[s];
+    const unsigned int m = __ballot_sync(0xffffffffu, live);
+    if (lane == 0) wsum[warp] = (unsigned int)__popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned int t = 0;
+      for (int w = 0; w < 8; ++w) {
+        const unsigned int c = wsum[w];
+        wsum[w] = t;
+        t += c;
+      }
+      base = t ? atomicAdd(P.ctr + C_ORD, t) : 0u;
+    }
+    __syncthreads();
+    if (live) {
+      P.q_ord[base + wsum[warp] + (unsigned int)__popc(m & ((1u << lane) - 1u))] = (int)s;
+      P.act_flag[s] = 0;
+    }
+    __syncthreads();
+  }
+}
+
 __global__ void __launch_bounds__(128) k_logic(Launch P, int cur) {
   const int nxt = cur ^ 1;
   const unsigned int n = P.ctr[C_ACT + cur];
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.stats + 3, (unsigned long long)n);
   unsigned int finished = 0;
   for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int slot = P.q_act[cur][i];
+    const int slot = P.q_ord ? P.q_ord[i] : P.q_act[cur][i];
     const float4 p0 = P.P0[slot], p3 = P.P3[slot];
     const int flags = __float_as_int(p0.w);
     f3 L = mk3(p3.x, p3.y, p3.z);
@@ -1155,7 +1200,8 @@ void release_render(tr_ctx* ctx) {
   for (DevBuf* b : {&rb->P0, &rb->P1, &rb->P2, &rb->P3, &rb->P4, &rb->rng, &rb->M0, &rb->M1, &rb->M2, &rb->HC,
                     &rb->HM, &rb->SC, &rb->NU, &rb->SH, &rb->acc, &rb->q_ext, &rb->q_act, &rb->q_mat, &rb->q_nee,
                     &rb->q_sh, &rb->ctr, &rb->stats, &rb->VR, &rb->NV, &rb->gfeat, &rb->gout, &rb->tb, &rb->jobs,
-                    &rb->GX, &rb->MT, &rb->q_srt, &rb->bin_key, &rb->bin_cnt, &rb->OC})
+                    &rb->GX, &rb->MT, &rb->q_srt, &rb->bin_key, &rb->bin_cnt, &rb->OC, &rb->q_ord,
+                    &rb->act_flag})
     b->release();
   if (rb->h_active) cudaFreeHost(rb->h_active);
   for (cudaEvent_t e : rb->ev_pool) cudaEventDestroy(e);
@@ -1335,6 +1381,13 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   P.q_sh = rb->q_sh.as<int>();
   P.ctr = rb->ctr.as<unsigned int>();
   P.stats = rb->stats.as<unsigned long long>();
+  {
+    cudaError_t e;
+    if ((e = rb->q_ord.reserve((size_t)n * 4)) != cudaSuccess || (e = rb->act_flag.reserve((size_t)n)) != cudaSuccess)
+      return cuda_fail(ctx, e, "ordered live-slot list");
+    P.q_ord = rb->q_ord.as<int>();
+    P.act_flag = rb->act_flag.as<unsigned char>();
+  }
   P.OC = nullptr;
   if (ctx->tune.occluder_cache && ctx->dsc.slot_leaf && !(flags & TR_RENDER_COUNT_VISITS)) {
     // (a counting render keeps the reference's walks: its visit counts are the oracle's)
@@ -1529,6 +1582,7 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   RCHK(cudaMemsetAsync(P.ctr, 0, kCtrWords * 4, st));
   RCHK(cudaMemsetAsync(P.stats, 0, kStatWords * 8, st));
   if (P.OC) RCHK(cudaMemsetAsync(P.OC, 0xff, (size_t)n * P.nl_max * 4, st));
+  if (P.act_flag) RCHK(cudaMemsetAsync(P.act_flag, 0, (size_t)n, st));
   RCHK(cudaEventRecord(e0, st));
   k_init<<<grid_init, 256, 0, st>>>(P);
   RCHK(cudaGetLastError());
@@ -1565,6 +1619,11 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     cudaMemsetAsync(P.ctr + C_ACT + nxt, 0, 4, st);
     cudaMemsetAsync(P.ctr + C_SH, 0, 4 * (C_FSH + 1 - C_SH), st);  // C_SH, C_MAT, C_NEE, C_FEXT, C_FSH
     mark();
+    if (P.q_ord) {  // the live slots in slot order (timed with k_logic)
+      cudaMemsetAsync(P.ctr + C_ORD, 0, 4, st);
+      k_act_mark<<<grid, 256, 0, st>>>(P, cur);
+      k_act_order<<<grid_init, 256, 0, st>>>(P);
+    }
     k_logic<<<grid, 128, 0, st>>>(P, cur);
     if (P.guide_alpha > 0.0f) {
       // decoded mixtures for this iteration's Phong-material vertices (inputs written by k_logic)
