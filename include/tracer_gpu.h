@@ -254,7 +254,8 @@ tr_status tr_synchronize(tr_ctx* ctx);
 
 /* Launch tuning of a context. Replaces PTRendererParams::worker_count and
  * task_tile_size, the reference's only performance knobs
- * (src/factory/renderer.hpp:13-14); results never depend on it.
+ * (src/factory/renderer.hpp:13-14); results never depend on it. A new
+ * context starts at {20, 0, 32, 8, 2, 3, 0, 1, TR_RENDER_MODE_AUTO, 1}.
  *  - trav_refill_lanes (1..32): a traversal warp refills its finished lanes
  *    once fewer than this many lanes still trace;
  *  - trav_blocks_per_sm: resident 128-thread blocks per SM of the
@@ -295,7 +296,13 @@ tr_status tr_synchronize(tr_ctx* ctx);
  *    graph_iterations > 0); TR_RENDER_MODE_AUTO picks the persistent kernel
  *    for renders of at most 2^17 pixels. Guided and instrumented renders
  *    (TR_RENDER_TIME_STAGES, TR_RENDER_COUNT_VISITS) and scenes with more
- *    than 16 lights always use the wavefront. Films are identical. */
+ *    than 16 lights always use the wavefront. Films are identical.
+ *  - any_hit_order: the child a binary any-hit walk enters first when both
+ *    children's boxes pass: 0 the reference's near child, 1 the far child
+ *    (the default: a shadow ray's occluder tends to lie toward the light,
+ *    behind whatever surrounds its origin), 2 the child with the larger box
+ *    surface. An occlusion answer does not depend on the order; the visits
+ *    do. */
 typedef struct tr_tuning {
   int32_t trav_refill_lanes;
   int32_t trav_blocks_per_sm;
@@ -306,6 +313,7 @@ typedef struct tr_tuning {
   int32_t treelet_nodes;
   int32_t occluder_cache;
   int32_t render_mode;
+  int32_t any_hit_order;
 } tr_tuning;
 enum { TR_RENDER_MODE_AUTO = 0, TR_RENDER_MODE_WAVEFRONT = 1, TR_RENDER_MODE_PERSISTENT = 2 };
 tr_status tr_ctx_set_tuning(tr_ctx* ctx, const tr_tuning* t);

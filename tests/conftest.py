@@ -26,7 +26,7 @@ class tuned:
     changed, restored afterwards (the `gpu` fixture is shared)."""
 
     FIELDS = ("trav_refill_lanes", "trav_blocks_per_sm", "shade_blocks_per_sm", "graph_iterations", "any_node_width",
-              "ray_bin_bits", "treelet_nodes", "occluder_cache", "render_mode")
+              "ray_bin_bits", "treelet_nodes", "occluder_cache", "render_mode", "any_hit_order")
 
     def __init__(self, gpu, **fields):
         self.gpu, self.fields = gpu, fields
@@ -42,4 +42,4 @@ class tuned:
     def _apply(self, v):
         self.gpu.set_tuning(v["trav_refill_lanes"], v["trav_blocks_per_sm"], v["shade_blocks_per_sm"],
                             v["graph_iterations"], v["any_node_width"], v["ray_bin_bits"], v["treelet_nodes"],
-                            v["occluder_cache"], v["render_mode"])
+                            v["occluder_cache"], v["render_mode"], v["any_hit_order"])

@@ -91,7 +91,7 @@ def test_status_strings():
 
 def test_tuning_struct_layout():
     from tracer_gb300.abi import TrTuning
-    assert ctypes.sizeof(TrTuning) == 36
+    assert ctypes.sizeof(TrTuning) == 40
 
 
 def test_guide_kappa_range_matches_header():

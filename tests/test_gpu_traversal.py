@@ -226,3 +226,33 @@ def test_binning_and_treelet_keep_results(gpu, bits, treelet):
                     p1, t1 = gpu.trace_closest(rays)
                     assert np.array_equal(p0, p1) and _same_bits(t0, t1)
                     assert np.array_equal(h0, gpu.trace_any(srays))
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_any_hit_order_keeps_results(gpu, order):
+    """tr_tuning.any_hit_order: a binary any-hit walk enters the far child,
+    or the child with the larger box, first. Occlusion answers equal the
+    oracle's (the reference's near-first walk) on random scenes with spheres,
+    the traversal workload and the occluded room, and a wavefront render of
+    the room is bit-identical."""
+    from conftest import tuned
+    from tracer_gb300.abi import TR_RENDER_MODE_WAVEFRONT
+    rng = np.random.default_rng(40 + order)
+    room = scenes.occluded_room(32, 24, 1, n_tris=30000)[0]
+    o = rng.uniform([-3.9, 0.1, -2.9], [3.9, 3.9, 2.9], (20000, 3)).astype(np.float32)
+    tgt = rng.uniform([4.5, 0.5, -1.5], [7.5, 3.5, 1.5], (20000, 3)).astype(np.float32)
+    cases = [(scenes.random_scene(order, n_tris=300, n_spheres=20), _random_rays(rng, 20000, shadow=True)),
+             (scenes.traversal(1 << 15, seed=3), scenes.traversal_rays(1 << 15, seed=3, shadow=True)),
+             (room, scenes.make_rays(o, tgt - o, 0.0, np.linalg.norm(tgt - o, axis=1).astype(np.float32) * 0.999))]
+    for sc, srays in cases:
+        want = oracle.Oracle(sc, "port").trace_any(srays)
+        gpu.upload(sc)
+        with tuned(gpu, any_hit_order=order, any_node_width=2):
+            assert np.array_equal(gpu.trace_any(srays), want)
+    sc, cam, filt, par = scenes.occluded_room(48, 36, 4, n_tris=20000)
+    gpu.upload(sc)
+    with tuned(gpu, render_mode=TR_RENDER_MODE_WAVEFRONT):
+        base, _ = gpu.render(cam, filt, par)
+        with tuned(gpu, any_hit_order=order):
+            got, _ = gpu.render(cam, filt, par)
+    assert np.array_equal(got.view(np.uint32), base.view(np.uint32))

@@ -127,7 +127,7 @@ class TrTuning(C.Structure):
     _fields_ = [("trav_refill_lanes", C.c_int32), ("trav_blocks_per_sm", C.c_int32),
                 ("shade_blocks_per_sm", C.c_int32), ("graph_iterations", C.c_int32),
                 ("any_node_width", C.c_int32), ("ray_bin_bits", C.c_int32), ("treelet_nodes", C.c_int32),
-                ("occluder_cache", C.c_int32), ("render_mode", C.c_int32)]
+                ("occluder_cache", C.c_int32), ("render_mode", C.c_int32), ("any_hit_order", C.c_int32)]
 
 
 class TrBatchJob(C.Structure):

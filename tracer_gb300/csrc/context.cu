@@ -273,6 +273,7 @@ tr_status upload_device_tables(tr_ctx* ctx) {
   sc.roots = ctx->d_roots.as<SceneRoot>();
   sc.num_scenes = (int)nsc;
   sc.max_lights = max_lights;
+  sc.any_order = ctx->tune.any_hit_order;
   sc.has_glass = 0;
   sc.has_metal = 0;
   sc.has_disney15 = 0;
@@ -650,10 +651,11 @@ tr_status tr_ctx_set_tuning(tr_ctx* ctx, const tr_tuning* t) {
       t->graph_iterations < 0 || t->graph_iterations > 64 || (t->any_node_width != 2 && t->any_node_width != 4) ||
       t->ray_bin_bits < 0 || t->ray_bin_bits > kBinBitsMax || t->treelet_nodes < 0 || t->treelet_nodes > kTreeletMax ||
       (t->occluder_cache != 0 && t->occluder_cache != 1) || t->render_mode < TR_RENDER_MODE_AUTO ||
-      t->render_mode > TR_RENDER_MODE_PERSISTENT)
+      t->render_mode > TR_RENDER_MODE_PERSISTENT || t->any_hit_order < 0 || t->any_hit_order > 2)
     return set_err(ctx, TR_ERR_ARG, "tuning out of range");
   const bool restage = t->treelet_nodes != ctx->tune.treelet_nodes;
   ctx->tune = *t;
+  ctx->dsc.any_order = t->any_hit_order;
   if (restage && ctx->has_scene) {
     TR_DEVICE_SCOPE(ctx);
     return upload_treelet(ctx);

@@ -100,7 +100,7 @@ struct tr_ctx {
   trg::DevBuf d_perm, d_bin_key, d_bin_cnt;  // ray binning of tr_trace_*: order, keys, bin counts
   std::atomic<int> cancel{0};
   trg::RenderBuffers* rb = nullptr;
-  tr_tuning tune{20, 0, 16, 8, 2, 3, 0, 1, TR_RENDER_MODE_AUTO};
+  tr_tuning tune{20, 0, 32, 8, 2, 3, 0, 1, TR_RENDER_MODE_AUTO, 1};
   int bvh_builder = TR_BVH_REFERENCE;
   size_t any4_nodes = 0;  // four-wide any-hit tree of the uploaded set (0: not available)
   int any4_stack = 0;     // its traversal stack bound

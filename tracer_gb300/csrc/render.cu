@@ -2061,7 +2061,7 @@ extern "C" tr_status tr_autotune(tr_ctx* ctx, const tr_batch_job* jobs, uint32_t
   // coordinate descent over the discrete settings, the execution model first
   static const int kMode[] = {TR_RENDER_MODE_WAVEFRONT, TR_RENDER_MODE_PERSISTENT}, kBlocks[] = {0, 4, 6, 8},
                    kRefill[] = {12, 20, 28}, kShade[] = {8, 16, 32}, kGraph[] = {0, 4, 8, 16}, kWidth[] = {2, 4},
-                   kBins[] = {0, 3, 4}, kTreelet[] = {0, 64, 256}, kCache[] = {0, 1};
+                   kBins[] = {0, 3, 4}, kTreelet[] = {0, 64, 256}, kCache[] = {0, 1}, kOrder[] = {0, 1, 2};
   struct Dim {
     int32_t tr_tuning::*field;
     const int* vals;
@@ -2071,7 +2071,7 @@ extern "C" tr_status tr_autotune(tr_ctx* ctx, const tr_batch_job* jobs, uint32_t
                               {&tr_tuning::trav_refill_lanes, kRefill, 3}, {&tr_tuning::shade_blocks_per_sm, kShade, 3},
                               {&tr_tuning::graph_iterations, kGraph, 4},   {&tr_tuning::any_node_width, kWidth, 2},
                               {&tr_tuning::ray_bin_bits, kBins, 3},        {&tr_tuning::treelet_nodes, kTreelet, 3},
-                              {&tr_tuning::occluder_cache, kCache, 2}};
+                              {&tr_tuning::occluder_cache, kCache, 2},    {&tr_tuning::any_hit_order, kOrder, 3}};
   tr_tuning cur = ctx->tune;
   double cur_ms = 0.0;
   tr_status s = time_once(cur, cur_ms);

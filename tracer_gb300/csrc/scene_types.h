@@ -229,6 +229,9 @@ struct DScene {
   // The materials' factory arguments and maps, by material index (only for
   // sets with image maps; null otherwise)
   const tr_material* msrc;
+  // Binary any-hit walks: the child entered first when both pass
+  // (tr_tuning.any_hit_order: 0 near, 1 far, 2 larger box surface).
+  int any_order;
 };
 
 }  // namespace trg

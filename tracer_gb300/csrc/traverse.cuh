@@ -318,7 +318,18 @@ struct TravLane {
     const bool hl = box_pass(a.x, a.y, a.z, a.w, b.x, b.y, o, inv, n0, n1, n2, tl) && tl < t_max;
     const bool hr = box_pass(b.z, b.w, c.x, c.y, c.z, c.w, o, inv, n0, n1, n2, tr) && tr < t_max;
     const int axis = __float_as_int(dd.w);
-    const bool second_near = axis == 0 ? n0 : (axis == 1 ? n1 : n2);
+    bool second_near = axis == 0 ? n0 : (axis == 1 ? n1 : n2);
+    if (ANY && !COUNT && sc.any_order != 0) {
+      // any hit: the answer does not depend on the order, only the visits do
+      // (the counting walk keeps the reference's visits)
+      if (sc.any_order == 1) {
+        second_near = !second_near;  // the far child first
+      } else {  // the child with the larger box surface first
+        const float lx = a.w - a.x, ly = b.x - a.y, lz = b.y - a.z;
+        const float rx = c.y - b.z, ry = c.z - b.w, rz = c.w - c.x;
+        second_near = rx * ry + ry * rz + rz * rx > lx * ly + ly * lz + lz * lx;
+      }
+    }
     const int lref = __float_as_int(dd.x), rref = __float_as_int(dd.y);
     const unsigned cc = (unsigned)__float_as_int(dd.z);
     const int lcnt = (int)(cc & 0xffffu), rcnt = (int)(cc >> 16);

@@ -231,8 +231,10 @@ class GpuContext:
                    shade_blocks_per_sm: int | None = None, graph_iterations: int | None = None,
                    any_node_width: int | None = None, ray_bin_bits: int | None = None,
                    treelet_nodes: int | None = None, occluder_cache: int | None = None,
-                   render_mode: int | None = None) -> None:
+                   render_mode: int | None = None, any_hit_order: int | None = None) -> None:
         t = self.tuning()
+        if any_hit_order is not None:
+            t.any_hit_order = any_hit_order
         if render_mode is not None:
             t.render_mode = render_mode
         if occluder_cache is not None:
