@@ -360,3 +360,31 @@ def test_converged_fp64_image_within_one_percent(gpu, maker):
     assert mre < noise
     assert bmre < 0.01
     assert abs(a.mean() - b.mean()) <= 0.005 * b.mean()
+
+
+@pytest.mark.parametrize("case", ["room", "cornell", "disney_grid", "metal_glass", "textured"])
+def test_mis_rays_that_reach_no_light_are_not_traced(gpu, case):
+    """An MIS BSDF ray contributes only when its closest hit is an area light
+    (or it escapes into an environment light): one that hits none of the
+    scene's emissive triangles under the traversal's own triangle test is
+    not traced. The film equals, bit for bit, a visit-counting render's,
+    which traces every MIS ray with the reference's walk; fewer rays are
+    traced."""
+    from tracer_gb300.abi import TR_RENDER_COUNT_VISITS, TrRenderParams
+    sc, cam, filt, par = {
+        "room": lambda: scenes.occluded_room(48, 36, 4, n_tris=20000),
+        "cornell": lambda: scenes.cornell(48, 48, 4),
+        "disney_grid": lambda: scenes.disney_grid(48, 48, 2),
+        "metal_glass": lambda: scenes.cornell(40, 40, 4, max_depth=8, min_depth=2, glass=True, metal=True),
+        "textured": lambda: scenes.cornell(40, 40, 4, textured=True)}[case]()
+    gpu.upload(sc)
+    from conftest import tuned
+    from tracer_gb300.abi import TR_RENDER_MODE_WAVEFRONT
+    with tuned(gpu, render_mode=TR_RENDER_MODE_WAVEFRONT):
+        got, st = gpu.render(cam, filt, par)
+    allp = TrRenderParams.from_buffer_copy(par)
+    allp.flags = TR_RENDER_COUNT_VISITS
+    want, st_all = gpu.render(cam, filt, allp)
+    print(f"{case}: extension rays traced {st.extend_rays} of {st_all.extend_rays}")
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    assert st.extend_rays < st_all.extend_rays

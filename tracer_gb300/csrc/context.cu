@@ -292,6 +292,30 @@ tr_status upload_device_tables(tr_ctx* ctx) {
   return TR_OK;
 }
 
+// A sphere around an area-light triangle as the triangle test sees it (A,
+// A + AB, A + AC, in double), widened by 1e-3 of its radius and of the
+// coordinates' scale: every point that test accepts lies well inside.
+static void light_sphere(DLight& L) {
+  const double A[3] = {L.A.x, L.A.y, L.A.z}, AB[3] = {L.AB.x, L.AB.y, L.AB.z}, AC[3] = {L.AC.x, L.AC.y, L.AC.z};
+  double c[3], scale = 1.0, r2 = 0.0;
+  for (int k = 0; k < 3; ++k) c[k] = A[k] + (AB[k] + AC[k]) / 3.0;
+  float cf[3];
+  for (int k = 0; k < 3; ++k) cf[k] = (float)c[k];
+  for (int v = 0; v < 3; ++v) {
+    double d2 = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      const double p = A[k] + (v == 1 ? AB[k] : v == 2 ? AC[k] : 0.0);
+      scale = std::max(scale, std::fabs(p));
+      const double e = p - (double)cf[k];
+      d2 += e * e;
+    }
+    r2 = std::max(r2, d2);
+  }
+  for (int k = 0; k < 3; ++k) L.bs[k] = cf[k];
+  L.bs[3] = (float)(std::sqrt(r2) * (1.0 + 1e-3) + 1e-3 * scale);
+  L.bs_cn = (float)std::sqrt((double)cf[0] * cf[0] + (double)cf[1] * cf[1] + (double)cf[2] * cf[2]);
+}
+
 tr_status upload_treelet(tr_ctx* ctx) {
   DScene& sc = ctx->dsc;
   sc.treelet = nullptr;
@@ -857,6 +881,9 @@ static tr_status build_host_scene(tr_ctx* ctx, const tr_scene_desc* d, HostScene
                fabsf(L.C.y) + fabsf(L.C.z) + 1.0f;
     L.prim = p;
     L.env = -1;
+    L.AB = hs.AB[pr.shape];
+    L.AC = hs.AC[pr.shape];
+    light_sphere(L);
     hs.lights.push_back(L);
   }
   if (d->env_texels || d->env_texels8) {

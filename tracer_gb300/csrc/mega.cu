@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(kMegaThreads, 1) k_mega(MegaLaunch P) {
 
     __syncthreads();
     // ---- vertex (k_logic, then k_material / k_glass)
-    bool vertex = false, term = false, mis = false;
+    bool vertex = false, term = false, mis = false, mis_trace = false;
     int kind = 0, mcode = 0;
     Isect is;
     f3 coef_prev = mk3(0.0f, 0.0f, 0.0f);
@@ -326,6 +326,7 @@ __global__ void __launch_bounds__(kMegaThreads, 1) k_mega(MegaLaunch P) {
                 mcos = abs_cos(is.g.z, md);
                 mf = ms.f;
                 mis = true;
+                mis_trace = mis_may_hit_light(sc, J, mo, md);
               }
               coef_prev = p.coef;
               p.coef = mulc(p.coef, divs(muls(bs.f, abs_cos(is.g.z, bs.wi)), bs.pdf));
@@ -444,10 +445,14 @@ __global__ void __launch_bounds__(kMegaThreads, 1) k_mega(MegaLaunch P) {
     // ---- mis: the BSDF-sampled ray's emission, weighted against the light
     //      (mis_contribution of render.cu, direct_illumination.cpp:144-198)
     if (__any_sync(kFull, mis)) {
-      const Traced mh = warp_trace<false>(sc, mis, mis ? p.J->scene : 0, mo, md, 0.0f, kRealMax, P.err);
-      n_ext += mis;
+      // a ray that can reach no light is not traced: its closest hit would give zero
+      Traced mh;
+      mh.h.prim = -1;
+      if (__any_sync(kFull, mis_trace))
+        mh = warp_trace<false>(sc, mis_trace, mis_trace ? p.J->scene : 0, mo, md, 0.0f, kRealMax, P.err);
+      n_ext += mis_trace;
       if (mis) {
-        const int pid = mh.h.prim;
+        const int pid = mis_trace ? mh.h.prim : -1;
         f3 c = mk3(0.0f, 0.0f, 0.0f);
         if (pid < 0) {
           const int ei = p.J->env;

@@ -131,6 +131,7 @@ struct Launch {
   int* OC;
   // the live-slot list in slot order (null: k_logic reads the list as appended)
   int* q_ord;
+  int mis_all;  // trace every MIS ray (visit-counting renders match the oracle's queries)
   unsigned char* act_flag;
   unsigned int* ctr;
   unsigned long long* stats;  // samples, extend rays, shadow rays, shade items, visit counts (4-7)
@@ -895,7 +896,10 @@ __global__ void __launch_bounds__(128, KIND == MAT_DISNEY12 ? 8 : 5) k_material(
         P.M0[slot] = make_float4(mo.x, mo.y, mo.z, ms.pdf);
         P.M1[slot] = make_float4(md.x, md.y, md.z, abs_cos(is.g.z, md));
         P.M2[slot] = make_float4(ms.f.x, ms.f.y, ms.f.z, 0.0f);
-        P.q_ext[nxt][append(P.ctr + C_EXT + nxt)] = 2 * slot + 1;
+        if (P.mis_all || mis_may_hit_light(P.sc, J, mo, md))
+          P.q_ext[nxt][append(P.ctr + C_EXT + nxt)] = 2 * slot + 1;
+        else
+          P.HM[slot] = make_float4(__int_as_float(-1), 0.0f, 0.0f, 0.0f);  // the zero of a miss
         flags |= F_MIS;
       }
     }
@@ -1300,6 +1304,38 @@ static JobDev make_job_dev(tr_ctx* ctx, const JobSpec& j, int slot_base, void* f
   J.light_base = (int)ctx->hs.scene_light[j.scene];
   J.nl = (int)ctx->hs.scene_nlight[j.scene];
   J.env = J.nl > 0 ? ctx->hs.lights[J.light_base + J.nl - 1].env : -1;
+  // the sphere of mis_may_hit_light: around the box of the area-light
+  // triangles as the triangle test sees them (A, A + AB, A + AC), widened
+  // by 1e-3 of the radius and of the coordinates' scale
+  {
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300}, scale = 1.0;
+    int tris = 0;
+    for (int l = 0; l < J.nl; ++l) {
+      const DLight& L = ctx->hs.lights[J.light_base + l];
+      if (L.env >= 0) continue;
+      const double A[3] = {L.A.x, L.A.y, L.A.z}, AB[3] = {L.AB.x, L.AB.y, L.AB.z}, AC[3] = {L.AC.x, L.AC.y, L.AC.z};
+      for (int k = 0; k < 3; ++k)
+        for (double v : {A[k], A[k] + AB[k], A[k] + AC[k]}) {
+          lo[k] = std::min(lo[k], v);
+          hi[k] = std::max(hi[k], v);
+          scale = std::max(scale, std::fabs(v));
+        }
+      ++tris;
+    }
+    if (tris) {
+      double r2 = 0.0;
+      for (int k = 0; k < 3; ++k) {
+        J.lsph[k] = (float)(0.5 * (lo[k] + hi[k]));
+        const double e = 0.5 * (hi[k] - lo[k]) + std::fabs(0.5 * (lo[k] + hi[k]) - (double)J.lsph[k]);
+        r2 += e * e;
+      }
+      J.lsph[3] = (float)(std::sqrt(r2) * (1.0 + 1e-3) + 1e-3 * scale);
+      J.lsph_cn = (float)std::sqrt((double)J.lsph[0] * J.lsph[0] + (double)J.lsph[1] * J.lsph[1] +
+                                   (double)J.lsph[2] * J.lsph[2]);
+    } else {
+      J.lsph[3] = -1.0f;
+    }
+  }
   J.filter_radius = j.filter.radius;
   J.filter_alpha = j.filter.alpha;
   J.filter_exp = std::exp(-j.filter.alpha * j.filter.radius * j.filter.radius);  // GaussianFilter ctor
@@ -1351,6 +1387,7 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   P.jobs = rb->jobs.as<JobDev>();
   P.njobs = njobs;
   P.nslots = n;
+  P.mis_all = (flags & TR_RENDER_COUNT_VISITS) != 0;
   P.nl_max = std::max(nl, 1);
   P.P0 = rb->P0.as<float4>();
   P.P1 = rb->P1.as<float4>();

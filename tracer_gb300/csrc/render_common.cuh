@@ -4,6 +4,7 @@
 #pragma once
 
 #include "shade.cuh"
+#include "traverse.cuh"
 
 namespace trg {
 
@@ -27,6 +28,8 @@ struct JobDev {
   int scene, slot_base;
   int light_base, nl;  // the scene's lights in DScene::lights
   int env;             // the scene's environment light in DScene::envs (its last light), or -1
+  float lsph[4];       // a sphere around the scene's area-light triangles with a margin (radius < 0: none)
+  float lsph_cn;       // |centre|
   float filter_radius, filter_alpha, filter_exp;
   int fp64;
   float4* film;  // film sums (float4 per pixel, or 2 x double2)
@@ -97,6 +100,58 @@ __device__ __forceinline__ void film_add(const JobDev& J, int slot, float px, fl
         atomicAdd(a + 3, fw);
       }
     }
+}
+
+// Lights of a job tested before its MIS rays are traced (more: always traced).
+constexpr int kMisLightTests = 32;
+
+// Whether the MIS BSDF ray of a vertex (sample_bsdf,
+// src/renderer/direct_illumination.cpp:144-198) can contribute, before it is
+// traced. It contributes only when it leaves a scene with an environment
+// light, or when its closest hit is an area light. That closest hit is a
+// primitive the triangle test hits -- the walk tests the same slot data with
+// the same arithmetic, and its culling only removes candidates -- so a ray
+// that hits none of the job's emissive triangles, in a scene without an
+// environment light, contributes the zero its traced closest hit would give,
+// and is not traced.
+// Whether a ray (d of unit length) may pass through a sphere (centre s, radius
+// s[3], |centre| cn). The spheres hold every point the triangle test can
+// accept with a margin far above that test's rounding; a false answer needs
+// the ray to pass outside, or move away, by more than this test's own
+// rounding (1e-5 of the distances).
+__device__ __forceinline__ bool ray_may_pass(const float* s, float cn, f3 o, f3 d, float on) {
+  const f3 v = mk3(s[0] - o.x, s[1] - o.y, s[2] - o.z);
+  const float r = s[3] + 1e-5f * (on + cn);
+  const float vv = dot(v, v), tca = dot(v, d);
+  if (tca < 0.0f && vv > r * r) return false;
+  const f3 w = v - scale(d, tca);
+  return dot(w, w) <= r * r;
+}
+
+// The traversal's triangle test on an area light (out of line: it is rarely
+// reached, and inlined it would weigh on the instruction cache of every
+// shading kernel).
+static __device__ __noinline__ bool light_tri_hit(const DLight& lt, f3 o, f3 d) {
+  float t, a, b;
+  return tri_test(make_float4(lt.A.x, lt.A.y, lt.A.z, 0.0f), make_float4(lt.AB.x, lt.AB.y, lt.AB.z, 0.0f),
+                  make_float4(lt.AC.x, lt.AC.y, lt.AC.z, 0.0f), o, d, 0.0f, kRealMax, t, a, b);
+}
+
+__device__ __forceinline__ bool mis_may_hit_light(const DScene& sc, const JobDev& J, f3 o, f3 d) {
+  if (J.env >= 0 || J.nl > kMisLightTests) return true;
+  if (J.lsph[3] < 0.0f) return false;
+  const float on = sqrtf(dot(o, o));
+  if (!ray_may_pass(J.lsph, J.lsph_cn, o, d, on)) return false;  // all lights
+  for (int l = 0; l < J.nl; ++l) {
+    const DLight& lt = sc.lights[J.light_base + l];
+    // an area light emits on its front side only: a hit on its back gives the
+    // zero that light_emit gives there (the contribution's own test, the same
+    // normal and direction)
+    if (!(dot(lt.gz, -d) > 0.0f)) continue;
+    if (!ray_may_pass(lt.bs, lt.bs_cn, o, d, on)) continue;
+    if (light_tri_hit(lt, o, d)) return true;
+  }
+  return false;
 }
 
 }  // namespace trg

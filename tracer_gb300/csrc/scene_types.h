@@ -167,6 +167,9 @@ struct DLight {
   int prim;
   float extent;   // sum of |coordinates| of A, B, C plus 1 (scale of the back-side margin)
   int env;        // >= 0: the environment light DScene::envs[env] (prim is -1), else -1
+  f3 AB, AC;      // the triangle's edges as its traversal slot holds them (B - A, C - A)
+  float bs[4];    // a sphere around the triangle with a margin (centre, radius)
+  float bs_cn;    // |centre|
 };
 
 // Environment light of one scene: the reference's IBL over an HDR texture
