@@ -176,7 +176,7 @@ def convergence(ctx, name: str, size=(1024, 768), ref_spp=4096, pass_spp=8, max_
         film = torch.zeros((H, W, 4), dtype=torch.float64, device=f"cuda:{torch.cuda.current_device()}")
         acc = np.zeros((H, W, 4), np.float64)
         spent, curve, reached, losses = 0.0, [], None, []
-        train_s = 0.0
+        train_s = light_s = render_s = 0.0
         use_alpha = 0.0
         if guided:
             ctx.guide_init(seed=0)
@@ -189,7 +189,10 @@ def convergence(ctx, name: str, size=(1024, 768), ref_spp=4096, pass_spp=8, max_
                 ctx.render_guided_dev(cam, filt, p, make_guide(use_alpha, *box, record=record_every,
                                                                light_guide=True, light_record=True),
                                       film.data_ptr(), fp64=True)
+                t1 = time.perf_counter()
+                render_s += t1 - t0
                 ctx.guide_light_update(light_share)
+                light_s += time.perf_counter() - t1
                 t1 = time.perf_counter()
                 loss = ctx.guide_train_on_records(train_steps + (warm_steps if k == 0 else 0), batch, lr, seed=k)
                 train_s += time.perf_counter() - t1
@@ -217,6 +220,7 @@ def convergence(ctx, name: str, size=(1024, 768), ref_spp=4096, pass_spp=8, max_
         if guided:
             res.update({"alpha": alpha, "train_steps_per_pass": train_steps, "warm_steps": warm_steps, "batch": batch,
                         "lr": lr, "record_every": record_every, "train_s": round(train_s, 4),
+                        "render_s": round(render_s, 4), "light_update_s": round(light_s, 4),
                         "light_table": {"grid": list(light_grid), "bins": light_bins, "uniform_share": light_share},
                         "mean_loss_per_pass": losses[:8] + (["..."] if len(losses) > 9 else []) + losses[-1:]})
         return res

@@ -936,7 +936,11 @@ __global__ void __launch_bounds__(128, KIND == MAT_DISNEY12 ? 8 : 5) k_material(
         P.M2[slot] = make_float4(g_fe.x, g_fe.y, g_fe.z, g_ps);
         sc6z = g_nc;
         sc6w = g_cos;
-        P.q_ext[nxt][append(P.ctr + C_EXT + nxt)] = 2 * slot + 1;
+        // (as the plain MIS ray: its emission is all it gives)
+        if (P.mis_all || mis_may_hit_light(P.sc, J, mo, md))
+          P.q_ext[nxt][append(P.ctr + C_EXT + nxt)] = 2 * slot + 1;
+        else
+          P.HM[slot] = make_float4(__int_as_float(-1), 0.0f, 0.0f, 0.0f);
       } else {
         gcode |= 1 << 30;
         float4* gxr = P.GX + 4 * (size_t)slot;
@@ -953,7 +957,10 @@ __global__ void __launch_bounds__(128, KIND == MAT_DISNEY12 ? 8 : 5) k_material(
           sc6z = gx.nc;
           sc6w = gx.cosv;
           flags |= F_GX;
-          P.q_ext[nxt][append(P.ctr + C_EXT + nxt)] = 2 * slot + 1;
+          if (P.mis_all || mis_may_hit_light(P.sc, J, xo, xd))
+            P.q_ext[nxt][append(P.ctr + C_EXT + nxt)] = 2 * slot + 1;
+          else
+            P.HM[slot] = make_float4(__int_as_float(-1), 0.0f, 0.0f, 0.0f);
         }
       }
     }
