@@ -550,6 +550,7 @@ typedef struct tr_guide_params {
   uint32_t max_records;
   int32_t light_guide;  /* 1: area-light samples from the light table */
   int32_t light_record; /* 1: unoccluded light samples update the table's statistics (needs light_guide) */
+  int32_t max_depth;    /* guide vertices at path depth < max_depth only, deeper ones sample plainly (0: all) */
 } tr_guide_params;
 /* Light table of learned light sampling: grid[0] x grid[1] x grid[2] cells
  * over the box of later guided renders' tr_guide_params, every light of the

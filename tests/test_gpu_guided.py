@@ -39,16 +39,19 @@ def test_alpha_zero_is_the_plain_renderer(gpu):
             assert st.guide_records == 0
 
 
-def test_guided_estimator_keeps_the_plain_expectation(gpu):
+@pytest.mark.parametrize("max_depth", [0, 2])
+def test_guided_estimator_keeps_the_plain_expectation(gpu, max_depth):
     """alpha = 0.5 with an untrained (random) mixture: a different proposal,
-    the same expected image. Compared on 8x8-pixel blocks at 1024 spp."""
+    the same expected image. Compared on 8x8-pixel blocks at 1024 spp; also
+    with guiding limited to the first two vertices of a path (max_depth 2;
+    deeper vertices sample plainly)."""
     sc, cam, filt, _ = scenes.cornell(32, 32, 1)
     gpu.upload(sc)
     gpu.guide_init(seed=4)
     par = scenes.make_params(32, 32, 1024, 5, 5, seed_base=1)
     plain, _ = gpu.render(cam, filt, par, fp64=True)
     par_g = scenes.make_params(32, 32, 1024, 5, 5, seed_base=7_000_000)
-    guided, st = _film(gpu, cam, filt, par_g, make_guide(0.5, (-1, -1, -1), (1, 1, 1)))
+    guided, st = _film(gpu, cam, filt, par_g, make_guide(0.5, (-1, -1, -1), (1, 1, 1), max_depth=max_depth))
     assert st.samples == 32 * 32 * 1024
     a = _image(plain).reshape(4, 8, 4, 8, 3).mean((1, 3))
     b = _image(guided).reshape(4, 8, 4, 8, 3).mean((1, 3))

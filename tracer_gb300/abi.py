@@ -117,7 +117,8 @@ class TrStats(C.Structure):
 
 class TrGuideParams(C.Structure):
     _fields_ = [("alpha", C.c_float), ("box_lo", C.c_float * 3), ("box_hi", C.c_float * 3), ("record", C.c_int32),
-                ("max_records", C.c_uint32), ("light_guide", C.c_int32), ("light_record", C.c_int32)]
+                ("max_records", C.c_uint32), ("light_guide", C.c_int32), ("light_record", C.c_int32),
+                ("max_depth", C.c_int32)]
 
 
 TR_RENDER_MODE_AUTO, TR_RENDER_MODE_WAVEFRONT, TR_RENDER_MODE_PERSISTENT = 0, 1, 2
@@ -312,10 +313,12 @@ def make_filter(radius=0.5, alpha=0.6) -> TrFilter:
 
 
 def make_guide(alpha: float, box_lo, box_hi, record: bool | int = False, max_records: int = 0,
-               light_guide: bool = False, light_record: bool = False) -> "TrGuideParams":
+               light_guide: bool = False, light_record: bool = False, max_depth: int = 0) -> "TrGuideParams":
     """record: False/0 none, True/1 every sample, n the first of every n samples of a pixel;
-    light_guide / light_record: learned light sampling from / statistics into the light table."""
+    light_guide / light_record: learned light sampling from / statistics into the light table;
+    max_depth: guide vertices at path depth < max_depth only (0: all)."""
     g = TrGuideParams()
+    g.max_depth = max_depth
     g.light_guide = int(light_guide)
     g.light_record = int(light_record)
     g.alpha = alpha

@@ -73,6 +73,7 @@ enum : int {  // counter slots
   C_TB = 16,      // guiding training records written (whole render)
   C_ERR = 17,     // traversal error word
   C_ORD = 18,     // live slots written in slot order (this iteration)
+  C_GROW = 19,    // network rows of this iteration's guided vertices
 };
 constexpr int kCtrWords = 32;  // the counter array
 // Statistics words: samples, extend rays, shadow rays, shade items, visit
@@ -90,6 +91,7 @@ struct RenderBuffers {
       stats;
   DevBuf VR, NV, gfeat, gout, tb;  // path guiding: vertex records, network rows, training records
   DevBuf GX;                        // path guiding: the continuation's MIS data (4 float4 per slot)
+  DevBuf grow;                      // path guiding: per slot, the network row of its vertex
   DevBuf MT;                        // Phong set-ups at hits with image maps (one DMat per slot)
   DevBuf jobs;                      // JobDev table of the current render
   DevBuf q_srt, bin_key, bin_cnt;   // ray binning: the reordered queue, keys, bin counts
@@ -132,6 +134,10 @@ struct Launch {
   // the live-slot list in slot order (null: k_logic reads the list as appended)
   int* q_ord;
   int mis_all;  // trace every MIS ray (visit-counting renders match the oracle's queries)
+  // guided renders: vertices at path depth < guide_depth (0: all) are
+  // guided; grow: per slot, the network row of its vertex (-1: not guided)
+  int guide_depth;
+  int* grow;
   unsigned char* act_flag;
   unsigned int* ctr;
   unsigned long long* stats;  // samples, extend rays, shadow rays, shade items, visit counts (4-7)
@@ -656,13 +662,18 @@ __global__ void __launch_bounds__(128) k_logic(Launch P, int cur) {
     const int qi = append(P.ctr + C_MAT + kind);
     P.q_mat[kind][qi] = slot;
     if (kind == MAT_PHONG && P.guide_alpha > 0.0f) {
-      // network inputs of the vertex, row qi of this iteration's forward pass
+      // network inputs of the vertex, a row of this iteration's forward pass
       const float4 p1 = P.P1[slot];
-      const f3 d = mk3(p1.x, p1.y, p1.z);
-      float f[7];
-      guide_features(P, mk3(p0.x, p0.y, p0.z) + scale(d, hit.y), -d, 1.0f, f);
-      float* out = P.gfeat + (size_t)qi * 7;
-      for (int k = 0; k < 7; ++k) out[k] = f[k];
+      int row = -1;
+      if (P.guide_depth == 0 || path_depth(p1.w) < P.guide_depth) {
+        row = append(P.ctr + C_GROW);
+        const f3 d = mk3(p1.x, p1.y, p1.z);
+        float f[7];
+        guide_features(P, mk3(p0.x, p0.y, p0.z) + scale(d, hit.y), -d, 1.0f, f);
+        float* out = P.gfeat + (size_t)row * 7;
+        for (int k = 0; k < 7; ++k) out[k] = f[k];
+      }
+      P.grow[slot] = row;
     }
   }
   count_add(P.stats, finished);
@@ -832,11 +843,12 @@ __global__ void __launch_bounds__(128, KIND == MAT_DISNEY12 ? 8 : 5) k_material(
     bool guided_end = false, g_trace = false;
     float g_ps = 0.0f, g_nc = 0.0f, g_pb = 0.0f, g_cos = 0.0f, g_pm = 0.0f;
     f3 g_fe = mk3(0.0f, 0.0f, 0.0f);
-    const bool gv = GUIDED && KIND == MAT_PHONG && P.guide_alpha > 0.0f && bsdf.m->w_specular == 0.0f &&
+    const int row = GUIDED && KIND == MAT_PHONG && P.guide_alpha > 0.0f ? P.grow[slot] : -1;
+    const bool gv = GUIDED && KIND == MAT_PHONG && P.guide_alpha > 0.0f && row >= 0 && bsdf.m->w_specular == 0.0f &&
                     !bsdf.fringe(is.wo);
     if (gv) {
       const float sel = Pcg::next(st), g0 = Pcg::next(st), g1 = Pcg::next(st);
-      guided_pick(P, bsdf, is, i, sel, g0, g1, bs, g_ps, g_nc, g_pm);
+      guided_pick(P, bsdf, is, row, sel, g0, g1, bs, g_ps, g_nc, g_pm);
       guided_end = black(bs.f) || bs.pdf < kEps;
       if (bs.pdf >= kEps) {
         const f3 wc = normalize(normalize(bs.wi));
@@ -885,7 +897,7 @@ __global__ void __launch_bounds__(128, KIND == MAT_DISNEY12 ? 8 : 5) k_material(
     gx.trace = false;
     if (gv) {
       const float x0 = Pcg::next(st), x1 = Pcg::next(st), x2 = Pcg::next(st);
-      guided_mixture_ray(P, bsdf, is, i, x0, x1, x2, gx);
+      guided_mixture_ray(P, bsdf, is, row, x0, x1, x2, gx);
     } else {
       const float v0 = Pcg::next(st), v1 = Pcg::next(st), v2 = Pcg::next(st);
       const BsdfSample ms = sample_bsdf_shared<KIND>(bsdf, is.wo, v0, v1, v2);
@@ -924,7 +936,7 @@ __global__ void __launch_bounds__(128, KIND == MAT_DISNEY12 ? 8 : 5) k_material(
     // the continuation (hit in HC, its data in GX) and the mixture ray in
     // the MIS slot (three strategies; bit 30 of the shading context's row
     // tells k_nee).
-    int gcode = gv ? (int)i : -1;
+    int gcode = gv ? row : -1;
     float sc6z = 0.0f, sc6w = 0.0f;
     if (gv && g_trace) {
       const f3 mo = is.eps_offset(bs.wi);
@@ -1211,7 +1223,7 @@ void release_render(tr_ctx* ctx) {
   for (DevBuf* b : {&rb->P0, &rb->P1, &rb->P2, &rb->P3, &rb->P4, &rb->rng, &rb->M0, &rb->M1, &rb->M2, &rb->HC,
                     &rb->HM, &rb->SC, &rb->NU, &rb->SH, &rb->acc, &rb->q_ext, &rb->q_act, &rb->q_mat, &rb->q_nee,
                     &rb->q_sh, &rb->ctr, &rb->stats, &rb->VR, &rb->NV, &rb->gfeat, &rb->gout, &rb->tb, &rb->jobs,
-                    &rb->GX, &rb->MT, &rb->q_srt, &rb->bin_key, &rb->bin_cnt, &rb->OC, &rb->q_ord,
+                    &rb->GX, &rb->grow, &rb->MT, &rb->q_srt, &rb->bin_key, &rb->bin_cnt, &rb->OC, &rb->q_ord,
                     &rb->act_flag})
     b->release();
   if (rb->h_active) cudaFreeHost(rb->h_active);
@@ -1479,11 +1491,14 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     cudaError_t e = cudaSuccess;
     if (P.guide_alpha > 0.0f) {
       if ((e = rb->gfeat.reserve(N * 7 * 4)) != cudaSuccess || (e = rb->gout.reserve(N * kMixFloats * 4)) != cudaSuccess ||
-          (e = rb->GX.reserve(N * 4 * sizeof(float4))) != cudaSuccess)
+          (e = rb->GX.reserve(N * 4 * sizeof(float4))) != cudaSuccess || (e = rb->grow.reserve(N * 4)) != cudaSuccess)
         return cuda_fail(ctx, e, "guide inference buffers");
       P.gfeat = rb->gfeat.as<float>();
       P.gout = rb->gout.as<float>();
       P.GX = rb->GX.as<float4>();
+      P.grow = rb->grow.as<int>();
+      if (gp->max_depth < 0) return set_err(ctx, TR_ERR_ARG, "guide max_depth must be >= 0");
+      P.guide_depth = gp->max_depth;
     }
     if (P.guide_record) {
       if ((e = rb->VR.reserve(N * P.maxd * 64)) != cudaSuccess || (e = rb->NV.reserve(N * 4)) != cudaSuccess ||
@@ -1662,6 +1677,7 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     cudaMemsetAsync(P.ctr + C_EXT + nxt, 0, 4, st);
     cudaMemsetAsync(P.ctr + C_ACT + nxt, 0, 4, st);
     cudaMemsetAsync(P.ctr + C_SH, 0, 4 * (C_FSH + 1 - C_SH), st);  // C_SH, C_MAT, C_NEE, C_FEXT, C_FSH
+    if (P.guide_alpha > 0.0f) cudaMemsetAsync(P.ctr + C_GROW, 0, 4, st);
     mark();
     if (P.q_ord) {  // the live slots in slot order (timed with k_logic)
       cudaMemsetAsync(P.ctr + C_ORD, 0, 4, st);
@@ -1671,7 +1687,7 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
     k_logic<<<grid, 128, 0, st>>>(P, cur);
     if (P.guide_alpha > 0.0f) {
       // decoded mixtures for this iteration's Phong-material vertices (inputs written by k_logic)
-      tr_status gs = guide_forward_rows_on_device(ctx, P.gfeat, P.ctr + C_MAT + MAT_PHONG, P.gout);
+      tr_status gs = guide_forward_rows_on_device(ctx, P.gfeat, P.ctr + C_GROW, P.gout);
       if (gs != TR_OK) return gs;
     }
     mark();
