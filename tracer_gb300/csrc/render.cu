@@ -87,7 +87,7 @@ constexpr int kMatScratch = 1 << 30;
 
 struct RenderBuffers {
   int n = 0, nl = 0;
-  DevBuf P0, P1, P2, P3, P4, rng, M0, M1, M2, HC, HM, SC, NU, SH, acc, q_ext, q_act, q_mat, q_nee, q_sh, ctr,
+  DevBuf P0, P1, P2, P3, P4, rng, M0, M1, M2, HC, HM, SC, NU, SH, SHC, acc, q_ext, q_act, q_mat, q_nee, q_sh, ctr,
       stats;
   DevBuf VR, NV, gfeat, gout, tb;  // path guiding: vertex records, network rows, training records
   DevBuf GX;                        // path guiding: the continuation's MIS data (4 float4 per slot)
@@ -116,7 +116,8 @@ struct Launch {
   float4* SC;            // shading context for nee: 7 per slot (pos|mat, wo, g, s frames; the last
                          // also holds the guided vertex's network row, normal correction and |cos|)
   float2* NU;            // light-sample draws per (slot, light)
-  float4* SH;            // shadow: 3 per (slot, light): o|t_max, d, contrib|valid
+  float4* SH;            // shadow rays: 2 per (slot, light): o|t_max, d|estimate
+  float4* SHC;           // per (slot, light): the light sample's contribution|valid (0: none or occluded)
   DMat* MT;              // per slot: the Phong set-up at a hit with image maps (null without maps)
   int* q_ext[2];
   int* q_act[2];
@@ -365,7 +366,7 @@ struct ShadowJob {
   __device__ __forceinline__ void load(unsigned int i, f3& o, f3& d, float& t_min, float& t_max, int& scene) const {
     const int r = q[i];
     scene = job_of(P, r / P.nl_max).scene;
-    const float4 a = P.SH[3 * r], b = P.SH[3 * r + 1];
+    const float4 a = P.SH[2 * r], b = P.SH[2 * r + 1];
     o = mk3(a.x, a.y, a.z);
     d = mk3(b.x, b.y, b.z);
     t_min = kEps;
@@ -373,7 +374,7 @@ struct ShadowJob {
   }
   __device__ __forceinline__ void store(unsigned int i, const Hit& h, float, bool occluded) const {
     if (occluded) {
-      P.SH[3 * q[i] + 2].w = 0.0f;
+      P.SHC[q[i]].w = 0.0f;
       if (P.OC) P.OC[q[i]] = h.prim;
     }
   }
@@ -602,13 +603,13 @@ __global__ void __launch_bounds__(128) k_logic(Launch P, int cur) {
       f3 direct = mk3(0.0f, 0.0f, 0.0f);
       const int nl = job_of(P, slot).nl;
       for (int l = 0; l < nl; ++l) {
-        const float4 c = P.SH[3 * (slot * P.nl_max + l) + 2];
+        const float4 c = P.SHC[slot * P.nl_max + l];
         if (c.w != 0.0f) direct = direct + mk3(c.x, c.y, c.z);
         if (P.lg_acc && c.w != 0.0f) {
           // an unoccluded learned light sample: its estimate into the
           // statistics of its (cell, light) bin (environment-light items
           // carry no estimate)
-          const float v = P.SH[3 * (slot * P.nl_max + l) + 1].w;
+          const float v = P.SH[2 * (slot * P.nl_max + l) + 1].w;
           if (v > 0.0f && v < 1e30f) {
             const float4 s0 = P.SC[7 * (size_t)slot];
             atomicAdd(P.lg_acc + lg_table(P, mk3(s0.x, s0.y, s0.z), l) + ((int)c.w - 1), v);
@@ -875,7 +876,7 @@ __global__ void __launch_bounds__(128, KIND == MAT_DISNEY12 ? 8 : 5) k_material(
       const float tol = 1e-4f * (pos_mag + lt.extent);
       if (side < -tol) {
         Pcg::skip<5>(st);
-        P.SH[3 * (size_t)item + 2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        P.SHC[item] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         continue;
       }
       const float lu = Pcg::next(st), lv = Pcg::next(st);
@@ -1083,7 +1084,7 @@ __global__ void __launch_bounds__(128) k_glass(Launch P, int cur) {
 // guided vertex's network row (bit 30: three strategies), else -1.
 template <int KIND>
 __device__ __noinline__ bool nee_env_item(const Launch& P, int item, int slot, int env, f3 pos, f3 wo,
-                                          const Bsdf& bsdf, float2 uv, int gcode, float4* rec) {
+                                          const Bsdf& bsdf, float2 uv, int gcode, float4* rec, float4* recc) {
   bool ok = false;
   // sample_environment_light (src/renderer/direct_illumination.cpp:73-106)
   f3 Le, lpos;
@@ -1116,7 +1117,7 @@ __device__ __noinline__ bool nee_env_item(const Launch& P, int item, int slot, i
         const f3 sd = normalize(to_light);
         rec[0] = make_float4(pos.x, pos.y, pos.z, dist);
         rec[1] = make_float4(sd.x, sd.y, sd.z, 0.0f);
-        rec[2] = make_float4(cc.x, cc.y, cc.z, 1.0f);
+        *recc = make_float4(cc.x, cc.y, cc.z, 1.0f);
         P.q_sh[append(P.ctr + C_SH)] = item;
         ok = true;
       }
@@ -1150,11 +1151,12 @@ __global__ void __launch_bounds__(128, 6) k_nee(Launch P) {
     bsdf.s.z = mk3(f.z, f.w, g.x);
     const float2 uv = P.NU[item];
     const DLight& lt = P.sc.lights[job_of(P, slot).light_base + l];
-    float4* rec = P.SH + 3 * (size_t)item;
+    float4* rec = P.SH + 2 * (size_t)item;
+    float4* recc = P.SHC + item;
     bool ok = false;
     if (lt.env >= 0) {  // out of line: its registers would otherwise count for every item
-      if (!nee_env_item<KIND>(P, item, slot, lt.env, pos, wo, bsdf, uv, __float_as_int(g.y), rec))
-        rec[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (!nee_env_item<KIND>(P, item, slot, lt.env, pos, wo, bsdf, uv, __float_as_int(g.y), rec, recc))
+        *recc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       continue;
     }
     // Triangle::sample via UniformSampleTriangle (src/shape/triangle.cpp:61-97),
@@ -1206,14 +1208,14 @@ __global__ void __launch_bounds__(128, 6) k_nee(Launch P) {
             rec[0] = make_float4(pos.x, pos.y, pos.z, dist);
             // statistics of the light table: the estimate's luminance, the bin + 1
             rec[1] = make_float4(sd.x, sd.y, sd.z, P.lg_acc ? lum(inner) : 0.0f);
-            rec[2] = make_float4(cc.x, cc.y, cc.z, P.lg_acc ? (float)(lbin + 1) : 1.0f);
+            *recc = make_float4(cc.x, cc.y, cc.z, P.lg_acc ? (float)(lbin + 1) : 1.0f);
             P.q_sh[append(P.ctr + C_SH)] = item;
             ok = true;
           }
         }
       }
     }
-    if (!ok) rec[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (!ok) *recc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   }
 }
 
@@ -1221,7 +1223,7 @@ void release_render(tr_ctx* ctx) {
   if (!ctx->rb) return;
   RenderBuffers* rb = ctx->rb;
   for (DevBuf* b : {&rb->P0, &rb->P1, &rb->P2, &rb->P3, &rb->P4, &rb->rng, &rb->M0, &rb->M1, &rb->M2, &rb->HC,
-                    &rb->HM, &rb->SC, &rb->NU, &rb->SH, &rb->acc, &rb->q_ext, &rb->q_act, &rb->q_mat, &rb->q_nee,
+                    &rb->HM, &rb->SC, &rb->NU, &rb->SH, &rb->SHC, &rb->acc, &rb->q_ext, &rb->q_act, &rb->q_mat, &rb->q_nee,
                     &rb->q_sh, &rb->ctr, &rb->stats, &rb->VR, &rb->NV, &rb->gfeat, &rb->gout, &rb->tb, &rb->jobs,
                     &rb->GX, &rb->grow, &rb->MT, &rb->q_srt, &rb->bin_key, &rb->bin_cnt, &rb->OC, &rb->q_ord,
                     &rb->act_flag})
@@ -1247,7 +1249,7 @@ tr_status reserve_render(tr_ctx* ctx, int n, int nl) {
                {&rb->P3, N * f4},           {&rb->P4, N * f4},          {&rb->rng, N * 8},
                {&rb->M0, N * f4},           {&rb->M1, N * f4},          {&rb->M2, N * f4},
                {&rb->HC, N * f4},           {&rb->HM, N * f4},          {&rb->SC, N * 7 * f4},
-               {&rb->NU, N * NL * 8},       {&rb->SH, N * NL * 3 * f4}, {&rb->acc, N * 32},
+               {&rb->NU, N * NL * 8},       {&rb->SH, N * NL * 2 * f4}, {&rb->SHC, N * NL * f4}, {&rb->acc, N * 32},
                {&rb->q_ext, 2 * 2 * N * 4}, {&rb->q_act, 2 * N * 4},   {&rb->q_mat, kMatKinds * N * 4},
                {&rb->q_nee, kNeeKinds * N * NL * 4}, {&rb->q_sh, N * NL * 4},  {&rb->ctr, kCtrWords * 4},
                {&rb->stats, kStatWords * 8}};
@@ -1422,6 +1424,7 @@ tr_status render_jobs(tr_ctx* ctx, const JobSpec* jobs, int njobs, uint32_t flag
   P.SC = rb->SC.as<float4>();
   P.NU = rb->NU.as<float2>();
   P.SH = rb->SH.as<float4>();
+  P.SHC = rb->SHC.as<float4>();
   P.MT = nullptr;
   if (ctx->dsc.has_textures) {
     cudaError_t e = rb->MT.reserve((size_t)n * sizeof(DMat));
@@ -1919,7 +1922,8 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   NoAllocLayout L;
   const size_t f4 = sizeof(float4);
   const size_t oP = L.take(5 * N * f4), oRng = L.take(N * 8), oM = L.take(3 * N * f4), oH = L.take(2 * N * f4),
-               oSC = L.take(N * 7 * f4), oNU = L.take(N * NL * 8), oSH = L.take(N * NL * 3 * f4),
+               oSC = L.take(N * 7 * f4), oNU = L.take(N * NL * 8), oSH = L.take(N * NL * 2 * f4),
+               oSHC = L.take(N * NL * f4),
                oQe = L.take(2 * 2 * N * 4), oQa = L.take(2 * N * 4), oQm = L.take(kMatKinds * N * 4),
                oQn = L.take(kNeeKinds * N * NL * 4), oQs = L.take(N * NL * 4), oCtr = L.take(kCtrWords * 4),
                oSt = L.take(kStatWords * 8),
@@ -1986,6 +1990,7 @@ tr_status render_noalloc_impl(tr_ctx* ctx, const tr_camera* cam, const tr_filter
   P.SC = reinterpret_cast<float4*>(base + oSC);
   P.NU = reinterpret_cast<float2*>(base + oNU);
   P.SH = reinterpret_cast<float4*>(base + oSH);
+  P.SHC = reinterpret_cast<float4*>(base + oSHC);
   int* qe = reinterpret_cast<int*>(base + oQe);
   int* qa = reinterpret_cast<int*>(base + oQa);
   int* qm = reinterpret_cast<int*>(base + oQm);
