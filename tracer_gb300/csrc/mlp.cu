@@ -92,7 +92,10 @@ __global__ void __launch_bounds__(128, 1)
   uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + kMbarOff);
   uint32_t* slot = reinterpret_cast<uint32_t*>(sm + kSlotOff);
   if (tid == 0) tc05::mbar_init(mbar, 1);
-  if (warp == 0) tc05::tmem_alloc(slot, 64);
+  if (warp == 0) {
+    tc05::tmem_alloc(slot, 64);
+    tc05::tmem_relinquish();  // at once: the SM's other CTAs allocate their columns meanwhile
+  }
   tc05::fence_before();
   __syncthreads();
   tc05::fence_after();
@@ -184,7 +187,6 @@ __global__ void __launch_bounds__(128, 1)
   __syncthreads();
   if (warp == 0) {
     tc05::tmem_dealloc(tmem, 64);
-    tc05::tmem_relinquish();
   }
 }
 
@@ -248,7 +250,10 @@ __global__ void __launch_bounds__(128, 1)
   uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + kBMbar);
   uint32_t* slot = reinterpret_cast<uint32_t*>(sm + kBSlot);
   if (tid == 0) tc05::mbar_init(mbar, 1);
-  if (warp == 0) tc05::tmem_alloc(slot, 512);
+  if (warp == 0) {
+    tc05::tmem_alloc(slot, 512);
+    tc05::tmem_relinquish();
+  }
   tc05::fence_before();
   __syncthreads();
   tc05::fence_after();
@@ -368,7 +373,6 @@ __global__ void __launch_bounds__(128, 1)
   __syncthreads();
   if (warp == 0) {
     tc05::tmem_dealloc(tmem, 512);
-    tc05::tmem_relinquish();
   }
 }
 
@@ -576,7 +580,10 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
   uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + kTMbar);
   uint32_t* slot = reinterpret_cast<uint32_t*>(sm + kTSlot);
   if (tid == 0) tc05::mbar_init(mbar, 1);
-  if (warp == 0) tc05::tmem_alloc(slot, 512);
+  if (warp == 0) {
+    tc05::tmem_alloc(slot, 512);
+    tc05::tmem_relinquish();
+  }
   tc05::fence_before();
   __syncthreads();
   tc05::fence_after();
@@ -785,7 +792,6 @@ __global__ void __launch_bounds__(kTrainThreads, 1)
   }
   if (warp == 0) {
     tc05::tmem_dealloc(tmem, 512);
-    tc05::tmem_relinquish();
   }
 }
 
