@@ -53,16 +53,19 @@ __device__ __forceinline__ void mixture_decode(const float (&z)[48], float (&d)[
 struct Mixture {
   const float* __restrict__ d;
 
+  // The hardware exponential (relative error about 1e-6, the arguments are
+  // <= 0): the density enters only MIS weights and the guided estimate's
+  // denominator, evaluated the same way for every strategy.
   __device__ float pdf(f3 w) const {
     const float4* q = reinterpret_cast<const float4*>(d);
     float p = 0.0f;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const float4 c = q[2 + h], k = q[4 + h], x = q[6 + h], y = q[8 + h], z = q[10 + h];
-      p += c.x * expf(k.x * (x.x * w.x + y.x * w.y + z.x * w.z - 1.0f));
-      p += c.y * expf(k.y * (x.y * w.x + y.y * w.y + z.y * w.z - 1.0f));
-      p += c.z * expf(k.z * (x.z * w.x + y.z * w.y + z.z * w.z - 1.0f));
-      p += c.w * expf(k.w * (x.w * w.x + y.w * w.y + z.w * w.z - 1.0f));
+      p += c.x * __expf(k.x * (x.x * w.x + y.x * w.y + z.x * w.z - 1.0f));
+      p += c.y * __expf(k.y * (x.y * w.x + y.y * w.y + z.y * w.z - 1.0f));
+      p += c.z * __expf(k.z * (x.z * w.x + y.z * w.y + z.z * w.z - 1.0f));
+      p += c.w * __expf(k.w * (x.w * w.x + y.w * w.y + z.w * w.z - 1.0f));
     }
     return p;
   }
