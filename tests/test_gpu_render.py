@@ -388,3 +388,25 @@ def test_mis_rays_that_reach_no_light_are_not_traced(gpu, case):
     print(f"{case}: extension rays traced {st.extend_rays} of {st_all.extend_rays}")
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
     assert st.extend_rays < st_all.extend_rays
+
+
+@pytest.mark.parametrize("mode", ["wavefront", "persistent"])
+def test_mis_rays_reach_emitters_outside_the_light_list(gpu, mode):
+    """A scene description may leave an emissive triangle out of its light
+    list: next-event estimation never samples it, but an MIS ray that hits it
+    still gathers its emission. Such a scene traces every MIS ray, so its film
+    equals, bit for bit, a visit-counting render's, which traces them all."""
+    from conftest import tuned
+    from tracer_gb300.abi import (TR_RENDER_COUNT_VISITS, TR_RENDER_MODE_PERSISTENT, TR_RENDER_MODE_WAVEFRONT,
+                                  TrRenderParams)
+    sc, cam, filt, par = scenes.cornell(48, 48, 4)
+    assert len(sc.light_prims) == 2
+    sc.light_prims = sc.light_prims[:1].copy()  # the light quad's second triangle stays emissive, unlisted
+    gpu.upload(sc)
+    with tuned(gpu, render_mode=TR_RENDER_MODE_PERSISTENT if mode == "persistent" else TR_RENDER_MODE_WAVEFRONT):
+        got, st = gpu.render(cam, filt, par)
+    allp = TrRenderParams.from_buffer_copy(par)
+    allp.flags = TR_RENDER_COUNT_VISITS
+    want, st_all = gpu.render(cam, filt, allp)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    assert st.extend_rays == st_all.extend_rays

@@ -864,11 +864,13 @@ static tr_status build_host_scene(tr_ctx* ctx, const tr_scene_desc* d, HostScene
     if (pr.emissive && pr.kind == PRIM_SPHERE)
       return set_err(ctx, TR_ERR_UNSUPPORTED, "emissive spheres are outside the GPU path");
   }
+  std::vector<uint8_t> listed(np, 0);
   for (uint32_t l = 0; l < d->num_lights; ++l) {
     const int p = d->light_prims[l];
     if (p < 0 || (uint32_t)p >= np) return set_err(ctx, TR_ERR_ARG, "light primitive out of range");
     const DPrim& pr = hs.prims[p];
     if (!pr.emissive) return set_err(ctx, TR_ERR_ARG, "light primitive is not emissive");
+    listed[p] = 1;
     DLight L;
     std::memset(&L, 0, sizeof(L));
     L.A = hs.A[pr.shape];
@@ -918,6 +920,9 @@ static tr_status build_host_scene(tr_ctx* ctx, const tr_scene_desc* d, HostScene
   }
   hs.scene_prim = {0};
   hs.scene_leaf = {(int)d->max_leaf_prims};
+  uint8_t unlisted = 0;
+  for (uint32_t p = 0; p < np; ++p) unlisted |= (uint8_t)(hs.prims[p].emissive && !listed[p]);
+  hs.scene_unlisted = {unlisted};
   hs.scene_node = {0};
   hs.scene_light = {0};
   hs.scene_nlight = {(uint32_t)hs.lights.size()};
@@ -935,6 +940,7 @@ static void append_scene(HostScene& dst, const HostScene& src) {
   dst.scene_nlight.push_back((uint32_t)src.lights.size());
   dst.scene_prim.push_back(prim_base);
   dst.scene_leaf.insert(dst.scene_leaf.end(), src.scene_leaf.begin(), src.scene_leaf.end());
+  dst.scene_unlisted.insert(dst.scene_unlisted.end(), src.scene_unlisted.begin(), src.scene_unlisted.end());
   dst.device_bvh = src.device_bvh;
   dst.blo.insert(dst.blo.end(), src.blo.begin(), src.blo.end());
   dst.bhi.insert(dst.bhi.end(), src.bhi.begin(), src.bhi.end());

@@ -53,6 +53,9 @@ struct HostScene {
   std::vector<uint32_t> scene_node, scene_light, scene_nlight;
   std::vector<uint32_t> scene_prim;  // first primitive of every scene
   std::vector<int> scene_leaf;       // max_leaf_prims of every scene
+  // 1 for a scene with an emissive primitive outside its light list (its
+  // MIS rays are all traced: the light list cannot tell which reach emission)
+  std::vector<uint8_t> scene_unlisted;
   // TR_BVH_DEVICE: no host tree; the primitive bounds (3 floats each) for the device build
   bool device_bvh = false;
   std::vector<float> blo, bhi;

@@ -1325,6 +1325,7 @@ static JobDev make_job_dev(tr_ctx* ctx, const JobSpec& j, int slot_base, void* f
   J.light_base = (int)ctx->hs.scene_light[j.scene];
   J.nl = (int)ctx->hs.scene_nlight[j.scene];
   J.env = J.nl > 0 ? ctx->hs.lights[J.light_base + J.nl - 1].env : -1;
+  J.mis_always = ctx->hs.scene_unlisted[j.scene];
   // the sphere of mis_may_hit_light: around the box of the area-light
   // triangles as the triangle test sees them (A, A + AB, A + AC), widened
   // by 1e-3 of the radius and of the coordinates' scale

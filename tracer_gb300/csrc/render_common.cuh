@@ -30,6 +30,7 @@ struct JobDev {
   int env;             // the scene's environment light in DScene::envs (its last light), or -1
   float lsph[4];       // a sphere around the scene's area-light triangles with a margin (radius < 0: none)
   float lsph_cn;       // |centre|
+  int mis_always;      // the scene has emissive primitives outside its light list: every MIS ray is traced
   float filter_radius, filter_alpha, filter_exp;
   int fp64;
   float4* film;  // film sums (float4 per pixel, or 2 x double2)
@@ -138,7 +139,7 @@ static __device__ __noinline__ bool light_tri_hit(const DLight& lt, f3 o, f3 d) 
 }
 
 __device__ __forceinline__ bool mis_may_hit_light(const DScene& sc, const JobDev& J, f3 o, f3 d) {
-  if (J.env >= 0 || J.nl > kMisLightTests) return true;
+  if (J.env >= 0 || J.nl > kMisLightTests || J.mis_always) return true;
   if (J.lsph[3] < 0.0f) return false;
   const float on = sqrtf(dot(o, o));
   if (!ray_may_pass(J.lsph, J.lsph_cn, o, d, on)) return false;  // all lights
