@@ -145,7 +145,9 @@ typedef struct tr_scene_desc {
   const int32_t* prim_material; /* material index per primitive */
   const float* prim_emission;   /* 3 * num_prims; all zero = not a light */
   uint32_t num_lights;
-  const int32_t* light_prims;   /* primitive indices, in scene.lights order */
+  const int32_t* light_prims;   /* primitive indices, in scene.lights order. The reference makes every
+                                   emissive primitive a light; one left out is never light-sampled but
+                                   still emits when a ray hits it (every MIS ray of such a scene is traced) */
   int32_t max_leaf_prims;       /* create_bvh_accel argument (src/accelerator/bvh.cpp:315) */
   /* Environment light: create_ibl_light(create_hdr_texture2d(image), world_to_light)
    * (src/light/environment_light.cpp:14-84,196-203, src/texture/hdr_texture.cpp:9-37)
