@@ -9,7 +9,7 @@ can send that path elsewhere. The tests therefore check:
   * every recorded extension/shadow query of the oracle's paths replays to
     identical hits on the GPU (bit-exact);
   * most pixels agree with the oracle's to 1e-5 relative (identical paths);
-  * the mean relative error of the image is below 1% (spec bound).
+  * the mean relative error of the image is below 1%.
 """
 import numpy as np
 import pytest
