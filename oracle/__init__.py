@@ -9,7 +9,8 @@ Python interface:
   ``make -C oracle ref`` (only where the reference checkout exists).
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
-this package, and only as the checker or the timed CPU baseline.
+this package, and only to check the GPU path's results or as the timed CPU
+baseline.
 """
 from __future__ import annotations
 

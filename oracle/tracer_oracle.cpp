@@ -1,6 +1,7 @@
 // tracer_oracle.cpp -- CPU restatement of Tracer's unidirectional path-tracing
-// hot path. TEST INFRASTRUCTURE ONLY: it is the parity checker for the GPU
-// path and the "port" CPU baseline. Nothing in the product links or calls it.
+// hot path. TEST INFRASTRUCTURE ONLY: the tests check the GPU path's results
+// against it, and it is the "port" CPU baseline. Nothing in the product links
+// or calls it.
 //
 // Parity is pinned: tests/test_oracle_vs_reference.py compares every entry
 // point here with the reference's own sources compiled by oracle/Makefile
