@@ -1,7 +1,11 @@
-"""bench.py's roofline helpers on the host: what bounds a kernel, from its
-measured DRAM bytes per launch, and the committed per-item DRAM figures."""
+"""bench.py on the host: the roofline helpers (what bounds a kernel, from its
+measured DRAM bytes per launch; the committed per-item DRAM figures) and the
+reference arm's JSON line, which needs no GPU."""
 import importlib.util
+import json
 import os
+import subprocess
+import sys
 
 import pytest
 
@@ -39,3 +43,33 @@ def test_committed_traffic_figures(bench):
     assert sh["bytes_per_unit"] == pytest.approx(239.7)
     assert "ncu" in ext["source"] and "ncu" in sh["source"]
     assert bench.traffic_per_unit("material") is None
+
+
+def _reference_arm(env_extra):
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="", **env_extra)
+    return subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload",
+                           "cornell", "--size", "32x32x2", "--steps", "2", "--warmup", "1"],
+                          env=env, capture_output=True, text=True, timeout=300, cwd=ROOT)
+
+
+def test_reference_arm_line():
+    """The reference arm times the CPU restatement on the host cores and
+    prints one JSON line carrying the keys the contract names."""
+    r = _reference_arm({})
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1
+    d = lines[0]
+    assert d["impl"] == "reference" and d["value"] > 0 and d["steps"] == 2 and d["warmup"] == 1
+    assert d["higher_is_better"] is True and d["unit"] == "Msamples/s"
+    assert d["config"]["workload"].startswith("cornell_box_36tris_32x32_2spp")
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_other_ranks_exit_quietly():
+    """Under torchrun only rank 0 runs and prints; the others exit 0."""
+    r = _reference_arm({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert not [x for x in r.stdout.splitlines() if x.startswith("{")]
