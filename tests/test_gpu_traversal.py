@@ -36,6 +36,26 @@ def test_random_scene_closest_and_any(gpu, seed):
     assert np.array_equal(orc.trace_any(srays), gpu.trace_any(srays))
 
 
+@pytest.mark.parametrize("seed", [0, 1])
+def test_adversarial_rays(gpu, seed):
+    """Rays aimed exactly at triangle vertices, edge midpoints and centroids,
+    axis-parallel rays with origins on vertex coordinates, and shadow rays
+    ending exactly at (or one ulp either side of) the closest hit: the same
+    hits, distances and occlusion flags as the oracle, which equals the
+    reference build on these rays."""
+    sc = scenes.random_scene(seed, n_tris=400, n_spheres=6)
+    orc = oracle.Oracle(sc, "port")
+    gpu.upload(sc)
+    rays = scenes.adversarial_rays(sc, seed)
+    p0, t0 = orc.trace_closest(rays)
+    p1, t1 = gpu.trace_closest(rays)
+    assert np.array_equal(p0, p1)
+    assert _same_bits(t0, t1)
+    for step in (-1, 0, 1):
+        s = scenes.shadow_rays_at_hits(rays, p0, t0, step)
+        assert np.array_equal(orc.trace_any(s), gpu.trace_any(s)), step
+
+
 def test_bvh_matches_oracle(gpu):
     sc = scenes.random_scene(7, n_tris=300, n_spheres=20)
     orc = oracle.Oracle(sc, "port")

@@ -474,6 +474,36 @@ def traversal_rays(n_rays=1 << 22, seed=0, shadow=False):
     return make_rays(o, d, 0.0, tmax)
 
 
+def adversarial_rays(sc, seed=0):
+    """Closest-hit rays at a scene's triangles' edge cases: aimed from random
+    origins exactly at each triangle's vertices, the midpoint of its first
+    edge and its centroid; and axis-parallel rays whose origin's x lies on a
+    vertex's coordinate (infinite inverse directions, slab planes through the
+    origin). Through the reference Ray constructor; t_min 0, t_max FLT_MAX."""
+    rng = np.random.default_rng(100 + seed)
+    tri = sc.positions[sc.indices]  # (T, 3, 3)
+    targets = np.concatenate([tri[:, 0], tri[:, 1], tri[:, 2],
+                              ((tri[:, 0] + tri[:, 1]) * np.float32(0.5)).astype(np.float32),
+                              ((tri[:, 0] + tri[:, 1] + tri[:, 2]) / np.float32(3)).astype(np.float32)])
+    origins = rng.uniform(-3, 3, (len(targets), 3)).astype(np.float32)
+    aimed = make_rays(origins, (targets - origins).astype(np.float32), 0.0, F32_MAX)
+    axes = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1],
+                     [1, 1, 0], [0, -1, 1], [1, 0, -1]], np.float32)
+    o_ax = np.repeat(tri[:, 0], len(axes), axis=0) - np.float32(2) * np.tile(axes, (len(tri), 1))
+    o_ax[:, 0] = np.repeat(tri[:, 1, 0], len(axes))
+    parallel = make_rays(o_ax, np.tile(axes, (len(tri), 1)), 0.0, F32_MAX)
+    return np.concatenate([aimed, parallel])
+
+
+def shadow_rays_at_hits(rays, prim, t, step):
+    """The rays that hit something, as shadow rays with t_max at the hit
+    distance (step 0) or one ulp below (-1) or above (+1) it."""
+    hit = prim >= 0
+    s = rays[hit].copy()
+    s["t_max"] = np.nextafter(t[hit], np.float32(np.inf if step > 0 else -np.inf)) if step else t[hit]
+    return s
+
+
 def random_scene(seed=0, n_tris=64, n_spheres=8, n_lights=2, disney_frac=0.5, max_leaf_prims=3):
     """Small closed-ish scene for parity tests: a floor, random triangles and
     spheres in [-1,1]^3, emissive triangles overhead."""
