@@ -251,3 +251,36 @@ def test_adversarial_rays(seed):
     for step in (-1, 0, 1):
         s = scenes.shadow_rays_at_hits(rays, p0, t0, step)
         assert np.array_equal(port.trace_any(s), ref.trace_any(s)), step
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_sphere_edge_rays(seed):
+    """Rays passing each sphere at 1 - 1e-6 to 1 + 1e-5 radii from its centre
+    (the hit/miss transition of the quadratic lies in between), rays from
+    its centre and from a point on its surface: hits, distances and
+    occlusion flags equal the reference build's."""
+    sc = scenes.random_scene(seed, n_tris=20, n_spheres=12)
+    port, ref = oracle.Oracle(sc, "port"), oracle.Oracle(sc, "reference")
+    m = sc.sphere_to_world.reshape(-1, 4, 4)
+    centre = m[:, :3, 3].astype(np.float32)
+    r = (sc.sphere_radius * np.abs(m[:, 0, 0])).astype(np.float32)  # uniform scale in these scenes
+    o, d = [], []
+    for c, rad in zip(centre, r):
+        for k, axis in enumerate(np.eye(3, dtype=np.float32)):
+            side = np.eye(3, dtype=np.float32)[(k + 1) % 3]
+            for f in (1 - 1e-6, 1.0, 1 + 1e-6, 1 + 2e-6, 1 + 3e-6, 1 + 5e-6, 1 + 1e-5):
+                o.append(c + side * np.float32(rad * f) - axis * np.float32(3))
+                d.append(axis)
+            o.append(c)  # from the centre
+            d.append(axis)
+            o.append(c + side * rad)  # from the surface, into the sphere and out of it
+            d.append(-side)
+            o.append(c + side * rad)
+            d.append(side)
+    rays = scenes.make_rays(np.array(o, np.float32), np.array(d, np.float32), 0.0, scenes.F32_MAX)
+    p0, t0 = port.trace_closest(rays)
+    p1, t1 = ref.trace_closest(rays)
+    assert np.array_equal(p0, p1) and np.array_equal(bits(t0), bits(t1))
+    for step in (-1, 0, 1):
+        s = scenes.shadow_rays_at_hits(rays, p0, t0, step)
+        assert np.array_equal(port.trace_any(s), ref.trace_any(s)), step
